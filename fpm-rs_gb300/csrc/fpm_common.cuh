@@ -1,0 +1,108 @@
+// Shared device building blocks: complex float arithmetic, in-register DFTs
+// of power-of-two length, and the twiddle table.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "twiddle256.cuh"
+
+#define FPM_DEVICE __device__ __forceinline__
+
+FPM_DEVICE float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+FPM_DEVICE float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+FPM_DEVICE float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+FPM_DEVICE float2 cmulc(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+FPM_DEVICE float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+FPM_DEVICE float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+FPM_DEVICE float cnorm2(float2 a) { return fmaf(a.x, a.x, a.y * a.y); }
+FPM_DEVICE float2 cfma(float s, float2 a, float2 acc) {
+    return make_float2(fmaf(s, a.x, acc.x), fmaf(s, a.y, acc.y));
+}
+
+// Multiplies by w_256^k (forward, exp(-2 pi i k/256)) or its conjugate
+// (inverse). k is a compile-time constant after unrolling, so the special
+// cases fold away and the general case reads the constant bank.
+template <bool INV>
+FPM_DEVICE float2 twiddle_const(float2 b, int k) {
+    if (k == 0) return b;
+    if (k == 64) return INV ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+    if (k == 128) return make_float2(-b.x, -b.y);
+    if (k == 192) return INV ? make_float2(b.y, -b.x) : make_float2(-b.y, b.x);
+    float2 w = c_tw256[k];
+    if (INV) w.y = -w.y;
+    return cmul(b, w);
+}
+
+// Runtime-index twiddle from a shared-memory copy of the forward table.
+template <bool INV>
+FPM_DEVICE float2 twiddle_smem(float2 b, const float2* tw, int k) {
+    float2 w = tw[k & 255];
+    if (INV) w.y = -w.y;
+    return cmul(b, w);
+}
+
+template <int L>
+FPM_DEVICE constexpr int bit_reverse(int i) {
+    int r = 0;
+    for (int b = 1, m = L >> 1; b < L; b <<= 1, m >>= 1)
+        if (i & b) r |= m;
+    return r;
+}
+
+// One radix-2 butterfly stage of span LEN, then the next stage.
+template <int L, bool INV, int LEN>
+FPM_DEVICE void dft_stages(float2 (&v)[L]) {
+    if constexpr (LEN <= L) {
+        constexpr int HALF = LEN / 2;
+        constexpr int STEP = 256 / LEN;
+#pragma unroll
+        for (int s = 0; s < L; s += LEN) {
+#pragma unroll
+            for (int j = 0; j < HALF; ++j) {
+                float2 a = v[s + j];
+                float2 b = twiddle_const<INV>(v[s + j + HALF], j * STEP);
+                v[s + j] = cadd(a, b);
+                v[s + j + HALF] = csub(a, b);
+            }
+        }
+        dft_stages<L, INV, LEN * 2>(v);
+    }
+}
+
+// In-place DFT of L values held in registers, natural order in and out:
+// v[k] <- sum_n v[n] w_L^{+-nk}. Unnormalised. Radix-2 decimation in time
+// with compile-time bit reversal (register renaming only).
+template <int L, bool INV>
+FPM_DEVICE void dft_reg(float2 (&v)[L]) {
+    if constexpr (L > 1) {
+#pragma unroll
+        for (int i = 0; i < L; ++i) {
+            const int r = bit_reverse<L>(i);
+            if (r > i) {
+                float2 t = v[i];
+                v[i] = v[r];
+                v[r] = t;
+            }
+        }
+        dft_stages<L, INV, 2>(v);
+    }
+}
+
+// Block-wide reductions used once per frame or iteration.
+FPM_DEVICE float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+FPM_DEVICE double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}

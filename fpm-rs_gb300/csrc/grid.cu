@@ -1,0 +1,349 @@
+// Whole-grid FP64 kernels that run once per reconstruction (initialise and
+// finalise) or once per iteration (EPRY gauge):
+//  * mixed-radix Stockham line FFTs of any length (reference convention of
+//    CpuBackend::fft2, src/backend/cpu.rs:130-175, applied as rows then
+//    columns by the caller),
+//  * fftshift / ifftshift conversions between the centred FP32 state and
+//    natural-order FP64 scratch (src/model/forward.rs:530-569),
+//  * object/pupil gauge canonicalisation (src/algorithms/gauge.rs:20-282).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "kernels.h"
+
+namespace fpm {
+
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double zabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+// One block per line. Stage s with radix R maps input index j + r*n/R to
+// output (j / Ns) * Ns * R + j % Ns + q * Ns (Stockham autosort), so lines
+// come out in natural order without a permutation pass.
+__global__ void fft_lines_kernel(double2* const* arrays, int n, long long stride, long long dist,
+                                 const double2* __restrict__ roots, const int* __restrict__ factors, int nfactors,
+                                 int inverse, double scale) {
+    extern __shared__ double2 zsm[];
+    double2* a = zsm;
+    double2* b = zsm + n;
+    double2* base = arrays[blockIdx.y] + (long long)blockIdx.x * dist;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a[k] = base[(long long)k * stride];
+    __syncthreads();
+    int ns = 1;
+    for (int s = 0; s < nfactors; ++s) {
+        const int radix = factors[s];
+        const int span = ns * radix;
+        const int tw_step = n / span;
+        const int in_step = n / radix;
+        for (int o = threadIdx.x; o < n; o += blockDim.x) {
+            const int q = (o / ns) % radix;
+            const int j = (o / span) * ns + (o % ns);
+            const int e0 = (j % ns) + q * ns;
+            double2 sum = make_double2(0.0, 0.0);
+            for (int r = 0; r < radix; ++r) {
+                double2 w = roots[(long long)((long long)r * e0 % span) * tw_step];
+                if (inverse) w.y = -w.y;
+                sum = zadd(sum, zmul(a[j + r * in_step], w));
+            }
+            b[o] = sum;
+        }
+        __syncthreads();
+        double2* t = a;
+        a = b;
+        b = t;
+        ns = span;
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        base[(long long)k * stride] = make_double2(a[k].x * scale, a[k].y * scale);
+}
+
+cudaError_t launch_fft_lines(double2* const* arrays, int count, int n, long long stride, long long dist, int lines,
+                             int inverse, const double2* roots, const int* factors, int nfactors, double scale,
+                             cudaStream_t s) {
+    const size_t smem = sizeof(double2) * 2 * (size_t)n;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fft_lines_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const int threads = n >= 256 ? 256 : (n >= 64 ? 64 : 32);
+    fft_lines_kernel<<<dim3(lines, count), threads, smem, s>>>(arrays, n, stride, dist, roots, factors, nfactors,
+                                                               inverse, scale);
+    return cudaGetLastError();
+}
+
+// Natural FP64 spectrum -> centred FP32 state (fftshift), anchor copy and
+// zero velocity for mPIE. The state row stride is M rounded up to even.
+__global__ void shift_to_state_kernel(double2* const* scratch, float2* const* object, float2* const* anchor,
+                                      float2* const* velocity, int m) {
+    const int tile = blockIdx.y;
+    const long long ms = m + (m & 1);
+    const long long total = (long long)m * ms;
+    const double2* src = scratch[tile];
+    float2* o = object[tile];
+    float2* a = anchor ? anchor[tile] : nullptr;
+    float2* v = velocity ? velocity[tile] : nullptr;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / ms), c = (int)(e % ms);
+        float2 val = make_float2(0.f, 0.f);
+        if (c < m) {
+            // fftshift_copy: dst[(r + m/2) % m] = src[r]  =>  src = (dst - m/2) mod m.
+            const int sr = (r + m - m / 2) % m, sc = (c + m - m / 2) % m;
+            const double2 z = src[(long long)sr * m + sc];
+            val = make_float2((float)z.x, (float)z.y);
+        }
+        o[e] = val;
+        if (a) a[e] = val;
+        if (v) v[e] = make_float2(0.f, 0.f);
+    }
+}
+
+cudaError_t launch_shift_to_state(double2* const* scratch, float2* const* object, float2* const* anchor,
+                                  float2* const* velocity, int count, int m, cudaStream_t s) {
+    const long long total = (long long)m * (m + (m & 1));
+    const int blocks = (int)((total + 255) / 256 < 512 ? (total + 255) / 256 : 512);
+    shift_to_state_kernel<<<dim3(blocks, count), 256, 0, s>>>(scratch, object, anchor, velocity, m);
+    return cudaGetLastError();
+}
+
+// Centred FP32 state -> natural FP64 scratch (ifftshift) before the inverse FFT.
+__global__ void state_to_natural_kernel(const float2* const* object, double2* const* scratch, int m) {
+    const int tile = blockIdx.y;
+    const long long ms = m + (m & 1);
+    const long long total = (long long)m * m;
+    const float2* o = object[tile];
+    double2* dst = scratch[tile];
+    const int h = (m + 1) / 2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / m), c = (int)(e % m);
+        const float2 v = o[(long long)r * ms + c];
+        dst[(long long)((r + h) % m) * m + (c + h) % m] = make_double2((double)v.x, (double)v.y);
+    }
+}
+
+cudaError_t launch_state_to_natural(const float2* const* object, double2* const* scratch, int count, int m,
+                                    cudaStream_t s) {
+    const long long total = (long long)m * m;
+    const int blocks = (int)((total + 255) / 256 < 512 ? (total + 255) / 256 : 512);
+    state_to_natural_kernel<<<dim3(blocks, count), 256, 0, s>>>(object, scratch, m);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ gauge
+
+constexpr int kGaugeThreads = 1024;
+
+struct ArgMax {
+    double weight;
+    long long index;
+    double2 value;
+};
+
+__device__ __forceinline__ void argmax_take(ArgMax& a, const ArgMax& b) {
+    if (b.weight > a.weight || (b.weight == a.weight && b.index < a.index && b.weight > 0.0)) a = b;
+}
+
+// Deterministic block reduction of (sum complex, sum real, argmax) triples.
+struct Reduction {
+    double2 sum;
+    double total;
+    ArgMax best;
+};
+
+__device__ Reduction block_reduce(Reduction v, Reduction* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Reduction other;
+        other.sum.x = __shfl_down_sync(0xffffffffu, v.sum.x, o);
+        other.sum.y = __shfl_down_sync(0xffffffffu, v.sum.y, o);
+        other.total = __shfl_down_sync(0xffffffffu, v.total, o);
+        other.best.weight = __shfl_down_sync(0xffffffffu, v.best.weight, o);
+        other.best.index = __shfl_down_sync(0xffffffffu, v.best.index, o);
+        other.best.value.x = __shfl_down_sync(0xffffffffu, v.best.value.x, o);
+        other.best.value.y = __shfl_down_sync(0xffffffffu, v.best.value.y, o);
+        v.sum = zadd(v.sum, other.sum);
+        v.total += other.total;
+        argmax_take(v.best, other.best);
+    }
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    Reduction r;
+    if (threadIdx.x == 0) {
+        r = scratch[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            r.sum = zadd(r.sum, scratch[w].sum);
+            r.total += scratch[w].total;
+            argmax_take(r.best, scratch[w].best);
+        }
+        scratch[0] = r;
+    }
+    __syncthreads();
+    r = scratch[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ Reduction empty_reduction() {
+    Reduction r;
+    r.sum = make_double2(0.0, 0.0);
+    r.total = 0.0;
+    r.best.weight = 0.0;
+    r.best.index = 0x7fffffffffffffffLL;
+    r.best.value = make_double2(0.0, 0.0);
+    return r;
+}
+
+__device__ __forceinline__ double2 load_z(const float2* p) {
+    const float2 v = *p;
+    return make_double2((double)v.x, (double)v.y);
+}
+
+__device__ __forceinline__ void store_z(float2* p, double2 z) { *p = make_float2((float)z.x, (float)z.y); }
+
+// relative_phase_slope (src/algorithms/gauge.rs:75-130).
+__device__ double phase_slope(const GaugeTile& T, int n, bool axis_row, double tol, Reduction* scratch) {
+    Reduction acc = empty_reduction();
+    const int rows = axis_row ? n - 1 : n, cols = axis_row ? n : n - 1;
+    for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
+        const int r = e / cols, c = e % cols;
+        const int cur = r * n + c;
+        const int nxt = axis_row ? (r + 1) * n + c : cur + 1;
+        if (T.support[cur] == 0 || T.support[nxt] == 0) continue;
+        const double2 ce = zmul(load_z(T.pupil + nxt), zconj(load_z(T.pupil + cur)));
+        const double2 re = zmul(T.reference[nxt], zconj(T.reference[cur]));
+        const double2 contribution = zmul(ce, zconj(re));
+        const double weight = hypot(contribution.x, contribution.y);
+        if (!isfinite(weight)) continue;
+        acc.sum = zadd(acc.sum, contribution);
+        acc.total += weight;
+        ArgMax b = {weight, (long long)cur, contribution};
+        argmax_take(acc.best, b);
+    }
+    Reduction r = block_reduce(acc, scratch);
+    if (r.total == 0.0) return 0.0;
+    if (hypot(r.sum.x, r.sum.y) > tol * r.total) return atan2(r.sum.y, r.sum.x);
+    if (r.best.weight > 0.0) return atan2(r.best.value.y, r.best.value.x);
+    return 0.0;
+}
+
+__global__ void __launch_bounds__(kGaugeThreads) gauge_kernel(const GaugeTile* tiles, int n, int m) {
+    __shared__ Reduction scratch[kGaugeThreads / 32];
+    __shared__ int s_fail;
+    const GaugeTile T = tiles[blockIdx.x];
+    const long long ms = m + (m & 1);
+    if (threadIdx.x == 0) s_fail = 0;
+    // support count
+    Reduction cnt = empty_reduction();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) cnt.total += T.support[e] != 0 ? 1.0 : 0.0;
+    cnt = block_reduce(cnt, scratch);
+    const double support_count = cnt.total;
+    if (support_count == 0.0) {
+        if (threadIdx.x == 0) atomicOr(T.status, 8);
+        return;
+    }
+    const double tol = 64.0 * 2.220446049250313e-16 * support_count;
+    const double row_slope = T.row_exact ? phase_slope(T, n, true, tol, scratch) : 0.0;
+    const double col_slope = T.col_exact ? phase_slope(T, n, false, tol, scratch) : 0.0;
+    if (fabs(row_slope) > tol || fabs(col_slope) > tol) {
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const double y = (double)(e / n) - (double)(n / 2), x = (double)(e % n) - (double)(n / 2);
+            double sn, cs;
+            sincos(-(row_slope * y + col_slope * x), &sn, &cs);
+            store_z(T.pupil + e, zmul(load_z(T.pupil + e), make_double2(cs, sn)));
+        }
+        for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+            const int r = (int)(e / m), c = (int)(e % m);
+            const double y = (double)r - (double)(m / 2), x = (double)c - (double)(m / 2);
+            double sn, cs;
+            sincos(row_slope * y + col_slope * x, &sn, &cs);
+            float2* p = T.object + (long long)r * ms + c;
+            store_z(p, zmul(load_z(p), make_double2(cs, sn)));
+        }
+        __syncthreads();
+    }
+    // normalize_pupil_scale_and_phase (src/algorithms/gauge.rs:158-240)
+    Reduction energy = empty_reduction();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        if (T.support[e] == 0) continue;
+        energy.sum.x += zabs2(T.reference[e]);
+        energy.sum.y += zabs2(load_z(T.pupil + e));
+    }
+    energy = block_reduce(energy, scratch);
+    const double ref_energy = energy.sum.x, cur_energy = energy.sum.y;
+    if (!isfinite(ref_energy) || ref_energy <= 0.0 || !isfinite(cur_energy) || cur_energy <= 0.0) {
+        if (threadIdx.x == 0) atomicOr(T.status, 8);
+        return;
+    }
+    const double computed = sqrt(ref_energy / cur_energy);
+    const double scale = fabs(computed - 1.0) <= tol ? 1.0 : computed;
+    Reduction overlap = empty_reduction();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        if (T.support[e] == 0) continue;
+        const double2 contribution = zmul(zconj(T.reference[e]), load_z(T.pupil + e));
+        const double weight = hypot(contribution.x, contribution.y);
+        overlap.sum = zadd(overlap.sum, contribution);
+        overlap.total += weight;
+        ArgMax b = {weight, (long long)e, contribution};
+        argmax_take(overlap.best, b);
+    }
+    overlap = block_reduce(overlap, scratch);
+    double phase;
+    if (overlap.total > 0.0 && hypot(overlap.sum.x, overlap.sum.y) > tol * overlap.total)
+        phase = atan2(overlap.sum.y, overlap.sum.x);
+    else if (overlap.best.weight > 0.0)
+        phase = atan2(overlap.best.value.y, overlap.best.value.x);
+    else {
+        if (threadIdx.x == 0) atomicOr(T.status, 8);
+        return;
+    }
+    if (fabs(phase) <= tol) phase = 0.0;
+    double sp, cp;
+    sincos(-phase, &sp, &cp);
+    const double2 pupil_factor = make_double2(scale * cp, scale * sp);
+    if (!(pupil_factor.x == 1.0 && pupil_factor.y == 0.0)) {
+        const double d = zabs2(pupil_factor);
+        const double2 object_factor = make_double2(pupil_factor.x / d, -pupil_factor.y / d);
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x)
+            store_z(T.pupil + e, zmul(load_z(T.pupil + e), pupil_factor));
+        for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+            float2* p = T.object + (e / m) * ms + (e % m);
+            store_z(p, zmul(load_z(p), object_factor));
+        }
+        __syncthreads();
+    }
+    // normalize_object_phase (src/algorithms/gauge.rs:242-282)
+    Reduction strongest = empty_reduction();
+    for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+        const double2 v = load_z(T.object + (e / m) * ms + (e % m));
+        if (!isfinite(v.x) || !isfinite(v.y)) s_fail = 1;
+        ArgMax b = {hypot(v.x, v.y), e, v};
+        argmax_take(strongest.best, b);
+    }
+    strongest = block_reduce(strongest, scratch);
+    if (s_fail) {
+        if (threadIdx.x == 0) atomicOr(T.status, 8);
+        return;
+    }
+    if (strongest.best.weight == 0.0) return;
+    const double2 dc = load_z(T.object + (long long)(m / 2) * ms + m / 2);
+    const double2 anchor = hypot(dc.x, dc.y) > tol * strongest.best.weight ? dc : strongest.best.value;
+    const double object_phase = atan2(anchor.y, anchor.x);
+    if (fabs(object_phase) <= tol) return;
+    double so, co;
+    sincos(-object_phase, &so, &co);
+    const double2 correction = make_double2(co, so);
+    for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+        float2* p = T.object + (e / m) * ms + (e % m);
+        store_z(p, zmul(load_z(p), correction));
+    }
+}
+
+cudaError_t launch_gauge(const GaugeTile* tiles, int count, int n, int m, cudaStream_t s) {
+    gauge_kernel<<<count, kGaugeThreads, 0, s>>>(tiles, n, m);
+    return cudaGetLastError();
+}
+
+}  // namespace fpm

@@ -1,0 +1,123 @@
+// Internal interface between the host runtime (runtime.cpp) and the device
+// kernels (engine.cu, grid.cu). Not part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fpm {
+
+// Per-frame constants, computed once per problem on the host in FP64 and
+// rounded to float. The bilinear stencil follows interpolation_axis
+// (src/model/crop.rs:266-313): rows lower_row .. lower_row + N (the last one
+// only when the row fraction is non-zero), likewise for columns.
+struct FrameParam {
+    int lower_row, lower_col;
+    int has_upper_row, has_upper_col;
+    float w00, w01, w10, w11;  // (lower,lower) (lower,upper) (upper,lower) (upper,upper)
+    float weight;              // measurement frame weight; 0 skips the frame
+    float gain;                // frame gain, > 0
+    float valid_scale;         // N*N / unmasked pixel count
+    float pad;
+    double loss_scale;         // weight / unmasked pixel count
+};
+
+// One reconstruction tile: device pointers into its resident buffers.
+struct TileDesc {
+    float2* object;            // M*M centred spectrum (state)
+    float2* pupil;             // N*N state pupil
+    const uint8_t* support;    // N*N
+    const float* meas;         // frames * N*N, engine-permuted layout
+    const uint8_t* masks;      // same layout, or null
+    const float* background;   // engine-permuted, or null
+    long long background_stride;  // floats between frames (0: one shared image)
+    const FrameParam* params;  // [frame_count]
+    const int* order;          // [frame_count] schedule, or null for sequential
+    float2* velocity;          // mPIE, M*M
+    float2* anchor;            // mPIE, M*M
+    double* partials;          // [iterations * cluster] objective partial sums
+    int* counter;              // mPIE effective frames since the last event
+    int* status;               // bit 0: non-finite momentum, bit 1: non-finite pupil
+    int M, frame_count;
+    float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
+    int pad;
+};
+
+enum EngineMode { kModeProjection = 0, kModeGradient = 1 };
+enum Denominator { kDenLocal = 0, kDenRpie = 1, kDenGlobal = 2 };
+
+struct EngineParams {
+    const TileDesc* tiles;
+    int mode;
+    int denominator;
+    float alpha, eps, object_step, pupil_step;
+    int recover_pupil, constrain_pupil;
+    int momentum, interval;
+    float friction, feedback;
+    int loss;
+    int it_begin, it_end;
+};
+
+// Forward-model (simulate) parameters: one model, cluster per frame.
+struct ForwardParams {
+    const float2* object;      // M*M centred spectrum
+    const float2* pupil;       // N*N
+    const FrameParam* params;  // [frame_count]
+    const float* background;   // natural layout, or null
+    long long background_stride;
+    float* out;                // frame_count * N*N natural-order intensities
+    int M, frame_count;
+};
+
+bool engine_supported(int n);
+cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t s);
+cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
+
+// Permutes natural-order frames [frames][N][N] into the engine layout.
+cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s);
+cudaError_t launch_permute_u8(int n, const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s);
+
+// Initial object (ReconstructionState::initialize_with_backend,
+// src/reconstruction/state.rs:280-355) for a batch of tiles of one size:
+// weighted mean amplitude -> nearest upsample into scratch (FP64).
+struct InitTile {
+    const float* meas;
+    const uint8_t* masks;
+    const float* background;
+    long long background_stride;
+    const FrameParam* params;
+    double2* scratch;          // M*M natural-order FP64 object
+    int* status;               // bit 2: no positive-weight unmasked pixel
+    int frames_count;
+    int pad;
+};
+// avg: [count * N*N] doubles; partial: [count * init_chunks(N) * 2] doubles.
+int init_chunks(int n);
+cudaError_t launch_init_mean(int n, int m, const InitTile* tiles, int count, double* avg, double* partial,
+                             cudaStream_t s);
+
+// FP64 mixed-radix line FFTs over a batch of arrays: lines of length n with
+// element stride `stride` and line distance `dist`, `lines` lines per array.
+cudaError_t launch_fft_lines(double2* const* arrays, int count, int n, long long stride, long long dist,
+                             int lines, int inverse, const double2* roots, const int* factors, int nfactors,
+                             double scale, cudaStream_t s);
+
+// Centred float state <-> natural FP64 scratch conversions.
+cudaError_t launch_shift_to_state(double2* const* scratch, float2* const* object, float2* const* anchor,
+                                  float2* const* velocity, int count, int m, cudaStream_t s);
+cudaError_t launch_state_to_natural(const float2* const* object, double2* const* scratch, int count, int m,
+                                    cudaStream_t s);
+
+// Object/pupil gauge canonicalisation (src/algorithms/gauge.rs:20-73), one
+// block per tile, FP64 reductions.
+struct GaugeTile {
+    float2* object;
+    float2* pupil;
+    const double2* reference;  // compiled pupil, FP64
+    const uint8_t* support;
+    int* status;               // bit 3: gauge failure
+    int row_exact, col_exact;  // every source offset is integer on that axis
+};
+cudaError_t launch_gauge(const GaugeTile* tiles, int count, int n, int m, cudaStream_t s);
+
+}  // namespace fpm

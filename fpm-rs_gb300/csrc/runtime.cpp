@@ -1,0 +1,1245 @@
+// Host runtime behind include/fpm_gpu.h: contexts, device-resident problems,
+// model compilation, and the reconstruction runner. Control flow follows
+// Runner::run (src/reconstruction/runner.rs:76-285): initialise the state,
+// canonicalise (EPRY), iterate the schedule, canonicalise per iteration,
+// record the weighted mean objective, and build the result. Every numerical
+// step runs on the GPU; there is no host fallback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "fpm_gpu.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_global_error;
+
+struct Status {
+    int32_t code = FPM_OK;
+    std::string message;
+    static Status ok() { return Status(); }
+    static Status make(int32_t c, const char* fmt, ...) {
+        Status s;
+        s.code = c;
+        char buf[1024];
+        va_list args;
+        va_start(args, fmt);
+        vsnprintf(buf, sizeof buf, fmt, args);
+        va_end(args);
+        s.message = buf;
+        return s;
+    }
+    explicit operator bool() const { return code != FPM_OK; }
+};
+
+#define FPM_CUDA(call)                                                                                        \
+    do {                                                                                                      \
+        cudaError_t err_ = (call);                                                                            \
+        if (err_ != cudaSuccess)                                                                              \
+            return Status::make(FPM_ERR_CUDA, "CUDA error %s (%s) at %s:%d", cudaGetErrorName(err_),          \
+                                cudaGetErrorString(err_), __FILE__, __LINE__);                                \
+    } while (0)
+
+#define FPM_TRY(expr)            \
+    do {                         \
+        Status st_ = (expr);     \
+        if (st_) return st_;     \
+    } while (0)
+
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    Status ensure(size_t n) {
+        if (n <= bytes && ptr) return Status::ok();
+        release();
+        if (n == 0) n = 16;
+        FPM_CUDA(cudaMalloc(&ptr, n));
+        bytes = n;
+        return Status::ok();
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(ptr);
+    }
+};
+
+struct FftPlan {
+    DeviceBuffer roots;
+    DeviceBuffer factors;
+    int nfactors = 0;
+};
+
+}  // namespace
+
+struct fpm_context {
+    int device = 0;
+    static constexpr int kStreams = 4;
+    cudaStream_t streams[kStreams] = {};
+    std::string error;
+    std::mutex mu;
+    std::map<int, std::unique_ptr<FftPlan>> plans;
+    DeviceBuffer staging;  // FP64 upload staging
+    DeviceBuffer scratch_a, scratch_b;
+    int engine_launches = 0;
+    double engine_ms = 0.0;
+    double engine_bytes = 0.0;
+};
+
+struct fpm_problem {
+    fpm_context* ctx = nullptr;
+    int n = 0, m = 0, frames = 0;
+    std::vector<int64_t> start_row, start_col;
+    std::vector<double> off_row, off_col, kx, ky, gains, weights, data_snr;
+    std::vector<uint8_t> support;
+    std::vector<double> pupil;  // complex128 interleaved
+    std::vector<fpm::FrameParam> params;
+    std::vector<double> stencil_cells;  // per frame: rows * cols of the bilinear stencil
+    bool has_masks = false, has_background = false;
+    long long background_stride = 0;
+    bool row_exact = true, col_exact = true;
+    double weight_sum = 0.0;
+    // resident device data
+    DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
+    // run state
+    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, avg, init_partial, order;
+};
+
+namespace {
+
+Status set_error(fpm_context* ctx, Status s) {
+    if (ctx) ctx->error = s.message;
+    g_global_error = s.message;
+    return s;
+}
+
+int32_t finish(fpm_context* ctx, const Status& s) {
+    if (s) set_error(ctx, s);
+    return s.code;
+}
+
+// ------------------------------------------------------------ geometry
+
+struct GridShift {
+    long long integer;
+    double offset;
+    long long lower, upper;
+};
+
+// checked_grid_shift (src/model/image_plane_fpm.rs:975-1024).
+Status grid_shift(double value, GridShift& g) {
+    if (!std::isfinite(value)) return Status::make(FPM_ERR_INVALID_MODEL, "illumination shift must be finite");
+    const double rounded = std::round(value);
+    g.integer = (long long)rounded;
+    g.offset = value - rounded;
+    const double nearest = std::round(g.offset);
+    if (std::fabs(g.offset - nearest) <= 1e-12) {
+        g.lower = g.upper = g.integer + (long long)nearest;
+    } else if (g.offset > 0.0) {
+        g.lower = g.integer;
+        g.upper = g.integer + 1;
+    } else {
+        g.lower = g.integer - 1;
+        g.upper = g.integer;
+    }
+    return Status::ok();
+}
+
+struct Axis {
+    long long lower_start;
+    bool upper;
+    double lower_weight, upper_weight;
+};
+
+// interpolation_axis (src/model/crop.rs:266-313).
+Status interpolation_axis(long long start, long long length, long long bound, double offset, Axis& a) {
+    if (length == 0 || bound == 0 || !std::isfinite(offset))
+        return Status::make(FPM_ERR_INVALID_MODEL, "subpixel crop dimensions and offset must be finite and non-zero");
+    const double nearest = std::round(offset);
+    double integer_offset, fraction;
+    if (std::fabs(offset - nearest) <= 1e-12) {
+        integer_offset = nearest;
+        fraction = 0.0;
+    } else {
+        integer_offset = std::floor(offset);
+        fraction = offset - integer_offset;
+    }
+    const long long lower = start + (long long)integer_offset;
+    if (lower < 0) return Status::make(FPM_ERR_INVALID_MODEL, "subpixel crop starts outside the grid");
+    const long long end = lower + length;
+    const bool upper = fraction > 0.0;
+    if (end > bound || (upper && end >= bound))
+        return Status::make(FPM_ERR_INVALID_MODEL, "subpixel crop interpolation stencil lies outside the grid");
+    a.lower_start = lower;
+    a.upper = upper;
+    a.lower_weight = 1.0 - fraction;
+    a.upper_weight = fraction;
+    return Status::ok();
+}
+
+Status validate_optics(const fpm_optics& o) {
+    const double v[6] = {o.wavelength_vacuum_m, o.objective_na, o.magnification, o.camera_pixel_size,
+                         o.illumination_refractive_index, o.objective_medium_refractive_index};
+    const char* names[6] = {"wavelength_vacuum_m", "objective_na", "magnification", "camera_pixel_size",
+                            "illumination_refractive_index", "objective_medium_refractive_index"};
+    for (int i = 0; i < 6; ++i)
+        if (!std::isfinite(v[i]) || v[i] <= 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "%s must be finite and positive, got %g", names[i], v[i]);
+    if (o.objective_na > o.objective_medium_refractive_index)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "objective_na cannot exceed the medium refractive index");
+    const double pixel = o.camera_pixel_size / o.magnification;
+    const double limit = o.wavelength_vacuum_m / (2.0 * o.objective_na);
+    if (!(pixel < limit))
+        return Status::make(FPM_ERR_INVALID_PARAMETER,
+                            "object-plane pitch camera_pixel_size / magnification (%.6e m) must be strictly less than "
+                            "wavelength_vacuum_m / (2 * objective_na) (%.6e m)",
+                            pixel, limit);
+    if (o.has_defocus && !std::isfinite(o.defocus_distance))
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "defocus_distance must be finite");
+    if (o.has_aberration) {
+        if (!std::isfinite(o.astigmatism) || !std::isfinite(o.coma) || !std::isfinite(o.spherical) ||
+            !std::isfinite(o.edge_apodization) || o.edge_apodization < 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_aberration coefficients are invalid");
+    }
+    return Status::ok();
+}
+
+struct Bounds {
+    long long min_row, max_row, min_col, max_col;
+};
+
+Status displacement_bounds(const fpm_optics& o, int n, const double* kx, const double* ky, int h, int w, Bounds& b) {
+    if (h <= 0 || w <= 0) return Status::make(FPM_ERR_INVALID_SHAPE, "image shape (%d, %d) must be non-zero", h, w);
+    if (n <= 0) return Status::make(FPM_ERR_INVALID_MODEL, "illumination must contain at least one frame");
+    const double pixel = o.camera_pixel_size / o.magnification;
+    const double dkx = 2.0 * M_PI / ((double)w * pixel), dky = 2.0 * M_PI / ((double)h * pixel);
+    b = {LLONG_MAX, LLONG_MIN, LLONG_MAX, LLONG_MIN};
+    for (int i = 0; i < n; ++i) {
+        GridShift r{}, c{};
+        FPM_TRY(grid_shift(ky[i] / dky, r));
+        FPM_TRY(grid_shift(kx[i] / dkx, c));
+        b.min_row = std::min(b.min_row, r.lower);
+        b.max_row = std::max(b.max_row, r.upper);
+        b.min_col = std::min(b.min_col, c.lower);
+        b.max_col = std::max(b.max_col, c.upper);
+    }
+    return Status::ok();
+}
+
+bool axis_contains(long long len, long long recon, long long lo, long long hi) {
+    const long long base = recon / 2 - len / 2;
+    return base + lo >= 0 && base + (len - 1) + hi < recon;
+}
+
+bool fits(int h, int w, long long mh, long long mw, const Bounds& b) {
+    return axis_contains(h, mh, b.min_row, b.max_row) && axis_contains(w, mw, b.min_col, b.max_col);
+}
+
+void smooth_visit(long long value, int prime, long long minimum, long long& best) {
+    static const long long primes[4] = {2, 3, 5, 7};
+    if (value >= minimum) {
+        if (best < 0 || value < best) best = value;
+        return;
+    }
+    for (int i = prime; i < 4; ++i) {
+        const long long next = value * primes[i];
+        if (best < 0 || next < best) smooth_visit(next, i, minimum, best);
+    }
+}
+
+// resolve_reconstruction_shape (src/model/image_plane_fpm.rs:287-348).
+Status resolve_shape(int h, int w, int policy, int& mh, int& mw, const Bounds& b) {
+    if (policy == FPM_SHAPE_EXACT) {
+        if (mh < h || mw < w)
+            return Status::make(FPM_ERR_INVALID_SHAPE, "image shape (%d, %d) must fit reconstruction shape (%d, %d)", h,
+                                w, mh, mw);
+        if ((long long)mh * w != (long long)mw * h)
+            return Status::make(FPM_ERR_INVALID_SHAPE, "reconstruction must use the same scale factor in both dimensions");
+        if (!fits(h, w, mh, mw, b))
+            return Status::make(FPM_ERR_INVALID_SHAPE,
+                                "reconstruction shape (%d, %d) does not contain every illumination crop and subpixel "
+                                "interpolation stencil",
+                                mh, mw);
+        return Status::ok();
+    }
+    if (policy < 0 || policy > 3) return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown reconstruction shape policy");
+    const long long d = std::gcd((long long)h, (long long)w);
+    const long long ah = h / d, aw = w / d;
+    const long long maximum = 1LL << 30;
+    long long mult;
+    if (fits(h, w, ah * d, aw * d, b)) {
+        mult = d;
+    } else {
+        long long lower = d, upper = d;
+        for (;;) {
+            upper = std::min(upper * 2, maximum);
+            if (upper == lower)
+                return Status::make(FPM_ERR_INVALID_SHAPE,
+                                    "illumination crops require a reconstruction shape outside the supported index range");
+            if (fits(h, w, ah * upper, aw * upper, b)) break;
+            lower = upper;
+        }
+        while (lower + 1 < upper) {
+            const long long mid = lower + (upper - lower) / 2;
+            if (fits(h, w, ah * mid, aw * mid, b))
+                upper = mid;
+            else
+                lower = mid;
+        }
+        mult = upper;
+    }
+    if (policy == FPM_SHAPE_SMOOTH) {
+        long long best = -1;
+        smooth_visit(1, 0, mult, best);
+        mult = best;
+    } else if (policy == FPM_SHAPE_POWER_OF_TWO) {
+        long long p = 1;
+        while (p < mult) p <<= 1;
+        mult = p;
+    }
+    mh = (int)(ah * mult);
+    mw = (int)(aw * mult);
+    return Status::ok();
+}
+
+// ------------------------------------------------------------- FFT plans
+
+std::vector<int> prime_factors(int n) {
+    std::vector<int> f;
+    for (int p = 2; (long long)p * p <= n; ++p)
+        while (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        }
+    if (n > 1) f.push_back(n);
+    return f;
+}
+
+Status get_plan(fpm_context* ctx, int n, FftPlan*& out) {
+    auto it = ctx->plans.find(n);
+    if (it != ctx->plans.end()) {
+        out = it->second.get();
+        return Status::ok();
+    }
+    if (n > 4096) return Status::make(FPM_ERR_UNSUPPORTED, "FP64 line FFT supports lengths up to 4096, got %d", n);
+    auto plan = std::make_unique<FftPlan>();
+    std::vector<double> roots(2 * (size_t)n);
+    for (int k = 0; k < n; ++k) {
+        const double a = 2.0 * M_PI * (double)k / (double)n;
+        roots[2 * k] = std::cos(a);
+        roots[2 * k + 1] = -std::sin(a);
+    }
+    std::vector<int> f = prime_factors(n);
+    FPM_TRY(plan->roots.ensure(roots.size() * sizeof(double)));
+    FPM_TRY(plan->factors.ensure(std::max<size_t>(f.size(), 1) * sizeof(int)));
+    FPM_CUDA(cudaMemcpy(plan->roots.ptr, roots.data(), roots.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!f.empty()) FPM_CUDA(cudaMemcpy(plan->factors.ptr, f.data(), f.size() * sizeof(int), cudaMemcpyHostToDevice));
+    plan->nfactors = (int)f.size();
+    out = plan.get();
+    ctx->plans[n] = std::move(plan);
+    return Status::ok();
+}
+
+// Forward (scaled by 1/(h*w)) or inverse 2-D transform of `count` natural
+// FP64 arrays of shape (h, w): rows, then columns, as CpuBackend::fft2.
+Status fft2_device(fpm_context* ctx, double2* const* arrays_dev, int count, int h, int w, bool inverse,
+                   cudaStream_t s) {
+    FftPlan* pw = nullptr;
+    FftPlan* ph = nullptr;
+    FPM_TRY(get_plan(ctx, w, pw));
+    FPM_TRY(get_plan(ctx, h, ph));
+    FPM_CUDA(fpm::launch_fft_lines(arrays_dev, count, w, 1, w, h, inverse ? 1 : 0, pw->roots.as<double2>(),
+                                   pw->factors.as<int>(), pw->nfactors, 1.0, s));
+    const double scale = inverse ? 1.0 : 1.0 / ((double)h * (double)w);
+    FPM_CUDA(fpm::launch_fft_lines(arrays_dev, count, h, w, 1, w, inverse ? 1 : 0, ph->roots.as<double2>(),
+                                   ph->factors.as<int>(), ph->nfactors, scale, s));
+    return Status::ok();
+}
+
+// ------------------------------------------------------------- problems
+
+Status validate_model(const fpm_model_desc* md) {
+    if (!md) return Status::make(FPM_ERR_INVALID_MODEL, "model descriptor is null");
+    const int h = md->image_height, w = md->image_width;
+    if (h <= 0 || w <= 0) return Status::make(FPM_ERR_INVALID_SHAPE, "image shape (%d, %d) must be non-zero", h, w);
+    if (md->recon_height < h || md->recon_width < w)
+        return Status::make(FPM_ERR_INVALID_MODEL, "reconstruction shape must contain a low-resolution crop");
+    if (md->sources <= 0) return Status::make(FPM_ERR_INVALID_MODEL, "0 source k-vectors and crops; counts must be equal and non-zero");
+    if (!md->crop_start_row || !md->crop_start_col || !md->pupil || !md->support)
+        return Status::make(FPM_ERR_INVALID_MODEL, "model crops, pupil and support are required");
+    const size_t n = (size_t)h * w;
+    for (size_t i = 0; i < n; ++i) {
+        if (!std::isfinite(md->pupil[2 * i]) || !std::isfinite(md->pupil[2 * i + 1]) || md->support[i] > 1)
+            return Status::make(FPM_ERR_INVALID_MODEL, "pupil support or numeric values are invalid");
+    }
+    for (int s = 0; s < md->sources; ++s) {
+        const long long sr = md->crop_start_row[s], sc = md->crop_start_col[s];
+        if (sr < 0 || sc < 0 || sr + h > md->recon_height || sc + w > md->recon_width)
+            return Status::make(FPM_ERR_INVALID_MODEL, "crop %d lies outside reconstruction shape", s);
+        const double orow = md->offset_row ? md->offset_row[s] : 0.0;
+        const double ocol = md->offset_col ? md->offset_col[s] : 0.0;
+        Axis a{};
+        FPM_TRY(interpolation_axis(sr, h, md->recon_height, orow, a));
+        FPM_TRY(interpolation_axis(sc, w, md->recon_width, ocol, a));
+        if (md->frame_gains && (!std::isfinite(md->frame_gains[s]) || md->frame_gains[s] < 0.0))
+            return Status::make(FPM_ERR_INVALID_MODEL, "frame gains must be finite and non-negative");
+    }
+    if (md->background) {
+        if (md->background_len != (int64_t)n && md->background_len != (int64_t)n * md->sources)
+            return Status::make(FPM_ERR_INVALID_MODEL, "background must be one image or one image per frame");
+        for (int64_t i = 0; i < md->background_len; ++i)
+            if (!std::isfinite(md->background[i]))
+                return Status::make(FPM_ERR_INVALID_MODEL, "background values must be finite");
+    }
+    return Status::ok();
+}
+
+Status validate_measurements(const fpm_model_desc* md, const fpm_measurement_desc* ms) {
+    if (!ms || !ms->measurements) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements are required");
+    if (ms->frames != md->sources)
+        return Status::make(FPM_ERR_INVALID_MODEL, "%d measurement frames but %d model frames", ms->frames, md->sources);
+    const size_t n = (size_t)md->image_height * md->image_width;
+    const size_t total = n * ms->frames;
+    for (size_t i = 0; i < total; ++i)
+        if (!std::isfinite(ms->measurements[i]))
+            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
+    int positive = 0;
+    for (int f = 0; f < ms->frames; ++f) {
+        const double wgt = ms->frame_weights ? ms->frame_weights[f] : 1.0;
+        if (!std::isfinite(wgt) || wgt < 0.0)
+            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "frame %d has invalid weight %g", f, wgt);
+        if (wgt > 0.0) {
+            ++positive;
+            if (ms->masks) {
+                const uint8_t* m = ms->masks + (size_t)f * n;
+                bool any = false;
+                for (size_t i = 0; i < n && !any; ++i) any = m[i] != 0;
+                if (!any)
+                    return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "positive-weight frame %d has no unmasked pixels", f);
+            }
+        }
+    }
+    if (positive == 0) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "at least one frame must have positive weight");
+    return Status::ok();
+}
+
+Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_measurement_desc* ms, fpm_problem** out) {
+    FPM_TRY(validate_model(md));
+    FPM_TRY(validate_measurements(md, ms));
+    const int h = md->image_height, w = md->image_width;
+    if (h != w || !fpm::engine_supported(h))
+        return Status::make(FPM_ERR_UNSUPPORTED,
+                            "the GB300 device path supports square detector frames of 32, 64, 128 or 256 pixels, got (%d, %d)",
+                            h, w);
+    if (md->recon_height != md->recon_width)
+        return Status::make(FPM_ERR_UNSUPPORTED, "the GB300 device path supports square reconstruction grids");
+    auto p = std::make_unique<fpm_problem>();
+    p->ctx = ctx;
+    p->n = h;
+    p->m = md->recon_height;
+    p->frames = ms->frames;
+    const int N = h, F = ms->frames;
+    const size_t n2 = (size_t)N * N;
+    p->start_row.assign(md->crop_start_row, md->crop_start_row + F);
+    p->start_col.assign(md->crop_start_col, md->crop_start_col + F);
+    p->off_row.assign(F, 0.0);
+    p->off_col.assign(F, 0.0);
+    if (md->offset_row) p->off_row.assign(md->offset_row, md->offset_row + F);
+    if (md->offset_col) p->off_col.assign(md->offset_col, md->offset_col + F);
+    p->kx.assign(F, 0.0);
+    p->ky.assign(F, 0.0);
+    if (md->kx) p->kx.assign(md->kx, md->kx + F);
+    if (md->ky) p->ky.assign(md->ky, md->ky + F);
+    p->gains.assign(F, 1.0);
+    if (md->frame_gains) p->gains.assign(md->frame_gains, md->frame_gains + F);
+    p->weights.assign(F, 1.0);
+    if (ms->frame_weights) p->weights.assign(ms->frame_weights, ms->frame_weights + F);
+    p->support.assign(md->support, md->support + n2);
+    p->pupil.assign(md->pupil, md->pupil + 2 * n2);
+    p->has_masks = ms->masks != nullptr;
+    p->has_background = md->background != nullptr;
+    p->background_stride = (md->background && md->background_len != (int64_t)n2) ? (long long)n2 : 0;
+
+    // Frame constants (FP64 on the host, rounded once).
+    p->params.resize(F);
+    p->stencil_cells.resize(F);
+    p->data_snr.assign(F, 0.0);
+    for (int f = 0; f < F; ++f) {
+        Axis r{}, c{};
+        FPM_TRY(interpolation_axis(p->start_row[f], N, p->m, p->off_row[f], r));
+        FPM_TRY(interpolation_axis(p->start_col[f], N, p->m, p->off_col[f], c));
+        if (std::fabs(p->off_row[f]) > 1e-12) p->row_exact = false;
+        if (std::fabs(p->off_col[f]) > 1e-12) p->col_exact = false;
+        const bool zero = std::fabs(p->off_row[f]) <= 1e-12 && std::fabs(p->off_col[f]) <= 1e-12;
+        fpm::FrameParam fp{};
+        if (zero) {
+            // extract_standard: integer crop at the stored origin.
+            fp.lower_row = (int)p->start_row[f];
+            fp.lower_col = (int)p->start_col[f];
+            fp.has_upper_row = fp.has_upper_col = 0;
+            fp.w00 = 1.f;
+            fp.w01 = fp.w10 = fp.w11 = 0.f;
+        } else {
+            fp.lower_row = (int)r.lower_start;
+            fp.lower_col = (int)c.lower_start;
+            fp.has_upper_row = r.upper ? 1 : 0;
+            fp.has_upper_col = c.upper ? 1 : 0;
+            fp.w00 = (float)(r.lower_weight * c.lower_weight);
+            fp.w01 = (float)(r.lower_weight * c.upper_weight);
+            fp.w10 = (float)(r.upper_weight * c.lower_weight);
+            fp.w11 = (float)(r.upper_weight * c.upper_weight);
+        }
+        p->stencil_cells[f] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
+        long long valid = (long long)n2;
+        if (ms->masks) {
+            valid = 0;
+            const uint8_t* mk = ms->masks + (size_t)f * n2;
+            for (size_t i = 0; i < n2; ++i) valid += mk[i] != 0;
+        }
+        fp.weight = (float)p->weights[f];
+        if (p->weights[f] > 0.0 && !(p->gains[f] > 0.0))
+            return Status::make(FPM_ERR_INVALID_MODEL, "state frame %d has invalid gain %g", f, p->gains[f]);
+        fp.gain = (float)(p->gains[f] > 0.0 ? p->gains[f] : 1.0);
+        fp.valid_scale = valid > 0 ? (float)((double)n2 / (double)valid) : 0.f;
+        fp.loss_scale = valid > 0 ? p->weights[f] / (double)valid : 0.0;
+        p->params[f] = fp;
+        p->weight_sum += p->weights[f];
+        // snr_weighted schedule score (src/reconstruction/schedule.rs:104-128).
+        if (p->weights[f] == 0.0) {
+            p->data_snr[f] = -INFINITY;
+        } else {
+            const double* m = ms->measurements + (size_t)f * n2;
+            double sum = 0.0;
+            long long cnt = 0;
+            for (size_t i = 0; i < n2; ++i) {
+                if (ms->masks && ms->masks[(size_t)f * n2 + i] == 0) continue;
+                double bg = 0.0;
+                if (md->background) bg = md->background[p->background_stride ? (size_t)f * n2 + i : i];
+                sum += std::max(m[i] - bg, 0.0);
+                ++cnt;
+            }
+            p->data_snr[f] = cnt == 0 ? -INFINITY : p->weights[f] * std::sqrt(sum / (double)cnt);
+        }
+    }
+
+    cudaStream_t s = ctx->streams[0];
+    // Measurements: FP64 upload, permuted to the engine's FP32 layout.
+    const size_t total = n2 * F;
+    FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
+    FPM_TRY(p->meas.ensure(total * sizeof(float)));
+    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->meas.as<float>(), F, s));
+    if (ms->masks) {
+        FPM_TRY(p->masks.ensure(total));
+        FPM_TRY(ctx->scratch_a.ensure(total));
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
+    }
+    if (md->background) {
+        const long long bg_frames = p->background_stride ? F : 1;
+        FPM_CUDA(cudaStreamSynchronize(s));
+        FPM_TRY(ctx->staging.ensure((size_t)md->background_len * sizeof(double)));
+        FPM_TRY(p->background.ensure((size_t)md->background_len * sizeof(float)));
+        FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, md->background, (size_t)md->background_len * sizeof(double),
+                                 cudaMemcpyHostToDevice, s));
+        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->background.as<float>(), bg_frames, s));
+    }
+    FPM_TRY(p->frame_params.ensure(sizeof(fpm::FrameParam) * F));
+    FPM_CUDA(cudaMemcpyAsync(p->frame_params.ptr, p->params.data(), sizeof(fpm::FrameParam) * F, cudaMemcpyHostToDevice, s));
+    FPM_TRY(p->support_d.ensure(n2));
+    FPM_CUDA(cudaMemcpyAsync(p->support_d.ptr, p->support.data(), n2, cudaMemcpyHostToDevice, s));
+    FPM_TRY(p->pupil_ref.ensure(n2 * sizeof(double2)));
+    FPM_CUDA(cudaMemcpyAsync(p->pupil_ref.ptr, p->pupil.data(), n2 * sizeof(double2), cudaMemcpyHostToDevice, s));
+    std::vector<float2> pf(n2);
+    for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)p->pupil[2 * i], (float)p->pupil[2 * i + 1]);
+    FPM_TRY(p->pupil_model.ensure(n2 * sizeof(float2)));
+    FPM_CUDA(cudaMemcpyAsync(p->pupil_model.ptr, pf.data(), n2 * sizeof(float2), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(cudaStreamSynchronize(s));
+    *out = p.release();
+    return Status::ok();
+}
+
+// ------------------------------------------------------------------ runs
+
+Status validate_params(const fpm_algorithm_params* a) {
+    if (!a) return Status::make(FPM_ERR_INVALID_PARAMETER, "algorithm parameters are required");
+    if (a->algorithm < FPM_ALG_AP || a->algorithm > FPM_ALG_GD)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown algorithm %d", a->algorithm);
+    if (a->iterations < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "iterations must be non-negative");
+    if (!std::isfinite(a->object_step) || a->object_step <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "object_step must be finite and positive");
+    if (!std::isfinite(a->epsilon) || a->epsilon <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "epsilon must be finite and positive");
+    if (a->batch_size <= 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "batch_size must be greater than zero");
+    if (a->loss_type < 0 || a->loss_type > 3) return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown loss_type");
+    if (a->schedule < 0 || a->schedule > 3) return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown schedule");
+    if (a->algorithm == FPM_ALG_FPIE || a->algorithm == FPM_ALG_MPIE) {
+        if (!std::isfinite(a->stability) || a->stability < 0.0 || a->stability > 1.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "stability must be finite and between zero and one");
+    }
+    if (a->algorithm == FPM_ALG_MPIE) {
+        if (a->momentum_interval <= 0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "momentum_interval must be greater than zero");
+        if (!std::isfinite(a->momentum_friction) || a->momentum_friction < 0.0 || a->momentum_friction >= 1.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "momentum_friction must be finite, at least zero, and less than one");
+        if (!std::isfinite(a->momentum_feedback) || a->momentum_feedback < 0.0 || a->momentum_feedback > 1.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "momentum_feedback must be finite and between zero and one");
+    }
+    if (a->algorithm == FPM_ALG_EPRY) {
+        if (!std::isfinite(a->pupil_step) || a->pupil_step < 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_step must be finite and non-negative");
+        if (a->recover_frame_gains || a->recover_background)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "EPRY frame-gain and background recovery are not implemented on the GB300 device path");
+    }
+    if (a->algorithm == FPM_ALG_GD) {
+        if (a->batch_size != 1)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "the GB300 device path runs gradient descent with batch_size 1 (the reference default)");
+        if (a->poisson_truncation || a->recover_pupil)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "gradient-descent truncation and pupil recovery are not implemented on the GB300 device path");
+    }
+    return Status::ok();
+}
+
+// FrameSchedule::order_for_problem (src/reconstruction/schedule.rs:35-102).
+std::vector<int> schedule_order(const fpm_problem* p, int schedule) {
+    std::vector<int> order(p->frames);
+    std::iota(order.begin(), order.end(), 0);
+    if (schedule == FPM_SCHEDULE_SEQUENTIAL) return order;
+    auto key = [](double v) {
+        int64_t bits;
+        std::memcpy(&bits, &v, sizeof bits);
+        bits ^= (int64_t)(((uint64_t)(bits >> 63)) >> 1);
+        return bits;
+    };
+    std::vector<std::pair<int64_t, int64_t>> keys(p->frames);
+    for (int f = 0; f < p->frames; ++f) {
+        if (schedule == FPM_SCHEDULE_SNR_WEIGHTED) {
+            keys[f] = {key(-p->data_snr[f]), 0};
+        } else {
+            const double radius = std::hypot(p->kx[f], p->ky[f]);
+            double angle = 0.0;
+            if (schedule == FPM_SCHEDULE_SPIRAL_OUT) {
+                angle = std::fmod(std::atan2(p->ky[f], p->kx[f]), 2.0 * M_PI);
+                if (angle < 0.0) angle += 2.0 * M_PI;
+            }
+            keys[f] = {key(radius), key(angle)};
+        }
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return keys[a] < keys[b]; });
+    return order;
+}
+
+struct Bucket {
+    int n, m;
+    std::vector<fpm_problem*> problems;
+    std::vector<int> indices;
+};
+
+template <class T>
+Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
+    FPM_TRY(buf.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) FPM_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return Status::ok();
+}
+
+struct BucketRun {
+    DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs;
+    std::vector<cudaEvent_t> events;
+    double bytes = 0.0;
+    ~BucketRun() {
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+    }
+};
+
+Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cudaStream_t s, BucketRun& br) {
+    const int N = b.n, M = b.m, count = (int)b.problems.size();
+    const int C = N / 32;
+    const long long ms = M + (M & 1);
+    const bool mpie = a->algorithm == FPM_ALG_MPIE;
+    const bool epry = a->algorithm == FPM_ALG_EPRY;
+    const bool canonical = epry && a->recover_pupil;
+    const int iters = a->iterations;
+    std::vector<fpm::TileDesc> tiles(count);
+    std::vector<fpm::InitTile> inits(count);
+    std::vector<fpm::GaugeTile> gauges(count);
+    std::vector<double2*> scratch(count);
+    std::vector<float2*> objects(count), anchors(count), velocities(count);
+    float max_pupil_power = 0.f;
+    for (int t = 0; t < count; ++t) {
+        fpm_problem* p = b.problems[t];
+        const size_t n2 = (size_t)N * N;
+        FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
+        FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
+        FPM_TRY(p->partials.ensure(sizeof(double) * std::max(iters, 1) * C));
+        FPM_TRY(p->counter.ensure(sizeof(int)));
+        FPM_TRY(p->status.ensure(sizeof(int)));
+        FPM_TRY(p->scratch64.ensure(sizeof(double2) * (size_t)M * M));
+        FPM_TRY(p->avg.ensure(sizeof(double) * n2));
+        FPM_TRY(p->init_partial.ensure(sizeof(double) * 2 * fpm::init_chunks(N)));
+        if (mpie) {
+            FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
+            FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
+        }
+        FPM_CUDA(cudaMemsetAsync(p->status.ptr, 0, sizeof(int), s));
+        FPM_CUDA(cudaMemsetAsync(p->counter.ptr, 0, sizeof(int), s));
+        FPM_CUDA(cudaMemcpyAsync(p->pupil_state.ptr, p->pupil_model.ptr, sizeof(float2) * n2, cudaMemcpyDeviceToDevice, s));
+        const int* order_dev = nullptr;
+        if (a->schedule != FPM_SCHEDULE_SEQUENTIAL) {
+            FPM_TRY(upload_array(p->order, schedule_order(p, a->schedule), s));
+            order_dev = p->order.as<int>();
+        }
+        // max(max |P|^2, eps) of the compiled pupil, FP64.
+        double mp = 0.0;
+        for (size_t i = 0; i < n2; ++i)
+            mp = std::max(mp, p->pupil[2 * i] * p->pupil[2 * i] + p->pupil[2 * i + 1] * p->pupil[2 * i + 1]);
+        mp = std::max(mp, a->epsilon);
+        max_pupil_power = (float)mp;
+        fpm::TileDesc& T = tiles[t];
+        T.object = p->object.as<float2>();
+        T.pupil = p->pupil_state.as<float2>();
+        T.support = p->support_d.as<uint8_t>();
+        T.meas = p->meas.as<float>();
+        T.masks = p->has_masks ? p->masks.as<uint8_t>() : nullptr;
+        T.background = p->has_background ? p->background.as<float>() : nullptr;
+        T.background_stride = p->background_stride;
+        T.params = p->frame_params.as<fpm::FrameParam>();
+        T.order = order_dev;
+        T.velocity = mpie ? p->velocity.as<float2>() : nullptr;
+        T.anchor = mpie ? p->anchor.as<float2>() : nullptr;
+        T.partials = p->partials.as<double>();
+        T.counter = p->counter.as<int>();
+        T.status = p->status.as<int>();
+        T.M = M;
+        T.frame_count = p->frames;
+        T.max_pupil_power = max_pupil_power;
+        fpm::InitTile& I = inits[t];
+        I.meas = T.meas;
+        I.masks = T.masks;
+        I.background = T.background;
+        I.background_stride = T.background_stride;
+        I.params = T.params;
+        I.scratch = p->scratch64.as<double2>();
+        I.status = T.status;
+        I.frames_count = p->frames;
+        fpm::GaugeTile& G = gauges[t];
+        G.object = T.object;
+        G.pupil = T.pupil;
+        G.reference = p->pupil_ref.as<double2>();
+        G.support = T.support;
+        G.status = T.status;
+        G.row_exact = p->row_exact ? 1 : 0;
+        G.col_exact = p->col_exact ? 1 : 0;
+        scratch[t] = p->scratch64.as<double2>();
+        objects[t] = T.object;
+        anchors[t] = T.anchor;
+        velocities[t] = T.velocity;
+        // Algorithmic bytes of the engine for this tile.
+        double frame_bytes = 0.0;
+        int effective = 0;
+        for (int f = 0; f < p->frames; ++f) {
+            if (p->params[f].weight == 0.f) continue;
+            ++effective;
+            frame_bytes += 16.0 * p->stencil_cells[f] + 4.0 * (double)n2 + (p->has_masks ? (double)n2 : 0.0) +
+                           (canonical ? 16.0 * (double)n2 : 0.0);
+        }
+        br.bytes += frame_bytes * iters;
+        if (mpie && a->momentum_interval > 0)
+            br.bytes += 48.0 * (double)M * (double)M * (double)((long long)effective * iters / a->momentum_interval);
+    }
+    FPM_TRY(upload_array(br.tiles, tiles, s));
+    FPM_TRY(upload_array(br.init, inits, s));
+    FPM_TRY(upload_array(br.gauge, gauges, s));
+    FPM_TRY(upload_array(br.scratch_ptrs, scratch, s));
+    FPM_TRY(upload_array(br.object_ptrs, objects, s));
+    FPM_TRY(upload_array(br.anchor_ptrs, anchors, s));
+    FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
+
+    // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift.
+    // avg/partial scratch: per tile buffers are contiguous only per problem,
+    // so run the mean pass one tile at a time into each problem's buffers.
+    for (int t = 0; t < count; ++t) {
+        fpm_problem* p = b.problems[t];
+        FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>() + t, 1, p->avg.as<double>(),
+                                       p->init_partial.as<double>(), s));
+    }
+    FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, false, s));
+    FPM_CUDA(fpm::launch_shift_to_state(br.scratch_ptrs.as<double2*>(), br.object_ptrs.as<float2*>(),
+                                        mpie ? br.anchor_ptrs.as<float2*>() : nullptr,
+                                        mpie ? br.velocity_ptrs.as<float2*>() : nullptr, count, M, s));
+    if (canonical) FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+
+    fpm::EngineParams ep{};
+    ep.tiles = br.tiles.as<fpm::TileDesc>();
+    ep.mode = a->algorithm == FPM_ALG_GD ? fpm::kModeGradient : fpm::kModeProjection;
+    switch (a->algorithm) {
+        case FPM_ALG_AP: ep.denominator = fpm::kDenLocal; break;
+        case FPM_ALG_FPIE:
+        case FPM_ALG_MPIE: ep.denominator = fpm::kDenRpie; break;
+        default: ep.denominator = fpm::kDenGlobal; break;
+    }
+    ep.alpha = (float)a->stability;
+    ep.eps = (float)a->epsilon;
+    ep.object_step = (float)a->object_step;
+    ep.pupil_step = (float)a->pupil_step;
+    ep.recover_pupil = canonical ? 1 : 0;
+    ep.constrain_pupil = a->constrain_pupil_support ? 1 : 0;
+    ep.momentum = mpie ? 1 : 0;
+    ep.interval = a->momentum_interval;
+    ep.friction = (float)a->momentum_friction;
+    ep.feedback = (float)a->momentum_feedback;
+    ep.loss = a->loss_type;
+    auto engine = [&](int it0, int it1) -> Status {
+        cudaEvent_t e0, e1;
+        FPM_CUDA(cudaEventCreate(&e0));
+        FPM_CUDA(cudaEventCreate(&e1));
+        br.events.push_back(e0);
+        br.events.push_back(e1);
+        ep.it_begin = it0;
+        ep.it_end = it1;
+        FPM_CUDA(cudaEventRecord(e0, s));
+        FPM_CUDA(fpm::launch_engine(N, ep, count, s));
+        FPM_CUDA(cudaEventRecord(e1, s));
+        return Status::ok();
+    };
+    if (iters > 0) {
+        if (epry) {
+            for (int it = 0; it < iters; ++it) {
+                FPM_TRY(engine(it, it + 1));
+                if (canonical) FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+            }
+        } else {
+            FPM_TRY(engine(0, iters));
+        }
+    }
+    // Finalise: ifftshift, inverse FFT (FP64) into scratch.
+    FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(br.object_ptrs.ptr),
+                                          br.scratch_ptrs.as<double2*>(), count, M, s));
+    FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, true, s));
+    return Status::ok();
+}
+
+Status collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_desc* r, cudaStream_t s) {
+    int status = 0;
+    FPM_CUDA(cudaMemcpyAsync(&status, p->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FPM_CUDA(cudaStreamSynchronize(s));
+    if (status & 4) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "no positive-weight, unmasked measurements are available");
+    if (status & 1) return Status::make(FPM_ERR_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
+    if (status & 8) return Status::make(FPM_ERR_NUMERICAL, "object/pupil gauge normalization failed on a non-finite or empty state");
+    if (!r) return Status::ok();
+    const int M = p->m, N = p->n, C = N / 32;
+    const long long ms = M + (M & 1);
+    if (r->object)
+        FPM_CUDA(cudaMemcpyAsync(r->object, p->scratch64.ptr, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+    std::vector<float2> spec;
+    if (r->object_spectrum) {
+        spec.resize((size_t)M * ms);
+        FPM_CUDA(cudaMemcpyAsync(spec.data(), p->object.ptr, sizeof(float2) * spec.size(), cudaMemcpyDeviceToHost, s));
+    }
+    std::vector<float2> pupil;
+    if (r->pupil) {
+        pupil.resize((size_t)N * N);
+        FPM_CUDA(cudaMemcpyAsync(pupil.data(), p->pupil_state.ptr, sizeof(float2) * pupil.size(), cudaMemcpyDeviceToHost, s));
+    }
+    std::vector<double> partials;
+    if (r->objectives && a->iterations > 0) {
+        partials.resize((size_t)a->iterations * C);
+        FPM_CUDA(cudaMemcpyAsync(partials.data(), p->partials.ptr, sizeof(double) * partials.size(), cudaMemcpyDeviceToHost, s));
+    }
+    FPM_CUDA(cudaStreamSynchronize(s));
+    if (r->object_spectrum)
+        for (int row = 0; row < M; ++row)
+            for (int col = 0; col < M; ++col) {
+                const float2 v = spec[(size_t)row * ms + col];
+                r->object_spectrum[2 * ((size_t)row * M + col)] = v.x;
+                r->object_spectrum[2 * ((size_t)row * M + col) + 1] = v.y;
+            }
+    if (r->pupil)
+        for (size_t i = 0; i < pupil.size(); ++i) {
+            r->pupil[2 * i] = pupil[i].x;
+            r->pupil[2 * i + 1] = pupil[i].y;
+        }
+    if (r->objectives)
+        for (int it = 0; it < a->iterations; ++it) {
+            double sum = 0.0;
+            for (int c = 0; c < C; ++c) sum += partials[(size_t)it * C + c];
+            r->objectives[it] = p->weight_sum > 0.0 ? sum / p->weight_sum : NAN;
+        }
+    r->completed_iterations = a->iterations;
+    return Status::ok();
+}
+
+Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                 fpm_result_desc* results) {
+    FPM_TRY(validate_params(a));
+    if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
+    std::vector<Bucket> buckets;
+    for (int i = 0; i < count; ++i) {
+        fpm_problem* p = problems[i];
+        if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
+        auto it = std::find_if(buckets.begin(), buckets.end(), [&](const Bucket& b) { return b.n == p->n && b.m == p->m; });
+        if (it == buckets.end()) {
+            buckets.push_back(Bucket{p->n, p->m, {}, {}});
+            it = buckets.end() - 1;
+        }
+        it->problems.push_back(p);
+        it->indices.push_back(i);
+    }
+    // Largest tiles first so the longest launches start earliest.
+    std::sort(buckets.begin(), buckets.end(), [](const Bucket& x, const Bucket& y) { return x.n > y.n; });
+    std::vector<std::unique_ptr<BucketRun>> runs;
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        runs.push_back(std::make_unique<BucketRun>());
+        FPM_TRY(run_bucket(ctx, buckets[k], a, ctx->streams[k % fpm_context::kStreams], *runs.back()));
+    }
+    ctx->engine_launches = 0;
+    ctx->engine_ms = 0.0;
+    ctx->engine_bytes = 0.0;
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
+        FPM_CUDA(cudaStreamSynchronize(s));
+        FPM_CUDA(cudaGetLastError());
+        for (size_t e = 0; e + 1 < runs[k]->events.size(); e += 2) {
+            float ms = 0.f;
+            FPM_CUDA(cudaEventElapsedTime(&ms, runs[k]->events[e], runs[k]->events[e + 1]));
+            ctx->engine_ms += ms;
+            ctx->engine_launches += 1;
+        }
+        ctx->engine_bytes += runs[k]->bytes;
+        for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
+            const int idx = buckets[k].indices[t];
+            FPM_TRY(collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr, s));
+        }
+    }
+    return Status::ok();
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+const char* fpm_global_last_error(void) { return g_global_error.c_str(); }
+
+int32_t fpm_create(fpm_context** out, int32_t device) {
+    if (!out) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "output pointer is null"));
+    auto ctx = std::make_unique<fpm_context>();
+    ctx->device = device;
+    auto init = [&]() -> Status {
+        int count = 0;
+        FPM_CUDA(cudaGetDeviceCount(&count));
+        if (device < 0 || device >= count)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "device %d is not available (%d devices)", device, count);
+        FPM_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop{};
+        FPM_CUDA(cudaGetDeviceProperties(&prop, device));
+        if (prop.major < 10)
+            return Status::make(FPM_ERR_UNSUPPORTED, "device %d (%s, sm_%d%d) is not a Blackwell GPU; this library targets sm_103a",
+                                device, prop.name, prop.major, prop.minor);
+        for (int i = 0; i < fpm_context::kStreams; ++i)
+            FPM_CUDA(cudaStreamCreateWithFlags(&ctx->streams[i], cudaStreamNonBlocking));
+        return Status::ok();
+    };
+    Status s = init();
+    if (s) return finish(nullptr, s);
+    *out = ctx.release();
+    return FPM_OK;
+}
+
+int32_t fpm_destroy(fpm_context* ctx) {
+    if (!ctx) return FPM_OK;
+    cudaSetDevice(ctx->device);
+    for (int i = 0; i < fpm_context::kStreams; ++i)
+        if (ctx->streams[i]) cudaStreamDestroy(ctx->streams[i]);
+    delete ctx;
+    return FPM_OK;
+}
+
+int32_t fpm_last_error(const fpm_context* ctx, char* buffer, size_t length) {
+    if (!buffer || length == 0) return FPM_ERR_INVALID_PARAMETER;
+    const std::string& msg = ctx ? ctx->error : g_global_error;
+    std::snprintf(buffer, length, "%s", msg.c_str());
+    return FPM_OK;
+}
+
+int32_t fpm_planar_led_kvectors(const fpm_optics* optics, int32_t rows, int32_t cols, double pitch_x, double pitch_y,
+                                double reference_col, double reference_row, const double* translation,
+                                const double* rotation_rad, double* kx, double* ky) {
+    auto body = [&]() -> Status {
+        if (!optics || !translation || !rotation_rad || !kx || !ky)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        FPM_TRY(validate_optics(*optics));
+        if (rows <= 0 || cols <= 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "shape rows and columns must be non-zero");
+        if (!std::isfinite(pitch_x) || !std::isfinite(pitch_y) || pitch_x <= 0.0 || pitch_y <= 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pitch_x and pitch_y must be finite and positive");
+        const double k = 2.0 * M_PI * optics->illumination_refractive_index / optics->wavelength_vacuum_m;
+        const double sx = std::sin(rotation_rad[0]), cx = std::cos(rotation_rad[0]);
+        const double sy = std::sin(rotation_rad[1]), cy = std::cos(rotation_rad[1]);
+        const double sz = std::sin(rotation_rad[2]), cz = std::cos(rotation_rad[2]);
+        for (int r = 0; r < rows; ++r)
+            for (int c = 0; c < cols; ++c) {
+                const double p[3] = {((double)c - reference_col) * pitch_x, ((double)r - reference_row) * pitch_y, 0.0};
+                const double ax[3] = {p[0], cx * p[1] - sx * p[2], sx * p[1] + cx * p[2]};
+                const double ay[3] = {cy * ax[0] + sy * ax[2], ax[1], -sy * ax[0] + cy * ax[2]};
+                const double az[3] = {cz * ay[0] - sz * ay[1], sz * ay[0] + cz * ay[1], ay[2]};
+                const double pos[3] = {az[0] + translation[0], az[1] + translation[1], az[2] + translation[2]};
+                const double norm = std::hypot(std::hypot(pos[0], pos[1]), pos[2]);
+                if (!std::isfinite(norm) || norm <= 0.0)
+                    return Status::make(FPM_ERR_INVALID_PARAMETER, "no source may coincide with the sample origin");
+                kx[r * cols + c] = k * (-pos[0] / norm);
+                ky[r * cols + c] = k * (-pos[1] / norm);
+            }
+        return Status::ok();
+    };
+    return finish(nullptr, body());
+}
+
+int32_t fpm_suggest_shape(const fpm_optics* optics, int32_t sources, const double* kx, const double* ky,
+                          int32_t image_height, int32_t image_width, int32_t policy, int32_t* recon_height,
+                          int32_t* recon_width) {
+    auto body = [&]() -> Status {
+        if (!optics || !kx || !ky || !recon_height || !recon_width)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        FPM_TRY(validate_optics(*optics));
+        Bounds b{};
+        FPM_TRY(displacement_bounds(*optics, sources, kx, ky, image_height, image_width, b));
+        int mh = *recon_height, mw = *recon_width;
+        FPM_TRY(resolve_shape(image_height, image_width, policy, mh, mw, b));
+        *recon_height = mh;
+        *recon_width = mw;
+        return Status::ok();
+    };
+    return finish(nullptr, body());
+}
+
+int32_t fpm_compile_model(const fpm_optics* optics, int32_t sources, const double* kx, const double* ky,
+                          int32_t h, int32_t w, int32_t policy, int32_t* recon_height, int32_t* recon_width,
+                          int64_t* start_row, int64_t* start_col, double* offset_row, double* offset_col,
+                          double* pupil, uint8_t* support, double* dkx_out, double* dky_out) {
+    auto body = [&]() -> Status {
+        if (!optics || !kx || !ky || !recon_height || !recon_width || !start_row || !start_col || !offset_row ||
+            !offset_col || !pupil || !support)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        FPM_TRY(validate_optics(*optics));
+        for (int s = 0; s < sources; ++s)
+            if (!std::isfinite(kx[s]) || !std::isfinite(ky[s]))
+                return Status::make(FPM_ERR_INVALID_MODEL, "k-vectors must contain finite values");
+        Bounds b{};
+        FPM_TRY(displacement_bounds(*optics, sources, kx, ky, h, w, b));
+        int mh = *recon_height, mw = *recon_width;
+        FPM_TRY(resolve_shape(h, w, policy, mh, mw, b));
+        const double low = optics->camera_pixel_size / optics->magnification;
+        const double dkx = 2.0 * M_PI / ((double)w * low), dky = 2.0 * M_PI / ((double)h * low);
+        // Pupil::circular (src/model/pupil.rs:78-123).
+        const double cutoff = 2.0 * M_PI * optics->objective_na / optics->wavelength_vacuum_m;
+        const double medium_k = 2.0 * M_PI * optics->objective_medium_refractive_index / optics->wavelength_vacuum_m;
+        for (int r = 0; r < h; ++r) {
+            const double y = ((double)r - (double)(h / 2)) * dky;
+            for (int c = 0; c < w; ++c) {
+                const double x = ((double)c - (double)(w / 2)) * dkx;
+                const double radius = std::hypot(x, y);
+                const size_t i = (size_t)r * w + c;
+                const bool inside = radius <= cutoff;
+                support[i] = inside ? 1 : 0;
+                if (!inside) {
+                    pupil[2 * i] = pupil[2 * i + 1] = 0.0;
+                    continue;
+                }
+                const double rho = cutoff > 0.0 ? radius / cutoff : 0.0;
+                const double theta = std::atan2(y, x);
+                double phase = 0.0, amplitude = 1.0;
+                if (optics->has_defocus) phase -= optics->defocus_distance * (x * x + y * y) / (2.0 * medium_k);
+                if (optics->has_aberration) {
+                    phase += optics->astigmatism * rho * rho * std::cos(2.0 * theta);
+                    phase += optics->coma * (3.0 * std::pow(rho, 3) - 2.0 * rho) * std::cos(theta);
+                    phase += optics->spherical * (6.0 * std::pow(rho, 4) - 6.0 * rho * rho + 1.0);
+                    amplitude = std::exp(-optics->edge_apodization * rho * rho);
+                }
+                pupil[2 * i] = amplitude * std::cos(phase);
+                pupil[2 * i + 1] = amplitude * std::sin(phase);
+            }
+        }
+        // crop_for_k_vector (src/model/image_plane_fpm.rs:750-797).
+        for (int s = 0; s < sources; ++s) {
+            GridShift row{}, col{};
+            FPM_TRY(grid_shift(ky[s] / dky, row));
+            FPM_TRY(grid_shift(kx[s] / dkx, col));
+            const long long sr = mh / 2 - h / 2 + row.integer, sc = mw / 2 - w / 2 + col.integer;
+            if (sr < 0 || sc < 0)
+                return Status::make(FPM_ERR_INVALID_MODEL, "illumination vector %d produces a crop outside the reconstruction grid", s);
+            Axis a{};
+            FPM_TRY(interpolation_axis(sr, h, mh, row.offset, a));
+            FPM_TRY(interpolation_axis(sc, w, mw, col.offset, a));
+            start_row[s] = sr;
+            start_col[s] = sc;
+            offset_row[s] = row.offset;
+            offset_col[s] = col.offset;
+        }
+        *recon_height = mh;
+        *recon_width = mw;
+        if (dkx_out) *dkx_out = dkx;
+        if (dky_out) *dky_out = dky;
+        return Status::ok();
+    };
+    return finish(nullptr, body());
+}
+
+int32_t fpm_fft2(fpm_context* ctx, double* values, int32_t height, int32_t width, int32_t inverse) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        if (!values) return Status::make(FPM_ERR_INVALID_PARAMETER, "values is null");
+        if (height <= 0 || width <= 0) return Status::make(FPM_ERR_INVALID_SHAPE, "FFT dimensions must be non-zero");
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->streams[0];
+        const size_t bytes = sizeof(double2) * (size_t)height * width;
+        FPM_TRY(ctx->scratch_a.ensure(bytes));
+        FPM_TRY(ctx->scratch_b.ensure(sizeof(double2*)));
+        double2* arr = ctx->scratch_a.as<double2>();
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, &arr, sizeof(double2*), cudaMemcpyHostToDevice, s));
+        FPM_CUDA(cudaMemcpyAsync(arr, values, bytes, cudaMemcpyHostToDevice, s));
+        FPM_TRY(fft2_device(ctx, ctx->scratch_b.as<double2*>(), 1, height, width, inverse != 0, s));
+        FPM_CUDA(cudaMemcpyAsync(values, arr, bytes, cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaStreamSynchronize(s));
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_forward_stack(fpm_context* ctx, const fpm_model_desc* md, const double* object, double* intensities) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        FPM_TRY(validate_model(md));
+        if (!object || !intensities) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        const int N = md->image_height, M = md->recon_height, F = md->sources;
+        if (md->image_width != N || !fpm::engine_supported(N) || md->recon_width != M)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "the GB300 device path supports square detector frames of 32, 64, 128 or 256 pixels");
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->streams[0];
+        const size_t n2 = (size_t)N * N, m2 = (size_t)M * M;
+        const long long ms = M + (M & 1);
+        // Frame constants (gains, stencils) as for a problem without masks.
+        std::vector<fpm::FrameParam> params(F);
+        for (int f = 0; f < F; ++f) {
+            Axis r{}, c{};
+            const double orow = md->offset_row ? md->offset_row[f] : 0.0, ocol = md->offset_col ? md->offset_col[f] : 0.0;
+            FPM_TRY(interpolation_axis(md->crop_start_row[f], N, M, orow, r));
+            FPM_TRY(interpolation_axis(md->crop_start_col[f], N, M, ocol, c));
+            fpm::FrameParam fp{};
+            const bool zero = std::fabs(orow) <= 1e-12 && std::fabs(ocol) <= 1e-12;
+            fp.lower_row = zero ? (int)md->crop_start_row[f] : (int)r.lower_start;
+            fp.lower_col = zero ? (int)md->crop_start_col[f] : (int)c.lower_start;
+            fp.has_upper_row = zero ? 0 : (r.upper ? 1 : 0);
+            fp.has_upper_col = zero ? 0 : (c.upper ? 1 : 0);
+            fp.w00 = zero ? 1.f : (float)(r.lower_weight * c.lower_weight);
+            fp.w01 = zero ? 0.f : (float)(r.lower_weight * c.upper_weight);
+            fp.w10 = zero ? 0.f : (float)(r.upper_weight * c.lower_weight);
+            fp.w11 = zero ? 0.f : (float)(r.upper_weight * c.upper_weight);
+            const double g = md->frame_gains ? md->frame_gains[f] : 1.0;
+            if (!(g > 0.0)) return Status::make(FPM_ERR_INVALID_MODEL, "frame %d has invalid gain %g", f, g);
+            fp.gain = (float)g;
+            fp.weight = 1.f;
+            params[f] = fp;
+        }
+        DeviceBuffer d_params, d_pupil, d_obj64, d_state, d_out, d_ptrs, d_ptrs2, d_bg;
+        FPM_TRY(upload_array(d_params, params, s));
+        std::vector<float2> pf(n2);
+        for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)md->pupil[2 * i], (float)md->pupil[2 * i + 1]);
+        FPM_TRY(upload_array(d_pupil, pf, s));
+        FPM_TRY(d_obj64.ensure(sizeof(double2) * m2));
+        FPM_CUDA(cudaMemcpyAsync(d_obj64.ptr, object, sizeof(double2) * m2, cudaMemcpyHostToDevice, s));
+        FPM_TRY(d_state.ensure(sizeof(float2) * (size_t)M * ms));
+        std::vector<double2*> p64 = {d_obj64.as<double2>()};
+        std::vector<float2*> pst = {d_state.as<float2>()};
+        FPM_TRY(upload_array(d_ptrs, p64, s));
+        FPM_TRY(upload_array(d_ptrs2, pst, s));
+        // object_spectrum (src/simulation/simulator.rs:209-226): forward FFT, fftshift.
+        FPM_TRY(fft2_device(ctx, d_ptrs.as<double2*>(), 1, M, M, false, s));
+        FPM_CUDA(fpm::launch_shift_to_state(d_ptrs.as<double2*>(), d_ptrs2.as<float2*>(), nullptr, nullptr, 1, M, s));
+        fpm::ForwardParams fwd{};
+        fwd.object = d_state.as<float2>();
+        fwd.pupil = d_pupil.as<float2>();
+        fwd.params = d_params.as<fpm::FrameParam>();
+        if (md->background) {
+            std::vector<float> bg(md->background, md->background + md->background_len);
+            FPM_TRY(upload_array(d_bg, bg, s));
+            fwd.background = d_bg.as<float>();
+            fwd.background_stride = md->background_len == (int64_t)n2 ? 0 : (long long)n2;
+        }
+        FPM_TRY(d_out.ensure(sizeof(float) * n2 * F));
+        fwd.out = d_out.as<float>();
+        fwd.M = M;
+        fwd.frame_count = F;
+        FPM_CUDA(fpm::launch_forward(N, fwd, s));
+        std::vector<float> host(n2 * F);
+        FPM_CUDA(cudaMemcpyAsync(host.data(), d_out.ptr, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaStreamSynchronize(s));
+        for (size_t i = 0; i < host.size(); ++i) intensities[i] = host[i];
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_problem_create(fpm_context* ctx, const fpm_model_desc* model, const fpm_measurement_desc* measurements,
+                           fpm_problem** problem) {
+    if (!ctx || !problem) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return finish(ctx, create_problem(ctx, model, measurements, problem));
+}
+
+int32_t fpm_problem_destroy(fpm_problem* problem) {
+    if (!problem) return FPM_OK;
+    fpm_context* ctx = problem->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    delete problem;
+    return FPM_OK;
+}
+
+int32_t fpm_run(fpm_context* ctx, fpm_problem* problem, const fpm_algorithm_params* params, fpm_result_desc* result) {
+    return fpm_run_batch(ctx, 1, &problem, params, result);
+}
+
+int32_t fpm_run_batch(fpm_context* ctx, int32_t count, fpm_problem* const* problems, const fpm_algorithm_params* params,
+                      fpm_result_desc* results) {
+    if (!ctx || (count > 0 && !problems)) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return finish(ctx, run_batch(ctx, count, problems, params, results));
+}
+
+int32_t fpm_last_engine_timing(const fpm_context* ctx, int32_t* launches, double* milliseconds, double* algorithmic_bytes) {
+    if (!ctx) return FPM_ERR_INVALID_PARAMETER;
+    if (launches) *launches = ctx->engine_launches;
+    if (milliseconds) *milliseconds = ctx->engine_ms;
+    if (algorithmic_bytes) *algorithmic_bytes = ctx->engine_bytes;
+    return FPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+"""fpm_rs: GB300-native drop-in for fpm-rs's image-plane forward model and
+reconstruction inner loop.
+
+The public names follow the reference's Python bindings (python/fpm_rs);
+the numerical work runs in libfpm_gpu.so, hand-written CUDA for sm_103a,
+reached through the C ABI declared in include/fpm_gpu.h.
+"""
+
+from __future__ import annotations
+
+import ctypes as _C
+
+import numpy as _np
+
+from . import _native
+from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasurementsError, InvalidModelError,
+                     InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
+                     UnsupportedError)
+from .experiment import (ArrayPose, CameraModel, Illumination, KVectorList, Optics, PlanarLEDArray,
+                         PupilAberration, ResolvedSources)
+from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
+from .reconstruction import (AlternatingProjection, Epry, Fpie, GradientDescent, Mpie, ReconstructionProblem,
+                             ReconstructionResult, RuntimeInfo, engine_timing, run_batch)
+from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
+
+
+def fft2(values, *, inverse: bool = False):
+    """Backend::fft2 (src/backend/traits.rs:123-131) on the GPU in FP64.
+
+    Forward transforms are scaled by 1/(height*width); inverse transforms are
+    not. Returns a new complex128 array.
+    """
+    out = _np.array(values, dtype=_np.complex128, order="C", copy=True)
+    if out.ndim != 2:
+        raise InvalidShapeError("fft2 expects a 2-D array")
+    ctx = _native.context()
+    _native.check(_native.library().fpm_fft2(ctx.handle, _native.ptr(out, _C.c_double), out.shape[0],
+                                             out.shape[1], int(bool(inverse))), ctx.handle)
+    return out
+
+
+__all__ = [
+    "AlternatingProjection", "ArrayPose", "CameraModel", "DeviceError", "Epry", "Fpie", "FpmError",
+    "FrameOutOfRangeError", "GradientDescent", "Illumination", "ImagePlaneModel", "InvalidMeasurementsError",
+    "InvalidModelError", "InvalidParameterError", "InvalidShapeError", "KVectorList", "LengthMismatchError",
+    "MeasurementStack", "Mpie", "NumericalError", "Optics", "PlanarLEDArray", "PupilAberration",
+    "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo", "SimulationResult",
+    "UnsupportedError", "compile_camera_model", "compile_model", "engine_timing", "fft2", "forward_intensities",
+    "run_batch", "simulate", "suggest_reconstruction_shape",
+]

@@ -1,0 +1,165 @@
+"""ctypes binding of libfpm_gpu.so (include/fpm_gpu.h).
+
+The library is built in-tree by fpm-rs_gb300/build.py. Loading never falls
+back to another implementation: a missing library raises ImportError with
+the build command, and device entry points raise FpmError when no Blackwell
+GPU is available.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import errors
+
+PACKAGE_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.environ.get("FPM_GPU_LIBRARY", os.path.join(PACKAGE_ROOT, "libfpm_gpu.so"))
+
+EXPORTED = (
+    "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
+    "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
+    "fpm_fft2", "fpm_forward_stack", "fpm_problem_create", "fpm_problem_destroy",
+    "fpm_run", "fpm_run_batch", "fpm_last_engine_timing",
+)
+
+
+class Optics(C.Structure):
+    _fields_ = [
+        ("wavelength_vacuum_m", C.c_double), ("objective_na", C.c_double),
+        ("magnification", C.c_double), ("camera_pixel_size", C.c_double),
+        ("illumination_refractive_index", C.c_double),
+        ("objective_medium_refractive_index", C.c_double),
+        ("has_defocus", C.c_int32), ("defocus_distance", C.c_double),
+        ("has_aberration", C.c_int32), ("astigmatism", C.c_double), ("coma", C.c_double),
+        ("spherical", C.c_double), ("edge_apodization", C.c_double),
+    ]
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("image_height", C.c_int32), ("image_width", C.c_int32),
+        ("recon_height", C.c_int32), ("recon_width", C.c_int32),
+        ("sources", C.c_int32),
+        ("crop_start_row", C.POINTER(C.c_int64)), ("crop_start_col", C.POINTER(C.c_int64)),
+        ("offset_row", C.POINTER(C.c_double)), ("offset_col", C.POINTER(C.c_double)),
+        ("pupil", C.POINTER(C.c_double)), ("support", C.POINTER(C.c_uint8)),
+        ("frame_gains", C.POINTER(C.c_double)), ("background", C.POINTER(C.c_double)),
+        ("background_len", C.c_int64),
+        ("kx", C.POINTER(C.c_double)), ("ky", C.POINTER(C.c_double)),
+    ]
+
+
+class MeasurementDesc(C.Structure):
+    _fields_ = [
+        ("frames", C.c_int32), ("measurements", C.POINTER(C.c_double)),
+        ("frame_weights", C.POINTER(C.c_double)), ("masks", C.POINTER(C.c_uint8)),
+    ]
+
+
+class AlgorithmParams(C.Structure):
+    _fields_ = [
+        ("algorithm", C.c_int32), ("iterations", C.c_int32), ("batch_size", C.c_int32),
+        ("loss_type", C.c_int32), ("schedule", C.c_int32),
+        ("object_step", C.c_double), ("epsilon", C.c_double), ("stability", C.c_double),
+        ("momentum_interval", C.c_int32), ("momentum_friction", C.c_double),
+        ("momentum_feedback", C.c_double),
+        ("recover_pupil", C.c_int32), ("constrain_pupil_support", C.c_int32),
+        ("pupil_step", C.c_double),
+        ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
+        ("poisson_truncation", C.c_int32),
+    ]
+
+
+class ResultDesc(C.Structure):
+    _fields_ = [
+        ("object", C.POINTER(C.c_double)), ("object_spectrum", C.POINTER(C.c_double)),
+        ("pupil", C.POINTER(C.c_double)), ("objectives", C.POINTER(C.c_double)),
+        ("completed_iterations", C.c_int32),
+    ]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library() -> C.CDLL:
+    """Loads libfpm_gpu.so, raising ImportError when it has not been built."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise ImportError(
+                        f"{LIB_PATH} is missing; build it with `python fpm-rs_gb300/build.py` "
+                        "(there is no CPU implementation of this path)")
+                lib = C.CDLL(LIB_PATH)
+                lib.fpm_global_last_error.restype = C.c_char_p
+                for name in EXPORTED:
+                    getattr(lib, name)
+                _lib = lib
+    return _lib
+
+
+def ptr(array, ctype):
+    if array is None:
+        return C.POINTER(ctype)()
+    return array.ctypes.data_as(C.POINTER(ctype))
+
+
+def check(status: int, context=None) -> None:
+    if status == 0:
+        return
+    lib = library()
+    if context is not None:
+        buf = C.create_string_buffer(2048)
+        lib.fpm_last_error(context, buf, len(buf))
+        message = buf.value.decode(errors="replace")
+    else:
+        message = lib.fpm_global_last_error().decode(errors="replace")
+    raise errors.from_status(status, message)
+
+
+class Context:
+    """A device context of libfpm_gpu (one per process and device)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = library()
+        handle = C.c_void_p()
+        check(self._lib.fpm_create(C.byref(handle), int(device)))
+        self.handle = handle
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.fpm_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_context: Context | None = None
+
+
+def context() -> Context:
+    global _context
+    if _context is None:
+        with _lock:
+            if _context is None:
+                _context = Context(int(os.environ.get("FPM_DEVICE", "0")))
+    return _context
+
+
+def c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)

@@ -1,0 +1,61 @@
+"""Exception hierarchy of the fpm_rs Python API (python/src/errors.rs:4-50)."""
+
+from __future__ import annotations
+
+
+class FpmError(Exception):
+    """Base class for errors raised by the device backend."""
+
+
+class InvalidShapeError(FpmError):
+    pass
+
+
+class InvalidParameterError(FpmError):
+    pass
+
+
+class InvalidModelError(FpmError):
+    pass
+
+
+class InvalidMeasurementsError(FpmError):
+    pass
+
+
+class LengthMismatchError(FpmError):
+    pass
+
+
+class FrameOutOfRangeError(FpmError):
+    pass
+
+
+class NumericalError(FpmError):
+    pass
+
+
+class UnsupportedError(FpmError):
+    pass
+
+
+class DeviceError(FpmError):
+    """A CUDA runtime call failed or no suitable GPU is present."""
+
+
+_BY_STATUS = {
+    1: InvalidShapeError,
+    2: InvalidParameterError,
+    3: InvalidModelError,
+    4: InvalidMeasurementsError,
+    5: LengthMismatchError,
+    6: FrameOutOfRangeError,
+    7: NumericalError,
+    8: UnsupportedError,
+    9: DeviceError,
+    10: DeviceError,
+}
+
+
+def from_status(status: int, message: str) -> FpmError:
+    return _BY_STATUS.get(status, FpmError)(message)

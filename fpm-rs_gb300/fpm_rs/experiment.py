@@ -1,0 +1,263 @@
+"""Experiment description: optics, LED geometry, illumination and camera.
+
+Mirrors the fpm_rs Python classes of the same names
+(python/fpm_rs/__init__.pyi: Optics 1411-1480, ArrayPose 1481-1511,
+PlanarLEDArray 1512-1560, KVectorList 1764-1780, Illumination 1871-1895,
+CameraModel 1956-2006). Resolution to k-vectors runs in the native library.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from .errors import InvalidParameterError, UnsupportedError
+
+
+@dataclass(frozen=True)
+class PupilAberration:
+    """Direct radian weights of the crate's pupil phase terms (src/experiment/optics.rs:84-94)."""
+
+    astigmatism: float = 0.0
+    coma: float = 0.0
+    spherical: float = 0.0
+    edge_apodization: float = 0.0
+
+    def __post_init__(self):
+        values = (self.astigmatism, self.coma, self.spherical, self.edge_apodization)
+        if any(not math.isfinite(v) for v in values) or self.edge_apodization < 0.0:
+            raise InvalidParameterError(
+                "pupil_aberration: phase coefficients must be finite and edge apodization must be "
+                "finite and non-negative")
+
+
+class Optics:
+    """Physical microscope parameters used to compile an image-plane model."""
+
+    def __init__(self, wavelength_vacuum_m: float, objective_na: float, magnification: float,
+                 camera_pixel_size: float, *, illumination_refractive_index: float = 1.0,
+                 objective_medium_refractive_index: float = 1.0,
+                 defocus_distance: float | None = None,
+                 pupil_aberration: PupilAberration | None = None):
+        self.wavelength_vacuum_m = float(wavelength_vacuum_m)
+        self.objective_na = float(objective_na)
+        self.magnification = float(magnification)
+        self.camera_pixel_size = float(camera_pixel_size)
+        self.illumination_refractive_index = float(illumination_refractive_index)
+        self.objective_medium_refractive_index = float(objective_medium_refractive_index)
+        self.defocus_distance = None if defocus_distance is None else float(defocus_distance)
+        self.pupil_aberration = pupil_aberration
+        self._validate()
+
+    def _validate(self) -> None:
+        for name in ("wavelength_vacuum_m", "objective_na", "magnification", "camera_pixel_size",
+                     "illumination_refractive_index", "objective_medium_refractive_index"):
+            value = getattr(self, name)
+            if not math.isfinite(value) or value <= 0.0:
+                raise InvalidParameterError(f"{name} must be finite and positive, got {value}")
+        if self.objective_na > self.objective_medium_refractive_index:
+            raise InvalidParameterError("objective_na cannot exceed the medium refractive index")
+        pitch = self.object_pixel_size
+        limit = self.wavelength_vacuum_m / (2.0 * self.objective_na)
+        if not pitch < limit:
+            raise InvalidParameterError(
+                f"object-plane pitch camera_pixel_size / magnification ({pitch:.6e} m) must be strictly "
+                f"less than wavelength_vacuum_m / (2 * objective_na) ({limit:.6e} m)")
+        if self.defocus_distance is not None and not math.isfinite(self.defocus_distance):
+            raise InvalidParameterError("defocus_distance must be finite")
+
+    @property
+    def object_pixel_size(self) -> float:
+        return self.camera_pixel_size / self.magnification
+
+    def _struct(self) -> N.Optics:
+        o = N.Optics()
+        o.wavelength_vacuum_m = self.wavelength_vacuum_m
+        o.objective_na = self.objective_na
+        o.magnification = self.magnification
+        o.camera_pixel_size = self.camera_pixel_size
+        o.illumination_refractive_index = self.illumination_refractive_index
+        o.objective_medium_refractive_index = self.objective_medium_refractive_index
+        o.has_defocus = int(self.defocus_distance is not None)
+        o.defocus_distance = self.defocus_distance or 0.0
+        ab = self.pupil_aberration
+        o.has_aberration = int(ab is not None)
+        if ab is not None:
+            o.astigmatism, o.coma, o.spherical, o.edge_apodization = (
+                ab.astigmatism, ab.coma, ab.spherical, ab.edge_apodization)
+        return o
+
+
+@dataclass(frozen=True)
+class ArrayPose:
+    """Rigid array-local to sample transform; rotation is extrinsic x, y, then z."""
+
+    translation_m: tuple = (0.0, 0.0, 0.0)
+    rotation_rad: tuple = (0.0, 0.0, 0.0)
+
+    @staticmethod
+    def identity() -> "ArrayPose":
+        return ArrayPose()
+
+    @staticmethod
+    def from_translation(translation_m) -> "ArrayPose":
+        return ArrayPose(tuple(float(v) for v in translation_m))
+
+    @staticmethod
+    def from_translation_and_extrinsic_xyz_radians(translation_m, rotation_rad) -> "ArrayPose":
+        return ArrayPose(tuple(float(v) for v in translation_m), tuple(float(v) for v in rotation_rad))
+
+    @staticmethod
+    def from_translation_and_extrinsic_xyz_degrees(translation_m, rotation_deg) -> "ArrayPose":
+        return ArrayPose(tuple(float(v) for v in translation_m),
+                         tuple(math.radians(float(v)) for v in rotation_deg))
+
+
+class ResolvedSources:
+    def __init__(self, k_vectors: np.ndarray):
+        self._k = np.ascontiguousarray(k_vectors, dtype=np.float64)
+
+    @property
+    def source_count(self) -> int:
+        return self._k.shape[0]
+
+    @property
+    def k_vectors(self) -> np.ndarray:
+        return self._k.copy()
+
+
+class PlanarLEDArray:
+    """Planar LED geometry (src/experiment/led_array.rs:292-313)."""
+
+    def __init__(self, shape, pitch_m, reference_index, pose: ArrayPose, *, position_offsets_m=None):
+        self.shape = (int(shape[0]), int(shape[1]))
+        if np.isscalar(pitch_m):
+            self.pitch_m = (float(pitch_m), float(pitch_m))
+        else:
+            self.pitch_m = (float(pitch_m[0]), float(pitch_m[1]))
+        self.reference_index = (float(reference_index[0]), float(reference_index[1]))
+        self.pose = pose
+        if position_offsets_m is not None and np.any(np.asarray(position_offsets_m) != 0.0):
+            raise UnsupportedError("position_offsets_m is not supported by this build")
+        if self.shape[0] <= 0 or self.shape[1] <= 0:
+            raise InvalidParameterError("shape rows and columns must be non-zero")
+
+    @property
+    def source_count(self) -> int:
+        return self.shape[0] * self.shape[1]
+
+    def source_index(self, row: int, column: int) -> int:
+        return row * self.shape[1] + column
+
+    def source_row_column(self, index: int):
+        return (index // self.shape[1], index % self.shape[1])
+
+    def resolve(self, optics: Optics) -> ResolvedSources:
+        n = self.source_count
+        kx = np.zeros(n)
+        ky = np.zeros(n)
+        t = np.asarray(self.pose.translation_m, dtype=np.float64)
+        r = np.asarray(self.pose.rotation_rad, dtype=np.float64)
+        o = optics._struct()
+        N.check(N.library().fpm_planar_led_kvectors(
+            C.byref(o), self.shape[0], self.shape[1], C.c_double(self.pitch_m[0]), C.c_double(self.pitch_m[1]),
+            C.c_double(self.reference_index[0]), C.c_double(self.reference_index[1]),
+            N.ptr(t, C.c_double), N.ptr(r, C.c_double), N.ptr(kx, C.c_double), N.ptr(ky, C.c_double)))
+        return ResolvedSources(np.stack([kx, ky], axis=1))
+
+
+class KVectorList:
+    """Explicit transverse wave vectors, float64 (sources, 2) of (kx, ky) rad/m."""
+
+    def __init__(self, k_vectors):
+        k = np.asarray(k_vectors, dtype=np.float64)
+        if k.ndim != 2 or k.shape[1] != 2 or k.shape[0] == 0:
+            raise InvalidParameterError("k_vectors must have shape (sources, 2)")
+        if not np.all(np.isfinite(k)):
+            raise InvalidParameterError("k_vectors must contain finite values")
+        self._k = k
+
+    @property
+    def source_count(self) -> int:
+        return self._k.shape[0]
+
+    @property
+    def k_vectors(self) -> np.ndarray:
+        return self._k.copy()
+
+    def resolve(self, optics: Optics) -> ResolvedSources:
+        optics._validate()
+        return ResolvedSources(self._k)
+
+
+class Illumination:
+    """Geometry plus (unit) calibration and the all-sources sequential acquisition."""
+
+    def __init__(self, geometry, *, calibration=None, acquisition=None):
+        if calibration is not None or acquisition is not None:
+            raise UnsupportedError(
+                "source calibration and multiplexed acquisition plans are not supported by this build")
+        self.geometry = geometry
+
+    def resolve(self, optics: Optics) -> ResolvedSources:
+        return self.geometry.resolve(optics)
+
+
+@dataclass
+class CameraModel:
+    """Detector response and acquisition noise (src/simulation/camera.rs:249-318).
+
+    Noise is drawn from NumPy's PCG64 generator, not the reference's ChaCha12
+    stream, so simulated counts match the reference only in distribution.
+    """
+
+    photons_per_pixel: float = 1000.0
+    gain_counts_per_electron: float = 1.0
+    offset_counts: float = 0.0
+    read_noise_electrons: float = 0.0
+    dark_current_electrons: float = 0.0
+    shot_noise: bool = False
+    pixel_sensitivity: np.ndarray | None = None
+    bit_depth: int | None = 16
+    saturation_counts: float | None = None
+    quantize: bool = True
+    bad_pixels: tuple = field(default_factory=tuple)
+    bad_pixel_value_counts: float | None = None
+
+    @staticmethod
+    def ideal() -> "CameraModel":
+        return CameraModel(photons_per_pixel=1.0, bit_depth=None, quantize=False)
+
+    def maximum_count(self) -> float:
+        limit = math.inf
+        if self.bit_depth is not None:
+            limit = float(2 ** int(self.bit_depth) - 1)
+        if self.saturation_counts is not None:
+            limit = min(limit, float(self.saturation_counts))
+        return limit
+
+    def measure(self, intensity: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+        """CameraModel::measure_frame applied to every frame in order."""
+        values = np.maximum(intensity, 0.0)
+        if self.pixel_sensitivity is not None:
+            values = values * np.asarray(self.pixel_sensitivity, dtype=np.float64)
+        electrons = values * self.photons_per_pixel + self.dark_current_electrons
+        if self.shot_noise:
+            electrons = rng.poisson(electrons).astype(np.float64)
+        if self.read_noise_electrons > 0.0:
+            electrons = electrons + rng.normal(0.0, self.read_noise_electrons, size=electrons.shape)
+        counts = np.clip(electrons * self.gain_counts_per_electron + self.offset_counts, 0.0, self.maximum_count())
+        if self.quantize:
+            counts = np.round(counts)
+        if self.bad_pixels:
+            value = self.bad_pixel_value_counts if self.bad_pixel_value_counts is not None else self.maximum_count()
+            value = min(max(value, 0.0), self.maximum_count())
+            if self.quantize:
+                value = round(value)
+            flat = counts.reshape(counts.shape[0], -1)
+            flat[:, list(self.bad_pixels)] = value
+        return counts

@@ -1,0 +1,349 @@
+"""Reconstruction problems, algorithms and results on the GB300 device backend.
+
+Mirrors python/src/reconstruction.rs (ReconstructionProblem 88-153,
+run_algorithm 1107-1141, AlternatingProjection 2238-2286, Mpie 2500-2560,
+Epry 2612-2680, GradientDescent 2831-2908) and python/fpm_rs/__init__.pyi
+(ReconstructionResult 2959-3000, _Algorithm.run 3312-3340). Every
+reconstruction runs to completion in libfpm_gpu; the Python layer only
+validates arguments, uploads arrays and wraps results.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from .errors import InvalidMeasurementsError, InvalidModelError, InvalidShapeError, UnsupportedError
+from .model import ImagePlaneModel
+from .simulation import MeasurementStack
+
+_LOSSES = {"amplitude_mse": 0, "intensity_mse": 1, "poisson_nll": 2, "huber_amplitude": 3}
+_SCHEDULES = {"sequential": 0, "brightfield_first": 1, "spiral_out": 2, "snr_weighted": 3}
+_ALG = {"ap": 0, "fpie": 1, "mpie": 2, "epry": 3, "gd": 4}
+
+
+def _loss(value: str) -> int:
+    if value not in _LOSSES:
+        raise ValueError("loss_type must be amplitude_mse, intensity_mse, poisson_nll, or huber_amplitude")
+    return _LOSSES[value]
+
+
+class ReconstructionProblem:
+    """Validated pairing of measurements and a compiled image-plane model.
+
+    The measurement stack is uploaded to the device on first use and stays
+    resident for later runs of the same problem.
+    """
+
+    def __init__(self, measurements, model: ImagePlaneModel, *, frame_weights=None, masks=None, name=None):
+        if not isinstance(measurements, MeasurementStack):
+            measurements = MeasurementStack(measurements, frame_weights=frame_weights, masks=masks)
+        self.measurements = measurements
+        self.model = model
+        self.name = name
+        self._handle = None
+        self._keep = None
+        if measurements.frame_count != model.frame_count:
+            raise InvalidModelError(
+                f"{measurements.frame_count} measurement frames but {model.frame_count} model frames")
+        if tuple(measurements.image_shape) != tuple(model.image_shape):
+            raise InvalidShapeError(
+                f"measurement shape {tuple(measurements.image_shape)} differs from model image shape {model.image_shape}")
+        weights = measurements._weights
+        if not np.any(weights > 0):
+            raise InvalidMeasurementsError("at least one frame must have positive weight")
+        if measurements._masks is not None:
+            empty = np.flatnonzero((weights > 0) & ~measurements._masks.reshape(len(weights), -1).any(axis=1))
+            if empty.size:
+                raise InvalidMeasurementsError(f"positive-weight frame {int(empty[0])} has no unmasked pixels")
+
+    @property
+    def frame_count(self) -> int:
+        return self.measurements.frame_count
+
+    @property
+    def image_shape(self):
+        return self.model.image_shape
+
+    @property
+    def reconstruction_shape(self):
+        return self.model.reconstruction_shape
+
+    def device_handle(self):
+        """Uploads the problem (once) and returns its opaque device handle."""
+        if self._handle is None:
+            ctx = N.context()
+            desc, keep = self.model._descriptor()
+            m = N.MeasurementDesc()
+            m.frames = self.measurements.frame_count
+            m.measurements = N.ptr(self.measurements._data, C.c_double)
+            m.frame_weights = N.ptr(self.measurements._weights, C.c_double)
+            m.masks = N.ptr(self.measurements._masks, C.c_uint8)
+            handle = C.c_void_p()
+            N.check(N.library().fpm_problem_create(ctx.handle, C.byref(desc), C.byref(m), C.byref(handle)),
+                    ctx.handle)
+            self._handle = handle
+            self._ctx = ctx
+        return self._handle
+
+    def release(self) -> None:
+        """Frees the problem's device buffers."""
+        if self._handle is not None:
+            N.library().fpm_problem_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+@dataclass
+class RuntimeInfo:
+    elapsed_seconds: float
+    completed_iterations: int
+    stopped_early: bool
+    algorithm: str
+
+
+@dataclass
+class ReconstructionResult:
+    """Owned reconstruction products (python/fpm_rs/__init__.pyi:2959-3000)."""
+
+    object: np.ndarray
+    object_spectrum: np.ndarray
+    recovered_pupil: np.ndarray
+    pupil_support: np.ndarray
+    trace: list
+    runtime: RuntimeInfo
+    recovered_frame_gains: np.ndarray | None = None
+    recovered_background: np.ndarray | None = None
+    calibrated_illumination: np.ndarray | None = None
+    physical_illumination_calibration: object = None
+    calibrated_model: object = None
+    algorithm_metrics: list = field(default_factory=list)
+    metadata: dict = field(default_factory=dict)
+
+    @property
+    def amplitude(self) -> np.ndarray:
+        return np.abs(self.object)
+
+    @property
+    def phase(self) -> np.ndarray:
+        return np.angle(self.object)
+
+    @property
+    def final_objective(self):
+        return self.trace[-1][1] if self.trace else None
+
+    @property
+    def scalar_diagnostics(self) -> dict:
+        return {} if not self.trace else {"final_objective": self.trace[-1][1]}
+
+
+class _Algorithm:
+    _name = ""
+    _code = 0
+
+    def _params(self, schedule: str) -> N.AlgorithmParams:
+        raise NotImplementedError
+
+    def _schedule(self, schedule: str) -> int:
+        if schedule == "random":
+            raise UnsupportedError(
+                "the random schedule depends on the reference's ChaCha12 stream and is not supported by this build")
+        if schedule not in _SCHEDULES:
+            raise ValueError("schedule must be sequential, brightfield_first, spiral_out, random, or snr_weighted")
+        return _SCHEDULES[schedule]
+
+    def run(self, problem: ReconstructionProblem, *, callbacks=None, resume_from=None, schedule="sequential",
+            schedule_seed=0) -> ReconstructionResult:
+        """Run the reconstruction on the GPU and return host results."""
+        return run_batch(self, [problem], callbacks=callbacks, resume_from=resume_from, schedule=schedule)[0]
+
+
+def _base_params(alg: _Algorithm, schedule: str, iterations, object_step, batch_size, epsilon, loss_type):
+    p = N.AlgorithmParams()
+    p.algorithm = alg._code
+    p.iterations = int(iterations)
+    p.batch_size = int(batch_size)
+    p.loss_type = _loss(loss_type)
+    p.schedule = alg._schedule(schedule)
+    p.object_step = float(object_step)
+    p.epsilon = float(epsilon)
+    p.constrain_pupil_support = 1
+    return p
+
+
+class AlternatingProjection(_Algorithm):
+    _name = "AlternatingProjection"
+    _code = _ALG["ap"]
+
+    def __init__(self, *, iterations=50, object_step=1.0, batch_size=1, epsilon=1e-10, loss_type="amplitude_mse"):
+        _loss(loss_type)
+        self.iterations, self.object_step, self.batch_size = iterations, object_step, batch_size
+        self.epsilon, self.loss_type = epsilon, loss_type
+
+    def _params(self, schedule):
+        return _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
+                            self.loss_type)
+
+
+class Fpie(_Algorithm):
+    _name = "Fpie"
+    _code = _ALG["fpie"]
+
+    def __init__(self, *, iterations=50, object_step=0.8, stability=0.1, batch_size=1, epsilon=1e-10,
+                 loss_type="amplitude_mse"):
+        _loss(loss_type)
+        self.iterations, self.object_step, self.stability = iterations, object_step, stability
+        self.batch_size, self.epsilon, self.loss_type = batch_size, epsilon, loss_type
+
+    def _params(self, schedule):
+        p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
+                         self.loss_type)
+        p.stability = float(self.stability)
+        return p
+
+
+class Mpie(_Algorithm):
+    _name = "Mpie"
+    _code = _ALG["mpie"]
+
+    def __init__(self, *, iterations=50, object_step=0.2, stability=0.05, momentum_interval=30,
+                 momentum_friction=0.9, momentum_feedback=0.9, batch_size=1, epsilon=1e-10,
+                 loss_type="amplitude_mse"):
+        _loss(loss_type)
+        self.iterations, self.object_step, self.stability = iterations, object_step, stability
+        self.momentum_interval, self.momentum_friction = momentum_interval, momentum_friction
+        self.momentum_feedback, self.batch_size = momentum_feedback, batch_size
+        self.epsilon, self.loss_type = epsilon, loss_type
+
+    def _params(self, schedule):
+        p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
+                         self.loss_type)
+        p.stability = float(self.stability)
+        p.momentum_interval = int(self.momentum_interval)
+        p.momentum_friction = float(self.momentum_friction)
+        p.momentum_feedback = float(self.momentum_feedback)
+        return p
+
+
+class Epry(_Algorithm):
+    _name = "Epry"
+    _code = _ALG["epry"]
+
+    def __init__(self, *, iterations=100, object_step=0.8, pupil_step=0.1, batch_size=1, recover_pupil=True,
+                 constrain_pupil_support=True, recover_frame_gains=False, gain_step=0.2, gain_bounds=(1e-6, 1e6),
+                 recover_background=False, background_step=0.2, background_bounds=(0.0, 1e12), epsilon=1e-10,
+                 loss_type="amplitude_mse"):
+        _loss(loss_type)
+        self.iterations, self.object_step, self.pupil_step = iterations, object_step, pupil_step
+        self.batch_size, self.recover_pupil = batch_size, recover_pupil
+        self.constrain_pupil_support = constrain_pupil_support
+        self.recover_frame_gains, self.gain_step, self.gain_bounds = recover_frame_gains, gain_step, gain_bounds
+        self.recover_background, self.background_step = recover_background, background_step
+        self.background_bounds, self.epsilon, self.loss_type = background_bounds, epsilon, loss_type
+
+    def _params(self, schedule):
+        p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
+                         self.loss_type)
+        p.pupil_step = float(self.pupil_step)
+        p.recover_pupil = int(bool(self.recover_pupil))
+        p.constrain_pupil_support = int(bool(self.constrain_pupil_support))
+        p.recover_frame_gains = int(bool(self.recover_frame_gains))
+        p.recover_background = int(bool(self.recover_background))
+        return p
+
+
+class GradientDescent(_Algorithm):
+    _name = "GradientDescent"
+    _code = _ALG["gd"]
+
+    def __init__(self, *, iterations=100, object_step=0.5, batch_size=1, epsilon=1e-10, loss_type="amplitude_mse",
+                 poisson_truncation_threshold=None, recover_illumination=False, illumination_step=0.1,
+                 illumination_finite_difference=0.05, illumination_bounds=1.0, recover_pupil=False, pupil_step=0.05,
+                 constrain_pupil_support=True, object_tv=0.0, object_tv_epsilon=1e-6, pupil_smoothing=0.0,
+                 parallel_workers=0):
+        _loss(loss_type)
+        self.iterations, self.object_step, self.batch_size = iterations, object_step, batch_size
+        self.epsilon, self.loss_type = epsilon, loss_type
+        self.poisson_truncation_threshold = poisson_truncation_threshold
+        self.recover_illumination, self.recover_pupil = recover_illumination, recover_pupil
+        self.object_tv, self.pupil_smoothing = object_tv, pupil_smoothing
+        self.parallel_workers = parallel_workers
+        if recover_illumination or object_tv or pupil_smoothing:
+            raise UnsupportedError(
+                "illumination recovery and object/pupil regularisation are not implemented on the GB300 device path")
+
+    def _params(self, schedule):
+        p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
+                         self.loss_type)
+        p.poisson_truncation = int(self.poisson_truncation_threshold is not None)
+        p.recover_pupil = int(bool(self.recover_pupil))
+        return p
+
+
+def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=None, schedule="sequential",
+              download=True):
+    """Runs one algorithm over many independent problems in shared device launches.
+
+    Tiles of one image size share one frame-engine launch (one thread-block
+    cluster per tile); different sizes run concurrently. Each tile follows
+    the exact frame order a single run would. With ``download=False`` the
+    results stay on the device and ``None`` is returned per problem.
+    """
+    if callbacks:
+        raise UnsupportedError("callbacks are not supported by the GB300 device path")
+    if resume_from is not None:
+        raise UnsupportedError("checkpoint resume is not supported by the GB300 device path")
+    params = algorithm._params(schedule)
+    problems = list(problems)
+    handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
+    ctx = N.context()
+    results = (N.ResultDesc * len(problems))()
+    arrays = []
+    if download:
+        for i, p in enumerate(problems):
+            mh, mw = p.reconstruction_shape
+            h, w = p.image_shape
+            a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
+                     pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)))
+            results[i].object = N.ptr(a["object"], C.c_double)
+            results[i].object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
+            results[i].pupil = N.ptr(a["pupil"], C.c_double)
+            results[i].objectives = N.ptr(a["objectives"], C.c_double)
+            arrays.append(a)
+    start = time.perf_counter()
+    N.check(N.library().fpm_run_batch(ctx.handle, len(problems), handles, C.byref(params),
+                                      results if download else None), ctx.handle)
+    elapsed = time.perf_counter() - start
+    if not download:
+        return [None] * len(problems)
+    out = []
+    for p, a in zip(problems, arrays):
+        trace = [(it + 1, float(a["objectives"][it]), elapsed) for it in range(params.iterations)]
+        gains = p.model.frame_gains
+        result = ReconstructionResult(
+            object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
+            pupil_support=p.model.pupil_support, trace=trace,
+            runtime=RuntimeInfo(elapsed, params.iterations, False, algorithm._name),
+            recovered_frame_gains=gains, recovered_background=p.model._background)
+        if p.name is not None:
+            result.metadata["problem_name"] = p.name
+        out.append(result)
+    return out
+
+
+def engine_timing():
+    """(launches, milliseconds, algorithmic bytes) of the last run's frame-engine launches."""
+    ctx = N.context()
+    launches, ms, nbytes = C.c_int32(), C.c_double(), C.c_double()
+    N.library().fpm_last_engine_timing(ctx.handle, C.byref(launches), C.byref(ms), C.byref(nbytes))
+    return launches.value, ms.value, nbytes.value

@@ -1,0 +1,192 @@
+/*
+ * fpm_gpu.h - C ABI of the GB300 (sm_103a) device backend for fpm-rs's
+ * image-plane FPM forward model and reconstruction inner loop.
+ *
+ * All entry points are extern "C", take plain pointers and sizes, and return an
+ * int32_t status (FPM_OK on success). Host arrays are caller-owned, row-major
+ * and C-contiguous, and are only read (or written, for outputs) for the
+ * duration of the call. Complex arrays are interleaved (re, im) float64, the
+ * layout of Rust's Complex64 and NumPy's complex128. Device buffers are owned
+ * by opaque handles; no device pointer crosses the boundary.
+ *
+ * Replaced reference interfaces (paths are within hgrecco/fpm-rs):
+ *   Backend::fft2 ................ src/backend/traits.rs:123-131 -> fpm_fft2
+ *   ImagePlaneModel::compile ..... src/model/image_plane_fpm.rs:196-253 -> fpm_compile_model
+ *   ForwardModel::forward_intensity_stack_into
+ *                                  src/model/forward.rs:300-372 -> fpm_forward_stack
+ *   ReconstructionProblem::new ... src/reconstruction/problem.rs:12-20 -> fpm_problem_create
+ *   Runner::run / ReconstructionAlgorithm::run
+ *                                  src/reconstruction/runner.rs:76-285 -> fpm_run
+ *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size)
+ *   Error / FpmError ............. src/error.rs:12, python/src/errors.rs:17-50 -> FPM_ERR_* + fpm_last_error
+ */
+#ifndef FPM_GPU_H
+#define FPM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes, one per reference Error variant that this path can raise. */
+enum {
+    FPM_OK = 0,
+    FPM_ERR_INVALID_SHAPE = 1,        /* Error::InvalidShape */
+    FPM_ERR_INVALID_PARAMETER = 2,    /* Error::InvalidParameter */
+    FPM_ERR_INVALID_MODEL = 3,        /* Error::InvalidModel */
+    FPM_ERR_INVALID_MEASUREMENTS = 4, /* Error::InvalidMeasurements */
+    FPM_ERR_LENGTH_MISMATCH = 5,      /* Error::LengthMismatch */
+    FPM_ERR_FRAME_OUT_OF_RANGE = 6,   /* Error::FrameOutOfRange */
+    FPM_ERR_NUMERICAL = 7,            /* Error::Numerical */
+    FPM_ERR_UNSUPPORTED = 8,          /* Error::Unsupported */
+    FPM_ERR_CUDA = 9,                 /* a CUDA runtime call failed */
+    FPM_ERR_TIMEOUT = 10              /* reserved: a bounded device wait expired */
+};
+
+enum { FPM_SHAPE_EXACT = 0, FPM_SHAPE_MINIMUM = 1, FPM_SHAPE_SMOOTH = 2, FPM_SHAPE_POWER_OF_TWO = 3 };
+enum { FPM_LOSS_AMPLITUDE_MSE = 0, FPM_LOSS_INTENSITY_MSE = 1, FPM_LOSS_POISSON_NLL = 2, FPM_LOSS_HUBER_AMPLITUDE = 3 };
+enum { FPM_ALG_AP = 0, FPM_ALG_FPIE = 1, FPM_ALG_MPIE = 2, FPM_ALG_EPRY = 3, FPM_ALG_GD = 4 };
+enum {
+    FPM_SCHEDULE_SEQUENTIAL = 0,
+    FPM_SCHEDULE_BRIGHTFIELD_FIRST = 1,
+    FPM_SCHEDULE_SPIRAL_OUT = 2,
+    FPM_SCHEDULE_SNR_WEIGHTED = 3
+};
+
+typedef struct fpm_context fpm_context;
+typedef struct fpm_problem fpm_problem;
+
+/* Microscope optics (src/experiment/optics.rs:44-68). */
+typedef struct {
+    double wavelength_vacuum_m, objective_na, magnification, camera_pixel_size;
+    double illumination_refractive_index, objective_medium_refractive_index;
+    int32_t has_defocus;
+    double defocus_distance;
+    int32_t has_aberration;
+    double astigmatism, coma, spherical, edge_apodization;
+} fpm_optics;
+
+/* Compiled, non-multiplexed image-plane model (src/model/image_plane_fpm.rs:57-73).
+ * frames == sources. Offsets may be NULL (integer crops). */
+typedef struct {
+    int32_t image_height, image_width;
+    int32_t recon_height, recon_width;
+    int32_t sources;
+    const int64_t *crop_start_row, *crop_start_col; /* [sources] */
+    const double *offset_row, *offset_col;          /* [sources] or NULL */
+    const double *pupil;                            /* complex128 [h*w] */
+    const uint8_t *support;                         /* [h*w], 0 or 1 */
+    const double *frame_gains;                      /* [sources] or NULL (all 1) */
+    const double *background;                       /* NULL, [h*w] or [sources*h*w] */
+    int64_t background_len;
+    const double *kx, *ky;                          /* [sources] rad/m; used by sorted schedules */
+} fpm_model_desc;
+
+/* Measurement stack (src/measurements/stack.rs:47-...). */
+typedef struct {
+    int32_t frames;
+    const double *measurements;  /* [frames*h*w] float64 */
+    const double *frame_weights; /* [frames] or NULL (all 1) */
+    const uint8_t *masks;        /* [frames*h*w] or NULL; 0 excludes a pixel */
+} fpm_measurement_desc;
+
+/* Algorithm parameters; fields not used by an algorithm are ignored.
+ * Defaults: AlternatingProjection src/algorithms/alternating_projection.rs:51-61,
+ * Fpie src/algorithms/fpie.rs, Mpie src/algorithms/mpie.rs:81-95,
+ * Epry src/algorithms/epry.rs:91-112, GradientDescent
+ * src/algorithms/gradient_descent.rs:171-193. */
+typedef struct {
+    int32_t algorithm;
+    int32_t iterations;
+    int32_t batch_size;
+    int32_t loss_type;
+    int32_t schedule;
+    double object_step;
+    double epsilon;
+    double stability;            /* FPIE / mPIE */
+    int32_t momentum_interval;   /* mPIE */
+    double momentum_friction;    /* mPIE */
+    double momentum_feedback;    /* mPIE */
+    int32_t recover_pupil;       /* EPRY */
+    int32_t constrain_pupil_support;
+    double pupil_step;
+    int32_t recover_frame_gains; /* EPRY extension (unsupported on the device path) */
+    int32_t recover_background;  /* EPRY extension (unsupported on the device path) */
+    int32_t poisson_truncation;  /* GD option (unsupported on the device path) */
+} fpm_algorithm_params;
+
+/* Result buffers; any pointer may be NULL. */
+typedef struct {
+    double *object;          /* complex128 [mh*mw] real-space object */
+    double *object_spectrum; /* complex128 [mh*mw] centred spectrum */
+    double *pupil;           /* complex128 [h*w] recovered pupil */
+    double *objectives;      /* [iterations] weighted mean objective per iteration */
+    int32_t completed_iterations;
+} fpm_result_desc;
+
+/* ------------------------------------------------------------------ context */
+int32_t fpm_create(fpm_context **ctx, int32_t device);
+int32_t fpm_destroy(fpm_context *ctx);
+/* Copies the last error message of this context (NUL-terminated, truncated). */
+int32_t fpm_last_error(const fpm_context *ctx, char *buffer, size_t length);
+/* Library-wide last error, for failures before a context exists. */
+const char *fpm_global_last_error(void);
+
+/* --------------------------------------------------------- host geometry */
+/* Planar LED array k-vectors (src/experiment/led_array.rs:292-313 and
+ * src/experiment/illumination.rs:385-421). translation/rotation are [3]. */
+int32_t fpm_planar_led_kvectors(const fpm_optics *optics, int32_t rows, int32_t cols, double pitch_x,
+                                double pitch_y, double reference_col, double reference_row,
+                                const double *translation, const double *rotation_rad, double *kx,
+                                double *ky);
+/* Resolves the reconstruction shape only (suggest_reconstruction_shape). */
+int32_t fpm_suggest_shape(const fpm_optics *optics, int32_t sources, const double *kx, const double *ky,
+                          int32_t image_height, int32_t image_width, int32_t policy, int32_t *recon_height,
+                          int32_t *recon_width);
+/* Compiles k-vectors into crops, fractional offsets and the circular pupil.
+ * Caller allocates start_row/start_col/offset_row/offset_col [sources],
+ * pupil [2*h*w] and support [h*w]. For FPM_SHAPE_EXACT the shape is read from
+ * *recon_height/*recon_width; otherwise it is written there. */
+int32_t fpm_compile_model(const fpm_optics *optics, int32_t sources, const double *kx, const double *ky,
+                          int32_t image_height, int32_t image_width, int32_t policy, int32_t *recon_height,
+                          int32_t *recon_width, int64_t *start_row, int64_t *start_col, double *offset_row,
+                          double *offset_col, double *pupil, uint8_t *support, double *dkx, double *dky);
+
+/* ------------------------------------------------------------- device work */
+/* Backend::fft2 on host data: complex128 [h*w] in place, reference convention
+ * (forward scaled by 1/(h*w), inverse unscaled). Computed in FP64 on the GPU. */
+int32_t fpm_fft2(fpm_context *ctx, double *values, int32_t height, int32_t width, int32_t inverse);
+
+/* Forward intensity stack [sources*h*w] of a complex128 object [mh*mw]
+ * (object FFT, crop, pupil, IFFT, |psi|^2 * gain + background). */
+int32_t fpm_forward_stack(fpm_context *ctx, const fpm_model_desc *model, const double *object,
+                          double *intensities);
+
+/* Uploads a validated model + measurement pair; the problem keeps its
+ * measurements resident on the device until fpm_problem_destroy. */
+int32_t fpm_problem_create(fpm_context *ctx, const fpm_model_desc *model,
+                           const fpm_measurement_desc *measurements, fpm_problem **problem);
+int32_t fpm_problem_destroy(fpm_problem *problem);
+
+/* Runs one reconstruction to completion (initialise, iterate, finalise). */
+int32_t fpm_run(fpm_context *ctx, fpm_problem *problem, const fpm_algorithm_params *params,
+                fpm_result_desc *result);
+
+/* Runs `count` independent reconstructions with the same parameters. Tiles of
+ * one image size share a launch; sizes run concurrently on separate streams.
+ * Each tile keeps the exact sequential frame order of a single run. */
+int32_t fpm_run_batch(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
+                      const fpm_algorithm_params *params, fpm_result_desc *results);
+
+/* Device timing of the frame-engine launches of the last fpm_run/fpm_run_batch
+ * (CUDA events recorded on each launch's stream). */
+int32_t fpm_last_engine_timing(const fpm_context *ctx, int32_t *launches, double *milliseconds,
+                               double *algorithmic_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

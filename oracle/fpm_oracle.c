@@ -1,0 +1,1506 @@
+/*
+ * FP64 CPU oracle for the fpm-rs image-plane FPM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: a complex128 restatement of the reference
+ * (hgrecco/fpm-rs 0.2.0-beta.2) used to check the CUDA product path and to
+ * time a CPU baseline. The product library never links or calls this file.
+ * Each function names the reference file:line it restates. The FFT is our own
+ * mixed-radix Cooley-Tukey; the reference uses rustfft 6.4.1, whose values any
+ * correct FFT reproduces to rounding (pinned by the round-trip and constant-
+ * object known-answer tests of tests/forward_model_tests.rs:12-31,75-101).
+ */
+#define _GNU_SOURCE
+#include "fpm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct {
+    double re, im;
+} cplx;
+
+static inline cplx cx(double re, double im) { cplx z = {re, im}; return z; }
+static inline cplx c_add(cplx a, cplx b) { return cx(a.re + b.re, a.im + b.im); }
+static inline cplx c_sub(cplx a, cplx b) { return cx(a.re - b.re, a.im - b.im); }
+static inline cplx c_mul(cplx a, cplx b) {
+    return cx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+static inline cplx c_scale(cplx a, double s) { return cx(a.re * s, a.im * s); }
+static inline cplx c_conj(cplx a) { return cx(a.re, -a.im); }
+static inline double c_norm_sqr(cplx a) { return a.re * a.re + a.im * a.im; }
+static inline double c_norm(cplx a) { return hypot(a.re, a.im); }
+static inline double c_arg(cplx a) { return atan2(a.im, a.re); }
+static inline cplx c_polar(double r, double t) { return cx(r * cos(t), r * sin(t)); }
+/* num_complex division (a / b) for a non-zero divisor. */
+static inline cplx c_div(cplx a, cplx b) {
+    double d = b.re * b.re + b.im * b.im;
+    return cx((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+}
+static inline cplx c_divr(cplx a, double d) { return cx(a.re / d, a.im / d); }
+
+/* ------------------------------------------------------------------ errors */
+
+static __thread char g_error[512];
+
+const char *orc_last_error(void) { return g_error; }
+
+static int32_t fail(int32_t code, const char *fmt, ...) {
+    va_list args;
+    va_start(args, fmt);
+    vsnprintf(g_error, sizeof g_error, fmt, args);
+    va_end(args);
+    return code;
+}
+
+/* --------------------------------------------------------------------- FFT */
+
+/* One cached 1-D plan: forward twiddles e^{-2 pi i t / n}. */
+typedef struct {
+    int n;
+    int pow2;
+    cplx *tw;
+    int *rev;
+} fft_plan;
+
+#define PLAN_CACHE 8
+static __thread fft_plan g_plans[PLAN_CACHE];
+static __thread int g_plan_next;
+
+static fft_plan *get_plan(int n) {
+    for (int i = 0; i < PLAN_CACHE; ++i)
+        if (g_plans[i].n == n) return &g_plans[i];
+    fft_plan *p = &g_plans[g_plan_next];
+    g_plan_next = (g_plan_next + 1) % PLAN_CACHE;
+    free(p->tw);
+    free(p->rev);
+    p->n = n;
+    p->tw = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+    for (int t = 0; t < n; ++t) {
+        double angle = 2.0 * M_PI * (double)t / (double)n;
+        p->tw[t] = cx(cos(angle), -sin(angle));
+    }
+    p->pow2 = (n & (n - 1)) == 0;
+    p->rev = NULL;
+    if (p->pow2) {
+        int bits = 0;
+        while ((1 << bits) < n) ++bits;
+        p->rev = (int *)malloc(sizeof(int) * (size_t)n);
+        for (int i = 0; i < n; ++i) {
+            int r = 0;
+            for (int b = 0; b < bits; ++b)
+                if (i & (1 << b)) r |= 1 << (bits - 1 - b);
+            p->rev[i] = r;
+        }
+    }
+    return p;
+}
+
+static int smallest_factor(int n) {
+    if (n % 2 == 0) return 2;
+    for (int f = 3; f * f <= n; f += 2)
+        if (n % f == 0) return f;
+    return n;
+}
+
+/* Mixed-radix decimation in time: out[k] = sum_j in[j*stride] w_n^{jk}. */
+static void dft_rec(const cplx *in, int stride, cplx *out, int n, const fft_plan *root,
+                    int inverse) {
+    if (n == 1) {
+        out[0] = in[0];
+        return;
+    }
+    int p = smallest_factor(n);
+    int m = n / p;
+    for (int r = 0; r < p; ++r) dft_rec(in + (size_t)r * stride, stride * p, out + (size_t)r * m, m, root, inverse);
+    int step = root->n / n;
+    cplx stack_t[16];
+    cplx *t = p <= 16 ? stack_t : (cplx *)malloc(sizeof(cplx) * (size_t)p);
+    cplx stack_y[16];
+    cplx *y = p <= 16 ? stack_y : (cplx *)malloc(sizeof(cplx) * (size_t)p);
+    for (int k = 0; k < m; ++k) {
+        for (int r = 0; r < p; ++r) {
+            cplx w = root->tw[(size_t)((long)r * k % n) * step];
+            if (inverse) w = c_conj(w);
+            t[r] = c_mul(out[(size_t)r * m + k], w);
+        }
+        for (int q = 0; q < p; ++q) {
+            cplx acc = cx(0.0, 0.0);
+            for (int r = 0; r < p; ++r) {
+                cplx w = root->tw[(size_t)((long)m * r * q % n) * step];
+                if (inverse) w = c_conj(w);
+                acc = c_add(acc, c_mul(t[r], w));
+            }
+            y[q] = acc;
+        }
+        for (int q = 0; q < p; ++q) out[(size_t)k + (size_t)m * q] = y[q];
+    }
+    if (p > 16) {
+        free(t);
+        free(y);
+    }
+}
+
+/* Unnormalised 1-D transform in place on contiguous values. */
+static void fft1(cplx *v, int n, int inverse, cplx *scratch) {
+    if (n <= 1) return;
+    fft_plan *plan = get_plan(n);
+    if (plan->pow2) {
+        for (int i = 0; i < n; ++i) {
+            int r = plan->rev[i];
+            if (r > i) {
+                cplx tmp = v[i];
+                v[i] = v[r];
+                v[r] = tmp;
+            }
+        }
+        for (int len = 2; len <= n; len <<= 1) {
+            int half = len >> 1;
+            int step = n / len;
+            for (int start = 0; start < n; start += len) {
+                for (int j = 0; j < half; ++j) {
+                    cplx w = plan->tw[(size_t)j * step];
+                    if (inverse) w = c_conj(w);
+                    cplx a = v[start + j];
+                    cplx b = c_mul(v[start + j + half], w);
+                    v[start + j] = c_add(a, b);
+                    v[start + j + half] = c_sub(a, b);
+                }
+            }
+        }
+        return;
+    }
+    memcpy(scratch, v, sizeof(cplx) * (size_t)n);
+    dft_rec(scratch, 1, v, n, plan, inverse);
+}
+
+/* CpuBackend::fft2 (src/backend/cpu.rs:130-175): rows, then columns; the
+ * forward transform is normalised by 1/(h*w) and the inverse is not. */
+static void fft2_c(cplx *v, int h, int w, int inverse) {
+    int longest = h > w ? h : w;
+    cplx *scratch = (cplx *)malloc(sizeof(cplx) * (size_t)longest * 2);
+    cplx *column = scratch + longest;
+    for (int r = 0; r < h; ++r) fft1(v + (size_t)r * w, w, inverse, scratch);
+    for (int c = 0; c < w; ++c) {
+        for (int r = 0; r < h; ++r) column[r] = v[(size_t)r * w + c];
+        fft1(column, h, inverse, scratch);
+        for (int r = 0; r < h; ++r) v[(size_t)r * w + c] = column[r];
+    }
+    if (!inverse) {
+        double norm = (double)h * (double)w;
+        for (size_t i = 0; i < (size_t)h * w; ++i) v[i] = c_divr(v[i], norm);
+    }
+    free(scratch);
+}
+
+int32_t orc_fft2(double *values, int32_t h, int32_t w, int32_t inverse) {
+    if (h <= 0 || w <= 0) return fail(ORC_INVALID_SHAPE, "FFT dimensions must be non-zero");
+    fft2_c((cplx *)values, h, w, inverse);
+    return ORC_OK;
+}
+
+/* shift_copy (src/model/forward.rs:552-569). */
+static void shift_copy(const cplx *src, cplx *dst, int h, int w, int rs, int cs) {
+    for (int r = 0; r < h; ++r)
+        for (int c = 0; c < w; ++c)
+            dst[(size_t)((r + rs) % h) * w + (c + cs) % w] = src[(size_t)r * w + c];
+}
+/* fftshift_copy / ifftshift_copy (src/model/forward.rs:530-550). */
+static void fftshift_c(const cplx *s, cplx *d, int h, int w) { shift_copy(s, d, h, w, h / 2, w / 2); }
+static void ifftshift_c(const cplx *s, cplx *d, int h, int w) {
+    shift_copy(s, d, h, w, (h + 1) / 2, (w + 1) / 2);
+}
+
+int32_t orc_fftshift(const double *src, double *dst, int32_t h, int32_t w) {
+    fftshift_c((const cplx *)src, (cplx *)dst, h, w);
+    return ORC_OK;
+}
+int32_t orc_ifftshift(const double *src, double *dst, int32_t h, int32_t w) {
+    ifftshift_c((const cplx *)src, (cplx *)dst, h, w);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------- geometry */
+
+/* Rust f64::round: half away from zero, like C round(). */
+
+typedef struct {
+    long integer;
+    double offset;
+    long lower, upper;
+} grid_shift;
+
+/* checked_grid_shift (src/model/image_plane_fpm.rs:975-1024). */
+static int32_t checked_grid_shift(double value, grid_shift *out) {
+    if (!isfinite(value)) return fail(ORC_INVALID_MODEL, "illumination shift must be finite");
+    double rounded = round(value);
+    long integer = (long)rounded;
+    double offset = value - rounded;
+    double nearest = round(offset);
+    out->integer = integer;
+    out->offset = offset;
+    if (fabs(offset - nearest) <= 1e-12) {
+        out->lower = out->upper = integer + (long)nearest;
+    } else if (offset > 0.0) {
+        out->lower = integer;
+        out->upper = integer + 1;
+    } else {
+        out->lower = integer - 1;
+        out->upper = integer;
+    }
+    return ORC_OK;
+}
+
+typedef struct {
+    long lower_start, upper_start;
+    double lower_weight, upper_weight;
+} axis_interp;
+
+/* interpolation_axis (src/model/crop.rs:266-313). */
+static int32_t interpolation_axis(long start, long length, long bound, double offset,
+                                  axis_interp *out) {
+    if (length == 0 || bound == 0 || !isfinite(offset))
+        return fail(ORC_INVALID_MODEL, "subpixel crop dimensions and offset must be finite and non-zero");
+    double nearest = round(offset);
+    double integer_offset, fraction;
+    if (fabs(offset - nearest) <= 1e-12) {
+        integer_offset = nearest;
+        fraction = 0.0;
+    } else {
+        integer_offset = floor(offset);
+        fraction = offset - integer_offset;
+    }
+    long lower_start = start + (long)integer_offset;
+    if (lower_start < 0) return fail(ORC_INVALID_MODEL, "subpixel crop starts outside the grid");
+    long lower_end = lower_start + length;
+    int needs_upper = fraction > 0.0;
+    if (lower_end > bound || (needs_upper && lower_end >= bound))
+        return fail(ORC_INVALID_MODEL, "subpixel crop interpolation stencil lies outside the grid");
+    out->lower_start = lower_start;
+    out->upper_start = lower_start + (needs_upper ? 1 : 0);
+    out->lower_weight = 1.0 - fraction;
+    out->upper_weight = fraction;
+    return ORC_OK;
+}
+
+static int offset_is_zero(double r, double c) { return fabs(r) <= 1e-12 && fabs(c) <= 1e-12; }
+
+/* FourierCrop::extract_subpixel_standard (src/model/crop.rs:129-167), with
+ * the integer path extract_standard (:79-102). */
+static int32_t extract_patch_c(const cplx *src, int mh, int mw, long sr, long sc, int h, int w,
+                               double orow, double ocol, cplx *dst) {
+    if (offset_is_zero(orow, ocol)) {
+        if (sr < 0 || sc < 0 || sr + h > mh || sc + w > mw)
+            return fail(ORC_INVALID_MODEL, "crop lies outside reconstruction shape");
+        for (int r = 0; r < h; ++r)
+            memcpy(dst + (size_t)r * w, src + (size_t)(sr + r) * mw + sc, sizeof(cplx) * (size_t)w);
+        return ORC_OK;
+    }
+    axis_interp rows, cols;
+    int32_t st = interpolation_axis(sr, h, mh, orow, &rows);
+    if (st) return st;
+    st = interpolation_axis(sc, w, mw, ocol, &cols);
+    if (st) return st;
+    for (int r = 0; r < h; ++r) {
+        long lr = rows.lower_start + r, ur = rows.upper_start + r;
+        for (int c = 0; c < w; ++c) {
+            long lc = cols.lower_start + c, uc = cols.upper_start + c;
+            cplx v = c_scale(src[lr * mw + lc], rows.lower_weight * cols.lower_weight);
+            v = c_add(v, c_scale(src[lr * mw + uc], rows.lower_weight * cols.upper_weight));
+            v = c_add(v, c_scale(src[ur * mw + lc], rows.upper_weight * cols.lower_weight));
+            v = c_add(v, c_scale(src[ur * mw + uc], rows.upper_weight * cols.upper_weight));
+            dst[(size_t)r * w + c] = v;
+        }
+    }
+    return ORC_OK;
+}
+
+/* FourierCrop::insert_subpixel_adjoint_slice (src/model/crop.rs:188-255). */
+static int32_t insert_adjoint_c(cplx *dst, int mh, int mw, long sr, long sc, int h, int w,
+                                double orow, double ocol, const cplx *update, double scale) {
+    if (!isfinite(scale)) return fail(ORC_INVALID_PARAMETER, "scale must be finite");
+    if (offset_is_zero(orow, ocol)) {
+        if (sr < 0 || sc < 0 || sr + h > mh || sc + w > mw)
+            return fail(ORC_INVALID_MODEL, "crop lies outside reconstruction shape");
+        for (int r = 0; r < h; ++r)
+            for (int c = 0; c < w; ++c) {
+                cplx *o = &dst[(size_t)(sr + r) * mw + sc + c];
+                *o = c_add(*o, c_scale(update[(size_t)r * w + c], scale));
+            }
+        return ORC_OK;
+    }
+    axis_interp rows, cols;
+    int32_t st = interpolation_axis(sr, h, mh, orow, &rows);
+    if (st) return st;
+    st = interpolation_axis(sc, w, mw, ocol, &cols);
+    if (st) return st;
+    for (int r = 0; r < h; ++r) {
+        long lr = rows.lower_start + r, ur = rows.upper_start + r;
+        for (int c = 0; c < w; ++c) {
+            long lc = cols.lower_start + c, uc = cols.upper_start + c;
+            cplx value = c_scale(update[(size_t)r * w + c], scale);
+            cplx *o;
+            o = &dst[lr * mw + lc];
+            *o = c_add(*o, c_scale(value, rows.lower_weight * cols.lower_weight));
+            o = &dst[lr * mw + uc];
+            *o = c_add(*o, c_scale(value, rows.lower_weight * cols.upper_weight));
+            o = &dst[ur * mw + lc];
+            *o = c_add(*o, c_scale(value, rows.upper_weight * cols.lower_weight));
+            o = &dst[ur * mw + uc];
+            *o = c_add(*o, c_scale(value, rows.upper_weight * cols.upper_weight));
+        }
+    }
+    return ORC_OK;
+}
+
+int32_t orc_extract_patch(const double *spectrum, int32_t mh, int32_t mw, int64_t start_row,
+                          int64_t start_col, int32_t h, int32_t w, double off_row, double off_col,
+                          double *patch) {
+    return extract_patch_c((const cplx *)spectrum, mh, mw, (long)start_row, (long)start_col, h, w,
+                           off_row, off_col, (cplx *)patch);
+}
+
+int32_t orc_insert_adjoint(double *spectrum, int32_t mh, int32_t mw, int64_t start_row,
+                           int64_t start_col, int32_t h, int32_t w, double off_row, double off_col,
+                           const double *update, double scale) {
+    return insert_adjoint_c((cplx *)spectrum, mh, mw, (long)start_row, (long)start_col, h, w,
+                            off_row, off_col, (const cplx *)update, scale);
+}
+
+/* Optics::validate (src/experiment/optics.rs:128-189). */
+static int32_t validate_optics(const orc_optics *o) {
+    const double values[6] = {o->wavelength_vacuum_m, o->objective_na, o->magnification,
+                              o->camera_pixel_size, o->illumination_refractive_index,
+                              o->objective_medium_refractive_index};
+    for (int i = 0; i < 6; ++i)
+        if (!isfinite(values[i]) || values[i] <= 0.0)
+            return fail(ORC_INVALID_PARAMETER, "optics parameters must be finite and positive");
+    if (o->objective_na > o->objective_medium_refractive_index)
+        return fail(ORC_INVALID_PARAMETER, "objective_na cannot exceed the medium refractive index");
+    double pixel = o->camera_pixel_size / o->magnification;
+    double limit = o->wavelength_vacuum_m / (2.0 * o->objective_na);
+    if (!(pixel < limit))
+        return fail(ORC_INVALID_PARAMETER, "camera_pixel_size / magnification violates coherent sampling");
+    if (o->has_defocus && !isfinite(o->defocus_distance))
+        return fail(ORC_INVALID_PARAMETER, "defocus_distance must be finite");
+    return ORC_OK;
+}
+
+/* PlanarLedArray::resolve (src/experiment/led_array.rs:292-313) with
+ * ArrayPose::transform_point (:87-112) and ResolvedSources::from_positions
+ * (src/experiment/illumination.rs:385-421). */
+int32_t orc_planar_kvectors(const orc_optics *optics, int32_t rows, int32_t cols, double pitch_x,
+                            double pitch_y, double ref_col, double ref_row,
+                            const double *translation, const double *rotation, double *kx,
+                            double *ky) {
+    int32_t st = validate_optics(optics);
+    if (st) return st;
+    double k = 2.0 * M_PI * optics->illumination_refractive_index / optics->wavelength_vacuum_m;
+    double sx = sin(rotation[0]), cxr = cos(rotation[0]);
+    double sy = sin(rotation[1]), cyr = cos(rotation[1]);
+    double sz = sin(rotation[2]), czr = cos(rotation[2]);
+    for (int r = 0; r < rows; ++r)
+        for (int c = 0; c < cols; ++c) {
+            double p[3] = {((double)c - ref_col) * pitch_x, ((double)r - ref_row) * pitch_y, 0.0};
+            double ax[3] = {p[0], cxr * p[1] - sx * p[2], sx * p[1] + cxr * p[2]};
+            double ay[3] = {cyr * ax[0] + sy * ax[2], ax[1], -sy * ax[0] + cyr * ax[2]};
+            double rz[3] = {czr * ay[0] - sz * ay[1], sz * ay[0] + czr * ay[1], ay[2]};
+            double pos[3] = {rz[0] + translation[0], rz[1] + translation[1], rz[2] + translation[2]};
+            double norm = hypot(hypot(pos[0], pos[1]), pos[2]);
+            if (!isfinite(norm) || norm <= 0.0)
+                return fail(ORC_INVALID_PARAMETER, "no source may coincide with the sample origin");
+            int i = r * cols + c;
+            kx[i] = k * (-pos[0] / norm);
+            ky[i] = k * (-pos[1] / norm);
+        }
+    return ORC_OK;
+}
+
+typedef struct {
+    long min_row, max_row, min_col, max_col;
+} disp_bounds;
+
+/* crop_displacement_bounds (src/model/image_plane_fpm.rs:255-285). */
+static int32_t displacement_bounds(const orc_optics *o, int n, const double *kx, const double *ky,
+                                   int h, int w, disp_bounds *b) {
+    if (h <= 0 || w <= 0) return fail(ORC_INVALID_SHAPE, "image shape must be non-zero");
+    if (n <= 0) return fail(ORC_INVALID_MODEL, "illumination must contain at least one frame");
+    double pixel = o->camera_pixel_size / o->magnification;
+    double dkx = 2.0 * M_PI / ((double)w * pixel);
+    double dky = 2.0 * M_PI / ((double)h * pixel);
+    b->min_row = b->min_col = 0x7fffffffffffffffL;
+    b->max_row = b->max_col = -0x7fffffffffffffffL - 1;
+    for (int i = 0; i < n; ++i) {
+        grid_shift row = {0, 0.0, 0, 0}, col = {0, 0.0, 0, 0};
+        int32_t st = checked_grid_shift(ky[i] / dky, &row);
+        if (st) return st;
+        st = checked_grid_shift(kx[i] / dkx, &col);
+        if (st) return st;
+        if (row.lower < b->min_row) b->min_row = row.lower;
+        if (row.upper > b->max_row) b->max_row = row.upper;
+        if (col.lower < b->min_col) b->min_col = col.lower;
+        if (col.upper > b->max_col) b->max_col = col.upper;
+    }
+    return ORC_OK;
+}
+
+/* axis_contains_bounds (src/model/image_plane_fpm.rs:1089-1114). */
+static int axis_contains(long len, long recon, long lo, long hi) {
+    long base = recon / 2 - len / 2;
+    long lower = base + lo;
+    long upper = base + (len - 1) + hi;
+    return lower >= 0 && upper < recon;
+}
+
+static int shape_fits(int h, int w, long mh, long mw, const disp_bounds *b) {
+    return axis_contains(h, mh, b->min_row, b->max_row) && axis_contains(w, mw, b->min_col, b->max_col);
+}
+
+static long gcd_l(long a, long b) {
+    while (b != 0) {
+        long t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+/* next_smooth_multiplier (src/model/image_plane_fpm.rs:1176-1198). */
+static void smooth_visit(long value, int prime_index, long minimum, long *best) {
+    static const long primes[4] = {2, 3, 5, 7};
+    if (value >= minimum) {
+        if (*best < 0 || value < *best) *best = value;
+        return;
+    }
+    for (int i = prime_index; i < 4; ++i) {
+        long next = value * primes[i];
+        if (*best < 0 || next < *best) smooth_visit(next, i, minimum, best);
+    }
+}
+
+int32_t orc_next_smooth(int64_t minimum, int64_t *out) {
+    long best = -1;
+    smooth_visit(1, 0, (long)minimum, &best);
+    *out = best;
+    return ORC_OK;
+}
+
+/* resolve_reconstruction_shape (src/model/image_plane_fpm.rs:287-348) with
+ * minimum_fitting_multiplier (:1116-1155). */
+static int32_t resolve_shape(int h, int w, int policy, int emh, int emw, const disp_bounds *b,
+                             int32_t *mh, int32_t *mw) {
+    if (policy == ORC_SHAPE_EXACT) {
+        if (emh < h || emw < w)
+            return fail(ORC_INVALID_SHAPE, "image shape must fit reconstruction shape");
+        if ((long)emh * w != (long)emw * h)
+            return fail(ORC_INVALID_SHAPE, "reconstruction must use the same scale factor in both dimensions");
+        if (!shape_fits(h, w, emh, emw, b))
+            return fail(ORC_INVALID_SHAPE,
+                        "reconstruction shape does not contain every illumination crop and subpixel interpolation stencil");
+        *mh = emh;
+        *mw = emw;
+        return ORC_OK;
+    }
+    long d = gcd_l(h, w);
+    long ah = h / d, aw = w / d;
+    long maximum = 1L << 40;
+    long multiplier;
+    if (shape_fits(h, w, ah * d, aw * d, b)) {
+        multiplier = d;
+    } else {
+        long lower = d, upper = d;
+        for (;;) {
+            long doubled = upper * 2;
+            upper = doubled < maximum ? doubled : maximum;
+            if (upper == lower)
+                return fail(ORC_INVALID_SHAPE, "illumination crops require a reconstruction shape outside the supported range");
+            if (shape_fits(h, w, ah * upper, aw * upper, b)) break;
+            lower = upper;
+        }
+        while (lower + 1 < upper) {
+            long middle = lower + (upper - lower) / 2;
+            if (shape_fits(h, w, ah * middle, aw * middle, b))
+                upper = middle;
+            else
+                lower = middle;
+        }
+        multiplier = upper;
+    }
+    if (policy == ORC_SHAPE_SMOOTH) {
+        long best = -1;
+        smooth_visit(1, 0, multiplier, &best);
+        multiplier = best;
+    } else if (policy == ORC_SHAPE_POW2) {
+        long p = 1;
+        while (p < multiplier) p <<= 1;
+        multiplier = p;
+    }
+    *mh = (int32_t)(ah * multiplier);
+    *mw = (int32_t)(aw * multiplier);
+    return ORC_OK;
+}
+
+int32_t orc_suggest_shape(const orc_optics *optics, int32_t sources, const double *kx,
+                          const double *ky, int32_t h, int32_t w, int32_t policy, int32_t *mh,
+                          int32_t *mw) {
+    int32_t st = validate_optics(optics);
+    if (st) return st;
+    disp_bounds b;
+    st = displacement_bounds(optics, sources, kx, ky, h, w, &b);
+    if (st) return st;
+    return resolve_shape(h, w, policy, *mh, *mw, &b, mh, mw);
+}
+
+/* ImagePlaneModel::compile (src/model/image_plane_fpm.rs:196-253),
+ * crop_for_k_vector (:750-797) and Pupil::circular (src/model/pupil.rs:78-123). */
+int32_t orc_compile(const orc_optics *optics, int32_t sources, const double *kx, const double *ky,
+                    int32_t h, int32_t w, int32_t policy, int32_t exact_mh, int32_t exact_mw,
+                    orc_compiled *out) {
+    int32_t st = validate_optics(optics);
+    if (st) return st;
+    disp_bounds b;
+    st = displacement_bounds(optics, sources, kx, ky, h, w, &b);
+    if (st) return st;
+    int32_t mh, mw;
+    st = resolve_shape(h, w, policy, exact_mh, exact_mw, &b, &mh, &mw);
+    if (st) return st;
+    double scale = (double)mw / (double)w;
+    double low = optics->camera_pixel_size / optics->magnification;
+    out->h = h;
+    out->w = w;
+    out->mh = mh;
+    out->mw = mw;
+    out->sources = sources;
+    out->low_res_pixel_size = low;
+    out->high_res_pixel_size = low / scale;
+    out->dkx = 2.0 * M_PI / ((double)w * low);
+    out->dky = 2.0 * M_PI / ((double)h * low);
+    double cutoff = 2.0 * M_PI * optics->objective_na / optics->wavelength_vacuum_m;
+    double medium_k = 2.0 * M_PI * optics->objective_medium_refractive_index / optics->wavelength_vacuum_m;
+    cplx *pupil = (cplx *)out->pupil;
+    for (int r = 0; r < h; ++r) {
+        double y = ((double)r - (double)(h / 2)) * out->dky;
+        for (int c = 0; c < w; ++c) {
+            double x = ((double)c - (double)(w / 2)) * out->dkx;
+            double radius = hypot(x, y);
+            int inside = radius <= cutoff;
+            size_t i = (size_t)r * w + c;
+            out->support[i] = (uint8_t)inside;
+            if (!inside) {
+                pupil[i] = cx(0.0, 0.0);
+                continue;
+            }
+            double rho = cutoff > 0.0 ? radius / cutoff : 0.0;
+            double theta = atan2(y, x);
+            double phase = 0.0;
+            if (optics->has_defocus) phase -= optics->defocus_distance * (x * x + y * y) / (2.0 * medium_k);
+            double amplitude = 1.0;
+            if (optics->has_aberration) {
+                phase += optics->astigmatism * rho * rho * cos(2.0 * theta);
+                phase += optics->coma * (3.0 * pow(rho, 3) - 2.0 * rho) * cos(theta);
+                phase += optics->spherical * (6.0 * pow(rho, 4) - 6.0 * rho * rho + 1.0);
+                amplitude = exp(-optics->edge_apodization * rho * rho);
+            }
+            pupil[i] = c_polar(amplitude, phase);
+        }
+    }
+    long center_row = mh / 2, center_col = mw / 2;
+    for (int s = 0; s < sources; ++s) {
+        grid_shift row = {0, 0.0, 0, 0}, col = {0, 0.0, 0, 0};
+        st = checked_grid_shift(ky[s] / out->dky, &row);
+        if (st) return st;
+        st = checked_grid_shift(kx[s] / out->dkx, &col);
+        if (st) return st;
+        long start_row = center_row - h / 2 + row.integer;
+        long start_col = center_col - w / 2 + col.integer;
+        if (start_row < 0 || start_col < 0)
+            return fail(ORC_INVALID_MODEL, "illumination vector produces a crop outside the reconstruction grid");
+        axis_interp ai;
+        st = interpolation_axis(start_row, h, mh, row.offset, &ai);
+        if (st) return st;
+        st = interpolation_axis(start_col, w, mw, col.offset, &ai);
+        if (st) return st;
+        out->start_row[s] = start_row;
+        out->start_col[s] = start_col;
+        out->off_row[s] = row.offset;
+        out->off_col[s] = col.offset;
+    }
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------- losses */
+
+/* point_loss (src/algorithms/objective.rs:47-71). */
+static double point_loss(double predicted, double measured, int loss) {
+    switch (loss) {
+    case ORC_LOSS_AMPLITUDE_MSE: {
+        double r = sqrt(fmax(predicted, 0.0)) - sqrt(fmax(measured, 0.0));
+        return r * r;
+    }
+    case ORC_LOSS_INTENSITY_MSE: {
+        double r = predicted - measured;
+        return r * r;
+    }
+    case ORC_LOSS_POISSON_NLL: {
+        double mean = fmax(predicted, 1e-12);
+        return mean - fmax(measured, 0.0) * log(mean);
+    }
+    default: {
+        double r = sqrt(fmax(predicted, 0.0)) - sqrt(fmax(measured, 0.0));
+        double a = fabs(r);
+        return a <= 1.0 ? 0.5 * r * r : a - 0.5;
+    }
+    }
+}
+
+/* descent_factor (src/algorithms/gradient_descent.rs:1167-1178). */
+static double descent_factor(double predicted, double measured, int loss, double epsilon) {
+    switch (loss) {
+    case ORC_LOSS_AMPLITUDE_MSE:
+        return 1.0 - sqrt(fmax(measured, 0.0)) / sqrt(fmax(predicted, epsilon));
+    case ORC_LOSS_INTENSITY_MSE:
+        return 2.0 * (predicted - measured);
+    case ORC_LOSS_POISSON_NLL:
+        return 1.0 - fmax(measured, 0.0) / fmax(predicted, epsilon);
+    default: {
+        double pa = sqrt(fmax(predicted, epsilon));
+        double r = pa - sqrt(fmax(measured, 0.0));
+        if (r < -1.0) r = -1.0;
+        if (r > 1.0) r = 1.0;
+        return r / (2.0 * pa);
+    }
+    }
+}
+
+/* ------------------------------------------------------------------ state */
+
+typedef struct {
+    const orc_problem *p;
+    int h, w, mh, mw, frames;
+    size_t n_low, n_high;
+    cplx *object;   /* centred spectrum */
+    cplx *pupil;
+    double *gains;  /* frames */
+    double *background; /* NULL or frames*n_low (expanded) */
+    cplx *velocity, *anchor;
+    long momentum_count;
+    /* scratch */
+    cplx *patch, *exit_spec, *field, *projected, *difference, *spectrum, *pupil_gradient, *gradient;
+    double *prediction;
+} orc_state;
+
+static double frame_weight(const orc_problem *p, int f) { return p->weights ? p->weights[f] : 1.0; }
+static const uint8_t *frame_mask(const orc_problem *p, int f) {
+    return p->masks ? p->masks + (size_t)f * p->h * p->w : NULL;
+}
+static double model_gain(const orc_problem *p, int f) { return p->gains ? p->gains[f] : 1.0; }
+static double model_background(const orc_problem *p, int f, size_t pixel) {
+    if (!p->background) return 0.0;
+    size_t n = (size_t)p->h * p->w;
+    return p->background_len == (int64_t)n ? p->background[pixel] : p->background[(size_t)f * n + pixel];
+}
+static double state_background(const orc_state *s, int f, size_t pixel) {
+    return s->background ? s->background[(size_t)f * s->n_low + pixel] : 0.0;
+}
+
+static void state_free(orc_state *s) {
+    free(s->object);
+    free(s->pupil);
+    free(s->gains);
+    free(s->background);
+    free(s->velocity);
+    free(s->anchor);
+    free(s->patch);
+    free(s->exit_spec);
+    free(s->field);
+    free(s->projected);
+    free(s->difference);
+    free(s->spectrum);
+    free(s->pupil_gradient);
+    free(s->gradient);
+    free(s->prediction);
+}
+
+/* ReconstructionProblem::validate (src/reconstruction/problem.rs:35-72) and
+ * MeasurementStack::validate (src/measurements/stack.rs:377-...). */
+static int32_t validate_problem(const orc_problem *p) {
+    size_t n = (size_t)p->h * p->w;
+    if (p->h <= 0 || p->w <= 0 || p->frames <= 0)
+        return fail(ORC_INVALID_MEASUREMENTS, "stored frame count, image shape, and data length are inconsistent");
+    for (size_t i = 0; i < n * p->frames; ++i)
+        if (!isfinite(p->data[i])) return fail(ORC_INVALID_MEASUREMENTS, "measurements contain non-finite values");
+    int positive = 0;
+    for (int f = 0; f < p->frames; ++f) {
+        double wgt = frame_weight(p, f);
+        if (!isfinite(wgt) || wgt < 0.0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has invalid weight", f);
+        if (wgt > 0.0) {
+            ++positive;
+            const uint8_t *m = frame_mask(p, f);
+            if (m) {
+                int any = 0;
+                for (size_t i = 0; i < n; ++i) any |= m[i] != 0;
+                if (!any) return fail(ORC_INVALID_MEASUREMENTS, "positive-weight frame %d has no unmasked pixels", f);
+            }
+        }
+        double g = model_gain(p, f);
+        if (!isfinite(g) || g < 0.0) return fail(ORC_INVALID_MODEL, "frame gains must be finite and non-negative");
+    }
+    if (positive == 0) return fail(ORC_INVALID_MEASUREMENTS, "at least one frame must have positive weight");
+    return ORC_OK;
+}
+
+/* ReconstructionState::initialize_with_backend (src/reconstruction/state.rs:280-355). */
+static int32_t state_init(orc_state *s, const orc_problem *p) {
+    memset(s, 0, sizeof *s);
+    s->p = p;
+    s->h = p->h;
+    s->w = p->w;
+    s->mh = p->mh;
+    s->mw = p->mw;
+    s->frames = p->frames;
+    s->n_low = (size_t)p->h * p->w;
+    s->n_high = (size_t)p->mh * p->mw;
+    int32_t st = validate_problem(p);
+    if (st) return st;
+    double *average = (double *)calloc(s->n_low, sizeof(double));
+    double *weight = (double *)calloc(s->n_low, sizeof(double));
+    double total_amplitude = 0.0, total_weight = 0.0;
+    for (int f = 0; f < p->frames; ++f) {
+        double fw = frame_weight(p, f);
+        if (fw == 0.0) continue;
+        const uint8_t *mask = frame_mask(p, f);
+        double gain = model_gain(p, f);
+        const double *frame = p->data + (size_t)f * s->n_low;
+        for (size_t i = 0; i < s->n_low; ++i) {
+            if (mask && mask[i] == 0) continue;
+            double amplitude = sqrt(fmax((frame[i] - model_background(p, f, i)) / gain, 0.0));
+            average[i] += fw * amplitude;
+            weight[i] += fw;
+            total_amplitude += fw * amplitude;
+            total_weight += fw;
+        }
+    }
+    if (total_weight == 0.0) {
+        free(average);
+        free(weight);
+        return fail(ORC_INVALID_MEASUREMENTS, "no positive-weight, unmasked measurements are available");
+    }
+    double fallback = total_amplitude / total_weight;
+    for (size_t i = 0; i < s->n_low; ++i) average[i] = weight[i] > 0.0 ? average[i] / weight[i] : fallback;
+    cplx *object = (cplx *)malloc(sizeof(cplx) * s->n_high);
+    for (int r = 0; r < s->mh; ++r) {
+        long lr = (long)r * s->h / s->mh;
+        for (int c = 0; c < s->mw; ++c) {
+            long lc = (long)c * s->w / s->mw;
+            object[(size_t)r * s->mw + c] = cx(average[lr * s->w + lc], 0.0);
+        }
+    }
+    free(average);
+    free(weight);
+    fft2_c(object, s->mh, s->mw, 0);
+    s->object = (cplx *)malloc(sizeof(cplx) * s->n_high);
+    fftshift_c(object, s->object, s->mh, s->mw);
+    free(object);
+    s->pupil = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    memcpy(s->pupil, p->pupil, sizeof(cplx) * s->n_low);
+    s->gains = (double *)malloc(sizeof(double) * (size_t)p->frames);
+    for (int f = 0; f < p->frames; ++f) s->gains[f] = model_gain(p, f);
+    if (p->background) {
+        s->background = (double *)malloc(sizeof(double) * s->n_low * p->frames);
+        for (int f = 0; f < p->frames; ++f)
+            for (size_t i = 0; i < s->n_low; ++i) s->background[(size_t)f * s->n_low + i] = model_background(p, f, i);
+    }
+    s->patch = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->exit_spec = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->field = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->projected = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->difference = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->spectrum = (cplx *)malloc(sizeof(cplx) * s->n_low);
+    s->pupil_gradient = (cplx *)calloc(s->n_low, sizeof(cplx));
+    s->prediction = (double *)malloc(sizeof(double) * s->n_low);
+    return ORC_OK;
+}
+
+static double src_off_row(const orc_problem *p, int s) { return p->off_row ? p->off_row[s] : 0.0; }
+static double src_off_col(const orc_problem *p, int s) { return p->off_col ? p->off_col[s] : 0.0; }
+
+/* Patch, pupil, ifftshift and inverse FFT: the coherent detector field of one
+ * source (src/algorithms/common.rs:94-131, gradient_descent.rs:1184-1213). */
+static int32_t source_field(orc_state *s, int source) {
+    const orc_problem *p = s->p;
+    int32_t st = extract_patch_c(s->object, s->mh, s->mw, (long)p->start_row[source], (long)p->start_col[source],
+                                 s->h, s->w, src_off_row(p, source), src_off_col(p, source), s->patch);
+    if (st) return st;
+    for (size_t i = 0; i < s->n_low; ++i) s->exit_spec[i] = c_mul(s->patch[i], s->pupil[i]);
+    ifftshift_c(s->exit_spec, s->field, s->h, s->w);
+    fft2_c(s->field, s->h, s->w, 1);
+    return ORC_OK;
+}
+
+typedef struct {
+    double object_step, epsilon;
+    int loss;
+    int denominator; /* 0 local, 1 rpie, 2 global */
+    double alpha;
+    int has_pupil_step;
+    double pupil_step;
+    int constrain_pupil;
+    int gain_update;
+    double gain_step, gain_min, gain_max;
+    int background_update;
+    double background_step, background_min, background_max;
+    int momentum;
+    long interval;
+    double friction, feedback;
+} update_config;
+
+typedef struct {
+    double objective_sum, weight_sum;
+} step_summary;
+
+/* apply_momentum_event (src/algorithms/common.rs:355-387). */
+int32_t orc_momentum_event(double *object_d, double *velocity_d, double *anchor_d, int64_t len,
+                           double friction, double feedback) {
+    cplx *object = (cplx *)object_d, *velocity = (cplx *)velocity_d, *anchor = (cplx *)anchor_d;
+    for (int64_t i = 0; i < len; ++i) {
+        cplx nv = c_add(c_scale(velocity[i], friction), c_sub(object[i], anchor[i]));
+        cplx no = feedback == 0.0 ? object[i] : c_add(object[i], c_scale(nv, feedback));
+        if (!isfinite(nv.re) || !isfinite(nv.im) || !isfinite(no.re) || !isfinite(no.im))
+            return fail(ORC_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
+        velocity[i] = nv;
+        object[i] = no;
+        anchor[i] = no;
+    }
+    return ORC_OK;
+}
+
+/* projection_update (src/algorithms/common.rs:57-306) for non-multiplexed
+ * frames, with update_gain (:390-422), update_background (:425-489) and
+ * apply_object_momentum (:308-353). */
+static int32_t projection_update(orc_state *s, const int *frames, int count, const update_config *cfg,
+                                 step_summary *summary) {
+    const orc_problem *p = s->p;
+    size_t n = s->n_low;
+    for (int b = 0; b < count; ++b) {
+        int frame = frames[b];
+        double fw = frame_weight(p, frame);
+        if (fw == 0.0) continue;
+        double source_weight_sum = 1.0;
+        int32_t st = source_field(s, frame);
+        if (st) return st;
+        for (size_t i = 0; i < n; ++i) s->prediction[i] = c_norm_sqr(s->field[i]);
+        const double *measured = p->data + (size_t)frame * n;
+        const uint8_t *mask = frame_mask(p, frame);
+        double gain = s->gains[frame];
+        if (!isfinite(gain) || gain <= 0.0) return fail(ORC_INVALID_MODEL, "state frame %d has invalid gain", frame);
+        if (cfg->gain_update) {
+            double num = 0.0, den = 0.0;
+            for (size_t i = 0; i < n; ++i) {
+                if (mask && mask[i] == 0) continue;
+                double pred = s->prediction[i];
+                num += pred * fmax(measured[i] - state_background(s, frame, i), 0.0);
+                den += pred * pred;
+            }
+            if (den > cfg->epsilon) {
+                double est = fmin(fmax(num / den, cfg->gain_min), cfg->gain_max);
+                gain = fmin(fmax((1.0 - cfg->gain_step) * gain + cfg->gain_step * est, cfg->gain_min), cfg->gain_max);
+                s->gains[frame] = gain;
+            }
+        }
+        if (cfg->background_update) {
+            double residual = 0.0;
+            long rc = 0;
+            for (size_t i = 0; i < n; ++i) {
+                if (mask && mask[i] == 0) continue;
+                residual += measured[i] - gain * s->prediction[i] - state_background(s, frame, i);
+                ++rc;
+            }
+            if (rc > 0) {
+                double correction = cfg->background_step * residual / (double)rc;
+                if (!s->background) s->background = (double *)calloc(n * s->frames, sizeof(double));
+                double *bg = s->background + (size_t)frame * n;
+                for (size_t i = 0; i < n; ++i)
+                    bg[i] = fmin(fmax(bg[i] + correction, cfg->background_min), cfg->background_max);
+            }
+        }
+        double frame_loss = 0.0;
+        long valid = 0;
+        for (size_t i = 0; i < n; ++i) {
+            double intrinsic = s->prediction[i];
+            if (mask && mask[i] == 0) {
+                s->projected[i] = cx(1.0, 0.0);
+                continue;
+            }
+            ++valid;
+            double bg = state_background(s, frame, i);
+            double predicted = gain * intrinsic + bg;
+            frame_loss += point_loss(predicted, measured[i], cfg->loss);
+            double target = fmax((measured[i] - bg) / gain, 0.0);
+            s->projected[i] = intrinsic > cfg->epsilon ? cx(sqrt(target / intrinsic), 0.0)
+                                                       : cx(0.0, sqrt(target / source_weight_sum));
+        }
+        if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", frame);
+        summary->objective_sum += fw * (frame_loss / (double)valid);
+        summary->weight_sum += fw;
+        double max_pupil = 0.0;
+        for (size_t i = 0; i < n; ++i) max_pupil = fmax(max_pupil, c_norm_sqr(s->pupil[i]));
+        max_pupil = fmax(max_pupil, cfg->epsilon);
+        if (cfg->has_pupil_step) memset(s->pupil_gradient, 0, sizeof(cplx) * n);
+        for (size_t i = 0; i < n; ++i) {
+            cplx proj = s->projected[i];
+            if (mask && mask[i] == 0)
+                s->difference[i] = s->field[i];
+            else if (s->prediction[i] > cfg->epsilon)
+                s->difference[i] = c_scale(s->field[i], proj.re);
+            else
+                s->difference[i] = cx(proj.im, 0.0);
+        }
+        fft2_c(s->difference, s->h, s->w, 0);
+        fftshift_c(s->difference, s->spectrum, s->h, s->w);
+        for (size_t i = 0; i < n; ++i) s->difference[i] = c_sub(s->spectrum[i], c_mul(s->patch[i], s->pupil[i]));
+        double normalized = 1.0 / source_weight_sum;
+        for (size_t i = 0; i < n; ++i) {
+            cplx pup = s->pupil[i];
+            double local = c_norm_sqr(pup);
+            double den;
+            if (cfg->denominator == 0)
+                den = local + cfg->epsilon;
+            else if (cfg->denominator == 2)
+                den = max_pupil + cfg->epsilon;
+            else
+                den = (1.0 - cfg->alpha) * local + cfg->alpha * max_pupil + cfg->epsilon;
+            s->exit_spec[i] = c_divr(c_mul(c_conj(pup), s->difference[i]), den);
+        }
+        st = insert_adjoint_c(s->object, s->mh, s->mw, (long)p->start_row[frame], (long)p->start_col[frame], s->h,
+                              s->w, src_off_row(p, frame), src_off_col(p, frame), s->exit_spec,
+                              fw * cfg->object_step * normalized);
+        if (st) return st;
+        if (cfg->has_pupil_step) {
+            double max_object = 0.0;
+            for (size_t i = 0; i < n; ++i) max_object = fmax(max_object, c_norm_sqr(s->patch[i]));
+            max_object = fmax(max_object, cfg->epsilon);
+            for (size_t i = 0; i < n; ++i)
+                s->pupil_gradient[i] = c_add(s->pupil_gradient[i],
+                                             c_divr(c_scale(c_mul(c_conj(s->patch[i]), s->difference[i]), normalized),
+                                                    max_object + cfg->epsilon));
+            for (size_t i = 0; i < n; ++i)
+                s->pupil[i] = c_add(s->pupil[i], c_scale(s->pupil_gradient[i], fw * cfg->pupil_step));
+            if (cfg->constrain_pupil)
+                for (size_t i = 0; i < n; ++i)
+                    if (p->support[i] == 0) s->pupil[i] = cx(0.0, 0.0);
+        }
+        if (cfg->momentum) {
+            s->momentum_count += 1;
+            if (s->momentum_count >= cfg->interval) {
+                if (s->momentum_count != cfg->interval)
+                    return fail(ORC_INVALID_MODEL, "mPIE frame counter exceeds the configured momentum interval");
+                st = orc_momentum_event((double *)s->object, (double *)s->velocity, (double *)s->anchor,
+                                        (int64_t)s->n_high, cfg->friction, cfg->feedback);
+                if (st) return st;
+                s->momentum_count = 0;
+            }
+        }
+    }
+    return ORC_OK;
+}
+
+/* GradientDescent::step (src/algorithms/gradient_descent.rs:405-671) for the
+ * ordinary object gradient: no truncation, pupil or illumination recovery,
+ * and no regularisation. */
+static int32_t gradient_step(orc_state *s, const int *frames, int count, double object_step, double epsilon,
+                             int loss, step_summary *summary) {
+    const orc_problem *p = s->p;
+    size_t n = s->n_low;
+    double max_pupil = 0.0;
+    for (size_t i = 0; i < n; ++i) max_pupil = fmax(max_pupil, c_norm_sqr(s->pupil[i]));
+    max_pupil = fmax(max_pupil, epsilon);
+    if (!s->gradient) s->gradient = (cplx *)malloc(sizeof(cplx) * s->n_high);
+    memset(s->gradient, 0, sizeof(cplx) * s->n_high);
+    long active = 0;
+    for (int b = 0; b < count; ++b) {
+        int frame = frames[b];
+        double fw = frame_weight(p, frame);
+        if (fw == 0.0) continue;
+        ++active;
+        int32_t st = source_field(s, frame);
+        if (st) return st;
+        for (size_t i = 0; i < n; ++i) s->projected[i] = cx(c_norm_sqr(s->field[i]), 0.0);
+        const double *measured = p->data + (size_t)frame * n;
+        const uint8_t *mask = frame_mask(p, frame);
+        double gain = s->gains[frame];
+        if (!isfinite(gain) || gain <= 0.0) return fail(ORC_INVALID_MODEL, "state frame %d has invalid gain", frame);
+        double frame_loss = 0.0;
+        long valid = 0;
+        for (size_t i = 0; i < n; ++i) {
+            if (mask && mask[i] == 0) {
+                s->projected[i] = cx(0.0, 0.0);
+                continue;
+            }
+            ++valid;
+            double bg = state_background(s, frame, i);
+            double intrinsic = fmax(s->projected[i].re, 0.0);
+            double target = fmax((measured[i] - bg) / gain, 0.0);
+            frame_loss += point_loss(intrinsic, target, loss);
+            s->projected[i] = cx(descent_factor(intrinsic, target, loss, epsilon), intrinsic);
+        }
+        if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", frame);
+        double valid_scale = (double)n / (double)valid;
+        summary->objective_sum += fw * (frame_loss / (double)valid);
+        summary->weight_sum += fw;
+        /* The reference recomputes the same field here; the object has not
+         * changed, so the field from above is reused. */
+        for (size_t i = 0; i < n; ++i) s->field[i] = c_scale(s->field[i], 1.0 * s->projected[i].re);
+        fft2_c(s->field, s->h, s->w, 0);
+        fftshift_c(s->field, s->spectrum, s->h, s->w);
+        for (size_t i = 0; i < n; ++i)
+            s->difference[i] = c_divr(c_mul(c_conj(s->pupil[i]), s->spectrum[i]), max_pupil + epsilon);
+        st = insert_adjoint_c(s->gradient, s->mh, s->mw, (long)p->start_row[frame], (long)p->start_col[frame], s->h,
+                              s->w, src_off_row(p, frame), src_off_col(p, frame), s->difference, fw * valid_scale);
+        if (st) return st;
+    }
+    if (active > 0) {
+        double step = object_step / (double)active;
+        for (size_t i = 0; i < s->n_high; ++i) s->object[i] = c_sub(s->object[i], c_scale(s->gradient[i], step));
+    }
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------- gauge */
+
+/* relative_phase_slope (src/algorithms/gauge.rs:75-130). */
+static double relative_phase_slope(const orc_state *s, int axis_row, double tol) {
+    const cplx *values = s->pupil, *ref = (const cplx *)s->p->pupil;
+    const uint8_t *support = s->p->support;
+    int h = s->h, w = s->w;
+    cplx resultant = cx(0, 0), strongest = cx(0, 0);
+    double total = 0.0, strongest_w = 0.0;
+    int rl = axis_row ? h - 1 : h, cl = axis_row ? w : w - 1;
+    for (int r = 0; r < rl; ++r)
+        for (int c = 0; c < cl; ++c) {
+            size_t cur = (size_t)r * w + c;
+            size_t nxt = axis_row ? (size_t)(r + 1) * w + c : cur + 1;
+            if (support[cur] == 0 || support[nxt] == 0) continue;
+            cplx ce = c_mul(values[nxt], c_conj(values[cur]));
+            cplx re = c_mul(ref[nxt], c_conj(ref[cur]));
+            cplx contribution = c_mul(ce, c_conj(re));
+            double weight = c_norm(contribution);
+            if (!isfinite(weight)) continue;
+            resultant = c_add(resultant, contribution);
+            total += weight;
+            if (weight > strongest_w) {
+                strongest = contribution;
+                strongest_w = weight;
+            }
+        }
+    if (total == 0.0) return 0.0;
+    if (c_norm(resultant) > tol * total) return c_arg(resultant);
+    if (strongest_w > 0.0) return c_arg(strongest);
+    return 0.0;
+}
+
+/* canonicalize_object_pupil (src/algorithms/gauge.rs:20-73) with
+ * apply_affine_correction (:132-156), normalize_pupil_scale_and_phase
+ * (:158-240) and normalize_object_phase (:242-282). */
+static int32_t canonicalize_gauge(orc_state *s) {
+    const orc_problem *p = s->p;
+    size_t n = s->n_low;
+    long support_count = 0;
+    for (size_t i = 0; i < n; ++i) support_count += p->support[i] != 0;
+    if (support_count == 0) return fail(ORC_INVALID_MODEL, "compiled reference pupil support is empty");
+    double tol = 64.0 * 2.220446049250313e-16 * (double)support_count;
+    int row_exact = 1, col_exact = 1;
+    for (int src = 0; src < s->frames; ++src) {
+        row_exact &= offset_is_zero(src_off_row(p, src), 0.0);
+        col_exact &= offset_is_zero(0.0, src_off_col(p, src));
+    }
+    double row_slope = row_exact ? relative_phase_slope(s, 1, tol) : 0.0;
+    double col_slope = col_exact ? relative_phase_slope(s, 0, tol) : 0.0;
+    if (fabs(row_slope) > tol || fabs(col_slope) > tol) {
+        for (int r = 0; r < s->h; ++r) {
+            double y = (double)r - (double)(s->h / 2);
+            for (int c = 0; c < s->w; ++c) {
+                double x = (double)c - (double)(s->w / 2);
+                s->pupil[(size_t)r * s->w + c] =
+                    c_mul(s->pupil[(size_t)r * s->w + c], c_polar(1.0, -(row_slope * y + col_slope * x)));
+            }
+        }
+        for (int r = 0; r < s->mh; ++r) {
+            double y = (double)r - (double)(s->mh / 2);
+            for (int c = 0; c < s->mw; ++c) {
+                double x = (double)c - (double)(s->mw / 2);
+                s->object[(size_t)r * s->mw + c] =
+                    c_mul(s->object[(size_t)r * s->mw + c], c_polar(1.0, row_slope * y + col_slope * x));
+            }
+        }
+    }
+    const cplx *ref = (const cplx *)p->pupil;
+    double ref_energy = 0.0, cur_energy = 0.0;
+    for (size_t i = 0; i < n; ++i)
+        if (p->support[i]) {
+            ref_energy += c_norm_sqr(ref[i]);
+            cur_energy += c_norm_sqr(s->pupil[i]);
+        }
+    if (!isfinite(ref_energy) || ref_energy <= 0.0)
+        return fail(ORC_INVALID_MODEL, "compiled reference pupil has invalid supported energy");
+    if (!isfinite(cur_energy) || cur_energy <= 0.0)
+        return fail(ORC_NUMERICAL, "object/pupil gauge normalization requires positive finite recovered pupil energy");
+    double computed = sqrt(ref_energy / cur_energy);
+    if (!isfinite(computed) || computed <= 0.0)
+        return fail(ORC_NUMERICAL, "object/pupil gauge normalization produced an invalid pupil scale");
+    double scale = fabs(computed - 1.0) <= tol ? 1.0 : computed;
+    cplx overlap = cx(0, 0), strongest = cx(0, 0);
+    double overlap_w = 0.0, strongest_w = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        if (p->support[i] == 0) continue;
+        cplx contribution = c_mul(c_conj(ref[i]), s->pupil[i]);
+        double weight = c_norm(contribution);
+        overlap = c_add(overlap, contribution);
+        overlap_w += weight;
+        if (weight > strongest_w) {
+            strongest = contribution;
+            strongest_w = weight;
+        }
+    }
+    double phase;
+    if (overlap_w > 0.0 && c_norm(overlap) > tol * overlap_w)
+        phase = c_arg(overlap);
+    else if (strongest_w > 0.0)
+        phase = c_arg(strongest);
+    else
+        return fail(ORC_NUMERICAL, "object/pupil gauge normalization could not anchor recovered pupil phase");
+    if (!isfinite(phase)) return fail(ORC_NUMERICAL, "object/pupil gauge normalization produced a non-finite pupil phase");
+    if (fabs(phase) <= tol) phase = 0.0;
+    cplx pupil_factor = c_polar(scale, -phase);
+    cplx object_factor = c_div(cx(1.0, 0.0), pupil_factor);
+    if (!(pupil_factor.re == 1.0 && pupil_factor.im == 0.0)) {
+        for (size_t i = 0; i < n; ++i) s->pupil[i] = c_mul(s->pupil[i], pupil_factor);
+        for (size_t i = 0; i < s->n_high; ++i) s->object[i] = c_mul(s->object[i], object_factor);
+    }
+    cplx strongest_o = cx(0, 0);
+    double strongest_m = 0.0;
+    for (size_t i = 0; i < s->n_high; ++i) {
+        cplx v = s->object[i];
+        if (!isfinite(v.re) || !isfinite(v.im))
+            return fail(ORC_NUMERICAL, "object/pupil gauge normalization requires a finite object spectrum");
+        double m = c_norm(v);
+        if (m > strongest_m) {
+            strongest_o = v;
+            strongest_m = m;
+        }
+    }
+    if (strongest_m == 0.0) return ORC_OK;
+    cplx dc = s->object[(size_t)(s->mh / 2) * s->mw + s->mw / 2];
+    cplx anchor = c_norm(dc) > tol * strongest_m ? dc : strongest_o;
+    double object_phase = c_arg(anchor);
+    if (!isfinite(object_phase)) return fail(ORC_NUMERICAL, "object/pupil gauge normalization produced a non-finite object phase");
+    if (fabs(object_phase) <= tol) return ORC_OK;
+    cplx correction = c_polar(1.0, -object_phase);
+    for (size_t i = 0; i < s->n_high; ++i) s->object[i] = c_mul(s->object[i], correction);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------- schedule */
+
+/* f64::total_cmp ordering key. */
+static int64_t total_key(double v) {
+    int64_t bits;
+    memcpy(&bits, &v, sizeof bits);
+    bits ^= (int64_t)(((uint64_t)(bits >> 63)) >> 1);
+    return bits;
+}
+
+typedef struct {
+    int frame;
+    double a, b;
+} sort_item;
+
+static int cmp_items(const void *x, const void *y) {
+    const sort_item *l = (const sort_item *)x, *r = (const sort_item *)y;
+    int64_t la = total_key(l->a), ra = total_key(r->a);
+    if (la != ra) return la < ra ? -1 : 1;
+    int64_t lb = total_key(l->b), rb = total_key(r->b);
+    if (lb != rb) return lb < rb ? -1 : 1;
+    return l->frame < r->frame ? -1 : (l->frame > r->frame);
+}
+
+/* FrameSchedule::order / order_for_problem (src/reconstruction/schedule.rs:35-102). */
+static int32_t schedule_order(const orc_problem *p, int schedule, int *order) {
+    int frames = p->frames;
+    for (int f = 0; f < frames; ++f) order[f] = f;
+    if (schedule == ORC_SCHEDULE_SEQUENTIAL) return ORC_OK;
+    sort_item *items = (sort_item *)malloc(sizeof(sort_item) * (size_t)frames);
+    for (int f = 0; f < frames; ++f) {
+        items[f].frame = f;
+        items[f].b = 0.0;
+        if (schedule == ORC_SCHEDULE_SNR_WEIGHTED) {
+            double w = frame_weight(p, f);
+            double score;
+            if (w == 0.0) {
+                score = -INFINITY;
+            } else {
+                size_t n = (size_t)p->h * p->w;
+                const double *m = p->data + (size_t)f * n;
+                const uint8_t *mask = frame_mask(p, f);
+                double sum = 0.0;
+                long valid = 0;
+                for (size_t i = 0; i < n; ++i)
+                    if (!mask || mask[i] != 0) {
+                        sum += fmax(m[i] - model_background(p, f, i), 0.0);
+                        ++valid;
+                    }
+                score = valid == 0 ? -INFINITY : w * sqrt(sum / (double)valid);
+            }
+            items[f].a = -score; /* descending score, then ascending frame */
+        } else {
+            double kx = p->kx[f], ky = p->ky[f];
+            items[f].a = hypot(kx, ky);
+            if (schedule == ORC_SCHEDULE_SPIRAL_OUT) {
+                double angle = fmod(atan2(ky, kx), 2.0 * M_PI);
+                if (angle < 0.0) angle += 2.0 * M_PI;
+                items[f].b = angle;
+            }
+        }
+    }
+    qsort(items, (size_t)frames, sizeof(sort_item), cmp_items);
+    for (int f = 0; f < frames; ++f) order[f] = items[f].frame;
+    free(items);
+    return ORC_OK;
+}
+
+/* --------------------------------------------------------------- runner */
+
+/* Runner::run (src/reconstruction/runner.rs:76-285) without callbacks,
+ * checkpoints or diagnostics, then ReconstructionResult::from_state
+ * (src/reconstruction/result.rs:76-105,397-413). */
+int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
+    if (prm->batch_size <= 0) return out->status = fail(ORC_INVALID_PARAMETER, "batch_size must be greater than zero");
+    if (!isfinite(prm->object_step) || prm->object_step <= 0.0)
+        return out->status = fail(ORC_INVALID_PARAMETER, "object_step must be finite and positive");
+    if (!isfinite(prm->epsilon) || prm->epsilon <= 0.0)
+        return out->status = fail(ORC_INVALID_PARAMETER, "epsilon must be finite and positive");
+    if (prm->algorithm == ORC_ALG_GD && prm->recover_pupil)
+        return out->status = fail(ORC_UNSUPPORTED, "gradient-descent pupil recovery is not restated");
+    orc_state s;
+    int32_t st = state_init(&s, p);
+    if (st) {
+        state_free(&s);
+        return out->status = st;
+    }
+    update_config cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.object_step = prm->object_step;
+    cfg.epsilon = prm->epsilon;
+    cfg.loss = prm->loss_type;
+    cfg.constrain_pupil = 1;
+    int canonical = 0;
+    switch (prm->algorithm) {
+    case ORC_ALG_AP:
+        cfg.denominator = 0;
+        break;
+    case ORC_ALG_FPIE:
+        cfg.denominator = 1;
+        cfg.alpha = prm->stability;
+        break;
+    case ORC_ALG_MPIE:
+        cfg.denominator = 1;
+        cfg.alpha = prm->stability;
+        cfg.momentum = 1;
+        cfg.interval = prm->momentum_interval;
+        cfg.friction = prm->momentum_friction;
+        cfg.feedback = prm->momentum_feedback;
+        s.velocity = (cplx *)calloc(s.n_high, sizeof(cplx));
+        s.anchor = (cplx *)malloc(sizeof(cplx) * s.n_high);
+        memcpy(s.anchor, s.object, sizeof(cplx) * s.n_high);
+        break;
+    case ORC_ALG_EPRY:
+        cfg.denominator = 2;
+        cfg.has_pupil_step = prm->recover_pupil;
+        cfg.pupil_step = prm->pupil_step;
+        cfg.constrain_pupil = prm->constrain_pupil;
+        cfg.gain_update = prm->recover_gains;
+        cfg.gain_step = prm->gain_step;
+        cfg.gain_min = prm->gain_min;
+        cfg.gain_max = prm->gain_max;
+        cfg.background_update = prm->recover_background;
+        cfg.background_step = prm->background_step;
+        cfg.background_min = prm->background_min;
+        cfg.background_max = prm->background_max;
+        canonical = prm->recover_pupil;
+        break;
+    case ORC_ALG_GD:
+        break;
+    default:
+        state_free(&s);
+        return out->status = fail(ORC_UNSUPPORTED, "unknown algorithm");
+    }
+    if (canonical && (st = canonicalize_gauge(&s))) {
+        state_free(&s);
+        return out->status = st;
+    }
+    int *order = (int *)malloc(sizeof(int) * (size_t)p->frames);
+    for (int it = 0; it < prm->iterations && !st; ++it) {
+        st = schedule_order(p, prm->schedule, order);
+        step_summary summary = {0.0, 0.0};
+        for (int start = 0; start < p->frames && !st; start += prm->batch_size) {
+            int count = p->frames - start < prm->batch_size ? p->frames - start : prm->batch_size;
+            if (prm->algorithm == ORC_ALG_GD)
+                st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type, &summary);
+            else
+                st = projection_update(&s, order + start, count, &cfg, &summary);
+        }
+        if (!st && canonical) st = canonicalize_gauge(&s);
+        if (out->objectives) out->objectives[it] = summary.weight_sum > 0.0 ? summary.objective_sum / summary.weight_sum : NAN;
+    }
+    free(order);
+    if (!st) {
+        if (out->object_spectrum) memcpy(out->object_spectrum, s.object, sizeof(cplx) * s.n_high);
+        if (out->pupil) memcpy(out->pupil, s.pupil, sizeof(cplx) * s.n_low);
+        if (out->object) {
+            ifftshift_c(s.object, (cplx *)out->object, s.mh, s.mw);
+            fft2_c((cplx *)out->object, s.mh, s.mw, 1);
+        }
+    }
+    state_free(&s);
+    return out->status = st;
+}
+
+/* ------------------------------------------------------------ threading */
+
+typedef struct {
+    int32_t count;
+    const orc_problem *problems;
+    const orc_params *params;
+    orc_output *outputs;
+    int next;
+    pthread_mutex_t lock;
+} run_pool;
+
+static void *run_worker(void *arg) {
+    run_pool *pool = (run_pool *)arg;
+    for (;;) {
+        pthread_mutex_lock(&pool->lock);
+        int i = pool->next++;
+        pthread_mutex_unlock(&pool->lock);
+        if (i >= pool->count) break;
+        orc_run(&pool->problems[i], pool->params, &pool->outputs[i]);
+    }
+    return NULL;
+}
+
+/* Independent tiles run concurrently; each tile keeps its own sequential
+ * frame order exactly as a single run would. */
+int32_t orc_run_many(int32_t count, const orc_problem *problems, const orc_params *params,
+                     orc_output *outputs, int32_t workers) {
+    if (workers < 1) workers = 1;
+    if (workers > count) workers = count;
+    run_pool pool = {count, problems, params, outputs, 0, PTHREAD_MUTEX_INITIALIZER};
+    pthread_t *threads = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)workers);
+    for (int t = 0; t < workers; ++t) pthread_create(&threads[t], NULL, run_worker, &pool);
+    for (int t = 0; t < workers; ++t) pthread_join(threads[t], NULL);
+    free(threads);
+    for (int i = 0; i < count; ++i)
+        if (outputs[i].status) return outputs[i].status;
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------ forward, result */
+
+int32_t orc_object_spectrum(const double *object, int32_t mh, int32_t mw, double *spectrum) {
+    size_t n = (size_t)mh * mw;
+    cplx *tmp = (cplx *)malloc(sizeof(cplx) * n);
+    memcpy(tmp, object, sizeof(cplx) * n);
+    fft2_c(tmp, mh, mw, 0);
+    fftshift_c(tmp, (cplx *)spectrum, mh, mw);
+    free(tmp);
+    return ORC_OK;
+}
+
+int32_t orc_state_object(const double *spectrum, int32_t mh, int32_t mw, double *object) {
+    ifftshift_c((const cplx *)spectrum, (cplx *)object, mh, mw);
+    fft2_c((cplx *)object, mh, mw, 1);
+    return ORC_OK;
+}
+
+typedef struct {
+    const orc_problem *p;
+    const cplx *spectrum;
+    double *out;
+    int first, last;
+    int32_t status;
+} forward_job;
+
+/* ForwardModel::forward_intensity_standard_into (src/model/forward.rs:245-292)
+ * for a contiguous chunk of frames. */
+static void *forward_worker(void *arg) {
+    forward_job *job = (forward_job *)arg;
+    const orc_problem *p = job->p;
+    size_t n = (size_t)p->h * p->w;
+    cplx *patch = (cplx *)malloc(sizeof(cplx) * n * 2);
+    cplx *field = patch + n;
+    const cplx *pupil = (const cplx *)p->pupil;
+    for (int f = job->first; f < job->last; ++f) {
+        int32_t st = extract_patch_c(job->spectrum, p->mh, p->mw, (long)p->start_row[f], (long)p->start_col[f], p->h,
+                                     p->w, src_off_row(p, f), src_off_col(p, f), patch);
+        if (st) {
+            job->status = st;
+            break;
+        }
+        for (size_t i = 0; i < n; ++i) patch[i] = c_mul(patch[i], pupil[i]);
+        ifftshift_c(patch, field, p->h, p->w);
+        fft2_c(field, p->h, p->w, 1);
+        double gain = model_gain(p, f);
+        double *dst = job->out + (size_t)f * n;
+        for (size_t i = 0; i < n; ++i) dst[i] = gain * c_norm_sqr(field[i]) + model_background(p, f, i);
+    }
+    free(patch);
+    return NULL;
+}
+
+/* ForwardModel::forward_intensity_stack_into (src/model/forward.rs:300-372):
+ * contiguous frame chunks per worker; results do not depend on the count. */
+int32_t orc_forward_stack(const orc_problem *p, const double *spectrum, double *out, int32_t workers) {
+    if (workers <= 0) return fail(ORC_INVALID_PARAMETER, "worker_count must be greater than zero");
+    if (workers > p->frames) workers = p->frames;
+    int per = (p->frames + workers - 1) / workers;
+    int jobs = (p->frames + per - 1) / per;
+    forward_job *job = (forward_job *)calloc((size_t)jobs, sizeof(forward_job));
+    pthread_t *threads = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)jobs);
+    for (int j = 0; j < jobs; ++j) {
+        job[j].p = p;
+        job[j].spectrum = (const cplx *)spectrum;
+        job[j].out = out;
+        job[j].first = j * per;
+        job[j].last = (j + 1) * per < p->frames ? (j + 1) * per : p->frames;
+        pthread_create(&threads[j], NULL, forward_worker, &job[j]);
+    }
+    int32_t st = ORC_OK;
+    for (int j = 0; j < jobs; ++j) {
+        pthread_join(threads[j], NULL);
+        if (job[j].status && !st) st = job[j].status;
+    }
+    free(job);
+    free(threads);
+    return st;
+}
+
+/* compare_complex_fields_masked complex_nrmse
+ * (src/metrics/complex_field/comparison.rs:60-121), unmasked. */
+double orc_complex_nrmse(const double *reference_d, const double *candidate_d, int64_t len) {
+    const cplx *reference = (const cplx *)reference_d, *candidate = (const cplx *)candidate_d;
+    cplx cross = cx(0, 0);
+    for (int64_t i = 0; i < len; ++i) cross = c_add(cross, c_mul(candidate[i], c_conj(reference[i])));
+    cplx correction = c_polar(1.0, -c_arg(cross));
+    double err = 0.0, ref = 0.0;
+    for (int64_t i = 0; i < len; ++i) {
+        cplx aligned = c_mul(candidate[i], correction);
+        err += c_norm_sqr(c_sub(aligned, reference[i]));
+        ref += c_norm_sqr(reference[i]);
+    }
+    double count = (double)len;
+    double denominator = sqrt(ref / count);
+    if (denominator < 2.220446049250313e-16) denominator = 2.220446049250313e-16;
+    return sqrt(err / count) / denominator;
+}

@@ -1,0 +1,204 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances: complex NRMSE (global-phase aligned, the reference's
+complex_nrmse) <= 1e-4 for reconstructed objects and EPRY pupils after the
+stated iteration count; FP64 device kernels (fft2) to 1e-12; the FP32 forward
+stack to 1e-5 relative; per-iteration objectives to 1e-4 relative. Integer
+work (crop origins, frame order) is bit-exact and checked on the host.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+NRMSE = 1e-4
+
+
+@pytest.fixture(scope="module")
+def fpm(native_library):
+    import fpm_rs
+
+    return fpm_rs
+
+
+def _objective_close(gpu, cpu, rtol=1e-4):
+    gpu = np.asarray(gpu)
+    cpu = np.asarray(cpu)
+    assert gpu.shape == cpu.shape
+    assert np.all(np.abs(gpu - cpu) <= rtol * np.abs(cpu) + 1e-12), (gpu, cpu)
+
+
+@pytest.mark.parametrize("shape", [(7, 9), (16, 16), (42, 42), (96, 96), (375, 375), (729, 729), (256, 256)])
+def test_fft2_matches_reference_convention(fpm, shape):
+    rng = np.random.default_rng(3)
+    values = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    forward = fpm.fft2(values)
+    expected = oracle.fft2(values)
+    assert np.abs(forward - expected).max() <= 1e-12 * max(1.0, np.abs(expected).max())
+    back = fpm.fft2(forward, inverse=True)
+    assert np.abs(back - values).max() <= 1e-10
+
+
+def test_fft2_constant_object_known_answer(fpm):
+    # tests/forward_model_tests.rs:75-101: forward normalisation by 1/N.
+    spectrum = fpm.fft2(np.full((16, 16), 2.0 + 0j))
+    assert abs(spectrum[0, 0] - 2.0) < 1e-12
+    assert np.abs(spectrum.ravel()[1:]).max() < 1e-12
+
+
+@pytest.mark.parametrize("n,side", [(32, 3), (64, 5), (128, 5), (256, 3)])
+def test_forward_stack_matches_oracle(fpm, n, side):
+    model, omodel = helpers.planar_model(fpm, side, n)
+    obj = W.smooth_random_object(model.reconstruction_shape, 17)
+    gpu = fpm.forward_intensities(model, obj)
+    cpu = oracle.forward_stack(oracle.Problem(omodel, None), oracle.object_spectrum(obj), workers=8)
+    assert np.abs(gpu - cpu).max() <= 1e-5 * np.abs(cpu).max()
+
+
+def _run_both(fpm, algorithm_gpu, name, kw, model, omodel, data, gains=None, weights=None, masks=None,
+              background=None, schedule="sequential"):
+    problem = fpm.ReconstructionProblem(data, model, frame_weights=weights, masks=masks)
+    result = algorithm_gpu.run(problem, schedule=schedule)
+    expected = oracle.run(oracle.Problem(omodel, data, weights=weights, masks=masks, gains=gains,
+                                         background=background), name, schedule=schedule, **kw)
+    return result, expected
+
+
+def test_ap_quickstart_config(fpm):
+    """Plain AP, README quickstart geometry: 3x3 LEDs, 32x32 frames, M=42, 20 iterations, ideal camera."""
+    model, omodel, data, truth, _ = helpers.simulated(fpm, 3, 32, seed=1234)
+    assert model.reconstruction_shape == (42, 42)
+    result, expected = _run_both(fpm, fpm.AlternatingProjection(iterations=20), "ap", dict(iterations=20),
+                                 model, omodel, data)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    assert oracle.complex_nrmse(expected["object_spectrum"], result.object_spectrum) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    assert result.trace[-1][1] < result.trace[0][1]
+
+
+@pytest.mark.parametrize("alg,kw", [
+    ("ap", dict(iterations=6)),
+    ("fpie", dict(iterations=6)),
+    ("mpie", dict(iterations=6, momentum_interval=7)),
+    ("epry", dict(iterations=6)),
+    ("gd", dict(iterations=6)),
+])
+@pytest.mark.parametrize("n,side", [(32, 5), (64, 5)])
+def test_algorithms_small(fpm, alg, kw, n, side):
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=7, photons=1e4)
+    cls = {"ap": fpm.AlternatingProjection, "fpie": fpm.Fpie, "mpie": fpm.Mpie, "epry": fpm.Epry,
+           "gd": fpm.GradientDescent}[alg]
+    result, expected = _run_both(fpm, cls(**kw), alg, kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    if alg == "epry":
+        assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
+
+
+def test_mpie_epry_pupil_config(fpm):
+    """mPIE and EPRY, 13x13 LEDs, 128x128 frames (M=336), Zernike true pupil, Poisson 5e3."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 13, 128, seed=1, photons=5e3, pupil_seed=11)
+    assert model.reconstruction_shape == (336, 336)
+    for name, algo, kw in (("mpie", fpm.Mpie(iterations=3), dict(iterations=3)),
+                           ("epry", fpm.Epry(iterations=3), dict(iterations=3))):
+        result, expected = _run_both(fpm, algo, name, kw, model, omodel, data, gains=gains)
+        assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, name
+        _objective_close([t[1] for t in result.trace], expected["objectives"])
+        if name == "epry":
+            assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
+
+
+def test_gradient_descent_full_tile(fpm):
+    """Wirtinger GD on one 256x256 tile with 15x15 LEDs (M=729), Poisson 1e4, 2 iterations."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 15, 256, seed=7, photons=1e4)
+    assert model.reconstruction_shape == (729, 729)
+    result, expected = _run_both(fpm, fpm.GradientDescent(iterations=2), "gd", dict(iterations=2), model, omodel,
+                                 data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
+def test_masks_weights_background(fpm):
+    """Masked pixels, a zero-weight frame and a broadcast background (AP and GD)."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=21, photons=2e3)
+    rng = np.random.default_rng(5)
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = np.ones(data.shape[0])
+    weights[3] = 0.0
+    weights[7] = 0.5
+    background = np.full(32 * 32, 3.0)
+    data = data + 3.0
+    model = model._replace(background=background)
+    for name, algo in (("ap", fpm.AlternatingProjection(iterations=4)), ("gd", fpm.GradientDescent(iterations=4))):
+        result, expected = _run_both(fpm, algo, name, dict(iterations=4), model, omodel, data, gains=gains,
+                                     weights=weights, masks=masks, background=background)
+        assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, name
+        _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
+@pytest.mark.parametrize("schedule", ["brightfield_first", "spiral_out", "snr_weighted"])
+def test_schedules(fpm, schedule):
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=9, photons=1e4)
+    result, expected = _run_both(fpm, fpm.Fpie(iterations=3), "fpie", dict(iterations=3), model, omodel, data,
+                                 gains=gains, schedule=schedule)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+
+
+def test_integer_offsets(fpm):
+    """k-vectors on exact grid multiples: integer crops, and EPRY's affine ramp gauge is active."""
+    optics = fpm.Optics(**W.OPTICS)
+    n = 32
+    dk = 2 * np.pi / (n * optics.object_pixel_size)
+    shifts = [(0, 0), (3, 0), (-3, 0), (0, 3), (0, -3), (2, 2), (-2, 2)]
+    k = np.array([[c * dk, r * dk] for r, c in shifts])
+    model = fpm.compile_model(optics, fpm.Illumination(fpm.KVectorList(k)), (n, n), (48, 48))
+    assert np.all(model.subpixel_offsets == 0.0)
+    omodel = oracle.compile_model(W.OPTICS, k[:, 0], k[:, 1], (n, n), (48, 48))
+    truth = W.smooth_random_object((48, 48), 4)
+    data = oracle.forward_stack(oracle.Problem(omodel, None), oracle.object_spectrum(truth))
+    for name, algo in (("ap", fpm.AlternatingProjection(iterations=5)), ("epry", fpm.Epry(iterations=5))):
+        result, expected = _run_both(fpm, algo, name, dict(iterations=5), model, omodel, data)
+        assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, name
+
+
+def test_deterministic_repeat(fpm):
+    """The scatter-add uses no atomics: two runs are bitwise identical."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 64, seed=2, photons=1e4)
+    problem = fpm.ReconstructionProblem(data, model)
+    a = fpm.Mpie(iterations=3, momentum_interval=5).run(problem)
+    b = fpm.Mpie(iterations=3, momentum_interval=5).run(problem)
+    assert np.array_equal(a.object, b.object)
+    assert [t[1] for t in a.trace] == [t[1] for t in b.trace]
+
+
+def test_batch_equals_alone(fpm):
+    """Tiles of several sizes in one batch give the same results as alone."""
+    problems = []
+    for n, side, seed in ((32, 3, 1), (64, 5, 2), (32, 5, 3), (128, 3, 4), (64, 3, 5)):
+        model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=seed, photons=1e4)
+        problems.append(fpm.ReconstructionProblem(data, model))
+    algo = fpm.Mpie(iterations=2, momentum_interval=4)
+    batch = fpm.run_batch(algo, problems)
+    for p, r in zip(problems, batch):
+        alone = algo.run(p)
+        assert np.array_equal(alone.object, r.object)
+
+
+def test_unsupported_and_invalid(fpm):
+    model, omodel = helpers.planar_model(fpm, 3, 48)
+    data = np.ones((model.frame_count, 48, 48))
+    with pytest.raises(fpm.UnsupportedError):
+        fpm.AlternatingProjection(iterations=1).run(fpm.ReconstructionProblem(data, model))
+    model, omodel = helpers.planar_model(fpm, 3, 32)
+    data = np.ones((model.frame_count, 32, 32))
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.AlternatingProjection(iterations=1, object_step=-1.0).run(fpm.ReconstructionProblem(data, model))
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.Mpie(iterations=1, momentum_friction=1.0).run(fpm.ReconstructionProblem(data, model))
