@@ -1,0 +1,451 @@
+"""Batched FPM tile reconstruction throughput on GB300.
+
+Workload (one rank): independent field-of-view tiles, each a 15 x 15 planar
+LED array (4 mm pitch, z = -90 mm; 532 nm, NA 0.10, 4x, 6.5 um pixels) with a
+square detector of N in {32, 64, 128, 256} drawn uniformly (seed 3), a
+smoothed random object per tile (per-tile seed), Poisson counts at 1e4
+photons at the bright-field peak, reconstructed by mPIE (reference defaults)
+for 30 iterations. One step = one pass of the whole job: initialise, 30
+iterations, finalise, for every tile. Tiles shard across ranks with no
+collective on the data path (weak scaling: each rank runs its own tiles).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "fpm-rs_gb300"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+import workloads as W  # noqa: E402
+
+METRIC = "FPM tiles/s batched FP32 vs plain at NRMSE<=1e-4 vs FP64; p50/p99 solve latency"
+SIZES = (32, 64, 128, 256)
+LED_SIDE = 15
+PHOTONS = 1e4
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--tiles", type=int, default=1024)
+    ap.add_argument("--iterations", type=int, default=30)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
+    ap.add_argument("--cpu-sample-iterations", type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (gloo on CPU tensors; no data-path collective)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, value: float) -> float:
+        if self.world == 1:
+            return value
+        import torch
+
+        t = torch.tensor([value], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, value: float) -> float:
+        if self.world == 1:
+            return value
+        import torch
+
+        t = torch.tensor([value], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+def tile_sizes(count: int, seed: int):
+    rng = np.random.default_rng(seed)
+    return [int(x) for x in rng.choice(SIZES, size=count)]
+
+
+# ------------------------------------------------------------------ ours
+
+def build_models(fpm):
+    optics = fpm.Optics(**W.OPTICS)
+    grid, ref = W.led_grid(LED_SIDE)
+    geometry = fpm.PlanarLEDArray(grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))
+    return {n: fpm.compile_model(optics, fpm.Illumination(geometry), (n, n)) for n in SIZES}
+
+
+def generate_tiles(fpm, models, sizes, seed_base):
+    """Host float64 Poisson count stacks per tile (forward model on the GPU, noise via torch)."""
+    import torch
+
+    gen = torch.Generator(device="cuda")
+    tiles = []
+    for i, n in enumerate(sizes):
+        model = models[n]
+        obj = W.smooth_random_object(model.reconstruction_shape, seed_base + i)
+        intensity = fpm.forward_intensities(model, obj)
+        scale = PHOTONS / float(intensity.max())
+        gen.manual_seed(seed_base + i)
+        rate = torch.from_numpy(intensity).to("cuda").mul_(scale).clamp_(min=0.0)
+        counts = torch.poisson(rate, generator=gen).cpu().numpy()
+        tiles.append((n, counts, scale, None))
+    return tiles
+
+
+class ClockSampler:
+    """nvidia-smi SM clock and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as handle:
+            data = json.load(handle)
+        return float(data["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(sizes, iterations, sample_tiles, sample_iterations, seed_base):
+    """Times the FP64 oracle on a bounded sample of the workload with all host cores."""
+    import oracle
+
+    oracle.build()
+    per_size = max(1, sample_tiles // len(SIZES))
+    problems = []
+    for n in SIZES:
+        for k in range(per_size):
+            grid, ref = W.led_grid(LED_SIDE)
+            kx, ky = oracle.planar_kvectors(W.OPTICS, grid, W.PITCH, ref, (0.0, 0.0, W.Z))
+            model = oracle.compile_model(W.OPTICS, kx, ky, (n, n))
+            obj = W.smooth_random_object((model["mh"], model["mw"]), seed_base + 100000 + 10 * n + k)
+            intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(obj),
+                                             workers=os.cpu_count() or 1)
+            counts, scale = W.poisson_counts(intensity, PHOTONS, seed_base + k)
+            problems.append(oracle.Problem(model, counts, gains=np.full(len(kx), scale)))
+    cores = os.cpu_count() or 1
+    from concurrent.futures import ThreadPoolExecutor
+
+    def timed(problem):
+        t = time.perf_counter()
+        oracle.run(problem, "mpie", iterations=sample_iterations)
+        return time.perf_counter() - t
+
+    start = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as pool:
+        per_tile = list(pool.map(timed, problems))
+    elapsed = time.perf_counter() - start
+    # One tile per thread and core; tiles are independent, so the host's
+    # throughput is cores / (mean single-tile time). The sample has equal
+    # tile counts per size (the workload's uniform mix); single-tile time is
+    # extrapolated linearly from the sampled iterations to the full count.
+    mean_tile_s = statistics.mean(per_tile) * (iterations / sample_iterations)
+    tiles_per_s = cores / mean_tile_s
+    sample = (f"{len(problems)} tiles ({per_size} per N in {list(SIZES)}), {sample_iterations} of {iterations} mPIE "
+              f"iterations each, FP64 oracle, one tile per thread on {cores} threads; tiles/s = cores / mean "
+              f"single-tile time extrapolated to {iterations} iterations ({sum(per_tile):.1f} CPU-s measured)")
+    return {"value": tiles_per_s, "unit": "tiles/s", "cores": cores, "kind": "port", "sample": sample,
+            "seconds": elapsed}
+
+
+def run_ours(args):
+    dist = Dist()
+    os.environ.setdefault("FPM_DEVICE", str(dist.local))
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    import fpm_rs as fpm
+    import oracle
+
+    models = build_models(fpm)
+    sizes = tile_sizes(args.tiles, args.seed)
+    seed_base = 1_000_000 * dist.rank + 10_000
+    t0 = time.perf_counter()
+    tiles = generate_tiles(fpm, models, sizes, seed_base)
+    # Host inputs as a user holds them: one MeasurementStack and model per tile.
+    host = [(fpm.MeasurementStack(counts), models[n]._replace(frame_gains=np.full(models[n].frame_count, s)))
+            for n, counts, s, _ in tiles]
+    problems = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
+    for p in problems:
+        p.device_handle()
+    setup_s = time.perf_counter() - t0
+    algo = fpm.Mpie(iterations=args.iterations)
+
+    # value: device-resident inputs, results left on the device.
+    for _ in range(args.warmup):
+        fpm.run_batch(algo, problems, download=False)
+    clocks = ClockSampler(dist.local)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks.start()
+    device_ms = 0.0
+    launches = 0
+    engine_bytes = engine_span = engine_sum = 0.0
+    engine_launches = 0
+    latencies = []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        fpm.run_batch(algo, problems, download=False)
+        st = fpm.last_run_stats()
+        device_ms += st["run_ms"]
+        launches += st["kernel_launches"]
+        engine_bytes += st["engine_bytes"]
+        engine_span += st["engine_span_ms"]
+        engine_sum += st["engine_ms_sum"]
+        engine_launches += st["engine_launches"]
+        for n, count, end_ms in st["buckets"]:
+            latencies += [end_ms] * count
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    dist.barrier()
+    clock_info = clocks.stop()
+    step_ms = dist.max(device_ms / args.steps)
+    total_tiles = dist.sum(len(problems))
+    value = total_tiles / (step_ms / 1e3)
+
+    # e2e: host float64 inputs uploaded and complex128 results downloaded every
+    # step, counted from what the library copies: measurements (8 B/pixel),
+    # support, FP64 and FP32 pupils and frame constants in; FP64 object, FP32
+    # spectrum, FP32 pupil, objective partials and status out.
+    h2d = d2h = 0
+    for stack, model in host:
+        h, w = model.image_shape
+        mh, mw = model.reconstruction_shape
+        ms = mw + (mw & 1)
+        h2d += stack._data.nbytes + h * w * (1 + 16 + 8) + 48 * model.frame_count
+        d2h += mh * mw * 16 + mh * ms * 8 + h * w * 8 + 8 * args.iterations * (h // 32) + 4
+    for p in problems:
+        p.release()
+    problems = None
+
+    def e2e_step():
+        fresh = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
+        out = fpm.run_batch(algo, fresh)
+        for p in fresh:
+            p.release()
+        return out
+
+    e2e_step()
+    torch.cuda.synchronize()
+    dist.barrier()
+    e0 = time.perf_counter()
+    e2e_steps = max(1, args.steps)
+    for _ in range(e2e_steps):
+        results = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = dist.max((time.perf_counter() - e0) / e2e_steps)
+    e2e_value = total_tiles / e2e_s
+
+    # Parity spot check: smallest tiles against the FP64 oracle.
+    nrmse = []
+    checked = [i for i, n in enumerate(sizes) if n == 32][:2]
+    for i in checked:
+        n, _, s, _ = tiles[i]
+        counts = host[i][0]._data
+        m = models[n]
+        om = oracle.compile_model(W.OPTICS, m.k_vectors[:, 0], m.k_vectors[:, 1], (n, n))
+        exp = oracle.run(oracle.Problem(om, counts, gains=np.full(m.frame_count, s)), "mpie",
+                         iterations=args.iterations)
+        nrmse.append(oracle.complex_nrmse(exp["object"], results[i].object))
+
+    # Plain single-tile form: one 256 x 256 tile alone.
+    plain_i = sizes.index(256) if 256 in sizes else 0
+    single = fpm.ReconstructionProblem(*host[plain_i])
+    fpm.run_batch(algo, [single], download=False)
+    fpm.run_batch(algo, [single], download=False)
+    plain_ms = fpm.last_run_stats()["run_ms"]
+
+    peak, peak_kind = peaks()
+    achieved = (engine_bytes / args.steps) / (engine_span / args.steps / 1e3) / 1e9 if engine_span > 0 else None
+    baseline = None
+    if dist.rank == 0 and dist.world >= 1:
+        baseline = cpu_baseline(sizes, args.iterations, args.cpu_sample_tiles, args.cpu_sample_iterations,
+                                seed_base)
+    if dist.rank != 0:
+        return
+    lat = sorted(latencies)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "tiles/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64",
+        "data": "synthetic (seeded objects, GPU forward model, Poisson counts)",
+        "config": {
+            "workload": (f"{args.tiles} independent FOV tiles per GPU, N~U{{32,64,128,256}} (seed {args.seed}), "
+                         f"15x15 LEDs (225 frames), mPIE {args.iterations} iterations, Poisson {PHOTONS:g} photons"),
+            "tiles_per_gpu": args.tiles,
+            "tile_sizes": {str(k): sizes.count(k) for k in SIZES},
+            "iterations": args.iterations,
+            "algorithm": "Mpie(defaults)",
+            "l2": "inputs larger than L2: float32 measurement stacks total "
+                  f"{sum(225 * n * n * 4 for n in sizes) / 1e9:.1f} GB per GPU vs 129 MB L2",
+            "timing": "device span of each batch from CUDA events on the library's streams",
+            "setup_s": round(setup_s, 1),
+        },
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak if achieved else None,
+            "traffic": None,
+            "kernel": "engine_kernel (all tile sizes, concurrent streams): algorithmic bytes / engine span",
+            "peak_kind": peak_kind,
+            "engine_launches_per_step": engine_launches // max(1, args.steps),
+            "engine_ms_sum_per_step": engine_sum / args.steps,
+            "engine_span_ms_per_step": engine_span / args.steps,
+            "algorithmic_bytes_per_step": engine_bytes / args.steps,
+        },
+        "cpu_baseline": baseline,
+        "e2e": {"value": e2e_value, "unit": "tiles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "seconds_per_step": e2e_s},
+        "gpu_launches": launches // max(1, args.steps),
+        "clocks": clock_info,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                       "definition": "batch start to the tile's results ready on the device"},
+        "nrmse_vs_fp64": {"tiles_checked": len(nrmse), "max": max(nrmse) if nrmse else None, "threshold": 1e-4},
+        "plain_single_tile": {"tiles_per_s": 1e3 / plain_ms, "ms": plain_ms, "tile": "256x256, 225 frames"},
+        "wall_s_per_step": wall / args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    sizes = tile_sizes(args.tiles, args.seed)
+    values = []
+    last = None
+    for step in range(args.warmup + args.steps):
+        last = cpu_baseline(sizes, args.iterations, args.cpu_sample_tiles, args.cpu_sample_iterations, 10_000)
+        if step >= args.warmup:
+            values.append(last["value"])
+    value = statistics.mean(values)
+    cb = dict(last)
+    cb["value"] = value
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "tiles/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": last["seconds"] * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex128",
+        "data": "synthetic (seeded objects, FP64 forward model, Poisson counts)",
+        "config": {
+            "workload": (f"{args.tiles} independent FOV tiles, N~U{{32,64,128,256}} (seed {args.seed}), "
+                         f"15x15 LEDs (225 frames), mPIE {args.iterations} iterations, Poisson {PHOTONS:g} photons"),
+            "implementation": "FP64 C restatement of the reference (the reference is Rust; cargo is absent)",
+        },
+        "cpu_baseline": cb,
+        "e2e": {"value": value, "unit": "tiles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

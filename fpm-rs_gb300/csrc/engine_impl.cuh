@@ -1,0 +1,841 @@
+// Frame engine: the per-frame FPM update of src/algorithms/common.rs:57-306
+// (AP / FPIE / mPIE / EPRY) and src/algorithms/gradient_descent.rs:405-671
+// (batch-1 Wirtinger gradient) for many independent tiles in one launch.
+//
+// One thread-block cluster owns one tile for the whole launch and walks its
+// frames in the reference's exact sequential order. A cluster has C = N/32
+// CTAs; CTA c holds 32 rows of the N x N detector field in shared memory:
+// the centred patch rows [32c, 32c + 32), which are natural rows of block
+// c ^ (C/2) because fftshift moves whole 32-row blocks when C >= 2. Per frame:
+//
+//   S0  stage the bilinear stencil of the object spectrum (33 x (N+1)) in smem
+//   P1  gather patch * pupil (ifftshifted), row IFFT step A (radix NA)
+//   P2  row IFFT step C (radix NB)                     -> cluster barrier
+//   P3  column IFFT across the cluster (radix C, DSMEM)-> cluster barrier
+//   P4  column IFFT (radix 32, registers), |psi|^2, projection or descent
+//       factor, column FFT (radix 32)                  -> cluster barrier
+//   P5  column FFT across the cluster (radix C, DSMEM) -> cluster barrier
+//   P6  row FFT step C'                                -> block barrier
+//   P7  row FFT step A', fftshift, correction U, EPRY pupil update
+//   P8  exact bilinear adjoint of U added into the object (src/model/crop.rs:188-255)
+//
+// The IFFT leaves its output in digit-permuted order and the FFT consumes that
+// order, so no bit-reversal or transpose pass exists. HBM traffic per frame is
+// the stencil read and write plus the measurement frame; the field never
+// leaves the cluster. Complex arithmetic is FP32; loss sums are FP64.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "fpm_common.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace fpm {
+
+template <int N_>
+struct Cfg {
+    static constexpr int N = N_;
+    static constexpr int R = 32;            // field rows per CTA
+    static constexpr int C = N / R;         // CTAs per cluster
+    static constexpr int NA = N >= 128 ? 16 : 8;
+    static constexpr int NB = N / NA;
+    // Padded field row stride (float2): one pad after each group of NB,
+    // stride chosen so that half-warps spanning two rows hit disjoint banks.
+    static constexpr int RS = N == 32 ? 40 : N == 64 ? 72 : N == 128 ? 152 : 272;
+    static constexpr int ORS = N + 2;       // staged stencil row: N + 2 columns from an even origin
+    static constexpr int THREADS = N;       // one thread per column position in P4
+    static constexpr int WARPS = THREADS / 32;
+    static constexpr int TW = 256 / N;      // w_N^k = w_256^(k * TW)
+    static constexpr int FIELD = (R + 1) * RS;  // raw row 0: halo U row from the previous CTA
+    static constexpr int STAGE = (R + 1) * ORS;
+    static constexpr int PSLAB = R * N;     // this CTA's 32 centred pupil rows
+    static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + 64 * 8 + 64 * 4;
+    static constexpr int T1 = R * NB / THREADS;      // P1 / P7 tasks per thread
+    static constexpr int T2 = R * NA / THREADS;      // P2 / P6 tasks per thread
+    static constexpr int TX = (R / C) * N / THREADS; // P3 / P5 tasks per thread
+    static constexpr int PAIRS = N / 2 + 1;          // 16-byte pairs per staged row
+    static_assert(N == 32 || N == 64 || N == 128 || N == 256, "unsupported tile size");
+    static_assert(RS >= N + NA && RS % 2 == 0, "row stride");
+    static_assert(T1 * THREADS == R * NB && T2 * THREADS == R * NA && TX * THREADS == (R / C) * N, "tasks");
+    static_assert(SMEM_BYTES <= 232448, "shared memory");
+};
+
+template <class K>
+FPM_DEVICE int phys(int q) { return q + q / K::NB; }
+
+// Centred patch row held by local row l of CTA c.
+template <class K>
+FPM_DEVICE int centred_row(int c, int l) {
+    if constexpr (K::C == 1) return (l + K::N / 2) & (K::N - 1);
+    else return c * K::R + l;
+}
+
+template <class K>
+FPM_DEVICE void cluster_barrier() {
+    if constexpr (K::C == 1) {
+        __syncthreads();
+    } else {
+        cg::this_cluster().sync();
+    }
+}
+
+// Bilinear sample at centred (il, j) of the staged stencil; `s` already
+// includes the odd-origin offset of the staged rows.
+FPM_DEVICE float2 patch_at(const float2* __restrict__ s, int ors, int il, int j, const FrameParam& fp) {
+    const float2* r0 = s + il * ors + j;
+    const float2* r1 = r0 + ors;
+    float2 p = cscale(r0[0], fp.w00);
+    p = cfma(fp.w01, r0[1], p);
+    p = cfma(fp.w10, r1[0], p);
+    p = cfma(fp.w11, r1[1], p);
+    return p;
+}
+
+// point_loss (src/algorithms/objective.rs:47-71) in FP32. LOSS >= 0 fixes
+// the loss at compile time; LOSS < 0 reads `loss` at run time.
+template <int LOSS>
+FPM_DEVICE float point_loss(float predicted, float measured, int runtime_loss) {
+    switch (LOSS >= 0 ? LOSS : runtime_loss) {
+        case 0: {
+            float r = sqrtf(fmaxf(predicted, 0.f)) - sqrtf(fmaxf(measured, 0.f));
+            return r * r;
+        }
+        case 1: {
+            float r = predicted - measured;
+            return r * r;
+        }
+        case 2: {
+            float mean = fmaxf(predicted, 1e-12f);
+            return mean - fmaxf(measured, 0.f) * logf(mean);
+        }
+        default: {
+            float r = sqrtf(fmaxf(predicted, 0.f)) - sqrtf(fmaxf(measured, 0.f));
+            float a = fabsf(r);
+            return a <= 1.f ? 0.5f * r * r : a - 0.5f;
+        }
+    }
+}
+
+// descent_factor (src/algorithms/gradient_descent.rs:1167-1178) in FP32.
+template <int LOSS>
+FPM_DEVICE float descent_factor(float predicted, float measured, int runtime_loss, float eps) {
+    switch (LOSS >= 0 ? LOSS : runtime_loss) {
+        case 0:
+            return 1.f - sqrtf(fmaxf(measured, 0.f)) * rsqrtf(fmaxf(predicted, eps));
+        case 1:
+            return 2.f * (predicted - measured);
+        case 2:
+            return 1.f - fmaxf(measured, 0.f) / fmaxf(predicted, eps);
+        default: {
+            float pa = sqrtf(fmaxf(predicted, eps));
+            float r = fminf(fmaxf(pa - sqrtf(fmaxf(measured, 0.f)), -1.f), 1.f);
+            return r / (2.f * pa);
+        }
+    }
+}
+
+// S0: asynchronous copy of the stencil rows [i_lo, i_lo + 32] x columns
+// [lower_col - odd, lower_col - odd + N + 2) into shared memory. Every copy
+// starts on an even column (16-byte aligned: the object row stride is even);
+// bytes beyond the grid are zero-filled and never read from global memory.
+template <class K>
+FPM_DEVICE void stage_object(float2* __restrict__ osm, const float2* __restrict__ object, int M, long long ostride,
+                             const FrameParam& fp, int i_lo) {
+    const int c0 = fp.lower_col & ~1;
+    for (int e = threadIdx.x; e < (K::R + 1) * K::PAIRS; e += K::THREADS) {
+        const int r = e / K::PAIRS, t = e - r * K::PAIRS;
+        const int gr = fp.lower_row + i_lo + r;
+        const int col = c0 + 2 * t;
+        int bytes = 0;
+        if (gr < M) bytes = M - col >= 2 ? 16 : (M - col == 1 ? 8 : 0);
+        const float2* src = bytes ? object + (long long)gr * ostride + col : object;
+        cp_async16(osm + r * K::ORS + 2 * t, src, bytes);
+    }
+    cp_async_wait_all();
+}
+
+// P1 + P2: patch * pupil, ifftshift, row inverse FFT into the field slab.
+// Tracks maxima of |patch|^2 and |P|^2 for EPRY.
+template <class K, bool TRACK_MAX>
+FPM_DEVICE void rows_inverse(float2* __restrict__ fld, const float2* __restrict__ ostage, const float2* __restrict__ tw,
+                             const float2* __restrict__ pslab, const FrameParam& fp, int c, int i_lo, float& max_obj,
+                             float& max_pup) {
+    constexpr int N = K::N, NA = K::NA, NB = K::NB;
+#pragma unroll 1
+    for (int t = 0; t < K::T1; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int l = task / NB, nb = task % NB;
+        const int il = centred_row<K>(c, l) - i_lo;
+        float2 v[NA];
+#pragma unroll
+        for (int na = 0; na < NA; ++na) {
+            const int j = (NB * na + nb + N / 2) & (N - 1);
+            const float2 pt = patch_at(ostage, K::ORS, il, j, fp);
+            const float2 pv = pslab[il * N + j];
+            if (TRACK_MAX) {
+                max_obj = fmaxf(max_obj, cnorm2(pt));
+                max_pup = fmaxf(max_pup, cnorm2(pv));
+            }
+            v[na] = cmul(pt, pv);
+        }
+        dft_reg<NA, true>(v);
+        float2* row = fld + l * K::RS;
+#pragma unroll
+        for (int ka = 0; ka < NA; ++ka) row[phys<K>(NB * ka + nb)] = twiddle_smem<true>(v[ka], tw, nb * ka * K::TW);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int t = 0; t < K::T2; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int l = task / NA, ka = task % NA;
+        float2* g = fld + l * K::RS + ka * (NB + 1);
+        float2 v[NB];
+#pragma unroll
+        for (int kb = 0; kb < NB; ++kb) v[kb] = g[kb];
+        dft_reg<NB, true>(v);
+#pragma unroll
+        for (int kb = 0; kb < NB; ++kb) g[kb] = v[kb];
+    }
+}
+
+// P3: radix-C column step across the cluster (inverse direction): per task,
+// C remote loads, one radix-C DFT, C remote stores.
+template <class K>
+FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __restrict__ tw, int c) {
+    if constexpr (K::C > 1) {
+        constexpr int C = K::C, N = K::N, ROWS = K::R / C;
+        cg::cluster_group cluster = cg::this_cluster();
+        float2* peer[C];
+#pragma unroll
+        for (int r = 0; r < C; ++r) peer[r] = cluster.map_shared_rank(fld, r);
+#pragma unroll 1
+        for (int t = 0; t < K::TX; ++t) {
+            const int task = threadIdx.x + t * K::THREADS;
+            const int l = c * ROWS + task / N;
+            const int off = l * K::RS + phys<K>(task % N);
+            float2 v[C];
+#pragma unroll
+            for (int nc = 0; nc < C; ++nc) v[nc] = peer[nc ^ (C / 2)][off];
+            dft_reg<C, true>(v);
+#pragma unroll
+            for (int k1 = 0; k1 < C; ++k1) peer[k1][off] = twiddle_smem<true>(v[k1], tw, l * k1 * K::TW);
+        }
+    }
+}
+
+// P5: radix-C column step across the cluster (forward direction); output
+// block j1 goes to the CTA holding natural rows of block j1.
+template <class K>
+FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c) {
+    if constexpr (K::C > 1) {
+        constexpr int C = K::C, N = K::N, ROWS = K::R / C;
+        cg::cluster_group cluster = cg::this_cluster();
+        float2* peer[C];
+#pragma unroll
+        for (int r = 0; r < C; ++r) peer[r] = cluster.map_shared_rank(fld, r);
+#pragma unroll 1
+        for (int t = 0; t < K::TX; ++t) {
+            const int task = threadIdx.x + t * K::THREADS;
+            const int off = (c * ROWS + task / N) * K::RS + phys<K>(task % N);
+            float2 v[C];
+#pragma unroll
+            for (int k1 = 0; k1 < C; ++k1) v[k1] = peer[k1][off];
+            dft_reg<C, false>(v);
+#pragma unroll
+            for (int j1 = 0; j1 < C; ++j1) peer[j1 ^ (C / 2)][off] = v[j1];
+        }
+    }
+}
+
+template <class K>
+FPM_DEVICE void load_pupil_slab(float2* __restrict__ pslab, const float2* __restrict__ pupil, int c) {
+    for (int e = threadIdx.x; e < K::R * K::N; e += K::THREADS) {
+        const int l = e / K::N, j = e % K::N;
+        const int i = K::C == 1 ? l : c * K::R + l;
+        pslab[e] = __ldcg(pupil + i * K::N + j);
+    }
+}
+
+template <int N_, int ALG, int LOSS>
+__global__ void __launch_bounds__(Cfg<N_>::THREADS) engine_kernel(const EngineParams P) {
+    using K = Cfg<N_>;
+    constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* field = reinterpret_cast<float2*>(smem_raw);
+    float2* fld = field + K::RS;  // FFT rows 0..31; raw row 0 is the U halo
+    float2* osm = field + K::FIELD;
+    float2* pslab = osm + K::STAGE;
+    float2* tw = pslab + K::PSLAB;
+    double* dred = reinterpret_cast<double*>(tw + 256);
+    float* fred = reinterpret_cast<float*>(dred + 64);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile = blockIdx.x / C;
+    const int c = C == 1 ? 0 : (int)(blockIdx.x % C);
+    // Tile and frame descriptors live in shared memory, not registers.
+    __shared__ TileDesc s_tile;
+    __shared__ FrameParam s_frame;
+    if (tid == 0) s_tile = P.tiles[tile];
+    for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
+    __syncthreads();
+    const TileDesc& T = s_tile;
+    const int M = T.M;
+    const long long ostride = M + (M & 1);
+    const int i_lo = C == 1 ? 0 : c * R;
+    constexpr bool projection = ALG != kAlgGradient;
+    constexpr bool epry = ALG == kAlgEpry;
+
+    load_pupil_slab<K>(pslab, T.pupil, c);
+    int counter = P.momentum ? *T.counter : 0;
+    double loss_acc = 0.0;
+    __syncthreads();
+
+    for (int it = P.it_begin; it < P.it_end; ++it) {
+        for (int idx = 0; idx < T.frame_count; ++idx) {
+            const int f = T.order ? T.order[idx] : idx;
+            if (tid == 0) s_frame = T.params[f];
+            __syncthreads();
+            const FrameParam& fp = s_frame;
+            if (fp.weight == 0.0f) {
+                __syncthreads();
+                continue;
+            }
+
+            // S0
+            stage_object<K>(osm, T.object, M, ostride, fp, i_lo);
+            __syncthreads();
+            const float2* ostage = osm + (fp.lower_col & 1);
+
+            // P1, P2
+            float max_obj = 0.f, max_pup = 0.f;
+            rows_inverse<K, epry>(fld, ostage, tw, pslab, fp, c, i_lo, max_obj, max_pup);
+            if constexpr (epry) {
+                max_obj = warp_max(max_obj);
+                max_pup = warp_max(max_pup);
+                if (lane == 0) {
+                    fred[warp] = max_obj;
+                    fred[K::WARPS + warp] = max_pup;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    float a = 0.f, b = 0.f;
+                    for (int w = 0; w < K::WARPS; ++w) {
+                        a = fmaxf(a, fred[w]);
+                        b = fmaxf(b, fred[K::WARPS + w]);
+                    }
+                    fred[2 * K::WARPS] = a;
+                    fred[2 * K::WARPS + 1] = b;
+                }
+            }
+            cluster_barrier<K>();
+
+            float frame_max_obj = 0.f, frame_max_pup = 0.f;
+            if constexpr (epry) {
+                if constexpr (C == 1) {
+                    frame_max_obj = fred[2 * K::WARPS];
+                    frame_max_pup = fred[2 * K::WARPS + 1];
+                } else {
+                    cg::cluster_group cluster = cg::this_cluster();
+#pragma unroll
+                    for (int r = 0; r < C; ++r) {
+                        const float* pf = cluster.map_shared_rank(fred, r);
+                        frame_max_obj = fmaxf(frame_max_obj, pf[2 * K::WARPS]);
+                        frame_max_pup = fmaxf(frame_max_pup, pf[2 * K::WARPS + 1]);
+                    }
+                }
+            }
+
+            // P3, then the measurement prefetch for P4 (issued before the
+            // barrier so its latency overlaps the wait).
+            if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c);
+            // Thread tid owns column position q = tid in P4.
+            float mreg[32];
+            unsigned mbits = 0xffffffffu;
+            {
+                const size_t off = (size_t)f * N * N + (size_t)c * 32 * N + tid;
+#pragma unroll
+                for (int k2 = 0; k2 < 32; ++k2) mreg[k2] = __ldcs(T.meas + off + (size_t)k2 * N);
+                if (T.masks) {
+                    mbits = 0u;
+#pragma unroll
+                    for (int k2 = 0; k2 < 32; ++k2) mbits |= (T.masks[off + (size_t)k2 * N] != 0 ? 1u : 0u) << k2;
+                }
+            }
+
+            if constexpr (C > 1) cluster_barrier<K>();
+
+            // P4: column inverse FFT, projection, column forward FFT.
+            {
+                const float* brow =
+                    T.background ? T.background + (size_t)f * T.background_stride + (size_t)c * 32 * N + tid : nullptr;
+                const float gain = fp.gain, inv_gain = 1.0f / fp.gain;
+                float2 v[32];
+                const int pq = phys<K>(tid);
+#pragma unroll
+                for (int l = 0; l < 32; ++l) v[l] = fld[l * K::RS + pq];
+                dft_reg<32, true>(v);
+                float frame_loss = 0.f;
+#pragma unroll
+                for (int k2 = 0; k2 < 32; ++k2) {
+                    const float meas = mreg[k2];
+                    const bool masked = ((mbits >> k2) & 1u) == 0u;
+                    const float bg = brow ? __ldg(brow + k2 * N) : 0.f;
+                    const float intrinsic = cnorm2(v[k2]);
+                    const float target = fmaxf((meas - bg) * inv_gain, 0.f);
+                    if constexpr (projection) {
+                        if (!masked) {
+                            frame_loss += point_loss<LOSS>(fmaf(gain, intrinsic, bg), meas, P.loss);
+                            v[k2] = intrinsic > P.eps ? cscale(v[k2], sqrtf(target) * rsqrtf(intrinsic))
+                                                      : make_float2(sqrtf(target), 0.f);
+                        }
+                    } else {
+                        if (masked) {
+                            v[k2] = make_float2(0.f, 0.f);
+                        } else {
+                            frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
+                            v[k2] = cscale(v[k2], descent_factor<LOSS>(intrinsic, target, P.loss, P.eps));
+                        }
+                    }
+                }
+                dft_reg<32, false>(v);
+#pragma unroll
+                for (int j2 = 0; j2 < 32; ++j2)
+                    fld[j2 * K::RS + pq] = C > 1 ? twiddle_smem<false>(v[j2], tw, c * j2 * K::TW) : v[j2];
+                loss_acc += (double)frame_loss * fp.loss_scale;
+            }
+            cluster_barrier<K>();
+
+            // P5
+            if constexpr (C > 1) {
+                columns_cross_forward<K>(fld, c);
+                cluster_barrier<K>();
+            }
+
+            // P6: row FFT step C' with twiddles.
+#pragma unroll 1
+            for (int t = 0; t < K::T2; ++t) {
+                const int task = tid + t * K::THREADS;
+                const int l = task / NA, ka = task % NA;
+                float2* g = fld + l * K::RS + ka * (NB + 1);
+                float2 v[NB];
+#pragma unroll
+                for (int kb = 0; kb < NB; ++kb) v[kb] = g[kb];
+                dft_reg<NB, false>(v);
+#pragma unroll
+                for (int jb = 0; jb < NB; ++jb) g[jb] = twiddle_smem<false>(v[jb], tw, ka * jb * K::TW);
+            }
+            __syncthreads();
+
+            // P7: row FFT step A', fftshift, correction U (+ EPRY pupil update).
+            {
+                float2 ureg[K::T1][NA];
+                const float inv_n2 = 1.0f / (float)(N * N);
+                const float max_p2 = epry ? fmaxf(frame_max_pup, P.eps) : T.max_pupil_power;
+                const float inv_global = 1.0f / (max_p2 + P.eps);
+                const float pupil_scale =
+                    epry ? fp.weight * P.pupil_step / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
+#pragma unroll
+                for (int t = 0; t < K::T1; ++t) {
+                    const int task = tid + t * K::THREADS;
+                    const int l = task / NB, jb = task % NB;
+                    float2 v[NA];
+#pragma unroll
+                    for (int ka = 0; ka < NA; ++ka) v[ka] = fld[l * K::RS + phys<K>(NB * ka + jb)];
+                    dft_reg<NA, false>(v);
+                    const int i = centred_row<K>(c, l);
+                    const int il = i - i_lo;
+#pragma unroll
+                    for (int ja = 0; ja < NA; ++ja) {
+                        const int j = (NB * ja + jb + N / 2) & (N - 1);
+                        const float2 psi = cscale(v[ja], inv_n2);
+                        const float2 pt = patch_at(ostage, K::ORS, il, j, fp);
+                        float2* pp = pslab + il * N + j;
+                        const float2 pv = *pp;
+                        float2 u;
+                        if constexpr (projection) {
+                            const float2 d = csub(psi, cmul(pt, pv));
+                            const float pw = cnorm2(pv);
+                            float inv_den;
+                            if constexpr (ALG == kAlgLocal)
+                                inv_den = 1.0f / (pw + P.eps);
+                            else if constexpr (ALG == kAlgRpie)
+                                inv_den = 1.0f / ((1.f - P.alpha) * pw + P.alpha * max_p2 + P.eps);
+                            else
+                                inv_den = inv_global;
+                            u = cscale(cmulc(d, pv), inv_den);
+                            if constexpr (epry) {
+                                float2 np = cfma(pupil_scale, cmulc(d, pt), pv);
+                                if (P.constrain_pupil && T.support[i * N + j] == 0) np = make_float2(0.f, 0.f);
+                                *pp = np;
+                            }
+                        } else {
+                            u = cscale(cmulc(psi, pv), inv_global);
+                        }
+                        ureg[t][ja] = u;
+                    }
+                }
+                __syncthreads();
+                float2* next_halo = nullptr;
+                if constexpr (C > 1) {
+                    if (c < C - 1) next_halo = cg::this_cluster().map_shared_rank(field, c + 1);
+                }
+#pragma unroll
+                for (int t = 0; t < K::T1; ++t) {
+                    const int task = tid + t * K::THREADS;
+                    const int l = task / NB, jb = task % NB;
+                    const int urow = centred_row<K>(c, l) - i_lo;
+#pragma unroll
+                    for (int ja = 0; ja < NA; ++ja) {
+                        const int j = (NB * ja + jb + N / 2) & (N - 1);
+                        fld[urow * K::RS + j] = ureg[t][ja];
+                        if (C > 1 && urow == R - 1 && next_halo) next_halo[j] = ureg[t][ja];
+                    }
+                }
+            }
+            cluster_barrier<K>();
+
+            // P8: exact bilinear adjoint scatter of scale * U into the object.
+            {
+                const float scale = projection ? fp.weight * P.object_step
+                                               : -P.object_step * fp.weight * fp.valid_scale;
+                const int rows8 = C == 1 ? N + fp.has_upper_row : R + (c == C - 1 ? fp.has_upper_row : 0);
+                const int cols8 = N + fp.has_upper_col;
+                constexpr int PER = (N + 1 + 31) / 32;
+                for (int r = warp; r < rows8; r += K::WARPS) {
+                    const int i = i_lo + r;
+                    const bool has0 = i < N, has1 = i >= 1;
+                    const float2* u0 = fld + r * K::RS;
+                    const float2* u1 = u0 - K::RS;  // r == 0: the halo row
+                    const float2* srow = ostage + r * K::ORS;
+                    float2* grow = T.object + (long long)(fp.lower_row + i) * ostride + fp.lower_col;
+                    float2 out[PER];
+#pragma unroll
+                    for (int t = 0; t < PER; ++t) {
+                        const int j = lane + 32 * t;
+                        const float2 z = make_float2(0.f, 0.f);
+                        const float2 a = has0 && j < N ? u0[j] : z;
+                        const float2 b = has0 && j >= 1 && j <= N ? u0[j - 1] : z;
+                        const float2 d0 = has1 && j < N ? u1[j] : z;
+                        const float2 d1 = has1 && j >= 1 && j <= N ? u1[j - 1] : z;
+                        float2 acc = cscale(a, fp.w00);
+                        acc = cfma(fp.w01, b, acc);
+                        acc = cfma(fp.w10, d0, acc);
+                        acc = cfma(fp.w11, d1, acc);
+                        out[t] = j < cols8 ? cfma(scale, acc, srow[j]) : z;
+                    }
+#pragma unroll
+                    for (int t = 0; t < PER; ++t) {
+                        const int j = lane + 32 * t;
+                        if (j < cols8) __stcg(grow + j, out[t]);
+                    }
+                }
+            }
+            cluster_barrier<K>();
+
+            // mPIE momentum event (src/algorithms/common.rs:308-387).
+            if (P.momentum) {
+                counter += 1;
+                if (counter >= P.interval) {
+                    counter = 0;
+                    const long long total = (long long)M * ostride / 2;  // float4 = two complex values
+                    const long long per = (total + C - 1) / C;
+                    const long long begin = c * per;
+                    const long long end = begin + per < total ? begin + per : total;
+                    float4* O4 = reinterpret_cast<float4*>(T.object);
+                    float4* V4 = reinterpret_cast<float4*>(T.velocity);
+                    float4* A4 = reinterpret_cast<float4*>(T.anchor);
+                    bool bad = false;
+                    constexpr int U = 4;
+                    for (long long e0 = begin + tid; e0 < end; e0 += (long long)K::THREADS * U) {
+                        float4 o[U], v[U], a[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const long long e = e0 + (long long)u * K::THREADS;
+                            if (e < end) {
+                                o[u] = __ldcg(O4 + e);
+                                v[u] = __ldcg(V4 + e);
+                                a[u] = __ldcg(A4 + e);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const long long e = e0 + (long long)u * K::THREADS;
+                            if (e < end) {
+                                float4 nv, no;
+                                nv.x = fmaf(P.friction, v[u].x, o[u].x - a[u].x);
+                                nv.y = fmaf(P.friction, v[u].y, o[u].y - a[u].y);
+                                nv.z = fmaf(P.friction, v[u].z, o[u].z - a[u].z);
+                                nv.w = fmaf(P.friction, v[u].w, o[u].w - a[u].w);
+                                if (P.feedback == 0.f) {
+                                    no = o[u];
+                                } else {
+                                    no.x = fmaf(P.feedback, nv.x, o[u].x);
+                                    no.y = fmaf(P.feedback, nv.y, o[u].y);
+                                    no.z = fmaf(P.feedback, nv.z, o[u].z);
+                                    no.w = fmaf(P.feedback, nv.w, o[u].w);
+                                }
+                                bad |= !isfinite(nv.x) || !isfinite(nv.y) || !isfinite(nv.z) || !isfinite(nv.w) ||
+                                       !isfinite(no.x) || !isfinite(no.y) || !isfinite(no.z) || !isfinite(no.w);
+                                __stcg(V4 + e, nv);
+                                __stcg(O4 + e, no);
+                                __stcg(A4 + e, no);
+                            }
+                        }
+                    }
+                    if (bad) atomicOr(T.status, 1);
+                    cluster_barrier<K>();
+                }
+            }
+        }
+        // Objective partial for this iteration and CTA (deterministic order).
+        double s = warp_sum(loss_acc);
+        loss_acc = 0.0;
+        if (lane == 0) dred[warp] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double total = 0.0;
+            for (int w = 0; w < K::WARPS; ++w) total += dred[w];
+            T.partials[(size_t)it * C + c] = total;
+        }
+        __syncthreads();
+    }
+    if constexpr (epry) {
+        for (int e = tid; e < R * N; e += K::THREADS) {
+            const int l = e / N, j = e % N;
+            const int i = C == 1 ? l : c * R + l;
+            __stcg(T.pupil + i * N + j, pslab[e]);
+        }
+    }
+    if (P.momentum && c == 0 && tid == 0) *T.counter = counter;
+    // Peers must not exit while their shared memory may still be addressed.
+    cluster_barrier<K>();
+}
+
+// Forward model (simulate): cluster f computes frame f's intensity.
+template <int N_>
+__global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const ForwardParams P) {
+    using K = Cfg<N_>;
+    constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* field = reinterpret_cast<float2*>(smem_raw);
+    float2* fld = field + K::RS;
+    float2* osm = field + K::FIELD;
+    float2* pslab = osm + K::STAGE;
+    float2* tw = pslab + K::PSLAB;
+    const int tid = threadIdx.x;
+    const int f = blockIdx.x / C;
+    const int c = C == 1 ? 0 : (int)(blockIdx.x % C);
+    const int i_lo = C == 1 ? 0 : c * R;
+    const long long ostride = P.M + (P.M & 1);
+    for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
+    load_pupil_slab<K>(pslab, P.pupil, c);
+    const FrameParam fp = P.params[f];
+    stage_object<K>(osm, P.object, P.M, ostride, fp, i_lo);
+    __syncthreads();
+    float a = 0.f, b = 0.f;
+    rows_inverse<K, false>(fld, osm + (fp.lower_col & 1), tw, pslab, fp, c, i_lo, a, b);
+    cluster_barrier<K>();
+    if constexpr (C > 1) {
+        columns_cross_inverse<K>(fld, tw, c);
+        cluster_barrier<K>();
+    }
+    float* out = P.out + (size_t)f * N * N;
+    const float* bg = P.background ? P.background + (size_t)f * P.background_stride : nullptr;
+    {
+        const int q = tid;
+        float2 v[32];
+        const int pq = phys<K>(q);
+#pragma unroll
+        for (int l = 0; l < 32; ++l) v[l] = fld[l * K::RS + pq];
+        dft_reg<32, true>(v);
+        const int ka = q / NB, kb = q % NB;
+        const int x = ka + NA * kb;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2) {
+            const int y = c + C * k2;
+            const float b0 = bg ? bg[y * N + x] : 0.f;
+            out[y * N + x] = fmaf(fp.gain, cnorm2(v[k2]), b0);
+        }
+    }
+    cluster_barrier<K>();
+}
+
+// Natural (y, x) -> engine layout index within one frame.
+template <class K>
+FPM_DEVICE int perm_index(int y, int x) {
+    const int c = y % K::C, k2 = y / K::C;
+    const int ka = x % K::NA, kb = x / K::NA;
+    return (c * 32 + k2) * K::N + K::NB * ka + kb;
+}
+
+template <int N_>
+__global__ void permute_f64_kernel(const double* __restrict__ src, float* __restrict__ dst, long long frames) {
+    using K = Cfg<N_>;
+    const long long total = frames * K::N * K::N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long f = e / (K::N * K::N);
+        const int p = (int)(e % (K::N * K::N));
+        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = (float)src[e];
+    }
+}
+
+template <int N_>
+__global__ void permute_u8_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, long long frames) {
+    using K = Cfg<N_>;
+    const long long total = frames * K::N * K::N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long f = e / (K::N * K::N);
+        const int p = (int)(e % (K::N * K::N));
+        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = src[e];
+    }
+}
+
+// Weighted mean amplitude per detector pixel, nearest upsample to M x M.
+// Block b of a tile handles pixels [b * 256, b * 256 + 256); a second pass
+// resolves the fallback for pixels without any positive-weight sample.
+constexpr int kInitBlock = 256;
+
+template <int N_>
+__global__ void init_mean_kernel(const InitTile* __restrict__ tiles, double* __restrict__ avg,
+                                 double* __restrict__ partial) {
+    using K = Cfg<N_>;
+    constexpr int N = K::N;
+    const InitTile T = tiles[blockIdx.y];
+    const int chunks = gridDim.x;
+    const int p = blockIdx.x * kInitBlock + threadIdx.x;  // natural pixel
+    __shared__ double s_amp[kInitBlock / 32], s_w[kInitBlock / 32];
+    double sum = 0.0, wsum = 0.0;
+    if (p < N * N) {
+        const int idx = perm_index<K>(p / N, p % N);
+        for (int f = 0; f < T.frames_count; ++f) {
+            const FrameParam fp = T.params[f];
+            if (fp.weight == 0.0f) continue;
+            const size_t off = (size_t)f * N * N + idx;
+            if (T.masks && T.masks[off] == 0) continue;
+            const double bg = T.background ? (double)T.background[(size_t)f * T.background_stride + idx] : 0.0;
+            const double amp = sqrt(fmax(((double)T.meas[off] - bg) / (double)fp.gain, 0.0));
+            sum += (double)fp.weight * amp;
+            wsum += (double)fp.weight;
+        }
+        avg[(size_t)blockIdx.y * N * N + p] = wsum > 0.0 ? sum / wsum : -1.0;
+    }
+    double a = warp_sum(sum), b = warp_sum(wsum);
+    if ((threadIdx.x & 31) == 0) {
+        s_amp[threadIdx.x >> 5] = a;
+        s_w[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < kInitBlock / 32; ++w) {
+            ta += s_amp[w];
+            tb += s_w[w];
+        }
+        partial[((size_t)blockIdx.y * chunks + blockIdx.x) * 2] = ta;
+        partial[((size_t)blockIdx.y * chunks + blockIdx.x) * 2 + 1] = tb;
+    }
+}
+
+template <int N_>
+__global__ void init_upsample_kernel(const InitTile* __restrict__ tiles, int m, const double* __restrict__ avg,
+                                     const double* __restrict__ partial, int chunks) {
+    constexpr int N = N_;
+    const InitTile T = tiles[blockIdx.y];
+    __shared__ double s_fallback;
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int k = 0; k < chunks; ++k) {
+            ta += partial[((size_t)blockIdx.y * chunks + k) * 2];
+            tb += partial[((size_t)blockIdx.y * chunks + k) * 2 + 1];
+        }
+        s_fallback = tb > 0.0 ? ta / tb : 0.0;
+        if (!(tb > 0.0) && blockIdx.x == 0) atomicOr(T.status, 4);
+    }
+    __syncthreads();
+    const double* a = avg + (size_t)blockIdx.y * N * N;
+    const long long total = (long long)m * m;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / m), col = (int)(e % m);
+        const int lr = (int)((long long)r * N / m), lc = (int)((long long)col * N / m);
+        double v = a[lr * N + lc];
+        if (v < 0.0) v = s_fallback;
+        T.scratch[e] = make_double2(v, 0.0);
+    }
+}
+
+// ------------------------------------------------------------- launchers
+
+template <int N_, class Kern, class Params>
+cudaError_t launch_cluster(Kern kernel, const Params& p, int clusters, cudaStream_t s) {
+    using K = Cfg<N_>;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusters * K::C);
+    cfg.blockDim = dim3(K::THREADS);
+    cfg.dynamicSmemBytes = K::SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = K::C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, p);
+}
+
+// Per-size entry points; each tile size is instantiated in its own
+// translation unit (engine_n32.cu ... engine_n256.cu) so they build in parallel.
+template <int N_>
+struct EngineEntry {
+    template <int ALG>
+    static cudaError_t engine_alg(const EngineParams& p, int tiles, cudaStream_t s) {
+        if (p.loss == 0) return launch_cluster<N_>(engine_kernel<N_, ALG, 0>, p, tiles, s);
+        return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+    }
+
+    static cudaError_t engine(const EngineParams& p, int tiles, cudaStream_t s) {
+        switch (p.alg) {
+            case kAlgLocal: return engine_alg<kAlgLocal>(p, tiles, s);
+            case kAlgRpie: return engine_alg<kAlgRpie>(p, tiles, s);
+            case kAlgGlobal: return engine_alg<kAlgGlobal>(p, tiles, s);
+            case kAlgEpry: return engine_alg<kAlgEpry>(p, tiles, s);
+            case kAlgGradient: return engine_alg<kAlgGradient>(p, tiles, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+
+    static cudaError_t forward(const ForwardParams& p, cudaStream_t s) {
+        return launch_cluster<N_>(forward_kernel<N_>, p, p.frame_count, s);
+    }
+
+    static cudaError_t permute_f64(const double* src, float* dst, long long frames, cudaStream_t s) {
+        const long long total = frames * N_ * N_;
+        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
+        permute_f64_kernel<N_><<<blocks, 256, 0, s>>>(src, dst, frames);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t permute_u8(const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s) {
+        const long long total = frames * N_ * N_;
+        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
+        permute_u8_kernel<N_><<<blocks, 256, 0, s>>>(src, dst, frames);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t init(int m, const InitTile* tiles, int count, double* avg, double* partial, cudaStream_t s) {
+        const int chunks = (N_ * N_ + kInitBlock - 1) / kInitBlock;
+        init_mean_kernel<N_><<<dim3(chunks, count), kInitBlock, 0, s>>>(tiles, avg, partial);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        const long long total = (long long)m * m;
+        const int blocks = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+        init_upsample_kernel<N_><<<dim3(blocks, count), 256, 0, s>>>(tiles, m, avg, partial, chunks);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace fpm

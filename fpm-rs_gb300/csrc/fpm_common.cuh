@@ -106,3 +106,13 @@ FPM_DEVICE double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+// 16-byte asynchronous global->shared copy that reads `src_bytes` (0, 8 or
+// 16) bytes and zero-fills the rest; .cg reads through L2 only, so data
+// written by other CTAs of the cluster is never served from a stale L1 line.
+FPM_DEVICE void cp_async16(void* smem, const void* gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+
+FPM_DEVICE void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }

@@ -43,15 +43,17 @@ struct TileDesc {
     int pad;
 };
 
-enum EngineMode { kModeProjection = 0, kModeGradient = 1 };
-enum Denominator { kDenLocal = 0, kDenRpie = 1, kDenGlobal = 2 };
+// Frame-engine kernel families, fixed at compile time so each instantiation
+// carries only its own update code: AP (local |P|^2 denominator), FPIE/mPIE
+// (rPIE blend), EPRY without and with pupil recovery (global max |P|^2), and
+// the Wirtinger gradient.
+enum EngineAlg { kAlgLocal = 0, kAlgRpie = 1, kAlgGlobal = 2, kAlgEpry = 3, kAlgGradient = 4 };
 
 struct EngineParams {
     const TileDesc* tiles;
-    int mode;
-    int denominator;
+    int alg;
     float alpha, eps, object_step, pupil_step;
-    int recover_pupil, constrain_pupil;
+    int constrain_pupil;
     int momentum, interval;
     float friction, feedback;
     int loss;

@@ -17,6 +17,8 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
+#include <atomic>
 #include <vector>
 
 #include "fpm_gpu.h"
@@ -101,9 +103,7 @@ struct fpm_context {
     std::map<int, std::unique_ptr<FftPlan>> plans;
     DeviceBuffer staging;  // FP64 upload staging
     DeviceBuffer scratch_a, scratch_b;
-    int engine_launches = 0;
-    double engine_ms = 0.0;
-    double engine_bytes = 0.0;
+    fpm_run_stats stats = {};
 };
 
 struct fpm_problem {
@@ -414,15 +414,38 @@ Status validate_model(const fpm_model_desc* md) {
     return Status::ok();
 }
 
+// Runs fn(frame) for every frame on the host's hardware threads.
+template <class Fn>
+void parallel_frames(int frames, Fn fn) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int workers = std::min(hw, frames);
+    if (workers <= 1) {
+        for (int f = 0; f < frames; ++f) fn(f);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::vector<std::thread> pool;
+    for (int w = 0; w < workers; ++w)
+        pool.emplace_back([&]() {
+            for (int f; (f = next.fetch_add(1)) < frames;) fn(f);
+        });
+    for (auto& t : pool) t.join();
+}
+
 Status validate_measurements(const fpm_model_desc* md, const fpm_measurement_desc* ms) {
     if (!ms || !ms->measurements) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements are required");
     if (ms->frames != md->sources)
         return Status::make(FPM_ERR_INVALID_MODEL, "%d measurement frames but %d model frames", ms->frames, md->sources);
     const size_t n = (size_t)md->image_height * md->image_width;
-    const size_t total = n * ms->frames;
-    for (size_t i = 0; i < total; ++i)
-        if (!std::isfinite(ms->measurements[i]))
-            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
+    std::vector<uint8_t> bad(ms->frames, 0);
+    parallel_frames(ms->frames, [&](int f) {
+        const double* m = ms->measurements + (size_t)f * n;
+        bool ok = true;
+        for (size_t i = 0; i < n; ++i) ok &= std::isfinite(m[i]);
+        bad[f] = ok ? 0 : 1;
+    });
+    for (int f = 0; f < ms->frames; ++f)
+        if (bad[f]) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
     int positive = 0;
     for (int f = 0; f < ms->frames; ++f) {
         const double wgt = ms->frame_weights ? ms->frame_weights[f] : 1.0;
@@ -484,6 +507,32 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
     p->params.resize(F);
     p->stencil_cells.resize(F);
     p->data_snr.assign(F, 0.0);
+    // Per-frame unmasked counts and snr_weighted scores
+    // (src/reconstruction/schedule.rs:104-128), computed in parallel.
+    std::vector<long long> valid_counts(F, (long long)n2);
+    parallel_frames(F, [&](int f) {
+        if (ms->masks) {
+            long long valid = 0;
+            const uint8_t* mk = ms->masks + (size_t)f * n2;
+            for (size_t i = 0; i < n2; ++i) valid += mk[i] != 0;
+            valid_counts[f] = valid;
+        }
+        if (p->weights[f] == 0.0) {
+            p->data_snr[f] = -INFINITY;
+            return;
+        }
+        const double* m = ms->measurements + (size_t)f * n2;
+        double sum = 0.0;
+        long long cnt = 0;
+        for (size_t i = 0; i < n2; ++i) {
+            if (ms->masks && ms->masks[(size_t)f * n2 + i] == 0) continue;
+            double bg = 0.0;
+            if (md->background) bg = md->background[p->background_stride ? (size_t)f * n2 + i : i];
+            sum += std::max(m[i] - bg, 0.0);
+            ++cnt;
+        }
+        p->data_snr[f] = cnt == 0 ? -INFINITY : p->weights[f] * std::sqrt(sum / (double)cnt);
+    });
     for (int f = 0; f < F; ++f) {
         Axis r{}, c{};
         FPM_TRY(interpolation_axis(p->start_row[f], N, p->m, p->off_row[f], r));
@@ -510,12 +559,7 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
             fp.w11 = (float)(r.upper_weight * c.upper_weight);
         }
         p->stencil_cells[f] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
-        long long valid = (long long)n2;
-        if (ms->masks) {
-            valid = 0;
-            const uint8_t* mk = ms->masks + (size_t)f * n2;
-            for (size_t i = 0; i < n2; ++i) valid += mk[i] != 0;
-        }
+        const long long valid = valid_counts[f];
         fp.weight = (float)p->weights[f];
         if (p->weights[f] > 0.0 && !(p->gains[f] > 0.0))
             return Status::make(FPM_ERR_INVALID_MODEL, "state frame %d has invalid gain %g", f, p->gains[f]);
@@ -524,22 +568,6 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
         fp.loss_scale = valid > 0 ? p->weights[f] / (double)valid : 0.0;
         p->params[f] = fp;
         p->weight_sum += p->weights[f];
-        // snr_weighted schedule score (src/reconstruction/schedule.rs:104-128).
-        if (p->weights[f] == 0.0) {
-            p->data_snr[f] = -INFINITY;
-        } else {
-            const double* m = ms->measurements + (size_t)f * n2;
-            double sum = 0.0;
-            long long cnt = 0;
-            for (size_t i = 0; i < n2; ++i) {
-                if (ms->masks && ms->masks[(size_t)f * n2 + i] == 0) continue;
-                double bg = 0.0;
-                if (md->background) bg = md->background[p->background_stride ? (size_t)f * n2 + i : i];
-                sum += std::max(m[i] - bg, 0.0);
-                ++cnt;
-            }
-            p->data_snr[f] = cnt == 0 ? -INFINITY : p->weights[f] * std::sqrt(sum / (double)cnt);
-        }
     }
 
     cudaStream_t s = ctx->streams[0];
@@ -667,10 +695,14 @@ Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) 
 
 struct BucketRun {
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs;
-    std::vector<cudaEvent_t> events;
+    std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
+    cudaEvent_t first = nullptr, last = nullptr;
+    int launches = 0;
     double bytes = 0.0;
     ~BucketRun() {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
+        if (first) cudaEventDestroy(first);
+        if (last) cudaEventDestroy(last);
     }
 };
 
@@ -769,6 +801,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         if (mpie && a->momentum_interval > 0)
             br.bytes += 48.0 * (double)M * (double)M * (double)((long long)effective * iters / a->momentum_interval);
     }
+    FPM_CUDA(cudaEventCreate(&br.first));
+    FPM_CUDA(cudaEventCreate(&br.last));
+    FPM_CUDA(cudaEventRecord(br.first, s));
     FPM_TRY(upload_array(br.tiles, tiles, s));
     FPM_TRY(upload_array(br.init, inits, s));
     FPM_TRY(upload_array(br.gauge, gauges, s));
@@ -784,27 +819,31 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         fpm_problem* p = b.problems[t];
         FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>() + t, 1, p->avg.as<double>(),
                                        p->init_partial.as<double>(), s));
+        br.launches += 2;
     }
     FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, false, s));
     FPM_CUDA(fpm::launch_shift_to_state(br.scratch_ptrs.as<double2*>(), br.object_ptrs.as<float2*>(),
                                         mpie ? br.anchor_ptrs.as<float2*>() : nullptr,
                                         mpie ? br.velocity_ptrs.as<float2*>() : nullptr, count, M, s));
-    if (canonical) FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+    br.launches += 3;
+    if (canonical) {
+        FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+        br.launches += 1;
+    }
 
     fpm::EngineParams ep{};
     ep.tiles = br.tiles.as<fpm::TileDesc>();
-    ep.mode = a->algorithm == FPM_ALG_GD ? fpm::kModeGradient : fpm::kModeProjection;
     switch (a->algorithm) {
-        case FPM_ALG_AP: ep.denominator = fpm::kDenLocal; break;
+        case FPM_ALG_AP: ep.alg = fpm::kAlgLocal; break;
         case FPM_ALG_FPIE:
-        case FPM_ALG_MPIE: ep.denominator = fpm::kDenRpie; break;
-        default: ep.denominator = fpm::kDenGlobal; break;
+        case FPM_ALG_MPIE: ep.alg = fpm::kAlgRpie; break;
+        case FPM_ALG_EPRY: ep.alg = canonical ? fpm::kAlgEpry : fpm::kAlgGlobal; break;
+        default: ep.alg = fpm::kAlgGradient; break;
     }
     ep.alpha = (float)a->stability;
     ep.eps = (float)a->epsilon;
     ep.object_step = (float)a->object_step;
     ep.pupil_step = (float)a->pupil_step;
-    ep.recover_pupil = canonical ? 1 : 0;
     ep.constrain_pupil = a->constrain_pupil_support ? 1 : 0;
     ep.momentum = mpie ? 1 : 0;
     ep.interval = a->momentum_interval;
@@ -822,13 +861,17 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_CUDA(cudaEventRecord(e0, s));
         FPM_CUDA(fpm::launch_engine(N, ep, count, s));
         FPM_CUDA(cudaEventRecord(e1, s));
+        br.launches += 1;
         return Status::ok();
     };
     if (iters > 0) {
         if (epry) {
             for (int it = 0; it < iters; ++it) {
                 FPM_TRY(engine(it, it + 1));
-                if (canonical) FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+                if (canonical) {
+                    FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+                    br.launches += 1;
+                }
             }
         } else {
             FPM_TRY(engine(0, iters));
@@ -838,6 +881,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(br.object_ptrs.ptr),
                                           br.scratch_ptrs.as<double2*>(), count, M, s));
     FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, true, s));
+    br.launches += 3;
+    FPM_CUDA(cudaEventRecord(br.last, s));
     return Status::ok();
 }
 
@@ -896,6 +941,11 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
     FPM_TRY(validate_params(a));
     if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
     std::vector<Bucket> buckets;
+    std::vector<const fpm_problem*> seen(problems, problems + count);
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
+        return Status::make(FPM_ERR_INVALID_PARAMETER,
+                            "a problem appears twice in one batch; each batched tile needs its own problem (its state is resident)");
     for (int i = 0; i < count; ++i) {
         fpm_problem* p = problems[i];
         if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
@@ -914,20 +964,49 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         runs.push_back(std::make_unique<BucketRun>());
         FPM_TRY(run_bucket(ctx, buckets[k], a, ctx->streams[k % fpm_context::kStreams], *runs.back()));
     }
-    ctx->engine_launches = 0;
-    ctx->engine_ms = 0.0;
-    ctx->engine_bytes = 0.0;
+    fpm_run_stats st = {};
+    cudaEvent_t first_event = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
     for (size_t k = 0; k < buckets.size(); ++k) {
         cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
         FPM_CUDA(cudaStreamSynchronize(s));
         FPM_CUDA(cudaGetLastError());
-        for (size_t e = 0; e + 1 < runs[k]->events.size(); e += 2) {
-            float ms = 0.f;
-            FPM_CUDA(cudaEventElapsedTime(&ms, runs[k]->events[e], runs[k]->events[e + 1]));
-            ctx->engine_ms += ms;
-            ctx->engine_launches += 1;
+        if (!first_event) first_event = runs[k]->first;
+        for (size_t e = 0; e + 1 < runs[k]->events.size(); e += 2)
+            engine_events.emplace_back(runs[k]->events[e], runs[k]->events[e + 1]);
+        st.kernel_launches += runs[k]->launches;
+        st.engine_bytes += runs[k]->bytes;
+    }
+    // Spans are measured from the earliest recorded start (the first bucket
+    // starts first on the host; later buckets start no earlier).
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        float last_ms = 0.f;
+        FPM_CUDA(cudaEventElapsedTime(&last_ms, first_event, runs[k]->last));
+        st.run_ms = std::max(st.run_ms, (double)last_ms);
+        if (k < 8) {
+            st.bucket_size[k] = buckets[k].n;
+            st.bucket_tiles[k] = (int32_t)buckets[k].problems.size();
+            st.bucket_end_ms[k] = last_ms;
+            st.buckets = (int32_t)k + 1;
         }
-        ctx->engine_bytes += runs[k]->bytes;
+    }
+    if (!engine_events.empty()) {
+        double lo = 1e300, hi = -1e300;
+        for (auto& pr : engine_events) {
+            float a = 0.f, b = 0.f, d = 0.f;
+            FPM_CUDA(cudaEventElapsedTime(&a, first_event, pr.first));
+            FPM_CUDA(cudaEventElapsedTime(&b, first_event, pr.second));
+            FPM_CUDA(cudaEventElapsedTime(&d, pr.first, pr.second));
+            lo = std::min(lo, (double)a);
+            hi = std::max(hi, (double)b);
+            st.engine_ms_sum += d;
+            st.engine_launches += 1;
+        }
+        st.engine_span_ms = hi - lo;
+    }
+    ctx->stats = st;
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
             const int idx = buckets[k].indices[t];
             FPM_TRY(collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr, s));
@@ -1234,11 +1313,9 @@ int32_t fpm_run_batch(fpm_context* ctx, int32_t count, fpm_problem* const* probl
     return finish(ctx, run_batch(ctx, count, problems, params, results));
 }
 
-int32_t fpm_last_engine_timing(const fpm_context* ctx, int32_t* launches, double* milliseconds, double* algorithmic_bytes) {
-    if (!ctx) return FPM_ERR_INVALID_PARAMETER;
-    if (launches) *launches = ctx->engine_launches;
-    if (milliseconds) *milliseconds = ctx->engine_ms;
-    if (algorithmic_bytes) *algorithmic_bytes = ctx->engine_bytes;
+int32_t fpm_last_run_stats(const fpm_context* ctx, fpm_run_stats* stats) {
+    if (!ctx || !stats) return FPM_ERR_INVALID_PARAMETER;
+    *stats = ctx->stats;
     return FPM_OK;
 }
 

@@ -20,7 +20,7 @@ from .experiment import (ArrayPose, CameraModel, Illumination, KVectorList, Opti
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
 from .reconstruction import (AlternatingProjection, Epry, Fpie, GradientDescent, Mpie, ReconstructionProblem,
-                             ReconstructionResult, RuntimeInfo, engine_timing, run_batch)
+                             ReconstructionResult, RuntimeInfo, last_run_stats, run_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
 
 
@@ -45,6 +45,6 @@ __all__ = [
     "InvalidModelError", "InvalidParameterError", "InvalidShapeError", "KVectorList", "LengthMismatchError",
     "MeasurementStack", "Mpie", "NumericalError", "Optics", "PlanarLEDArray", "PupilAberration",
     "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo", "SimulationResult",
-    "UnsupportedError", "compile_camera_model", "compile_model", "engine_timing", "fft2", "forward_intensities",
+    "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
     "run_batch", "simulate", "suggest_reconstruction_shape",
 ]

@@ -23,7 +23,7 @@ EXPORTED = (
     "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
     "fpm_fft2", "fpm_forward_stack", "fpm_problem_create", "fpm_problem_destroy",
-    "fpm_run", "fpm_run_batch", "fpm_last_engine_timing",
+    "fpm_run", "fpm_run_batch", "fpm_last_run_stats",
 )
 
 
@@ -82,8 +82,17 @@ class ResultDesc(C.Structure):
     ]
 
 
+class RunStats(C.Structure):
+    _fields_ = [
+        ("kernel_launches", C.c_int32), ("engine_launches", C.c_int32), ("run_ms", C.c_double),
+        ("engine_ms_sum", C.c_double), ("engine_span_ms", C.c_double), ("engine_bytes", C.c_double),
+        ("buckets", C.c_int32), ("bucket_size", C.c_int32 * 8), ("bucket_tiles", C.c_int32 * 8),
+        ("bucket_end_ms", C.c_double * 8),
+    ]
+
+
 _lib = None
-_lock = threading.Lock()
+_lock = threading.RLock()
 
 
 def library() -> C.CDLL:

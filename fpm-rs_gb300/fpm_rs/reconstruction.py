@@ -341,9 +341,17 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
     return out
 
 
-def engine_timing():
-    """(launches, milliseconds, algorithmic bytes) of the last run's frame-engine launches."""
+def last_run_stats() -> dict:
+    """Device statistics of the last run (CUDA events on the launching streams).
+
+    kernel_launches: kernels this library launched; engine_launches: frame
+    engine launches; run_ms: first kernel start to last kernel end;
+    engine_ms_sum / engine_span_ms: frame-engine durations summed / spanned;
+    engine_bytes: the engine's algorithmic HBM bytes.
+    """
     ctx = N.context()
-    launches, ms, nbytes = C.c_int32(), C.c_double(), C.c_double()
-    N.library().fpm_last_engine_timing(ctx.handle, C.byref(launches), C.byref(ms), C.byref(nbytes))
-    return launches.value, ms.value, nbytes.value
+    st = N.RunStats()
+    N.check(N.library().fpm_last_run_stats(ctx.handle, C.byref(st)), ctx.handle)
+    out = {name: getattr(st, name) for name, _ in N.RunStats._fields_[:6]}
+    out["buckets"] = [(st.bucket_size[k], st.bucket_tiles[k], st.bucket_end_ms[k]) for k in range(st.buckets)]
+    return out

@@ -180,10 +180,22 @@ int32_t fpm_run(fpm_context *ctx, fpm_problem *problem, const fpm_algorithm_para
 int32_t fpm_run_batch(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
                       const fpm_algorithm_params *params, fpm_result_desc *results);
 
-/* Device timing of the frame-engine launches of the last fpm_run/fpm_run_batch
- * (CUDA events recorded on each launch's stream). */
-int32_t fpm_last_engine_timing(const fpm_context *ctx, int32_t *launches, double *milliseconds,
-                               double *algorithmic_bytes);
+/* Device-side statistics of the last fpm_run / fpm_run_batch, from CUDA
+ * events recorded on the streams the kernels ran on. */
+typedef struct {
+    int32_t kernel_launches;   /* every kernel this library launched */
+    int32_t engine_launches;   /* frame-engine launches */
+    double run_ms;             /* first kernel start to last kernel end */
+    double engine_ms_sum;      /* sum of frame-engine launch durations */
+    double engine_span_ms;     /* first engine start to last engine end */
+    double engine_bytes;       /* algorithmic HBM bytes of the engine launches */
+    int32_t buckets;           /* tile-size groups of the run (at most 8 reported) */
+    int32_t bucket_size[8];    /* detector size N of each group */
+    int32_t bucket_tiles[8];   /* tiles in each group */
+    double bucket_end_ms[8];   /* run start to the group's results being ready */
+} fpm_run_stats;
+
+int32_t fpm_last_run_stats(const fpm_context *ctx, fpm_run_stats *stats);
 
 #ifdef __cplusplus
 }
