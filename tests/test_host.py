@@ -1,0 +1,162 @@
+"""Host-side checks that need no GPU: the C ABI library, model compilation
+against the oracle (integer crop origins bit-exact), validation and error
+mapping, and unsupported options failing before any device work."""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def fpm(native_library, oracle_module):
+    import fpm_rs
+
+    return fpm_rs
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "fpm_gpu.h")).read()
+    return sorted(set(re.findall(r"^(?:int32_t|const char \*)\s*(fpm_\w+)\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(native_library):
+    lib = C.CDLL(native_library)
+    names = _declared_symbols()
+    assert "fpm_run" in names and "fpm_problem_create" in names and len(names) >= 14
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+@pytest.mark.parametrize("side,n", [(3, 32), (15, 256), (13, 128), (15, 64), (9, 128), (5, 64)])
+@pytest.mark.parametrize("policy", ["smooth", "minimum", "power_of_two"])
+def test_compile_matches_oracle_bit_exact(fpm, side, n, policy):
+    optics = fpm.Optics(**W.OPTICS)
+    grid, ref = W.led_grid(side)
+    geometry = fpm.PlanarLEDArray(grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))
+    model = fpm.compile_model(optics, fpm.Illumination(geometry), (n, n), policy)
+    kx, ky = oracle.planar_kvectors(W.OPTICS, grid, W.PITCH, ref, (0.0, 0.0, W.Z))
+    om = oracle.compile_model(W.OPTICS, kx, ky, (n, n), policy)
+    assert model.reconstruction_shape == (om["mh"], om["mw"])
+    assert np.array_equal(model.crop_origins[:, 0], om["start_row"])
+    assert np.array_equal(model.crop_origins[:, 1], om["start_col"])
+    assert np.array_equal(model.subpixel_offsets[:, 0], om["off_row"])
+    assert np.array_equal(model.subpixel_offsets[:, 1], om["off_col"])
+    assert np.array_equal(model.pupil_support, om["support"])
+    assert np.array_equal(model.pupil, om["pupil"])
+    assert np.array_equal(model.k_vectors[:, 0], kx) and np.array_equal(model.k_vectors[:, 1], ky)
+
+
+def test_compile_with_defocus_aberration_and_rotation(fpm):
+    ab = fpm.PupilAberration(astigmatism=0.3, coma=-0.2, spherical=0.1, edge_apodization=0.5)
+    optics = fpm.Optics(**W.OPTICS, defocus_distance=5e-6, pupil_aberration=ab)
+    pose = fpm.ArrayPose.from_translation_and_extrinsic_xyz_degrees((1e-3, -2e-3, -85e-3), (2.0, -1.0, 15.0))
+    geometry = fpm.PlanarLEDArray((5, 7), (4e-3, 3.5e-3), (3.2, 1.7), pose)
+    model = fpm.compile_model(optics, fpm.Illumination(geometry), (64, 64))
+    odict = dict(W.OPTICS, defocus_distance=5e-6,
+                 pupil_aberration=dict(astigmatism=0.3, coma=-0.2, spherical=0.1, edge_apodization=0.5))
+    kx, ky = oracle.planar_kvectors(odict, (5, 7), (4e-3, 3.5e-3), (3.2, 1.7), (1e-3, -2e-3, -85e-3),
+                                    tuple(np.radians([2.0, -1.0, 15.0])))
+    om = oracle.compile_model(odict, kx, ky, (64, 64))
+    assert np.array_equal(model.crop_origins[:, 0], om["start_row"])
+    assert np.array_equal(model.crop_origins[:, 1], om["start_col"])
+    assert np.abs(model.pupil - om["pupil"]).max() <= 1e-15
+
+
+def test_exact_shape_validation(fpm):
+    optics = fpm.Optics(**W.OPTICS)
+    grid, ref = W.led_grid(3)
+    geometry = fpm.PlanarLEDArray(grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))
+    with pytest.raises(fpm.InvalidShapeError):
+        fpm.compile_model(optics, fpm.Illumination(geometry), (32, 32), (40, 40))
+    with pytest.raises(fpm.InvalidShapeError):
+        fpm.compile_model(optics, fpm.Illumination(geometry), (32, 32), (48, 50))
+    assert fpm.suggest_reconstruction_shape(optics, fpm.Illumination(geometry), (32, 32)) == (42, 42)
+
+
+def test_optics_validation(fpm):
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.Optics(532e-9, 0.1, 4.0, -6.5e-6)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.Optics(532e-9, 0.5, 1.0, 6.5e-6)  # coherent sampling violated
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.Optics(532e-9, 1.2, 40.0, 6.5e-6)  # NA above the medium index
+
+
+def test_measurement_and_problem_validation(fpm):
+    model = fpm.compile_model(fpm.Optics(**W.OPTICS), fpm.Illumination(fpm.PlanarLEDArray(
+        (3, 3), W.PITCH, (1.0, 1.0), fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))), (32, 32))
+    data = np.ones((9, 32, 32))
+    bad = data.copy()
+    bad[0, 0, 0] = np.nan
+    with pytest.raises(fpm.InvalidMeasurementsError):
+        fpm.MeasurementStack(bad)
+    with pytest.raises(fpm.InvalidMeasurementsError):
+        fpm.MeasurementStack(data, frame_weights=[-1.0] + [1.0] * 8)
+    with pytest.raises(fpm.InvalidModelError):
+        fpm.ReconstructionProblem(np.ones((8, 32, 32)), model)
+    with pytest.raises(fpm.InvalidShapeError):
+        fpm.ReconstructionProblem(np.ones((9, 16, 16)), model)
+    with pytest.raises(fpm.InvalidMeasurementsError):
+        fpm.ReconstructionProblem(data, model, frame_weights=[0.0] * 9)
+    masks = np.ones((9, 32, 32), np.uint8)
+    masks[4] = 0
+    with pytest.raises(fpm.InvalidMeasurementsError):
+        fpm.ReconstructionProblem(data, model, masks=masks)
+
+
+def test_unsupported_options_fail_before_device_work(fpm):
+    model = fpm.compile_model(fpm.Optics(**W.OPTICS), fpm.Illumination(fpm.PlanarLEDArray(
+        (3, 3), W.PITCH, (1.0, 1.0), fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))), (32, 32))
+    problem = fpm.ReconstructionProblem(np.ones((9, 32, 32)), model)
+    with pytest.raises(fpm.UnsupportedError):
+        fpm.AlternatingProjection(iterations=1).run(problem, schedule="random")
+    with pytest.raises(ValueError):
+        fpm.AlternatingProjection(iterations=1).run(problem, schedule="spiral")
+    with pytest.raises(fpm.UnsupportedError):
+        fpm.AlternatingProjection(iterations=1).run(problem, callbacks=[object()])
+    with pytest.raises(fpm.UnsupportedError):
+        fpm.GradientDescent(recover_illumination=True)
+    with pytest.raises(ValueError):
+        fpm.Mpie(loss_type="l1")
+
+
+def test_error_status_mapping(fpm):
+    from fpm_rs import errors
+
+    assert isinstance(errors.from_status(1, "x"), fpm.InvalidShapeError)
+    assert isinstance(errors.from_status(3, "x"), fpm.InvalidModelError)
+    assert isinstance(errors.from_status(7, "x"), fpm.NumericalError)
+    assert isinstance(errors.from_status(8, "x"), fpm.UnsupportedError)
+    assert isinstance(errors.from_status(9, "x"), fpm.DeviceError)
+
+
+def test_device_calls_fail_loudly_without_a_gpu(fpm):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(fpm.DeviceError):
+        fpm.fft2(np.ones((4, 4)))
+
+
+def test_model_json_round_trip(fpm, tmp_path):
+    grid, ref = W.led_grid(3)
+    model = fpm.compile_model(fpm.Optics(**W.OPTICS), fpm.Illumination(fpm.PlanarLEDArray(
+        grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))), (32, 32))
+    path = tmp_path / "model.json"
+    model.save_json(path=path)
+    loaded = fpm.ImagePlaneModel.load_json(path=path)
+    assert loaded.reconstruction_shape == model.reconstruction_shape
+    assert np.array_equal(loaded.crop_origins, model.crop_origins)
+    assert np.array_equal(loaded.subpixel_offsets, model.subpixel_offsets)
+    assert np.array_equal(loaded.pupil, model.pupil)
