@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+struct fpm_context;
+
 namespace fpm {
 
 // Per-frame constants, computed once per problem on the host in FP64 and
@@ -121,5 +123,9 @@ struct GaugeTile {
     int row_exact, col_exact;  // every source offset is integer on that axis
 };
 cudaError_t launch_gauge(const GaugeTile* tiles, int count, int n, int m, cudaStream_t s);
+
+// Context accessors for entry points that live outside runtime.cpp.
+void set_context_error(fpm_context* ctx, const char* message);
+void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream);
 
 }  // namespace fpm

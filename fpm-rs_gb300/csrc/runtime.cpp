@@ -1017,6 +1017,20 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
 
 }  // namespace
 
+namespace fpm {
+
+void set_context_error(fpm_context* ctx, const char* message) {
+    if (ctx) ctx->error = message;
+    g_global_error = message;
+}
+
+void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream) {
+    *device = ctx->device;
+    *stream = ctx->streams[0];
+}
+
+}  // namespace fpm
+
 // ====================================================================== ABI
 
 extern "C" {

@@ -159,6 +159,17 @@ int32_t fpm_compile_model(const fpm_optics *optics, int32_t sources, const doubl
  * (forward scaled by 1/(h*w), inverse unscaled). Computed in FP64 on the GPU. */
 int32_t fpm_fft2(fpm_context *ctx, double *values, int32_t height, int32_t width, int32_t inverse);
 
+/* fpm_fft2 without device allocation, for callers that cannot call
+ * cudaMalloc (device memory owned by another allocator or admitted against a
+ * fixed HBM budget; loops that must not synchronise the device). No
+ * counterpart in the reference. Scratch is one fixed file-scope device array
+ * (768*768 complex128 values, at most 4096 per row or column; larger shapes
+ * return FPM_ERR_INVALID_SHAPE) that each GPU holds until the process exits.
+ * Calls are serialised by a process-wide lock because they share that array.
+ * The first call on a device looks up the array's address; make it before any
+ * stream capture. */
+int32_t fpm_fft2_noalloc(fpm_context *ctx, double *values, int32_t height, int32_t width, int32_t inverse);
+
 /* Forward intensity stack [sources*h*w] of a complex128 object [mh*mw]
  * (object FFT, crop, pupil, IFFT, |psi|^2 * gain + background). */
 int32_t fpm_forward_stack(fpm_context *ctx, const fpm_model_desc *model, const double *object,
