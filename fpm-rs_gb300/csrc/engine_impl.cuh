@@ -45,8 +45,10 @@ struct Cfg {
     // stride chosen so that half-warps spanning two rows hit disjoint banks.
     static constexpr int RS = N == 32 ? 40 : N == 64 ? 72 : N == 128 ? 152 : 272;
     static constexpr int ORS = N + 2;       // staged stencil row: N + 2 columns from an even origin
-    static constexpr int THREADS = N;       // one thread per column position in P4
+    static constexpr int THREADS = 2 * N;   // two threads per column position in P4 (lanes l, l ^ 16)
     static constexpr int WARPS = THREADS / 32;
+    // Resident CTAs per SM that shared memory allows; registers are capped to match.
+    static constexpr int MIN_BLOCKS = N == 256 ? 1 : N == 128 ? 2 : N == 64 ? 4 : 7;
     static constexpr int TW = 256 / N;      // w_N^k = w_256^(k * TW)
     static constexpr int FIELD = (R + 1) * RS;  // raw row 0: halo U row from the previous CTA
     static constexpr int STAGE = (R + 1) * ORS;
@@ -201,26 +203,26 @@ FPM_DEVICE void rows_inverse(float2* __restrict__ fld, const float2* __restrict_
 }
 
 // P3: radix-C column step across the cluster (inverse direction): per task,
-// C remote loads, one radix-C DFT, C remote stores.
+// C remote loads, one radix-C DFT and C remote stores, through explicit
+// cluster-shared addresses (mapa + ld/st.shared::cluster).
 template <class K>
 FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __restrict__ tw, int c) {
     if constexpr (K::C > 1) {
         constexpr int C = K::C, N = K::N, ROWS = K::R / C;
-        cg::cluster_group cluster = cg::this_cluster();
-        float2* peer[C];
+        unsigned base[C];
 #pragma unroll
-        for (int r = 0; r < C; ++r) peer[r] = cluster.map_shared_rank(fld, r);
+        for (int r = 0; r < C; ++r) base[r] = dsmem_address(fld, r);
 #pragma unroll 1
         for (int t = 0; t < K::TX; ++t) {
             const int task = threadIdx.x + t * K::THREADS;
             const int l = c * ROWS + task / N;
-            const int off = l * K::RS + phys<K>(task % N);
+            const unsigned off = 8u * (unsigned)(l * K::RS + phys<K>(task % N));
             float2 v[C];
 #pragma unroll
-            for (int nc = 0; nc < C; ++nc) v[nc] = peer[nc ^ (C / 2)][off];
+            for (int nc = 0; nc < C; ++nc) v[nc] = dsmem_load(base[nc ^ (C / 2)] + off);
             dft_reg<C, true>(v);
 #pragma unroll
-            for (int k1 = 0; k1 < C; ++k1) peer[k1][off] = twiddle_smem<true>(v[k1], tw, l * k1 * K::TW);
+            for (int k1 = 0; k1 < C; ++k1) dsmem_store(base[k1] + off, twiddle_smem<true>(v[k1], tw, l * k1 * K::TW));
         }
     }
 }
@@ -231,21 +233,73 @@ template <class K>
 FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c) {
     if constexpr (K::C > 1) {
         constexpr int C = K::C, N = K::N, ROWS = K::R / C;
-        cg::cluster_group cluster = cg::this_cluster();
-        float2* peer[C];
+        unsigned base[C];
 #pragma unroll
-        for (int r = 0; r < C; ++r) peer[r] = cluster.map_shared_rank(fld, r);
+        for (int r = 0; r < C; ++r) base[r] = dsmem_address(fld, r);
 #pragma unroll 1
         for (int t = 0; t < K::TX; ++t) {
             const int task = threadIdx.x + t * K::THREADS;
-            const int off = (c * ROWS + task / N) * K::RS + phys<K>(task % N);
+            const unsigned off = 8u * (unsigned)((c * ROWS + task / N) * K::RS + phys<K>(task % N));
             float2 v[C];
 #pragma unroll
-            for (int k1 = 0; k1 < C; ++k1) v[k1] = peer[k1][off];
+            for (int k1 = 0; k1 < C; ++k1) v[k1] = dsmem_load(base[k1] + off);
             dft_reg<C, false>(v);
 #pragma unroll
-            for (int j1 = 0; j1 < C; ++j1) peer[j1 ^ (C / 2)][off] = v[j1];
+            for (int j1 = 0; j1 < C; ++j1) dsmem_store(base[j1 ^ (C / 2)] + off, v[j1]);
         }
+    }
+}
+
+// P4 column transforms with two threads per column: lanes l and l ^ 16 of a
+// warp share column position q; half h = lane / 16 holds local rows
+// n2 and n2 + 16 for n2 in [8h, 8h + 8). The 32-point transform is split as
+// 2 x 16: a radix-2 step with twiddles, an exchange of half the values with
+// the partner lane, and a 16-point register DFT.
+//
+// Inverse: natural rows in, z[k] = X[h + 2k] out.
+template <class K>
+FPM_DEVICE void column_inverse_split(const float2* __restrict__ fld, int pq, int h, const float2* __restrict__ tw,
+                                     float2 (&z)[16]) {
+    float2 y0[8], y1[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int n2 = 8 * h + i;
+        const float2 a = fld[n2 * K::RS + pq], b = fld[(n2 + 16) * K::RS + pq];
+        y0[i] = cadd(a, b);
+        y1[i] = twiddle_smem<true>(csub(a, b), tw, 8 * n2);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float2 send = h ? y0[i] : y1[i];
+        const float2 recv = make_float2(__shfl_xor_sync(0xffffffffu, send.x, 16), __shfl_xor_sync(0xffffffffu, send.y, 16));
+        const float2 own = h ? y1[i] : y0[i];
+        z[i] = h ? recv : own;
+        z[i + 8] = h ? own : recv;
+    }
+    dft_reg<16, true>(z);
+}
+
+// Forward, the dual: z[k] holds x'[h + 2k]; writes natural rows n2 and n2 + 16
+// for n2 in [8h, 8h + 8), each times w_N^(-c * row) when the cluster splits
+// the column (C > 1).
+template <class K>
+FPM_DEVICE void column_forward_split(float2* __restrict__ fld, int pq, int h, int c, const float2* __restrict__ tw,
+                                     float2 (&z)[16]) {
+    dft_reg<16, false>(z);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float2 send = h ? twiddle_smem<false>(z[i], tw, 8 * i) : z[i + 8];
+        const float2 recv = make_float2(__shfl_xor_sync(0xffffffffu, send.x, 16), __shfl_xor_sync(0xffffffffu, send.y, 16));
+        const float2 own = h ? twiddle_smem<false>(z[i + 8], tw, 8 * (i + 8)) : z[i];
+        const float2 w0 = h ? recv : own, w1 = h ? own : recv;
+        const int row = 8 * h + i;
+        float2 lo = cadd(w0, w1), hi = csub(w0, w1);
+        if constexpr (K::C > 1) {
+            lo = twiddle_smem<false>(lo, tw, c * row * K::TW);
+            hi = twiddle_smem<false>(hi, tw, c * (row + 16) * K::TW);
+        }
+        fld[row * K::RS + pq] = lo;
+        fld[(row + 16) * K::RS + pq] = hi;
     }
 }
 
@@ -259,7 +313,7 @@ FPM_DEVICE void load_pupil_slab(float2* __restrict__ pslab, const float2* __rest
 }
 
 template <int N_, int ALG, int LOSS>
-__global__ void __launch_bounds__(Cfg<N_>::THREADS) engine_kernel(const EngineParams P) {
+__global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_kernel(const EngineParams P) {
     using K = Cfg<N_>;
     constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -347,20 +401,22 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) engine_kernel(const EnginePa
                 }
             }
 
-            // P3, then the measurement prefetch for P4 (issued before the
-            // barrier so its latency overlaps the wait).
+            // P3
             if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c);
-            // Thread tid owns column position q = tid in P4.
-            float mreg[32];
-            unsigned mbits = 0xffffffffu;
+            // Measurement prefetch for P4, issued before the barrier so its
+            // latency overlaps the wait.
+            // P4 ownership: column position q, half h (rows h + 2k of the spatial column).
+            const int q4 = (warp << 4) | (lane & 15), h4 = lane >> 4;
+            float mreg[16];
+            unsigned mbits = 0xffffu;
             {
-                const size_t off = (size_t)f * N * N + (size_t)c * 32 * N + tid;
+                const size_t off = (size_t)f * N * N + (size_t)(c * 32 + h4) * N + q4;
 #pragma unroll
-                for (int k2 = 0; k2 < 32; ++k2) mreg[k2] = __ldcs(T.meas + off + (size_t)k2 * N);
+                for (int k = 0; k < 16; ++k) mreg[k] = __ldcs(T.meas + off + (size_t)(2 * k) * N);
                 if (T.masks) {
                     mbits = 0u;
 #pragma unroll
-                    for (int k2 = 0; k2 < 32; ++k2) mbits |= (T.masks[off + (size_t)k2 * N] != 0 ? 1u : 0u) << k2;
+                    for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)(2 * k) * N] != 0 ? 1u : 0u) << k;
                 }
             }
 
@@ -368,41 +424,73 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) engine_kernel(const EnginePa
 
             // P4: column inverse FFT, projection, column forward FFT.
             {
-                const float* brow =
-                    T.background ? T.background + (size_t)f * T.background_stride + (size_t)c * 32 * N + tid : nullptr;
+                const float* brow = T.background ? T.background + (size_t)f * T.background_stride +
+                                                       (size_t)(c * 32 + h4) * N + q4
+                                                 : nullptr;
                 const float gain = fp.gain, inv_gain = 1.0f / fp.gain;
-                float2 v[32];
-                const int pq = phys<K>(tid);
-#pragma unroll
-                for (int l = 0; l < 32; ++l) v[l] = fld[l * K::RS + pq];
-                dft_reg<32, true>(v);
+                const int pq = phys<K>(q4);
+                float2 v[16];
+                column_inverse_split<K>(fld, pq, h4, tw, v);
                 float frame_loss = 0.f;
+                if (T.amplitude) {
+                    // a = sqrt(max(I / g, 0)), -1 where masked; with no
+                    // background, I = g a^2 exactly as the reference uses it.
 #pragma unroll
-                for (int k2 = 0; k2 < 32; ++k2) {
-                    const float meas = mreg[k2];
-                    const bool masked = ((mbits >> k2) & 1u) == 0u;
-                    const float bg = brow ? __ldg(brow + k2 * N) : 0.f;
-                    const float intrinsic = cnorm2(v[k2]);
+                    for (int k = 0; k < 16; ++k) {
+                        const float a = mreg[k];
+                        const float intrinsic = cnorm2(v[k]);
+                        const float r = rsqrtf(fmaxf(intrinsic, 1.17549435e-38f));
+                        const float s_amp = intrinsic * r;
+                        if constexpr (projection) {
+                            if (a >= 0.f) {
+                                if constexpr (LOSS == 0) {
+                                    const float d = s_amp - a;
+                                    frame_loss = fmaf(d, d, frame_loss);
+                                } else {
+                                    frame_loss += point_loss<LOSS>(gain * intrinsic, gain * a * a, P.loss);
+                                }
+                                v[k] = intrinsic > P.eps ? cscale(v[k], a * r) : make_float2(a, 0.f);
+                            }
+                        } else {
+                            if (a < 0.f) {
+                                v[k] = make_float2(0.f, 0.f);
+                            } else if constexpr (LOSS == 0) {
+                                const float d = s_amp - a;
+                                frame_loss = fmaf(d, d, frame_loss);
+                                v[k] = cscale(v[k], 1.f - a * rsqrtf(fmaxf(intrinsic, P.eps)));
+                            } else {
+                                frame_loss += point_loss<LOSS>(intrinsic, a * a, P.loss);
+                                v[k] = cscale(v[k], descent_factor<LOSS>(intrinsic, a * a, P.loss, P.eps));
+                            }
+                        }
+                    }
+                    // Amplitude MSE of the projection family is gain * (sqrt(intrinsic) - a)^2.
+                    if (projection && LOSS == 0) frame_loss *= gain;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const float meas = mreg[k];
+                    const bool masked = ((mbits >> k) & 1u) == 0u;
+                    const float bg = brow ? __ldg(brow + 2 * k * N) : 0.f;
+                    const float intrinsic = cnorm2(v[k]);
                     const float target = fmaxf((meas - bg) * inv_gain, 0.f);
                     if constexpr (projection) {
                         if (!masked) {
                             frame_loss += point_loss<LOSS>(fmaf(gain, intrinsic, bg), meas, P.loss);
-                            v[k2] = intrinsic > P.eps ? cscale(v[k2], sqrtf(target) * rsqrtf(intrinsic))
-                                                      : make_float2(sqrtf(target), 0.f);
+                            v[k] = intrinsic > P.eps ? cscale(v[k], sqrtf(target) * rsqrtf(intrinsic))
+                                                     : make_float2(sqrtf(target), 0.f);
                         }
                     } else {
                         if (masked) {
-                            v[k2] = make_float2(0.f, 0.f);
+                            v[k] = make_float2(0.f, 0.f);
                         } else {
                             frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
-                            v[k2] = cscale(v[k2], descent_factor<LOSS>(intrinsic, target, P.loss, P.eps));
+                            v[k] = cscale(v[k], descent_factor<LOSS>(intrinsic, target, P.loss, P.eps));
                         }
                     }
+                    }
                 }
-                dft_reg<32, false>(v);
-#pragma unroll
-                for (int j2 = 0; j2 < 32; ++j2)
-                    fld[j2 * K::RS + pq] = C > 1 ? twiddle_smem<false>(v[j2], tw, c * j2 * K::TW) : v[j2];
+                column_forward_split<K>(fld, pq, h4, c, tw, v);
                 loss_acc += (double)frame_loss * fp.loss_scale;
             }
             cluster_barrier<K>();
@@ -644,19 +732,17 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const Forward
     float* out = P.out + (size_t)f * N * N;
     const float* bg = P.background ? P.background + (size_t)f * P.background_stride : nullptr;
     {
-        const int q = tid;
-        float2 v[32];
-        const int pq = phys<K>(q);
-#pragma unroll
-        for (int l = 0; l < 32; ++l) v[l] = fld[l * K::RS + pq];
-        dft_reg<32, true>(v);
+        const int warp = tid >> 5, lane = tid & 31;
+        const int q = (warp << 4) | (lane & 15), h = lane >> 4;
+        float2 v[16];
+        column_inverse_split<K>(fld, phys<K>(q), h, tw, v);
         const int ka = q / NB, kb = q % NB;
         const int x = ka + NA * kb;
 #pragma unroll
-        for (int k2 = 0; k2 < 32; ++k2) {
-            const int y = c + C * k2;
+        for (int k = 0; k < 16; ++k) {
+            const int y = c + C * (h + 2 * k);
             const float b0 = bg ? bg[y * N + x] : 0.f;
-            out[y * N + x] = fmaf(fp.gain, cnorm2(v[k2]), b0);
+            out[y * N + x] = fmaf(fp.gain, cnorm2(v[k]), b0);
         }
     }
     cluster_barrier<K>();
@@ -678,6 +764,19 @@ __global__ void permute_f64_kernel(const double* __restrict__ src, float* __rest
         const long long f = e / (K::N * K::N);
         const int p = (int)(e % (K::N * K::N));
         dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = (float)src[e];
+    }
+}
+
+template <int N_>
+__global__ void permute_amplitude_kernel(const double* __restrict__ src, const uint8_t* __restrict__ masks,
+                                         const double* __restrict__ gains, float* __restrict__ dst, long long frames) {
+    using K = Cfg<N_>;
+    const long long total = frames * K::N * K::N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long f = e / (K::N * K::N);
+        const int p = (int)(e % (K::N * K::N));
+        const float a = (masks && masks[e] == 0) ? -1.0f : (float)sqrt(fmax(src[e] / gains[f], 0.0));
+        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = a;
     }
 }
 
@@ -713,9 +812,15 @@ __global__ void init_mean_kernel(const InitTile* __restrict__ tiles, double* __r
             const FrameParam fp = T.params[f];
             if (fp.weight == 0.0f) continue;
             const size_t off = (size_t)f * N * N + idx;
-            if (T.masks && T.masks[off] == 0) continue;
-            const double bg = T.background ? (double)T.background[(size_t)f * T.background_stride + idx] : 0.0;
-            const double amp = sqrt(fmax(((double)T.meas[off] - bg) / (double)fp.gain, 0.0));
+            double amp;
+            if (T.amplitude) {
+                if (T.meas[off] < 0.0f) continue;
+                amp = (double)T.meas[off];
+            } else {
+                if (T.masks && T.masks[off] == 0) continue;
+                const double bg = T.background ? (double)T.background[(size_t)f * T.background_stride + idx] : 0.0;
+                amp = sqrt(fmax(((double)T.meas[off] - bg) / (double)fp.gain, 0.0));
+            }
             sum += (double)fp.weight * amp;
             wsum += (double)fp.weight;
         }
@@ -823,6 +928,14 @@ struct EngineEntry {
         const long long total = frames * N_ * N_;
         const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
         permute_u8_kernel<N_><<<blocks, 256, 0, s>>>(src, dst, frames);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t permute_amplitude(const double* src, const uint8_t* masks, const double* gains, float* dst,
+                                         long long frames, cudaStream_t s) {
+        const long long total = frames * N_ * N_;
+        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
+        permute_amplitude_kernel<N_><<<blocks, 256, 0, s>>>(src, masks, gains, dst, frames);
         return cudaGetLastError();
     }
 

@@ -116,3 +116,22 @@ FPM_DEVICE void cp_async16(void* smem, const void* gmem, int src_bytes) {
 }
 
 FPM_DEVICE void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Distributed shared memory: the cluster-shared address of `local` (a shared
+// memory location of this CTA) in CTA `rank`, and 8-byte accesses to it.
+FPM_DEVICE unsigned dsmem_address(const void* local, int rank) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+
+FPM_DEVICE float2 dsmem_load(unsigned address) {
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(address) : "memory");
+    return v;
+}
+
+FPM_DEVICE void dsmem_store(unsigned address, float2 v) {
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(address), "f"(v.x), "f"(v.y) : "memory");
+}

@@ -42,7 +42,7 @@ struct TileDesc {
     int* status;               // bit 0: non-finite momentum, bit 1: non-finite pupil
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
-    int pad;
+    int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
 };
 
 // Frame-engine kernel families, fixed at compile time so each instantiation
@@ -80,6 +80,10 @@ cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
 // Permutes natural-order frames [frames][N][N] into the engine layout.
 cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s);
 cudaError_t launch_permute_u8(int n, const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s);
+// Amplitude form: dst = sqrt(max(src / gain[f], 0)) in FP64, rounded once to
+// float, or -1 where masks (natural order, may be null) is zero.
+cudaError_t launch_permute_amplitude(int n, const double* src, const uint8_t* masks, const double* gains, float* dst,
+                                     long long frames, cudaStream_t s);
 
 // Initial object (ReconstructionState::initialize_with_backend,
 // src/reconstruction/state.rs:280-355) for a batch of tiles of one size:
@@ -93,7 +97,7 @@ struct InitTile {
     double2* scratch;          // M*M natural-order FP64 object
     int* status;               // bit 2: no positive-weight unmasked pixel
     int frames_count;
-    int pad;
+    int amplitude;             // measurement form, as TileDesc::amplitude
 };
 // avg: [count * N*N] doubles; partial: [count * init_chunks(N) * 2] doubles.
 int init_chunks(int n);

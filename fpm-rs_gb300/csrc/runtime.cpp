@@ -116,6 +116,7 @@ struct fpm_problem {
     std::vector<fpm::FrameParam> params;
     std::vector<double> stencil_cells;  // per frame: rows * cols of the bilinear stencil
     bool has_masks = false, has_background = false;
+    bool amplitude = false;  // device measurements hold sqrt(max(I / g, 0)), -1 where masked
     long long background_stride = 0;
     bool row_exact = true, col_exact = true;
     double weight_sum = 0.0;
@@ -571,17 +572,37 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
     }
 
     cudaStream_t s = ctx->streams[0];
-    // Measurements: FP64 upload, permuted to the engine's FP32 layout.
+    // Measurements: FP64 upload, permuted to the engine's FP32 layout. With no
+    // background the engine reads the amplitude form sqrt(max(I / g, 0))
+    // (computed in FP64, -1 on masked pixels): one float per pixel, no mask
+    // bytes, and no divide or square root in the frame loop.
     const size_t total = n2 * F;
+    p->amplitude = md->background == nullptr;
     FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
     FPM_TRY(p->meas.ensure(total * sizeof(float)));
     FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
-    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->meas.as<float>(), F, s));
-    if (ms->masks) {
-        FPM_TRY(p->masks.ensure(total));
-        FPM_TRY(ctx->scratch_a.ensure(total));
-        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
-        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
+    if (p->amplitude) {
+        std::vector<double> gains(F);
+        for (int f = 0; f < F; ++f) gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
+        FPM_TRY(ctx->scratch_b.ensure(F * sizeof(double)));
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (ms->masks) {
+            FPM_TRY(ctx->scratch_a.ensure(total));
+            FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+        }
+        FPM_CUDA(fpm::launch_permute_amplitude(N, ctx->staging.as<double>(),
+                                               ms->masks ? ctx->scratch_a.as<uint8_t>() : nullptr,
+                                               ctx->scratch_b.as<double>(), p->meas.as<float>(), F, s));
+        // The host vector must outlive the copy.
+        FPM_CUDA(cudaStreamSynchronize(s));
+    } else {
+        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->meas.as<float>(), F, s));
+        if (ms->masks) {
+            FPM_TRY(p->masks.ensure(total));
+            FPM_TRY(ctx->scratch_a.ensure(total));
+            FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+            FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
+        }
     }
     if (md->background) {
         const long long bg_frames = p->background_stride ? F : 1;
@@ -754,7 +775,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.pupil = p->pupil_state.as<float2>();
         T.support = p->support_d.as<uint8_t>();
         T.meas = p->meas.as<float>();
-        T.masks = p->has_masks ? p->masks.as<uint8_t>() : nullptr;
+        T.amplitude = p->amplitude ? 1 : 0;
+        T.masks = p->has_masks && !p->amplitude ? p->masks.as<uint8_t>() : nullptr;
         T.background = p->has_background ? p->background.as<float>() : nullptr;
         T.background_stride = p->background_stride;
         T.params = p->frame_params.as<fpm::FrameParam>();
@@ -769,6 +791,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.max_pupil_power = max_pupil_power;
         fpm::InitTile& I = inits[t];
         I.meas = T.meas;
+        I.amplitude = T.amplitude;
         I.masks = T.masks;
         I.background = T.background;
         I.background_stride = T.background_stride;
@@ -794,7 +817,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         for (int f = 0; f < p->frames; ++f) {
             if (p->params[f].weight == 0.f) continue;
             ++effective;
-            frame_bytes += 16.0 * p->stencil_cells[f] + 4.0 * (double)n2 + (p->has_masks ? (double)n2 : 0.0) +
+            frame_bytes += 16.0 * p->stencil_cells[f] + 4.0 * (double)n2 + (p->has_masks && !p->amplitude ? (double)n2 : 0.0) +
                            (canonical ? 16.0 * (double)n2 : 0.0);
         }
         br.bytes += frame_bytes * iters;
