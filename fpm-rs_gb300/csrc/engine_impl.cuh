@@ -144,10 +144,15 @@ FPM_DEVICE float descent_factor(float predicted, float measured, int runtime_los
 // bytes beyond the grid are zero-filled and never read from global memory.
 template <class K>
 FPM_DEVICE void stage_object(float2* __restrict__ osm, const float2* __restrict__ object, int M, long long ostride,
-                             const FrameParam& fp, int i_lo) {
+                             const FrameParam& fp, int i_lo, int row_lo, int row_hi) {
     const int c0 = fp.lower_col & ~1;
-    for (int e = threadIdx.x; e < (K::R + 1) * K::PAIRS; e += K::THREADS) {
-        const int r = e / K::PAIRS, t = e - r * K::PAIRS;
+    // Staged row r serves patch rows i_lo + r (and i_lo + r - 1): rows outside
+    // [row_lo, row_hi + 1] are never read.
+    const int r_begin = max(row_lo - i_lo, 0), r_end = min(row_hi + 1 - i_lo, K::R);
+    if (r_begin > r_end) return;
+    const int count = (r_end - r_begin + 1) * K::PAIRS;
+    for (int e = threadIdx.x; e < count; e += K::THREADS) {
+        const int r = r_begin + e / K::PAIRS, t = e % K::PAIRS;
         const int gr = fp.lower_row + i_lo + r;
         const int col = c0 + 2 * t;
         int bytes = 0;
@@ -162,14 +167,16 @@ FPM_DEVICE void stage_object(float2* __restrict__ osm, const float2* __restrict_
 // Tracks maxima of |patch|^2 and |P|^2 for EPRY.
 template <class K, bool TRACK_MAX>
 FPM_DEVICE void rows_inverse(float2* __restrict__ fld, const float2* __restrict__ ostage, const float2* __restrict__ tw,
-                             const float2* __restrict__ pslab, const FrameParam& fp, int c, int i_lo, float& max_obj,
-                             float& max_pup) {
+                             const float2* __restrict__ pslab, const FrameParam& fp, int c, int i_lo, int row_lo,
+                             int row_hi, float& max_obj, float& max_pup) {
     constexpr int N = K::N, NA = K::NA, NB = K::NB;
 #pragma unroll 1
     for (int t = 0; t < K::T1; ++t) {
         const int task = threadIdx.x + t * K::THREADS;
         const int l = task / NB, nb = task % NB;
-        const int il = centred_row<K>(c, l) - i_lo;
+        const int i = centred_row<K>(c, l);
+        if (i < row_lo || i > row_hi) continue;
+        const int il = i - i_lo;
         float2 v[NA];
 #pragma unroll
         for (int na = 0; na < NA; ++na) {
@@ -192,7 +199,17 @@ FPM_DEVICE void rows_inverse(float2* __restrict__ fld, const float2* __restrict_
     for (int t = 0; t < K::T2; ++t) {
         const int task = threadIdx.x + t * K::THREADS;
         const int l = task / NA, ka = task % NA;
+        const int i = centred_row<K>(c, l);
         float2* g = fld + l * K::RS + ka * (NB + 1);
+        if (i < row_lo || i > row_hi) {
+            // A cluster's radix-C step substitutes zeros for such rows; a
+            // single CTA's column transform reads the slab directly.
+            if constexpr (K::C == 1) {
+#pragma unroll
+                for (int kb = 0; kb < NB; ++kb) g[kb] = make_float2(0.f, 0.f);
+            }
+            continue;
+        }
         float2 v[NB];
 #pragma unroll
         for (int kb = 0; kb < NB; ++kb) v[kb] = g[kb];
@@ -206,7 +223,8 @@ FPM_DEVICE void rows_inverse(float2* __restrict__ fld, const float2* __restrict_
 // C remote loads, one radix-C DFT and C remote stores, through explicit
 // cluster-shared addresses (mapa + ld/st.shared::cluster).
 template <class K>
-FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __restrict__ tw, int c) {
+FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __restrict__ tw, int c, int row_lo,
+                                      int row_hi) {
     if constexpr (K::C > 1) {
         constexpr int C = K::C, N = K::N, ROWS = K::R / C;
         unsigned base[C];
@@ -219,7 +237,11 @@ FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __
             const unsigned off = 8u * (unsigned)(l * K::RS + phys<K>(task % N));
             float2 v[C];
 #pragma unroll
-            for (int nc = 0; nc < C; ++nc) v[nc] = dsmem_load(base[nc ^ (C / 2)] + off);
+            for (int nc = 0; nc < C; ++nc) {
+                // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * 32 + l.
+                const int i = (nc ^ (C / 2)) * K::R + l;
+                v[nc] = i >= row_lo && i <= row_hi ? dsmem_load(base[nc ^ (C / 2)] + off) : make_float2(0.f, 0.f);
+            }
             dft_reg<C, true>(v);
 #pragma unroll
             for (int k1 = 0; k1 < C; ++k1) dsmem_store(base[k1] + off, twiddle_smem<true>(v[k1], tw, l * k1 * K::TW));
@@ -230,7 +252,7 @@ FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __
 // P5: radix-C column step across the cluster (forward direction); output
 // block j1 goes to the CTA holding natural rows of block j1.
 template <class K>
-FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c) {
+FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c, int row_lo, int row_hi) {
     if constexpr (K::C > 1) {
         constexpr int C = K::C, N = K::N, ROWS = K::R / C;
         unsigned base[C];
@@ -245,7 +267,10 @@ FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c) {
             for (int k1 = 0; k1 < C; ++k1) v[k1] = dsmem_load(base[k1] + off);
             dft_reg<C, false>(v);
 #pragma unroll
-            for (int j1 = 0; j1 < C; ++j1) dsmem_store(base[j1 ^ (C / 2)] + off, v[j1]);
+            for (int j1 = 0; j1 < C; ++j1) {
+                const int i = (j1 ^ (C / 2)) * K::R + c * ROWS + task / N;
+                if (i >= row_lo && i <= row_hi) dsmem_store(base[j1 ^ (C / 2)] + off, v[j1]);
+            }
         }
     }
 }
@@ -340,6 +365,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     const int i_lo = C == 1 ? 0 : c * R;
     constexpr bool projection = ALG != kAlgGradient;
     constexpr bool epry = ALG == kAlgEpry;
+    // Rows of psi that can be non-zero (all rows when the pupil evolves).
+    const int row_lo = epry ? 0 : T.row_lo, row_hi = epry ? N - 1 : T.row_hi;
 
     load_pupil_slab<K>(pslab, T.pupil, c);
     int counter = P.momentum ? *T.counter : 0;
@@ -358,13 +385,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
 
             // S0
-            stage_object<K>(osm, T.object, M, ostride, fp, i_lo);
+            stage_object<K>(osm, T.object, M, ostride, fp, i_lo, row_lo, row_hi);
             __syncthreads();
             const float2* ostage = osm + (fp.lower_col & 1);
 
             // P1, P2
             float max_obj = 0.f, max_pup = 0.f;
-            rows_inverse<K, epry>(fld, ostage, tw, pslab, fp, c, i_lo, max_obj, max_pup);
+            rows_inverse<K, epry>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj, max_pup);
             if constexpr (epry) {
                 max_obj = warp_max(max_obj);
                 max_pup = warp_max(max_pup);
@@ -402,7 +429,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
 
             // P3
-            if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c);
+            if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
             // Measurement prefetch for P4, issued before the barrier so its
             // latency overlaps the wait.
             // P4 ownership: column position q, half h (rows h + 2k of the spatial column).
@@ -497,7 +524,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P5
             if constexpr (C > 1) {
-                columns_cross_forward<K>(fld, c);
+                columns_cross_forward<K>(fld, c, row_lo, row_hi);
                 cluster_barrier<K>();
             }
 
@@ -506,6 +533,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             for (int t = 0; t < K::T2; ++t) {
                 const int task = tid + t * K::THREADS;
                 const int l = task / NA, ka = task % NA;
+                const int i = centred_row<K>(c, l);
+                if (i < row_lo || i > row_hi) continue;
                 float2* g = fld + l * K::RS + ka * (NB + 1);
                 float2 v[NB];
 #pragma unroll
@@ -528,11 +557,16 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 for (int t = 0; t < K::T1; ++t) {
                     const int task = tid + t * K::THREADS;
                     const int l = task / NB, jb = task % NB;
+                    const int i = centred_row<K>(c, l);
+                    if (i < row_lo || i > row_hi) {
+#pragma unroll
+                        for (int ja = 0; ja < NA; ++ja) ureg[t][ja] = make_float2(0.f, 0.f);
+                        continue;
+                    }
                     float2 v[NA];
 #pragma unroll
                     for (int ka = 0; ka < NA; ++ka) v[ka] = fld[l * K::RS + phys<K>(NB * ka + jb)];
                     dft_reg<NA, false>(v);
-                    const int i = centred_row<K>(c, l);
                     const int il = i - i_lo;
 #pragma unroll
                     for (int ja = 0; ja < NA; ++ja) {
@@ -593,6 +627,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 constexpr int PER = (N + 1 + 31) / 32;
                 for (int r = warp; r < rows8; r += K::WARPS) {
                     const int i = i_lo + r;
+                    // Object row i takes U rows i and i - 1: both zero outside [row_lo, row_hi + 1].
+                    if (i < row_lo || i > row_hi + 1) continue;
                     const bool has0 = i < N, has1 = i >= 1;
                     const float2* u0 = fld + r * K::RS;
                     const float2* u1 = u0 - K::RS;  // r == 0: the halo row
@@ -720,13 +756,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const Forward
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
     load_pupil_slab<K>(pslab, P.pupil, c);
     const FrameParam fp = P.params[f];
-    stage_object<K>(osm, P.object, P.M, ostride, fp, i_lo);
+    stage_object<K>(osm, P.object, P.M, ostride, fp, i_lo, 0, N - 1);
     __syncthreads();
     float a = 0.f, b = 0.f;
-    rows_inverse<K, false>(fld, osm + (fp.lower_col & 1), tw, pslab, fp, c, i_lo, a, b);
+    rows_inverse<K, false>(fld, osm + (fp.lower_col & 1), tw, pslab, fp, c, i_lo, 0, N - 1, a, b);
     cluster_barrier<K>();
     if constexpr (C > 1) {
-        columns_cross_inverse<K>(fld, tw, c);
+        columns_cross_inverse<K>(fld, tw, c, 0, N - 1);
         cluster_barrier<K>();
     }
     float* out = P.out + (size_t)f * N * N;

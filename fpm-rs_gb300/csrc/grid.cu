@@ -131,6 +131,25 @@ cudaError_t launch_state_to_natural(const float2* const* object, double2* const*
     return cudaGetLastError();
 }
 
+// Complex64 rows (row stride src_stride) widened to dense complex128.
+__global__ void widen_kernel(const float2* __restrict__ src, long long src_stride, int rows, int cols,
+                             double2* __restrict__ dst) {
+    const long long total = (long long)rows * cols;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / cols, c = e % cols;
+        const float2 v = src[r * src_stride + c];
+        dst[e] = make_double2((double)v.x, (double)v.y);
+    }
+}
+
+cudaError_t launch_widen(const float2* src, long long src_stride, int rows, int cols, double2* dst, cudaStream_t s) {
+    const long long total = (long long)rows * cols;
+    if (total == 0) return cudaSuccess;
+    const int blocks = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+    widen_kernel<<<blocks, 256, 0, s>>>(src, src_stride, rows, cols, dst);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ gauge
 
 constexpr int kGaugeThreads = 1024;

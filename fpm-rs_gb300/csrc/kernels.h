@@ -43,6 +43,11 @@ struct TileDesc {
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
+    // Centred pupil rows [row_lo, row_hi] that hold a non-zero pupil value.
+    // With a fixed pupil every other row of psi = P * patch is zero and the
+    // correction U there is zero, so the engine skips those rows (EPRY,
+    // whose pupil evolves, uses the full range).
+    int row_lo, row_hi;
 };
 
 // Frame-engine kernel families, fixed at compile time so each instantiation
@@ -115,6 +120,8 @@ cudaError_t launch_shift_to_state(double2* const* scratch, float2* const* object
                                   float2* const* velocity, int count, int m, cudaStream_t s);
 cudaError_t launch_state_to_natural(const float2* const* object, double2* const* scratch, int count, int m,
                                     cudaStream_t s);
+// Complex64 rows (row stride src_stride) widened to dense complex128.
+cudaError_t launch_widen(const float2* src, long long src_stride, int rows, int cols, double2* dst, cudaStream_t s);
 
 // Object/pupil gauge canonicalisation (src/algorithms/gauge.rs:20-73), one
 // block per tile, FP64 reductions.

@@ -19,7 +19,11 @@
 #include <string>
 #include <thread>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <vector>
+
+#include <unistd.h>
 
 #include "fpm_gpu.h"
 #include "kernels.h"
@@ -63,12 +67,26 @@ struct Status {
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
+    // Pooled buffers are stream-ordered allocations from the context's pool
+    // on `stream`; others use cudaMalloc.
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;
     DeviceBuffer() = default;
     DeviceBuffer(const DeviceBuffer&) = delete;
     DeviceBuffer& operator=(const DeviceBuffer&) = delete;
     ~DeviceBuffer() { release(); }
+    // Later allocations and the free are ordered on s; an existing allocation
+    // is kept (callers synchronise between runs on different streams).
+    void bind(cudaMemPool_t p, cudaStream_t s) {
+        if (ptr && p != pool) release();
+        pool = p;
+        stream = s;
+    }
     void release() {
-        if (ptr) cudaFree(ptr);
+        if (ptr) {
+            if (pool) cudaFreeAsync(ptr, stream);
+            else cudaFree(ptr);
+        }
         ptr = nullptr;
         bytes = 0;
     }
@@ -76,7 +94,8 @@ struct DeviceBuffer {
         if (n <= bytes && ptr) return Status::ok();
         release();
         if (n == 0) n = 16;
-        FPM_CUDA(cudaMalloc(&ptr, n));
+        if (pool) FPM_CUDA(cudaMallocFromPoolAsync(&ptr, n, pool, stream));
+        else FPM_CUDA(cudaMalloc(&ptr, n));
         bytes = n;
         return Status::ok();
     }
@@ -84,6 +103,71 @@ struct DeviceBuffer {
     T* as() const {
         return static_cast<T*>(ptr);
     }
+};
+
+// Persistent host worker pool for the per-frame scans of problem creation:
+// fn(i) for i in [0, count) on all hardware threads, the caller included.
+// A forked child (the workers do not survive fork) runs serially.
+class HostPool {
+public:
+    static HostPool& get() {
+        static HostPool* pool = new HostPool();  // never destroyed: workers may still block at exit
+        return *pool;
+    }
+    void run(long long count, const std::function<void(long long)>& fn) {
+        if (count <= 0) return;
+        if (workers_.empty() || count == 1 || getpid() != pid_) {
+            for (long long i = 0; i < count; ++i) fn(i);
+            return;
+        }
+        std::lock_guard<std::mutex> serial(run_mu_);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            task_ = &fn;
+            count_ = count;
+            next_.store(0);
+            active_ = (int)workers_.size();
+            ++generation_;
+        }
+        cv_.notify_all();
+        drain(fn, count);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return active_ == 0; });
+        task_ = nullptr;
+    }
+
+private:
+    HostPool() : pid_(getpid()) {
+        const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+        for (int w = 0; w + 1 < hw; ++w) workers_.emplace_back([this] { loop(); });
+        for (auto& t : workers_) t.detach();
+    }
+    void drain(const std::function<void(long long)>& fn, long long count) {
+        for (long long i; (i = next_.fetch_add(1)) < count;) fn(i);
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return generation_ != seen; });
+            seen = generation_;
+            const std::function<void(long long)>* fn = task_;
+            const long long count = count_;
+            lk.unlock();
+            drain(*fn, count);
+            lk.lock();
+            if (--active_ == 0) done_.notify_all();
+        }
+    }
+    pid_t pid_;
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(long long)>* task_ = nullptr;
+    long long count_ = 0;
+    std::atomic<long long> next_{0};
+    int active_ = 0;
+    unsigned long long generation_ = 0;
 };
 
 struct FftPlan {
@@ -103,6 +187,7 @@ struct fpm_context {
     std::map<int, std::unique_ptr<FftPlan>> plans;
     DeviceBuffer staging;  // FP64 upload staging
     DeviceBuffer scratch_a, scratch_b;
+    cudaMemPool_t pool = nullptr;  // problem buffers: stream-ordered, memory kept for reuse
     fpm_run_stats stats = {};
 };
 
@@ -113,6 +198,10 @@ struct fpm_problem {
     std::vector<double> off_row, off_col, kx, ky, gains, weights, data_snr;
     std::vector<uint8_t> support;
     std::vector<double> pupil;  // complex128 interleaved
+    std::vector<double> upload_gains;  // host sources of asynchronous uploads
+    std::vector<float2> pupil_f32;
+    int host_status = 0;                // result downloads
+    std::vector<double> host_partials;
     std::vector<fpm::FrameParam> params;
     std::vector<double> stencil_cells;  // per frame: rows * cols of the bilinear stencil
     bool has_masks = false, has_background = false;
@@ -415,61 +504,19 @@ Status validate_model(const fpm_model_desc* md) {
     return Status::ok();
 }
 
-// Runs fn(frame) for every frame on the host's hardware threads.
-template <class Fn>
-void parallel_frames(int frames, Fn fn) {
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int workers = std::min(hw, frames);
-    if (workers <= 1) {
-        for (int f = 0; f < frames; ++f) fn(f);
-        return;
-    }
-    std::atomic<int> next(0);
-    std::vector<std::thread> pool;
-    for (int w = 0; w < workers; ++w)
-        pool.emplace_back([&]() {
-            for (int f; (f = next.fetch_add(1)) < frames;) fn(f);
-        });
-    for (auto& t : pool) t.join();
-}
-
-Status validate_measurements(const fpm_model_desc* md, const fpm_measurement_desc* ms) {
+// Header checks of a measurement stack that need no pass over the pixels.
+Status check_measurement_header(const fpm_model_desc* md, const fpm_measurement_desc* ms) {
     if (!ms || !ms->measurements) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements are required");
     if (ms->frames != md->sources)
         return Status::make(FPM_ERR_INVALID_MODEL, "%d measurement frames but %d model frames", ms->frames, md->sources);
-    const size_t n = (size_t)md->image_height * md->image_width;
-    std::vector<uint8_t> bad(ms->frames, 0);
-    parallel_frames(ms->frames, [&](int f) {
-        const double* m = ms->measurements + (size_t)f * n;
-        bool ok = true;
-        for (size_t i = 0; i < n; ++i) ok &= std::isfinite(m[i]);
-        bad[f] = ok ? 0 : 1;
-    });
-    for (int f = 0; f < ms->frames; ++f)
-        if (bad[f]) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
     int positive = 0;
     for (int f = 0; f < ms->frames; ++f) {
         const double wgt = ms->frame_weights ? ms->frame_weights[f] : 1.0;
         if (!std::isfinite(wgt) || wgt < 0.0)
             return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "frame %d has invalid weight %g", f, wgt);
-        if (wgt > 0.0) {
-            ++positive;
-            if (ms->masks) {
-                const uint8_t* m = ms->masks + (size_t)f * n;
-                bool any = false;
-                for (size_t i = 0; i < n && !any; ++i) any = m[i] != 0;
-                if (!any)
-                    return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "positive-weight frame %d has no unmasked pixels", f);
-            }
-        }
+        if (wgt > 0.0) ++positive;
     }
     if (positive == 0) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "at least one frame must have positive weight");
-    return Status::ok();
-}
-
-Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_measurement_desc* ms, fpm_problem** out) {
-    FPM_TRY(validate_model(md));
-    FPM_TRY(validate_measurements(md, ms));
     const int h = md->image_height, w = md->image_width;
     if (h != w || !fpm::engine_supported(h))
         return Status::make(FPM_ERR_UNSUPPORTED,
@@ -477,13 +524,64 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
                             h, w);
     if (md->recon_height != md->recon_width)
         return Status::make(FPM_ERR_UNSUPPORTED, "the GB300 device path supports square reconstruction grids");
+    return Status::ok();
+}
+
+// One pass over a frame's pixels: finiteness, the unmasked count, and the
+// snr_weighted score weight * sqrt(mean over unmasked pixels of
+// max(I - background, 0)) (src/reconstruction/schedule.rs:104-128), summed in
+// pixel order.
+struct FrameScan {
+    bool finite = true, any_unmasked = true;
+    long long valid = 0;
+    double snr = 0.0;
+};
+
+void scan_frame(const fpm_model_desc* md, const fpm_measurement_desc* ms, int f, FrameScan& out) {
+    const size_t n2 = (size_t)md->image_height * md->image_width;
+    const double* m = ms->measurements + (size_t)f * n2;
+    const uint8_t* mk = ms->masks ? ms->masks + (size_t)f * n2 : nullptr;
+    const double weight = ms->frame_weights ? ms->frame_weights[f] : 1.0;
+    const long long bg_stride = (md->background && md->background_len != (int64_t)n2) ? (long long)n2 : 0;
+    const double* bg = md->background ? md->background + (size_t)f * bg_stride : nullptr;
+    bool finite = true;
+    long long valid = 0;
+    double sum = 0.0;
+    for (size_t i = 0; i < n2; ++i) {
+        const double v = m[i];
+        finite &= std::isfinite(v);
+        if (mk && mk[i] == 0) continue;
+        ++valid;
+        sum += std::max(v - (bg ? bg[i] : 0.0), 0.0);
+    }
+    out.finite = finite;
+    out.valid = valid;
+    out.any_unmasked = valid > 0;
+    out.snr = weight == 0.0 || valid == 0 ? -INFINITY : weight * std::sqrt(sum / (double)valid);
+}
+
+Status check_scans(const fpm_measurement_desc* ms, const FrameScan* scans) {
+    for (int f = 0; f < ms->frames; ++f)
+        if (!scans[f].finite) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
+    for (int f = 0; f < ms->frames; ++f) {
+        const double wgt = ms->frame_weights ? ms->frame_weights[f] : 1.0;
+        if (wgt > 0.0 && ms->masks && !scans[f].any_unmasked)
+            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "positive-weight frame %d has no unmasked pixels", f);
+    }
+    return Status::ok();
+}
+
+// Host part of a problem: copies of the model and the frame constants.
+Status prepare_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_measurement_desc* ms,
+                       const FrameScan* scans, std::unique_ptr<fpm_problem>& out) {
     auto p = std::make_unique<fpm_problem>();
     p->ctx = ctx;
-    p->n = h;
+    p->n = md->image_height;
     p->m = md->recon_height;
     p->frames = ms->frames;
-    const int N = h, F = ms->frames;
+    const int N = p->n, F = ms->frames;
     const size_t n2 = (size_t)N * N;
+    const bool masks = ms->masks != nullptr;
     p->start_row.assign(md->crop_start_row, md->crop_start_row + F);
     p->start_col.assign(md->crop_start_col, md->crop_start_col + F);
     p->off_row.assign(F, 0.0);
@@ -500,40 +598,16 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
     if (ms->frame_weights) p->weights.assign(ms->frame_weights, ms->frame_weights + F);
     p->support.assign(md->support, md->support + n2);
     p->pupil.assign(md->pupil, md->pupil + 2 * n2);
-    p->has_masks = ms->masks != nullptr;
+    p->has_masks = masks;
     p->has_background = md->background != nullptr;
     p->background_stride = (md->background && md->background_len != (int64_t)n2) ? (long long)n2 : 0;
+    p->amplitude = md->background == nullptr;
 
     // Frame constants (FP64 on the host, rounded once).
     p->params.resize(F);
     p->stencil_cells.resize(F);
-    p->data_snr.assign(F, 0.0);
-    // Per-frame unmasked counts and snr_weighted scores
-    // (src/reconstruction/schedule.rs:104-128), computed in parallel.
-    std::vector<long long> valid_counts(F, (long long)n2);
-    parallel_frames(F, [&](int f) {
-        if (ms->masks) {
-            long long valid = 0;
-            const uint8_t* mk = ms->masks + (size_t)f * n2;
-            for (size_t i = 0; i < n2; ++i) valid += mk[i] != 0;
-            valid_counts[f] = valid;
-        }
-        if (p->weights[f] == 0.0) {
-            p->data_snr[f] = -INFINITY;
-            return;
-        }
-        const double* m = ms->measurements + (size_t)f * n2;
-        double sum = 0.0;
-        long long cnt = 0;
-        for (size_t i = 0; i < n2; ++i) {
-            if (ms->masks && ms->masks[(size_t)f * n2 + i] == 0) continue;
-            double bg = 0.0;
-            if (md->background) bg = md->background[p->background_stride ? (size_t)f * n2 + i : i];
-            sum += std::max(m[i] - bg, 0.0);
-            ++cnt;
-        }
-        p->data_snr[f] = cnt == 0 ? -INFINITY : p->weights[f] * std::sqrt(sum / (double)cnt);
-    });
+    p->data_snr.resize(F);
+    for (int f = 0; f < F; ++f) p->data_snr[f] = scans[f].snr;
     for (int f = 0; f < F; ++f) {
         Axis r{}, c{};
         FPM_TRY(interpolation_axis(p->start_row[f], N, p->m, p->off_row[f], r));
@@ -560,7 +634,7 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
             fp.w11 = (float)(r.upper_weight * c.upper_weight);
         }
         p->stencil_cells[f] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
-        const long long valid = valid_counts[f];
+        const long long valid = masks ? scans[f].valid : (long long)n2;
         fp.weight = (float)p->weights[f];
         if (p->weights[f] > 0.0 && !(p->gains[f] > 0.0))
             return Status::make(FPM_ERR_INVALID_MODEL, "state frame %d has invalid gain %g", f, p->gains[f]);
@@ -571,21 +645,34 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
         p->weight_sum += p->weights[f];
     }
 
-    cudaStream_t s = ctx->streams[0];
+    out = std::move(p);
+    return Status::ok();
+}
+
+// Device part: allocations from the context's pool and uploads on stream s.
+// The context's staging buffers are reused, so the previous upload is waited
+// for first; host vectors copied from live in the problem.
+Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md, const fpm_measurement_desc* ms,
+                      cudaStream_t s) {
+    const int N = p->n, F = p->frames;
+    const size_t n2 = (size_t)N * N;
+    FPM_CUDA(cudaStreamSynchronize(s));
+    for (DeviceBuffer* b : {&p->meas, &p->masks, &p->background, &p->frame_params, &p->support_d, &p->pupil_ref,
+                            &p->pupil_model})
+        b->bind(ctx->pool, s);
     // Measurements: FP64 upload, permuted to the engine's FP32 layout. With no
     // background the engine reads the amplitude form sqrt(max(I / g, 0))
     // (computed in FP64, -1 on masked pixels): one float per pixel, no mask
     // bytes, and no divide or square root in the frame loop.
     const size_t total = n2 * F;
-    p->amplitude = md->background == nullptr;
     FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
     FPM_TRY(p->meas.ensure(total * sizeof(float)));
     FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
     if (p->amplitude) {
-        std::vector<double> gains(F);
-        for (int f = 0; f < F; ++f) gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
+        p->upload_gains.resize(F);
+        for (int f = 0; f < F; ++f) p->upload_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
         FPM_TRY(ctx->scratch_b.ensure(F * sizeof(double)));
-        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, p->upload_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
         if (ms->masks) {
             FPM_TRY(ctx->scratch_a.ensure(total));
             FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
@@ -593,8 +680,6 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
         FPM_CUDA(fpm::launch_permute_amplitude(N, ctx->staging.as<double>(),
                                                ms->masks ? ctx->scratch_a.as<uint8_t>() : nullptr,
                                                ctx->scratch_b.as<double>(), p->meas.as<float>(), F, s));
-        // The host vector must outlive the copy.
-        FPM_CUDA(cudaStreamSynchronize(s));
     } else {
         FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->meas.as<float>(), F, s));
         if (ms->masks) {
@@ -619,12 +704,60 @@ Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_meas
     FPM_CUDA(cudaMemcpyAsync(p->support_d.ptr, p->support.data(), n2, cudaMemcpyHostToDevice, s));
     FPM_TRY(p->pupil_ref.ensure(n2 * sizeof(double2)));
     FPM_CUDA(cudaMemcpyAsync(p->pupil_ref.ptr, p->pupil.data(), n2 * sizeof(double2), cudaMemcpyHostToDevice, s));
-    std::vector<float2> pf(n2);
+    std::vector<float2>& pf = p->pupil_f32;
+    pf.resize(n2);
     for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)p->pupil[2 * i], (float)p->pupil[2 * i + 1]);
     FPM_TRY(p->pupil_model.ensure(n2 * sizeof(float2)));
     FPM_CUDA(cudaMemcpyAsync(p->pupil_model.ptr, pf.data(), n2 * sizeof(float2), cudaMemcpyHostToDevice, s));
+    return Status::ok();
+}
+
+Status create_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_measurement_desc* ms, fpm_problem** out) {
+    FPM_TRY(validate_model(md));
+    FPM_TRY(check_measurement_header(md, ms));
+    std::vector<FrameScan> scans(ms->frames);
+    HostPool::get().run(ms->frames, [&](long long f) { scan_frame(md, ms, (int)f, scans[f]); });
+    FPM_TRY(check_scans(ms, scans.data()));
+    std::unique_ptr<fpm_problem> p;
+    FPM_TRY(prepare_problem(ctx, md, ms, scans.data(), p));
+    cudaStream_t s = ctx->streams[0];
+    FPM_TRY(upload_problem(ctx, p.get(), md, ms, s));
     FPM_CUDA(cudaStreamSynchronize(s));
     *out = p.release();
+    return Status::ok();
+}
+
+// Many problems at once: every frame of every problem is scanned in one pass
+// over the host threads, then all uploads are queued and synchronised once.
+Status create_problems(fpm_context* ctx, int count, const fpm_model_desc* mds, const fpm_measurement_desc* mss,
+                       std::vector<std::unique_ptr<fpm_problem>>& made) {
+    std::vector<long long> first(count + 1, 0);
+    for (int i = 0; i < count; ++i) {
+        Status st = validate_model(&mds[i]);
+        if (!st) st = check_measurement_header(&mds[i], &mss[i]);
+        if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+        first[i + 1] = first[i] + mss[i].frames;
+    }
+    std::vector<FrameScan> scans(first[count]);
+    std::vector<int> owner(first[count]);
+    for (int i = 0; i < count; ++i)
+        for (long long k = first[i]; k < first[i + 1]; ++k) owner[k] = i;
+    HostPool::get().run(first[count], [&](long long k) {
+        const int i = owner[k];
+        scan_frame(&mds[i], &mss[i], (int)(k - first[i]), scans[k]);
+    });
+    made.resize(count);
+    size_t staging = 0;
+    for (int i = 0; i < count; ++i) {
+        Status st = check_scans(&mss[i], scans.data() + first[i]);
+        if (!st) st = prepare_problem(ctx, &mds[i], &mss[i], scans.data() + first[i], made[i]);
+        if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+        staging = std::max(staging, (size_t)mds[i].image_height * mds[i].image_width * mss[i].frames * sizeof(double));
+    }
+    cudaStream_t s = ctx->streams[0];
+    FPM_TRY(ctx->staging.ensure(staging));
+    for (int i = 0; i < count; ++i) FPM_TRY(upload_problem(ctx, made[i].get(), &mds[i], &mss[i], s));
+    FPM_CUDA(cudaStreamSynchronize(s));
     return Status::ok();
 }
 
@@ -744,6 +877,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     for (int t = 0; t < count; ++t) {
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
+        for (DeviceBuffer* buf : {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
+                                  &p->avg, &p->init_partial, &p->velocity, &p->anchor, &p->order})
+            buf->bind(ctx->pool, s);
         FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
         FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
         FPM_TRY(p->partials.ensure(sizeof(double) * std::max(iters, 1) * C));
@@ -776,6 +912,17 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.support = p->support_d.as<uint8_t>();
         T.meas = p->meas.as<float>();
         T.amplitude = p->amplitude ? 1 : 0;
+        // Centred rows holding a non-zero (FP32) pupil value.
+        T.row_lo = N;
+        T.row_hi = -1;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                const float2 v = p->pupil_f32[(size_t)i * N + j];
+                if (v.x != 0.f || v.y != 0.f) {
+                    T.row_lo = std::min(T.row_lo, i);
+                    T.row_hi = std::max(T.row_hi, i);
+                }
+            }
         T.masks = p->has_masks && !p->amplitude ? p->masks.as<uint8_t>() : nullptr;
         T.background = p->has_background ? p->background.as<float>() : nullptr;
         T.background_stride = p->background_stride;
@@ -909,50 +1056,46 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     return Status::ok();
 }
 
-Status collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_desc* r, cudaStream_t s) {
-    int status = 0;
-    FPM_CUDA(cudaMemcpyAsync(&status, p->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    FPM_CUDA(cudaStreamSynchronize(s));
+// Queues one problem's result downloads on stream s: complex64 state is
+// widened to complex128 on the device and copied straight into the caller's
+// arrays. The status word and objective partials land in the problem's host
+// vectors for finish_collect, after the stream is synchronised.
+Status queue_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_desc* r, cudaStream_t s) {
+    p->host_status = 0;
+    FPM_CUDA(cudaMemcpyAsync(&p->host_status, p->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!r) return Status::ok();
+    const int M = p->m, N = p->n, C = N / 32;
+    const long long ms = M + (M & 1);
+    double2* wide = p->scratch64.as<double2>();  // M * M complex128; holds the natural FP64 object first
+    if (r->object)
+        FPM_CUDA(cudaMemcpyAsync(r->object, wide, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+    if (r->object_spectrum) {
+        FPM_CUDA(fpm::launch_widen(p->object.as<float2>(), ms, M, M, wide, s));
+        FPM_CUDA(cudaMemcpyAsync(r->object_spectrum, wide, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+    }
+    if (r->pupil) {
+        FPM_CUDA(fpm::launch_widen(p->pupil_state.as<float2>(), N, N, N, wide, s));
+        FPM_CUDA(cudaMemcpyAsync(r->pupil, wide, sizeof(double2) * (size_t)N * N, cudaMemcpyDeviceToHost, s));
+    }
+    if (r->objectives && a->iterations > 0) {
+        p->host_partials.resize((size_t)a->iterations * C);
+        FPM_CUDA(cudaMemcpyAsync(p->host_partials.data(), p->partials.ptr, sizeof(double) * p->host_partials.size(),
+                                 cudaMemcpyDeviceToHost, s));
+    }
+    return Status::ok();
+}
+
+Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_desc* r) {
+    const int status = p->host_status;
     if (status & 4) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "no positive-weight, unmasked measurements are available");
     if (status & 1) return Status::make(FPM_ERR_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
     if (status & 8) return Status::make(FPM_ERR_NUMERICAL, "object/pupil gauge normalization failed on a non-finite or empty state");
     if (!r) return Status::ok();
-    const int M = p->m, N = p->n, C = N / 32;
-    const long long ms = M + (M & 1);
-    if (r->object)
-        FPM_CUDA(cudaMemcpyAsync(r->object, p->scratch64.ptr, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
-    std::vector<float2> spec;
-    if (r->object_spectrum) {
-        spec.resize((size_t)M * ms);
-        FPM_CUDA(cudaMemcpyAsync(spec.data(), p->object.ptr, sizeof(float2) * spec.size(), cudaMemcpyDeviceToHost, s));
-    }
-    std::vector<float2> pupil;
-    if (r->pupil) {
-        pupil.resize((size_t)N * N);
-        FPM_CUDA(cudaMemcpyAsync(pupil.data(), p->pupil_state.ptr, sizeof(float2) * pupil.size(), cudaMemcpyDeviceToHost, s));
-    }
-    std::vector<double> partials;
-    if (r->objectives && a->iterations > 0) {
-        partials.resize((size_t)a->iterations * C);
-        FPM_CUDA(cudaMemcpyAsync(partials.data(), p->partials.ptr, sizeof(double) * partials.size(), cudaMemcpyDeviceToHost, s));
-    }
-    FPM_CUDA(cudaStreamSynchronize(s));
-    if (r->object_spectrum)
-        for (int row = 0; row < M; ++row)
-            for (int col = 0; col < M; ++col) {
-                const float2 v = spec[(size_t)row * ms + col];
-                r->object_spectrum[2 * ((size_t)row * M + col)] = v.x;
-                r->object_spectrum[2 * ((size_t)row * M + col) + 1] = v.y;
-            }
-    if (r->pupil)
-        for (size_t i = 0; i < pupil.size(); ++i) {
-            r->pupil[2 * i] = pupil[i].x;
-            r->pupil[2 * i + 1] = pupil[i].y;
-        }
+    const int C = p->n / 32;
     if (r->objectives)
         for (int it = 0; it < a->iterations; ++it) {
             double sum = 0.0;
-            for (int c = 0; c < C; ++c) sum += partials[(size_t)it * C + c];
+            for (int c = 0; c < C; ++c) sum += p->host_partials[(size_t)it * C + c];
             r->objectives[it] = p->weight_sum > 0.0 ? sum / p->weight_sum : NAN;
         }
     r->completed_iterations = a->iterations;
@@ -1032,9 +1175,15 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
             const int idx = buckets[k].indices[t];
-            FPM_TRY(collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr, s));
+            FPM_TRY(queue_collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr, s));
         }
     }
+    for (size_t k = 0; k < buckets.size(); ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
+    for (size_t k = 0; k < buckets.size(); ++k)
+        for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
+            const int idx = buckets[k].indices[t];
+            FPM_TRY(finish_collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr));
+        }
     return Status::ok();
 }
 
@@ -1077,6 +1226,16 @@ int32_t fpm_create(fpm_context** out, int32_t device) {
                                 device, prop.name, prop.major, prop.minor);
         for (int i = 0; i < fpm_context::kStreams; ++i)
             FPM_CUDA(cudaStreamCreateWithFlags(&ctx->streams[i], cudaStreamNonBlocking));
+        // Problem buffers come from a private stream-ordered pool that keeps
+        // freed memory for the next problems instead of returning it.
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        FPM_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+        uint64_t threshold = ~0ull;
+        FPM_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &threshold));
         return Status::ok();
     };
     Status s = init();
@@ -1089,7 +1248,12 @@ int32_t fpm_destroy(fpm_context* ctx) {
     if (!ctx) return FPM_OK;
     cudaSetDevice(ctx->device);
     for (int i = 0; i < fpm_context::kStreams; ++i)
+        if (ctx->streams[i]) cudaStreamSynchronize(ctx->streams[i]);
+    for (int i = 0; i < fpm_context::kStreams; ++i)
         if (ctx->streams[i]) cudaStreamDestroy(ctx->streams[i]);
+    // Outstanding pooled allocations (problems not yet destroyed) keep the
+    // pool's memory until they are freed.
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
     return FPM_OK;
 }
@@ -1327,6 +1491,23 @@ int32_t fpm_problem_create(fpm_context* ctx, const fpm_model_desc* model, const 
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
     return finish(ctx, create_problem(ctx, model, measurements, problem));
+}
+
+int32_t fpm_problem_create_batch(fpm_context* ctx, int32_t count, const fpm_model_desc* models,
+                                 const fpm_measurement_desc* measurements, fpm_problem** problems) {
+    if (!ctx || count < 0 || (count > 0 && (!models || !measurements || !problems)))
+        return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument or negative count"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    for (int i = 0; i < count; ++i) problems[i] = nullptr;
+    std::vector<std::unique_ptr<fpm_problem>> made;
+    Status s = create_problems(ctx, count, models, measurements, made);
+    if (s) {
+        made.clear();
+        return finish(ctx, s);
+    }
+    for (int i = 0; i < count; ++i) problems[i] = made[i].release();
+    return finish(ctx, s);
 }
 
 int32_t fpm_problem_destroy(fpm_problem* problem) {

@@ -74,16 +74,20 @@ class ReconstructionProblem:
     def reconstruction_shape(self):
         return self.model.reconstruction_shape
 
+    def _descriptors(self):
+        desc, keep = self.model._descriptor()
+        m = N.MeasurementDesc()
+        m.frames = self.measurements.frame_count
+        m.measurements = N.ptr(self.measurements._data, C.c_double)
+        m.frame_weights = N.ptr(self.measurements._weights, C.c_double)
+        m.masks = N.ptr(self.measurements._masks, C.c_uint8)
+        return desc, m, keep
+
     def device_handle(self):
         """Uploads the problem (once) and returns its opaque device handle."""
         if self._handle is None:
             ctx = N.context()
-            desc, keep = self.model._descriptor()
-            m = N.MeasurementDesc()
-            m.frames = self.measurements.frame_count
-            m.measurements = N.ptr(self.measurements._data, C.c_double)
-            m.frame_weights = N.ptr(self.measurements._weights, C.c_double)
-            m.masks = N.ptr(self.measurements._masks, C.c_uint8)
+            desc, m, keep = self._descriptors()
             handle = C.c_void_p()
             N.check(N.library().fpm_problem_create(ctx.handle, C.byref(desc), C.byref(m), C.byref(handle)),
                     ctx.handle)
@@ -290,6 +294,31 @@ class GradientDescent(_Algorithm):
         return p
 
 
+def upload(problems) -> None:
+    """Uploads every problem that has no device handle yet in one batched call
+    (one parallel validation pass over all frames, one synchronisation)."""
+    pending = []
+    seen = set()
+    for p in problems:
+        if p._handle is None and id(p) not in seen:
+            seen.add(id(p))
+            pending.append(p)
+    if not pending:
+        return
+    if len(pending) == 1:
+        pending[0].device_handle()
+        return
+    ctx = N.context()
+    descs = [p._descriptors() for p in pending]
+    models = (N.ModelDesc * len(pending))(*[d[0] for d in descs])
+    meas = (N.MeasurementDesc * len(pending))(*[d[1] for d in descs])
+    handles = (C.c_void_p * len(pending))()
+    N.check(N.library().fpm_problem_create_batch(ctx.handle, len(pending), models, meas, handles), ctx.handle)
+    for p, h in zip(pending, handles):
+        p._handle = C.c_void_p(h)
+        p._ctx = ctx
+
+
 def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=None, schedule="sequential",
               download=True):
     """Runs one algorithm over many independent problems in shared device launches.
@@ -305,6 +334,7 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
         raise UnsupportedError("checkpoint resume is not supported by the GB300 device path")
     params = algorithm._params(schedule)
     problems = list(problems)
+    upload(problems)
     handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
     ctx = N.context()
     results = (N.ResultDesc * len(problems))()

@@ -14,7 +14,8 @@
  *   ImagePlaneModel::compile ..... src/model/image_plane_fpm.rs:196-253 -> fpm_compile_model
  *   ForwardModel::forward_intensity_stack_into
  *                                  src/model/forward.rs:300-372 -> fpm_forward_stack
- *   ReconstructionProblem::new ... src/reconstruction/problem.rs:12-20 -> fpm_problem_create
+ *   ReconstructionProblem::new ... src/reconstruction/problem.rs:12-20 -> fpm_problem_create,
+ *                                  fpm_problem_create_batch (many problems, one host scan)
  *   Runner::run / ReconstructionAlgorithm::run
  *                                  src/reconstruction/runner.rs:76-285 -> fpm_run
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size)
@@ -180,6 +181,14 @@ int32_t fpm_forward_stack(fpm_context *ctx, const fpm_model_desc *model, const d
 int32_t fpm_problem_create(fpm_context *ctx, const fpm_model_desc *model,
                            const fpm_measurement_desc *measurements, fpm_problem **problem);
 int32_t fpm_problem_destroy(fpm_problem *problem);
+
+/* Creates `count` problems from parallel arrays of descriptors, as
+ * fpm_problem_create would one by one: every frame of every problem is
+ * validated in one pass over the host's threads, then all uploads run with a
+ * single final synchronisation. On error no problem is returned (all entries
+ * of `problems` are set to NULL) and the message names the failing index. */
+int32_t fpm_problem_create_batch(fpm_context *ctx, int32_t count, const fpm_model_desc *models,
+                                 const fpm_measurement_desc *measurements, fpm_problem **problems);
 
 /* Runs one reconstruction to completion (initialise, iterate, finalise). */
 int32_t fpm_run(fpm_context *ctx, fpm_problem *problem, const fpm_algorithm_params *params,

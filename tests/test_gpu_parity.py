@@ -143,6 +143,66 @@ def test_masks_weights_background(fpm):
         _objective_close([t[1] for t in result.trace], expected["objectives"])
 
 
+@pytest.mark.parametrize("n,side", [(32, 5), (128, 3)])
+def test_masks_and_weights_without_background(fpm, n, side):
+    """Masks with no background: the device keeps amplitudes, -1 on masked pixels.
+
+    Negative counts (possible after dark subtraction) must clamp to zero
+    amplitude exactly as max(I / g, 0) does in the reference."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=31, photons=3e3)
+    rng = np.random.default_rng(8)
+    masks = (rng.random(data.shape) > 0.2).astype(np.uint8)
+    data = data.copy()
+    data[1, :4, :4] = -2.0
+    weights = np.ones(data.shape[0])
+    weights[2] = 0.0
+    weights[4] = 0.25
+    for name, algo, kw in (("ap", fpm.AlternatingProjection(iterations=3), dict(iterations=3)),
+                           ("mpie", fpm.Mpie(iterations=3, momentum_interval=4), dict(iterations=3, momentum_interval=4)),
+                           ("gd", fpm.GradientDescent(iterations=3), dict(iterations=3))):
+        result, expected = _run_both(fpm, algo, name, kw, model, omodel, data, gains=gains, weights=weights,
+                                     masks=masks)
+        assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, name
+        _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
+def test_batched_upload_matches_single_uploads(fpm):
+    """fpm_problem_create_batch gives the same problems as one-by-one creation."""
+    cases = [helpers.simulated(fpm, side, n, seed=seed, photons=1e4)
+             for n, side, seed in ((32, 3, 11), (64, 3, 12), (32, 5, 13))]
+    algo = fpm.Fpie(iterations=2)
+    single = []
+    for model, _, data, _, _ in cases:
+        p = fpm.ReconstructionProblem(data, model)
+        p.device_handle()
+        single.append(algo.run(p).object)
+    batched = [fpm.ReconstructionProblem(data, model) for model, _, data, _, _ in cases]
+    results = fpm.run_batch(algo, batched)  # uploads all three in one batched call
+    for a, r in zip(single, results):
+        assert np.array_equal(a, r.object)
+
+
+def test_batched_upload_error_names_the_problem(fpm):
+    import ctypes as C
+    from fpm_rs import _native as N
+
+    model, _, data, _, _ = helpers.simulated(fpm, 3, 32, seed=14, photons=1e4)
+    problems = [fpm.ReconstructionProblem(data, model) for _ in range(3)]
+    descs = [p._descriptors() for p in problems]
+    bad = np.full(model.frame_count, -1.0)
+    descs[1][1].frame_weights = N.ptr(bad, C.c_double)
+    models = (N.ModelDesc * 3)(*[d[0] for d in descs])
+    meas = (N.MeasurementDesc * 3)(*[d[1] for d in descs])
+    handles = (C.c_void_p * 3)(1, 2, 3)
+    ctx = N.context()
+    status = N.library().fpm_problem_create_batch(ctx.handle, 3, models, meas, handles)
+    assert status == 4  # InvalidMeasurements
+    buf = C.create_string_buffer(512)
+    N.library().fpm_last_error(ctx.handle, buf, len(buf))
+    assert buf.value.decode().startswith("problem 1:")
+    assert all(h is None for h in handles)
+
+
 @pytest.mark.parametrize("schedule", ["brightfield_first", "spiral_out", "snr_weighted"])
 def test_schedules(fpm, schedule):
     model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=9, photons=1e4)
