@@ -12,6 +12,16 @@ extern template struct EngineEntry<256>;
 
 bool engine_supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
 
+int engine_ctas(int n) {
+    switch (n) {
+        case 32: return Cfg<32>::C;
+        case 64: return Cfg<64>::C;
+        case 128: return Cfg<128>::C;
+        case 256: return Cfg<256>::C;
+        default: return 0;
+    }
+}
+
 int init_chunks(int n) { return (n * n + kInitBlock - 1) / kInitBlock; }
 
 #define FPM_DISPATCH(call)                       \

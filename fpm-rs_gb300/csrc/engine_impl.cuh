@@ -37,7 +37,10 @@ namespace fpm {
 template <int N_>
 struct Cfg {
     static constexpr int N = N_;
-    static constexpr int R = 32;            // field rows per CTA
+    // Field rows per CTA. 256-point tiles use 16-row CTAs in 16-CTA
+    // clusters: about 107 KB of shared memory each, so two tiles' CTAs share
+    // an SM and hide each other's barrier and exchange latency.
+    static constexpr int R = N == 256 ? 16 : 32;
     static constexpr int C = N / R;         // CTAs per cluster
     static constexpr int NA = N >= 128 ? 16 : 8;
     static constexpr int NB = N / NA;
@@ -45,14 +48,16 @@ struct Cfg {
     // stride chosen so that half-warps spanning two rows hit disjoint banks.
     static constexpr int RS = N == 32 ? 40 : N == 64 ? 72 : N == 128 ? 152 : 272;
     static constexpr int ORS = N + 2;       // staged stencil row: N + 2 columns from an even origin
-    static constexpr int THREADS = 2 * N;   // two threads per column position in P4 (lanes l, l ^ 16)
+    // P4 column transforms: R = 32 splits each column over two threads
+    // (lanes l, l ^ 16); R = 16 gives each column one thread.
+    static constexpr int THREADS = R == 32 ? 2 * N : N;
     static constexpr int WARPS = THREADS / 32;
     // Resident CTAs per SM that shared memory allows; registers are capped to match.
-    static constexpr int MIN_BLOCKS = N == 256 ? 1 : N == 128 ? 2 : N == 64 ? 4 : 7;
+    static constexpr int MIN_BLOCKS = N == 256 ? 2 : N == 128 ? 2 : N == 64 ? 4 : 7;
     static constexpr int TW = 256 / N;      // w_N^k = w_256^(k * TW)
     static constexpr int FIELD = (R + 1) * RS;  // raw row 0: halo U row from the previous CTA
     static constexpr int STAGE = (R + 1) * ORS;
-    static constexpr int PSLAB = R * N;     // this CTA's 32 centred pupil rows
+    static constexpr int PSLAB = R * N;     // this CTA's R centred pupil rows
     static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + 64 * 8 + 64 * 4;
     static constexpr int T1 = R * NB / THREADS;      // P1 / P7 tasks per thread
     static constexpr int T2 = R * NA / THREADS;      // P2 / P6 tasks per thread
@@ -60,8 +65,9 @@ struct Cfg {
     static constexpr int PAIRS = N / 2 + 1;          // 16-byte pairs per staged row
     static_assert(N == 32 || N == 64 || N == 128 || N == 256, "unsupported tile size");
     static_assert(RS >= N + NA && RS % 2 == 0, "row stride");
+    static_assert(R % C == 0 && (R == 32 || R == 16) && (C == 1 || R * C == N), "cluster split");
     static_assert(T1 * THREADS == R * NB && T2 * THREADS == R * NA && TX * THREADS == (R / C) * N, "tasks");
-    static_assert(SMEM_BYTES <= 232448, "shared memory");
+    static_assert(SMEM_BYTES * MIN_BLOCKS + 1024 * MIN_BLOCKS <= 233472, "shared memory");
 };
 
 template <class K>
@@ -238,7 +244,7 @@ FPM_DEVICE void columns_cross_inverse(float2* __restrict__ fld, const float2* __
             float2 v[C];
 #pragma unroll
             for (int nc = 0; nc < C; ++nc) {
-                // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * 32 + l.
+                // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * R + l.
                 const int i = (nc ^ (C / 2)) * K::R + l;
                 v[nc] = i >= row_lo && i <= row_hi ? dsmem_load(base[nc ^ (C / 2)] + off) : make_float2(0.f, 0.f);
             }
@@ -326,6 +332,25 @@ FPM_DEVICE void column_forward_split(float2* __restrict__ fld, int pq, int h, in
         fld[row * K::RS + pq] = lo;
         fld[(row + 16) * K::RS + pq] = hi;
     }
+}
+
+// P4 column transforms for 16-row CTAs: one thread per column position,
+// the 16 local rows in registers. Inverse: z[m] = sum_l X[l] w_16^{+lm}
+// (spatial row c + C * m). Forward: the 16-point DFT, then the cluster
+// twiddle w_N^(-c * b) on local row b ahead of the cross-CTA step.
+template <class K>
+FPM_DEVICE void column_inverse_local(const float2* __restrict__ fld, int pq, float2 (&z)[16]) {
+#pragma unroll
+    for (int l = 0; l < 16; ++l) z[l] = fld[l * K::RS + pq];
+    dft_reg<16, true>(z);
+}
+
+template <class K>
+FPM_DEVICE void column_forward_local(float2* __restrict__ fld, int pq, int c, const float2* __restrict__ tw,
+                                     float2 (&z)[16]) {
+    dft_reg<16, false>(z);
+#pragma unroll
+    for (int b = 0; b < 16; ++b) fld[b * K::RS + pq] = K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b];
 }
 
 template <class K>
@@ -430,34 +455,39 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P3
             if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
-            // Measurement prefetch for P4, issued before the barrier so its
-            // latency overlaps the wait.
-            // P4 ownership: column position q, half h (rows h + 2k of the spatial column).
-            const int q4 = (warp << 4) | (lane & 15), h4 = lane >> 4;
-            float mreg[16];
-            unsigned mbits = 0xffffu;
-            {
-                const size_t off = (size_t)f * N * N + (size_t)(c * 32 + h4) * N + q4;
-#pragma unroll
-                for (int k = 0; k < 16; ++k) mreg[k] = __ldcs(T.meas + off + (size_t)(2 * k) * N);
-                if (T.masks) {
-                    mbits = 0u;
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)(2 * k) * N] != 0 ? 1u : 0u) << k;
-                }
-            }
+            // P4 ownership. R = 32: column position q4, half h4, slot k =
+            // local spatial row h4 + 2k. R = 16: column position tid, slot k =
+            // local row k. Local row m of CTA c is spatial row c + C * m, and
+            // the engine layout stores it at (c * R + m) * N + q.
+            const int q4 = R == 32 ? (warp << 4) | (lane & 15) : tid, h4 = R == 32 ? lane >> 4 : 0;
+            const int mbase = (c * R + h4) * N + q4;
+            constexpr int mstride = R == 32 ? 2 * N : N;
 
             if constexpr (C > 1) cluster_barrier<K>();
 
             // P4: column inverse FFT, projection, column forward FFT.
             {
-                const float* brow = T.background ? T.background + (size_t)f * T.background_stride +
-                                                       (size_t)(c * 32 + h4) * N + q4
-                                                 : nullptr;
+                const float* brow =
+                    T.background ? T.background + (size_t)f * T.background_stride + mbase : nullptr;
                 const float gain = fp.gain, inv_gain = 1.0f / fp.gain;
                 const int pq = phys<K>(q4);
                 float2 v[16];
-                column_inverse_split<K>(fld, pq, h4, tw, v);
+                if constexpr (R == 32) column_inverse_split<K>(fld, pq, h4, tw, v);
+                else column_inverse_local<K>(fld, pq, v);
+                // Measurements are loaded next to their use: a prefetch ahead
+                // of the cluster barrier measured slower.
+                float mreg[16];
+                unsigned mbits = 0xffffu;
+                {
+                    const size_t off = (size_t)f * N * N + mbase;
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) mreg[k] = __ldcs(T.meas + off + (size_t)k * mstride);
+                    if (T.masks) {
+                        mbits = 0u;
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)k * mstride] != 0 ? 1u : 0u) << k;
+                    }
+                }
                 float frame_loss = 0.f;
                 if (T.amplitude) {
                     // a = sqrt(max(I / g, 0)), -1 where masked; with no
@@ -498,7 +528,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     for (int k = 0; k < 16; ++k) {
                         const float meas = mreg[k];
                     const bool masked = ((mbits >> k) & 1u) == 0u;
-                    const float bg = brow ? __ldg(brow + 2 * k * N) : 0.f;
+                    const float bg = brow ? __ldg(brow + k * mstride) : 0.f;
                     const float intrinsic = cnorm2(v[k]);
                     const float target = fmaxf((meas - bg) * inv_gain, 0.f);
                     if constexpr (projection) {
@@ -517,7 +547,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                     }
                 }
-                column_forward_split<K>(fld, pq, h4, c, tw, v);
+                if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
+                else column_forward_local<K>(fld, pq, c, tw, v);
                 loss_acc += (double)frame_loss * fp.loss_scale;
             }
             cluster_barrier<K>();
@@ -769,14 +800,15 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const Forward
     const float* bg = P.background ? P.background + (size_t)f * P.background_stride : nullptr;
     {
         const int warp = tid >> 5, lane = tid & 31;
-        const int q = (warp << 4) | (lane & 15), h = lane >> 4;
+        const int q = R == 32 ? (warp << 4) | (lane & 15) : tid, h = R == 32 ? lane >> 4 : 0;
         float2 v[16];
-        column_inverse_split<K>(fld, phys<K>(q), h, tw, v);
+        if constexpr (R == 32) column_inverse_split<K>(fld, phys<K>(q), h, tw, v);
+        else column_inverse_local<K>(fld, phys<K>(q), v);
         const int ka = q / NB, kb = q % NB;
         const int x = ka + NA * kb;
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-            const int y = c + C * (h + 2 * k);
+            const int y = c + C * (R == 32 ? h + 2 * k : k);
             const float b0 = bg ? bg[y * N + x] : 0.f;
             out[y * N + x] = fmaf(fp.gain, cnorm2(v[k]), b0);
         }
@@ -787,9 +819,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const Forward
 // Natural (y, x) -> engine layout index within one frame.
 template <class K>
 FPM_DEVICE int perm_index(int y, int x) {
-    const int c = y % K::C, k2 = y / K::C;
+    const int c = y % K::C, m = y / K::C;  // CTA c holds spatial rows c + C * m
     const int ka = x % K::NA, kb = x / K::NA;
-    return (c * 32 + k2) * K::N + K::NB * ka + kb;
+    return (c * K::R + m) * K::N + K::NB * ka + kb;
 }
 
 template <int N_>
@@ -913,6 +945,11 @@ cudaError_t launch_cluster(Kern kernel, const Params& p, int clusters, cudaStrea
     using K = Cfg<N_>;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM_BYTES);
     if (e != cudaSuccess) return e;
+    if constexpr (K::C > 8) {
+        // 16-CTA clusters are beyond the portable size of 8.
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(clusters * K::C);
     cfg.blockDim = dim3(K::THREADS);

@@ -79,6 +79,8 @@ struct ForwardParams {
 };
 
 bool engine_supported(int n);
+// CTAs in the thread-block cluster that reconstructs one n x n tile.
+int engine_ctas(int n);
 cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t s);
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
 

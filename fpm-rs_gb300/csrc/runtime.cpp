@@ -862,7 +862,7 @@ struct BucketRun {
 
 Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cudaStream_t s, BucketRun& br) {
     const int N = b.n, M = b.m, count = (int)b.problems.size();
-    const int C = N / 32;
+    const int C = fpm::engine_ctas(N);
     const long long ms = M + (M & 1);
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     const bool epry = a->algorithm == FPM_ALG_EPRY;
@@ -1064,7 +1064,7 @@ Status queue_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_d
     p->host_status = 0;
     FPM_CUDA(cudaMemcpyAsync(&p->host_status, p->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
     if (!r) return Status::ok();
-    const int M = p->m, N = p->n, C = N / 32;
+    const int M = p->m, N = p->n, C = fpm::engine_ctas(N);
     const long long ms = M + (M & 1);
     double2* wide = p->scratch64.as<double2>();  // M * M complex128; holds the natural FP64 object first
     if (r->object)
@@ -1091,7 +1091,7 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 1) return Status::make(FPM_ERR_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
     if (status & 8) return Status::make(FPM_ERR_NUMERICAL, "object/pupil gauge normalization failed on a non-finite or empty state");
     if (!r) return Status::ok();
-    const int C = p->n / 32;
+    const int C = fpm::engine_ctas(p->n);
     if (r->objectives)
         for (int it = 0; it < a->iterations; ++it) {
             double sum = 0.0;
