@@ -40,6 +40,11 @@ SIZES = (32, 64, 128, 256)
 LED_SIDE = 15
 PHOTONS = 1e4
 L2_BYTES = 129 * 1024 * 1024
+# Measured DRAM bytes (read + write) of engine_kernel per tile and mPIE
+# iteration, by tile size: ncu dram__bytes_read.sum + dram__bytes_write.sum
+# of the four engine launches of a 64-tile run (profiles/engine_dram_traffic_64tiles.txt).
+# roofline.traffic scales them by this run's tile counts and iterations.
+DRAM_BYTES_PER_TILE_ITERATION = {256: 243.49e6, 128: 21.97e6, 64: 0.881e6, 32: 0.040e6}
 
 
 def parse():
@@ -378,7 +383,9 @@ def run_ours(args):
             "peak": peak,
             "unit": "GB/s",
             "frac": achieved / peak if achieved else None,
-            "traffic": None,
+            "traffic": sum(DRAM_BYTES_PER_TILE_ITERATION[n] for n in sizes) * args.iterations,
+            "traffic_note": "DRAM bytes per step, all engine launches: ncu per tile-iteration figures of a "
+                            "64-tile capture scaled by this run's tiles and iterations",
             "kernel": "engine_kernel (all tile sizes, concurrent streams): algorithmic bytes / engine span",
             "peak_kind": peak_kind,
             "engine_launches_per_step": engine_launches // max(1, args.steps),
