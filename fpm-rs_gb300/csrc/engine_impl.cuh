@@ -37,10 +37,11 @@ namespace fpm {
 template <int N_>
 struct Cfg {
     static constexpr int N = N_;
-    // Field rows per CTA. 256-point tiles use 16-row CTAs in 16-CTA
-    // clusters: about 107 KB of shared memory each, so two tiles' CTAs share
-    // an SM and hide each other's barrier and exchange latency.
-    static constexpr int R = N == 256 ? 16 : 32;
+    // Field rows per CTA. 128- and 256-point tiles use 16-row CTAs (8- and
+    // 16-CTA clusters): about 56 KB and 108 KB of shared memory each, so four
+    // or two tiles' CTAs share an SM and hide each other's barrier and
+    // exchange latency.
+    static constexpr int R = N >= 128 ? 16 : 32;
     static constexpr int C = N / R;         // CTAs per cluster
     static constexpr int NA = N >= 128 ? 16 : 8;
     static constexpr int NB = N / NA;
@@ -53,12 +54,13 @@ struct Cfg {
     static constexpr int THREADS = R == 32 ? 2 * N : N;
     static constexpr int WARPS = THREADS / 32;
     // Resident CTAs per SM that shared memory allows; registers are capped to match.
-    static constexpr int MIN_BLOCKS = N == 256 ? 2 : N == 128 ? 2 : N == 64 ? 4 : 7;
+    static constexpr int MIN_BLOCKS = N == 256 ? 2 : N == 128 ? 4 : N == 64 ? 4 : 7;
     static constexpr int TW = 256 / N;      // w_N^k = w_256^(k * TW)
     static constexpr int FIELD = (R + 1) * RS;  // raw row 0: halo U row from the previous CTA
     static constexpr int STAGE = (R + 1) * ORS;
     static constexpr int PSLAB = R * N;     // this CTA's R centred pupil rows
-    static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + 64 * 8 + 64 * 4;
+    // + per-warp FP64 loss partials and the EPRY per-warp / per-CTA maxima.
+    static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + WARPS * 8 + (2 * WARPS + 2) * 4;
     static constexpr int T1 = R * NB / THREADS;      // P1 / P7 tasks per thread
     static constexpr int T2 = R * NA / THREADS;      // P2 / P6 tasks per thread
     static constexpr int TX = (R / C) * N / THREADS; // P3 / P5 tasks per thread
@@ -67,7 +69,8 @@ struct Cfg {
     static_assert(RS >= N + NA && RS % 2 == 0, "row stride");
     static_assert(R % C == 0 && (R == 32 || R == 16) && (C == 1 || R * C == N), "cluster split");
     static_assert(T1 * THREADS == R * NB && T2 * THREADS == R * NA && TX * THREADS == (R / C) * N, "tasks");
-    static_assert(SMEM_BYTES * MIN_BLOCKS + 1024 * MIN_BLOCKS <= 233472, "shared memory");
+    // Dynamic + static (descriptors, about 256 B) + 1 KB reserved per CTA.
+    static_assert((SMEM_BYTES + 256 + 1024) * MIN_BLOCKS <= 233472, "shared memory");
 };
 
 template <class K>
@@ -373,7 +376,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     float2* pslab = osm + K::STAGE;
     float2* tw = pslab + K::PSLAB;
     double* dred = reinterpret_cast<double*>(tw + 256);
-    float* fred = reinterpret_cast<float*>(dred + 64);
+    float* fred = reinterpret_cast<float*>(dred + K::WARPS);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tile = blockIdx.x / C;
