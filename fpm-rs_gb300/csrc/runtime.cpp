@@ -188,6 +188,7 @@ struct fpm_context {
     DeviceBuffer staging;  // FP64 upload staging
     DeviceBuffer scratch_a, scratch_b;
     cudaMemPool_t pool = nullptr;  // problem buffers: stream-ordered, memory kept for reuse
+    cudaStream_t upload = nullptr, download = nullptr;  // host-input batches: copies beside compute
     fpm_run_stats stats = {};
 };
 
@@ -212,7 +213,7 @@ struct fpm_problem {
     // resident device data
     DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
     // run state
-    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, avg, init_partial, order;
+    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order;
 };
 
 namespace {
@@ -848,7 +849,7 @@ Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) 
 }
 
 struct BucketRun {
-    DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs;
+    DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
     cudaEvent_t first = nullptr, last = nullptr;
     int launches = 0;
@@ -878,7 +879,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
         for (DeviceBuffer* buf : {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-                                  &p->avg, &p->init_partial, &p->velocity, &p->anchor, &p->order})
+                                  &p->velocity, &p->anchor, &p->order})
             buf->bind(ctx->pool, s);
         FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
         FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
@@ -886,8 +887,6 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(p->counter.ensure(sizeof(int)));
         FPM_TRY(p->status.ensure(sizeof(int)));
         FPM_TRY(p->scratch64.ensure(sizeof(double2) * (size_t)M * M));
-        FPM_TRY(p->avg.ensure(sizeof(double) * n2));
-        FPM_TRY(p->init_partial.ensure(sizeof(double) * 2 * fpm::init_chunks(N)));
         if (mpie) {
             FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
@@ -971,6 +970,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         if (mpie && a->momentum_interval > 0)
             br.bytes += 48.0 * (double)M * (double)M * (double)((long long)effective * iters / a->momentum_interval);
     }
+    for (DeviceBuffer* buf : {&br.tiles, &br.init, &br.gauge, &br.scratch_ptrs, &br.object_ptrs, &br.anchor_ptrs,
+                              &br.velocity_ptrs, &br.avg, &br.init_partial})
+        buf->bind(ctx->pool, s);
     FPM_CUDA(cudaEventCreate(&br.first));
     FPM_CUDA(cudaEventCreate(&br.last));
     FPM_CUDA(cudaEventRecord(br.first, s));
@@ -982,15 +984,13 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     FPM_TRY(upload_array(br.anchor_ptrs, anchors, s));
     FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
 
-    // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift.
-    // avg/partial scratch: per tile buffers are contiguous only per problem,
-    // so run the mean pass one tile at a time into each problem's buffers.
-    for (int t = 0; t < count; ++t) {
-        fpm_problem* p = b.problems[t];
-        FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>() + t, 1, p->avg.as<double>(),
-                                       p->init_partial.as<double>(), s));
-        br.launches += 2;
-    }
+    // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift;
+    // one launch pair for all tiles of the bucket.
+    FPM_TRY(br.avg.ensure(sizeof(double) * (size_t)N * N * count));
+    FPM_TRY(br.init_partial.ensure(sizeof(double) * 2 * (size_t)fpm::init_chunks(N) * count));
+    FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>(), count, br.avg.as<double>(),
+                                   br.init_partial.as<double>(), s));
+    br.launches += 2;
     FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, false, s));
     FPM_CUDA(fpm::launch_shift_to_state(br.scratch_ptrs.as<double2*>(), br.object_ptrs.as<float2*>(),
                                         mpie ? br.anchor_ptrs.as<float2*>() : nullptr,
@@ -1102,34 +1102,10 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     return Status::ok();
 }
 
-Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
-                 fpm_result_desc* results) {
-    FPM_TRY(validate_params(a));
-    if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
-    std::vector<Bucket> buckets;
-    std::vector<const fpm_problem*> seen(problems, problems + count);
-    std::sort(seen.begin(), seen.end());
-    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
-        return Status::make(FPM_ERR_INVALID_PARAMETER,
-                            "a problem appears twice in one batch; each batched tile needs its own problem (its state is resident)");
-    for (int i = 0; i < count; ++i) {
-        fpm_problem* p = problems[i];
-        if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
-        auto it = std::find_if(buckets.begin(), buckets.end(), [&](const Bucket& b) { return b.n == p->n && b.m == p->m; });
-        if (it == buckets.end()) {
-            buckets.push_back(Bucket{p->n, p->m, {}, {}});
-            it = buckets.end() - 1;
-        }
-        it->problems.push_back(p);
-        it->indices.push_back(i);
-    }
-    // Largest tiles first so the longest launches start earliest.
-    std::sort(buckets.begin(), buckets.end(), [](const Bucket& x, const Bucket& y) { return x.n > y.n; });
-    std::vector<std::unique_ptr<BucketRun>> runs;
-    for (size_t k = 0; k < buckets.size(); ++k) {
-        runs.push_back(std::make_unique<BucketRun>());
-        FPM_TRY(run_bucket(ctx, buckets[k], a, ctx->streams[k % fpm_context::kStreams], *runs.back()));
-    }
+// Device statistics of one batch from the events its buckets recorded
+// (synchronises the buckets' streams first).
+Status record_stats(fpm_context* ctx, const std::vector<Bucket>& buckets,
+                    const std::vector<std::unique_ptr<BucketRun>>& runs) {
     fpm_run_stats st = {};
     cudaEvent_t first_event = nullptr;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
@@ -1171,6 +1147,38 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         st.engine_span_ms = hi - lo;
     }
     ctx->stats = st;
+    return Status::ok();
+}
+
+Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                 fpm_result_desc* results) {
+    FPM_TRY(validate_params(a));
+    if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
+    std::vector<Bucket> buckets;
+    std::vector<const fpm_problem*> seen(problems, problems + count);
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
+        return Status::make(FPM_ERR_INVALID_PARAMETER,
+                            "a problem appears twice in one batch; each batched tile needs its own problem (its state is resident)");
+    for (int i = 0; i < count; ++i) {
+        fpm_problem* p = problems[i];
+        if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
+        auto it = std::find_if(buckets.begin(), buckets.end(), [&](const Bucket& b) { return b.n == p->n && b.m == p->m; });
+        if (it == buckets.end()) {
+            buckets.push_back(Bucket{p->n, p->m, {}, {}});
+            it = buckets.end() - 1;
+        }
+        it->problems.push_back(p);
+        it->indices.push_back(i);
+    }
+    // Largest tiles first so the longest launches start earliest.
+    std::sort(buckets.begin(), buckets.end(), [](const Bucket& x, const Bucket& y) { return x.n > y.n; });
+    std::vector<std::unique_ptr<BucketRun>> runs;
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        runs.push_back(std::make_unique<BucketRun>());
+        FPM_TRY(run_bucket(ctx, buckets[k], a, ctx->streams[k % fpm_context::kStreams], *runs.back()));
+    }
+    FPM_TRY(record_stats(ctx, buckets, runs));
     for (size_t k = 0; k < buckets.size(); ++k) {
         cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
@@ -1183,6 +1191,105 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
             const int idx = buckets[k].indices[t];
             FPM_TRY(finish_collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr));
+        }
+    return Status::ok();
+}
+
+// Host-input batch: problems are created, run and downloaded in chunks so
+// that the host validation and upload of chunk k + 1 overlap the run of
+// chunk k, and the downloads of finished chunks overlap the runs still in
+// flight. Chunks follow run_batch's order (largest tiles first) and hold at
+// most kChunkBytes of float64 measurements.
+Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, const fpm_measurement_desc* mss,
+                      const fpm_algorithm_params* a, fpm_result_desc* results,
+                      std::vector<std::unique_ptr<fpm_problem>>& made) {
+    constexpr size_t kChunkBytes = size_t(1) << 31;
+    FPM_TRY(validate_params(a));
+    if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
+    made.clear();
+    made.resize(count);
+    size_t staging = 0;
+    std::vector<size_t> bytes(count);
+    for (int i = 0; i < count; ++i) {
+        Status st = validate_model(&mds[i]);
+        if (!st) st = check_measurement_header(&mds[i], &mss[i]);
+        if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+        bytes[i] = (size_t)mds[i].image_height * mds[i].image_width * mss[i].frames * sizeof(double);
+        staging = std::max(staging, bytes[i]);
+    }
+    // Buckets by (n, m), largest tiles first, then chunks.
+    std::vector<std::pair<std::pair<int, int>, std::vector<int>>> groups;
+    for (int i = 0; i < count; ++i) {
+        const std::pair<int, int> key(mds[i].image_height, mds[i].recon_height);
+        auto it = std::find_if(groups.begin(), groups.end(), [&](const auto& g) { return g.first == key; });
+        if (it == groups.end()) {
+            groups.push_back({key, {}});
+            it = groups.end() - 1;
+        }
+        it->second.push_back(i);
+    }
+    std::stable_sort(groups.begin(), groups.end(), [](const auto& x, const auto& y) { return x.first.first > y.first.first; });
+    std::vector<Bucket> chunks;
+    for (const auto& g : groups) {
+        size_t acc = 0;
+        for (int i : g.second) {
+            if (chunks.empty() || chunks.back().n != g.first.first || chunks.back().m != g.first.second ||
+                acc + bytes[i] > kChunkBytes) {
+                chunks.push_back(Bucket{g.first.first, g.first.second, {}, {}});
+                acc = 0;
+            }
+            chunks.back().indices.push_back(i);
+            acc += bytes[i];
+        }
+    }
+    FPM_TRY(ctx->staging.ensure(staging));
+    std::vector<std::unique_ptr<BucketRun>> runs;
+    for (size_t k = 0; k < chunks.size(); ++k) {
+        Bucket& ch = chunks[k];
+        std::vector<long long> first(ch.indices.size() + 1, 0);
+        for (size_t t = 0; t < ch.indices.size(); ++t) first[t + 1] = first[t] + mss[ch.indices[t]].frames;
+        std::vector<FrameScan> scans(first.back());
+        std::vector<int> owner(first.back());
+        for (size_t t = 0; t < ch.indices.size(); ++t)
+            for (long long q = first[t]; q < first[t + 1]; ++q) owner[q] = (int)t;
+        HostPool::get().run(first.back(), [&](long long q) {
+            const int i = ch.indices[owner[q]];
+            scan_frame(&mds[i], &mss[i], (int)(q - first[owner[q]]), scans[q]);
+        });
+        for (size_t t = 0; t < ch.indices.size(); ++t) {
+            const int i = ch.indices[t];
+            Status st = check_scans(&mss[i], scans.data() + first[t]);
+            if (!st) st = prepare_problem(ctx, &mds[i], &mss[i], scans.data() + first[t], made[i]);
+            if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+            FPM_TRY(upload_problem(ctx, made[i].get(), &mds[i], &mss[i], ctx->upload));
+            ch.problems.push_back(made[i].get());
+        }
+        cudaEvent_t ready;
+        FPM_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+        FPM_CUDA(cudaEventRecord(ready, ctx->upload));
+        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
+        const cudaError_t wait = cudaStreamWaitEvent(s, ready, 0);
+        cudaEventDestroy(ready);
+        FPM_CUDA(wait);
+        runs.push_back(std::make_unique<BucketRun>());
+        FPM_TRY(run_bucket(ctx, ch, a, s, *runs.back()));
+    }
+    // Downloads on their own stream, each after its chunk's last kernel;
+    // the last launched (smallest) chunks finish first.
+    for (size_t k = chunks.size(); k-- > 0;) {
+        FPM_CUDA(cudaStreamWaitEvent(ctx->download, runs[k]->last, 0));
+        for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
+            const int idx = chunks[k].indices[t];
+            FPM_TRY(queue_collect(chunks[k].problems[t], a, results ? &results[idx] : nullptr, ctx->download));
+        }
+    }
+    FPM_CUDA(cudaStreamSynchronize(ctx->download));
+    for (size_t k = 0; k < chunks.size(); ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
+    FPM_TRY(record_stats(ctx, chunks, runs));
+    for (size_t k = 0; k < chunks.size(); ++k)
+        for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
+            const int idx = chunks[k].indices[t];
+            FPM_TRY(finish_collect(chunks[k].problems[t], a, results ? &results[idx] : nullptr));
         }
     return Status::ok();
 }
@@ -1226,6 +1333,8 @@ int32_t fpm_create(fpm_context** out, int32_t device) {
                                 device, prop.name, prop.major, prop.minor);
         for (int i = 0; i < fpm_context::kStreams; ++i)
             FPM_CUDA(cudaStreamCreateWithFlags(&ctx->streams[i], cudaStreamNonBlocking));
+        FPM_CUDA(cudaStreamCreateWithFlags(&ctx->upload, cudaStreamNonBlocking));
+        FPM_CUDA(cudaStreamCreateWithFlags(&ctx->download, cudaStreamNonBlocking));
         // Problem buffers come from a private stream-ordered pool that keeps
         // freed memory for the next problems instead of returning it.
         cudaMemPoolProps props{};
@@ -1249,8 +1358,12 @@ int32_t fpm_destroy(fpm_context* ctx) {
     cudaSetDevice(ctx->device);
     for (int i = 0; i < fpm_context::kStreams; ++i)
         if (ctx->streams[i]) cudaStreamSynchronize(ctx->streams[i]);
+    for (cudaStream_t extra : {ctx->upload, ctx->download})
+        if (extra) cudaStreamSynchronize(extra);
     for (int i = 0; i < fpm_context::kStreams; ++i)
         if (ctx->streams[i]) cudaStreamDestroy(ctx->streams[i]);
+    for (cudaStream_t extra : {ctx->upload, ctx->download})
+        if (extra) cudaStreamDestroy(extra);
     // Outstanding pooled allocations (problems not yet destroyed) keep the
     // pool's memory until they are freed.
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
@@ -1529,6 +1642,28 @@ int32_t fpm_run_batch(fpm_context* ctx, int32_t count, fpm_problem* const* probl
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
     return finish(ctx, run_batch(ctx, count, problems, params, results));
+}
+
+int32_t fpm_run_batch_host(fpm_context* ctx, int32_t count, const fpm_model_desc* models,
+                           const fpm_measurement_desc* measurements, const fpm_algorithm_params* params,
+                           fpm_result_desc* results, fpm_problem** problems) {
+    if (!ctx || count < 0 || (count > 0 && (!models || !measurements || !problems)))
+        return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument or negative count"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    for (int i = 0; i < count; ++i) problems[i] = nullptr;
+    std::vector<std::unique_ptr<fpm_problem>> made;
+    Status s = run_batch_host(ctx, count, models, measurements, params, results, made);
+    if (s) {
+        // Work already queued must finish before its buffers are released.
+        for (int i = 0; i < fpm_context::kStreams; ++i) cudaStreamSynchronize(ctx->streams[i]);
+        cudaStreamSynchronize(ctx->upload);
+        cudaStreamSynchronize(ctx->download);
+        made.clear();
+        return finish(ctx, s);
+    }
+    for (int i = 0; i < count; ++i) problems[i] = made[i].release();
+    return finish(ctx, s);
 }
 
 int32_t fpm_last_run_stats(const fpm_context* ctx, fpm_run_stats* stats) {

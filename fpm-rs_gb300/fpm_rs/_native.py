@@ -23,7 +23,7 @@ EXPORTED = (
     "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
     "fpm_fft2", "fpm_forward_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
-    "fpm_run", "fpm_run_batch", "fpm_last_run_stats",
+    "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_last_run_stats",
 )
 
 

@@ -334,8 +334,13 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
         raise UnsupportedError("checkpoint resume is not supported by the GB300 device path")
     params = algorithm._params(schedule)
     problems = list(problems)
-    upload(problems)
-    handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
+    # Problems that are all still on the host take the overlapped path:
+    # uploads and downloads run beside the reconstructions.
+    host_path = len(problems) > 1 and len({id(p) for p in problems}) == len(problems) and all(
+        p._handle is None for p in problems)
+    if not host_path:
+        upload(problems)
+    handles = None if host_path else (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
     ctx = N.context()
     results = (N.ResultDesc * len(problems))()
     arrays = []
@@ -351,8 +356,19 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
             results[i].objectives = N.ptr(a["objectives"], C.c_double)
             arrays.append(a)
     start = time.perf_counter()
-    N.check(N.library().fpm_run_batch(ctx.handle, len(problems), handles, C.byref(params),
-                                      results if download else None), ctx.handle)
+    if host_path:
+        descs = [p._descriptors() for p in problems]
+        models = (N.ModelDesc * len(problems))(*[d[0] for d in descs])
+        meas = (N.MeasurementDesc * len(problems))(*[d[1] for d in descs])
+        made = (C.c_void_p * len(problems))()
+        N.check(N.library().fpm_run_batch_host(ctx.handle, len(problems), models, meas, C.byref(params),
+                                               results if download else None, made), ctx.handle)
+        for p, h in zip(problems, made):
+            p._handle = C.c_void_p(h)
+            p._ctx = ctx
+    else:
+        N.check(N.library().fpm_run_batch(ctx.handle, len(problems), handles, C.byref(params),
+                                          results if download else None), ctx.handle)
     elapsed = time.perf_counter() - start
     if not download:
         return [None] * len(problems)

@@ -18,7 +18,8 @@
  *                                  fpm_problem_create_batch (many problems, one host scan)
  *   Runner::run / ReconstructionAlgorithm::run
  *                                  src/reconstruction/runner.rs:76-285 -> fpm_run
- *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size)
+ *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
+ *                                  fpm_run_batch_host (host inputs, copies overlapped with the runs)
  *   Error / FpmError ............. src/error.rs:12, python/src/errors.rs:17-50 -> FPM_ERR_* + fpm_last_error
  */
 #ifndef FPM_GPU_H
@@ -199,6 +200,18 @@ int32_t fpm_run(fpm_context *ctx, fpm_problem *problem, const fpm_algorithm_para
  * Each tile keeps the exact sequential frame order of a single run. */
 int32_t fpm_run_batch(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
                       const fpm_algorithm_params *params, fpm_result_desc *results);
+
+/* fpm_problem_create_batch + fpm_run_batch for host-resident inputs, with
+ * the copies overlapped: problems are created, run and downloaded in chunks
+ * (largest tiles first, at most 2 GiB of float64 measurements each), so the
+ * validation and upload of one chunk run beside the reconstruction of the
+ * previous ones and downloads overlap the runs still in flight. Results are
+ * identical to the two-call form. The created problems are returned in
+ * `problems` (caller-owned, resident for later runs; fpm_problem_destroy
+ * frees them); on error none is returned. */
+int32_t fpm_run_batch_host(fpm_context *ctx, int32_t count, const fpm_model_desc *models,
+                           const fpm_measurement_desc *measurements, const fpm_algorithm_params *params,
+                           fpm_result_desc *results, fpm_problem **problems);
 
 /* Device-side statistics of the last fpm_run / fpm_run_batch, from CUDA
  * events recorded on the streams the kernels ran on. */

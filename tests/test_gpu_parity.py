@@ -177,9 +177,57 @@ def test_batched_upload_matches_single_uploads(fpm):
         p.device_handle()
         single.append(algo.run(p).object)
     batched = [fpm.ReconstructionProblem(data, model) for model, _, data, _, _ in cases]
-    results = fpm.run_batch(algo, batched)  # uploads all three in one batched call
+    from fpm_rs import reconstruction
+
+    reconstruction.upload(batched)  # fpm_problem_create_batch
+    results = fpm.run_batch(algo, batched)
     for a, r in zip(single, results):
         assert np.array_equal(a, r.object)
+
+
+def test_host_input_batch_matches_resident_batch(fpm):
+    """fpm_run_batch_host (copies overlapped with the runs) gives the resident
+    path's results bit for bit, and leaves the problems resident."""
+    cases = [helpers.simulated(fpm, side, n, seed=seed, photons=1e4)
+             for n, side, seed in ((64, 3, 21), (32, 3, 22), (128, 3, 23), (32, 5, 24), (64, 5, 25))]
+    algo = fpm.Mpie(iterations=2, momentum_interval=3)
+    resident = [fpm.ReconstructionProblem(data, model) for model, _, data, _, _ in cases]
+    for p in resident:
+        p.device_handle()
+    expected = fpm.run_batch(algo, resident)
+    host = [fpm.ReconstructionProblem(data, model) for model, _, data, _, _ in cases]
+    got = fpm.run_batch(algo, host)  # no handles yet: the host-input path
+    for e, g in zip(expected, got):
+        assert np.array_equal(e.object, g.object)
+        assert np.array_equal(e.object_spectrum, g.object_spectrum)
+        assert [t[1] for t in e.trace] == [t[1] for t in g.trace]
+    assert all(p._handle is not None for p in host)
+    again = fpm.run_batch(algo, host)  # resident now
+    for e, g in zip(expected, again):
+        assert np.array_equal(e.object, g.object)
+
+
+def test_host_input_batch_error_returns_no_problems(fpm):
+    import ctypes as C
+    from fpm_rs import _native as N
+
+    model, _, data, _, _ = helpers.simulated(fpm, 3, 32, seed=26, photons=1e4)
+    problems = [fpm.ReconstructionProblem(data, model) for _ in range(2)]
+    descs = [p._descriptors() for p in problems]
+    bad = data.copy()
+    bad[0, 0, 0] = np.nan
+    descs[1][1].measurements = N.ptr(bad, C.c_double)
+    models = (N.ModelDesc * 2)(*[d[0] for d in descs])
+    meas = (N.MeasurementDesc * 2)(*[d[1] for d in descs])
+    made = (C.c_void_p * 2)(1, 2)
+    ctx = N.context()
+    params = fpm.AlternatingProjection(iterations=1)._params("sequential")
+    status = N.library().fpm_run_batch_host(ctx.handle, 2, models, meas, C.byref(params), None, made)
+    assert status == 4
+    buf = C.create_string_buffer(512)
+    N.library().fpm_last_error(ctx.handle, buf, len(buf))
+    assert buf.value.decode().startswith("problem 1:")
+    assert all(h is None for h in made)
 
 
 def test_batched_upload_error_names_the_problem(fpm):
