@@ -356,6 +356,29 @@ FPM_DEVICE void column_forward_local(float2* __restrict__ fld, int pq, int c, co
     for (int b = 0; b < 16; ++b) fld[b * K::RS + pq] = K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b];
 }
 
+// End of a gradient-descent mini-batch (src/algorithms/gradient_descent.rs:
+// 628-640): O -= (object_step / active) * G over the whole grid, then G = 0.
+// The cluster's CTAs split the grid; one float4 holds two complex values.
+template <class K>
+FPM_DEVICE void gd_batch_apply(const TileDesc& T, float step, int c) {
+    const long long total = (long long)T.M * (T.M + (T.M & 1)) / 2;
+    const long long per = (total + K::C - 1) / K::C;
+    const long long begin = c * per;
+    const long long end = begin + per < total ? begin + per : total;
+    float4* O4 = reinterpret_cast<float4*>(T.object);
+    float4* G4 = reinterpret_cast<float4*>(T.gradient);
+    for (long long e = begin + threadIdx.x; e < end; e += K::THREADS) {
+        const float4 g = __ldcg(G4 + e);
+        float4 o = __ldcg(O4 + e);
+        o.x = fmaf(-step, g.x, o.x);
+        o.y = fmaf(-step, g.y, o.y);
+        o.z = fmaf(-step, g.z, o.z);
+        o.w = fmaf(-step, g.w, o.w);
+        __stcg(O4 + e, o);
+        __stcg(G4 + e, make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+}
+
 template <class K>
 FPM_DEVICE void load_pupil_slab(float2* __restrict__ pslab, const float2* __restrict__ pupil, int c) {
     for (int e = threadIdx.x; e < K::R * K::N; e += K::THREADS) {
@@ -399,6 +422,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     load_pupil_slab<K>(pslab, T.pupil, c);
     int counter = P.momentum ? *T.counter : 0;
     double loss_acc = 0.0;
+    // Mini-batch gradient descent: frames add into T.gradient and the object
+    // moves once per batch of gd_batch consecutive frames of the order.
+    const bool gd_batched = ALG == kAlgGradient && P.gd_batch > 1;
+    int batch_active = 0;
     __syncthreads();
 
     for (int it = P.it_begin; it < P.it_end; ++it) {
@@ -407,10 +434,17 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             if (tid == 0) s_frame = T.params[f];
             __syncthreads();
             const FrameParam& fp = s_frame;
+            const bool batch_end = gd_batched && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
             if (fp.weight == 0.0f) {
                 __syncthreads();
+                if (batch_end) {
+                    if (batch_active > 0) gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
+                    batch_active = 0;
+                    cluster_barrier<K>();
+                }
                 continue;
             }
+            if (gd_batched) ++batch_active;
 
             // S0
             stage_object<K>(osm, T.object, M, ostride, fp, i_lo, row_lo, row_hi);
@@ -654,8 +688,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P8: exact bilinear adjoint scatter of scale * U into the object.
             {
-                const float scale = projection ? fp.weight * P.object_step
-                                               : -P.object_step * fp.weight * fp.valid_scale;
+                // Projection: O += w * step * adj(U). Gradient descent: O -= step *
+                // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
+                // (N^2 / valid) * adj(U).
+                const float scale = projection   ? fp.weight * P.object_step
+                                    : gd_batched ? fp.weight * fp.valid_scale
+                                                 : -P.object_step * fp.weight * fp.valid_scale;
+                float2* target = gd_batched ? T.gradient : T.object;
                 const int rows8 = C == 1 ? N + fp.has_upper_row : R + (c == C - 1 ? fp.has_upper_row : 0);
                 const int cols8 = N + fp.has_upper_col;
                 constexpr int PER = (N + 1 + 31) / 32;
@@ -667,7 +706,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     const float2* u0 = fld + r * K::RS;
                     const float2* u1 = u0 - K::RS;  // r == 0: the halo row
                     const float2* srow = ostage + r * K::ORS;
-                    float2* grow = T.object + (long long)(fp.lower_row + i) * ostride + fp.lower_col;
+                    float2* grow = target + (long long)(fp.lower_row + i) * ostride + fp.lower_col;
                     float2 out[PER];
 #pragma unroll
                     for (int t = 0; t < PER; ++t) {
@@ -681,7 +720,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
                         acc = cfma(fp.w11, d1, acc);
-                        out[t] = j < cols8 ? cfma(scale, acc, srow[j]) : z;
+                        const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
+                        out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
 #pragma unroll
                     for (int t = 0; t < PER; ++t) {
@@ -691,6 +731,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 }
             }
             cluster_barrier<K>();
+
+            if (batch_end) {
+                gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
+                batch_active = 0;
+                cluster_barrier<K>();
+            }
 
             // mPIE momentum event (src/algorithms/common.rs:308-387).
             if (P.momentum) {

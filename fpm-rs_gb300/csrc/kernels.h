@@ -37,6 +37,7 @@ struct TileDesc {
     const int* order;          // [frame_count] schedule, or null for sequential
     float2* velocity;          // mPIE, M*M
     float2* anchor;            // mPIE, M*M
+    float2* gradient;          // mini-batch gradient descent: M*M accumulator, zero between batches
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event
     int* status;               // bit 0: non-finite momentum, bit 1: non-finite pupil
@@ -65,6 +66,7 @@ struct EngineParams {
     float friction, feedback;
     int loss;
     int it_begin, it_end;
+    int gd_batch;              // gradient descent frames per mini-batch (1: update after every frame)
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.

@@ -213,7 +213,7 @@ struct fpm_problem {
     // resident device data
     DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
     // run state
-    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order;
+    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient;
 };
 
 namespace {
@@ -796,9 +796,6 @@ Status validate_params(const fpm_algorithm_params* a) {
                                 "EPRY frame-gain and background recovery are not implemented on the GB300 device path");
     }
     if (a->algorithm == FPM_ALG_GD) {
-        if (a->batch_size != 1)
-            return Status::make(FPM_ERR_UNSUPPORTED,
-                                "the GB300 device path runs gradient descent with batch_size 1 (the reference default)");
         if (a->poisson_truncation || a->recover_pupil)
             return Status::make(FPM_ERR_UNSUPPORTED,
                                 "gradient-descent truncation and pupil recovery are not implemented on the GB300 device path");
@@ -868,6 +865,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     const bool epry = a->algorithm == FPM_ALG_EPRY;
     const bool canonical = epry && a->recover_pupil;
+    const bool gd_batched = a->algorithm == FPM_ALG_GD && a->batch_size > 1;
     const int iters = a->iterations;
     std::vector<fpm::TileDesc> tiles(count);
     std::vector<fpm::InitTile> inits(count);
@@ -879,7 +877,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
         for (DeviceBuffer* buf : {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-                                  &p->velocity, &p->anchor, &p->order})
+                                  &p->velocity, &p->anchor, &p->order, &p->gradient})
             buf->bind(ctx->pool, s);
         FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
         FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
@@ -887,6 +885,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(p->counter.ensure(sizeof(int)));
         FPM_TRY(p->status.ensure(sizeof(int)));
         FPM_TRY(p->scratch64.ensure(sizeof(double2) * (size_t)M * M));
+        if (gd_batched) {
+            FPM_TRY(p->gradient.ensure(sizeof(float2) * (size_t)M * ms));
+            FPM_CUDA(cudaMemsetAsync(p->gradient.ptr, 0, sizeof(float2) * (size_t)M * ms, s));
+        }
         if (mpie) {
             FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
@@ -929,6 +931,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.order = order_dev;
         T.velocity = mpie ? p->velocity.as<float2>() : nullptr;
         T.anchor = mpie ? p->anchor.as<float2>() : nullptr;
+        T.gradient = gd_batched ? p->gradient.as<float2>() : nullptr;
         T.partials = p->partials.as<double>();
         T.counter = p->counter.as<int>();
         T.status = p->status.as<int>();
@@ -967,6 +970,14 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                            (canonical ? 16.0 * (double)n2 : 0.0);
         }
         br.bytes += frame_bytes * iters;
+        if (gd_batched) {
+            // Gradient read-modify-write per frame; object and gradient pass per batch.
+            double stencil = 0.0;
+            for (int f = 0; f < p->frames; ++f)
+                if (p->params[f].weight != 0.f) stencil += 16.0 * p->stencil_cells[f];
+            const long long batches = (p->frames + a->batch_size - 1) / a->batch_size;
+            br.bytes += (stencil + 32.0 * (double)M * (double)ms * (double)batches) * iters;
+        }
         if (mpie && a->momentum_interval > 0)
             br.bytes += 48.0 * (double)M * (double)M * (double)((long long)effective * iters / a->momentum_interval);
     }
@@ -1020,6 +1031,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.friction = (float)a->momentum_friction;
     ep.feedback = (float)a->momentum_feedback;
     ep.loss = a->loss_type;
+    ep.gd_batch = gd_batched ? a->batch_size : 1;
     auto engine = [&](int it0, int it1) -> Status {
         cudaEvent_t e0, e1;
         FPM_CUDA(cudaEventCreate(&e0));

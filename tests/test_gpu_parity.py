@@ -125,6 +125,24 @@ def test_gradient_descent_full_tile(fpm):
     _objective_close([t[1] for t in result.trace], expected["objectives"])
 
 
+@pytest.mark.parametrize("n,side,batch", [(32, 5, 4), (64, 3, 9), (128, 3, 2)])
+def test_gradient_descent_mini_batches(fpm, n, side, batch):
+    """GD with batch_size > 1: gradients of a batch accumulate, the object
+    moves once per batch by object_step / active frames
+    (src/algorithms/gradient_descent.rs:405-640); zero-weight frames count
+    toward batch boundaries but not toward the active frames."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=41, photons=1e4)
+    weights = np.ones(data.shape[0])
+    weights[1] = 0.0
+    weights[3] = 0.5
+    for loss in ("amplitude_mse", "poisson_nll"):
+        algo = fpm.GradientDescent(iterations=3, batch_size=batch, loss_type=loss)
+        result, expected = _run_both(fpm, algo, "gd", dict(iterations=3, batch_size=batch, loss_type=loss), model,
+                                     omodel, data, gains=gains, weights=weights)
+        assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, loss
+        _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
 def test_masks_weights_background(fpm):
     """Masked pixels, a zero-weight frame and a broadcast background (AP and GD)."""
     model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=21, photons=2e3)
