@@ -60,7 +60,7 @@ struct Cfg {
     static constexpr int STAGE = (R + 1) * ORS;
     static constexpr int PSLAB = R * N;     // this CTA's R centred pupil rows
     // + per-warp FP64 loss partials and the EPRY per-warp / per-CTA maxima.
-    static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + WARPS * 8 + (2 * WARPS + 2) * 4;
+    static constexpr int SMEM_BYTES = (FIELD + STAGE + PSLAB + 256) * 8 + (WARPS + 4) * 8 + (2 * WARPS + 2) * 4;
     static constexpr int T1 = R * NB / THREADS;      // P1 / P7 tasks per thread
     static constexpr int T2 = R * NA / THREADS;      // P2 / P6 tasks per thread
     static constexpr int TX = (R / C) * N / THREADS; // P3 / P5 tasks per thread
@@ -399,7 +399,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     float2* pslab = osm + K::STAGE;
     float2* tw = pslab + K::PSLAB;
     double* dred = reinterpret_cast<double*>(tw + 256);
-    float* fred = reinterpret_cast<float*>(dred + K::WARPS);
+    double* tred = dred + K::WARPS;  // this CTA's truncation partials (residual, weight, |O|^2)
+    float* fred = reinterpret_cast<float*>(dred + K::WARPS + 4);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tile = blockIdx.x / C;
@@ -426,15 +427,90 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     // moves once per batch of gd_batch consecutive frames of the order.
     const bool gd_batched = ALG == kAlgGradient && P.gd_batch > 1;
     int batch_active = 0;
+    // Poisson truncation (src/algorithms/gradient_descent.rs:701-792): each
+    // batch is walked twice, first forward-only for the residual statistic,
+    // then with the gate |y - p| <= scale * sqrt(p) on the gradient.
+    const bool truncating = ALG == kAlgGradient && P.trunc_threshold > 0.f;
+    const int batch_len = ALG == kAlgGradient ? P.gd_batch : 1;
+    double trunc_res = 0.0, trunc_pw = 0.0, trunc_norm = 0.0;
+    float trunc_scale = 0.f;
     __syncthreads();
 
     for (int it = P.it_begin; it < P.it_end; ++it) {
-        for (int idx = 0; idx < T.frame_count; ++idx) {
+        const int steps = truncating ? 2 * T.frame_count : T.frame_count;
+        for (int step = 0; step < steps; ++step) {
+            // Truncating: batch k covers steps [2kB, 2kB + 2b): b statistics
+            // steps, then the b update steps of the same frames.
+            int idx = step;
+            bool stats = false;
+            if (truncating) {
+                const int k = step / (2 * batch_len), base = k * batch_len;
+                const int blen = min(batch_len, T.frame_count - base), within = step - 2 * k * batch_len;
+                stats = within < blen;
+                idx = base + (stats ? within : within - blen);
+                if (within == 0) {
+                    // Batch start: |O|^2 of this CTA's share of the grid.
+                    const long long total = (long long)M * ostride;
+                    const long long per = (total + C - 1) / C;
+                    const long long begin = c * per;
+                    const long long end = begin + per < total ? begin + per : total;
+                    double nacc = 0.0;
+                    for (long long e = begin + tid; e < end; e += K::THREADS) {
+                        if ((int)(e % ostride) >= M) continue;  // padding column
+                        const float2 o = __ldcg(T.object + e);
+                        nacc += (double)o.x * o.x + (double)o.y * o.y;
+                    }
+                    trunc_norm = nacc;
+                    trunc_res = trunc_pw = 0.0;
+                }
+                if (within == blen) {
+                    // First update step: reduce the statistic over the cluster
+                    // in a fixed order, identically in every CTA.
+                    const double part[3] = {trunc_res, trunc_pw, trunc_norm};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const double w = warp_sum(part[q]);
+                        __syncthreads();
+                        if (lane == 0) dred[warp] = w;
+                        __syncthreads();
+                        if (tid == 0) {
+                            double t = 0.0;
+                            for (int ww = 0; ww < K::WARPS; ++ww) t += dred[ww];
+                            tred[q] = t;
+                        }
+                    }
+                    cluster_barrier<K>();
+                    double tot[3] = {0.0, 0.0, 0.0};
+                    if constexpr (C == 1) {
+                        tot[0] = tred[0];
+                        tot[1] = tred[1];
+                        tot[2] = tred[2];
+                    } else {
+                        cg::cluster_group cluster = cg::this_cluster();
+                        for (int r = 0; r < C; ++r) {
+                            const double* pr = cluster.map_shared_rank(tred, r);
+                            tot[0] += pr[0];
+                            tot[1] += pr[1];
+                            tot[2] += pr[2];
+                        }
+                    }
+                    const double rms = fmax(sqrt(tot[2]), sqrt((double)P.eps));
+                    const double mean = tot[1] > 0.0 ? tot[0] / tot[1] : 0.0;
+                    const double sc = (double)P.trunc_threshold * mean / rms;
+                    trunc_scale = (float)sc;
+                    if (!isfinite(sc) || sc < 0.0) {
+                        trunc_scale = 0.f;
+                        if (tid == 0) atomicOr(T.status, 16);
+                    }
+                    cluster_barrier<K>();  // partials read before the next batch rewrites them
+                }
+            }
             const int f = T.order ? T.order[idx] : idx;
             if (tid == 0) s_frame = T.params[f];
             __syncthreads();
             const FrameParam& fp = s_frame;
-            const bool batch_end = gd_batched && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
+            const bool batch_end =
+                gd_batched && !stats && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
             if (fp.weight == 0.0f) {
                 __syncthreads();
                 if (batch_end) {
@@ -444,7 +520,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 }
                 continue;
             }
-            if (gd_batched) ++batch_active;
+            if (gd_batched && !stats) ++batch_active;
 
             // S0
             stage_object<K>(osm, T.object, M, ostride, fp, i_lo, row_lo, row_hi);
@@ -525,8 +601,36 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)k * mstride] != 0 ? 1u : 0u) << k;
                     }
                 }
+                if constexpr (ALG == kAlgGradient) {
+                    if (stats) {
+                        // Statistic: |y - p| and the count over unmasked pixels.
+                        float res = 0.f, cnt = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) {
+                            const float intrinsic = cnorm2(v[k]);
+                            float target;
+                            bool valid;
+                            if (T.amplitude) {
+                                valid = mreg[k] >= 0.f;
+                                target = mreg[k] * mreg[k];
+                            } else {
+                                valid = ((mbits >> k) & 1u) != 0u;
+                                const float bg = brow ? __ldg(brow + k * mstride) : 0.f;
+                                target = fmaxf((mreg[k] - bg) * inv_gain, 0.f);
+                            }
+                            if (valid) {
+                                res += fabsf(target - intrinsic);
+                                cnt += 1.f;
+                            }
+                        }
+                        trunc_res += (double)fp.weight * res;
+                        trunc_pw += (double)fp.weight * cnt;
+                    }
+                }
                 float frame_loss = 0.f;
-                if (T.amplitude) {
+                if (stats) {
+                    // Forward-only statistics step: nothing to write back.
+                } else if (T.amplitude) {
                     // a = sqrt(max(I / g, 0)), -1 where masked; with no
                     // background, I = g a^2 exactly as the reference uses it.
 #pragma unroll
@@ -553,8 +657,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                                 frame_loss = fmaf(d, d, frame_loss);
                                 v[k] = cscale(v[k], 1.f - a * rsqrtf(fmaxf(intrinsic, P.eps)));
                             } else {
-                                frame_loss += point_loss<LOSS>(intrinsic, a * a, P.loss);
-                                v[k] = cscale(v[k], descent_factor<LOSS>(intrinsic, a * a, P.loss, P.eps));
+                                const float target = a * a;
+                                frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
+                                const bool kept = !truncating || fabsf(target - intrinsic) <= trunc_scale * sqrtf(intrinsic);
+                                v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, P.eps) : 0.f);
                             }
                         }
                     }
@@ -579,14 +685,21 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                             v[k] = make_float2(0.f, 0.f);
                         } else {
                             frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
-                            v[k] = cscale(v[k], descent_factor<LOSS>(intrinsic, target, P.loss, P.eps));
+                            const bool kept = !truncating || fabsf(target - intrinsic) <= trunc_scale * sqrtf(intrinsic);
+                            v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, P.eps) : 0.f);
                         }
                     }
                     }
                 }
-                if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
-                else column_forward_local<K>(fld, pq, c, tw, v);
-                loss_acc += (double)frame_loss * fp.loss_scale;
+                if (!stats) {
+                    if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
+                    else column_forward_local<K>(fld, pq, c, tw, v);
+                    loss_acc += (double)frame_loss * fp.loss_scale;
+                }
+            }
+            if (stats) {
+                __syncthreads();
+                continue;
             }
             cluster_barrier<K>();
 

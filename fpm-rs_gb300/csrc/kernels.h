@@ -40,7 +40,7 @@ struct TileDesc {
     float2* gradient;          // mini-batch gradient descent: M*M accumulator, zero between batches
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event
-    int* status;               // bit 0: non-finite momentum, bit 1: non-finite pupil
+    int* status;               // bits: 1 non-finite momentum, 4 no valid data, 8 gauge, 16 truncation statistic
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
@@ -67,6 +67,7 @@ struct EngineParams {
     int loss;
     int it_begin, it_end;
     int gd_batch;              // gradient descent frames per mini-batch (1: update after every frame)
+    float trunc_threshold;     // gradient descent Poisson truncation threshold (0: off)
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.

@@ -796,9 +796,18 @@ Status validate_params(const fpm_algorithm_params* a) {
                                 "EPRY frame-gain and background recovery are not implemented on the GB300 device path");
     }
     if (a->algorithm == FPM_ALG_GD) {
-        if (a->poisson_truncation || a->recover_pupil)
+        if (a->recover_pupil)
             return Status::make(FPM_ERR_UNSUPPORTED,
-                                "gradient-descent truncation and pupil recovery are not implemented on the GB300 device path");
+                                "gradient-descent pupil recovery is not implemented on the GB300 device path");
+        // GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331).
+        if (a->poisson_truncation) {
+            if (!std::isfinite(a->poisson_truncation_threshold) || a->poisson_truncation_threshold <= 0.0)
+                return Status::make(FPM_ERR_INVALID_PARAMETER,
+                                    "poisson_truncation_threshold must be finite and positive when provided");
+            if (a->loss_type != FPM_LOSS_POISSON_NLL)
+                return Status::make(FPM_ERR_INVALID_PARAMETER,
+                                    "poisson_truncation_threshold requires Poisson negative log likelihood");
+        }
     }
     return Status::ok();
 }
@@ -970,6 +979,15 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                            (canonical ? 16.0 * (double)n2 : 0.0);
         }
         br.bytes += frame_bytes * iters;
+        if (a->algorithm == FPM_ALG_GD && a->poisson_truncation) {
+            // Forward-only statistics pass: stencil read and measurement per frame,
+            // and |O|^2 of the grid per batch.
+            double fwd = 0.0;
+            for (int f = 0; f < p->frames; ++f)
+                if (p->params[f].weight != 0.f) fwd += 8.0 * p->stencil_cells[f] + 4.0 * (double)n2;
+            const long long batches = (p->frames + a->batch_size - 1) / a->batch_size;
+            br.bytes += (fwd + 8.0 * (double)M * (double)ms * (double)batches) * iters;
+        }
         if (gd_batched) {
             // Gradient read-modify-write per frame; object and gradient pass per batch.
             double stencil = 0.0;
@@ -1031,7 +1049,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.friction = (float)a->momentum_friction;
     ep.feedback = (float)a->momentum_feedback;
     ep.loss = a->loss_type;
-    ep.gd_batch = gd_batched ? a->batch_size : 1;
+    ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
+    ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
     auto engine = [&](int it0, int it1) -> Status {
         cudaEvent_t e0, e1;
         FPM_CUDA(cudaEventCreate(&e0));
@@ -1102,6 +1121,7 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 4) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "no positive-weight, unmasked measurements are available");
     if (status & 1) return Status::make(FPM_ERR_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
     if (status & 8) return Status::make(FPM_ERR_NUMERICAL, "object/pupil gauge normalization failed on a non-finite or empty state");
+    if (status & 16) return Status::make(FPM_ERR_NUMERICAL, "Poisson truncation statistic is non-finite");
     if (!r) return Status::ok();
     const int C = fpm::engine_ctas(p->n);
     if (r->objectives)

@@ -70,7 +70,7 @@ class AlgorithmParams(C.Structure):
         ("recover_pupil", C.c_int32), ("constrain_pupil_support", C.c_int32),
         ("pupil_step", C.c_double),
         ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
-        ("poisson_truncation", C.c_int32),
+        ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
     ]
 
 

@@ -290,6 +290,8 @@ class GradientDescent(_Algorithm):
         p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
                          self.loss_type)
         p.poisson_truncation = int(self.poisson_truncation_threshold is not None)
+        if self.poisson_truncation_threshold is not None:
+            p.poisson_truncation_threshold = float(self.poisson_truncation_threshold)
         p.recover_pupil = int(bool(self.recover_pupil))
         return p
 

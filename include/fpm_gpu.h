@@ -116,7 +116,8 @@ typedef struct {
     double pupil_step;
     int32_t recover_frame_gains; /* EPRY extension (unsupported on the device path) */
     int32_t recover_background;  /* EPRY extension (unsupported on the device path) */
-    int32_t poisson_truncation;  /* GD option (unsupported on the device path) */
+    int32_t poisson_truncation;  /* GD: nonzero enables the Poisson truncation gate */
+    double poisson_truncation_threshold; /* GD: the gate's threshold (finite, positive; Poisson NLL only) */
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */

@@ -1010,10 +1010,59 @@ static int32_t projection_update(orc_state *s, const int *frames, int count, con
 /* GradientDescent::step (src/algorithms/gradient_descent.rs:405-671) for the
  * ordinary object gradient: no truncation, pupil or illumination recovery,
  * and no regularisation. */
-static int32_t gradient_step(orc_state *s, const int *frames, int count, double object_step, double epsilon,
-                             int loss, step_summary *summary) {
+/* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */
+int32_t orc_truncation_accepts(double predicted, double measured, double scale) {
+    return fabs(measured - predicted) <= scale * sqrt(fmax(predicted, 0.0));
+}
+
+/* compute_truncation_statistics (src/algorithms/gradient_descent.rs:701-792):
+ * frame-weighted mean absolute residual of the batch's unmasked pixels over
+ * the object RMS amplitude, times the threshold. */
+static int32_t truncation_scale(orc_state *s, const int *frames, int count, double threshold, double epsilon,
+                                double *scale) {
     const orc_problem *p = s->p;
     size_t n = s->n_low;
+    double residual_sum = 0.0, pixel_weight = 0.0;
+    for (int b = 0; b < count; ++b) {
+        int frame = frames[b];
+        double fw = frame_weight(p, frame);
+        if (fw == 0.0) continue;
+        int32_t st = source_field(s, frame);
+        if (st) return st;
+        const double *measured = p->data + (size_t)frame * n;
+        const uint8_t *mask = frame_mask(p, frame);
+        double gain = s->gains[frame];
+        if (!isfinite(gain) || gain <= 0.0) return fail(ORC_INVALID_MODEL, "state frame %d has invalid gain", frame);
+        long valid = 0;
+        for (size_t i = 0; i < n; ++i) {
+            if (mask && mask[i] == 0) continue;
+            ++valid;
+            double predicted = fmax(c_norm_sqr(s->field[i]), 0.0);
+            double target = fmax((measured[i] - state_background(s, frame, i)) / gain, 0.0);
+            residual_sum += fw * fabs(target - predicted);
+            pixel_weight += fw;
+        }
+        if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", frame);
+    }
+    double norm = 0.0;
+    for (size_t i = 0; i < s->n_high; ++i) norm += c_norm_sqr(s->object[i]);
+    double object_rms = fmax(sqrt(norm), sqrt(epsilon));
+    double mean_residual = pixel_weight > 0.0 ? residual_sum / pixel_weight : 0.0;
+    *scale = threshold * mean_residual / object_rms;
+    if (!isfinite(*scale) || *scale < 0.0) return fail(ORC_NUMERICAL, "Poisson truncation statistic is non-finite");
+    return ORC_OK;
+}
+
+static int32_t gradient_step(orc_state *s, const int *frames, int count, double object_step, double epsilon,
+                             int loss, double truncation_threshold, step_summary *summary) {
+    const orc_problem *p = s->p;
+    size_t n = s->n_low;
+    double scale = 0.0;
+    const int truncate = truncation_threshold > 0.0;
+    if (truncate) {
+        int32_t st = truncation_scale(s, frames, count, truncation_threshold, epsilon, &scale);
+        if (st) return st;
+    }
     double max_pupil = 0.0;
     for (size_t i = 0; i < n; ++i) max_pupil = fmax(max_pupil, c_norm_sqr(s->pupil[i]));
     max_pupil = fmax(max_pupil, epsilon);
@@ -1044,7 +1093,8 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
             double intrinsic = fmax(s->projected[i].re, 0.0);
             double target = fmax((measured[i] - bg) / gain, 0.0);
             frame_loss += point_loss(intrinsic, target, loss);
-            s->projected[i] = cx(descent_factor(intrinsic, target, loss, epsilon), intrinsic);
+            const int retained = !truncate || orc_truncation_accepts(intrinsic, target, scale);
+            s->projected[i] = cx(retained ? descent_factor(intrinsic, target, loss, epsilon) : 0.0, intrinsic);
         }
         if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", frame);
         double valid_scale = (double)n / (double)valid;
@@ -1283,6 +1333,13 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         return out->status = fail(ORC_INVALID_PARAMETER, "epsilon must be finite and positive");
     if (prm->algorithm == ORC_ALG_GD && prm->recover_pupil)
         return out->status = fail(ORC_UNSUPPORTED, "gradient-descent pupil recovery is not restated");
+    /* GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331). */
+    if (prm->poisson_truncation_threshold != 0.0) {
+        if (!isfinite(prm->poisson_truncation_threshold) || prm->poisson_truncation_threshold < 0.0)
+            return out->status = fail(ORC_INVALID_PARAMETER, "poisson_truncation_threshold must be finite and positive");
+        if (prm->loss_type != ORC_LOSS_POISSON_NLL)
+            return out->status = fail(ORC_INVALID_PARAMETER, "poisson_truncation_threshold requires Poisson negative log likelihood");
+    }
     orc_state s;
     int32_t st = state_init(&s, p);
     if (st) {
@@ -1347,7 +1404,8 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         for (int start = 0; start < p->frames && !st; start += prm->batch_size) {
             int count = p->frames - start < prm->batch_size ? p->frames - start : prm->batch_size;
             if (prm->algorithm == ORC_ALG_GD)
-                st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type, &summary);
+                st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type,
+                                   prm->poisson_truncation_threshold, &summary);
             else
                 st = projection_update(&s, order + start, count, &cfg, &summary);
         }

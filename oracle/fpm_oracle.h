@@ -93,7 +93,11 @@ typedef struct {
     double gain_step, gain_min, gain_max;
     int32_t recover_background;
     double background_step, background_min, background_max;
+    double poisson_truncation_threshold;   /* GD: 0 disables the truncation gate */
 } orc_params;
+
+/* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */
+int32_t orc_truncation_accepts(double predicted, double measured, double scale);
 
 typedef struct {
     double *object_spectrum;  /* mh*mw complex, centred */

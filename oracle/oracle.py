@@ -95,6 +95,7 @@ class _Params(C.Structure):
         ("gain_max", C.c_double),
         ("recover_background", C.c_int32), ("background_step", C.c_double),
         ("background_min", C.c_double), ("background_max", C.c_double),
+        ("poisson_truncation_threshold", C.c_double),
     ]
 
 
@@ -275,6 +276,13 @@ def momentum_event(obj, velocity, anchor, friction, feedback):
     return o, v, a
 
 
+def truncation_accepts(predicted: float, measured: float, scale: float) -> bool:
+    fn = lib().orc_truncation_accepts
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_double, C.c_double, C.c_double]
+    return bool(fn(predicted, measured, scale))
+
+
 def complex_nrmse(reference, candidate) -> float:
     r = _c128(reference)
     c = _c128(candidate)
@@ -355,7 +363,7 @@ def params(algorithm: str, **kw) -> _Params:
                stability=0.0, momentum_interval=30, momentum_friction=0.9, momentum_feedback=0.9,
                recover_pupil=False, constrain_pupil=True, pupil_step=0.1, recover_gains=False,
                gain_step=0.2, gain_min=1e-6, gain_max=1e6, recover_background=False,
-               background_step=0.2, background_min=0.0, background_max=1e12)
+               background_step=0.2, background_min=0.0, background_max=1e12, poisson_truncation_threshold=0.0)
     cfg.update(DEFAULTS[algorithm])
     cfg.update(kw)
     p = _Params()
@@ -366,7 +374,7 @@ def params(algorithm: str, **kw) -> _Params:
     p.schedule = SCHEDULES[cfg["schedule"]]
     for name in ("object_step", "epsilon", "stability", "momentum_friction", "momentum_feedback",
                  "pupil_step", "gain_step", "gain_min", "gain_max", "background_step",
-                 "background_min", "background_max"):
+                 "background_min", "background_max", "poisson_truncation_threshold"):
         setattr(p, name, float(cfg[name]))
     p.momentum_interval = int(cfg["momentum_interval"])
     p.recover_pupil = int(bool(cfg["recover_pupil"]))

@@ -143,6 +143,32 @@ def test_gradient_descent_mini_batches(fpm, n, side, batch):
         _objective_close([t[1] for t in result.trace], expected["objectives"])
 
 
+@pytest.mark.parametrize("n,side,batch,threshold", [(32, 5, 5, 25.0), (64, 3, 1, 2.0), (128, 3, 9, 4.0)])
+def test_gradient_descent_poisson_truncation(fpm, n, side, batch, threshold):
+    """Poisson truncation (src/algorithms/gradient_descent.rs:701-792,1180-1182):
+    per batch, a forward-only pass gives the gate scale; pixels with
+    |y - p| > scale * sqrt(p) leave the gradient but stay in the objective."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=43, photons=3e3)
+    kw = dict(iterations=3, batch_size=batch, loss_type="poisson_nll", poisson_truncation_threshold=threshold)
+    result, expected = _run_both(fpm, fpm.GradientDescent(**kw), "gd", kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "gd", iterations=3, batch_size=batch,
+                       loss_type="poisson_nll")
+    if threshold < 10.0:
+        # The gate rejects pixels at this threshold: results differ from plain GD.
+        assert oracle.complex_nrmse(plain["object"], expected["object"]) > 10 * NRMSE
+
+
+def test_poisson_truncation_validation(fpm):
+    model, omodel = helpers.planar_model(fpm, 3, 32)
+    problem = fpm.ReconstructionProblem(np.ones((model.frame_count, 32, 32)), model)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.GradientDescent(iterations=1, poisson_truncation_threshold=25.0).run(problem)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.GradientDescent(iterations=1, loss_type="poisson_nll", poisson_truncation_threshold=-1.0).run(problem)
+
+
 def test_masks_weights_background(fpm):
     """Masked pixels, a zero-weight frame and a broadcast background (AP and GD)."""
     model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=21, photons=2e3)

@@ -212,3 +212,27 @@ def test_zero_weight_frames_are_ignored():
     a = oracle.run(oracle.Problem(m, data, weights=w), "ap", iterations=2)
     b = oracle.run(oracle.Problem(m, corrupted, weights=w), "ap", iterations=2)
     assert np.array_equal(a["object_spectrum"], b["object_spectrum"])
+
+
+def test_poisson_truncation_gate_includes_its_boundary():
+    # src/algorithms/gradient_descent.rs:1389-1395
+    assert oracle.truncation_accepts(4.0, 10.0, 3.0)
+    assert not oracle.truncation_accepts(4.0, 10.000_001, 3.0)
+    assert oracle.truncation_accepts(0.0, 0.0, 1.0)
+    assert not oracle.truncation_accepts(0.0, 1.0, 1.0)
+
+
+def test_poisson_truncation_requires_poisson_loss_and_is_inert_when_wide():
+    # GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331);
+    # a threshold so large that every pixel passes leaves GD unchanged.
+    m, data = _direct_problem(11)
+    with pytest.raises(oracle.OracleError):
+        oracle.run(oracle.Problem(m, data), "gd", iterations=1, poisson_truncation_threshold=25.0)
+    plain = oracle.run(oracle.Problem(m, data), "gd", iterations=3, batch_size=5, loss_type="poisson_nll")
+    wide = oracle.run(oracle.Problem(m, data), "gd", iterations=3, batch_size=5, loss_type="poisson_nll",
+                      poisson_truncation_threshold=1e30)
+    assert np.array_equal(plain["object_spectrum"], wide["object_spectrum"])
+    tight = oracle.run(oracle.Problem(m, data * 1.7), "gd", iterations=3, batch_size=5, loss_type="poisson_nll",
+                       poisson_truncation_threshold=0.05)
+    loose = oracle.run(oracle.Problem(m, data * 1.7), "gd", iterations=3, batch_size=5, loss_type="poisson_nll")
+    assert not np.array_equal(tight["object_spectrum"], loose["object_spectrum"])
