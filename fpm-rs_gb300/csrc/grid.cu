@@ -150,6 +150,26 @@ cudaError_t launch_widen(const float2* src, long long src_stride, int rows, int 
     return cudaGetLastError();
 }
 
+// Dense complex128 rows narrowed to complex64 rows of stride dst_stride
+// (checkpoint restore: the values were widened from complex64, so this is exact).
+__global__ void narrow_kernel(const double2* __restrict__ src, int rows, int cols, float2* __restrict__ dst,
+                              long long dst_stride) {
+    const long long total = (long long)rows * cols;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / cols, c = e % cols;
+        const double2 v = src[e];
+        dst[r * dst_stride + c] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+cudaError_t launch_narrow(const double2* src, int rows, int cols, float2* dst, long long dst_stride, cudaStream_t s) {
+    const long long total = (long long)rows * cols;
+    if (total == 0) return cudaSuccess;
+    const int blocks = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+    narrow_kernel<<<blocks, 256, 0, s>>>(src, rows, cols, dst, dst_stride);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ gauge
 
 constexpr int kGaugeThreads = 1024;

@@ -125,6 +125,8 @@ cudaError_t launch_shift_to_state(double2* const* scratch, float2* const* object
                                   float2* const* velocity, int count, int m, cudaStream_t s);
 cudaError_t launch_state_to_natural(const float2* const* object, double2* const* scratch, int count, int m,
                                     cudaStream_t s);
+// Dense complex128 rows narrowed to complex64 rows of stride dst_stride.
+cudaError_t launch_narrow(const double2* src, int rows, int cols, float2* dst, long long dst_stride, cudaStream_t s);
 // Complex64 rows (row stride src_stride) widened to dense complex128.
 cudaError_t launch_widen(const float2* src, long long src_stride, int rows, int cols, double2* dst, cudaStream_t s);
 

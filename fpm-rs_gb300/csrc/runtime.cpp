@@ -203,6 +203,9 @@ struct fpm_problem {
     std::vector<float2> pupil_f32;
     int host_status = 0;                // result downloads
     std::vector<double> host_partials;
+    int it0 = 0;                        // first iteration of the last run (resumed runs start later)
+    std::vector<double> resume_objectives;
+    int host_counter = 0;
     std::vector<fpm::FrameParam> params;
     std::vector<double> stencil_cells;  // per frame: rows * cols of the bilinear stencil
     bool has_masks = false, has_background = false;
@@ -845,6 +848,7 @@ struct Bucket {
     int n, m;
     std::vector<fpm_problem*> problems;
     std::vector<int> indices;
+    std::vector<const fpm_state_desc*> resume;  // per problem, or empty for a fresh start
 };
 
 template <class T>
@@ -876,6 +880,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     const bool canonical = epry && a->recover_pupil;
     const bool gd_batched = a->algorithm == FPM_ALG_GD && a->batch_size > 1;
     const int iters = a->iterations;
+    const bool resumed = !b.resume.empty();
+    const int it0 = resumed ? b.resume[0]->completed_iterations : 0;
     std::vector<fpm::TileDesc> tiles(count);
     std::vector<fpm::InitTile> inits(count);
     std::vector<fpm::GaugeTile> gauges(count);
@@ -903,8 +909,31 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
         }
         FPM_CUDA(cudaMemsetAsync(p->status.ptr, 0, sizeof(int), s));
-        FPM_CUDA(cudaMemsetAsync(p->counter.ptr, 0, sizeof(int), s));
-        FPM_CUDA(cudaMemcpyAsync(p->pupil_state.ptr, p->pupil_model.ptr, sizeof(float2) * n2, cudaMemcpyDeviceToDevice, s));
+        p->it0 = it0;
+        p->resume_objectives.clear();
+        if (resumed) {
+            // Restore the saved state: complex128 host arrays through scratch64
+            // into the complex64 state (stream-ordered reuse of scratch64).
+            const fpm_state_desc* r = b.resume[t];
+            p->resume_objectives.assign(r->objectives, r->objectives + it0);
+            p->host_counter = mpie ? r->momentum_counter : 0;
+            FPM_CUDA(cudaMemcpyAsync(p->counter.ptr, &p->host_counter, sizeof(int), cudaMemcpyHostToDevice, s));
+            double2* wide = p->scratch64.as<double2>();
+            FPM_CUDA(cudaMemcpyAsync(wide, r->pupil, sizeof(double2) * n2, cudaMemcpyHostToDevice, s));
+            FPM_CUDA(fpm::launch_narrow(wide, N, N, p->pupil_state.as<float2>(), N, s));
+            const struct {
+                const double* src;
+                DeviceBuffer* dst;
+            } grids[3] = {{r->object_spectrum, &p->object}, {r->velocity, &p->velocity}, {r->anchor, &p->anchor}};
+            for (int g = 0; g < (mpie ? 3 : 1); ++g) {
+                FPM_CUDA(cudaMemcpyAsync(wide, grids[g].src, sizeof(double2) * (size_t)M * M, cudaMemcpyHostToDevice, s));
+                FPM_CUDA(fpm::launch_narrow(wide, M, M, grids[g].dst->as<float2>(), ms, s));
+            }
+            br.launches += mpie ? 4 : 2;
+        } else {
+            FPM_CUDA(cudaMemsetAsync(p->counter.ptr, 0, sizeof(int), s));
+            FPM_CUDA(cudaMemcpyAsync(p->pupil_state.ptr, p->pupil_model.ptr, sizeof(float2) * n2, cudaMemcpyDeviceToDevice, s));
+        }
         const int* order_dev = nullptr;
         if (a->schedule != FPM_SCHEDULE_SEQUENTIAL) {
             FPM_TRY(upload_array(p->order, schedule_order(p, a->schedule), s));
@@ -1014,17 +1043,20 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
 
     // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift;
-    // one launch pair for all tiles of the bucket.
-    FPM_TRY(br.avg.ensure(sizeof(double) * (size_t)N * N * count));
-    FPM_TRY(br.init_partial.ensure(sizeof(double) * 2 * (size_t)fpm::init_chunks(N) * count));
-    FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>(), count, br.avg.as<double>(),
-                                   br.init_partial.as<double>(), s));
-    br.launches += 2;
-    FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, false, s));
-    FPM_CUDA(fpm::launch_shift_to_state(br.scratch_ptrs.as<double2*>(), br.object_ptrs.as<float2*>(),
-                                        mpie ? br.anchor_ptrs.as<float2*>() : nullptr,
-                                        mpie ? br.velocity_ptrs.as<float2*>() : nullptr, count, M, s));
-    br.launches += 3;
+    // one launch pair for all tiles of the bucket. A resumed run has restored
+    // its state above. Pupil-recovering runs canonicalise either way.
+    if (!resumed) {
+        FPM_TRY(br.avg.ensure(sizeof(double) * (size_t)N * N * count));
+        FPM_TRY(br.init_partial.ensure(sizeof(double) * 2 * (size_t)fpm::init_chunks(N) * count));
+        FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>(), count, br.avg.as<double>(),
+                                       br.init_partial.as<double>(), s));
+        br.launches += 2;
+        FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, false, s));
+        FPM_CUDA(fpm::launch_shift_to_state(br.scratch_ptrs.as<double2*>(), br.object_ptrs.as<float2*>(),
+                                            mpie ? br.anchor_ptrs.as<float2*>() : nullptr,
+                                            mpie ? br.velocity_ptrs.as<float2*>() : nullptr, count, M, s));
+        br.launches += 3;
+    }
     if (canonical) {
         FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
         br.launches += 1;
@@ -1065,9 +1097,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         br.launches += 1;
         return Status::ok();
     };
-    if (iters > 0) {
+    if (iters > it0) {
         if (epry) {
-            for (int it = 0; it < iters; ++it) {
+            for (int it = it0; it < iters; ++it) {
                 FPM_TRY(engine(it, it + 1));
                 if (canonical) {
                     FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
@@ -1075,7 +1107,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 }
             }
         } else {
-            FPM_TRY(engine(0, iters));
+            FPM_TRY(engine(it0, iters));
         }
     }
     // Finalise: ifftshift, inverse FFT (FP64) into scratch.
@@ -1116,6 +1148,52 @@ Status queue_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_d
     return Status::ok();
 }
 
+// Weighted mean objective per iteration: the resumed prefix, then the
+// per-CTA partials of the iterations this run executed.
+void fill_objectives(const fpm_problem* p, const fpm_algorithm_params* a, double* objectives) {
+    const int C = fpm::engine_ctas(p->n);
+    for (int it = 0; it < a->iterations; ++it) {
+        if (it < p->it0) {
+            objectives[it] = p->resume_objectives[it];
+            continue;
+        }
+        double sum = 0.0;
+        for (int c = 0; c < C; ++c) sum += p->host_partials[(size_t)it * C + c];
+        objectives[it] = p->weight_sum > 0.0 ? sum / p->weight_sum : NAN;
+    }
+}
+
+// Queues the download of one problem's resumable state (after queue_collect
+// on the same stream, which it follows in the use of scratch64).
+Status queue_capture(fpm_problem* p, const fpm_algorithm_params* a, fpm_state_desc* cap, cudaStream_t s) {
+    const int M = p->m, N = p->n, C = fpm::engine_ctas(N);
+    const long long ms = M + (M & 1);
+    double2* wide = p->scratch64.as<double2>();
+    FPM_CUDA(fpm::launch_widen(p->object.as<float2>(), ms, M, M, wide, s));
+    FPM_CUDA(cudaMemcpyAsync(cap->object_spectrum, wide, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+    FPM_CUDA(fpm::launch_widen(p->pupil_state.as<float2>(), N, N, N, wide, s));
+    FPM_CUDA(cudaMemcpyAsync(cap->pupil, wide, sizeof(double2) * (size_t)N * N, cudaMemcpyDeviceToHost, s));
+    if (a->algorithm == FPM_ALG_MPIE) {
+        FPM_CUDA(fpm::launch_widen(p->velocity.as<float2>(), ms, M, M, wide, s));
+        FPM_CUDA(cudaMemcpyAsync(cap->velocity, wide, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(fpm::launch_widen(p->anchor.as<float2>(), ms, M, M, wide, s));
+        FPM_CUDA(cudaMemcpyAsync(cap->anchor, wide, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaMemcpyAsync(&p->host_counter, p->counter.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    if (a->iterations > 0) {
+        p->host_partials.resize((size_t)a->iterations * C);
+        FPM_CUDA(cudaMemcpyAsync(p->host_partials.data(), p->partials.ptr, sizeof(double) * p->host_partials.size(),
+                                 cudaMemcpyDeviceToHost, s));
+    }
+    return Status::ok();
+}
+
+void finish_capture(const fpm_problem* p, const fpm_algorithm_params* a, fpm_state_desc* cap) {
+    cap->completed_iterations = a->iterations;
+    cap->momentum_counter = a->algorithm == FPM_ALG_MPIE ? p->host_counter : 0;
+    if (cap->objectives) fill_objectives(p, a, cap->objectives);
+}
+
 Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_desc* r) {
     const int status = p->host_status;
     if (status & 4) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "no positive-weight, unmasked measurements are available");
@@ -1124,12 +1202,7 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 16) return Status::make(FPM_ERR_NUMERICAL, "Poisson truncation statistic is non-finite");
     if (!r) return Status::ok();
     const int C = fpm::engine_ctas(p->n);
-    if (r->objectives)
-        for (int it = 0; it < a->iterations; ++it) {
-            double sum = 0.0;
-            for (int c = 0; c < C; ++c) sum += p->host_partials[(size_t)it * C + c];
-            r->objectives[it] = p->weight_sum > 0.0 ? sum / p->weight_sum : NAN;
-        }
+    if (r->objectives) fill_objectives(p, a, r->objectives);
     r->completed_iterations = a->iterations;
     return Status::ok();
 }
@@ -1182,8 +1255,45 @@ Status record_stats(fpm_context* ctx, const std::vector<Bucket>& buckets,
     return Status::ok();
 }
 
+// Checks resumable-state descriptors before any device work.
+Status validate_resume(int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                       const fpm_state_desc* resume, const fpm_state_desc* capture) {
+    const bool mpie = a->algorithm == FPM_ALG_MPIE;
+    for (int i = 0; i < count && resume; ++i) {
+        const fpm_state_desc& r = resume[i];
+        const fpm_problem* p = problems[i];
+        if (r.completed_iterations != resume[0].completed_iterations)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "resumed problems in one batch must share completed_iterations");
+        if (r.completed_iterations < 0 || r.completed_iterations > a->iterations)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: checkpoint has %d completed iterations of %d", i,
+                                r.completed_iterations, a->iterations);
+        if (!r.object_spectrum || !r.pupil || (r.completed_iterations > 0 && !r.objectives))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: checkpoint arrays are missing", i);
+        if (mpie && (!r.velocity || !r.anchor))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: mPIE resume needs its velocity and anchor", i);
+        if (mpie && (r.momentum_counter < 0 || r.momentum_counter >= a->momentum_interval))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: momentum counter %d outside [0, %d)", i,
+                                r.momentum_counter, a->momentum_interval);
+        const size_t m2 = (size_t)p->m * p->m, n2 = (size_t)p->n * p->n;
+        auto finite = [](const double* v, size_t n) {
+            for (size_t k = 0; k < 2 * n; ++k)
+                if (!std::isfinite(v[k])) return false;
+            return true;
+        };
+        if (!finite(r.object_spectrum, m2) || !finite(r.pupil, n2) ||
+            (mpie && (!finite(r.velocity, m2) || !finite(r.anchor, m2))))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: checkpoint holds non-finite values", i);
+    }
+    for (int i = 0; i < count && capture; ++i) {
+        const fpm_state_desc& c = capture[i];
+        if (!c.object_spectrum || !c.pupil || (mpie && (!c.velocity || !c.anchor)) || (a->iterations > 0 && !c.objectives))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: capture arrays are missing", i);
+    }
+    return Status::ok();
+}
+
 Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
-                 fpm_result_desc* results) {
+                 fpm_result_desc* results, const fpm_state_desc* resume = nullptr, fpm_state_desc* capture = nullptr) {
     FPM_TRY(validate_params(a));
     if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
     std::vector<Bucket> buckets;
@@ -1202,7 +1312,9 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         }
         it->problems.push_back(p);
         it->indices.push_back(i);
+        if (resume) it->resume.push_back(&resume[i]);
     }
+    FPM_TRY(validate_resume(count, problems, a, resume, capture));
     // Largest tiles first so the longest launches start earliest.
     std::sort(buckets.begin(), buckets.end(), [](const Bucket& x, const Bucket& y) { return x.n > y.n; });
     std::vector<std::unique_ptr<BucketRun>> runs;
@@ -1216,6 +1328,7 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
             const int idx = buckets[k].indices[t];
             FPM_TRY(queue_collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr, s));
+            if (capture) FPM_TRY(queue_capture(buckets[k].problems[t], a, &capture[idx], s));
         }
     }
     for (size_t k = 0; k < buckets.size(); ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
@@ -1223,6 +1336,7 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         for (size_t t = 0; t < buckets[k].problems.size(); ++t) {
             const int idx = buckets[k].indices[t];
             FPM_TRY(finish_collect(buckets[k].problems[t], a, results ? &results[idx] : nullptr));
+            if (capture) finish_capture(buckets[k].problems[t], a, &capture[idx]);
         }
     return Status::ok();
 }
@@ -1674,6 +1788,15 @@ int32_t fpm_run_batch(fpm_context* ctx, int32_t count, fpm_problem* const* probl
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
     return finish(ctx, run_batch(ctx, count, problems, params, results));
+}
+
+int32_t fpm_run_batch_resumable(fpm_context* ctx, int32_t count, fpm_problem* const* problems,
+                                const fpm_algorithm_params* params, const fpm_state_desc* resume,
+                                fpm_result_desc* results, fpm_state_desc* capture) {
+    if (!ctx || (count > 0 && !problems)) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return finish(ctx, run_batch(ctx, count, problems, params, results, resume, capture));
 }
 
 int32_t fpm_run_batch_host(fpm_context* ctx, int32_t count, const fpm_model_desc* models,

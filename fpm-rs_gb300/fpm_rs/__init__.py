@@ -19,6 +19,7 @@ from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasure
 from .experiment import (ArrayPose, CameraModel, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
+from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
 from .reconstruction import (AlternatingProjection, Epry, Fpie, GradientDescent, Mpie, ReconstructionProblem,
                              ReconstructionResult, RuntimeInfo, last_run_stats, run_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
@@ -40,11 +41,12 @@ def fft2(values, *, inverse: bool = False):
 
 
 __all__ = [
-    "AlternatingProjection", "ArrayPose", "CameraModel", "DeviceError", "Epry", "Fpie", "FpmError",
+    "AlternatingProjection", "ArrayPose", "CameraModel", "CheckpointEvery", "DeviceError", "Epry", "Fpie", "FpmError",
     "FrameOutOfRangeError", "GradientDescent", "Illumination", "ImagePlaneModel", "InvalidMeasurementsError",
     "InvalidModelError", "InvalidParameterError", "InvalidShapeError", "KVectorList", "LengthMismatchError",
     "MeasurementStack", "Mpie", "NumericalError", "Optics", "PlanarLEDArray", "PupilAberration",
-    "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo", "SimulationResult",
+    "ReconstructionCheckpoint", "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo",
+    "SimulationResult",
     "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
     "run_batch", "simulate", "suggest_reconstruction_shape",
 ]

@@ -23,7 +23,7 @@ EXPORTED = (
     "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
     "fpm_fft2", "fpm_forward_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
-    "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_last_run_stats",
+    "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
 )
 
 
@@ -71,6 +71,15 @@ class AlgorithmParams(C.Structure):
         ("pupil_step", C.c_double),
         ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
         ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
+    ]
+
+
+class StateDesc(C.Structure):
+    _fields_ = [
+        ("completed_iterations", C.c_int32), ("momentum_counter", C.c_int32),
+        ("object_spectrum", C.POINTER(C.c_double)), ("pupil", C.POINTER(C.c_double)),
+        ("velocity", C.POINTER(C.c_double)), ("anchor", C.POINTER(C.c_double)),
+        ("objectives", C.POINTER(C.c_double)),
     ]
 
 

@@ -18,7 +18,9 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native as N
-from .errors import InvalidMeasurementsError, InvalidModelError, InvalidShapeError, UnsupportedError
+from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
+from .errors import (InvalidMeasurementsError, InvalidModelError, InvalidParameterError, InvalidShapeError,
+                     UnsupportedError)
 from .model import ImagePlaneModel
 from .simulation import MeasurementStack
 
@@ -330,12 +332,14 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
     the exact frame order a single run would. With ``download=False`` the
     results stay on the device and ``None`` is returned per problem.
     """
-    if callbacks:
-        raise UnsupportedError("callbacks are not supported by the GB300 device path")
-    if resume_from is not None:
-        raise UnsupportedError("checkpoint resume is not supported by the GB300 device path")
-    params = algorithm._params(schedule)
+    callbacks = list(callbacks or [])
+    for cb in callbacks:
+        if not isinstance(cb, CheckpointEvery):
+            raise UnsupportedError("the GB300 device path supports the CheckpointEvery callback only")
     problems = list(problems)
+    if callbacks or resume_from is not None:
+        return _run_resumable(algorithm, problems, callbacks, resume_from, schedule, download)
+    params = algorithm._params(schedule)
     # Problems that are all still on the host take the overlapped path:
     # uploads and downloads run beside the reconstructions.
     host_path = len(problems) > 1 and len({id(p) for p in problems}) == len(problems) and all(
@@ -386,6 +390,115 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
         if p.name is not None:
             result.metadata["problem_name"] = p.name
         out.append(result)
+    return out
+
+
+def _state_arrays(problem, algorithm, iterations):
+    mh, mw = problem.reconstruction_shape
+    h, w = problem.image_shape
+    mpie = isinstance(algorithm, Mpie)
+    return dict(object_spectrum=np.zeros((mh, mw), np.complex128), pupil=np.zeros((h, w), np.complex128),
+                velocity=np.zeros((mh, mw), np.complex128) if mpie else None,
+                anchor=np.zeros((mh, mw), np.complex128) if mpie else None,
+                objectives=np.zeros(max(int(iterations), 1)))
+
+
+def _state_desc(arrays, completed, counter):
+    d = N.StateDesc()
+    d.completed_iterations = int(completed)
+    d.momentum_counter = int(counter)
+    for name in ("object_spectrum", "pupil", "velocity", "anchor", "objectives"):
+        setattr(d, name, N.ptr(arrays[name], C.c_double))
+    return d
+
+
+def _checkpoint_arrays(cp: ReconstructionCheckpoint, problem, algorithm):
+    """Host arrays of a checkpoint, validated against the problem and algorithm."""
+    if cp.algorithm != algorithm._name:
+        raise InvalidParameterError(f"checkpoint of {cp.algorithm} cannot resume {algorithm._name}")
+    mh, mw = problem.reconstruction_shape
+    h, w = problem.image_shape
+    if cp.object_spectrum.shape != (mh, mw) or cp.pupil.shape != (h, w):
+        raise InvalidShapeError("checkpoint arrays do not match the problem's shapes")
+    mpie = isinstance(algorithm, Mpie)
+    if mpie and (cp.velocity is None or cp.anchor is None):
+        raise InvalidParameterError("an mPIE checkpoint needs its velocity and anchor")
+    arrays = dict(object_spectrum=np.ascontiguousarray(cp.object_spectrum, np.complex128),
+                  pupil=np.ascontiguousarray(cp.pupil, np.complex128),
+                  velocity=np.ascontiguousarray(cp.velocity, np.complex128) if mpie else None,
+                  anchor=np.ascontiguousarray(cp.anchor, np.complex128) if mpie else None,
+                  objectives=np.asarray(cp.objectives + [0.0], np.float64))
+    return arrays
+
+
+def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, download):
+    """Runs in segments through fpm_run_batch_resumable: from a checkpoint,
+    and/or stopping at every CheckpointEvery boundary to save the state."""
+    if callbacks and len(problems) != 1:
+        raise UnsupportedError("CheckpointEvery is supported for single-problem runs")
+    if resume_from is not None and not isinstance(resume_from, (list, tuple)):
+        resume_from = [resume_from]
+    if resume_from is not None and len(resume_from) != len(problems):
+        raise InvalidParameterError("one checkpoint is needed per problem")
+    params = algorithm._params(schedule)
+    total = params.iterations
+    upload(problems)
+    handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
+    ctx = N.context()
+    keep = []
+    resume = None
+    start = 0
+    if resume_from is not None:
+        arrays = [_checkpoint_arrays(cp, p, algorithm) for cp, p in zip(resume_from, problems)]
+        keep.append(arrays)
+        start = resume_from[0].completed_iterations
+        resume = (N.StateDesc * len(problems))(
+            *[_state_desc(a, cp.completed_iterations, cp.momentum_counter) for a, cp in zip(arrays, resume_from)])
+    ends = sorted({k for cb in callbacks for k in range(start + 1, total) if k % cb.every == 0} | {total})
+    result_arrays = []
+    results = None
+    elapsed_total = 0.0
+    for end in ends:
+        params.iterations = end
+        captured = [_state_arrays(p, algorithm, end) for p in problems]
+        capture = (N.StateDesc * len(problems))(*[_state_desc(a, 0, 0) for a in captured])
+        last = end == ends[-1]
+        if last and download:
+            results = (N.ResultDesc * len(problems))()
+            for i, p in enumerate(problems):
+                mh, mw = p.reconstruction_shape
+                h, w = p.image_shape
+                a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
+                         pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(end, 1)))
+                for name in ("object", "object_spectrum", "pupil", "objectives"):
+                    setattr(results[i], name, N.ptr(a[name], C.c_double))
+                result_arrays.append(a)
+        t0 = time.perf_counter()
+        N.check(N.library().fpm_run_batch_resumable(ctx.handle, len(problems), handles, C.byref(params), resume,
+                                                    results, capture), ctx.handle)
+        elapsed_total += time.perf_counter() - t0
+        checkpoints = [ReconstructionCheckpoint(
+            completed_iterations=end, algorithm=algorithm._name, object_spectrum=a["object_spectrum"],
+            pupil=a["pupil"], velocity=a["velocity"], anchor=a["anchor"],
+            momentum_counter=capture[i].momentum_counter, objectives=[float(v) for v in a["objectives"][:end]])
+            for i, a in enumerate(captured)]
+        for cb in callbacks:
+            if end % cb.every == 0 and end > start:
+                cb.directory.mkdir(parents=True, exist_ok=True)
+                checkpoints[0].save(cb.path_for(end))
+        keep.append(captured)
+        resume = (N.StateDesc * len(problems))(
+            *[_state_desc(a, end, capture[i].momentum_counter) for i, a in enumerate(captured)])
+    if not download:
+        return [None] * len(problems)
+    out = []
+    for p, a in zip(problems, result_arrays):
+        trace = [(it + 1, float(a["objectives"][it]), elapsed_total) for it in range(total)]
+        out.append(ReconstructionResult(
+            object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
+            pupil_support=p.model.pupil_support, trace=trace,
+            runtime=RuntimeInfo(elapsed_total, total, False, algorithm._name),
+            recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background))
     return out
 
 

@@ -18,6 +18,8 @@
  *                                  fpm_problem_create_batch (many problems, one host scan)
  *   Runner::run / ReconstructionAlgorithm::run
  *                                  src/reconstruction/runner.rs:76-285 -> fpm_run
+ *   ReconstructionCheckpoint capture / run_from_checkpoint
+ *                                  src/reconstruction/checkpoint.rs:38-146 -> fpm_run_batch_resumable
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
  *                                  fpm_run_batch_host (host inputs, copies overlapped with the runs)
  *   Error / FpmError ............. src/error.rs:12, python/src/errors.rs:17-50 -> FPM_ERR_* + fpm_last_error
@@ -201,6 +203,33 @@ int32_t fpm_run(fpm_context *ctx, fpm_problem *problem, const fpm_algorithm_para
  * Each tile keeps the exact sequential frame order of a single run. */
 int32_t fpm_run_batch(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
                       const fpm_algorithm_params *params, fpm_result_desc *results);
+
+/* Resumable reconstruction state, the device counterpart of
+ * ReconstructionCheckpoint (src/reconstruction/checkpoint.rs:38-52):
+ * complex128 arrays, centred object spectrum. As an input it restores a run;
+ * as an output the library fills the caller's arrays. The device state is
+ * complex64, so a capture restores exactly and a resumed run reproduces the
+ * uninterrupted one bit for bit. */
+typedef struct {
+    int32_t completed_iterations;   /* complete iterations the state represents */
+    int32_t momentum_counter;       /* mPIE: effective frames since the last momentum event */
+    double *object_spectrum;        /* mh*mw complex */
+    double *pupil;                  /* h*w complex */
+    double *velocity;               /* mPIE: mh*mw complex, else NULL */
+    double *anchor;                 /* mPIE: mh*mw complex, else NULL */
+    double *objectives;             /* one objective per completed iteration (the trace) */
+} fpm_state_desc;
+
+/* fpm_run_batch that can start from saved state and save state at the end.
+ * `resume` (count entries, or NULL) restores each problem's state and runs
+ * iterations [completed_iterations, params->iterations); every entry must
+ * have the same completed_iterations. Results carry the full objective
+ * trace, resumed prefix included. `capture` (count entries, or NULL)
+ * receives each problem's state after the run; its objectives array holds
+ * params->iterations values. */
+int32_t fpm_run_batch_resumable(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
+                                const fpm_algorithm_params *params, const fpm_state_desc *resume,
+                                fpm_result_desc *results, fpm_state_desc *capture);
 
 /* fpm_problem_create_batch + fpm_run_batch for host-resident inputs, with
  * the copies overlapped: problems are created, run and downloaded in chunks

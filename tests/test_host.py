@@ -160,3 +160,23 @@ def test_model_json_round_trip(fpm, tmp_path):
     assert np.array_equal(loaded.crop_origins, model.crop_origins)
     assert np.array_equal(loaded.subpixel_offsets, model.subpixel_offsets)
     assert np.array_equal(loaded.pupil, model.pupil)
+
+
+def test_checkpoint_json_round_trip(fpm, tmp_path):
+    rng = np.random.default_rng(4)
+    obj = rng.standard_normal((42, 42)) + 1j * rng.standard_normal((42, 42))
+    pupil = rng.standard_normal((32, 32)) + 1j * rng.standard_normal((32, 32))
+    cp = fpm.ReconstructionCheckpoint(completed_iterations=3, algorithm="Mpie", object_spectrum=obj, pupil=pupil,
+                                      velocity=obj * 0.5, anchor=obj * 2, momentum_counter=7,
+                                      objectives=[3.0, 2.0, 1.5])
+    path = tmp_path / "checkpoint_00003.json"
+    cp.save(path)
+    back = fpm.ReconstructionCheckpoint.load(path)
+    assert back.completed_iterations == 3 and back.algorithm == "Mpie" and back.momentum_counter == 7
+    assert back.format_version == 2
+    for name in ("object_spectrum", "pupil", "velocity", "anchor"):
+        assert np.array_equal(getattr(back, name), getattr(cp, name)), name
+    assert back.objectives == [3.0, 2.0, 1.5]
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.CheckpointEvery(0, tmp_path)
+    assert fpm.CheckpointEvery(2, tmp_path).path_for(2).name == "checkpoint_00002.json"
