@@ -434,9 +434,33 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     const int batch_len = ALG == kAlgGradient ? P.gd_batch : 1;
     double trunc_res = 0.0, trunc_pw = 0.0, trunc_norm = 0.0;
     float trunc_scale = 0.f;
+    // Adaptive AP (src/algorithms/adaptive_alternating_projection.rs:245-307):
+    // the per-tile step, identical in every CTA of the cluster.
+    const bool adaptive = ALG == kAlgLocal && P.adaptive;
+    double ada_step = P.object_step;
+    double ada_previous = 0.0;
+    bool ada_has_previous = false;
     __syncthreads();
 
     for (int it = P.it_begin; it < P.it_end; ++it) {
+        if (adaptive && it > P.it_begin) {
+            // Objective of the pass just finished, from every CTA's partial.
+            cluster_barrier<K>();
+            double sum = 0.0;
+            for (int r = 0; r < C; ++r) sum += __ldcg(T.partials + (size_t)(it - 1) * C + r);
+            const double objective = T.weight_sum > 0.0 ? sum / T.weight_sum : NAN;
+            if (!isfinite(objective) || objective < 0.0) {
+                if (tid == 0) atomicOr(T.status, 32);
+            } else {
+                if (ada_has_previous) {
+                    const double progress = (ada_previous - objective) / fmax(ada_previous, (double)P.eps);
+                    if (progress <= P.progress_threshold)
+                        ada_step = fmax(ada_step * P.reduction_factor, P.minimum_step);
+                }
+                ada_previous = objective;
+                ada_has_previous = true;
+            }
+        }
         const int steps = truncating ? 2 * T.frame_count : T.frame_count;
         for (int step = 0; step < steps; ++step) {
             // Truncating: batch k covers steps [2kB, 2kB + 2b): b statistics
@@ -804,7 +828,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // Projection: O += w * step * adj(U). Gradient descent: O -= step *
                 // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
                 // (N^2 / valid) * adj(U).
-                const float scale = projection   ? fp.weight * P.object_step
+                const float scale = projection   ? fp.weight * (adaptive ? (float)ada_step : P.object_step)
                                     : gd_batched ? fp.weight * fp.valid_scale
                                                  : -P.object_step * fp.weight * fp.valid_scale;
                 float2* target = gd_batched ? T.gradient : T.object;

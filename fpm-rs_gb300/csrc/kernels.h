@@ -40,10 +40,12 @@ struct TileDesc {
     float2* gradient;          // mini-batch gradient descent: M*M accumulator, zero between batches
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event
-    int* status;               // bits: 1 non-finite momentum, 4 no valid data, 8 gauge, 16 truncation statistic
+    int* status;               // bits: 1 non-finite momentum, 4 no valid data, 8 gauge, 16 truncation statistic,
+                               // 32 adaptive pass objective
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
+    double weight_sum;         // sum of frame weights: the objective's denominator
     // Centred pupil rows [row_lo, row_hi] that hold a non-zero pupil value.
     // With a fixed pupil every other row of psi = P * patch is zero and the
     // correction U there is zero, so the engine skips those rows (EPRY,
@@ -68,6 +70,8 @@ struct EngineParams {
     int it_begin, it_end;
     int gd_batch;              // gradient descent frames per mini-batch (1: update after every frame)
     float trunc_threshold;     // gradient descent Poisson truncation threshold (0: off)
+    int adaptive;              // AP with the adaptive step controller
+    double progress_threshold, reduction_factor, minimum_step;
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.

@@ -769,7 +769,7 @@ Status create_problems(fpm_context* ctx, int count, const fpm_model_desc* mds, c
 
 Status validate_params(const fpm_algorithm_params* a) {
     if (!a) return Status::make(FPM_ERR_INVALID_PARAMETER, "algorithm parameters are required");
-    if (a->algorithm < FPM_ALG_AP || a->algorithm > FPM_ALG_GD)
+    if (a->algorithm < FPM_ALG_AP || a->algorithm > FPM_ALG_ADAPTIVE_AP)
         return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown algorithm %d", a->algorithm);
     if (a->iterations < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "iterations must be non-negative");
     if (!std::isfinite(a->object_step) || a->object_step <= 0.0)
@@ -797,6 +797,18 @@ Status validate_params(const fpm_algorithm_params* a) {
         if (a->recover_frame_gains || a->recover_background)
             return Status::make(FPM_ERR_UNSUPPORTED,
                                 "EPRY frame-gain and background recovery are not implemented on the GB300 device path");
+    }
+    if (a->algorithm == FPM_ALG_ADAPTIVE_AP) {
+        // AdaptiveAlternatingProjection::validate (src/algorithms/adaptive_alternating_projection.rs:350-403).
+        if (a->iterations == 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "iterations must be greater than zero");
+        if (!std::isfinite(a->progress_threshold) || a->progress_threshold < 0.0 || a->progress_threshold >= 1.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "progress_threshold must be finite, at least zero, and less than one");
+        if (!std::isfinite(a->reduction_factor) || a->reduction_factor <= 0.0 || a->reduction_factor >= 1.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "reduction_factor must be finite, greater than zero, and less than one");
+        if (!std::isfinite(a->minimum_object_step) || a->minimum_object_step <= 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "minimum_object_step must be finite and positive");
+        if (a->minimum_object_step > a->object_step)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "minimum_object_step must not exceed initial_object_step");
     }
     if (a->algorithm == FPM_ALG_GD) {
         if (a->recover_pupil)
@@ -951,6 +963,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.support = p->support_d.as<uint8_t>();
         T.meas = p->meas.as<float>();
         T.amplitude = p->amplitude ? 1 : 0;
+        T.weight_sum = p->weight_sum;
         // Centred rows holding a non-zero (FP32) pupil value.
         T.row_lo = N;
         T.row_hi = -1;
@@ -1065,7 +1078,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     fpm::EngineParams ep{};
     ep.tiles = br.tiles.as<fpm::TileDesc>();
     switch (a->algorithm) {
-        case FPM_ALG_AP: ep.alg = fpm::kAlgLocal; break;
+        case FPM_ALG_AP:
+        case FPM_ALG_ADAPTIVE_AP: ep.alg = fpm::kAlgLocal; break;
         case FPM_ALG_FPIE:
         case FPM_ALG_MPIE: ep.alg = fpm::kAlgRpie; break;
         case FPM_ALG_EPRY: ep.alg = canonical ? fpm::kAlgEpry : fpm::kAlgGlobal; break;
@@ -1080,7 +1094,12 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.interval = a->momentum_interval;
     ep.friction = (float)a->momentum_friction;
     ep.feedback = (float)a->momentum_feedback;
-    ep.loss = a->loss_type;
+    // The adaptive controller's objective is always amplitude MSE.
+    ep.loss = a->algorithm == FPM_ALG_ADAPTIVE_AP ? FPM_LOSS_AMPLITUDE_MSE : a->loss_type;
+    ep.adaptive = a->algorithm == FPM_ALG_ADAPTIVE_AP ? 1 : 0;
+    ep.progress_threshold = a->progress_threshold;
+    ep.reduction_factor = a->reduction_factor;
+    ep.minimum_step = a->minimum_object_step;
     ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
     ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
     auto engine = [&](int it0, int it1) -> Status {
@@ -1259,6 +1278,8 @@ Status record_stats(fpm_context* ctx, const std::vector<Bucket>& buckets,
 Status validate_resume(int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
                        const fpm_state_desc* resume, const fpm_state_desc* capture) {
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
+    if (resume && a->algorithm == FPM_ALG_ADAPTIVE_AP)
+        return Status::make(FPM_ERR_UNSUPPORTED, "adaptive alternating projection does not resume on the GB300 device path");
     for (int i = 0; i < count && resume; ++i) {
         const fpm_state_desc& r = resume[i];
         const fpm_problem* p = problems[i];

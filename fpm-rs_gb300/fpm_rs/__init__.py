@@ -20,7 +20,8 @@ from .experiment import (ArrayPose, CameraModel, Illumination, KVectorList, Opti
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
-from .reconstruction import (AlternatingProjection, Epry, Fpie, GradientDescent, Mpie, ReconstructionProblem,
+from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjection, Epry, Fpie, GradientDescent, Mpie,
+                             ReconstructionProblem,
                              ReconstructionResult, RuntimeInfo, last_run_stats, run_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
 
@@ -41,7 +42,7 @@ def fft2(values, *, inverse: bool = False):
 
 
 __all__ = [
-    "AlternatingProjection", "ArrayPose", "CameraModel", "CheckpointEvery", "DeviceError", "Epry", "Fpie", "FpmError",
+    "AdaptiveAlternatingProjection", "AlternatingProjection", "ArrayPose", "CameraModel", "CheckpointEvery", "DeviceError", "Epry", "Fpie", "FpmError",
     "FrameOutOfRangeError", "GradientDescent", "Illumination", "ImagePlaneModel", "InvalidMeasurementsError",
     "InvalidModelError", "InvalidParameterError", "InvalidShapeError", "KVectorList", "LengthMismatchError",
     "MeasurementStack", "Mpie", "NumericalError", "Optics", "PlanarLEDArray", "PupilAberration",

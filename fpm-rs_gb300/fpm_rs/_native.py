@@ -71,6 +71,7 @@ class AlgorithmParams(C.Structure):
         ("pupil_step", C.c_double),
         ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
         ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
+        ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
     ]
 
 

@@ -26,7 +26,7 @@ from .simulation import MeasurementStack
 
 _LOSSES = {"amplitude_mse": 0, "intensity_mse": 1, "poisson_nll": 2, "huber_amplitude": 3}
 _SCHEDULES = {"sequential": 0, "brightfield_first": 1, "spiral_out": 2, "snr_weighted": 3}
-_ALG = {"ap": 0, "fpie": 1, "mpie": 2, "epry": 3, "gd": 4}
+_ALG = {"ap": 0, "fpie": 1, "mpie": 2, "epry": 3, "gd": 4, "adaptive_ap": 5}
 
 
 def _loss(value: str) -> int:
@@ -199,6 +199,31 @@ class AlternatingProjection(_Algorithm):
     def _params(self, schedule):
         return _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
                             self.loss_type)
+
+
+class AdaptiveAlternatingProjection(_Algorithm):
+    """AP with the adaptive step rule of Zuo et al.
+    (src/algorithms/adaptive_alternating_projection.rs:96-126): after two
+    passes, a pass whose relative objective progress is at most
+    progress_threshold multiplies the step by reduction_factor, not below
+    minimum_object_step. The objective is always amplitude MSE."""
+
+    _name = "AdaptiveAlternatingProjection"
+    _code = _ALG["adaptive_ap"]
+
+    def __init__(self, *, iterations=50, initial_object_step=1.0, progress_threshold=0.01, reduction_factor=0.5,
+                 minimum_object_step=0.001, batch_size=1, epsilon=1e-10):
+        self.iterations, self.initial_object_step = iterations, initial_object_step
+        self.progress_threshold, self.reduction_factor = progress_threshold, reduction_factor
+        self.minimum_object_step, self.batch_size, self.epsilon = minimum_object_step, batch_size, epsilon
+
+    def _params(self, schedule):
+        p = _base_params(self, schedule, self.iterations, self.initial_object_step, self.batch_size, self.epsilon,
+                         "amplitude_mse")
+        p.progress_threshold = float(self.progress_threshold)
+        p.reduction_factor = float(self.reduction_factor)
+        p.minimum_object_step = float(self.minimum_object_step)
+        return p
 
 
 class Fpie(_Algorithm):

@@ -18,6 +18,8 @@
  *                                  fpm_problem_create_batch (many problems, one host scan)
  *   Runner::run / ReconstructionAlgorithm::run
  *                                  src/reconstruction/runner.rs:76-285 -> fpm_run
+ *   AdaptiveAlternatingProjection  src/algorithms/adaptive_alternating_projection.rs:245-470
+ *                                  -> fpm_run with FPM_ALG_ADAPTIVE_AP
  *   ReconstructionCheckpoint capture / run_from_checkpoint
  *                                  src/reconstruction/checkpoint.rs:38-146 -> fpm_run_batch_resumable
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
@@ -51,7 +53,7 @@ enum {
 
 enum { FPM_SHAPE_EXACT = 0, FPM_SHAPE_MINIMUM = 1, FPM_SHAPE_SMOOTH = 2, FPM_SHAPE_POWER_OF_TWO = 3 };
 enum { FPM_LOSS_AMPLITUDE_MSE = 0, FPM_LOSS_INTENSITY_MSE = 1, FPM_LOSS_POISSON_NLL = 2, FPM_LOSS_HUBER_AMPLITUDE = 3 };
-enum { FPM_ALG_AP = 0, FPM_ALG_FPIE = 1, FPM_ALG_MPIE = 2, FPM_ALG_EPRY = 3, FPM_ALG_GD = 4 };
+enum { FPM_ALG_AP = 0, FPM_ALG_FPIE = 1, FPM_ALG_MPIE = 2, FPM_ALG_EPRY = 3, FPM_ALG_GD = 4, FPM_ALG_ADAPTIVE_AP = 5 };
 enum {
     FPM_SCHEDULE_SEQUENTIAL = 0,
     FPM_SCHEDULE_BRIGHTFIELD_FIRST = 1,
@@ -120,6 +122,10 @@ typedef struct {
     int32_t recover_background;  /* EPRY extension (unsupported on the device path) */
     int32_t poisson_truncation;  /* GD: nonzero enables the Poisson truncation gate */
     double poisson_truncation_threshold; /* GD: the gate's threshold (finite, positive; Poisson NLL only) */
+    /* Adaptive AP (object_step is the initial step): the step is multiplied by
+     * reduction_factor, not below minimum_object_step, after a pass whose
+     * relative objective progress is at most progress_threshold. */
+    double progress_threshold, reduction_factor, minimum_object_step;
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */

@@ -1333,6 +1333,17 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         return out->status = fail(ORC_INVALID_PARAMETER, "epsilon must be finite and positive");
     if (prm->algorithm == ORC_ALG_GD && prm->recover_pupil)
         return out->status = fail(ORC_UNSUPPORTED, "gradient-descent pupil recovery is not restated");
+    /* AdaptiveAlternatingProjection::validate (src/algorithms/adaptive_alternating_projection.rs:350-403). */
+    if (prm->algorithm == ORC_ALG_ADAPTIVE_AP) {
+        if (prm->iterations == 0) return out->status = fail(ORC_INVALID_PARAMETER, "iterations must be greater than zero");
+        if (!isfinite(prm->progress_threshold) || prm->progress_threshold < 0.0 || prm->progress_threshold >= 1.0)
+            return out->status = fail(ORC_INVALID_PARAMETER, "progress_threshold must be in [0, 1)");
+        if (!isfinite(prm->reduction_factor) || prm->reduction_factor <= 0.0 || prm->reduction_factor >= 1.0)
+            return out->status = fail(ORC_INVALID_PARAMETER, "reduction_factor must be in (0, 1)");
+        if (!isfinite(prm->minimum_object_step) || prm->minimum_object_step <= 0.0 ||
+            prm->minimum_object_step > prm->object_step)
+            return out->status = fail(ORC_INVALID_PARAMETER, "minimum_object_step must be positive and at most the initial step");
+    }
     /* GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331). */
     if (prm->poisson_truncation_threshold != 0.0) {
         if (!isfinite(prm->poisson_truncation_threshold) || prm->poisson_truncation_threshold < 0.0)
@@ -1355,6 +1366,7 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
     int canonical = 0;
     switch (prm->algorithm) {
     case ORC_ALG_AP:
+    case ORC_ALG_ADAPTIVE_AP:
         cfg.denominator = 0;
         break;
     case ORC_ALG_FPIE:
@@ -1397,8 +1409,26 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         state_free(&s);
         return out->status = st;
     }
+    /* AdaptiveAlternatingProjection::begin_iteration
+     * (src/algorithms/adaptive_alternating_projection.rs:245-307): the step
+     * shrinks by reduction_factor (not below the minimum) when a pass's
+     * relative objective progress is at most progress_threshold. */
+    const int adaptive = prm->algorithm == ORC_ALG_ADAPTIVE_AP;
+    double previous_objective = NAN, last_objective = NAN;
     int *order = (int *)malloc(sizeof(int) * (size_t)p->frames);
     for (int it = 0; it < prm->iterations && !st; ++it) {
+        if (adaptive && it > 0) {
+            if (!isfinite(last_objective) || last_objective < 0.0) {
+                st = fail(ORC_NUMERICAL, "adaptive alternating projection produced an invalid pass objective");
+                break;
+            }
+            if (isfinite(previous_objective)) {
+                double progress = (previous_objective - last_objective) / fmax(previous_objective, prm->epsilon);
+                if (progress <= prm->progress_threshold)
+                    cfg.object_step = fmax(cfg.object_step * prm->reduction_factor, prm->minimum_object_step);
+            }
+            previous_objective = last_objective;
+        }
         st = schedule_order(p, prm->schedule, order);
         step_summary summary = {0.0, 0.0};
         for (int start = 0; start < p->frames && !st; start += prm->batch_size) {
@@ -1410,7 +1440,8 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
                 st = projection_update(&s, order + start, count, &cfg, &summary);
         }
         if (!st && canonical) st = canonicalize_gauge(&s);
-        if (out->objectives) out->objectives[it] = summary.weight_sum > 0.0 ? summary.objective_sum / summary.weight_sum : NAN;
+        last_objective = summary.weight_sum > 0.0 ? summary.objective_sum / summary.weight_sum : NAN;
+        if (out->objectives) out->objectives[it] = last_objective;
     }
     free(order);
     if (!st) {

@@ -36,7 +36,7 @@ enum { ORC_SHAPE_EXACT = 0, ORC_SHAPE_MINIMUM = 1, ORC_SHAPE_SMOOTH = 2, ORC_SHA
 
 enum { ORC_LOSS_AMPLITUDE_MSE = 0, ORC_LOSS_INTENSITY_MSE = 1, ORC_LOSS_POISSON_NLL = 2, ORC_LOSS_HUBER = 3 };
 
-enum { ORC_ALG_AP = 0, ORC_ALG_FPIE = 1, ORC_ALG_MPIE = 2, ORC_ALG_EPRY = 3, ORC_ALG_GD = 4 };
+enum { ORC_ALG_AP = 0, ORC_ALG_FPIE = 1, ORC_ALG_MPIE = 2, ORC_ALG_EPRY = 3, ORC_ALG_GD = 4, ORC_ALG_ADAPTIVE_AP = 5 };
 
 enum {
     ORC_SCHEDULE_SEQUENTIAL = 0,
@@ -94,6 +94,7 @@ typedef struct {
     int32_t recover_background;
     double background_step, background_min, background_max;
     double poisson_truncation_threshold;   /* GD: 0 disables the truncation gate */
+    double progress_threshold, reduction_factor, minimum_object_step;  /* adaptive AP controller */
 } orc_params;
 
 /* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */

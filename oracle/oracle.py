@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "libfpm_oracle.so")
 
 SHAPE_POLICIES = {"exact": 0, "minimum": 1, "smooth": 2, "power_of_two": 3}
 LOSSES = {"amplitude_mse": 0, "intensity_mse": 1, "poisson_nll": 2, "huber_amplitude": 3}
-ALGORITHMS = {"ap": 0, "fpie": 1, "mpie": 2, "epry": 3, "gd": 4}
+ALGORITHMS = {"ap": 0, "fpie": 1, "mpie": 2, "epry": 3, "gd": 4, "adaptive_ap": 5}
 SCHEDULES = {"sequential": 0, "brightfield_first": 1, "spiral_out": 2, "snr_weighted": 3}
 
 
@@ -96,6 +96,7 @@ class _Params(C.Structure):
         ("recover_background", C.c_int32), ("background_step", C.c_double),
         ("background_min", C.c_double), ("background_max", C.c_double),
         ("poisson_truncation_threshold", C.c_double),
+        ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
     ]
 
 
@@ -355,6 +356,8 @@ DEFAULTS = {
     "epry": dict(iterations=100, object_step=0.8, pupil_step=0.1, recover_pupil=True,
                  constrain_pupil=True),
     "gd": dict(iterations=100, object_step=0.5),
+    "adaptive_ap": dict(iterations=50, object_step=1.0, progress_threshold=0.01, reduction_factor=0.5,
+                        minimum_object_step=0.001),
 }
 
 
@@ -363,7 +366,8 @@ def params(algorithm: str, **kw) -> _Params:
                stability=0.0, momentum_interval=30, momentum_friction=0.9, momentum_feedback=0.9,
                recover_pupil=False, constrain_pupil=True, pupil_step=0.1, recover_gains=False,
                gain_step=0.2, gain_min=1e-6, gain_max=1e6, recover_background=False,
-               background_step=0.2, background_min=0.0, background_max=1e12, poisson_truncation_threshold=0.0)
+               background_step=0.2, background_min=0.0, background_max=1e12, poisson_truncation_threshold=0.0,
+               progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001)
     cfg.update(DEFAULTS[algorithm])
     cfg.update(kw)
     p = _Params()
@@ -374,7 +378,8 @@ def params(algorithm: str, **kw) -> _Params:
     p.schedule = SCHEDULES[cfg["schedule"]]
     for name in ("object_step", "epsilon", "stability", "momentum_friction", "momentum_feedback",
                  "pupil_step", "gain_step", "gain_min", "gain_max", "background_step",
-                 "background_min", "background_max", "poisson_truncation_threshold"):
+                 "background_min", "background_max", "poisson_truncation_threshold", "progress_threshold",
+                 "reduction_factor", "minimum_object_step"):
         setattr(p, name, float(cfg[name]))
     p.momentum_interval = int(cfg["momentum_interval"])
     p.recover_pupil = int(bool(cfg["recover_pupil"]))

@@ -399,3 +399,29 @@ def test_checkpoint_resume_rejects_mismatches(fpm, tmp_path):
         fpm.Mpie(iterations=3).run(problem, resume_from=cp)
     with pytest.raises(fpm.InvalidParameterError):
         fpm.AlternatingProjection(iterations=0).run(problem, resume_from=cp)
+
+
+@pytest.mark.parametrize("n,side,threshold", [(32, 5, 0.01), (64, 5, 0.9), (128, 3, 0.5)])
+def test_adaptive_alternating_projection(fpm, n, side, threshold):
+    """AdaptiveAlternatingProjection: the device controller reads each pass's
+    objective from the cluster's partials and shrinks the step like the
+    FP64 restatement does."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=61, photons=1e4)
+    kw = dict(iterations=6, progress_threshold=threshold, reduction_factor=0.5, minimum_object_step=0.05)
+    algo = fpm.AdaptiveAlternatingProjection(iterations=6, initial_object_step=1.0, progress_threshold=threshold,
+                                             reduction_factor=0.5, minimum_object_step=0.05)
+    result, expected = _run_both(fpm, algo, "adaptive_ap", kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    if threshold >= 0.5:
+        plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "ap", iterations=6)
+        assert oracle.complex_nrmse(plain["object"], expected["object"]) > 10 * NRMSE  # the step did shrink
+
+
+def test_adaptive_ap_validation(fpm):
+    model, omodel = helpers.planar_model(fpm, 3, 32)
+    problem = fpm.ReconstructionProblem(np.ones((model.frame_count, 32, 32)), model)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.AdaptiveAlternatingProjection(iterations=2, reduction_factor=1.0).run(problem)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.AdaptiveAlternatingProjection(iterations=2, minimum_object_step=2.0).run(problem)

@@ -236,3 +236,22 @@ def test_poisson_truncation_requires_poisson_loss_and_is_inert_when_wide():
                        poisson_truncation_threshold=0.05)
     loose = oracle.run(oracle.Problem(m, data * 1.7), "gd", iterations=3, batch_size=5, loss_type="poisson_nll")
     assert not np.array_equal(tight["object_spectrum"], loose["object_spectrum"])
+
+
+def test_adaptive_ap_step_controller():
+    # AdaptiveAlternatingProjection (src/algorithms/adaptive_alternating_projection.rs:245-307):
+    # with progress_threshold 0 a pass that improves keeps the step; with a
+    # threshold no pass can meet, the step halves every pass after the second
+    # (floored at the minimum), so the run differs from AP at a fixed step.
+    m, data = _direct_problem(13)
+    ap = oracle.run(oracle.Problem(m, data), "ap", iterations=4)
+    keep = oracle.run(oracle.Problem(m, data), "adaptive_ap", iterations=4, progress_threshold=0.0)
+    assert np.array_equal(ap["object_spectrum"], keep["object_spectrum"])
+    shrink = oracle.run(oracle.Problem(m, data), "adaptive_ap", iterations=4, progress_threshold=0.999,
+                        minimum_object_step=0.3)
+    assert not np.array_equal(ap["object_spectrum"], shrink["object_spectrum"])
+    two = oracle.run(oracle.Problem(m, data), "adaptive_ap", iterations=2, progress_threshold=0.999)
+    ap2 = oracle.run(oracle.Problem(m, data), "ap", iterations=2)
+    assert np.array_equal(ap2["object_spectrum"], two["object_spectrum"])  # no comparison before pass 3
+    with pytest.raises(oracle.OracleError):
+        oracle.run(oracle.Problem(m, data), "adaptive_ap", iterations=2, reduction_factor=1.0)
