@@ -415,7 +415,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     const int M = T.M;
     const long long ostride = M + (M & 1);
     const int i_lo = C == 1 ? 0 : c * R;
-    constexpr bool projection = ALG != kAlgGradient;
+    constexpr bool gradient = ALG == kAlgGradient || ALG == kAlgGradientTruncated;
+    constexpr bool projection = !gradient;
     constexpr bool epry = ALG == kAlgEpry;
     // Rows of psi that can be non-zero (all rows when the pupil evolves).
     const int row_lo = epry ? 0 : T.row_lo, row_hi = epry ? N - 1 : T.row_hi;
@@ -425,18 +426,18 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     double loss_acc = 0.0;
     // Mini-batch gradient descent: frames add into T.gradient and the object
     // moves once per batch of gd_batch consecutive frames of the order.
-    const bool gd_batched = ALG == kAlgGradient && P.gd_batch > 1;
+    const bool gd_batched = gradient && P.gd_batch > 1;
     int batch_active = 0;
     // Poisson truncation (src/algorithms/gradient_descent.rs:701-792): each
     // batch is walked twice, first forward-only for the residual statistic,
     // then with the gate |y - p| <= scale * sqrt(p) on the gradient.
-    const bool truncating = ALG == kAlgGradient && P.trunc_threshold > 0.f;
-    const int batch_len = ALG == kAlgGradient ? P.gd_batch : 1;
+    constexpr bool truncating = ALG == kAlgGradientTruncated;
+    const int batch_len = gradient ? P.gd_batch : 1;
     double trunc_res = 0.0, trunc_pw = 0.0, trunc_norm = 0.0;
     float trunc_scale = 0.f;
     // Adaptive AP (src/algorithms/adaptive_alternating_projection.rs:245-307):
     // the per-tile step, identical in every CTA of the cluster.
-    const bool adaptive = ALG == kAlgLocal && P.adaptive;
+    constexpr bool adaptive = ALG == kAlgLocalAdaptive;
     double ada_step = P.object_step;
     double ada_previous = 0.0;
     bool ada_has_previous = false;
@@ -625,7 +626,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)k * mstride] != 0 ? 1u : 0u) << k;
                     }
                 }
-                if constexpr (ALG == kAlgGradient) {
+                if constexpr (truncating) {
                     if (stats) {
                         // Statistic: |y - p| and the count over unmasked pixels.
                         float res = 0.f, cnt = 0.f;
@@ -785,7 +786,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                             const float2 d = csub(psi, cmul(pt, pv));
                             const float pw = cnorm2(pv);
                             float inv_den;
-                            if constexpr (ALG == kAlgLocal)
+                            if constexpr (ALG == kAlgLocal || ALG == kAlgLocalAdaptive)
                                 inv_den = 1.0f / (pw + P.eps);
                             else if constexpr (ALG == kAlgRpie)
                                 inv_den = 1.0f / ((1.f - P.alpha) * pw + P.alpha * max_p2 + P.eps);
@@ -1153,12 +1154,27 @@ cudaError_t launch_cluster(Kern kernel, const Params& p, int clusters, cudaStrea
 
 // Per-size entry points; each tile size is instantiated in its own
 // translation unit (engine_n32.cu ... engine_n256.cu) so they build in parallel.
+// One algorithm family's engine launch (amplitude-MSE specialisation, or the
+// runtime-selected loss). Instantiated per tile size; the gradient-descent
+// and adaptive families live in their own translation units
+// (engine_n*_gd.cu) so each size builds as two parallel halves.
+template <int N_, int ALG>
+cudaError_t launch_engine_alg(const EngineParams& p, int tiles, cudaStream_t s) {
+    if (p.loss == 0) return launch_cluster<N_>(engine_kernel<N_, ALG, 0>, p, tiles, s);
+    return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+}
+
+#define FPM_ENGINE_SECOND_HALF(N, SPEC)                                                                  \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgGradient>(const EngineParams&, int, cudaStream_t); \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgGradientTruncated>(const EngineParams&, int,      \
+                                                                          cudaStream_t);               \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgLocalAdaptive>(const EngineParams&, int, cudaStream_t);
+
 template <int N_>
 struct EngineEntry {
     template <int ALG>
     static cudaError_t engine_alg(const EngineParams& p, int tiles, cudaStream_t s) {
-        if (p.loss == 0) return launch_cluster<N_>(engine_kernel<N_, ALG, 0>, p, tiles, s);
-        return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+        return launch_engine_alg<N_, ALG>(p, tiles, s);
     }
 
     static cudaError_t engine(const EngineParams& p, int tiles, cudaStream_t s) {
@@ -1168,6 +1184,8 @@ struct EngineEntry {
             case kAlgGlobal: return engine_alg<kAlgGlobal>(p, tiles, s);
             case kAlgEpry: return engine_alg<kAlgEpry>(p, tiles, s);
             case kAlgGradient: return engine_alg<kAlgGradient>(p, tiles, s);
+            case kAlgGradientTruncated: return engine_alg<kAlgGradientTruncated>(p, tiles, s);
+            case kAlgLocalAdaptive: return engine_alg<kAlgLocalAdaptive>(p, tiles, s);
             default: return cudaErrorInvalidValue;
         }
     }

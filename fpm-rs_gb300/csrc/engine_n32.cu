@@ -2,5 +2,6 @@
 #include "engine_impl.cuh"
 
 namespace fpm {
+FPM_ENGINE_SECOND_HALF(32, extern)  // in engine_n32_gd.cu
 template struct EngineEntry<32>;
 }  // namespace fpm

@@ -57,7 +57,15 @@ struct TileDesc {
 // carries only its own update code: AP (local |P|^2 denominator), FPIE/mPIE
 // (rPIE blend), EPRY without and with pupil recovery (global max |P|^2), and
 // the Wirtinger gradient.
-enum EngineAlg { kAlgLocal = 0, kAlgRpie = 1, kAlgGlobal = 2, kAlgEpry = 3, kAlgGradient = 4 };
+enum EngineAlg {
+    kAlgLocal = 0,
+    kAlgRpie = 1,
+    kAlgGlobal = 2,
+    kAlgEpry = 3,
+    kAlgGradient = 4,
+    kAlgGradientTruncated = 5,  // gradient descent with the Poisson truncation gate
+    kAlgLocalAdaptive = 6,      // AP with the adaptive step controller
+};
 
 struct EngineParams {
     const TileDesc* tiles;
@@ -70,8 +78,7 @@ struct EngineParams {
     int it_begin, it_end;
     int gd_batch;              // gradient descent frames per mini-batch (1: update after every frame)
     float trunc_threshold;     // gradient descent Poisson truncation threshold (0: off)
-    int adaptive;              // AP with the adaptive step controller
-    double progress_threshold, reduction_factor, minimum_step;
+    double progress_threshold, reduction_factor, minimum_step;  // adaptive AP controller
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.

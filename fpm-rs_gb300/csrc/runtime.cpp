@@ -1078,12 +1078,12 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     fpm::EngineParams ep{};
     ep.tiles = br.tiles.as<fpm::TileDesc>();
     switch (a->algorithm) {
-        case FPM_ALG_AP:
-        case FPM_ALG_ADAPTIVE_AP: ep.alg = fpm::kAlgLocal; break;
+        case FPM_ALG_AP: ep.alg = fpm::kAlgLocal; break;
+        case FPM_ALG_ADAPTIVE_AP: ep.alg = fpm::kAlgLocalAdaptive; break;
         case FPM_ALG_FPIE:
         case FPM_ALG_MPIE: ep.alg = fpm::kAlgRpie; break;
         case FPM_ALG_EPRY: ep.alg = canonical ? fpm::kAlgEpry : fpm::kAlgGlobal; break;
-        default: ep.alg = fpm::kAlgGradient; break;
+        default: ep.alg = a->poisson_truncation ? fpm::kAlgGradientTruncated : fpm::kAlgGradient; break;
     }
     ep.alpha = (float)a->stability;
     ep.eps = (float)a->epsilon;
@@ -1096,7 +1096,6 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.feedback = (float)a->momentum_feedback;
     // The adaptive controller's objective is always amplitude MSE.
     ep.loss = a->algorithm == FPM_ALG_ADAPTIVE_AP ? FPM_LOSS_AMPLITUDE_MSE : a->loss_type;
-    ep.adaptive = a->algorithm == FPM_ALG_ADAPTIVE_AP ? 1 : 0;
     ep.progress_threshold = a->progress_threshold;
     ep.reduction_factor = a->reduction_factor;
     ep.minimum_step = a->minimum_object_step;
