@@ -136,6 +136,19 @@ cudaError_t launch_shift_to_state(double2* const* scratch, float2* const* object
                                   float2* const* velocity, int count, int m, cudaStream_t s);
 cudaError_t launch_state_to_natural(const float2* const* object, double2* const* scratch, int count, int m,
                                     cudaStream_t s);
+// Detector response (CameraModel::measure_frame, src/simulation/camera.rs:249-290).
+struct CameraParams {
+    double photons_per_pixel, gain_counts_per_electron, offset_counts, read_noise, dark_current;
+    double maximum_count;             // clamp; infinity when unbounded
+    int shot_noise, quantize;
+    const double* sensitivity;        // per-pixel sensitivity of one frame, or null
+    unsigned long long seed;
+};
+// counts[e] from intensity[e] for e < total (frames of frame_len pixels).
+// status bit 1: a Poisson draw hit its iteration bound.
+cudaError_t launch_camera(const float* intensity, double* counts, long long total, long long frame_len,
+                          const CameraParams& params, int* status, cudaStream_t s);
+
 // Dense complex128 rows narrowed to complex64 rows of stride dst_stride.
 cudaError_t launch_narrow(const double2* src, int rows, int cols, float2* dst, long long dst_stride, cudaStream_t s);
 // Complex64 rows (row stride src_stride) widened to dense complex128.

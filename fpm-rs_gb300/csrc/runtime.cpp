@@ -1478,6 +1478,103 @@ void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream) 
 
 // ====================================================================== ABI
 
+namespace {
+
+// Forward intensity stack into the device buffer `out` (float, F*N*N).
+Status forward_stack_device(fpm_context* ctx, const fpm_model_desc* md, const double* object, DeviceBuffer& out,
+                            cudaStream_t s) {
+        FPM_TRY(validate_model(md));
+        if (!object) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        const int N = md->image_height, M = md->recon_height, F = md->sources;
+        if (md->image_width != N || !fpm::engine_supported(N) || md->recon_width != M)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "the GB300 device path supports square detector frames of 32, 64, 128 or 256 pixels");
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        const size_t n2 = (size_t)N * N, m2 = (size_t)M * M;
+        const long long ms = M + (M & 1);
+        // Frame constants (gains, stencils) as for a problem without masks.
+        std::vector<fpm::FrameParam> params(F);
+        for (int f = 0; f < F; ++f) {
+            Axis r{}, c{};
+            const double orow = md->offset_row ? md->offset_row[f] : 0.0, ocol = md->offset_col ? md->offset_col[f] : 0.0;
+            FPM_TRY(interpolation_axis(md->crop_start_row[f], N, M, orow, r));
+            FPM_TRY(interpolation_axis(md->crop_start_col[f], N, M, ocol, c));
+            fpm::FrameParam fp{};
+            const bool zero = std::fabs(orow) <= 1e-12 && std::fabs(ocol) <= 1e-12;
+            fp.lower_row = zero ? (int)md->crop_start_row[f] : (int)r.lower_start;
+            fp.lower_col = zero ? (int)md->crop_start_col[f] : (int)c.lower_start;
+            fp.has_upper_row = zero ? 0 : (r.upper ? 1 : 0);
+            fp.has_upper_col = zero ? 0 : (c.upper ? 1 : 0);
+            fp.w00 = zero ? 1.f : (float)(r.lower_weight * c.lower_weight);
+            fp.w01 = zero ? 0.f : (float)(r.lower_weight * c.upper_weight);
+            fp.w10 = zero ? 0.f : (float)(r.upper_weight * c.lower_weight);
+            fp.w11 = zero ? 0.f : (float)(r.upper_weight * c.upper_weight);
+            const double g = md->frame_gains ? md->frame_gains[f] : 1.0;
+            if (!(g > 0.0)) return Status::make(FPM_ERR_INVALID_MODEL, "frame %d has invalid gain %g", f, g);
+            fp.gain = (float)g;
+            fp.weight = 1.f;
+            params[f] = fp;
+        }
+        DeviceBuffer d_params, d_pupil, d_obj64, d_state, d_ptrs, d_ptrs2, d_bg;
+        FPM_TRY(upload_array(d_params, params, s));
+        std::vector<float2> pf(n2);
+        for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)md->pupil[2 * i], (float)md->pupil[2 * i + 1]);
+        FPM_TRY(upload_array(d_pupil, pf, s));
+        FPM_TRY(d_obj64.ensure(sizeof(double2) * m2));
+        FPM_CUDA(cudaMemcpyAsync(d_obj64.ptr, object, sizeof(double2) * m2, cudaMemcpyHostToDevice, s));
+        FPM_TRY(d_state.ensure(sizeof(float2) * (size_t)M * ms));
+        std::vector<double2*> p64 = {d_obj64.as<double2>()};
+        std::vector<float2*> pst = {d_state.as<float2>()};
+        FPM_TRY(upload_array(d_ptrs, p64, s));
+        FPM_TRY(upload_array(d_ptrs2, pst, s));
+        // object_spectrum (src/simulation/simulator.rs:209-226): forward FFT, fftshift.
+        FPM_TRY(fft2_device(ctx, d_ptrs.as<double2*>(), 1, M, M, false, s));
+        FPM_CUDA(fpm::launch_shift_to_state(d_ptrs.as<double2*>(), d_ptrs2.as<float2*>(), nullptr, nullptr, 1, M, s));
+        fpm::ForwardParams fwd{};
+        fwd.object = d_state.as<float2>();
+        fwd.pupil = d_pupil.as<float2>();
+        fwd.params = d_params.as<fpm::FrameParam>();
+        if (md->background) {
+            std::vector<float> bg(md->background, md->background + md->background_len);
+            FPM_TRY(upload_array(d_bg, bg, s));
+            fwd.background = d_bg.as<float>();
+            fwd.background_stride = md->background_len == (int64_t)n2 ? 0 : (long long)n2;
+        }
+        FPM_TRY(out.ensure(sizeof(float) * n2 * F));
+        fwd.out = out.as<float>();
+        fwd.M = M;
+        fwd.frame_count = F;
+        FPM_CUDA(fpm::launch_forward(N, fwd, s));
+        // The temporaries above are freed on return: wait for the kernels that use them.
+        FPM_CUDA(cudaStreamSynchronize(s));
+        return Status::ok();
+}
+
+Status validate_camera(const fpm_camera_desc* c, size_t frame_len) {
+    if (!c) return Status::ok();
+    auto bad = [](double v) { return !std::isfinite(v) || v < 0.0; };
+    if (!std::isfinite(c->photons_per_pixel) || c->photons_per_pixel <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "photons_per_pixel must be finite and positive");
+    if (!std::isfinite(c->gain_counts_per_electron) || c->gain_counts_per_electron <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "gain_counts_per_electron must be finite and positive");
+    if (!std::isfinite(c->offset_counts) || bad(c->read_noise_electrons) || bad(c->dark_current_electrons))
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "offset, read noise and dark current must be finite (noise and dark current non-negative)");
+    if (std::isnan(c->maximum_count) || c->maximum_count < 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "maximum_count must be non-negative");
+    if (c->pixel_sensitivity)
+        for (size_t i = 0; i < frame_len; ++i)
+            if (bad(c->pixel_sensitivity[i]))
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "pixel_sensitivity must be finite and non-negative");
+    if (c->bad_pixel_count < 0 || (c->bad_pixel_count > 0 && !c->bad_pixels))
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "bad pixel list is invalid");
+    for (int64_t k = 0; k < c->bad_pixel_count; ++k)
+        if (c->bad_pixels[k] < 0 || (size_t)c->bad_pixels[k] >= frame_len)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "bad_pixels indices must be below the frame size %zu", frame_len);
+    return Status::ok();
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* fpm_global_last_error(void) { return g_global_error.c_str(); }
@@ -1688,77 +1785,79 @@ int32_t fpm_fft2(fpm_context* ctx, double* values, int32_t height, int32_t width
     return finish(ctx, body());
 }
 
+
 int32_t fpm_forward_stack(fpm_context* ctx, const fpm_model_desc* md, const double* object, double* intensities) {
     if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
     std::lock_guard<std::mutex> lock(ctx->mu);
     auto body = [&]() -> Status {
+        if (!intensities) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
         FPM_TRY(validate_model(md));
-        if (!object || !intensities) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
-        const int N = md->image_height, M = md->recon_height, F = md->sources;
-        if (md->image_width != N || !fpm::engine_supported(N) || md->recon_width != M)
-            return Status::make(FPM_ERR_UNSUPPORTED,
-                                "the GB300 device path supports square detector frames of 32, 64, 128 or 256 pixels");
-        FPM_CUDA(cudaSetDevice(ctx->device));
         cudaStream_t s = ctx->streams[0];
-        const size_t n2 = (size_t)N * N, m2 = (size_t)M * M;
-        const long long ms = M + (M & 1);
-        // Frame constants (gains, stencils) as for a problem without masks.
-        std::vector<fpm::FrameParam> params(F);
-        for (int f = 0; f < F; ++f) {
-            Axis r{}, c{};
-            const double orow = md->offset_row ? md->offset_row[f] : 0.0, ocol = md->offset_col ? md->offset_col[f] : 0.0;
-            FPM_TRY(interpolation_axis(md->crop_start_row[f], N, M, orow, r));
-            FPM_TRY(interpolation_axis(md->crop_start_col[f], N, M, ocol, c));
-            fpm::FrameParam fp{};
-            const bool zero = std::fabs(orow) <= 1e-12 && std::fabs(ocol) <= 1e-12;
-            fp.lower_row = zero ? (int)md->crop_start_row[f] : (int)r.lower_start;
-            fp.lower_col = zero ? (int)md->crop_start_col[f] : (int)c.lower_start;
-            fp.has_upper_row = zero ? 0 : (r.upper ? 1 : 0);
-            fp.has_upper_col = zero ? 0 : (c.upper ? 1 : 0);
-            fp.w00 = zero ? 1.f : (float)(r.lower_weight * c.lower_weight);
-            fp.w01 = zero ? 0.f : (float)(r.lower_weight * c.upper_weight);
-            fp.w10 = zero ? 0.f : (float)(r.upper_weight * c.lower_weight);
-            fp.w11 = zero ? 0.f : (float)(r.upper_weight * c.upper_weight);
-            const double g = md->frame_gains ? md->frame_gains[f] : 1.0;
-            if (!(g > 0.0)) return Status::make(FPM_ERR_INVALID_MODEL, "frame %d has invalid gain %g", f, g);
-            fp.gain = (float)g;
-            fp.weight = 1.f;
-            params[f] = fp;
-        }
-        DeviceBuffer d_params, d_pupil, d_obj64, d_state, d_out, d_ptrs, d_ptrs2, d_bg;
-        FPM_TRY(upload_array(d_params, params, s));
-        std::vector<float2> pf(n2);
-        for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)md->pupil[2 * i], (float)md->pupil[2 * i + 1]);
-        FPM_TRY(upload_array(d_pupil, pf, s));
-        FPM_TRY(d_obj64.ensure(sizeof(double2) * m2));
-        FPM_CUDA(cudaMemcpyAsync(d_obj64.ptr, object, sizeof(double2) * m2, cudaMemcpyHostToDevice, s));
-        FPM_TRY(d_state.ensure(sizeof(float2) * (size_t)M * ms));
-        std::vector<double2*> p64 = {d_obj64.as<double2>()};
-        std::vector<float2*> pst = {d_state.as<float2>()};
-        FPM_TRY(upload_array(d_ptrs, p64, s));
-        FPM_TRY(upload_array(d_ptrs2, pst, s));
-        // object_spectrum (src/simulation/simulator.rs:209-226): forward FFT, fftshift.
-        FPM_TRY(fft2_device(ctx, d_ptrs.as<double2*>(), 1, M, M, false, s));
-        FPM_CUDA(fpm::launch_shift_to_state(d_ptrs.as<double2*>(), d_ptrs2.as<float2*>(), nullptr, nullptr, 1, M, s));
-        fpm::ForwardParams fwd{};
-        fwd.object = d_state.as<float2>();
-        fwd.pupil = d_pupil.as<float2>();
-        fwd.params = d_params.as<fpm::FrameParam>();
-        if (md->background) {
-            std::vector<float> bg(md->background, md->background + md->background_len);
-            FPM_TRY(upload_array(d_bg, bg, s));
-            fwd.background = d_bg.as<float>();
-            fwd.background_stride = md->background_len == (int64_t)n2 ? 0 : (long long)n2;
-        }
-        FPM_TRY(d_out.ensure(sizeof(float) * n2 * F));
-        fwd.out = d_out.as<float>();
-        fwd.M = M;
-        fwd.frame_count = F;
-        FPM_CUDA(fpm::launch_forward(N, fwd, s));
-        std::vector<float> host(n2 * F);
-        FPM_CUDA(cudaMemcpyAsync(host.data(), d_out.ptr, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, s));
+        DeviceBuffer d_out;
+        FPM_TRY(forward_stack_device(ctx, md, object, d_out, s));
+        const size_t total = (size_t)md->image_height * md->image_width * md->sources;
+        std::vector<float> host(total);
+        FPM_CUDA(cudaMemcpyAsync(host.data(), d_out.ptr, sizeof(float) * total, cudaMemcpyDeviceToHost, s));
         FPM_CUDA(cudaStreamSynchronize(s));
-        for (size_t i = 0; i < host.size(); ++i) intensities[i] = host[i];
+        for (size_t i = 0; i < total; ++i) intensities[i] = host[i];
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_simulate_stack(fpm_context* ctx, const fpm_model_desc* md, const double* object,
+                           const fpm_camera_desc* camera, uint64_t seed, double* counts) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        if (!counts) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        FPM_TRY(validate_model(md));
+        const size_t frame_len = (size_t)md->image_height * md->image_width;
+        FPM_TRY(validate_camera(camera, frame_len));
+        const size_t total = frame_len * md->sources;
+        cudaStream_t s = ctx->streams[0];
+        DeviceBuffer d_out, d_counts, d_sens, d_status;
+        FPM_TRY(forward_stack_device(ctx, md, object, d_out, s));
+        fpm::CameraParams cp{};
+        if (camera) {
+            cp.photons_per_pixel = camera->photons_per_pixel;
+            cp.gain_counts_per_electron = camera->gain_counts_per_electron;
+            cp.offset_counts = camera->offset_counts;
+            cp.read_noise = camera->read_noise_electrons;
+            cp.dark_current = camera->dark_current_electrons;
+            cp.maximum_count = camera->maximum_count;
+            cp.shot_noise = camera->shot_noise;
+            cp.quantize = camera->quantize;
+            if (camera->pixel_sensitivity) {
+                FPM_TRY(d_sens.ensure(sizeof(double) * frame_len));
+                FPM_CUDA(cudaMemcpyAsync(d_sens.ptr, camera->pixel_sensitivity, sizeof(double) * frame_len,
+                                         cudaMemcpyHostToDevice, s));
+                cp.sensitivity = d_sens.as<double>();
+            }
+        } else {
+            // No camera: the intensities themselves (CameraModel::ideal).
+            cp.photons_per_pixel = 1.0;
+            cp.gain_counts_per_electron = 1.0;
+            cp.maximum_count = INFINITY;
+        }
+        cp.seed = seed;
+        FPM_TRY(d_counts.ensure(sizeof(double) * total));
+        FPM_TRY(d_status.ensure(sizeof(int)));
+        FPM_CUDA(cudaMemsetAsync(d_status.ptr, 0, sizeof(int), s));
+        FPM_CUDA(fpm::launch_camera(d_out.as<float>(), d_counts.as<double>(), (long long)total, (long long)frame_len, cp,
+                                    d_status.as<int>(), s));
+        int status = 0;
+        FPM_CUDA(cudaMemcpyAsync(counts, d_counts.ptr, sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaMemcpyAsync(&status, d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaStreamSynchronize(s));
+        if (status) return Status::make(FPM_ERR_NUMERICAL, "a Poisson draw did not terminate within its bound");
+        if (camera && camera->bad_pixel_count > 0) {
+            double value = std::isnan(camera->bad_pixel_value) ? camera->maximum_count : camera->bad_pixel_value;
+            value = std::min(std::max(value, 0.0), camera->maximum_count);
+            if (camera->quantize) value = std::round(value);
+            for (int f = 0; f < md->sources; ++f)
+                for (int64_t k = 0; k < camera->bad_pixel_count; ++k) counts[(size_t)f * frame_len + camera->bad_pixels[k]] = value;
+        }
         return Status::ok();
     };
     return finish(ctx, body());

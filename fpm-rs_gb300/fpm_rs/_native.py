@@ -22,7 +22,7 @@ LIB_PATH = os.environ.get("FPM_GPU_LIBRARY", os.path.join(PACKAGE_ROOT, "libfpm_
 EXPORTED = (
     "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
-    "fpm_fft2", "fpm_forward_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
+    "fpm_fft2", "fpm_forward_stack", "fpm_simulate_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
 )
 
@@ -72,6 +72,16 @@ class AlgorithmParams(C.Structure):
         ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
         ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
         ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
+    ]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [
+        ("photons_per_pixel", C.c_double), ("gain_counts_per_electron", C.c_double), ("offset_counts", C.c_double),
+        ("read_noise_electrons", C.c_double), ("dark_current_electrons", C.c_double),
+        ("shot_noise", C.c_int32), ("quantize", C.c_int32), ("maximum_count", C.c_double),
+        ("pixel_sensitivity", C.POINTER(C.c_double)), ("bad_pixels", C.POINTER(C.c_int64)),
+        ("bad_pixel_count", C.c_int64), ("bad_pixel_value", C.c_double),
     ]
 
 

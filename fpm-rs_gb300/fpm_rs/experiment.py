@@ -211,7 +211,8 @@ class Illumination:
 class CameraModel:
     """Detector response and acquisition noise (src/simulation/camera.rs:249-318).
 
-    Noise is drawn from NumPy's PCG64 generator, not the reference's ChaCha12
+    Applied on the GPU by fpm_simulate_stack. Noise comes from a counter-based
+    Philox-4x32-10 stream keyed by the seed, not the reference's ChaCha12
     stream, so simulated counts match the reference only in distribution.
     """
 
@@ -240,24 +241,59 @@ class CameraModel:
             limit = min(limit, float(self.saturation_counts))
         return limit
 
-    def measure(self, intensity: np.ndarray, rng: np.random.Generator) -> np.ndarray:
-        """CameraModel::measure_frame applied to every frame in order."""
-        values = np.maximum(intensity, 0.0)
+    def validate_for_frame(self, frame_len: int) -> None:
+        """CameraModel::validate / validate_for_frame (src/simulation/camera.rs)."""
+        for name in ("photons_per_pixel", "gain_counts_per_electron"):
+            value = float(getattr(self, name))
+            if not math.isfinite(value) or value <= 0.0:
+                raise InvalidParameterError(f"{name} must be finite and positive")
+        if (not math.isfinite(self.offset_counts) or not math.isfinite(self.read_noise_electrons)
+                or self.read_noise_electrons < 0.0 or not math.isfinite(self.dark_current_electrons)
+                or self.dark_current_electrons < 0.0):
+            raise InvalidParameterError(
+                "camera noise/offset: offset must be finite; read noise and dark current must be non-negative")
+        if self.bit_depth is not None and not 1 <= int(self.bit_depth) <= 32:
+            raise InvalidParameterError("bit_depth must be between 1 and 32")
+        if self.saturation_counts is not None and (not math.isfinite(self.saturation_counts)
+                                                   or self.saturation_counts <= 0.0):
+            raise InvalidParameterError("saturation_counts must be finite and positive")
+        if self.bad_pixel_value_counts is not None and (not math.isfinite(self.bad_pixel_value_counts)
+                                                        or self.bad_pixel_value_counts < 0.0):
+            raise InvalidParameterError("bad_pixel_value_counts must be finite and non-negative")
+        if self.bad_pixels and self.bad_pixel_value_counts is None and not math.isfinite(self.maximum_count()):
+            raise InvalidParameterError("bad_pixels: a finite bad-pixel value or camera maximum is required")
         if self.pixel_sensitivity is not None:
-            values = values * np.asarray(self.pixel_sensitivity, dtype=np.float64)
-        electrons = values * self.photons_per_pixel + self.dark_current_electrons
-        if self.shot_noise:
-            electrons = rng.poisson(electrons).astype(np.float64)
-        if self.read_noise_electrons > 0.0:
-            electrons = electrons + rng.normal(0.0, self.read_noise_electrons, size=electrons.shape)
-        counts = np.clip(electrons * self.gain_counts_per_electron + self.offset_counts, 0.0, self.maximum_count())
-        if self.quantize:
-            counts = np.round(counts)
-        if self.bad_pixels:
-            value = self.bad_pixel_value_counts if self.bad_pixel_value_counts is not None else self.maximum_count()
-            value = min(max(value, 0.0), self.maximum_count())
-            if self.quantize:
-                value = round(value)
-            flat = counts.reshape(counts.shape[0], -1)
-            flat[:, list(self.bad_pixels)] = value
-        return counts
+            sens = np.asarray(self.pixel_sensitivity, dtype=np.float64)
+            if not np.all(np.isfinite(sens)) or np.any(sens < 0.0):
+                raise InvalidParameterError("pixel_sensitivity values must be finite and non-negative")
+            if sens.size != frame_len:
+                raise InvalidParameterError(f"pixel_sensitivity must contain {frame_len} values")
+        if len(set(self.bad_pixels)) != len(self.bad_pixels):
+            raise InvalidParameterError("bad_pixels must not repeat")
+        if any(int(p) < 0 or int(p) >= frame_len for p in self.bad_pixels):
+            raise InvalidParameterError(f"bad_pixels indices must be below the frame size {frame_len}")
+
+    def _descriptor(self, frame_len: int):
+        """C-ABI descriptor (fpm_camera_desc) and the arrays it points into."""
+        d = N.CameraDesc()
+        d.photons_per_pixel = float(self.photons_per_pixel)
+        d.gain_counts_per_electron = float(self.gain_counts_per_electron)
+        d.offset_counts = float(self.offset_counts)
+        d.read_noise_electrons = float(self.read_noise_electrons)
+        d.dark_current_electrons = float(self.dark_current_electrons)
+        d.shot_noise = int(bool(self.shot_noise))
+        d.quantize = int(bool(self.quantize))
+        d.maximum_count = float(self.maximum_count())
+        keep = []
+        if self.pixel_sensitivity is not None:
+            sens = np.ascontiguousarray(self.pixel_sensitivity, dtype=np.float64).ravel()
+            if sens.size != frame_len:
+                raise InvalidParameterError("pixel_sensitivity must have one value per detector pixel")
+            keep.append(sens)
+            d.pixel_sensitivity = N.ptr(sens, C.c_double)
+        bad = np.ascontiguousarray(list(self.bad_pixels), dtype=np.int64)
+        keep.append(bad)
+        d.bad_pixels = N.ptr(bad, C.c_int64) if bad.size else C.POINTER(C.c_int64)()
+        d.bad_pixel_count = int(bad.size)
+        d.bad_pixel_value = float("nan") if self.bad_pixel_value_counts is None else float(self.bad_pixel_value_counts)
+        return d, keep

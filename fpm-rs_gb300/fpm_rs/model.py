@@ -243,6 +243,7 @@ def compile_model(optics, illumination, image_shape, reconstruction_shape="smoot
 
 def compile_camera_model(model: ImagePlaneModel, camera) -> ImagePlaneModel:
     """CameraModel::compile_reconstruction_model (src/simulation/camera.rs:296-318)."""
+    camera.validate_for_frame(model.image_shape[0] * model.image_shape[1])
     scale = camera.photons_per_pixel * camera.gain_counts_per_electron
     gains = model._gains * scale if model._gains is not None else np.full(model.frame_count, scale)
     additive = camera.dark_current_electrons * camera.gain_counts_per_electron + camera.offset_counts

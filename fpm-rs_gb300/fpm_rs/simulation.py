@@ -109,8 +109,24 @@ def simulate(true_model: ImagePlaneModel, object, *, reconstruction_model=None, 
     if (recon.image_shape != true_model.image_shape or recon.reconstruction_shape != true_model.reconstruction_shape
             or recon.frame_count != true_model.frame_count):
         raise InvalidShapeError("true and reconstruction models must have matching image, object, and frame dimensions")
-    data = forward_intensities(true_model, field)
-    if camera is not None:
+    if camera is None:
+        data = forward_intensities(true_model, field)
+    else:
         recon = compile_camera_model(recon, camera)
-        data = camera.measure(data, np.random.default_rng(seed))
+        data = _simulate_counts(true_model, field, camera, seed)
     return SimulationResult(MeasurementStack(data), field.copy(), true_model, recon, camera is None, seed)
+
+
+def _simulate_counts(model: ImagePlaneModel, field: np.ndarray, camera: CameraModel, seed: int) -> np.ndarray:
+    """Forward stack and detector in one device call (fpm_simulate_stack)."""
+    if field.shape != model.reconstruction_shape:
+        raise InvalidShapeError(
+            f"object shape {field.shape} differs from reconstruction shape {model.reconstruction_shape}")
+    h, w = model.image_shape
+    desc, keep = model._descriptor()
+    cam, cam_keep = camera._descriptor(h * w)
+    out = np.empty((model.frame_count, h, w), np.float64)
+    ctx = N.context()
+    N.check(N.library().fpm_simulate_stack(ctx.handle, C.byref(desc), N.ptr(field, C.c_double), C.byref(cam),
+                                           C.c_uint64(int(seed) & (2**64 - 1)), N.ptr(out, C.c_double)), ctx.handle)
+    return out

@@ -14,6 +14,8 @@
  *   ImagePlaneModel::compile ..... src/model/image_plane_fpm.rs:196-253 -> fpm_compile_model
  *   ForwardModel::forward_intensity_stack_into
  *                                  src/model/forward.rs:300-372 -> fpm_forward_stack
+ *   Simulator::simulate + CameraModel::measure_frame
+ *                                  src/simulation/simulator.rs:107-206, camera.rs:249-290 -> fpm_simulate_stack
  *   ReconstructionProblem::new ... src/reconstruction/problem.rs:12-20 -> fpm_problem_create,
  *                                  fpm_problem_create_batch (many problems, one host scan)
  *   Runner::run / ReconstructionAlgorithm::run
@@ -185,6 +187,30 @@ int32_t fpm_fft2_noalloc(fpm_context *ctx, double *values, int32_t height, int32
  * (object FFT, crop, pupil, IFFT, |psi|^2 * gain + background). */
 int32_t fpm_forward_stack(fpm_context *ctx, const fpm_model_desc *model, const double *object,
                           double *intensities);
+
+/* Detector response of CameraModel (src/simulation/camera.rs:249-318). */
+typedef struct {
+    double photons_per_pixel;        /* expected electrons = max(I, 0) * sensitivity * photons + dark */
+    double gain_counts_per_electron;
+    double offset_counts;
+    double read_noise_electrons;     /* standard deviation of Gaussian read noise, 0 for none */
+    double dark_current_electrons;
+    int32_t shot_noise;              /* Poisson electrons */
+    int32_t quantize;                /* round counts (half away from zero) */
+    double maximum_count;            /* counts are clamped to [0, maximum_count]; INFINITY for none */
+    const double *pixel_sensitivity; /* h*w, or NULL */
+    const int64_t *bad_pixels;       /* pixel indices within a frame, or NULL */
+    int64_t bad_pixel_count;
+    double bad_pixel_value;          /* counts of a bad pixel; NAN for maximum_count */
+} fpm_camera_desc;
+
+/* Simulator::simulate's measurement stack (src/simulation/simulator.rs:
+ * 107-206) on the device: the forward intensity stack of `object`, then the
+ * detector, counts[sources*h*w]. Random draws come from a counter-based
+ * generator keyed by `seed` (reproducible for a given seed; equal to the
+ * reference's ChaCha12 draws only in distribution). */
+int32_t fpm_simulate_stack(fpm_context *ctx, const fpm_model_desc *model, const double *object,
+                           const fpm_camera_desc *camera, uint64_t seed, double *counts);
 
 /* Uploads a validated model + measurement pair; the problem keeps its
  * measurements resident on the device until fpm_problem_destroy. */
