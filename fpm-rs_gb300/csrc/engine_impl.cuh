@@ -379,6 +379,27 @@ FPM_DEVICE void gd_batch_apply(const TileDesc& T, float step, int c) {
     }
 }
 
+// Pupil update of gradient descent at a batch end
+// (src/algorithms/gradient_descent.rs:641-656, 688-690): this CTA's pupil
+// rows move by -(pupil_step / active) * gradient, the accumulator is
+// cleared, and the support is imposed. The caller's barriers order it.
+template <class K>
+FPM_DEVICE void gd_pupil_apply(const TileDesc& T, float2* __restrict__ pslab, const EngineParams& P, int c, float step) {
+    const int i_lo = K::C == 1 ? 0 : c * K::R;
+    __syncthreads();
+    bool bad = false;
+    for (int e = threadIdx.x; e < K::R * K::N; e += K::THREADS) {
+        const size_t g = (size_t)i_lo * K::N + e;
+        float2 p = cfma(-step, __ldcg(T.pupil_gradient + g), pslab[e]);
+        bad |= !isfinite(p.x) || !isfinite(p.y);
+        if (P.constrain_pupil && T.support[g] == 0) p = make_float2(0.f, 0.f);
+        pslab[e] = p;
+        __stcg(T.pupil_gradient + g, make_float2(0.f, 0.f));
+    }
+    if (bad) atomicOr(T.status, 64);
+    __syncthreads();
+}
+
 template <class K>
 FPM_DEVICE void load_pupil_slab(float2* __restrict__ pslab, const float2* __restrict__ pupil, int c) {
     for (int e = threadIdx.x; e < K::R * K::N; e += K::THREADS) {
@@ -415,11 +436,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     const int M = T.M;
     const long long ostride = M + (M & 1);
     const int i_lo = C == 1 ? 0 : c * R;
-    constexpr bool gradient = ALG == kAlgGradient || ALG == kAlgGradientTruncated;
+    constexpr bool gradient = ALG == kAlgGradient || ALG == kAlgGradientTruncated || ALG == kAlgGradientPupil;
     constexpr bool projection = !gradient;
+    // Families whose pupil evolves during the launch: per-frame maxima, all rows.
+    constexpr bool gd_pupil = ALG == kAlgGradientPupil;
     constexpr bool epry = ALG == kAlgEpry;
     // Rows of psi that can be non-zero (all rows when the pupil evolves).
-    const int row_lo = epry ? 0 : T.row_lo, row_hi = epry ? N - 1 : T.row_hi;
+    const int row_lo = epry || gd_pupil ? 0 : T.row_lo, row_hi = epry || gd_pupil ? N - 1 : T.row_hi;
 
     load_pupil_slab<K>(pslab, T.pupil, c);
     int counter = P.momentum ? *T.counter : 0;
@@ -428,6 +451,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     // moves once per batch of gd_batch consecutive frames of the order.
     const bool gd_batched = gradient && P.gd_batch > 1;
     int batch_active = 0;
+    int pupil_active = 0;  // positive-weight frames since the last pupil update
     // Poisson truncation (src/algorithms/gradient_descent.rs:701-792): each
     // batch is walked twice, first forward-only for the residual statistic,
     // then with the gate |y - p| <= scale * sqrt(p) on the gradient.
@@ -534,10 +558,16 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             if (tid == 0) s_frame = T.params[f];
             __syncthreads();
             const FrameParam& fp = s_frame;
-            const bool batch_end =
-                gd_batched && !stats && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
+            const bool batch_boundary = gradient && !stats && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
+            const bool batch_end = gd_batched && batch_boundary;
             if (fp.weight == 0.0f) {
                 __syncthreads();
+                if constexpr (gd_pupil) {
+                    if (batch_boundary) {
+                        if (pupil_active > 0) gd_pupil_apply<K>(T, pslab, P, c, P.pupil_step / (float)pupil_active);
+                        pupil_active = 0;
+                    }
+                }
                 if (batch_end) {
                     if (batch_active > 0) gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
                     batch_active = 0;
@@ -546,6 +576,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 continue;
             }
             if (gd_batched && !stats) ++batch_active;
+            if (gd_pupil && !stats) ++pupil_active;
 
             // S0
             stage_object<K>(osm, T.object, M, ostride, fp, i_lo, row_lo, row_hi);
@@ -554,8 +585,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P1, P2
             float max_obj = 0.f, max_pup = 0.f;
-            rows_inverse<K, epry>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj, max_pup);
-            if constexpr (epry) {
+            rows_inverse<K, epry || gd_pupil>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj, max_pup);
+            if constexpr (epry || gd_pupil) {
                 max_obj = warp_max(max_obj);
                 max_pup = warp_max(max_pup);
                 if (lane == 0) {
@@ -576,7 +607,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             cluster_barrier<K>();
 
             float frame_max_obj = 0.f, frame_max_pup = 0.f;
-            if constexpr (epry) {
+            if constexpr (epry || gd_pupil) {
                 if constexpr (C == 1) {
                     frame_max_obj = fred[2 * K::WARPS];
                     frame_max_pup = fred[2 * K::WARPS + 1];
@@ -755,7 +786,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             {
                 float2 ureg[K::T1][NA];
                 const float inv_n2 = 1.0f / (float)(N * N);
-                const float max_p2 = epry ? fmaxf(frame_max_pup, P.eps) : T.max_pupil_power;
+                const float max_p2 = epry || gd_pupil ? fmaxf(frame_max_pup, P.eps) : T.max_pupil_power;
+                // Pupil gradient weight w * (N^2 / valid) / (max |patch|^2 + eps).
+                const float pupil_grad_scale =
+                    gd_pupil ? fp.weight * fp.valid_scale / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
                 const float inv_global = 1.0f / (max_p2 + P.eps);
                 const float pupil_scale =
                     epry ? fp.weight * P.pupil_step / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
@@ -800,6 +834,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                             }
                         } else {
                             u = cscale(cmulc(psi, pv), inv_global);
+                            if constexpr (gd_pupil) {
+                                float2* g = T.pupil_gradient + (size_t)i * N + j;
+                                __stcg(g, cfma(pupil_grad_scale, cmulc(psi, pt), __ldcg(g)));
+                            }
                         }
                         ureg[t][ja] = u;
                     }
@@ -870,6 +908,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
             cluster_barrier<K>();
 
+            if constexpr (gd_pupil) {
+                if (batch_boundary) {
+                    gd_pupil_apply<K>(T, pslab, P, c, P.pupil_step / (float)pupil_active);
+                    pupil_active = 0;
+                }
+            }
             if (batch_end) {
                 gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
                 batch_active = 0;
@@ -943,7 +987,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         }
         __syncthreads();
     }
-    if constexpr (epry) {
+    if constexpr (epry || gd_pupil) {
         for (int e = tid; e < R * N; e += K::THREADS) {
             const int l = e / N, j = e % N;
             const int i = C == 1 ? l : c * R + l;
@@ -1168,7 +1212,8 @@ cudaError_t launch_engine_alg(const EngineParams& p, int tiles, cudaStream_t s) 
     SPEC template cudaError_t launch_engine_alg<N, kAlgGradient>(const EngineParams&, int, cudaStream_t); \
     SPEC template cudaError_t launch_engine_alg<N, kAlgGradientTruncated>(const EngineParams&, int,      \
                                                                           cudaStream_t);               \
-    SPEC template cudaError_t launch_engine_alg<N, kAlgLocalAdaptive>(const EngineParams&, int, cudaStream_t);
+    SPEC template cudaError_t launch_engine_alg<N, kAlgLocalAdaptive>(const EngineParams&, int, cudaStream_t); \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgGradientPupil>(const EngineParams&, int, cudaStream_t);
 
 template <int N_>
 struct EngineEntry {
@@ -1186,6 +1231,7 @@ struct EngineEntry {
             case kAlgGradient: return engine_alg<kAlgGradient>(p, tiles, s);
             case kAlgGradientTruncated: return engine_alg<kAlgGradientTruncated>(p, tiles, s);
             case kAlgLocalAdaptive: return engine_alg<kAlgLocalAdaptive>(p, tiles, s);
+            case kAlgGradientPupil: return engine_alg<kAlgGradientPupil>(p, tiles, s);
             default: return cudaErrorInvalidValue;
         }
     }

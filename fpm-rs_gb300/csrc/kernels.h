@@ -38,10 +38,11 @@ struct TileDesc {
     float2* velocity;          // mPIE, M*M
     float2* anchor;            // mPIE, M*M
     float2* gradient;          // mini-batch gradient descent: M*M accumulator, zero between batches
+    float2* pupil_gradient;    // gradient descent with pupil recovery: N*N accumulator, zero between batches
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event
     int* status;               // bits: 1 non-finite momentum, 4 no valid data, 8 gauge, 16 truncation statistic,
-                               // 32 adaptive pass objective
+                               // 32 adaptive pass objective, 64 non-finite recovered pupil
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
@@ -65,6 +66,7 @@ enum EngineAlg {
     kAlgGradient = 4,
     kAlgGradientTruncated = 5,  // gradient descent with the Poisson truncation gate
     kAlgLocalAdaptive = 6,      // AP with the adaptive step controller
+    kAlgGradientPupil = 7,      // gradient descent with pupil recovery
 };
 
 struct EngineParams {

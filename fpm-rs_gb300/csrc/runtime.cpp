@@ -216,7 +216,8 @@ struct fpm_problem {
     // resident device data
     DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
     // run state
-    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient;
+    DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
+        pupil_gradient;
 };
 
 namespace {
@@ -811,9 +812,12 @@ Status validate_params(const fpm_algorithm_params* a) {
             return Status::make(FPM_ERR_INVALID_PARAMETER, "minimum_object_step must not exceed initial_object_step");
     }
     if (a->algorithm == FPM_ALG_GD) {
-        if (a->recover_pupil)
+        if (a->recover_pupil && (!std::isfinite(a->pupil_step) || a->pupil_step <= 0.0))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_step must be finite and positive");
+        if (a->recover_pupil && a->poisson_truncation)
             return Status::make(FPM_ERR_UNSUPPORTED,
-                                "gradient-descent pupil recovery is not implemented on the GB300 device path");
+                                "gradient descent with both pupil recovery and Poisson truncation is not implemented "
+                                "on the GB300 device path");
         // GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331).
         if (a->poisson_truncation) {
             if (!std::isfinite(a->poisson_truncation_threshold) || a->poisson_truncation_threshold <= 0.0)
@@ -889,7 +893,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     const long long ms = M + (M & 1);
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     const bool epry = a->algorithm == FPM_ALG_EPRY;
-    const bool canonical = epry && a->recover_pupil;
+    const bool gd_pupil = a->algorithm == FPM_ALG_GD && a->recover_pupil;
+    // Pupil-recovering runs canonicalise the object/pupil gauge at the start
+    // and after every iteration (Runner::run, src/reconstruction/runner.rs:122,220).
+    const bool canonical = (epry && a->recover_pupil) || gd_pupil;
     const bool gd_batched = a->algorithm == FPM_ALG_GD && a->batch_size > 1;
     const int iters = a->iterations;
     const bool resumed = !b.resume.empty();
@@ -904,7 +911,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
         for (DeviceBuffer* buf : {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-                                  &p->velocity, &p->anchor, &p->order, &p->gradient})
+                                  &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient})
             buf->bind(ctx->pool, s);
         FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
         FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
@@ -915,6 +922,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         if (gd_batched) {
             FPM_TRY(p->gradient.ensure(sizeof(float2) * (size_t)M * ms));
             FPM_CUDA(cudaMemsetAsync(p->gradient.ptr, 0, sizeof(float2) * (size_t)M * ms, s));
+        }
+        if (gd_pupil) {
+            FPM_TRY(p->pupil_gradient.ensure(sizeof(float2) * n2));
+            FPM_CUDA(cudaMemsetAsync(p->pupil_gradient.ptr, 0, sizeof(float2) * n2, s));
         }
         if (mpie) {
             FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
@@ -983,6 +994,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.velocity = mpie ? p->velocity.as<float2>() : nullptr;
         T.anchor = mpie ? p->anchor.as<float2>() : nullptr;
         T.gradient = gd_batched ? p->gradient.as<float2>() : nullptr;
+        T.pupil_gradient = gd_pupil ? p->pupil_gradient.as<float2>() : nullptr;
         T.partials = p->partials.as<double>();
         T.counter = p->counter.as<int>();
         T.status = p->status.as<int>();
@@ -1083,7 +1095,11 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         case FPM_ALG_FPIE:
         case FPM_ALG_MPIE: ep.alg = fpm::kAlgRpie; break;
         case FPM_ALG_EPRY: ep.alg = canonical ? fpm::kAlgEpry : fpm::kAlgGlobal; break;
-        default: ep.alg = a->poisson_truncation ? fpm::kAlgGradientTruncated : fpm::kAlgGradient; break;
+        default:
+            ep.alg = a->recover_pupil       ? fpm::kAlgGradientPupil
+                     : a->poisson_truncation ? fpm::kAlgGradientTruncated
+                                             : fpm::kAlgGradient;
+            break;
     }
     ep.alpha = (float)a->stability;
     ep.eps = (float)a->epsilon;
@@ -1116,7 +1132,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         return Status::ok();
     };
     if (iters > it0) {
-        if (epry) {
+        if (epry || canonical) {
             for (int it = it0; it < iters; ++it) {
                 FPM_TRY(engine(it, it + 1));
                 if (canonical) {
@@ -1218,6 +1234,8 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 1) return Status::make(FPM_ERR_NUMERICAL, "mPIE momentum produced a non-finite object or velocity");
     if (status & 8) return Status::make(FPM_ERR_NUMERICAL, "object/pupil gauge normalization failed on a non-finite or empty state");
     if (status & 16) return Status::make(FPM_ERR_NUMERICAL, "Poisson truncation statistic is non-finite");
+    if (status & 32) return Status::make(FPM_ERR_NUMERICAL, "adaptive alternating projection produced an invalid pass objective");
+    if (status & 64) return Status::make(FPM_ERR_NUMERICAL, "pupil update produced a non-finite value");
     if (!r) return Status::ok();
     const int C = fpm::engine_ctas(p->n);
     if (r->objectives) fill_objectives(p, a, r->objectives);

@@ -307,6 +307,7 @@ class GradientDescent(_Algorithm):
         self.epsilon, self.loss_type = epsilon, loss_type
         self.poisson_truncation_threshold = poisson_truncation_threshold
         self.recover_illumination, self.recover_pupil = recover_illumination, recover_pupil
+        self.pupil_step, self.constrain_pupil_support = pupil_step, constrain_pupil_support
         self.object_tv, self.pupil_smoothing = object_tv, pupil_smoothing
         self.parallel_workers = parallel_workers
         if recover_illumination or object_tv or pupil_smoothing:
@@ -320,6 +321,8 @@ class GradientDescent(_Algorithm):
         if self.poisson_truncation_threshold is not None:
             p.poisson_truncation_threshold = float(self.poisson_truncation_threshold)
         p.recover_pupil = int(bool(self.recover_pupil))
+        p.pupil_step = float(self.pupil_step)
+        p.constrain_pupil_support = int(bool(self.constrain_pupil_support))
         return p
 
 

@@ -1053,8 +1053,20 @@ static int32_t truncation_scale(orc_state *s, const int *frames, int count, doub
     return ORC_OK;
 }
 
+/* Pupil recovery of GradientDescent::step (src/algorithms/gradient_descent.rs:
+ * 563-577, 624-640, 654-656): per frame the pupil gradient adds
+ * w * (N^2 / valid) * conj(patch) * spectrum / (max |patch|^2 + eps); at
+ * the batch end the pupil moves by pupil_step / active frames, then the
+ * support is imposed. */
+typedef struct {
+    int recover;
+    double step;
+    int constrain;
+} gd_pupil_config;
+
 static int32_t gradient_step(orc_state *s, const int *frames, int count, double object_step, double epsilon,
-                             int loss, double truncation_threshold, step_summary *summary) {
+                             int loss, double truncation_threshold, const gd_pupil_config *pupil_cfg,
+                             step_summary *summary) {
     const orc_problem *p = s->p;
     size_t n = s->n_low;
     double scale = 0.0;
@@ -1068,6 +1080,8 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
     max_pupil = fmax(max_pupil, epsilon);
     if (!s->gradient) s->gradient = (cplx *)malloc(sizeof(cplx) * s->n_high);
     memset(s->gradient, 0, sizeof(cplx) * s->n_high);
+    const int recover_pupil = pupil_cfg && pupil_cfg->recover;
+    if (recover_pupil) memset(s->pupil_gradient, 0, sizeof(cplx) * n);
     long active = 0;
     for (int b = 0; b < count; ++b) {
         int frame = frames[b];
@@ -1105,6 +1119,15 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
         for (size_t i = 0; i < n; ++i) s->field[i] = c_scale(s->field[i], 1.0 * s->projected[i].re);
         fft2_c(s->field, s->h, s->w, 0);
         fftshift_c(s->field, s->spectrum, s->h, s->w);
+        if (recover_pupil) {
+            double max_object = 0.0;
+            for (size_t i = 0; i < n; ++i) max_object = fmax(max_object, c_norm_sqr(s->patch[i]));
+            max_object = fmax(max_object, epsilon);
+            for (size_t i = 0; i < n; ++i)
+                s->pupil_gradient[i] = c_add(s->pupil_gradient[i],
+                                             c_scale(c_mul(c_conj(s->patch[i]), s->spectrum[i]),
+                                                     fw * valid_scale / (max_object + epsilon)));
+        }
         for (size_t i = 0; i < n; ++i)
             s->difference[i] = c_divr(c_mul(c_conj(s->pupil[i]), s->spectrum[i]), max_pupil + epsilon);
         st = insert_adjoint_c(s->gradient, s->mh, s->mw, (long)p->start_row[frame], (long)p->start_col[frame], s->h,
@@ -1114,6 +1137,19 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
     if (active > 0) {
         double step = object_step / (double)active;
         for (size_t i = 0; i < s->n_high; ++i) s->object[i] = c_sub(s->object[i], c_scale(s->gradient[i], step));
+        if (recover_pupil) {
+            double pstep = pupil_cfg->step / (double)active;
+            for (size_t i = 0; i < n; ++i) {
+                s->pupil[i] = c_sub(s->pupil[i], c_scale(s->pupil_gradient[i], pstep));
+                if (!isfinite(s->pupil[i].re) || !isfinite(s->pupil[i].im))
+                    return fail(ORC_NUMERICAL, "pupil update produced a non-finite value");
+            }
+        }
+    }
+    if (recover_pupil && pupil_cfg->constrain) {
+        const uint8_t *support = s->p->support;
+        for (size_t i = 0; i < n; ++i)
+            if (support[i] == 0) s->pupil[i] = cx(0.0, 0.0);
     }
     return ORC_OK;
 }
@@ -1331,8 +1367,8 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         return out->status = fail(ORC_INVALID_PARAMETER, "object_step must be finite and positive");
     if (!isfinite(prm->epsilon) || prm->epsilon <= 0.0)
         return out->status = fail(ORC_INVALID_PARAMETER, "epsilon must be finite and positive");
-    if (prm->algorithm == ORC_ALG_GD && prm->recover_pupil)
-        return out->status = fail(ORC_UNSUPPORTED, "gradient-descent pupil recovery is not restated");
+    if (prm->algorithm == ORC_ALG_GD && prm->recover_pupil && (!isfinite(prm->pupil_step) || prm->pupil_step <= 0.0))
+        return out->status = fail(ORC_INVALID_PARAMETER, "pupil_step must be finite and positive");
     /* AdaptiveAlternatingProjection::validate (src/algorithms/adaptive_alternating_projection.rs:350-403). */
     if (prm->algorithm == ORC_ALG_ADAPTIVE_AP) {
         if (prm->iterations == 0) return out->status = fail(ORC_INVALID_PARAMETER, "iterations must be greater than zero");
@@ -1400,6 +1436,7 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         canonical = prm->recover_pupil;
         break;
     case ORC_ALG_GD:
+        canonical = prm->recover_pupil;
         break;
     default:
         state_free(&s);
@@ -1434,8 +1471,11 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         for (int start = 0; start < p->frames && !st; start += prm->batch_size) {
             int count = p->frames - start < prm->batch_size ? p->frames - start : prm->batch_size;
             if (prm->algorithm == ORC_ALG_GD)
+            {
+                const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil};
                 st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type,
-                                   prm->poisson_truncation_threshold, &summary);
+                                   prm->poisson_truncation_threshold, &pc, &summary);
+            }
             else
                 st = projection_update(&s, order + start, count, &cfg, &summary);
         }

@@ -425,3 +425,18 @@ def test_adaptive_ap_validation(fpm):
         fpm.AdaptiveAlternatingProjection(iterations=2, reduction_factor=1.0).run(problem)
     with pytest.raises(fpm.InvalidParameterError):
         fpm.AdaptiveAlternatingProjection(iterations=2, minimum_object_step=2.0).run(problem)
+
+
+@pytest.mark.parametrize("n,side,batch", [(32, 5, 1), (64, 3, 4), (128, 3, 9)])
+def test_gradient_descent_pupil_recovery(fpm, n, side, batch):
+    """GD with recover_pupil (src/algorithms/gradient_descent.rs:563-656):
+    pupil gradient per frame, pupil step per batch, support projection, and
+    the object/pupil gauge after every iteration."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=71, photons=1e4, pupil_seed=5)
+    kw = dict(iterations=4, batch_size=batch, recover_pupil=True, pupil_step=0.05)
+    result, expected = _run_both(fpm, fpm.GradientDescent(**kw), "gd", kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "gd", iterations=4, batch_size=batch)
+    assert oracle.complex_nrmse(plain["pupil"], expected["pupil"]) > 2 * NRMSE  # the pupil did move

@@ -255,3 +255,22 @@ def test_adaptive_ap_step_controller():
     assert np.array_equal(ap2["object_spectrum"], two["object_spectrum"])  # no comparison before pass 3
     with pytest.raises(oracle.OracleError):
         oracle.run(oracle.Problem(m, data), "adaptive_ap", iterations=2, reduction_factor=1.0)
+
+
+def test_gd_pupil_recovery_moves_the_pupil_inside_its_support():
+    # GradientDescent pupil recovery (src/algorithms/gradient_descent.rs:563-656):
+    # the pupil changes, stays zero outside the support, and the gauge keeps
+    # the compiled pupil's supported energy (src/algorithms/gauge.rs:158-240).
+    m, data = _direct_problem(17)
+    m = dict(m)
+    support = np.ones((8, 8), np.uint8)
+    support[0, :] = 0
+    m["support"] = support
+    m["pupil"] = m["pupil"] * support
+    out = oracle.run(oracle.Problem(m, data * 1.2), "gd", iterations=3, batch_size=5, recover_pupil=True,
+                     pupil_step=0.05)
+    plain = oracle.run(oracle.Problem(m, data * 1.2), "gd", iterations=3, batch_size=5)
+    assert not np.array_equal(out["pupil"], plain["pupil"])
+    assert np.all(out["pupil"][support == 0] == 0)
+    energy = np.sum(np.abs(out["pupil"][support != 0]) ** 2)
+    assert abs(energy - np.sum(support)) <= 1e-9 * energy
