@@ -102,6 +102,53 @@ def test_algorithms_small(fpm, alg, kw, n, side):
         assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
 
 
+@pytest.mark.parametrize("alg,kw", [
+    ("ap", dict(iterations=3)),
+    ("fpie", dict(iterations=3)),
+    ("mpie", dict(iterations=3, momentum_interval=7)),
+    ("epry", dict(iterations=3)),
+])
+def test_algorithms_256(fpm, alg, kw):
+    """256-point tiles: 16-row CTAs in 16-CTA clusters."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 256, seed=8, photons=1e4)
+    cls = {"ap": fpm.AlternatingProjection, "fpie": fpm.Fpie, "mpie": fpm.Mpie, "epry": fpm.Epry}[alg]
+    result, expected = _run_both(fpm, cls(**kw), alg, kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    if alg == "epry":
+        assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
+
+
+def test_mpie_full_tile_bench_config(fpm):
+    """The bench's largest tile: 256 x 256 frames, 15x15 LEDs (M=729), mPIE
+    defaults (momentum every 30 frames), Poisson 1e4."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 15, 256, seed=9, photons=1e4)
+    assert model.reconstruction_shape == (729, 729)
+    result, expected = _run_both(fpm, fpm.Mpie(iterations=2), "mpie", dict(iterations=2), model, omodel, data,
+                                 gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
+def test_masks_background_256(fpm):
+    """Raw measurement form (background present) and amplitude form with
+    masks at 256 x 256."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 3, 256, seed=22, photons=3e3)
+    rng = np.random.default_rng(6)
+    masks = (rng.random(data.shape) > 0.15).astype(np.uint8)
+    weights = np.ones(data.shape[0])
+    weights[2] = 0.0
+    result, expected = _run_both(fpm, fpm.Mpie(iterations=2), "mpie", dict(iterations=2), model, omodel, data,
+                                 gains=gains, weights=weights, masks=masks)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    background = np.full(256 * 256, 2.0)
+    model_bg = model._replace(background=background)
+    result, expected = _run_both(fpm, fpm.AlternatingProjection(iterations=2), "ap", dict(iterations=2), model_bg,
+                                 omodel, data + 2.0, gains=gains, weights=weights, masks=masks, background=background)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
 def test_mpie_epry_pupil_config(fpm):
     """mPIE and EPRY, 13x13 LEDs, 128x128 frames (M=336), Zernike true pupil, Poisson 5e3."""
     model, omodel, data, truth, gains = helpers.simulated(fpm, 13, 128, seed=1, photons=5e3, pupil_seed=11)
