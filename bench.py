@@ -44,7 +44,7 @@ L2_BYTES = 129 * 1024 * 1024
 # iteration, by tile size: ncu dram__bytes_read.sum + dram__bytes_write.sum
 # of the four engine launches of a 64-tile run (profiles/engine_dram_traffic_64tiles.txt).
 # roofline.traffic scales them by this run's tile counts and iterations.
-DRAM_BYTES_PER_TILE_ITERATION = {256: 243.49e6, 128: 21.97e6, 64: 0.881e6, 32: 0.040e6}
+DRAM_BYTES_PER_TILE_ITERATION = {256: 244.23e6, 128: 23.32e6, 64: 0.827e6, 32: 0.040e6}
 
 
 def parse():
