@@ -429,6 +429,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     // Tile and frame descriptors live in shared memory, not registers.
     __shared__ TileDesc s_tile;
     __shared__ FrameParam s_frame;
+    __shared__ SpectralStep s_step;
     if (tid == 0) s_tile = P.tiles[tile];
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
     __syncthreads();
@@ -441,10 +442,15 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     // Families whose pupil evolves during the launch: per-frame maxima, all rows.
     constexpr bool gd_pupil = ALG == kAlgGradientPupil;
     constexpr bool epry = ALG == kAlgEpry;
-    // Rows of psi that can be non-zero (all rows when the pupil evolves).
-    const int row_lo = epry || gd_pupil ? 0 : T.row_lo, row_hi = epry || gd_pupil ? N - 1 : T.row_hi;
+    // Narrowband spectral AP: per-mode channel pupils and stored objects.
+    constexpr bool spectral = ALG == kAlgSpectral;
+    // Rows of psi that can be non-zero (all rows when the pupil evolves or
+    // changes with the channel).
+    const int row_lo = epry || gd_pupil || spectral ? 0 : T.row_lo;
+    const int row_hi = epry || gd_pupil || spectral ? N - 1 : T.row_hi;
 
     load_pupil_slab<K>(pslab, T.pupil, c);
+    int slab_channel = 0;  // spectral: channel whose pupil rows pslab holds
     int counter = P.momentum ? *T.counter : 0;
     double loss_acc = 0.0;
     // Mini-batch gradient descent: frames add into T.gradient and the object
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 ada_has_previous = true;
             }
         }
-        const int steps = truncating ? 2 * T.frame_count : T.frame_count;
+        const int steps = truncating ? 2 * T.frame_count : spectral ? T.step_count : T.frame_count;
         for (int step = 0; step < steps; ++step) {
             // Truncating: batch k covers steps [2kB, 2kB + 2b): b statistics
             // steps, then the b update steps of the same frames.
@@ -554,10 +560,28 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     cluster_barrier<K>();  // partials read before the next batch rewrites them
                 }
             }
-            const int f = T.order ? T.order[idx] : idx;
-            if (tid == 0) s_frame = T.params[f];
+            const int f = spectral ? T.steps[step].exposure : T.order ? T.order[idx] : idx;
+            if (tid == 0) {
+                if constexpr (spectral) {
+                    s_step = T.steps[step];
+                    s_frame = T.params[s_step.mode];
+                } else {
+                    s_frame = T.params[f];
+                }
+            }
             __syncthreads();
             const FrameParam& fp = s_frame;
+            // Spectral update steps start from the stored mode field: no
+            // staging and no inverse transform.
+            const bool spectral_update = spectral && s_step.update != 0;
+            float2* const obj = spectral ? T.object + (size_t)s_step.object * M * ostride : T.object;
+            if constexpr (spectral) {
+                if (s_step.channel != slab_channel) {
+                    // Previous readers of pslab finished behind the last step's barriers.
+                    load_pupil_slab<K>(pslab, T.pupil + (size_t)s_step.channel * N * N, c);
+                    slab_channel = s_step.channel;
+                }
+            }
             const bool batch_boundary = gradient && !stats && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
             const bool batch_end = gd_batched && batch_boundary;
             if (fp.weight == 0.0f) {
@@ -579,13 +603,15 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             if (gd_pupil && !stats) ++pupil_active;
 
             // S0
-            stage_object<K>(osm, T.object, M, ostride, fp, i_lo, row_lo, row_hi);
+            if (!spectral_update) stage_object<K>(osm, obj, M, ostride, fp, i_lo, row_lo, row_hi);
             __syncthreads();
             const float2* ostage = osm + (fp.lower_col & 1);
 
             // P1, P2
             float max_obj = 0.f, max_pup = 0.f;
-            rows_inverse<K, epry || gd_pupil>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj, max_pup);
+            if (!spectral_update)
+                rows_inverse<K, epry || gd_pupil>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj,
+                                                  max_pup);
             if constexpr (epry || gd_pupil) {
                 max_obj = warp_max(max_obj);
                 max_pup = warp_max(max_pup);
@@ -604,7 +630,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     fred[2 * K::WARPS + 1] = b;
                 }
             }
-            cluster_barrier<K>();
+            if (!spectral_update) cluster_barrier<K>();
 
             float frame_max_obj = 0.f, frame_max_pup = 0.f;
             if constexpr (epry || gd_pupil) {
@@ -623,7 +649,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
 
             // P3
-            if constexpr (C > 1) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
+            if constexpr (C > 1) {
+                if (!spectral_update) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
+            }
             // P4 ownership. R = 32: column position q4, half h4, slot k =
             // local spatial row h4 + 2k. R = 16: column position tid, slot k =
             // local row k. Local row m of CTA c is spatial row c + C * m, and
@@ -632,8 +660,60 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             const int mbase = (c * R + h4) * N + q4;
             constexpr int mstride = R == 32 ? 2 * N : N;
 
-            if constexpr (C > 1) cluster_barrier<K>();
+            if constexpr (C > 1) {
+                if (!spectral_update) cluster_barrier<K>();
+            }
 
+            if constexpr (spectral) {
+                // P4 of spectral AP (src/algorithms/spectral.rs:218-270). Each
+                // thread owns the same detector pixels in every step, so the
+                // mode fields and the prediction need no synchronisation.
+                float2 v[16];
+                float2* const slot = T.mode_fields + (size_t)s_step.slot * N * N + mbase;
+                float* const pred = T.prediction + mbase;
+                const int pq = phys<K>(q4);
+                if (!spectral_update) {
+                    // Evaluation: psi_k, and prediction += w_k |psi_k|^2.
+                    if constexpr (R == 32) column_inverse_split<K>(fld, pq, h4, tw, v);
+                    else column_inverse_local<K>(fld, pq, v);
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        __stcg(slot + (size_t)k * mstride, v[k]);
+                        float pk = s_step.mode_weight * cnorm2(v[k]);
+                        if (s_step.slot > 0) pk += __ldcg(pred + (size_t)k * mstride);
+                        __stcg(pred + (size_t)k * mstride, pk);
+                    }
+                    __syncthreads();
+                    continue;
+                }
+                // Update: psi' - psi with the exposure's shared amplitude
+                // ratio sqrt(target / prediction); masked pixels keep psi and
+                // dark pixels take sqrt(target / weight sum).
+                const size_t off = (size_t)f * N * N + mbase;
+                const float gain = s_step.gain, inv_gain = 1.0f / s_step.gain, bg = s_step.background;
+                const bool first = s_step.first_update != 0;
+                float frame_loss = 0.f;
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const float meas = __ldcs(T.meas + off + (size_t)k * mstride);
+                    const bool masked = T.masks && T.masks[off + (size_t)k * mstride] == 0;
+                    const float2 psi = __ldcg(slot + (size_t)k * mstride);
+                    const float pk = __ldcg(pred + (size_t)k * mstride);
+                    if (masked) {
+                        v[k] = make_float2(0.f, 0.f);
+                        continue;
+                    }
+                    if (first) frame_loss += point_loss<LOSS>(fmaf(gain, pk, bg), meas, P.loss);
+                    const float target = fmaxf((meas - bg) * inv_gain, 0.f);
+                    if (pk > P.eps)
+                        v[k] = cscale(psi, sqrtf(target / pk) - 1.f);
+                    else
+                        v[k] = make_float2(sqrtf(target * s_step.inv_weight_sum) - psi.x, -psi.y);
+                }
+                if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
+                else column_forward_local<K>(fld, pq, c, tw, v);
+                if (first) loss_acc += (double)frame_loss * s_step.loss_scale;
+            } else {
             // P4: column inverse FFT, projection, column forward FFT.
             {
                 const float* brow =
@@ -753,6 +833,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     loss_acc += (double)frame_loss * fp.loss_scale;
                 }
             }
+            }  // non-spectral P4
             if (stats) {
                 __syncthreads();
                 continue;
@@ -812,15 +893,16 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     for (int ja = 0; ja < NA; ++ja) {
                         const int j = (NB * ja + jb + N / 2) & (N - 1);
                         const float2 psi = cscale(v[ja], inv_n2);
-                        const float2 pt = patch_at(ostage, K::ORS, il, j, fp);
+                        // Spectral update steps transform psi' - psi, so psi is already the difference.
+                        const float2 pt = spectral ? make_float2(0.f, 0.f) : patch_at(ostage, K::ORS, il, j, fp);
                         float2* pp = pslab + il * N + j;
                         const float2 pv = *pp;
                         float2 u;
                         if constexpr (projection) {
-                            const float2 d = csub(psi, cmul(pt, pv));
+                            const float2 d = spectral ? psi : csub(psi, cmul(pt, pv));
                             const float pw = cnorm2(pv);
                             float inv_den;
-                            if constexpr (ALG == kAlgLocal || ALG == kAlgLocalAdaptive)
+                            if constexpr (ALG == kAlgLocal || ALG == kAlgLocalAdaptive || spectral)
                                 inv_den = 1.0f / (pw + P.eps);
                             else if constexpr (ALG == kAlgRpie)
                                 inv_den = 1.0f / ((1.f - P.alpha) * pw + P.alpha * max_p2 + P.eps);
@@ -867,10 +949,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // Projection: O += w * step * adj(U). Gradient descent: O -= step *
                 // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
                 // (N^2 / valid) * adj(U).
-                const float scale = projection   ? fp.weight * (adaptive ? (float)ada_step : P.object_step)
+                const float scale = spectral     ? s_step.update_scale * P.object_step
+                                    : projection ? fp.weight * (adaptive ? (float)ada_step : P.object_step)
                                     : gd_batched ? fp.weight * fp.valid_scale
                                                  : -P.object_step * fp.weight * fp.valid_scale;
-                float2* target = gd_batched ? T.gradient : T.object;
+                // Spectral updates read the current object: an earlier mode of the
+                // same exposure may have changed it after the evaluation staging.
+                float2* target = gd_batched ? T.gradient : obj;
                 const int rows8 = C == 1 ? N + fp.has_upper_row : R + (c == C - 1 ? fp.has_upper_row : 0);
                 const int cols8 = N + fp.has_upper_col;
                 constexpr int PER = (N + 1 + 31) / 32;
@@ -896,7 +981,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
                         acc = cfma(fp.w11, d1, acc);
-                        const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
+                        const float2 base = j < cols8 ? (gd_batched || spectral ? __ldcg(grow + j) : srow[j]) : z;
                         out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
 #pragma unroll
@@ -1204,8 +1289,13 @@ cudaError_t launch_cluster(Kern kernel, const Params& p, int clusters, cudaStrea
 // (engine_n*_gd.cu) so each size builds as two parallel halves.
 template <int N_, int ALG>
 cudaError_t launch_engine_alg(const EngineParams& p, int tiles, cudaStream_t s) {
-    if (p.loss == 0) return launch_cluster<N_>(engine_kernel<N_, ALG, 0>, p, tiles, s);
-    return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+    if constexpr (ALG == kAlgSpectral) {
+        // Spectral AP's loss is a diagnostic: one runtime-selected variant.
+        return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+    } else {
+        if (p.loss == 0) return launch_cluster<N_>(engine_kernel<N_, ALG, 0>, p, tiles, s);
+        return launch_cluster<N_>(engine_kernel<N_, ALG, -1>, p, tiles, s);
+    }
 }
 
 #define FPM_ENGINE_SECOND_HALF(N, SPEC)                                                                  \
@@ -1213,7 +1303,8 @@ cudaError_t launch_engine_alg(const EngineParams& p, int tiles, cudaStream_t s) 
     SPEC template cudaError_t launch_engine_alg<N, kAlgGradientTruncated>(const EngineParams&, int,      \
                                                                           cudaStream_t);               \
     SPEC template cudaError_t launch_engine_alg<N, kAlgLocalAdaptive>(const EngineParams&, int, cudaStream_t); \
-    SPEC template cudaError_t launch_engine_alg<N, kAlgGradientPupil>(const EngineParams&, int, cudaStream_t);
+    SPEC template cudaError_t launch_engine_alg<N, kAlgGradientPupil>(const EngineParams&, int, cudaStream_t); \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgSpectral>(const EngineParams&, int, cudaStream_t);
 
 template <int N_>
 struct EngineEntry {
@@ -1232,6 +1323,7 @@ struct EngineEntry {
             case kAlgGradientTruncated: return engine_alg<kAlgGradientTruncated>(p, tiles, s);
             case kAlgLocalAdaptive: return engine_alg<kAlgLocalAdaptive>(p, tiles, s);
             case kAlgGradientPupil: return engine_alg<kAlgGradientPupil>(p, tiles, s);
+            case kAlgSpectral: return engine_alg<kAlgSpectral>(p, tiles, s);
             default: return cudaErrorInvalidValue;
         }
     }

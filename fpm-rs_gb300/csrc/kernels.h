@@ -24,6 +24,27 @@ struct FrameParam {
     double loss_scale;         // weight / unmasked pixel count
 };
 
+// One virtual step of narrowband spectral AP (src/algorithms/spectral.rs:
+// 182-271). An exposure with K coherent modes takes K evaluation steps (the
+// detector field of mode k from the pre-exposure objects into scratch slot k,
+// its weighted intensity into the prediction) and then K update steps (the
+// shared amplitude ratio, forward transform and local-denominator correction
+// into the mode's stored object).
+struct SpectralStep {
+    int mode;             // FrameParam of the mode's crop and bilinear weights
+    int exposure;         // measurement frame
+    int object, channel;  // stored object and channel pupil
+    int update;           // 0: evaluate, 1: update
+    int slot;             // mode position within the exposure
+    float mode_weight;    // effective intensity weight of the mode
+    float update_scale;   // frame weight * mode weight / exposure weight sum
+    float gain;           // effective detector gain of the exposure, > 0
+    float background;     // scalar exposure background
+    float inv_weight_sum; // 1 / exposure weight sum (fill of dark pixels)
+    int first_update;     // 1 on the exposure's first update step, which adds its loss
+    double loss_scale;    // frame weight / unmasked pixels
+};
+
 // One reconstruction tile: device pointers into its resident buffers.
 struct TileDesc {
     float2* object;            // M*M centred spectrum (state)
@@ -52,6 +73,12 @@ struct TileDesc {
     // correction U there is zero, so the engine skips those rows (EPRY,
     // whose pupil evolves, uses the full range).
     int row_lo, row_hi;
+    // Spectral AP: objects are consecutive M x (M + M % 2) grids from
+    // `object`, channel pupils consecutive N x N grids from `pupil`.
+    const SpectralStep* steps;  // [step_count] per pass
+    int step_count;
+    float2* mode_fields;        // [modes per exposure][N*N] fields, engine layout
+    float* prediction;          // N*N weighted intensity sum, engine layout
 };
 
 // Frame-engine kernel families, fixed at compile time so each instantiation
@@ -67,6 +94,7 @@ enum EngineAlg {
     kAlgGradientTruncated = 5,  // gradient descent with the Poisson truncation gate
     kAlgLocalAdaptive = 6,      // AP with the adaptive step controller
     kAlgGradientPupil = 7,      // gradient descent with pupil recovery
+    kAlgSpectral = 8,           // narrowband spectral AP over multi-mode exposures
 };
 
 struct EngineParams {

@@ -576,6 +576,34 @@ Status check_scans(const fpm_measurement_desc* ms, const FrameScan* scans) {
     return Status::ok();
 }
 
+// Bilinear stencil of one source's crop (interpolation_axis,
+// src/model/crop.rs:266-313; extract_standard :79-102 for integer offsets),
+// FP64 on the host, weights rounded once.
+Status crop_frame_param(long long start_row, long long start_col, double off_row, double off_col, int N, int M,
+                        fpm::FrameParam& fp) {
+    Axis r{}, c{};
+    FPM_TRY(interpolation_axis(start_row, N, M, off_row, r));
+    FPM_TRY(interpolation_axis(start_col, N, M, off_col, c));
+    fp = fpm::FrameParam{};
+    if (std::fabs(off_row) <= 1e-12 && std::fabs(off_col) <= 1e-12) {
+        fp.lower_row = (int)start_row;
+        fp.lower_col = (int)start_col;
+        fp.has_upper_row = fp.has_upper_col = 0;
+        fp.w00 = 1.f;
+        fp.w01 = fp.w10 = fp.w11 = 0.f;
+    } else {
+        fp.lower_row = (int)r.lower_start;
+        fp.lower_col = (int)c.lower_start;
+        fp.has_upper_row = r.upper ? 1 : 0;
+        fp.has_upper_col = c.upper ? 1 : 0;
+        fp.w00 = (float)(r.lower_weight * c.lower_weight);
+        fp.w01 = (float)(r.lower_weight * c.upper_weight);
+        fp.w10 = (float)(r.upper_weight * c.lower_weight);
+        fp.w11 = (float)(r.upper_weight * c.upper_weight);
+    }
+    return Status::ok();
+}
+
 // Host part of a problem: copies of the model and the frame constants.
 Status prepare_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_measurement_desc* ms,
                        const FrameScan* scans, std::unique_ptr<fpm_problem>& out) {
@@ -614,30 +642,10 @@ Status prepare_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_mea
     p->data_snr.resize(F);
     for (int f = 0; f < F; ++f) p->data_snr[f] = scans[f].snr;
     for (int f = 0; f < F; ++f) {
-        Axis r{}, c{};
-        FPM_TRY(interpolation_axis(p->start_row[f], N, p->m, p->off_row[f], r));
-        FPM_TRY(interpolation_axis(p->start_col[f], N, p->m, p->off_col[f], c));
         if (std::fabs(p->off_row[f]) > 1e-12) p->row_exact = false;
         if (std::fabs(p->off_col[f]) > 1e-12) p->col_exact = false;
-        const bool zero = std::fabs(p->off_row[f]) <= 1e-12 && std::fabs(p->off_col[f]) <= 1e-12;
         fpm::FrameParam fp{};
-        if (zero) {
-            // extract_standard: integer crop at the stored origin.
-            fp.lower_row = (int)p->start_row[f];
-            fp.lower_col = (int)p->start_col[f];
-            fp.has_upper_row = fp.has_upper_col = 0;
-            fp.w00 = 1.f;
-            fp.w01 = fp.w10 = fp.w11 = 0.f;
-        } else {
-            fp.lower_row = (int)r.lower_start;
-            fp.lower_col = (int)c.lower_start;
-            fp.has_upper_row = r.upper ? 1 : 0;
-            fp.has_upper_col = c.upper ? 1 : 0;
-            fp.w00 = (float)(r.lower_weight * c.lower_weight);
-            fp.w01 = (float)(r.lower_weight * c.upper_weight);
-            fp.w10 = (float)(r.upper_weight * c.lower_weight);
-            fp.w11 = (float)(r.upper_weight * c.upper_weight);
-        }
+        FPM_TRY(crop_frame_param(p->start_row[f], p->start_col[f], p->off_row[f], p->off_col[f], N, p->m, fp));
         p->stencil_cells[f] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
         const long long valid = masks ? scans[f].valid : (long long)n2;
         fp.weight = (float)p->weights[f];
@@ -1478,6 +1486,427 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
     return Status::ok();
 }
 
+// ------------------------------------------------------------ spectral AP
+
+// SpectralImagePlaneModel::validate (src/model/spectral.rs:302-398),
+// SpectralReconstructionProblem::validate (src/reconstruction/spectral.rs:
+// 55-92) and SpectralAlternatingProjection::validate
+// (src/algorithms/spectral.rs:149-173), before any device work.
+Status validate_spectral(const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
+                         const fpm_spectral_params* a) {
+    if (!sm || !ms || !a) return Status::make(FPM_ERR_INVALID_PARAMETER, "spectral model, measurements and parameters are required");
+    if (!std::isfinite(a->object_step) || a->object_step <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "object_step must be finite and positive");
+    if (!std::isfinite(a->epsilon) || a->epsilon <= 0.0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "epsilon must be finite and positive");
+    if (a->iterations <= 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "iterations must be positive");
+    if (a->batch_size <= 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "batch_size must be positive");
+    if (a->loss_type < 0 || a->loss_type > 3) return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown loss type %d", a->loss_type);
+    if (sm->channels <= 0 || !sm->channel_models)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "at least one spectral channel is required");
+    if (sm->object_coupling != FPM_COUPLING_INDEPENDENT && sm->object_coupling != FPM_COUPLING_SHARED_COMPLEX)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown object coupling %d", sm->object_coupling);
+    const fpm_model_desc& c0 = sm->channel_models[0];
+    for (int c = 0; c < sm->channels; ++c) {
+        const fpm_model_desc& md = sm->channel_models[c];
+        FPM_TRY(validate_model(&md));
+        if (md.image_height != c0.image_height || md.image_width != c0.image_width ||
+            md.recon_height != c0.recon_height || md.recon_width != c0.recon_width)
+            return Status::make(FPM_ERR_INVALID_PARAMETER,
+                                "all channel kernels must share detector shape, reconstruction grid, and object-plane pixel pitch");
+        if (md.background)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "background belongs to physical detector rows, not channel kernels");
+    }
+    const int N = c0.image_height;
+    if (c0.image_width != N || !fpm::engine_supported(N) || c0.recon_width != c0.recon_height)
+        return Status::make(FPM_ERR_UNSUPPORTED,
+                            "the GB300 device path reconstructs square tiles of 32, 64, 128 or 256 pixels on a square grid");
+    const int E = sm->exposures;
+    if (E <= 0 || !sm->contribution_offsets || !sm->exposure_gain || !sm->exposure_background)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "at least one detector frame is required");
+    if (sm->contribution_offsets[0] != 0)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "contribution offsets must start at zero");
+    std::vector<std::vector<char>> covered(sm->channels), positive(sm->channels);
+    for (int c = 0; c < sm->channels; ++c) {
+        covered[c].assign(sm->channel_models[c].sources, 0);
+        positive[c].assign(sm->channel_models[c].sources, 0);
+    }
+    for (int e = 0; e < E; ++e) {
+        const int first = sm->contribution_offsets[e], last = sm->contribution_offsets[e + 1];
+        if (last <= first) return Status::make(FPM_ERR_INVALID_PARAMETER, "each detector frame must have a positive contribution");
+        if (!std::isfinite(sm->exposure_gain[e]) || sm->exposure_gain[e] <= 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "spectral frame gain must be finite and positive");
+        if (!std::isfinite(sm->exposure_background[e]) || sm->exposure_background[e] < 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "spectral frame background must be finite and non-negative");
+        double mode_weight_sum = 0.0;
+        for (int k = first; k < last; ++k) {
+            const int c = sm->contribution_channel[k], l = sm->contribution_local_frame[k];
+            if (c < 0 || c >= sm->channels || l < 0 || l >= sm->channel_models[c].sources)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "channel/local_frame reference is out of range");
+            for (int j = first; j < k; ++j)
+                if (sm->contribution_channel[j] == c && sm->contribution_local_frame[j] == l)
+                    return Status::make(FPM_ERR_INVALID_PARAMETER, "duplicate (channel, local_frame) contribution in frame %d", e);
+            const double w = sm->contribution_weight[k];
+            if (!std::isfinite(w) || w <= 0.0)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "spectral weights must be finite and positive");
+            covered[c][l] = 1;
+            const double fg = sm->channel_models[c].frame_gains ? sm->channel_models[c].frame_gains[l] : 1.0;
+            mode_weight_sum += w * fg;
+        }
+        if (!std::isfinite(mode_weight_sum) || mode_weight_sum <= 0.0 ||
+            !std::isfinite(sm->exposure_gain[e] * mode_weight_sum) || sm->exposure_gain[e] * mode_weight_sum <= 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "effective source-mode weight sum must be finite and positive");
+    }
+    for (auto& v : covered)
+        for (char x : v)
+            if (!x) return Status::make(FPM_ERR_INVALID_PARAMETER, "every channel and local frame must participate in the detector plan");
+    if (ms->frames != E || !ms->measurements)
+        return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "spectral detector frame count and shape must match the compiled model");
+    const size_t n2 = (size_t)N * N;
+    for (size_t i = 0; i < n2 * E; ++i)
+        if (!std::isfinite(ms->measurements[i]))
+            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "measurements contain non-finite values");
+    for (int e = 0; e < E; ++e) {
+        const double w = ms->frame_weights ? ms->frame_weights[e] : 1.0;
+        if (!std::isfinite(w) || w < 0.0)
+            return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "frame weights must be finite and non-negative");
+        if (w == 0.0) continue;
+        if (ms->masks) {
+            bool any = false;
+            for (size_t i = 0; i < n2 && !any; ++i) any = ms->masks[(size_t)e * n2 + i] != 0;
+            if (!any) return Status::make(FPM_ERR_INVALID_MEASUREMENTS, "positive-weight frame %d has no unmasked pixels", e);
+        }
+        for (int k = sm->contribution_offsets[e]; k < sm->contribution_offsets[e + 1]; ++k)
+            positive[sm->contribution_channel[k]][sm->contribution_local_frame[k]] = 1;
+    }
+    for (auto& v : positive)
+        for (char x : v)
+            if (!x)
+                return Status::make(FPM_ERR_INVALID_MEASUREMENTS,
+                                    "every spectral channel and local frame must participate in a positive-weight detector frame");
+    return Status::ok();
+}
+
+double spectral_frame_gain(const fpm_spectral_model_desc* sm, int c, int l) {
+    return sm->channel_models[c].frame_gains ? sm->channel_models[c].frame_gains[l] : 1.0;
+}
+
+// SpectralReconstructionState::initialize (src/reconstruction/spectral.rs:
+// 123-199) on the host in FP64: per stored object, the weighted mask-aware
+// mean of sqrt(max((I - background) / gain, 0)) over the exposures that use
+// it, nearest-upsampled to the common grid (natural order, complex128).
+Status spectral_initial_objects(const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms, int objects,
+                                std::vector<double>& out) {
+    const fpm_model_desc& c0 = sm->channel_models[0];
+    const int h = c0.image_height, w = c0.image_width, mh = c0.recon_height, mw = c0.recon_width;
+    const size_t n = (size_t)h * w, nm = (size_t)mh * mw;
+    out.assign(2 * nm * objects, 0.0);
+    std::vector<double> amplitude(n), weights(n);
+    for (int o = 0; o < objects; ++o) {
+        std::fill(amplitude.begin(), amplitude.end(), 0.0);
+        std::fill(weights.begin(), weights.end(), 0.0);
+        double total_amplitude = 0.0, total_weight = 0.0;
+        for (int e = 0; e < sm->exposures; ++e) {
+            const int first = sm->contribution_offsets[e], last = sm->contribution_offsets[e + 1];
+            bool uses = false;
+            for (int k = first; k < last; ++k)
+                uses |= (sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : sm->contribution_channel[k]) == o;
+            if (!uses) continue;
+            const double fw = ms->frame_weights ? ms->frame_weights[e] : 1.0;
+            if (fw == 0.0) continue;
+            double gain = 0.0;
+            for (int k = first; k < last; ++k)
+                gain += sm->contribution_weight[k] *
+                        spectral_frame_gain(sm, sm->contribution_channel[k], sm->contribution_local_frame[k]);
+            gain *= sm->exposure_gain[e];
+            if (!std::isfinite(gain) || gain <= 0.0)
+                return Status::make(FPM_ERR_NUMERICAL, "spectral initialization gain must be finite and positive");
+            const double* m = ms->measurements + (size_t)e * n;
+            const uint8_t* mk = ms->masks ? ms->masks + (size_t)e * n : nullptr;
+            const double bg = sm->exposure_background[e];
+            for (size_t i = 0; i < n; ++i) {
+                if (mk && mk[i] == 0) continue;
+                const double value = std::sqrt(std::max((m[i] - bg) / gain, 0.0));
+                amplitude[i] += fw * value;
+                weights[i] += fw;
+                total_amplitude += fw * value;
+                total_weight += fw;
+            }
+        }
+        const double fallback = total_amplitude / total_weight;
+        for (size_t i = 0; i < n; ++i) amplitude[i] = weights[i] > 0.0 ? amplitude[i] / weights[i] : fallback;
+        double* obj = out.data() + 2 * nm * o;
+        for (long long r = 0; r < mh; ++r)
+            for (long long c = 0; c < mw; ++c) obj[2 * (r * mw + c)] = amplitude[(r * h / mh) * w + c * w / mw];
+    }
+    return Status::ok();
+}
+
+// SpectralRunner::run with SpectralAlternatingProjection
+// (src/reconstruction/spectral.rs:494-642, src/algorithms/spectral.rs:
+// 182-271): one frame-engine launch over the pass range, each exposure as
+// its modes' evaluation steps followed by their update steps.
+Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
+                    const fpm_spectral_params* a, const int32_t* order, const double* initial_objects,
+                    const double* resume_spectra, int completed, double* objects_out, double* spectra_out,
+                    double* objectives_out) {
+    FPM_TRY(validate_spectral(sm, ms, a));
+    if (completed < 0 || completed > a->iterations)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "total target cannot precede checkpoint iterations");
+    if (initial_objects && resume_spectra)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "cannot combine initial objects with a checkpoint");
+    if (completed > 0 && !resume_spectra)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "completed iterations need the checkpoint's spectra");
+    const fpm_model_desc& c0 = sm->channel_models[0];
+    const int N = c0.image_height, M = c0.recon_height, E = sm->exposures, CH = sm->channels;
+    const int C = fpm::engine_ctas(N);
+    const int objects = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 1 : CH;
+    const long long ostride = M + (M & 1);
+    const size_t n2 = (size_t)N * N, nm = (size_t)M * M;
+    std::vector<int> schedule(E);
+    for (int e = 0; e < E; ++e) schedule[e] = e;
+    if (order) {
+        std::vector<char> seen(E, 0);
+        for (int e = 0; e < E; ++e) {
+            if (order[e] < 0 || order[e] >= E || seen[order[e]])
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "explicit order must be a permutation of all detector frames");
+            seen[order[e]] = 1;
+            schedule[e] = order[e];
+        }
+    }
+    for (const double* arr : {initial_objects, resume_spectra})
+        if (arr)
+            for (size_t i = 0; i < 2 * nm * objects; ++i)
+                if (!std::isfinite(arr[i])) return Status::make(FPM_ERR_INVALID_PARAMETER, "complex values must be finite");
+
+    // Crops of every channel source; FrameParam k = source_offset[c] + l.
+    std::vector<int> source_offset(CH + 1, 0);
+    for (int c = 0; c < CH; ++c) source_offset[c + 1] = source_offset[c] + sm->channel_models[c].sources;
+    std::vector<fpm::FrameParam> params(source_offset[CH]);
+    std::vector<double> stencil(source_offset[CH]);
+    for (int c = 0; c < CH; ++c) {
+        const fpm_model_desc& md = sm->channel_models[c];
+        for (int l = 0; l < md.sources; ++l) {
+            fpm::FrameParam& fp = params[source_offset[c] + l];
+            FPM_TRY(crop_frame_param(md.crop_start_row[l], md.crop_start_col[l], md.offset_row ? md.offset_row[l] : 0.0,
+                                     md.offset_col ? md.offset_col[l] : 0.0, N, M, fp));
+            fp.weight = 1.f;
+            fp.gain = 1.f;
+            stencil[source_offset[c] + l] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
+        }
+    }
+    // Virtual steps of one pass, in schedule order.
+    std::vector<fpm::SpectralStep> steps;
+    double weight_total = 0.0, bytes_per_pass = 0.0;
+    int max_modes = 1;
+    for (int idx = 0; idx < E; ++idx) {
+        const int e = schedule[idx];
+        const double fw = ms->frame_weights ? ms->frame_weights[e] : 1.0;
+        if (fw == 0.0) continue;
+        const int first = sm->contribution_offsets[e], count = sm->contribution_offsets[e + 1] - first;
+        max_modes = std::max(max_modes, count);
+        const bool separate = count == 1;
+        double gain = sm->exposure_gain[e];
+        if (separate)
+            gain *= sm->contribution_weight[first] *
+                    spectral_frame_gain(sm, sm->contribution_channel[first], sm->contribution_local_frame[first]);
+        std::vector<double> wk(count);
+        double wsum = 0.0;
+        for (int k = 0; k < count; ++k) {
+            const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
+            wk[k] = separate ? 1.0 : sm->contribution_weight[first + k] * spectral_frame_gain(sm, c, l);
+            wsum += wk[k];
+        }
+        long long valid = (long long)n2;
+        if (ms->masks) {
+            valid = 0;
+            for (size_t i = 0; i < n2; ++i) valid += ms->masks[(size_t)e * n2 + i] != 0;
+        }
+        weight_total += fw;
+        for (int phase = 0; phase < 2; ++phase)
+            for (int k = 0; k < count; ++k) {
+                const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
+                fpm::SpectralStep st{};
+                st.mode = source_offset[c] + l;
+                st.exposure = e;
+                st.object = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : c;
+                st.channel = c;
+                st.update = phase;
+                st.slot = k;
+                st.mode_weight = (float)wk[k];
+                st.update_scale = (float)(fw * (wk[k] / wsum));
+                st.gain = (float)gain;
+                st.background = (float)sm->exposure_background[e];
+                st.inv_weight_sum = (float)(1.0 / wsum);
+                st.first_update = phase == 1 && k == 0 ? 1 : 0;
+                st.loss_scale = fw / (double)valid;
+                steps.push_back(st);
+                // Algorithmic HBM bytes: stencil read (evaluation), object
+                // read-modify-write (update), measurement (+ mask) once.
+                bytes_per_pass += phase == 0 ? 8.0 * stencil[st.mode] : 16.0 * stencil[st.mode];
+            }
+        bytes_per_pass += 4.0 * (double)n2 + (ms->masks ? (double)n2 : 0.0);
+    }
+    if (!(weight_total > 0.0)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration has no positive frame weight");
+
+    std::vector<double> natural;
+    if (!resume_spectra && !initial_objects) FPM_TRY(spectral_initial_objects(sm, ms, objects, natural));
+    const double* start_objects = initial_objects ? initial_objects : natural.data();
+    std::vector<float2> pupils(n2 * CH);
+    for (int c = 0; c < CH; ++c)
+        for (size_t i = 0; i < n2; ++i)
+            pupils[c * n2 + i] = make_float2((float)sm->channel_models[c].pupil[2 * i],
+                                             (float)sm->channel_models[c].pupil[2 * i + 1]);
+
+    FPM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->streams[0];
+    // The context's staging buffers may still feed an earlier upload.
+    FPM_CUDA(cudaStreamSynchronize(ctx->upload));
+    FPM_CUDA(cudaStreamSynchronize(s));
+    DeviceBuffer meas, masks, d_pupils, d_params, d_steps, object, wide, fields, prediction, partials, status, tiles,
+        object_ptrs, wide_ptrs;
+    for (DeviceBuffer* b : {&meas, &masks, &d_pupils, &d_params, &d_steps, &object, &wide, &fields, &prediction,
+                            &partials, &status, &tiles, &object_ptrs, &wide_ptrs})
+        b->bind(ctx->pool, s);
+    cudaEvent_t ev[4] = {};
+    for (auto& e : ev) FPM_CUDA(cudaEventCreate(&e));
+    struct EventGuard {
+        cudaEvent_t* e;
+        ~EventGuard() {
+            for (int i = 0; i < 4; ++i)
+                if (e[i]) cudaEventDestroy(e[i]);
+        }
+    } guard{ev};
+    int launches = 0;
+    FPM_CUDA(cudaEventRecord(ev[0], s));
+    // Measurements in the engine's FP32 layout (raw form: per-exposure gain and background).
+    const size_t total = n2 * E;
+    FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
+    FPM_TRY(meas.ensure(total * sizeof(float)));
+    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), meas.as<float>(), E, s));
+    ++launches;
+    if (ms->masks) {
+        FPM_TRY(masks.ensure(total));
+        FPM_TRY(ctx->scratch_a.ensure(total));
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), masks.as<uint8_t>(), E, s));
+        ++launches;
+    }
+    FPM_TRY(upload_array(d_pupils, pupils, s));
+    FPM_TRY(upload_array(d_params, params, s));
+    FPM_TRY(upload_array(d_steps, steps, s));
+    FPM_TRY(object.ensure(sizeof(float2) * (size_t)M * ostride * objects));
+    FPM_TRY(wide.ensure(sizeof(double2) * nm * objects));
+    FPM_TRY(fields.ensure(sizeof(float2) * n2 * max_modes));
+    FPM_TRY(prediction.ensure(sizeof(float) * n2));
+    FPM_TRY(partials.ensure(sizeof(double) * (size_t)a->iterations * C));
+    FPM_TRY(status.ensure(sizeof(int)));
+    FPM_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(int), s));
+    FPM_CUDA(cudaMemsetAsync(partials.ptr, 0, sizeof(double) * (size_t)a->iterations * C, s));
+    std::vector<float2*> optr(objects);
+    std::vector<double2*> wptr(objects);
+    for (int o = 0; o < objects; ++o) {
+        optr[o] = object.as<float2>() + (size_t)o * M * ostride;
+        wptr[o] = wide.as<double2>() + (size_t)o * nm;
+    }
+    FPM_TRY(upload_array(object_ptrs, optr, s));
+    FPM_TRY(upload_array(wide_ptrs, wptr, s));
+    if (resume_spectra) {
+        // Checkpoint spectra are the widened complex64 state: narrowing restores it exactly.
+        FPM_CUDA(cudaMemcpyAsync(wide.ptr, resume_spectra, sizeof(double2) * nm * objects, cudaMemcpyHostToDevice, s));
+        for (int o = 0; o < objects; ++o) FPM_CUDA(fpm::launch_narrow(wptr[o], M, M, optr[o], ostride, s));
+        launches += objects;
+    } else {
+        // Forward FFT (FP64) and fftshift of the natural-order objects.
+        FPM_CUDA(cudaMemcpyAsync(wide.ptr, start_objects, sizeof(double2) * nm * objects, cudaMemcpyHostToDevice, s));
+        FPM_TRY(fft2_device(ctx, wide_ptrs.as<double2*>(), objects, M, M, false, s));
+        FPM_CUDA(fpm::launch_shift_to_state(wide_ptrs.as<double2*>(), object_ptrs.as<float2*>(), nullptr, nullptr,
+                                            objects, M, s));
+        launches += 3;
+    }
+    fpm::TileDesc T{};
+    T.object = object.as<float2>();
+    T.pupil = d_pupils.as<float2>();
+    T.support = nullptr;
+    T.meas = meas.as<float>();
+    T.masks = ms->masks ? masks.as<uint8_t>() : nullptr;
+    T.params = d_params.as<fpm::FrameParam>();
+    T.partials = partials.as<double>();
+    T.status = status.as<int>();
+    T.M = M;
+    T.frame_count = E;
+    T.max_pupil_power = 1.f;
+    T.amplitude = 0;
+    T.weight_sum = weight_total;
+    T.row_lo = 0;
+    T.row_hi = N - 1;
+    T.steps = d_steps.as<fpm::SpectralStep>();
+    T.step_count = (int)steps.size();
+    T.mode_fields = fields.as<float2>();
+    T.prediction = prediction.as<float>();
+    const std::vector<fpm::TileDesc> tile_list{T};
+    FPM_TRY(upload_array(tiles, tile_list, s));
+    fpm::EngineParams ep{};
+    ep.tiles = tiles.as<fpm::TileDesc>();
+    ep.alg = fpm::kAlgSpectral;
+    ep.eps = (float)a->epsilon;
+    ep.object_step = (float)a->object_step;
+    ep.loss = a->loss_type;
+    ep.gd_batch = 1;
+    ep.it_begin = completed;
+    ep.it_end = a->iterations;
+    FPM_CUDA(cudaEventRecord(ev[1], s));
+    if (a->iterations > completed) {
+        FPM_CUDA(fpm::launch_engine(N, ep, 1, s));
+        ++launches;
+    }
+    FPM_CUDA(cudaEventRecord(ev[2], s));
+    // Final objects: ifftshift and inverse FFT (FP64).
+    FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(object_ptrs.ptr),
+                                          wide_ptrs.as<double2*>(), objects, M, s));
+    FPM_TRY(fft2_device(ctx, wide_ptrs.as<double2*>(), objects, M, M, true, s));
+    launches += 3;
+    FPM_CUDA(cudaEventRecord(ev[3], s));
+    if (objects_out)
+        FPM_CUDA(cudaMemcpyAsync(objects_out, wide.ptr, sizeof(double2) * nm * objects, cudaMemcpyDeviceToHost, s));
+    if (spectra_out) {
+        FPM_CUDA(cudaStreamSynchronize(s));
+        for (int o = 0; o < objects; ++o) FPM_CUDA(fpm::launch_widen(optr[o], ostride, M, M, wptr[o], s));
+        launches += objects;
+        FPM_CUDA(cudaMemcpyAsync(spectra_out, wide.ptr, sizeof(double2) * nm * objects, cudaMemcpyDeviceToHost, s));
+    }
+    std::vector<double> host_partials((size_t)a->iterations * C);
+    int host_status = 0;
+    FPM_CUDA(cudaMemcpyAsync(host_partials.data(), partials.ptr, sizeof(double) * host_partials.size(),
+                             cudaMemcpyDeviceToHost, s));
+    FPM_CUDA(cudaMemcpyAsync(&host_status, status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FPM_CUDA(cudaStreamSynchronize(s));
+    FPM_CUDA(cudaGetLastError());
+    for (int it = completed; it < a->iterations; ++it) {
+        double sum = 0.0;
+        for (int r = 0; r < C; ++r) sum += host_partials[(size_t)it * C + r];
+        const double objective = sum / weight_total;
+        if (!std::isfinite(objective)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration objective is non-finite");
+        if (objectives_out) objectives_out[it - completed] = objective;
+    }
+    fpm_run_stats st = {};
+    float run_ms = 0.f, engine_ms = 0.f;
+    FPM_CUDA(cudaEventElapsedTime(&run_ms, ev[0], ev[3]));
+    FPM_CUDA(cudaEventElapsedTime(&engine_ms, ev[1], ev[2]));
+    st.kernel_launches = launches;
+    st.engine_launches = a->iterations > completed ? 1 : 0;
+    st.run_ms = run_ms;
+    st.engine_ms_sum = st.engine_span_ms = engine_ms;
+    st.engine_bytes = bytes_per_pass * (a->iterations - completed);
+    st.buckets = 1;
+    st.bucket_size[0] = N;
+    st.bucket_tiles[0] = 1;
+    st.bucket_end_ms[0] = run_ms;
+    ctx->stats = st;
+    return Status::ok();
+}
+
 }  // namespace
 
 namespace fpm {
@@ -1499,8 +1928,10 @@ void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream) 
 namespace {
 
 // Forward intensity stack into the device buffer `out` (float, F*N*N).
+// `object` is the natural-order object, or with `centred` its centred
+// spectrum (the state of a reconstruction).
 Status forward_stack_device(fpm_context* ctx, const fpm_model_desc* md, const double* object, DeviceBuffer& out,
-                            cudaStream_t s) {
+                            cudaStream_t s, bool centred = false) {
         FPM_TRY(validate_model(md));
         if (!object) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
         const int N = md->image_height, M = md->recon_height, F = md->sources;
@@ -1545,9 +1976,13 @@ Status forward_stack_device(fpm_context* ctx, const fpm_model_desc* md, const do
         std::vector<float2*> pst = {d_state.as<float2>()};
         FPM_TRY(upload_array(d_ptrs, p64, s));
         FPM_TRY(upload_array(d_ptrs2, pst, s));
-        // object_spectrum (src/simulation/simulator.rs:209-226): forward FFT, fftshift.
-        FPM_TRY(fft2_device(ctx, d_ptrs.as<double2*>(), 1, M, M, false, s));
-        FPM_CUDA(fpm::launch_shift_to_state(d_ptrs.as<double2*>(), d_ptrs2.as<float2*>(), nullptr, nullptr, 1, M, s));
+        if (centred) {
+            FPM_CUDA(fpm::launch_narrow(d_obj64.as<double2>(), M, M, d_state.as<float2>(), ms, s));
+        } else {
+            // object_spectrum (src/simulation/simulator.rs:209-226): forward FFT, fftshift.
+            FPM_TRY(fft2_device(ctx, d_ptrs.as<double2*>(), 1, M, M, false, s));
+            FPM_CUDA(fpm::launch_shift_to_state(d_ptrs.as<double2*>(), d_ptrs2.as<float2*>(), nullptr, nullptr, 1, M, s));
+        }
         fpm::ForwardParams fwd{};
         fwd.object = d_state.as<float2>();
         fwd.pupil = d_pupil.as<float2>();
@@ -1956,6 +2391,67 @@ int32_t fpm_run_batch_host(fpm_context* ctx, int32_t count, const fpm_model_desc
     }
     for (int i = 0; i < count; ++i) problems[i] = made[i].release();
     return finish(ctx, s);
+}
+
+int32_t fpm_spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* model,
+                         const fpm_measurement_desc* measurements, const fpm_spectral_params* params,
+                         const int32_t* order, const double* initial_objects, const double* resume_spectra,
+                         int32_t completed_iterations, double* objects, double* object_spectra, double* objectives) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return finish(ctx, spectral_run(ctx, model, measurements, params, order, initial_objects, resume_spectra,
+                                    completed_iterations, objects, object_spectra, objectives));
+}
+
+int32_t fpm_spectral_forward(fpm_context* ctx, const fpm_spectral_model_desc* model, const double* spectra,
+                             double* intensities) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        if (!model || !spectra || !intensities) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        fpm_measurement_desc none{};
+        if (model->channels <= 0 || !model->channel_models)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "at least one spectral channel is required");
+        const fpm_model_desc& c0 = model->channel_models[0];
+        const size_t n2 = (size_t)c0.image_height * c0.image_width, nm = (size_t)c0.recon_height * c0.recon_width;
+        // Model checks only: a stand-in measurement header of the right frame count.
+        std::vector<double> zeros;
+        none.frames = model->exposures;
+        zeros.assign(n2 * (size_t)std::max(model->exposures, 0), 1.0);
+        none.measurements = zeros.data();
+        fpm_spectral_params prm{1, 1, 0, 1.0, 1e-10};
+        FPM_TRY(validate_spectral(model, &none, &prm));
+        const size_t objects = model->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 1 : (size_t)model->channels;
+        for (size_t i = 0; i < 2 * nm * objects; ++i)
+            if (!std::isfinite(spectra[i])) return Status::make(FPM_ERR_INVALID_PARAMETER, "complex values must be finite");
+        cudaStream_t s = ctx->streams[0];
+        std::vector<double> out(n2 * model->exposures, 0.0);
+        std::vector<float> local;
+        for (int c = 0; c < model->channels; ++c) {
+            const fpm_model_desc& md = model->channel_models[c];
+            const size_t o = model->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : (size_t)c;
+            DeviceBuffer d_out;
+            FPM_TRY(forward_stack_device(ctx, &md, spectra + 2 * nm * o, d_out, s, true));
+            local.resize(n2 * md.sources);
+            FPM_CUDA(cudaMemcpyAsync(local.data(), d_out.ptr, sizeof(float) * local.size(), cudaMemcpyDeviceToHost, s));
+            FPM_CUDA(cudaStreamSynchronize(s));
+            // gain[f] * sum_k w_k * local_k + background[f]
+            // (SpectralImagePlaneModel::forward_intensity, src/model/spectral.rs:400-446).
+            for (int e = 0; e < model->exposures; ++e)
+                for (int k = model->contribution_offsets[e]; k < model->contribution_offsets[e + 1]; ++k) {
+                    if (model->contribution_channel[k] != c) continue;
+                    const double w = model->contribution_weight[k];
+                    const float* src = local.data() + n2 * model->contribution_local_frame[k];
+                    double* dst = out.data() + n2 * e;
+                    for (size_t i = 0; i < n2; ++i) dst[i] += w * (double)src[i];
+                }
+        }
+        for (int e = 0; e < model->exposures; ++e)
+            for (size_t i = 0; i < n2; ++i)
+                intensities[n2 * e + i] = model->exposure_gain[e] * out[n2 * e + i] + model->exposure_background[e];
+        return Status::ok();
+    };
+    return finish(ctx, body());
 }
 
 int32_t fpm_last_run_stats(const fpm_context* ctx, fpm_run_stats* stats) {

@@ -16,7 +16,7 @@ from . import _native
 from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasurementsError, InvalidModelError,
                      InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
                      UnsupportedError)
-from .experiment import (ArrayPose, CameraModel, Illumination, KVectorList, Optics, PlanarLEDArray,
+from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
@@ -24,6 +24,10 @@ from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjectio
                              ReconstructionProblem,
                              ReconstructionResult, RuntimeInfo, last_run_stats, run_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
+from .spectral import (SpectralAcquisitionPlan, SpectralAlternatingProjection, SpectralChannel, SpectralFrame,
+                       SpectralGeometry, SpectralImagePlaneModel, SpectralMixingDiagnostics,
+                       SpectralReconstructionCheckpoint, SpectralReconstructionProblem, SpectralReconstructionResult,
+                       compile_spectral_model)
 
 
 def fft2(values, *, inverse: bool = False):
@@ -42,7 +46,10 @@ def fft2(values, *, inverse: bool = False):
 
 
 __all__ = [
-    "AdaptiveAlternatingProjection", "AlternatingProjection", "ArrayPose", "CameraModel", "CheckpointEvery", "DeviceError", "Epry", "Fpie", "FpmError",
+    "AdaptiveAlternatingProjection", "AlternatingProjection", "ArrayPose", "CameraModel", "CheckpointEvery", "DeviceError",
+    "DirectionList", "SpectralAcquisitionPlan", "SpectralAlternatingProjection", "SpectralChannel", "SpectralFrame",
+    "SpectralGeometry", "SpectralImagePlaneModel", "SpectralMixingDiagnostics", "SpectralReconstructionCheckpoint",
+    "SpectralReconstructionProblem", "SpectralReconstructionResult", "compile_spectral_model", "Epry", "Fpie", "FpmError",
     "FrameOutOfRangeError", "GradientDescent", "Illumination", "ImagePlaneModel", "InvalidMeasurementsError",
     "InvalidModelError", "InvalidParameterError", "InvalidShapeError", "KVectorList", "LengthMismatchError",
     "MeasurementStack", "Mpie", "NumericalError", "Optics", "PlanarLEDArray", "PupilAberration",

@@ -24,6 +24,7 @@ EXPORTED = (
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
     "fpm_fft2", "fpm_forward_stack", "fpm_simulate_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
+    "fpm_spectral_run", "fpm_spectral_forward",
 )
 
 
@@ -92,6 +93,21 @@ class StateDesc(C.Structure):
         ("velocity", C.POINTER(C.c_double)), ("anchor", C.POINTER(C.c_double)),
         ("objectives", C.POINTER(C.c_double)),
     ]
+
+
+class SpectralModelDesc(C.Structure):
+    _fields_ = [
+        ("channels", C.c_int32), ("channel_models", C.POINTER(ModelDesc)), ("object_coupling", C.c_int32),
+        ("exposures", C.c_int32), ("contribution_offsets", C.POINTER(C.c_int32)),
+        ("contribution_channel", C.POINTER(C.c_int32)), ("contribution_local_frame", C.POINTER(C.c_int32)),
+        ("contribution_weight", C.POINTER(C.c_double)), ("exposure_gain", C.POINTER(C.c_double)),
+        ("exposure_background", C.POINTER(C.c_double)),
+    ]
+
+
+class SpectralParams(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("batch_size", C.c_int32), ("loss_type", C.c_int32),
+                ("object_step", C.c_double), ("epsilon", C.c_double)]
 
 
 class ResultDesc(C.Structure):

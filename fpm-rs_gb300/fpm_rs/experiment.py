@@ -170,6 +170,54 @@ class PlanarLEDArray:
         return ResolvedSources(np.stack([kx, ky], axis=1))
 
 
+class DirectionList:
+    """Illumination propagation directions (src/experiment/illumination.rs:76-254),
+    stored as unit vectors with non-negative z; resolves to k * (ux, uy)
+    with k = 2 pi n_illumination / wavelength."""
+
+    def __init__(self, unit_vectors):
+        u = np.array(unit_vectors, dtype=np.float64)
+        if u.ndim != 2 or u.shape[1] != 3 or u.shape[0] == 0:
+            raise InvalidParameterError("unit_vectors: at least one (x, y, z) direction is required")
+        if not np.all(np.isfinite(u)):
+            raise InvalidParameterError("unit_vectors: components must be finite")
+        norm = np.sqrt(np.sum(u * u, axis=1))
+        if np.any(np.abs(norm - 1.0) > 128.0 * np.finfo(np.float64).eps):
+            raise InvalidParameterError("unit_vectors: vectors must be normalized")
+        if np.any(u[:, 2] < -128.0 * np.finfo(np.float64).eps):
+            raise InvalidParameterError("unit_vectors: directions must lie in the positive-z illumination hemisphere")
+        u[:, 2] = np.maximum(u[:, 2], 0.0)
+        self._u = u
+
+    @staticmethod
+    def from_unit_vectors(*, values) -> "DirectionList":
+        return DirectionList(values)
+
+    @staticmethod
+    def from_direction_cosines(*, values) -> "DirectionList":
+        """Transverse direction cosines (dx, dy); z = sqrt(1 - dx^2 - dy^2)."""
+        d = np.asarray(values, dtype=np.float64).reshape(-1, 2)
+        if not np.all(np.isfinite(d)):
+            raise InvalidParameterError("directions: components must be finite")
+        t = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]
+        if np.any(t > 1.0 + 128.0 * np.finfo(np.float64).eps):
+            raise InvalidParameterError("directions: squared transverse direction magnitude cannot exceed one")
+        return DirectionList(np.stack([d[:, 0], d[:, 1], np.sqrt(np.maximum(1.0 - t, 0.0))], axis=1))
+
+    @property
+    def source_count(self) -> int:
+        return self._u.shape[0]
+
+    @property
+    def unit_vectors(self) -> np.ndarray:
+        return self._u.copy()
+
+    def resolve(self, optics: Optics) -> ResolvedSources:
+        optics._validate()
+        k = 2.0 * math.pi * optics.illumination_refractive_index / optics.wavelength_vacuum_m
+        return ResolvedSources(np.stack([k * self._u[:, 0], k * self._u[:, 1]], axis=1))
+
+
 class KVectorList:
     """Explicit transverse wave vectors, float64 (sources, 2) of (kx, ky) rad/m."""
 

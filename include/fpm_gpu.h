@@ -24,6 +24,11 @@
  *                                  -> fpm_run with FPM_ALG_ADAPTIVE_AP
  *   ReconstructionCheckpoint capture / run_from_checkpoint
  *                                  src/reconstruction/checkpoint.rs:38-146 -> fpm_run_batch_resumable
+ *   SpectralRunner::run + SpectralAlternatingProjection
+ *                                  src/reconstruction/spectral.rs:494-642,
+ *                                  src/algorithms/spectral.rs:182-271 -> fpm_spectral_run
+ *   SpectralImagePlaneModel::forward_intensity
+ *                                  src/model/spectral.rs:400-446 -> fpm_spectral_forward
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
  *                                  fpm_run_batch_host (host inputs, copies overlapped with the runs)
  *   Error / FpmError ............. src/error.rs:12, python/src/errors.rs:17-50 -> FPM_ERR_* + fpm_last_error
@@ -291,6 +296,59 @@ typedef struct {
 } fpm_run_stats;
 
 int32_t fpm_last_run_stats(const fpm_context *ctx, fpm_run_stats *stats);
+
+/* ------------------------------------------------- narrowband spectral AP */
+/* ObjectCoupling (src/model/spectral.rs:21-30). */
+enum { FPM_COUPLING_INDEPENDENT = 0, FPM_COUPLING_SHARED_COMPLEX = 1 };
+
+/* SpectralImagePlaneModel (src/model/spectral.rs:46-54): channel kernels
+ * compiled on one common grid (equal image and reconstruction shapes, no
+ * background) and the canonical sparse detector plan
+ * (SpectralAcquisitionPlan, src/experiment/spectral.rs:44-70). Exposure e
+ * sums contributions [contribution_offsets[e], contribution_offsets[e + 1]):
+ * (channel, local frame, spectral weight > 0), unique per exposure. */
+typedef struct {
+    int32_t channels;
+    const fpm_model_desc *channel_models;   /* [channels] */
+    int32_t object_coupling;                /* FPM_COUPLING_* */
+    int32_t exposures;                      /* physical detector frames */
+    const int32_t *contribution_offsets;    /* [exposures + 1], starting at 0 */
+    const int32_t *contribution_channel;    /* [contributions] */
+    const int32_t *contribution_local_frame;
+    const double *contribution_weight;
+    const double *exposure_gain;            /* [exposures], finite and > 0 */
+    const double *exposure_background;      /* [exposures], finite and >= 0 */
+} fpm_spectral_model_desc;
+
+/* SpectralAlternatingProjection (src/algorithms/spectral.rs:111-145);
+ * defaults iterations 50, batch_size 1, amplitude MSE, object_step 1,
+ * epsilon 1e-10. batch_size does not change the per-exposure updates. */
+typedef struct {
+    int32_t iterations;
+    int32_t batch_size;
+    int32_t loss_type;      /* diagnostic objective, FPM_LOSS_* */
+    double object_step;
+    double epsilon;
+} fpm_spectral_params;
+
+/* Object-only spectral alternating projection on the device. Stored objects:
+ * one per channel (independent) or one (shared complex), each mh*mw.
+ *   order            NULL (acquisition order) or a permutation of the exposures, every pass
+ *   initial_objects  NULL (measured-amplitude initialisation) or natural-order complex objects
+ *   resume_spectra   NULL, or centred spectra after completed_iterations passes (a checkpoint)
+ * Outputs, each NULL or sized for the stored objects: objects (natural order),
+ * object_spectra (centred), objectives [iterations - completed_iterations],
+ * the weighted mean diagnostic loss of each pass before its updates. */
+int32_t fpm_spectral_run(fpm_context *ctx, const fpm_spectral_model_desc *model,
+                         const fpm_measurement_desc *measurements, const fpm_spectral_params *params,
+                         const int32_t *order, const double *initial_objects, const double *resume_spectra,
+                         int32_t completed_iterations, double *objects, double *object_spectra,
+                         double *objectives);
+
+/* Detector intensities of every exposure, [exposures*h*w], from the stored
+ * objects' centred spectra: gain * sum(weight * local intensity) + background. */
+int32_t fpm_spectral_forward(fpm_context *ctx, const fpm_spectral_model_desc *model, const double *spectra,
+                             double *intensities);
 
 #ifdef __cplusplus
 }

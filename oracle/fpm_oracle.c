@@ -1633,3 +1633,265 @@ double orc_complex_nrmse(const double *reference_d, const double *candidate_d, i
     if (denominator < 2.220446049250313e-16) denominator = 2.220446049250313e-16;
     return sqrt(err / count) / denominator;
 }
+
+/* ------------------------------------------------- narrowband spectral AP */
+
+typedef struct {
+    int channel, source;    /* channel kernel and its global source index */
+    int object;             /* stored object index */
+    double weight;          /* effective mode weight */
+    cplx *field, *exit;     /* detector field and pupil-weighted patch, pre-update */
+} spectral_mode;
+
+static int spectral_source(const orc_spectral_problem *p, int channel, int local) {
+    int offset = 0;
+    for (int c = 0; c < channel; ++c) offset += p->channel_sources[c];
+    return offset + local;
+}
+
+static double spectral_frame_gain(const orc_spectral_problem *p, int channel, int local) {
+    return p->frame_gains ? p->frame_gains[spectral_source(p, channel, local)] : 1.0;
+}
+
+static int spectral_object_index(const orc_spectral_problem *p, int channel) {
+    return p->shared_object ? 0 : channel;
+}
+
+static int spectral_object_count(const orc_spectral_problem *p) { return p->shared_object ? 1 : p->channels; }
+
+/* Coherent field and exit of one channel source from a centred spectrum:
+ * ForwardModel::forward_source_field_standard_into (src/model/forward.rs:146-169)
+ * and the pupil-weighted patch of SpectralReconstructionState::evaluate_frame
+ * (src/reconstruction/spectral.rs:330-385). */
+static int32_t spectral_source_field(const orc_spectral_problem *p, const cplx *spectrum, int channel, int source,
+                                     cplx *exit, cplx *field) {
+    size_t n = (size_t)p->h * p->w;
+    int32_t st = extract_patch_c(spectrum, p->mh, p->mw, (long)p->start_row[source], (long)p->start_col[source],
+                                 p->h, p->w, p->off_row ? p->off_row[source] : 0.0,
+                                 p->off_col ? p->off_col[source] : 0.0, exit);
+    if (st) return st;
+    const cplx *pupil = (const cplx *)p->pupils + (size_t)channel * n;
+    for (size_t i = 0; i < n; ++i) exit[i] = c_mul(exit[i], pupil[i]);
+    ifftshift_c(exit, field, p->h, p->w);
+    fft2_c(field, p->h, p->w, 1);
+    return ORC_OK;
+}
+
+/* SpectralReconstructionState::initialize (src/reconstruction/spectral.rs:123-199):
+ * weighted, mask-aware measured amplitude per stored object, nearest
+ * upsampling to the common grid. objects: object_count*mh*mw complex. */
+static int32_t spectral_initial_objects(const orc_spectral_problem *p, cplx *objects) {
+    size_t n = (size_t)p->h * p->w;
+    double *amplitude = (double *)malloc(sizeof(double) * n);
+    double *weights = (double *)malloc(sizeof(double) * n);
+    int32_t st = ORC_OK;
+    for (int o = 0; o < spectral_object_count(p) && !st; ++o) {
+        memset(amplitude, 0, sizeof(double) * n);
+        memset(weights, 0, sizeof(double) * n);
+        double total_amplitude = 0.0, total_weight = 0.0;
+        for (int e = 0; e < p->exposures; ++e) {
+            int first = p->contribution_offsets[e], last = p->contribution_offsets[e + 1];
+            int uses = 0;
+            for (int k = first; k < last; ++k)
+                if (spectral_object_index(p, p->contribution_channel[k]) == o) uses = 1;
+            if (!uses) continue;
+            double fw = p->weights ? p->weights[e] : 1.0;
+            if (fw == 0.0) continue;
+            double gain = 0.0;
+            for (int k = first; k < last; ++k)
+                gain += p->contribution_weight[k] *
+                        spectral_frame_gain(p, p->contribution_channel[k], p->contribution_local[k]);
+            gain *= p->exposure_gain[e];
+            if (!isfinite(gain) || gain <= 0.0) {
+                st = fail(ORC_NUMERICAL, "spectral initialization gain must be finite and positive");
+                break;
+            }
+            const double *measured = p->data + (size_t)e * n;
+            const uint8_t *mask = p->masks ? p->masks + (size_t)e * n : NULL;
+            for (size_t i = 0; i < n; ++i) {
+                if (mask && mask[i] == 0) continue;
+                double value = sqrt(fmax((measured[i] - p->exposure_background[e]) / gain, 0.0));
+                amplitude[i] += fw * value;
+                weights[i] += fw;
+                total_amplitude += fw * value;
+                total_weight += fw;
+            }
+        }
+        if (st) break;
+        double fallback = total_amplitude / total_weight;
+        for (size_t i = 0; i < n; ++i) amplitude[i] = weights[i] > 0.0 ? amplitude[i] / weights[i] : fallback;
+        cplx *object = objects + (size_t)o * p->mh * p->mw;
+        for (long r = 0; r < p->mh; ++r)
+            for (long c = 0; c < p->mw; ++c)
+                object[r * p->mw + c] = cx(amplitude[(r * p->h / p->mh) * p->w + c * p->w / p->mw], 0.0);
+    }
+    free(amplitude);
+    free(weights);
+    return st;
+}
+
+/* One exposure of SpectralAlternatingProjection::step
+ * (src/algorithms/spectral.rs:182-271): every mode from the pre-frame state,
+ * one amplitude ratio from their weighted intensity sum, then each mode's
+ * local-denominator correction into its stored object. */
+static int32_t spectral_exposure(const orc_spectral_problem *p, const orc_spectral_params *prm, cplx *spectra, int e,
+                                 spectral_mode *modes, double *predicted, cplx *projection, cplx *work, cplx *centered,
+                                 double *objective_sum, double *weight_sum_out) {
+    size_t n = (size_t)p->h * p->w, n_high = (size_t)p->mh * p->mw;
+    double fw = p->weights ? p->weights[e] : 1.0;
+    if (fw == 0.0) return ORC_OK;
+    int first = p->contribution_offsets[e], last = p->contribution_offsets[e + 1];
+    int count = last - first;
+    int separate = count == 1;
+    double effective_gain = p->exposure_gain[e];
+    if (separate)
+        effective_gain *= p->contribution_weight[first] *
+                          spectral_frame_gain(p, p->contribution_channel[first], p->contribution_local[first]);
+    memset(predicted, 0, sizeof(double) * n);
+    double weight_sum = 0.0;
+    for (int k = 0; k < count; ++k) {
+        int channel = p->contribution_channel[first + k], local = p->contribution_local[first + k];
+        spectral_mode *m = &modes[k];
+        m->channel = channel;
+        m->source = spectral_source(p, channel, local);
+        m->object = spectral_object_index(p, channel);
+        m->weight = separate ? 1.0 : p->contribution_weight[first + k] * spectral_frame_gain(p, channel, local);
+        int32_t st = spectral_source_field(p, spectra + (size_t)m->object * n_high, channel, m->source, m->exit,
+                                           m->field);
+        if (st) return st;
+        for (size_t i = 0; i < n; ++i) predicted[i] += m->weight * c_norm_sqr(m->field[i]);
+        weight_sum += m->weight;
+    }
+    const double *measured = p->data + (size_t)e * n;
+    const uint8_t *mask = p->masks ? p->masks + (size_t)e * n : NULL;
+    double background = p->exposure_background[e];
+    double loss = 0.0;
+    long valid = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (mask && mask[i] == 0) {
+            projection[i] = cx(1.0, 0.0);
+            continue;
+        }
+        ++valid;
+        loss += point_loss(effective_gain * predicted[i] + background, measured[i], prm->loss_type);
+        double target = fmax((measured[i] - background) / effective_gain, 0.0);
+        projection[i] = predicted[i] > prm->epsilon ? cx(sqrt(target / predicted[i]), 0.0)
+                                                    : cx(0.0, sqrt(target / weight_sum));
+    }
+    if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", e);
+    *objective_sum += fw * (loss / (double)valid);
+    *weight_sum_out += fw;
+    for (int k = 0; k < count; ++k) {
+        spectral_mode *m = &modes[k];
+        const cplx *pupil = (const cplx *)p->pupils + (size_t)m->channel * n;
+        for (size_t i = 0; i < n; ++i) {
+            if (mask && mask[i] == 0)
+                work[i] = m->field[i];
+            else if (predicted[i] > prm->epsilon)
+                work[i] = c_scale(m->field[i], projection[i].re);
+            else
+                work[i] = cx(projection[i].im, 0.0);
+        }
+        fft2_c(work, p->h, p->w, 0);
+        fftshift_c(work, centered, p->h, p->w);
+        for (size_t i = 0; i < n; ++i)
+            work[i] = c_divr(c_mul(c_conj(pupil[i]), c_sub(centered[i], m->exit[i])),
+                             c_norm_sqr(pupil[i]) + prm->epsilon);
+        int32_t st = insert_adjoint_c(spectra + (size_t)m->object * n_high, p->mh, p->mw,
+                                      (long)p->start_row[m->source], (long)p->start_col[m->source], p->h, p->w,
+                                      p->off_row ? p->off_row[m->source] : 0.0,
+                                      p->off_col ? p->off_col[m->source] : 0.0, work,
+                                      fw * prm->object_step * (m->weight / weight_sum));
+        if (st) return st;
+    }
+    return ORC_OK;
+}
+
+int32_t orc_spectral_run(const orc_spectral_problem *p, const orc_spectral_params *prm, const int32_t *order,
+                         const double *initial_objects, const double *initial_spectra,
+                         int32_t completed_iterations, double *spectra_out, double *objectives) {
+    if (prm->iterations <= 0 || !(prm->object_step > 0.0) || !isfinite(prm->object_step) ||
+        !(prm->epsilon > 0.0) || !isfinite(prm->epsilon))
+        return fail(ORC_INVALID_PARAMETER, "spectral AP parameters must be positive and finite");
+    if (completed_iterations < 0 || completed_iterations > prm->iterations)
+        return fail(ORC_INVALID_PARAMETER, "total target cannot precede checkpoint iterations");
+    size_t n = (size_t)p->h * p->w, n_high = (size_t)p->mh * p->mw;
+    int objects = spectral_object_count(p);
+    cplx *spectra = (cplx *)spectra_out;
+    int32_t st = ORC_OK;
+    if (initial_spectra) {
+        memcpy(spectra, initial_spectra, sizeof(cplx) * n_high * objects);
+    } else {
+        cplx *natural = (cplx *)malloc(sizeof(cplx) * n_high * objects);
+        if (initial_objects)
+            memcpy(natural, initial_objects, sizeof(cplx) * n_high * objects);
+        else
+            st = spectral_initial_objects(p, natural);
+        for (int o = 0; o < objects && !st; ++o) {
+            fft2_c(natural + (size_t)o * n_high, p->mh, p->mw, 0);
+            fftshift_c(natural + (size_t)o * n_high, spectra + (size_t)o * n_high, p->mh, p->mw);
+        }
+        free(natural);
+        if (st) return st;
+    }
+    int max_count = 1;
+    for (int e = 0; e < p->exposures; ++e) {
+        int count = p->contribution_offsets[e + 1] - p->contribution_offsets[e];
+        if (count > max_count) max_count = count;
+    }
+    spectral_mode *modes = (spectral_mode *)calloc((size_t)max_count, sizeof(spectral_mode));
+    cplx *buffers = (cplx *)malloc(sizeof(cplx) * n * (2 * (size_t)max_count + 3));
+    for (int k = 0; k < max_count; ++k) {
+        modes[k].field = buffers + (size_t)(2 * k) * n;
+        modes[k].exit = buffers + (size_t)(2 * k + 1) * n;
+    }
+    cplx *projection = buffers + (size_t)(2 * max_count) * n;
+    cplx *work = projection + n, *centered = work + n;
+    double *predicted = (double *)malloc(sizeof(double) * n);
+    for (int it = completed_iterations; it < prm->iterations && !st; ++it) {
+        double objective_sum = 0.0, weight_sum = 0.0;
+        for (int idx = 0; idx < p->exposures && !st; ++idx) {
+            int e = order ? order[idx] : idx;
+            st = spectral_exposure(p, prm, spectra, e, modes, predicted, projection, work, centered, &objective_sum,
+                                   &weight_sum);
+        }
+        if (st) break;
+        if (!(weight_sum > 0.0)) {
+            st = fail(ORC_NUMERICAL, "spectral iteration has no positive frame weight");
+            break;
+        }
+        double objective = objective_sum / weight_sum;
+        if (!isfinite(objective)) {
+            st = fail(ORC_NUMERICAL, "spectral iteration objective is non-finite");
+            break;
+        }
+        if (objectives) objectives[it - completed_iterations] = objective;
+    }
+    free(predicted);
+    free(buffers);
+    free(modes);
+    return st;
+}
+
+int32_t orc_spectral_forward(const orc_spectral_problem *p, const double *spectra_d, double *out) {
+    size_t n = (size_t)p->h * p->w, n_high = (size_t)p->mh * p->mw;
+    const cplx *spectra = (const cplx *)spectra_d;
+    cplx *exit = (cplx *)malloc(sizeof(cplx) * n * 2);
+    cplx *field = exit + n;
+    int32_t st = ORC_OK;
+    for (int e = 0; e < p->exposures && !st; ++e) {
+        double *dst = out + (size_t)e * n;
+        memset(dst, 0, sizeof(double) * n);
+        for (int k = p->contribution_offsets[e]; k < p->contribution_offsets[e + 1] && !st; ++k) {
+            int channel = p->contribution_channel[k], local = p->contribution_local[k];
+            int source = spectral_source(p, channel, local);
+            st = spectral_source_field(p, spectra + (size_t)spectral_object_index(p, channel) * n_high, channel,
+                                       source, exit, field);
+            double gain = spectral_frame_gain(p, channel, local), weight = p->contribution_weight[k];
+            for (size_t i = 0; i < n && !st; ++i) dst[i] += weight * (gain * c_norm_sqr(field[i]));
+        }
+        for (size_t i = 0; i < n; ++i) dst[i] = p->exposure_gain[e] * dst[i] + p->exposure_background[e];
+    }
+    free(exit);
+    return st;
+}

@@ -147,6 +147,51 @@ int32_t orc_run_many(int32_t count, const orc_problem *problems, const orc_param
 
 double orc_complex_nrmse(const double *reference, const double *candidate, int64_t len);
 
+/* Narrowband spectral problem (src/model/spectral.rs:46-54,
+ * src/experiment/spectral.rs:44-70): channel kernels on one common grid and a
+ * canonical sparse detector plan. Channel c's local frames are sources
+ * [source_offset(c), source_offset(c) + channel_sources[c]) of the
+ * concatenated per-source arrays. */
+typedef struct {
+    int32_t h, w, mh, mw;
+    int32_t channels;
+    int32_t shared_object;               /* 1: ObjectCoupling::SharedComplex */
+    const int32_t *channel_sources;      /* [channels] */
+    const int64_t *start_row, *start_col;
+    const double *off_row, *off_col;     /* NULL: integer crops */
+    const double *frame_gains;           /* NULL (unit) or concatenated per source */
+    const double *pupils;                /* channels*h*w complex */
+    int32_t exposures;
+    const int32_t *contribution_offsets; /* [exposures + 1] */
+    const int32_t *contribution_channel, *contribution_local;
+    const double *contribution_weight;
+    const double *exposure_gain, *exposure_background;  /* [exposures] */
+    const double *data;                  /* exposures*h*w */
+    const double *weights;               /* NULL or exposures */
+    const uint8_t *masks;                /* NULL or exposures*h*w */
+} orc_spectral_problem;
+
+typedef struct {
+    int32_t iterations, loss_type;
+    double object_step, epsilon;
+} orc_spectral_params;
+
+/* SpectralRunner::run with SpectralAlternatingProjection
+ * (src/reconstruction/spectral.rs:494-642, src/algorithms/spectral.rs:182-271).
+ * order: NULL (sequential) or an exposure permutation used every pass.
+ * initial_objects: NULL (measured-amplitude initialisation) or
+ * object_count*mh*mw natural-order complex objects. initial_spectra, when not
+ * NULL, replaces both: centred spectra to continue from, with
+ * completed_iterations passes already done. spectra receives object_count
+ * centred spectra; objectives one value per executed pass. */
+int32_t orc_spectral_run(const orc_spectral_problem *problem, const orc_spectral_params *params,
+                         const int32_t *order, const double *initial_objects, const double *initial_spectra,
+                         int32_t completed_iterations, double *spectra, double *objectives);
+
+/* SpectralImagePlaneModel::forward_intensity (src/model/spectral.rs:400-446)
+ * for every exposure: out is exposures*h*w. */
+int32_t orc_spectral_forward(const orc_spectral_problem *problem, const double *spectra, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -424,3 +424,119 @@ def run_many(problems: Sequence[Problem], algorithm: str, workers: int, **kw) ->
         arrays.append(a)
     _check(lib().orc_run_many(len(problems), structs, C.byref(prm), outs, workers))
     return arrays
+
+
+# ------------------------------------------------------------ spectral ----
+
+class _SpectralProblem(C.Structure):
+    _fields_ = [
+        ("h", C.c_int32), ("w", C.c_int32), ("mh", C.c_int32), ("mw", C.c_int32),
+        ("channels", C.c_int32), ("shared_object", C.c_int32),
+        ("channel_sources", C.POINTER(C.c_int32)),
+        ("start_row", C.POINTER(C.c_int64)), ("start_col", C.POINTER(C.c_int64)),
+        ("off_row", C.POINTER(C.c_double)), ("off_col", C.POINTER(C.c_double)),
+        ("frame_gains", C.POINTER(C.c_double)),
+        ("pupils", C.POINTER(C.c_double)),
+        ("exposures", C.c_int32),
+        ("contribution_offsets", C.POINTER(C.c_int32)),
+        ("contribution_channel", C.POINTER(C.c_int32)), ("contribution_local", C.POINTER(C.c_int32)),
+        ("contribution_weight", C.POINTER(C.c_double)),
+        ("exposure_gain", C.POINTER(C.c_double)), ("exposure_background", C.POINTER(C.c_double)),
+        ("data", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double)), ("masks", C.POINTER(C.c_uint8)),
+    ]
+
+
+class _SpectralParams(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("loss_type", C.c_int32), ("object_step", C.c_double),
+                ("epsilon", C.c_double)]
+
+
+@dataclass
+class SpectralProblem:
+    """Channel models (dicts of compile_model's form, frame gains under
+    "frame_gains"), a canonical detector plan and measurements.
+
+    frames: one (gain, background, [(channel, local_frame, spectral_weight), ...])
+    per exposure, already canonical (positive weights, unique pairs)."""
+
+    channels: list
+    frames: list
+    data: np.ndarray | None = None
+    shared_object: bool = False
+    weights: np.ndarray | None = None
+    masks: np.ndarray | None = None
+
+    @property
+    def object_count(self) -> int:
+        return 1 if self.shared_object else len(self.channels)
+
+    def struct(self) -> _SpectralProblem:
+        ch = self.channels
+        self._keep = []
+
+        def keep(a):
+            self._keep.append(a)
+            return a
+
+        p = _SpectralProblem()
+        p.h, p.w, p.mh, p.mw = ch[0]["h"], ch[0]["w"], ch[0]["mh"], ch[0]["mw"]
+        p.channels = len(ch)
+        p.shared_object = int(bool(self.shared_object))
+        p.channel_sources = _ptr(keep(np.array([len(c["start_row"]) for c in ch], np.int32)), C.c_int32)
+        cat = lambda key, dtype: keep(np.ascontiguousarray(np.concatenate([np.asarray(c[key]) for c in ch]), dtype))
+        p.start_row = _ptr(cat("start_row", np.int64), C.c_int64)
+        p.start_col = _ptr(cat("start_col", np.int64), C.c_int64)
+        p.off_row = _ptr(cat("off_row", np.float64), C.c_double)
+        p.off_col = _ptr(cat("off_col", np.float64), C.c_double)
+        gains = [np.asarray(c.get("frame_gains", np.ones(len(c["start_row"]))), np.float64) for c in ch]
+        p.frame_gains = _ptr(keep(np.ascontiguousarray(np.concatenate(gains))), C.c_double)
+        p.pupils = _ptr(keep(_c128(np.stack([c["pupil"] for c in ch]))), C.c_double)
+        p.exposures = len(self.frames)
+        offsets = np.zeros(len(self.frames) + 1, np.int32)
+        chan, local, weight = [], [], []
+        for e, (_, _, contributions) in enumerate(self.frames):
+            for c, l, w in contributions:
+                chan.append(c)
+                local.append(l)
+                weight.append(w)
+            offsets[e + 1] = len(chan)
+        p.contribution_offsets = _ptr(keep(offsets), C.c_int32)
+        p.contribution_channel = _ptr(keep(np.array(chan, np.int32)), C.c_int32)
+        p.contribution_local = _ptr(keep(np.array(local, np.int32)), C.c_int32)
+        p.contribution_weight = _ptr(keep(np.array(weight, np.float64)), C.c_double)
+        p.exposure_gain = _ptr(keep(np.array([f[0] for f in self.frames], np.float64)), C.c_double)
+        p.exposure_background = _ptr(keep(np.array([f[1] for f in self.frames], np.float64)), C.c_double)
+        data = self.data if self.data is not None else np.zeros((len(self.frames), p.h, p.w))
+        p.data = _ptr(keep(_f64(data)), C.c_double)
+        p.weights = _ptr(keep(_f64(self.weights)) if self.weights is not None else None, C.c_double)
+        p.masks = _ptr(keep(np.ascontiguousarray(self.masks, np.uint8)) if self.masks is not None else None,
+                       C.c_uint8)
+        return p
+
+
+def spectral_forward(problem: SpectralProblem, spectra) -> np.ndarray:
+    """Detector intensities of every exposure from centred spectra (object_count, mh, mw)."""
+    s = _c128(spectra)
+    st = problem.struct()
+    out = np.zeros((st.exposures, st.h, st.w))
+    _check(lib().orc_spectral_forward(C.byref(st), _ptr(s, C.c_double), _ptr(out, C.c_double)))
+    return out
+
+
+def spectral_run(problem: SpectralProblem, *, iterations=50, object_step=1.0, epsilon=1e-10,
+                 loss_type="amplitude_mse", order=None, initial_objects=None, initial_spectra=None,
+                 completed_iterations=0) -> dict:
+    """Spectral alternating projection; returns centred spectra, objects and objectives."""
+    st = problem.struct()
+    prm = _SpectralParams(int(iterations), LOSSES[loss_type], float(object_step), float(epsilon))
+    k = problem.object_count
+    spectra = np.zeros((k, st.mh, st.mw), np.complex128)
+    objectives = np.zeros(int(iterations) - int(completed_iterations))
+    order_a = None if order is None else np.ascontiguousarray(order, np.int32)
+    init_o = None if initial_objects is None else _c128(initial_objects)
+    init_s = None if initial_spectra is None else _c128(initial_spectra)
+    _check(lib().orc_spectral_run(C.byref(st), C.byref(prm), _ptr(order_a, C.c_int32), _ptr(init_o, C.c_double),
+                                  _ptr(init_s, C.c_double), int(completed_iterations), _ptr(spectra, C.c_double),
+                                  _ptr(objectives, C.c_double)))
+    objects = np.stack([state_object(s) for s in spectra])
+    return dict(spectra=spectra, objects=objects, objectives=objectives)
