@@ -12,6 +12,15 @@ collective on the data path (weak scaling: each rank runs its own tiles).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line on rank 0.
+
+  python bench.py --workload spectral [--requests R]
+
+times instead the spectral AP share of the served three-wavelength request
+stream: R independent requests (N ~ U{64,128,256}, LED grids 9x9 to 15x15,
+seed 5), each a shared complex object seen through 470/532/630 nm channels
+with fixed per-wavelength pupils, one exposure per LED with all three
+wavelengths lit, Poisson counts at 1e4 photons, SpectralAlternatingProjection
+(50 passes), reconstructed together by fpm_spectral_run_batch.
 """
 
 from __future__ import annotations
@@ -54,7 +63,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--tiles", type=int, default=1024)
-    ap.add_argument("--iterations", type=int, default=30)
+    ap.add_argument("--iterations", type=int, default=None, help="30 (tiles) or 50 (spectral) when omitted")
+    ap.add_argument("--workload", choices=("tiles", "spectral"), default="tiles")
+    ap.add_argument("--requests", type=int, default=64, help="spectral requests per step")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
     ap.add_argument("--cpu-sample-iterations", type=int, default=1)
@@ -448,11 +459,198 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ spectral
+
+SPECTRAL_SIZES = (64, 128, 256)
+SPECTRAL_SIDES = (9, 11, 13, 15)
+SPECTRAL_WAVELENGTHS = (470e-9, 532e-9, 630e-9)
+
+
+def spectral_requests(count: int, seed: int):
+    rng = np.random.default_rng(seed)
+    return [(int(rng.choice(SPECTRAL_SIZES)), int(rng.choice(SPECTRAL_SIDES))) for _ in range(count)]
+
+
+def spectral_optics(wavelength):
+    o = dict(W.OPTICS)
+    o["wavelength_vacuum_m"] = wavelength
+    return o
+
+
+def build_spectral(fpm, n, side, seed):
+    """(problem, oracle channel models, oracle frames, truth) of one request."""
+    import oracle
+
+    channels = [fpm.SpectralChannel(channel_id=name, optics=fpm.Optics(**spectral_optics(w)))
+                for name, w in zip(("470nm", "532nm", "630nm"), SPECTRAL_WAVELENGTHS)]
+    grid, ref = W.led_grid(side)
+    geometry = fpm.SpectralGeometry.shared(
+        geometry=fpm.PlanarLEDArray(grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z))))
+    leds = side * side
+    unit = fpm.SpectralAcquisitionPlan.multiplexed(
+        frames=[fpm.SpectralFrame(contributions=[(c, l, 1.0) for c in range(3)]) for l in range(leds)])
+    model = fpm.compile_spectral_model(channels=channels, geometry=geometry, acquisition=unit, image_shape=(n, n),
+                                       object_coupling="shared_complex")
+    truth = W.smooth_random_object(model.reconstruction_shape, seed)[None]
+    intensity = model.forward_intensities(object_spectra=np.ascontiguousarray(
+        np.stack([oracle.object_spectrum(truth[0])])))
+    counts, scale = W.poisson_counts(intensity, PHOTONS, seed + 1)
+    plan = fpm.SpectralAcquisitionPlan.multiplexed(
+        frames=[fpm.SpectralFrame(contributions=[(c, l, 1.0) for c in range(3)], gain=scale) for l in range(leds)])
+    model = fpm.SpectralImagePlaneModel.from_compiled_channels(
+        channel_ids=model.channel_ids, models=model.channel_models, acquisition=plan, object_coupling="shared_complex")
+    problem = fpm.SpectralReconstructionProblem(measurements=counts, model=model)
+    omodels = []
+    for m in model.channel_models:
+        om = oracle.compile_model(spectral_optics(m._wavelength), m.k_vectors[:, 0], m.k_vectors[:, 1], (n, n),
+                                  model.reconstruction_shape)
+        om["frame_gains"] = np.ones(m.frame_count)
+        omodels.append(om)
+    frames = [(f.gain, f.background, f.contributions) for f in plan.frames]
+    return problem, omodels, frames, truth
+
+
+def run_spectral(args):
+    dist = Dist()
+    os.environ.setdefault("FPM_DEVICE", str(dist.local))
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    import fpm_rs as fpm
+    import oracle
+
+    iterations = args.iterations or 50
+    reqs = spectral_requests(args.requests, 5 + 1000 * dist.rank)
+    t0 = time.perf_counter()
+    built = [build_spectral(fpm, n, side, 50_000 + 1000 * dist.rank + i) for i, (n, side) in enumerate(reqs)]
+    problems = [b[0] for b in built]
+    setup_s = time.perf_counter() - t0
+    solver = fpm.SpectralAlternatingProjection(iterations=iterations)
+    for _ in range(args.warmup):
+        solver.run_many(problems=problems)
+    clocks = ClockSampler(dist.local)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks.start()
+    device_ms = engine_bytes = engine_span = 0.0
+    launches = 0
+    latencies = []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        results = solver.run_many(problems=problems)
+        st = fpm.last_run_stats()
+        device_ms += st["run_ms"]
+        launches += st["kernel_launches"]
+        engine_bytes += st["engine_bytes"]
+        engine_span += st["engine_span_ms"]
+        for n, count, end_ms in st["buckets"]:
+            latencies += [end_ms] * count
+    torch.cuda.synchronize()
+    wall_s = dist.max((time.perf_counter() - wall0) / args.steps)
+    dist.barrier()
+    clock_info = clocks.stop()
+    step_ms = dist.max(device_ms / args.steps)
+    total = dist.sum(len(problems))
+    value = total / (step_ms / 1e3)
+    # e2e: the public call with host inputs, every step uploading float64
+    # measurements and the channel constants and downloading complex128
+    # objects, spectra and the objectives.
+    h2d = d2h = 0
+    for p in problems:
+        n = p.image_shape[0]
+        mh, mw = p.reconstruction_shape
+        h2d += p.measurements._data.nbytes + 3 * n * n * 8 + 3 * p.frame_count * (48 + 56)
+        d2h += 2 * mh * mw * 16 + 8 * iterations * 16
+    peak, peak_kind = peaks()
+    achieved = (engine_bytes / args.steps) / (engine_span / args.steps / 1e3) / 1e9 if engine_span > 0 else None
+
+    # Parity spot check: the smallest request against the FP64 oracle.
+    check = min(range(len(reqs)), key=lambda i: (reqs[i][0], reqs[i][1]))
+    p, om, frames, truth = built[check]
+    expected = oracle.spectral_run(oracle.SpectralProblem(om, frames, p.measurements._data, shared_object=True),
+                                   iterations=iterations)
+    nrmse = oracle.complex_nrmse(expected["objects"][0], results[check].object[0])
+    truth_nrmse = oracle.complex_nrmse(truth[0], results[check].object[0])
+
+    # CPU baseline: the oracle on one request per size for one pass, one request per thread.
+    baseline = None
+    if dist.rank == 0:
+        sample = []
+        for n in SPECTRAL_SIZES:
+            i = next((k for k, r in enumerate(reqs) if r[0] == n), None)
+            if i is not None:
+                sample.append(i)
+        from concurrent.futures import ThreadPoolExecutor
+
+        def timed(i):
+            b = built[i]
+            t = time.perf_counter()
+            oracle.spectral_run(oracle.SpectralProblem(b[1], b[2], b[0].measurements._data, shared_object=True),
+                                iterations=1)
+            return time.perf_counter() - t
+
+        cores = os.cpu_count() or 1
+        with ThreadPoolExecutor(max_workers=cores) as pool:
+            per = list(pool.map(timed, sample))
+        # Requests of this workload weighted by their pass counts and frame counts.
+        per_pass = {reqs[i][0]: per[k] / (reqs[i][1] ** 2) for k, i in enumerate(sample)}
+        mean_request_s = statistics.mean(per_pass[n] * side * side * iterations for n, side in reqs)
+        baseline = {"value": cores / mean_request_s, "unit": "requests/s", "cores": cores, "kind": "port",
+                    "sample": (f"{len(sample)} requests (one per N), 1 of {iterations} passes each, FP64 oracle, one "
+                               f"request per thread; requests/s = cores / mean request time, scaled per LED and "
+                               f"pass to this workload's mix ({sum(per):.1f} CPU-s measured)")}
+    if dist.rank != 0:
+        return
+    lat = sorted(latencies)
+    line = {
+        "metric": "spectral AP requests/s (3-wavelength multiplexed, shared complex object)",
+        "value": value,
+        "unit": "requests/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64",
+        "data": "synthetic (seeded objects, GPU spectral forward model, Poisson counts)",
+        "config": {
+            "workload": (f"{args.requests} spectral AP requests per GPU, N~U{{64,128,256}}, LED grids "
+                         f"{{9,11,13,15}}^2 (seed 5), 470/532/630 nm shared complex object, one exposure per LED "
+                         f"with all three wavelengths, Poisson {PHOTONS:g}, {iterations} passes"),
+            "request_sizes": {str(n): sum(1 for r in reqs if r[0] == n) for n in SPECTRAL_SIZES},
+            "exposures": sum(side * side for _, side in reqs),
+            "timing": "device span from the inputs being resident to the last result, CUDA events",
+            "l2": f"float32 measurements {sum(side * side * n * n * 4 for n, side in reqs) / 1e9:.1f} GB vs 129 MB L2",
+            "setup_s": round(setup_s, 1),
+        },
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "engine_kernel<N, kAlgSpectral>: algorithmic bytes / engine span"},
+        "cpu_baseline": baseline,
+        "e2e": {"value": total / wall_s, "unit": "requests/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches // max(1, args.steps),
+        "clocks": clock_info,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                       "definition": "inputs resident to the request's tile-size group finished, one batch"},
+        "nrmse_vs_fp64": {"request": list(reqs[check]), "value": nrmse, "threshold": 1e-4},
+        "nrmse_vs_truth": truth_nrmse,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "spectral":
+        if args.impl == "reference":
+            raise SystemExit("the spectral workload has no reference arm; its CPU baseline is in the line")
+        run_spectral(args)
+    elif args.impl == "reference":
+        args.iterations = args.iterations or 30
         run_reference(args)
     else:
+        args.iterations = args.iterations or 30
         run_ours(args)
 
 

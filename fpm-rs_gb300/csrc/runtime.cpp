@@ -1642,14 +1642,36 @@ Status spectral_initial_objects(const fpm_spectral_model_desc* sm, const fpm_mea
     return Status::ok();
 }
 
-// SpectralRunner::run with SpectralAlternatingProjection
+// One spectral reconstruction on the device: host constants, resident
+// buffers and the result downloads.
+struct SpectralJob {
+    const fpm_spectral_model_desc* sm = nullptr;
+    const fpm_measurement_desc* ms = nullptr;
+    int N = 0, M = 0, E = 0, CH = 0, objects = 0, completed = 0, max_modes = 1;
+    long long ostride = 0;
+    double weight_total = 0.0, bytes_per_pass = 0.0;
+    std::vector<fpm::FrameParam> params;
+    std::vector<fpm::SpectralStep> steps;
+    std::vector<float2> pupils;
+    std::vector<double> natural;
+    const double* start_objects = nullptr;
+    const double* resume_spectra = nullptr;
+    std::vector<float2*> optr;
+    std::vector<double2*> wptr;
+    std::vector<double> host_partials;
+    int host_status = 0;
+    DeviceBuffer meas, masks, d_pupils, d_params, d_steps, object, wide, fields, prediction, partials, status,
+        object_ptrs, wide_ptrs;
+};
+
+// Host part of SpectralRunner::run with SpectralAlternatingProjection
 // (src/reconstruction/spectral.rs:494-642, src/algorithms/spectral.rs:
-// 182-271): one frame-engine launch over the pass range, each exposure as
-// its modes' evaluation steps followed by their update steps.
-Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
-                    const fpm_spectral_params* a, const int32_t* order, const double* initial_objects,
-                    const double* resume_spectra, int completed, double* objects_out, double* spectra_out,
-                    double* objectives_out) {
+// 182-271): validation, crops, the virtual steps of one pass in schedule
+// order (each exposure's evaluation steps, then its update steps) and the
+// starting objects.
+Status spectral_prepare(SpectralJob& j, const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
+                        const fpm_spectral_params* a, const int32_t* order, const double* initial_objects,
+                        const double* resume_spectra, int completed) {
     FPM_TRY(validate_spectral(sm, ms, a));
     if (completed < 0 || completed > a->iterations)
         return Status::make(FPM_ERR_INVALID_PARAMETER, "total target cannot precede checkpoint iterations");
@@ -1658,10 +1680,16 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
     if (completed > 0 && !resume_spectra)
         return Status::make(FPM_ERR_INVALID_PARAMETER, "completed iterations need the checkpoint's spectra");
     const fpm_model_desc& c0 = sm->channel_models[0];
-    const int N = c0.image_height, M = c0.recon_height, E = sm->exposures, CH = sm->channels;
-    const int C = fpm::engine_ctas(N);
-    const int objects = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 1 : CH;
-    const long long ostride = M + (M & 1);
+    j.sm = sm;
+    j.ms = ms;
+    j.N = c0.image_height;
+    j.M = c0.recon_height;
+    j.E = sm->exposures;
+    j.CH = sm->channels;
+    j.objects = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 1 : j.CH;
+    j.ostride = j.M + (j.M & 1);
+    j.completed = completed;
+    const int N = j.N, M = j.M, E = j.E, CH = j.CH;
     const size_t n2 = (size_t)N * N, nm = (size_t)M * M;
     std::vector<int> schedule(E);
     for (int e = 0; e < E; ++e) schedule[e] = e;
@@ -1676,18 +1704,18 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
     }
     for (const double* arr : {initial_objects, resume_spectra})
         if (arr)
-            for (size_t i = 0; i < 2 * nm * objects; ++i)
+            for (size_t i = 0; i < 2 * nm * j.objects; ++i)
                 if (!std::isfinite(arr[i])) return Status::make(FPM_ERR_INVALID_PARAMETER, "complex values must be finite");
 
     // Crops of every channel source; FrameParam k = source_offset[c] + l.
     std::vector<int> source_offset(CH + 1, 0);
     for (int c = 0; c < CH; ++c) source_offset[c + 1] = source_offset[c] + sm->channel_models[c].sources;
-    std::vector<fpm::FrameParam> params(source_offset[CH]);
+    j.params.assign(source_offset[CH], fpm::FrameParam{});
     std::vector<double> stencil(source_offset[CH]);
     for (int c = 0; c < CH; ++c) {
         const fpm_model_desc& md = sm->channel_models[c];
         for (int l = 0; l < md.sources; ++l) {
-            fpm::FrameParam& fp = params[source_offset[c] + l];
+            fpm::FrameParam& fp = j.params[source_offset[c] + l];
             FPM_TRY(crop_frame_param(md.crop_start_row[l], md.crop_start_col[l], md.offset_row ? md.offset_row[l] : 0.0,
                                      md.offset_col ? md.offset_col[l] : 0.0, N, M, fp));
             fp.weight = 1.f;
@@ -1695,16 +1723,13 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
             stencil[source_offset[c] + l] = (double)(N + fp.has_upper_row) * (double)(N + fp.has_upper_col);
         }
     }
-    // Virtual steps of one pass, in schedule order.
-    std::vector<fpm::SpectralStep> steps;
-    double weight_total = 0.0, bytes_per_pass = 0.0;
-    int max_modes = 1;
+    j.steps.clear();
     for (int idx = 0; idx < E; ++idx) {
         const int e = schedule[idx];
         const double fw = ms->frame_weights ? ms->frame_weights[e] : 1.0;
         if (fw == 0.0) continue;
         const int first = sm->contribution_offsets[e], count = sm->contribution_offsets[e + 1] - first;
-        max_modes = std::max(max_modes, count);
+        j.max_modes = std::max(j.max_modes, count);
         const bool separate = count == 1;
         double gain = sm->exposure_gain[e];
         if (separate)
@@ -1722,7 +1747,7 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
             valid = 0;
             for (size_t i = 0; i < n2; ++i) valid += ms->masks[(size_t)e * n2 + i] != 0;
         }
-        weight_total += fw;
+        j.weight_total += fw;
         for (int phase = 0; phase < 2; ++phase)
             for (int k = 0; k < count; ++k) {
                 const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
@@ -1740,115 +1765,107 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
                 st.inv_weight_sum = (float)(1.0 / wsum);
                 st.first_update = phase == 1 && k == 0 ? 1 : 0;
                 st.loss_scale = fw / (double)valid;
-                steps.push_back(st);
+                j.steps.push_back(st);
                 // Algorithmic HBM bytes: stencil read (evaluation), object
                 // read-modify-write (update), measurement (+ mask) once.
-                bytes_per_pass += phase == 0 ? 8.0 * stencil[st.mode] : 16.0 * stencil[st.mode];
+                j.bytes_per_pass += phase == 0 ? 8.0 * stencil[st.mode] : 16.0 * stencil[st.mode];
             }
-        bytes_per_pass += 4.0 * (double)n2 + (ms->masks ? (double)n2 : 0.0);
+        j.bytes_per_pass += 4.0 * (double)n2 + (ms->masks ? (double)n2 : 0.0);
     }
-    if (!(weight_total > 0.0)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration has no positive frame weight");
-
-    std::vector<double> natural;
-    if (!resume_spectra && !initial_objects) FPM_TRY(spectral_initial_objects(sm, ms, objects, natural));
-    const double* start_objects = initial_objects ? initial_objects : natural.data();
-    std::vector<float2> pupils(n2 * CH);
+    if (!(j.weight_total > 0.0)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration has no positive frame weight");
+    j.resume_spectra = resume_spectra;
+    if (!resume_spectra && !initial_objects) FPM_TRY(spectral_initial_objects(sm, ms, j.objects, j.natural));
+    j.start_objects = initial_objects ? initial_objects : j.natural.data();
+    j.pupils.resize(n2 * CH);
     for (int c = 0; c < CH; ++c)
         for (size_t i = 0; i < n2; ++i)
-            pupils[c * n2 + i] = make_float2((float)sm->channel_models[c].pupil[2 * i],
-                                             (float)sm->channel_models[c].pupil[2 * i + 1]);
+            j.pupils[c * n2 + i] = make_float2((float)sm->channel_models[c].pupil[2 * i],
+                                               (float)sm->channel_models[c].pupil[2 * i + 1]);
+    return Status::ok();
+}
 
-    FPM_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = ctx->streams[0];
-    // The context's staging buffers may still feed an earlier upload.
-    FPM_CUDA(cudaStreamSynchronize(ctx->upload));
-    FPM_CUDA(cudaStreamSynchronize(s));
-    DeviceBuffer meas, masks, d_pupils, d_params, d_steps, object, wide, fields, prediction, partials, status, tiles,
-        object_ptrs, wide_ptrs;
-    for (DeviceBuffer* b : {&meas, &masks, &d_pupils, &d_params, &d_steps, &object, &wide, &fields, &prediction,
-                            &partials, &status, &tiles, &object_ptrs, &wide_ptrs})
+// Device part: resident buffers from the context's pool, measurements in the
+// engine's FP32 layout (raw form: per-exposure gain and background), and the
+// starting state. Uploads share the context's staging buffer, so the jobs of
+// one call queue them on one stream.
+Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_params* a, cudaStream_t s, int& launches) {
+    const int N = j.N, M = j.M, E = j.E, C = fpm::engine_ctas(N);
+    const size_t n2 = (size_t)N * N, nm = (size_t)M * M;
+    for (DeviceBuffer* b : {&j.meas, &j.masks, &j.d_pupils, &j.d_params, &j.d_steps, &j.object, &j.wide, &j.fields,
+                            &j.prediction, &j.partials, &j.status, &j.object_ptrs, &j.wide_ptrs})
         b->bind(ctx->pool, s);
-    cudaEvent_t ev[4] = {};
-    for (auto& e : ev) FPM_CUDA(cudaEventCreate(&e));
-    struct EventGuard {
-        cudaEvent_t* e;
-        ~EventGuard() {
-            for (int i = 0; i < 4; ++i)
-                if (e[i]) cudaEventDestroy(e[i]);
-        }
-    } guard{ev};
-    int launches = 0;
-    FPM_CUDA(cudaEventRecord(ev[0], s));
-    // Measurements in the engine's FP32 layout (raw form: per-exposure gain and background).
     const size_t total = n2 * E;
     FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
-    FPM_TRY(meas.ensure(total * sizeof(float)));
-    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
-    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), meas.as<float>(), E, s));
+    FPM_TRY(j.meas.ensure(total * sizeof(float)));
+    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, j.ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), j.meas.as<float>(), E, s));
     ++launches;
-    if (ms->masks) {
-        FPM_TRY(masks.ensure(total));
+    if (j.ms->masks) {
+        FPM_TRY(j.masks.ensure(total));
         FPM_TRY(ctx->scratch_a.ensure(total));
-        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
-        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), masks.as<uint8_t>(), E, s));
+        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, j.ms->masks, total, cudaMemcpyHostToDevice, s));
+        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), j.masks.as<uint8_t>(), E, s));
         ++launches;
     }
-    FPM_TRY(upload_array(d_pupils, pupils, s));
-    FPM_TRY(upload_array(d_params, params, s));
-    FPM_TRY(upload_array(d_steps, steps, s));
-    FPM_TRY(object.ensure(sizeof(float2) * (size_t)M * ostride * objects));
-    FPM_TRY(wide.ensure(sizeof(double2) * nm * objects));
-    FPM_TRY(fields.ensure(sizeof(float2) * n2 * max_modes));
-    FPM_TRY(prediction.ensure(sizeof(float) * n2));
-    FPM_TRY(partials.ensure(sizeof(double) * (size_t)a->iterations * C));
-    FPM_TRY(status.ensure(sizeof(int)));
-    FPM_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(int), s));
-    FPM_CUDA(cudaMemsetAsync(partials.ptr, 0, sizeof(double) * (size_t)a->iterations * C, s));
-    std::vector<float2*> optr(objects);
-    std::vector<double2*> wptr(objects);
-    for (int o = 0; o < objects; ++o) {
-        optr[o] = object.as<float2>() + (size_t)o * M * ostride;
-        wptr[o] = wide.as<double2>() + (size_t)o * nm;
+    FPM_TRY(upload_array(j.d_pupils, j.pupils, s));
+    FPM_TRY(upload_array(j.d_params, j.params, s));
+    FPM_TRY(upload_array(j.d_steps, j.steps, s));
+    FPM_TRY(j.object.ensure(sizeof(float2) * (size_t)M * j.ostride * j.objects));
+    FPM_TRY(j.wide.ensure(sizeof(double2) * nm * j.objects));
+    FPM_TRY(j.fields.ensure(sizeof(float2) * n2 * j.max_modes));
+    FPM_TRY(j.prediction.ensure(sizeof(float) * n2));
+    FPM_TRY(j.partials.ensure(sizeof(double) * (size_t)a->iterations * C));
+    FPM_TRY(j.status.ensure(sizeof(int)));
+    FPM_CUDA(cudaMemsetAsync(j.status.ptr, 0, sizeof(int), s));
+    FPM_CUDA(cudaMemsetAsync(j.partials.ptr, 0, sizeof(double) * (size_t)a->iterations * C, s));
+    j.optr.resize(j.objects);
+    j.wptr.resize(j.objects);
+    for (int o = 0; o < j.objects; ++o) {
+        j.optr[o] = j.object.as<float2>() + (size_t)o * M * j.ostride;
+        j.wptr[o] = j.wide.as<double2>() + (size_t)o * nm;
     }
-    FPM_TRY(upload_array(object_ptrs, optr, s));
-    FPM_TRY(upload_array(wide_ptrs, wptr, s));
-    if (resume_spectra) {
+    FPM_TRY(upload_array(j.object_ptrs, j.optr, s));
+    FPM_TRY(upload_array(j.wide_ptrs, j.wptr, s));
+    if (j.resume_spectra) {
         // Checkpoint spectra are the widened complex64 state: narrowing restores it exactly.
-        FPM_CUDA(cudaMemcpyAsync(wide.ptr, resume_spectra, sizeof(double2) * nm * objects, cudaMemcpyHostToDevice, s));
-        for (int o = 0; o < objects; ++o) FPM_CUDA(fpm::launch_narrow(wptr[o], M, M, optr[o], ostride, s));
-        launches += objects;
+        FPM_CUDA(cudaMemcpyAsync(j.wide.ptr, j.resume_spectra, sizeof(double2) * nm * j.objects, cudaMemcpyHostToDevice, s));
+        for (int o = 0; o < j.objects; ++o) FPM_CUDA(fpm::launch_narrow(j.wptr[o], M, M, j.optr[o], j.ostride, s));
+        launches += j.objects;
     } else {
         // Forward FFT (FP64) and fftshift of the natural-order objects.
-        FPM_CUDA(cudaMemcpyAsync(wide.ptr, start_objects, sizeof(double2) * nm * objects, cudaMemcpyHostToDevice, s));
-        FPM_TRY(fft2_device(ctx, wide_ptrs.as<double2*>(), objects, M, M, false, s));
-        FPM_CUDA(fpm::launch_shift_to_state(wide_ptrs.as<double2*>(), object_ptrs.as<float2*>(), nullptr, nullptr,
-                                            objects, M, s));
+        FPM_CUDA(cudaMemcpyAsync(j.wide.ptr, j.start_objects, sizeof(double2) * nm * j.objects, cudaMemcpyHostToDevice, s));
+        FPM_TRY(fft2_device(ctx, j.wide_ptrs.as<double2*>(), j.objects, M, M, false, s));
+        FPM_CUDA(fpm::launch_shift_to_state(j.wide_ptrs.as<double2*>(), j.object_ptrs.as<float2*>(), nullptr, nullptr,
+                                            j.objects, M, s));
         launches += 3;
     }
+    return Status::ok();
+}
+
+fpm::TileDesc spectral_tile(const SpectralJob& j) {
     fpm::TileDesc T{};
-    T.object = object.as<float2>();
-    T.pupil = d_pupils.as<float2>();
-    T.support = nullptr;
-    T.meas = meas.as<float>();
-    T.masks = ms->masks ? masks.as<uint8_t>() : nullptr;
-    T.params = d_params.as<fpm::FrameParam>();
-    T.partials = partials.as<double>();
-    T.status = status.as<int>();
-    T.M = M;
-    T.frame_count = E;
+    T.object = j.object.as<float2>();
+    T.pupil = j.d_pupils.as<float2>();
+    T.meas = j.meas.as<float>();
+    T.masks = j.ms->masks ? j.masks.as<uint8_t>() : nullptr;
+    T.params = j.d_params.as<fpm::FrameParam>();
+    T.partials = j.partials.as<double>();
+    T.status = j.status.as<int>();
+    T.M = j.M;
+    T.frame_count = j.E;
     T.max_pupil_power = 1.f;
-    T.amplitude = 0;
-    T.weight_sum = weight_total;
+    T.weight_sum = j.weight_total;
     T.row_lo = 0;
-    T.row_hi = N - 1;
-    T.steps = d_steps.as<fpm::SpectralStep>();
-    T.step_count = (int)steps.size();
-    T.mode_fields = fields.as<float2>();
-    T.prediction = prediction.as<float>();
-    const std::vector<fpm::TileDesc> tile_list{T};
-    FPM_TRY(upload_array(tiles, tile_list, s));
+    T.row_hi = j.N - 1;
+    T.steps = j.d_steps.as<fpm::SpectralStep>();
+    T.step_count = (int)j.steps.size();
+    T.mode_fields = j.fields.as<float2>();
+    T.prediction = j.prediction.as<float>();
+    return T;
+}
+
+fpm::EngineParams spectral_engine_params(const fpm_spectral_params* a, int completed) {
     fpm::EngineParams ep{};
-    ep.tiles = tiles.as<fpm::TileDesc>();
     ep.alg = fpm::kAlgSpectral;
     ep.eps = (float)a->epsilon;
     ep.object_step = (float)a->object_step;
@@ -1856,55 +1873,171 @@ Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const f
     ep.gd_batch = 1;
     ep.it_begin = completed;
     ep.it_end = a->iterations;
-    FPM_CUDA(cudaEventRecord(ev[1], s));
-    if (a->iterations > completed) {
-        FPM_CUDA(fpm::launch_engine(N, ep, 1, s));
-        ++launches;
-    }
-    FPM_CUDA(cudaEventRecord(ev[2], s));
-    // Final objects: ifftshift and inverse FFT (FP64).
-    FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(object_ptrs.ptr),
-                                          wide_ptrs.as<double2*>(), objects, M, s));
-    FPM_TRY(fft2_device(ctx, wide_ptrs.as<double2*>(), objects, M, M, true, s));
+    return ep;
+}
+
+// Final objects (ifftshift, FP64 inverse FFT) and the result downloads on s.
+Status spectral_queue_collect(fpm_context* ctx, SpectralJob& j, const fpm_spectral_params* a, cudaStream_t s,
+                              double* objects_out, double* spectra_out, int& launches) {
+    const int M = j.M, C = fpm::engine_ctas(j.N);
+    const size_t nm = (size_t)M * M;
+    FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(j.object_ptrs.ptr),
+                                          j.wide_ptrs.as<double2*>(), j.objects, M, s));
+    FPM_TRY(fft2_device(ctx, j.wide_ptrs.as<double2*>(), j.objects, M, M, true, s));
     launches += 3;
-    FPM_CUDA(cudaEventRecord(ev[3], s));
     if (objects_out)
-        FPM_CUDA(cudaMemcpyAsync(objects_out, wide.ptr, sizeof(double2) * nm * objects, cudaMemcpyDeviceToHost, s));
+        FPM_CUDA(cudaMemcpyAsync(objects_out, j.wide.ptr, sizeof(double2) * nm * j.objects, cudaMemcpyDeviceToHost, s));
     if (spectra_out) {
-        FPM_CUDA(cudaStreamSynchronize(s));
-        for (int o = 0; o < objects; ++o) FPM_CUDA(fpm::launch_widen(optr[o], ostride, M, M, wptr[o], s));
-        launches += objects;
-        FPM_CUDA(cudaMemcpyAsync(spectra_out, wide.ptr, sizeof(double2) * nm * objects, cudaMemcpyDeviceToHost, s));
+        // The natural objects leave j.wide first (stream order), then the spectra reuse it.
+        for (int o = 0; o < j.objects; ++o) FPM_CUDA(fpm::launch_widen(j.optr[o], j.ostride, M, M, j.wptr[o], s));
+        launches += j.objects;
+        FPM_CUDA(cudaMemcpyAsync(spectra_out, j.wide.ptr, sizeof(double2) * nm * j.objects, cudaMemcpyDeviceToHost, s));
     }
-    std::vector<double> host_partials((size_t)a->iterations * C);
-    int host_status = 0;
-    FPM_CUDA(cudaMemcpyAsync(host_partials.data(), partials.ptr, sizeof(double) * host_partials.size(),
+    j.host_partials.resize((size_t)a->iterations * C);
+    FPM_CUDA(cudaMemcpyAsync(j.host_partials.data(), j.partials.ptr, sizeof(double) * j.host_partials.size(),
                              cudaMemcpyDeviceToHost, s));
-    FPM_CUDA(cudaMemcpyAsync(&host_status, status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    FPM_CUDA(cudaStreamSynchronize(s));
-    FPM_CUDA(cudaGetLastError());
-    for (int it = completed; it < a->iterations; ++it) {
+    FPM_CUDA(cudaMemcpyAsync(&j.host_status, j.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return Status::ok();
+}
+
+// Pass objectives from the per-CTA partials, after the stream is synchronised.
+Status spectral_objectives(const SpectralJob& j, const fpm_spectral_params* a, double* objectives_out) {
+    const int C = fpm::engine_ctas(j.N);
+    for (int it = j.completed; it < a->iterations; ++it) {
         double sum = 0.0;
-        for (int r = 0; r < C; ++r) sum += host_partials[(size_t)it * C + r];
-        const double objective = sum / weight_total;
+        for (int r = 0; r < C; ++r) sum += j.host_partials[(size_t)it * C + r];
+        const double objective = sum / j.weight_total;
         if (!std::isfinite(objective)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration objective is non-finite");
-        if (objectives_out) objectives_out[it - completed] = objective;
+        if (objectives_out) objectives_out[it - j.completed] = objective;
     }
+    return Status::ok();
+}
+
+// Runs jobs on the device: one engine launch per tile size over all its
+// jobs (one cluster each), sizes on separate streams, the largest (longest)
+// tiles first so that they take SMs before the short ones. Statistics from
+// CUDA events on the launching streams.
+Status spectral_execute(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fpm_spectral_params* a,
+                        const std::vector<fpm_spectral_result_desc>& results) {
+    FPM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s0 = ctx->streams[0];
+    // The context's staging buffers may still feed an earlier upload.
+    FPM_CUDA(cudaStreamSynchronize(ctx->upload));
+    for (cudaStream_t st : ctx->streams) FPM_CUDA(cudaStreamSynchronize(st));
+    std::vector<cudaEvent_t> ev;
+    struct EventGuard {
+        std::vector<cudaEvent_t>& e;
+        ~EventGuard() {
+            for (cudaEvent_t x : e) cudaEventDestroy(x);
+        }
+    } guard{ev};
+    auto event = [&](cudaEvent_t& e) -> Status {
+        FPM_CUDA(cudaEventCreate(&e));
+        ev.push_back(e);
+        return Status::ok();
+    };
+    int launches = 0;
+    cudaEvent_t start, uploaded;
+    FPM_TRY(event(start));
+    FPM_TRY(event(uploaded));
+    FPM_CUDA(cudaEventRecord(start, s0));
+    for (SpectralJob& j : jobs) FPM_TRY(spectral_upload(ctx, j, a, s0, launches));
+    FPM_CUDA(cudaEventRecord(uploaded, s0));
+    std::map<int, std::vector<int>, std::greater<int>> by_size;
+    for (size_t i = 0; i < jobs.size(); ++i) by_size[jobs[i].N].push_back((int)i);
+    std::vector<DeviceBuffer> tile_bufs(by_size.size());
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
+    std::vector<cudaEvent_t> ends;
     fpm_run_stats st = {};
-    float run_ms = 0.f, engine_ms = 0.f;
-    FPM_CUDA(cudaEventElapsedTime(&run_ms, ev[0], ev[3]));
-    FPM_CUDA(cudaEventElapsedTime(&engine_ms, ev[1], ev[2]));
+    size_t k = 0;
+    for (auto& [N, idx] : by_size) {
+        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
+        FPM_CUDA(cudaStreamWaitEvent(s, uploaded, 0));
+        std::vector<fpm::TileDesc> tiles;
+        double bytes = 0.0;
+        int completed = jobs[idx[0]].completed;
+        for (int i : idx) {
+            tiles.push_back(spectral_tile(jobs[i]));
+            bytes += jobs[i].bytes_per_pass * (a->iterations - jobs[i].completed);
+            if (jobs[i].completed != completed)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "every resumed problem must have the same completed iterations");
+        }
+        tile_bufs[k].bind(ctx->pool, s);
+        FPM_TRY(upload_array(tile_bufs[k], tiles, s));
+        fpm::EngineParams ep = spectral_engine_params(a, completed);
+        ep.tiles = tile_bufs[k].as<fpm::TileDesc>();
+        cudaEvent_t e0, e1, done;
+        FPM_TRY(event(e0));
+        FPM_TRY(event(e1));
+        FPM_TRY(event(done));
+        FPM_CUDA(cudaEventRecord(e0, s));
+        if (a->iterations > completed) {
+            FPM_CUDA(fpm::launch_engine(N, ep, (int)tiles.size(), s));
+            ++launches;
+            st.engine_launches += 1;
+        }
+        FPM_CUDA(cudaEventRecord(e1, s));
+        engine_events.emplace_back(e0, e1);
+        for (int i : idx)
+            FPM_TRY(spectral_queue_collect(ctx, jobs[i], a, s, results[i].objects, results[i].object_spectra, launches));
+        FPM_CUDA(cudaEventRecord(done, s));
+        ends.push_back(done);
+        if (k < 8) {
+            st.bucket_size[k] = N;
+            st.bucket_tiles[k] = (int32_t)idx.size();
+            st.buckets = (int32_t)k + 1;
+        }
+        st.engine_bytes += bytes;
+        ++k;
+    }
+    for (cudaStream_t s : ctx->streams) FPM_CUDA(cudaStreamSynchronize(s));
+    FPM_CUDA(cudaGetLastError());
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        if (jobs[i].host_status != 0)
+            return Status::make(FPM_ERR_NUMERICAL, "problem %zu: device status %d", i, jobs[i].host_status);
+        FPM_TRY(spectral_objectives(jobs[i], a, results[i].objectives));
+    }
+    double lo = 1e300, hi = -1e300;
+    for (size_t b = 0; b < engine_events.size(); ++b) {
+        float t0 = 0.f, t1 = 0.f, d = 0.f, end = 0.f;
+        FPM_CUDA(cudaEventElapsedTime(&t0, start, engine_events[b].first));
+        FPM_CUDA(cudaEventElapsedTime(&t1, start, engine_events[b].second));
+        FPM_CUDA(cudaEventElapsedTime(&d, engine_events[b].first, engine_events[b].second));
+        // run_ms and the bucket ends count from the inputs being resident
+        // (after the measurement uploads), as for resident problems.
+        FPM_CUDA(cudaEventElapsedTime(&end, uploaded, ends[b]));
+        lo = std::min(lo, (double)t0);
+        hi = std::max(hi, (double)t1);
+        st.engine_ms_sum += d;
+        st.run_ms = std::max(st.run_ms, (double)end);
+        if (b < 8) st.bucket_end_ms[b] = end;
+    }
+    st.engine_span_ms = engine_events.empty() ? 0.0 : hi - lo;
     st.kernel_launches = launches;
-    st.engine_launches = a->iterations > completed ? 1 : 0;
-    st.run_ms = run_ms;
-    st.engine_ms_sum = st.engine_span_ms = engine_ms;
-    st.engine_bytes = bytes_per_pass * (a->iterations - completed);
-    st.buckets = 1;
-    st.bucket_size[0] = N;
-    st.bucket_tiles[0] = 1;
-    st.bucket_end_ms[0] = run_ms;
     ctx->stats = st;
     return Status::ok();
+}
+
+Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
+                    const fpm_spectral_params* a, const int32_t* order, const double* initial_objects,
+                    const double* resume_spectra, int completed, double* objects_out, double* spectra_out,
+                    double* objectives_out) {
+    std::vector<SpectralJob> jobs(1);
+    FPM_TRY(spectral_prepare(jobs[0], sm, ms, a, order, initial_objects, resume_spectra, completed));
+    return spectral_execute(ctx, jobs, a, {fpm_spectral_result_desc{objects_out, spectra_out, objectives_out}});
+}
+
+Status spectral_run_batch(fpm_context* ctx, int count, const fpm_spectral_model_desc* models,
+                          const fpm_measurement_desc* measurements, const fpm_spectral_params* a,
+                          fpm_spectral_result_desc* results) {
+    if (count <= 0 || !models || !measurements || !results)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "a positive problem count and its arrays are required");
+    std::vector<SpectralJob> jobs(count);
+    for (int i = 0; i < count; ++i) {
+        Status st = spectral_prepare(jobs[i], &models[i], &measurements[i], a, nullptr, nullptr, nullptr, 0);
+        if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+    }
+    return spectral_execute(ctx, jobs, a, std::vector<fpm_spectral_result_desc>(results, results + count));
 }
 
 }  // namespace
@@ -2401,6 +2534,14 @@ int32_t fpm_spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* model,
     std::lock_guard<std::mutex> lock(ctx->mu);
     return finish(ctx, spectral_run(ctx, model, measurements, params, order, initial_objects, resume_spectra,
                                     completed_iterations, objects, object_spectra, objectives));
+}
+
+int32_t fpm_spectral_run_batch(fpm_context* ctx, int32_t count, const fpm_spectral_model_desc* models,
+                               const fpm_measurement_desc* measurements, const fpm_spectral_params* params,
+                               fpm_spectral_result_desc* results) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return finish(ctx, spectral_run_batch(ctx, count, models, measurements, params, results));
 }
 
 int32_t fpm_spectral_forward(fpm_context* ctx, const fpm_spectral_model_desc* model, const double* spectra,

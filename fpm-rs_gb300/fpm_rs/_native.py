@@ -24,7 +24,7 @@ EXPORTED = (
     "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
     "fpm_fft2", "fpm_forward_stack", "fpm_simulate_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
-    "fpm_spectral_run", "fpm_spectral_forward",
+    "fpm_spectral_run", "fpm_spectral_run_batch", "fpm_spectral_forward",
 )
 
 
@@ -108,6 +108,11 @@ class SpectralModelDesc(C.Structure):
 class SpectralParams(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("batch_size", C.c_int32), ("loss_type", C.c_int32),
                 ("object_step", C.c_double), ("epsilon", C.c_double)]
+
+
+class SpectralResultDesc(C.Structure):
+    _fields_ = [("objects", C.POINTER(C.c_double)), ("object_spectra", C.POINTER(C.c_double)),
+                ("objectives", C.POINTER(C.c_double))]
 
 
 class ResultDesc(C.Structure):

@@ -558,6 +558,54 @@ class SpectralAlternatingProjection:
         return dict(object_step=float(self.object_step), batch_size=int(self.batch_size), epsilon=float(self.epsilon),
                     loss_type=self.loss_type)
 
+    def run_many(self, *, problems) -> list:
+        """Independent problems in one device call (fpm_spectral_run_batch):
+        one engine launch per tile size, one thread-block cluster per problem,
+        acquisition order and measured-amplitude initialisation. Each result
+        equals the problem's own run()."""
+        problems = list(problems)
+        if not problems:
+            return []
+        params = self._params()
+        keep = []
+        models = (N.SpectralModelDesc * len(problems))()
+        meas = (N.MeasurementDesc * len(problems))()
+        outs = (N.SpectralResultDesc * len(problems))()
+        arrays = []
+        for i, p in enumerate(problems):
+            sd, k = p.model._descriptor()
+            keep.append(k)
+            models[i] = sd
+            m = meas[i]
+            m.frames = p.measurements.frame_count
+            m.measurements = N.ptr(p.measurements._data, C.c_double)
+            m.frame_weights = N.ptr(p.measurements._weights, C.c_double)
+            m.masks = N.ptr(p.measurements._masks, C.c_uint8)
+            shape = (p.model.object_count, *p.model.reconstruction_shape)
+            a = dict(objects=np.zeros(shape, np.complex128), spectra=np.zeros(shape, np.complex128),
+                     objectives=np.zeros(int(self.iterations)))
+            outs[i].objects = N.ptr(a["objects"], C.c_double)
+            outs[i].object_spectra = N.ptr(a["spectra"], C.c_double)
+            outs[i].objectives = N.ptr(a["objectives"], C.c_double)
+            arrays.append(a)
+        ctx = N.context()
+        started = time.perf_counter()
+        N.check(N.library().fpm_spectral_run_batch(ctx.handle, len(problems), models, meas, C.byref(params), outs),
+                ctx.handle)
+        elapsed = time.perf_counter() - started
+        results = []
+        for p, a in zip(problems, arrays):
+            model = p.model
+            index = [0 if model.object_coupling == "shared_complex" else c for c in range(len(model.channel_ids))]
+            results.append(SpectralReconstructionResult(
+                channel_ids=model.channel_ids, wavelengths_vacuum_m=model.wavelengths_vacuum_m,
+                object_coupling=model.object_coupling, _objects=a["objects"][index], _spectra=a["spectra"][index],
+                _pupils=np.stack([m.pupil for m in model.channel_models]),
+                trace=[(it + 1, float(a["objectives"][it]), elapsed) for it in range(int(self.iterations))],
+                completed_iterations=int(self.iterations),
+                runtime=dict(elapsed_seconds=elapsed, algorithm="SpectralAlternatingProjection")))
+        return results
+
     def run(self, *, problem: SpectralReconstructionProblem, initial_objects=None, frame_order=None, seed=None,
             resume=None, checkpoint_directory=None, checkpoint_every=1) -> SpectralReconstructionResult:
         """Runs the passes on the device and returns owned channel records

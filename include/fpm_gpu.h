@@ -26,7 +26,8 @@
  *                                  src/reconstruction/checkpoint.rs:38-146 -> fpm_run_batch_resumable
  *   SpectralRunner::run + SpectralAlternatingProjection
  *                                  src/reconstruction/spectral.rs:494-642,
- *                                  src/algorithms/spectral.rs:182-271 -> fpm_spectral_run
+ *                                  src/algorithms/spectral.rs:182-271 -> fpm_spectral_run,
+ *                                  fpm_spectral_run_batch (many requests, one launch per tile size)
  *   SpectralImagePlaneModel::forward_intensity
  *                                  src/model/spectral.rs:400-446 -> fpm_spectral_forward
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
@@ -344,6 +345,22 @@ int32_t fpm_spectral_run(fpm_context *ctx, const fpm_spectral_model_desc *model,
                          const int32_t *order, const double *initial_objects, const double *resume_spectra,
                          int32_t completed_iterations, double *objects, double *object_spectra,
                          double *objectives);
+
+/* Result buffers of one spectral problem; any pointer may be NULL. */
+typedef struct {
+    double *objects;         /* object_count*mh*mw complex, natural order */
+    double *object_spectra;  /* object_count*mh*mw complex, centred */
+    double *objectives;      /* [iterations] */
+} fpm_spectral_result_desc;
+
+/* fpm_spectral_run for `count` independent problems (acquisition order,
+ * measured-amplitude initialisation) with one engine launch per tile size:
+ * each problem is one thread-block cluster, so a batch of requests fills the
+ * GPU where one request occupies a single cluster. Results equal separate
+ * fpm_spectral_run calls. */
+int32_t fpm_spectral_run_batch(fpm_context *ctx, int32_t count, const fpm_spectral_model_desc *models,
+                               const fpm_measurement_desc *measurements, const fpm_spectral_params *params,
+                               fpm_spectral_result_desc *results);
 
 /* Detector intensities of every exposure, [exposures*h*w], from the stored
  * objects' centred spectra: gain * sum(weight * local intensity) + background. */

@@ -176,3 +176,19 @@ def test_bounded_rgb_multiplexed_recovery(fpm):
     assert result.trace[-1][1] < result.trace[0][1] * 0.01
     for c in range(3):
         assert oracle.complex_nrmse(truth[c], result.object[c]) < 0.03
+
+
+def test_batched_requests_equal_single_runs(fpm):
+    # Mixed tile sizes and couplings in one call: one launch per size.
+    cases = [_case(fpm, 32, mixed=True), _case(fpm, 64, gains=[1.0, 0.8, 1.2]),
+             _case(fpm, 32, mixed=True, shared=True, background=0.2), _case(fpm, 128, mixed=True)]
+    problems = [fpm.SpectralReconstructionProblem(measurements=c[3], model=c[0]) for c in cases]
+    solver = fpm.SpectralAlternatingProjection(iterations=3)
+    batch = solver.run_many(problems=problems)
+    stats = fpm.last_run_stats()
+    assert stats["engine_launches"] == 3
+    assert [b[:2] for b in stats["buckets"]] == [(128, 1), (64, 1), (32, 2)]
+    for problem, got in zip(problems, batch):
+        alone = solver.run(problem=problem)
+        np.testing.assert_array_equal(alone.object_spectrum, got.object_spectrum)
+        np.testing.assert_array_equal([t[1] for t in alone.trace], [t[1] for t in got.trace])
