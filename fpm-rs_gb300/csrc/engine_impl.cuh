@@ -70,7 +70,10 @@ struct Cfg {
     static_assert(R % C == 0 && (R == 32 || R == 16) && (C == 1 || R * C == N), "cluster split");
     static_assert(T1 * THREADS == R * NB && T2 * THREADS == R * NA && TX * THREADS == (R / C) * N, "tasks");
     // Dynamic + static (descriptors, about 256 B) + 1 KB reserved per CTA.
-    static_assert((SMEM_BYTES + 256 + 1024) * MIN_BLOCKS <= 233472, "shared memory");
+    // Dynamic + static (tile and step descriptors, at most those of the
+    // spectral family) + the 1 KB the SM reserves per CTA, times the CTAs per SM.
+    static_assert((SMEM_BYTES + sizeof(TileDesc) + 2 * sizeof(SpectralStep) + 1024) * MIN_BLOCKS <= 233472,
+                  "shared memory");
 };
 
 template <class K>
@@ -151,7 +154,7 @@ FPM_DEVICE float descent_factor(float predicted, float measured, int runtime_los
 // [lower_col - odd, lower_col - odd + N + 2) into shared memory. Every copy
 // starts on an even column (16-byte aligned: the object row stride is even);
 // bytes beyond the grid are zero-filled and never read from global memory.
-template <class K>
+template <class K, bool WAIT = true>
 FPM_DEVICE void stage_object(float2* __restrict__ osm, const float2* __restrict__ object, int M, long long ostride,
                              const FrameParam& fp, int i_lo, int row_lo, int row_hi) {
     const int c0 = fp.lower_col & ~1;
@@ -169,7 +172,7 @@ FPM_DEVICE void stage_object(float2* __restrict__ osm, const float2* __restrict_
         const float2* src = bytes ? object + (long long)gr * ostride + col : object;
         cp_async16(osm + r * K::ORS + 2 * t, src, bytes);
     }
-    cp_async_wait_all();
+    if constexpr (WAIT) cp_async_wait_all();
 }
 
 // P1 + P2: patch * pupil, ifftshift, row inverse FFT into the field slab.
@@ -409,6 +412,27 @@ FPM_DEVICE void load_pupil_slab(float2* __restrict__ pslab, const float2* __rest
     }
 }
 
+// The same rows as 16-byte asynchronous copies; the caller waits
+// (cp.async.wait_all) and synchronises before the slab is read.
+template <class K>
+FPM_DEVICE void load_pupil_slab_async(float2* __restrict__ pslab, const float2* __restrict__ pupil, int c) {
+    constexpr int PAIRS = K::N / 2;
+    for (int e = threadIdx.x; e < K::R * PAIRS; e += K::THREADS) {
+        const int l = e / PAIRS, j2 = e % PAIRS;
+        const int i = K::C == 1 ? l : c * K::R + l;
+        cp_async16(pslab + l * K::N + 2 * j2, pupil + (size_t)i * K::N + 2 * j2, 16);
+    }
+}
+
+// Asynchronous copy of spectral step `step` into a shared descriptor slot
+// (one 16-byte piece per thread of the first warp).
+FPM_DEVICE void prefetch_step(SpectralStep* slot, const SpectralStep* steps, int step) {
+    constexpr int PIECES = (int)(sizeof(SpectralStep) / 16);
+    if (threadIdx.x < PIECES)
+        cp_async16(reinterpret_cast<char*>(slot) + 16 * threadIdx.x,
+                   reinterpret_cast<const char*>(steps + step) + 16 * threadIdx.x, 16);
+}
+
 template <int N_, int ALG, int LOSS>
 __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_kernel(const EngineParams P) {
     using K = Cfg<N_>;
@@ -428,8 +452,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     const int c = C == 1 ? 0 : (int)(blockIdx.x % C);
     // Tile and frame descriptors live in shared memory, not registers.
     __shared__ TileDesc s_tile;
-    __shared__ FrameParam s_frame;
-    __shared__ SpectralStep s_step;
+    // Frame descriptor; spectral AP holds this step's descriptor and the
+    // next one (prefetched) instead. Sized per family so the others keep
+    // their shared-memory budget.
+    __shared__ __align__(16) unsigned char s_desc[ALG == kAlgSpectral ? 2 * sizeof(SpectralStep) : sizeof(FrameParam)];
+    FrameParam& s_frame = *reinterpret_cast<FrameParam*>(s_desc);
+    SpectralStep* const s_steps = reinterpret_cast<SpectralStep*>(s_desc);
     if (tid == 0) s_tile = P.tiles[tile];
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
     __syncthreads();
@@ -451,6 +479,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
     load_pupil_slab<K>(pslab, T.pupil, c);
     int slab_channel = 0;  // spectral: channel whose pupil rows pslab holds
+    int vstep = 0;         // spectral: steps taken in this launch (descriptor slot parity)
+    if constexpr (spectral) {
+        if (T.step_count > 0) prefetch_step(&s_steps[0], T.steps, 0);
+    }
     int counter = P.momentum ? *T.counter : 0;
     double loss_acc = 0.0;
     // Mini-batch gradient descent: frames add into T.gradient and the object
@@ -560,27 +592,35 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     cluster_barrier<K>();  // partials read before the next batch rewrites them
                 }
             }
-            const int f = spectral ? T.steps[step].exposure : T.order ? T.order[idx] : idx;
-            if (tid == 0) {
-                if constexpr (spectral) {
-                    s_step = T.steps[step];
-                    s_frame = T.params[s_step.mode];
-                } else {
-                    s_frame = T.params[f];
-                }
-            }
-            __syncthreads();
-            const FrameParam& fp = s_frame;
-            // Spectral update steps start from the stored mode field: no
-            // staging and no inverse transform.
-            const bool spectral_update = spectral && s_step.update != 0;
-            float2* const obj = spectral ? T.object + (size_t)s_step.object * M * ostride : T.object;
             if constexpr (spectral) {
-                if (s_step.channel != slab_channel) {
+                // This step's descriptor arrived during the previous step; the
+                // slot of the previous step is free again (its readers passed
+                // that step's closing barrier) and takes the next descriptor.
+                cp_async_wait_all();
+                __syncthreads();
+                const int next = step + 1 < steps ? step + 1 : 0;
+                prefetch_step(&s_steps[(vstep + 1) & 1], T.steps, next);
+            } else {
+                const int f0 = T.order ? T.order[idx] : idx;
+                if (tid == 0) s_frame = T.params[f0];
+                __syncthreads();
+            }
+            const SpectralStep& sp = s_steps[vstep & 1];
+            ++vstep;
+            const int f = spectral ? sp.exposure : T.order ? T.order[idx] : idx;
+            const FrameParam& fp = spectral ? sp.frame : s_frame;
+            // Spectral update steps start from the stored mode field: no
+            // inverse transform; the object stencil for P8 and a changed
+            // channel's pupil rows arrive asynchronously behind P4-P6.
+            const bool spectral_update = spectral && sp.update != 0;
+            float2* const obj = spectral ? T.object + (size_t)sp.object * M * ostride : T.object;
+            if constexpr (spectral) {
+                if (sp.channel != slab_channel) {
                     // Previous readers of pslab finished behind the last step's barriers.
-                    load_pupil_slab<K>(pslab, T.pupil + (size_t)s_step.channel * N * N, c);
-                    slab_channel = s_step.channel;
+                    load_pupil_slab_async<K>(pslab, T.pupil + (size_t)sp.channel * N * N, c);
+                    slab_channel = sp.channel;
                 }
+                if (spectral_update) stage_object<K, false>(osm, obj, M, ostride, fp, i_lo, row_lo, row_hi);
             }
             const bool batch_boundary = gradient && !stats && ((idx + 1) % P.gd_batch == 0 || idx + 1 == T.frame_count);
             const bool batch_end = gd_batched && batch_boundary;
@@ -604,7 +644,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // S0
             if (!spectral_update) stage_object<K>(osm, obj, M, ostride, fp, i_lo, row_lo, row_hi);
-            __syncthreads();
+            if (!spectral) __syncthreads();
+            if (spectral && !spectral_update) __syncthreads();
             const float2* ostage = osm + (fp.lower_col & 1);
 
             // P1, P2
@@ -669,7 +710,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // thread owns the same detector pixels in every step, so the
                 // mode fields and the prediction need no synchronisation.
                 float2 v[16];
-                float2* const slot = T.mode_fields + (size_t)s_step.slot * N * N + mbase;
+                float2* const slot = T.mode_fields + (size_t)sp.slot * N * N + mbase;
                 float* const pred = T.prediction + mbase;
                 const int pq = phys<K>(q4);
                 if (!spectral_update) {
@@ -679,8 +720,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
                         __stcg(slot + (size_t)k * mstride, v[k]);
-                        float pk = s_step.mode_weight * cnorm2(v[k]);
-                        if (s_step.slot > 0) pk += __ldcg(pred + (size_t)k * mstride);
+                        float pk = sp.mode_weight * cnorm2(v[k]);
+                        if (sp.slot > 0) pk += __ldcg(pred + (size_t)k * mstride);
                         __stcg(pred + (size_t)k * mstride, pk);
                     }
                     __syncthreads();
@@ -690,8 +731,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // ratio sqrt(target / prediction); masked pixels keep psi and
                 // dark pixels take sqrt(target / weight sum).
                 const size_t off = (size_t)f * N * N + mbase;
-                const float gain = s_step.gain, inv_gain = 1.0f / s_step.gain, bg = s_step.background;
-                const bool first = s_step.first_update != 0;
+                const float gain = sp.gain, inv_gain = 1.0f / sp.gain, bg = sp.background;
+                const bool first = sp.first_update != 0;
                 float frame_loss = 0.f;
 #pragma unroll
                 for (int k = 0; k < 16; ++k) {
@@ -708,11 +749,11 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     if (pk > P.eps)
                         v[k] = cscale(psi, sqrtf(target / pk) - 1.f);
                     else
-                        v[k] = make_float2(sqrtf(target * s_step.inv_weight_sum) - psi.x, -psi.y);
+                        v[k] = make_float2(sqrtf(target * sp.inv_weight_sum) - psi.x, -psi.y);
                 }
                 if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
                 else column_forward_local<K>(fld, pq, c, tw, v);
-                if (first) loss_acc += (double)frame_loss * s_step.loss_scale;
+                if (first) loss_acc += (double)frame_loss * sp.loss_scale;
             } else {
             // P4: column inverse FFT, projection, column forward FFT.
             {
@@ -861,6 +902,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 #pragma unroll
                 for (int jb = 0; jb < NB; ++jb) g[jb] = twiddle_smem<false>(v[jb], tw, ka * jb * K::TW);
             }
+            // Spectral update steps: the pupil rows and object stencil copied
+            // since the step start are needed from P7 on.
+            if (spectral_update) cp_async_wait_all();
             __syncthreads();
 
             // P7: row FFT step A', fftshift, correction U (+ EPRY pupil update).
@@ -949,12 +993,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // Projection: O += w * step * adj(U). Gradient descent: O -= step *
                 // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
                 // (N^2 / valid) * adj(U).
-                const float scale = spectral     ? s_step.update_scale * P.object_step
+                const float scale = spectral     ? sp.update_scale * P.object_step
                                     : projection ? fp.weight * (adaptive ? (float)ada_step : P.object_step)
                                     : gd_batched ? fp.weight * fp.valid_scale
                                                  : -P.object_step * fp.weight * fp.valid_scale;
-                // Spectral updates read the current object: an earlier mode of the
-                // same exposure may have changed it after the evaluation staging.
+                // Spectral updates stage the current object at the step start: an
+                // earlier mode of the same exposure may have changed it.
                 float2* target = gd_batched ? T.gradient : obj;
                 const int rows8 = C == 1 ? N + fp.has_upper_row : R + (c == C - 1 ? fp.has_upper_row : 0);
                 const int cols8 = N + fp.has_upper_col;
@@ -981,7 +1025,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
                         acc = cfma(fp.w11, d1, acc);
-                        const float2 base = j < cols8 ? (gd_batched || spectral ? __ldcg(grow + j) : srow[j]) : z;
+                        const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
                         out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
 #pragma unroll

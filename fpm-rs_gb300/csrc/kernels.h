@@ -31,19 +31,22 @@ struct FrameParam {
 // shared amplitude ratio, forward transform and local-denominator correction
 // into the mode's stored object).
 struct SpectralStep {
-    int mode;             // FrameParam of the mode's crop and bilinear weights
+    FrameParam frame;     // the mode's crop and bilinear weights
     int exposure;         // measurement frame
     int object, channel;  // stored object and channel pupil
     int update;           // 0: evaluate, 1: update
     int slot;             // mode position within the exposure
+    int first_update;     // 1 on the exposure's first update step, which adds its loss
     float mode_weight;    // effective intensity weight of the mode
     float update_scale;   // frame weight * mode weight / exposure weight sum
     float gain;           // effective detector gain of the exposure, > 0
     float background;     // scalar exposure background
     float inv_weight_sum; // 1 / exposure weight sum (fill of dark pixels)
-    int first_update;     // 1 on the exposure's first update step, which adds its loss
+    float pad;
     double loss_scale;    // frame weight / unmasked pixels
 };
+// Steps are copied to shared memory in 16-byte pieces.
+static_assert(sizeof(SpectralStep) % 16 == 0, "SpectralStep must be a whole number of 16-byte chunks");
 
 // One reconstruction tile: device pointers into its resident buffers.
 struct TileDesc {

@@ -1752,7 +1752,8 @@ Status spectral_prepare(SpectralJob& j, const fpm_spectral_model_desc* sm, const
             for (int k = 0; k < count; ++k) {
                 const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
                 fpm::SpectralStep st{};
-                st.mode = source_offset[c] + l;
+                const int mode = source_offset[c] + l;
+                st.frame = j.params[mode];
                 st.exposure = e;
                 st.object = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : c;
                 st.channel = c;
@@ -1768,7 +1769,7 @@ Status spectral_prepare(SpectralJob& j, const fpm_spectral_model_desc* sm, const
                 j.steps.push_back(st);
                 // Algorithmic HBM bytes: stencil read (evaluation), object
                 // read-modify-write (update), measurement (+ mask) once.
-                j.bytes_per_pass += phase == 0 ? 8.0 * stencil[st.mode] : 16.0 * stencil[st.mode];
+                j.bytes_per_pass += phase == 0 ? 8.0 * stencil[mode] : 16.0 * stencil[mode];
             }
         j.bytes_per_pass += 4.0 * (double)n2 + (ms->masks ? (double)n2 : 0.0);
     }
@@ -1808,7 +1809,6 @@ Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_para
         ++launches;
     }
     FPM_TRY(upload_array(j.d_pupils, j.pupils, s));
-    FPM_TRY(upload_array(j.d_params, j.params, s));
     FPM_TRY(upload_array(j.d_steps, j.steps, s));
     FPM_TRY(j.object.ensure(sizeof(float2) * (size_t)M * j.ostride * j.objects));
     FPM_TRY(j.wide.ensure(sizeof(double2) * nm * j.objects));
@@ -1848,7 +1848,7 @@ fpm::TileDesc spectral_tile(const SpectralJob& j) {
     T.pupil = j.d_pupils.as<float2>();
     T.meas = j.meas.as<float>();
     T.masks = j.ms->masks ? j.masks.as<uint8_t>() : nullptr;
-    T.params = j.d_params.as<fpm::FrameParam>();
+    T.params = nullptr;  // each step carries its crop
     T.partials = j.partials.as<double>();
     T.status = j.status.as<int>();
     T.M = j.M;
