@@ -21,6 +21,18 @@ seed 5), each a shared complex object seen through 470/532/630 nm channels
 with fixed per-wavelength pupils, one exposure per LED with all three
 wavelengths lit, Poisson counts at 1e4 photons, SpectralAlternatingProjection
 (50 passes), reconstructed together by fpm_spectral_run_batch.
+
+  python bench.py --workload serving [--requests R]
+
+serves the request stream itself: Poisson arrivals at 200 requests/s (seed
+5), each request N ~ U{64,128,256}, a 9x9 to 15x15 LED grid and an algorithm
+drawn from {AP, mPIE, GD}. AP requests are the spectral form above; mPIE and
+GD requests are three single-wavelength problems (470/532/630 nm), an
+extension, since the reference has no multi-wavelength mPIE or GD. A
+dispatcher batches arrivals over a short window and submits each batch as
+device jobs (fpm_run_batch_submit / fpm_spectral_run_batch_submit) that run
+side by side, within a 150 GB HBM admission budget, and reports latency from
+arrival to results on the host.
 """
 
 from __future__ import annotations
@@ -64,7 +76,7 @@ def parse():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--tiles", type=int, default=1024)
     ap.add_argument("--iterations", type=int, default=None, help="30 (tiles) or 50 (spectral) when omitted")
-    ap.add_argument("--workload", choices=("tiles", "spectral"), default="tiles")
+    ap.add_argument("--workload", choices=("tiles", "spectral", "serving"), default="tiles")
     ap.add_argument("--requests", type=int, default=64, help="spectral requests per step")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
@@ -640,9 +652,189 @@ def run_spectral(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- serving
+
+SERVING_RATE = 200.0
+SERVING_ALGORITHMS = ("ap", "mpie", "gd")
+SERVING_BUDGET_BYTES = 150e9
+SERVING_MAX_JOBS = 64        # jobs in flight; each runs on its own streams
+SERVING_WINDOW_S = 0.005     # dispatch when the oldest waiting request is this old ...
+SERVING_BATCH = 16           # ... or this many requests wait
+
+
+def serving_requests(count: int, seed: int):
+    """(arrival s, N, LED side, algorithm) of a Poisson request stream."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / SERVING_RATE, size=count)
+    arrivals = np.concatenate([[0.0], np.cumsum(gaps[1:])])
+    return [(float(arrivals[i]), int(rng.choice(SPECTRAL_SIZES)), int(rng.choice(SPECTRAL_SIDES)),
+             str(rng.choice(SERVING_ALGORITHMS))) for i in range(count)]
+
+
+def device_poisson(intensity, seed):
+    """Poisson counts at PHOTONS at the peak, drawn on the GPU (test data only)."""
+    import torch
+
+    scale = PHOTONS / float(intensity.max())
+    g = torch.Generator(device="cuda").manual_seed(int(seed))
+    lam = torch.as_tensor(np.maximum(intensity, 0.0) * scale, device="cuda")
+    return torch.poisson(lam, generator=g).cpu().numpy(), scale
+
+
+def build_channel_problems(fpm, n, side, seed):
+    """Three single-wavelength (stack, model) pairs of one mPIE/GD request."""
+    grid, ref = W.led_grid(side)
+    geometry = fpm.PlanarLEDArray(grid, W.PITCH, ref, fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))
+    out = []
+    for c, w in enumerate(SPECTRAL_WAVELENGTHS):
+        model = fpm.compile_model(fpm.Optics(**spectral_optics(w)), fpm.Illumination(geometry), (n, n))
+        truth = W.smooth_random_object(model.reconstruction_shape, seed)
+        counts, scale = device_poisson(fpm.forward_intensities(model, truth), seed + 10 * c + 1)
+        out.append((fpm.MeasurementStack(counts), model._replace(frame_gains=np.full(model.frame_count, scale))))
+    return out
+
+
+def request_bytes(n, side, channels, m):
+    """Device bytes a request holds: FP32 measurements, object state and FP64 scratch per channel."""
+    return channels * (side * side * n * n * 4 + m * m * (8 * 3 + 16))
+
+
+def run_serving(args):
+    dist = Dist()
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    import fpm_rs as fpm
+
+    reqs = serving_requests(args.requests, 5 + 1000 * dist.rank)
+    t0 = time.perf_counter()
+    payload = []
+    for i, (arrival, n, side, algo) in enumerate(reqs):
+        seed = 70_000 + 1000 * dist.rank + i
+        if algo == "ap":
+            problem = build_spectral(fpm, n, side, seed)[0]
+            payload.append(problem)
+        else:
+            payload.append(build_channel_problems(fpm, n, side, seed))
+    setup_s = time.perf_counter() - t0
+    solvers = {"ap": fpm.SpectralAlternatingProjection(), "mpie": fpm.Mpie(), "gd": fpm.GradientDescent()}
+    sizes = []
+    for (arrival, n, side, algo), p in zip(reqs, payload):
+        m = p.reconstruction_shape[0] if algo == "ap" else max(model.reconstruction_shape[0] for _, model in p)
+        sizes.append(request_bytes(n, side, 1 if algo == "ap" else 3, m))
+
+    def submit(kind, idxs):
+        if kind == "ap":
+            return solvers["ap"].submit_many(problems=[payload[i] for i in idxs]), []
+        problems = [fpm.ReconstructionProblem(stack, model) for i in idxs for stack, model in payload[i]]
+        return fpm.submit_batch(solvers[kind], problems), problems
+
+    # Warm-up: one job per algorithm family and tile size (kernel loading,
+    # FFT plans, the memory pool), from the stream's own requests.
+    for kind in SERVING_ALGORITHMS:
+        for n in SPECTRAL_SIZES:
+            first = next((i for i, r in enumerate(reqs) if r[3] == kind and r[1] == n), None)
+            if first is None:
+                continue
+            job, problems = submit(kind, [first])
+            job.wait()
+            for p in problems:
+                p.release()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    waiting, inflight, latency = [], [], {}
+    resident = 0.0
+    nxt = 0
+    jobs_submitted = 0
+    start = time.perf_counter()
+    while len(latency) < len(reqs):
+        now = time.perf_counter() - start
+        while nxt < len(reqs) and reqs[nxt][0] <= now:
+            waiting.append(nxt)
+            nxt += 1
+        progressed = False
+        ready = waiting and (len(waiting) >= SERVING_BATCH or now - reqs[waiting[0]][0] >= SERVING_WINDOW_S or
+                             nxt == len(reqs))
+        if ready and len(inflight) < SERVING_MAX_JOBS:
+            # Admit in arrival order within the HBM budget, one job per algorithm.
+            admitted = []
+            for i in list(waiting):
+                if resident + sizes[i] > SERVING_BUDGET_BYTES and (admitted or inflight):
+                    break
+                admitted.append(i)
+                resident += sizes[i]
+                waiting.remove(i)
+            for kind in SERVING_ALGORITHMS:
+                idxs = [i for i in admitted if reqs[i][3] == kind]
+                if idxs:
+                    job, problems = submit(kind, idxs)
+                    inflight.append((job, idxs, problems))
+                    jobs_submitted += 1
+            progressed = bool(admitted)
+        for entry in list(inflight):
+            job, idxs, problems = entry
+            if job.done():
+                job.wait()
+                done_t = job.finished_at - start
+                for i in idxs:
+                    latency[i] = done_t - reqs[i][0]
+                    resident -= sizes[i]
+                for p in problems:
+                    p.release()
+                inflight.remove(entry)
+                progressed = True
+        if not progressed:
+            time.sleep(0.0002)
+    total_s = time.perf_counter() - start
+    clock_info = clocks.stop()
+    if dist.rank != 0:
+        return
+    lat = sorted(latency.values())
+    served_s = max(latency[i] + reqs[i][0] for i in latency)
+    by_kind = {k: sorted(latency[i] for i in latency if reqs[i][3] == k) for k in SERVING_ALGORITHMS}
+    line = {
+        "metric": "served FPM requests/s and p50/p99 latency (3-wavelength, Poisson arrivals at 200 req/s)",
+        "value": len(reqs) / served_s,
+        "unit": "requests/s",
+        "n_gpus": dist.world,
+        "steps": 1,
+        "warmup": 3,
+        "ms_per_step": served_s * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64",
+        "data": "synthetic (seeded objects, GPU forward model, GPU Poisson counts)",
+        "config": {
+            "workload": (f"{len(reqs)} requests arriving as a Poisson process at {SERVING_RATE:g}/s (seed 5); "
+                         "N~U{64,128,256}, LED grids {9,11,13,15}^2, algorithm~U{AP, mPIE, GD} at reference "
+                         "defaults (AP: spectral, shared object; mPIE/GD: three single-wavelength problems)"),
+            "requests": {k: len(v) for k, v in by_kind.items()},
+            "jobs": jobs_submitted,
+            "dispatch": (f"batch arrivals until the oldest has waited {1e3 * SERVING_WINDOW_S:g} ms or "
+                         f"{SERVING_BATCH} wait, one job per algorithm per batch, at most {SERVING_MAX_JOBS} jobs "
+                         f"in flight, {SERVING_BUDGET_BYTES / 1e9:g} GB HBM admission budget"),
+            "setup_s": round(setup_s, 1),
+        },
+        "latency_ms": {"p50": 1e3 * lat[len(lat) // 2], "p99": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                       "max": 1e3 * lat[-1],
+                       "by_algorithm_p50": {k: 1e3 * v[len(v) // 2] for k, v in by_kind.items() if v},
+                       "definition": "arrival to results on the host (uploads, reconstruction, downloads)"},
+        "offered_s": reqs[-1][0],
+        "served_s": served_s,
+        "wall_s": total_s,
+        "clocks": clock_info,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.workload == "spectral":
+    if args.workload == "serving":
+        if args.impl == "reference":
+            raise SystemExit("the serving workload has no reference arm")
+        run_serving(args)
+    elif args.workload == "spectral":
         if args.impl == "reference":
             raise SystemExit("the spectral workload has no reference arm; its CPU baseline is in the line")
         run_spectral(args)

@@ -185,7 +185,6 @@ struct fpm_context {
     std::string error;
     std::mutex mu;
     std::map<int, std::unique_ptr<FftPlan>> plans;
-    DeviceBuffer staging;  // FP64 upload staging
     DeviceBuffer scratch_a, scratch_b;
     cudaMemPool_t pool = nullptr;  // problem buffers: stream-ordered, memory kept for reuse
     cudaStream_t upload = nullptr, download = nullptr;  // host-input batches: copies beside compute
@@ -218,6 +217,7 @@ struct fpm_problem {
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
         pupil_gradient;
+    fpm_job* busy = nullptr;  // the submitted job that owns the problem until it finishes
 };
 
 namespace {
@@ -447,8 +447,12 @@ Status get_plan(fpm_context* ctx, int n, FftPlan*& out) {
     std::vector<int> f = prime_factors(n);
     FPM_TRY(plan->roots.ensure(roots.size() * sizeof(double)));
     FPM_TRY(plan->factors.ensure(std::max<size_t>(f.size(), 1) * sizeof(int)));
-    FPM_CUDA(cudaMemcpy(plan->roots.ptr, roots.data(), roots.size() * sizeof(double), cudaMemcpyHostToDevice));
-    if (!f.empty()) FPM_CUDA(cudaMemcpy(plan->factors.ptr, f.data(), f.size() * sizeof(int), cudaMemcpyHostToDevice));
+    // Stream-ordered copies: a synchronous copy would also wait for device work in flight.
+    cudaStream_t s = ctx->streams[0];
+    FPM_CUDA(cudaMemcpyAsync(plan->roots.ptr, roots.data(), roots.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (!f.empty())
+        FPM_CUDA(cudaMemcpyAsync(plan->factors.ptr, f.data(), f.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(cudaStreamSynchronize(s));
     plan->nfactors = (int)f.size();
     out = plan.get();
     ctx->plans[n] = std::move(plan);
@@ -663,53 +667,55 @@ Status prepare_problem(fpm_context* ctx, const fpm_model_desc* md, const fpm_mea
 }
 
 // Device part: allocations from the context's pool and uploads on stream s.
-// The context's staging buffers are reused, so the previous upload is waited
-// for first; host vectors copied from live in the problem.
+// FP64 staging comes from the pool too and is freed stream-ordered once
+// permuted, so uploads never wait for one another or for device work in
+// flight; host vectors copied from live in the problem.
 Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md, const fpm_measurement_desc* ms,
                       cudaStream_t s) {
     const int N = p->n, F = p->frames;
     const size_t n2 = (size_t)N * N;
-    FPM_CUDA(cudaStreamSynchronize(s));
     for (DeviceBuffer* b : {&p->meas, &p->masks, &p->background, &p->frame_params, &p->support_d, &p->pupil_ref,
                             &p->pupil_model})
         b->bind(ctx->pool, s);
+    DeviceBuffer staging, mask_staging, gain_staging;
+    for (DeviceBuffer* b : {&staging, &mask_staging, &gain_staging}) b->bind(ctx->pool, s);
     // Measurements: FP64 upload, permuted to the engine's FP32 layout. With no
     // background the engine reads the amplitude form sqrt(max(I / g, 0))
     // (computed in FP64, -1 on masked pixels): one float per pixel, no mask
     // bytes, and no divide or square root in the frame loop.
     const size_t total = n2 * F;
-    FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
+    FPM_TRY(staging.ensure(total * sizeof(double)));
     FPM_TRY(p->meas.ensure(total * sizeof(float)));
-    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(cudaMemcpyAsync(staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
     if (p->amplitude) {
         p->upload_gains.resize(F);
         for (int f = 0; f < F; ++f) p->upload_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
-        FPM_TRY(ctx->scratch_b.ensure(F * sizeof(double)));
-        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, p->upload_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
+        FPM_TRY(gain_staging.ensure(F * sizeof(double)));
+        FPM_CUDA(cudaMemcpyAsync(gain_staging.ptr, p->upload_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
         if (ms->masks) {
-            FPM_TRY(ctx->scratch_a.ensure(total));
-            FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+            FPM_TRY(mask_staging.ensure(total));
+            FPM_CUDA(cudaMemcpyAsync(mask_staging.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
         }
-        FPM_CUDA(fpm::launch_permute_amplitude(N, ctx->staging.as<double>(),
-                                               ms->masks ? ctx->scratch_a.as<uint8_t>() : nullptr,
-                                               ctx->scratch_b.as<double>(), p->meas.as<float>(), F, s));
+        FPM_CUDA(fpm::launch_permute_amplitude(N, staging.as<double>(), ms->masks ? mask_staging.as<uint8_t>() : nullptr,
+                                               gain_staging.as<double>(), p->meas.as<float>(), F, s));
     } else {
-        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->meas.as<float>(), F, s));
+        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, staging.as<double>(), p->meas.as<float>(), F, s));
         if (ms->masks) {
             FPM_TRY(p->masks.ensure(total));
-            FPM_TRY(ctx->scratch_a.ensure(total));
-            FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
-            FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
+            FPM_TRY(mask_staging.ensure(total));
+            FPM_CUDA(cudaMemcpyAsync(mask_staging.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+            FPM_CUDA(fpm::launch_permute_u8(N, mask_staging.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
         }
     }
     if (md->background) {
         const long long bg_frames = p->background_stride ? F : 1;
-        FPM_CUDA(cudaStreamSynchronize(s));
-        FPM_TRY(ctx->staging.ensure((size_t)md->background_len * sizeof(double)));
+        DeviceBuffer bg_staging;
+        bg_staging.bind(ctx->pool, s);
+        FPM_TRY(bg_staging.ensure((size_t)md->background_len * sizeof(double)));
         FPM_TRY(p->background.ensure((size_t)md->background_len * sizeof(float)));
-        FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, md->background, (size_t)md->background_len * sizeof(double),
+        FPM_CUDA(cudaMemcpyAsync(bg_staging.ptr, md->background, (size_t)md->background_len * sizeof(double),
                                  cudaMemcpyHostToDevice, s));
-        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), p->background.as<float>(), bg_frames, s));
+        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, bg_staging.as<double>(), p->background.as<float>(), bg_frames, s));
     }
     FPM_TRY(p->frame_params.ensure(sizeof(fpm::FrameParam) * F));
     FPM_CUDA(cudaMemcpyAsync(p->frame_params.ptr, p->params.data(), sizeof(fpm::FrameParam) * F, cudaMemcpyHostToDevice, s));
@@ -760,15 +766,12 @@ Status create_problems(fpm_context* ctx, int count, const fpm_model_desc* mds, c
         scan_frame(&mds[i], &mss[i], (int)(k - first[i]), scans[k]);
     });
     made.resize(count);
-    size_t staging = 0;
     for (int i = 0; i < count; ++i) {
         Status st = check_scans(&mss[i], scans.data() + first[i]);
         if (!st) st = prepare_problem(ctx, &mds[i], &mss[i], scans.data() + first[i], made[i]);
         if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
-        staging = std::max(staging, (size_t)mds[i].image_height * mds[i].image_width * mss[i].frames * sizeof(double));
     }
     cudaStream_t s = ctx->streams[0];
-    FPM_TRY(ctx->staging.ensure(staging));
     for (int i = 0; i < count; ++i) FPM_TRY(upload_problem(ctx, made[i].get(), &mds[i], &mss[i], s));
     FPM_CUDA(cudaStreamSynchronize(s));
     return Status::ok();
@@ -882,6 +885,12 @@ Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) 
     return Status::ok();
 }
 
+// A problem's per-run buffers: bound to the stream of the run that uses them.
+std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
+    return {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
+            &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient};
+}
+
 struct BucketRun {
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
@@ -918,9 +927,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     for (int t = 0; t < count; ++t) {
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
-        for (DeviceBuffer* buf : {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-                                  &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient})
-            buf->bind(ctx->pool, s);
+        for (DeviceBuffer* buf : run_buffers(p)) buf->bind(ctx->pool, s);
         FPM_TRY(p->object.ensure(sizeof(float2) * (size_t)M * ms));
         FPM_TRY(p->pupil_state.ensure(sizeof(float2) * n2));
         FPM_TRY(p->partials.ensure(sizeof(double) * std::max(iters, 1) * C));
@@ -1253,15 +1260,25 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
 
 // Device statistics of one batch from the events its buckets recorded
 // (synchronises the buckets' streams first).
+Status compute_stats(const std::vector<Bucket>& buckets, const std::vector<std::unique_ptr<BucketRun>>& runs,
+                     fpm_run_stats& out);
+
 Status record_stats(fpm_context* ctx, const std::vector<Bucket>& buckets,
                     const std::vector<std::unique_ptr<BucketRun>>& runs) {
+    for (size_t k = 0; k < buckets.size(); ++k) {
+        FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
+        FPM_CUDA(cudaGetLastError());
+    }
+    return compute_stats(buckets, runs, ctx->stats);
+}
+
+// Statistics from the events of finished buckets.
+Status compute_stats(const std::vector<Bucket>& buckets, const std::vector<std::unique_ptr<BucketRun>>& runs,
+                     fpm_run_stats& out) {
     fpm_run_stats st = {};
     cudaEvent_t first_event = nullptr;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
     for (size_t k = 0; k < buckets.size(); ++k) {
-        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
-        FPM_CUDA(cudaStreamSynchronize(s));
-        FPM_CUDA(cudaGetLastError());
         if (!first_event) first_event = runs[k]->first;
         for (size_t e = 0; e + 1 < runs[k]->events.size(); e += 2)
             engine_events.emplace_back(runs[k]->events[e], runs[k]->events[e + 1]);
@@ -1295,7 +1312,7 @@ Status record_stats(fpm_context* ctx, const std::vector<Bucket>& buckets,
         }
         st.engine_span_ms = hi - lo;
     }
-    ctx->stats = st;
+    out = st;
     return Status::ok();
 }
 
@@ -1338,11 +1355,12 @@ Status validate_resume(int count, fpm_problem* const* problems, const fpm_algori
     return Status::ok();
 }
 
-Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
-                 fpm_result_desc* results, const fpm_state_desc* resume = nullptr, fpm_state_desc* capture = nullptr) {
-    FPM_TRY(validate_params(a));
+// Groups a batch's problems by tile and grid size, largest tiles first so
+// the longest launches start earliest; rejects foreign, repeated and busy
+// problems.
+Status build_buckets(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_state_desc* resume,
+                     std::vector<Bucket>& buckets) {
     if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
-    std::vector<Bucket> buckets;
     std::vector<const fpm_problem*> seen(problems, problems + count);
     std::sort(seen.begin(), seen.end());
     if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
@@ -1351,6 +1369,7 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
     for (int i = 0; i < count; ++i) {
         fpm_problem* p = problems[i];
         if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
+        if (p->busy) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d is in use by a submitted job", i);
         auto it = std::find_if(buckets.begin(), buckets.end(), [&](const Bucket& b) { return b.n == p->n && b.m == p->m; });
         if (it == buckets.end()) {
             buckets.push_back(Bucket{p->n, p->m, {}, {}});
@@ -1360,9 +1379,16 @@ Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, cons
         it->indices.push_back(i);
         if (resume) it->resume.push_back(&resume[i]);
     }
-    FPM_TRY(validate_resume(count, problems, a, resume, capture));
-    // Largest tiles first so the longest launches start earliest.
     std::sort(buckets.begin(), buckets.end(), [](const Bucket& x, const Bucket& y) { return x.n > y.n; });
+    return Status::ok();
+}
+
+Status run_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                 fpm_result_desc* results, const fpm_state_desc* resume = nullptr, fpm_state_desc* capture = nullptr) {
+    FPM_TRY(validate_params(a));
+    std::vector<Bucket> buckets;
+    FPM_TRY(build_buckets(ctx, count, problems, resume, buckets));
+    FPM_TRY(validate_resume(count, problems, a, resume, capture));
     std::vector<std::unique_ptr<BucketRun>> runs;
     for (size_t k = 0; k < buckets.size(); ++k) {
         runs.push_back(std::make_unique<BucketRun>());
@@ -1400,14 +1426,12 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
     if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
     made.clear();
     made.resize(count);
-    size_t staging = 0;
     std::vector<size_t> bytes(count);
     for (int i = 0; i < count; ++i) {
         Status st = validate_model(&mds[i]);
         if (!st) st = check_measurement_header(&mds[i], &mss[i]);
         if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
         bytes[i] = (size_t)mds[i].image_height * mds[i].image_width * mss[i].frames * sizeof(double);
-        staging = std::max(staging, bytes[i]);
     }
     // Buckets by (n, m), largest tiles first, then chunks.
     std::vector<std::pair<std::pair<int, int>, std::vector<int>>> groups;
@@ -1434,7 +1458,6 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
             acc += bytes[i];
         }
     }
-    FPM_TRY(ctx->staging.ensure(staging));
     std::vector<std::unique_ptr<BucketRun>> runs;
     for (size_t k = 0; k < chunks.size(); ++k) {
         Bucket& ch = chunks[k];
@@ -1787,8 +1810,7 @@ Status spectral_prepare(SpectralJob& j, const fpm_spectral_model_desc* sm, const
 
 // Device part: resident buffers from the context's pool, measurements in the
 // engine's FP32 layout (raw form: per-exposure gain and background), and the
-// starting state. Uploads share the context's staging buffer, so the jobs of
-// one call queue them on one stream.
+// starting state, queued on stream s.
 Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_params* a, cudaStream_t s, int& launches) {
     const int N = j.N, M = j.M, E = j.E, C = fpm::engine_ctas(N);
     const size_t n2 = (size_t)N * N, nm = (size_t)M * M;
@@ -1796,16 +1818,21 @@ Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_para
                             &j.prediction, &j.partials, &j.status, &j.object_ptrs, &j.wide_ptrs})
         b->bind(ctx->pool, s);
     const size_t total = n2 * E;
-    FPM_TRY(ctx->staging.ensure(total * sizeof(double)));
+    // Staging from the pool, freed (stream-ordered) once permuted: jobs in
+    // flight never share it.
+    DeviceBuffer staging, mask_staging;
+    staging.bind(ctx->pool, s);
+    mask_staging.bind(ctx->pool, s);
+    FPM_TRY(staging.ensure(total * sizeof(double)));
     FPM_TRY(j.meas.ensure(total * sizeof(float)));
-    FPM_CUDA(cudaMemcpyAsync(ctx->staging.ptr, j.ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
-    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, ctx->staging.as<double>(), j.meas.as<float>(), E, s));
+    FPM_CUDA(cudaMemcpyAsync(staging.ptr, j.ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_CUDA(fpm::launch_permute_f64_to_f32(N, staging.as<double>(), j.meas.as<float>(), E, s));
     ++launches;
     if (j.ms->masks) {
         FPM_TRY(j.masks.ensure(total));
-        FPM_TRY(ctx->scratch_a.ensure(total));
-        FPM_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, j.ms->masks, total, cudaMemcpyHostToDevice, s));
-        FPM_CUDA(fpm::launch_permute_u8(N, ctx->scratch_a.as<uint8_t>(), j.masks.as<uint8_t>(), E, s));
+        FPM_TRY(mask_staging.ensure(total));
+        FPM_CUDA(cudaMemcpyAsync(mask_staging.ptr, j.ms->masks, total, cudaMemcpyHostToDevice, s));
+        FPM_CUDA(fpm::launch_permute_u8(N, mask_staging.as<uint8_t>(), j.masks.as<uint8_t>(), E, s));
         ++launches;
     }
     FPM_TRY(upload_array(j.d_pupils, j.pupils, s));
@@ -1913,46 +1940,48 @@ Status spectral_objectives(const SpectralJob& j, const fpm_spectral_params* a, d
     return Status::ok();
 }
 
-// Runs jobs on the device: one engine launch per tile size over all its
-// jobs (one cluster each), sizes on separate streams, the largest (longest)
-// tiles first so that they take SMs before the short ones. Statistics from
-// CUDA events on the launching streams.
-Status spectral_execute(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fpm_spectral_params* a,
-                        const std::vector<fpm_spectral_result_desc>& results) {
-    FPM_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s0 = ctx->streams[0];
-    // The context's staging buffers may still feed an earlier upload.
-    FPM_CUDA(cudaStreamSynchronize(ctx->upload));
-    for (cudaStream_t st : ctx->streams) FPM_CUDA(cudaStreamSynchronize(st));
+// Device timeline of a spectral batch: its events and launch buffers,
+// kept until the work has finished.
+struct SpectralBatch {
     std::vector<cudaEvent_t> ev;
-    struct EventGuard {
-        std::vector<cudaEvent_t>& e;
-        ~EventGuard() {
-            for (cudaEvent_t x : e) cudaEventDestroy(x);
-        }
-    } guard{ev};
-    auto event = [&](cudaEvent_t& e) -> Status {
+    cudaEvent_t start = nullptr, uploaded = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
+    std::vector<cudaEvent_t> ends;
+    std::vector<std::unique_ptr<DeviceBuffer>> tile_bufs;
+    std::vector<int> groups;  // job indices in launch order, per tile size
+    fpm_run_stats st{};
+    int launches = 0;
+    ~SpectralBatch() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+    Status event(cudaEvent_t& e) {
         FPM_CUDA(cudaEventCreate(&e));
         ev.push_back(e);
         return Status::ok();
-    };
-    int launches = 0;
-    cudaEvent_t start, uploaded;
-    FPM_TRY(event(start));
-    FPM_TRY(event(uploaded));
-    FPM_CUDA(cudaEventRecord(start, s0));
-    for (SpectralJob& j : jobs) FPM_TRY(spectral_upload(ctx, j, a, s0, launches));
-    FPM_CUDA(cudaEventRecord(uploaded, s0));
+    }
+};
+
+// Queues jobs on the device: uploads on streams[0], then one engine launch
+// per tile size over all its jobs (one cluster each), the largest (longest)
+// tiles first so that they take SMs before the short ones, sizes on
+// separate streams. With `collect` the finalisation and result downloads
+// follow on the same streams.
+Status spectral_queue(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fpm_spectral_params* a,
+                      const std::vector<fpm_spectral_result_desc>& results, const std::vector<cudaStream_t>& streams,
+                      bool collect, SpectralBatch& b) {
+    FPM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s0 = streams[0];
+    FPM_TRY(b.event(b.start));
+    FPM_TRY(b.event(b.uploaded));
+    FPM_CUDA(cudaEventRecord(b.start, s0));
+    for (SpectralJob& j : jobs) FPM_TRY(spectral_upload(ctx, j, a, s0, b.launches));
+    FPM_CUDA(cudaEventRecord(b.uploaded, s0));
     std::map<int, std::vector<int>, std::greater<int>> by_size;
     for (size_t i = 0; i < jobs.size(); ++i) by_size[jobs[i].N].push_back((int)i);
-    std::vector<DeviceBuffer> tile_bufs(by_size.size());
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> engine_events;
-    std::vector<cudaEvent_t> ends;
-    fpm_run_stats st = {};
     size_t k = 0;
     for (auto& [N, idx] : by_size) {
-        cudaStream_t s = ctx->streams[k % fpm_context::kStreams];
-        FPM_CUDA(cudaStreamWaitEvent(s, uploaded, 0));
+        cudaStream_t s = streams[k % streams.size()];
+        FPM_CUDA(cudaStreamWaitEvent(s, b.uploaded, 0));
         std::vector<fpm::TileDesc> tiles;
         double bytes = 0.0;
         int completed = jobs[idx[0]].completed;
@@ -1962,60 +1991,81 @@ Status spectral_execute(fpm_context* ctx, std::vector<SpectralJob>& jobs, const 
             if (jobs[i].completed != completed)
                 return Status::make(FPM_ERR_INVALID_PARAMETER, "every resumed problem must have the same completed iterations");
         }
-        tile_bufs[k].bind(ctx->pool, s);
-        FPM_TRY(upload_array(tile_bufs[k], tiles, s));
+        b.tile_bufs.push_back(std::make_unique<DeviceBuffer>());
+        b.tile_bufs.back()->bind(ctx->pool, s);
+        FPM_TRY(upload_array(*b.tile_bufs.back(), tiles, s));
         fpm::EngineParams ep = spectral_engine_params(a, completed);
-        ep.tiles = tile_bufs[k].as<fpm::TileDesc>();
+        ep.tiles = b.tile_bufs.back()->as<fpm::TileDesc>();
         cudaEvent_t e0, e1, done;
-        FPM_TRY(event(e0));
-        FPM_TRY(event(e1));
-        FPM_TRY(event(done));
+        FPM_TRY(b.event(e0));
+        FPM_TRY(b.event(e1));
+        FPM_TRY(b.event(done));
         FPM_CUDA(cudaEventRecord(e0, s));
         if (a->iterations > completed) {
             FPM_CUDA(fpm::launch_engine(N, ep, (int)tiles.size(), s));
-            ++launches;
-            st.engine_launches += 1;
+            ++b.launches;
+            b.st.engine_launches += 1;
         }
         FPM_CUDA(cudaEventRecord(e1, s));
-        engine_events.emplace_back(e0, e1);
-        for (int i : idx)
-            FPM_TRY(spectral_queue_collect(ctx, jobs[i], a, s, results[i].objects, results[i].object_spectra, launches));
+        b.engine_events.emplace_back(e0, e1);
+        if (collect)
+            for (int i : idx)
+                FPM_TRY(spectral_queue_collect(ctx, jobs[i], a, s, results[i].objects, results[i].object_spectra,
+                                               b.launches));
         FPM_CUDA(cudaEventRecord(done, s));
-        ends.push_back(done);
+        b.ends.push_back(done);
         if (k < 8) {
-            st.bucket_size[k] = N;
-            st.bucket_tiles[k] = (int32_t)idx.size();
-            st.buckets = (int32_t)k + 1;
+            b.st.bucket_size[k] = N;
+            b.st.bucket_tiles[k] = (int32_t)idx.size();
+            b.st.buckets = (int32_t)k + 1;
         }
-        st.engine_bytes += bytes;
+        b.st.engine_bytes += bytes;
+        b.groups.insert(b.groups.end(), idx.begin(), idx.end());
         ++k;
     }
-    for (cudaStream_t s : ctx->streams) FPM_CUDA(cudaStreamSynchronize(s));
-    FPM_CUDA(cudaGetLastError());
+    return Status::ok();
+}
+
+// After the queued work (and the result copies) have finished: status
+// words, pass objectives and statistics from the recorded events.
+Status spectral_finish(std::vector<SpectralJob>& jobs, const fpm_spectral_params* a,
+                       const std::vector<fpm_spectral_result_desc>& results, SpectralBatch& b, fpm_run_stats& out) {
     for (size_t i = 0; i < jobs.size(); ++i) {
         if (jobs[i].host_status != 0)
             return Status::make(FPM_ERR_NUMERICAL, "problem %zu: device status %d", i, jobs[i].host_status);
         FPM_TRY(spectral_objectives(jobs[i], a, results[i].objectives));
     }
+    fpm_run_stats st = b.st;
     double lo = 1e300, hi = -1e300;
-    for (size_t b = 0; b < engine_events.size(); ++b) {
+    for (size_t g = 0; g < b.engine_events.size(); ++g) {
         float t0 = 0.f, t1 = 0.f, d = 0.f, end = 0.f;
-        FPM_CUDA(cudaEventElapsedTime(&t0, start, engine_events[b].first));
-        FPM_CUDA(cudaEventElapsedTime(&t1, start, engine_events[b].second));
-        FPM_CUDA(cudaEventElapsedTime(&d, engine_events[b].first, engine_events[b].second));
-        // run_ms and the bucket ends count from the inputs being resident
+        FPM_CUDA(cudaEventElapsedTime(&t0, b.start, b.engine_events[g].first));
+        FPM_CUDA(cudaEventElapsedTime(&t1, b.start, b.engine_events[g].second));
+        FPM_CUDA(cudaEventElapsedTime(&d, b.engine_events[g].first, b.engine_events[g].second));
+        // run_ms and the group ends count from the inputs being resident
         // (after the measurement uploads), as for resident problems.
-        FPM_CUDA(cudaEventElapsedTime(&end, uploaded, ends[b]));
+        FPM_CUDA(cudaEventElapsedTime(&end, b.uploaded, b.ends[g]));
         lo = std::min(lo, (double)t0);
         hi = std::max(hi, (double)t1);
         st.engine_ms_sum += d;
         st.run_ms = std::max(st.run_ms, (double)end);
-        if (b < 8) st.bucket_end_ms[b] = end;
+        if (g < 8) st.bucket_end_ms[g] = end;
     }
-    st.engine_span_ms = engine_events.empty() ? 0.0 : hi - lo;
-    st.kernel_launches = launches;
-    ctx->stats = st;
+    st.engine_span_ms = b.engine_events.empty() ? 0.0 : hi - lo;
+    st.kernel_launches = b.launches;
+    out = st;
     return Status::ok();
+}
+
+Status spectral_execute(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fpm_spectral_params* a,
+                        const std::vector<fpm_spectral_result_desc>& results) {
+    FPM_CUDA(cudaSetDevice(ctx->device));
+    const std::vector<cudaStream_t> streams(ctx->streams, ctx->streams + fpm_context::kStreams);
+    SpectralBatch b;
+    FPM_TRY(spectral_queue(ctx, jobs, a, results, streams, true, b));
+    for (cudaStream_t s : streams) FPM_CUDA(cudaStreamSynchronize(s));
+    FPM_CUDA(cudaGetLastError());
+    return spectral_finish(jobs, a, results, b, ctx->stats);
 }
 
 Status spectral_run(fpm_context* ctx, const fpm_spectral_model_desc* sm, const fpm_measurement_desc* ms,
@@ -2040,6 +2090,164 @@ Status spectral_run_batch(fpm_context* ctx, int count, const fpm_spectral_model_
     return spectral_execute(ctx, jobs, a, std::vector<fpm_spectral_result_desc>(results, results + count));
 }
 
+}  // namespace
+
+// A submitted batch: its buckets, device events and result destinations,
+// completed by fpm_job_poll / fpm_job_wait.
+struct fpm_job {
+    fpm_context* ctx = nullptr;
+    fpm_algorithm_params params{};
+    fpm_result_desc* results = nullptr;
+    std::vector<Bucket> buckets;
+    std::vector<std::unique_ptr<BucketRun>> runs;
+    // Spectral AP jobs instead of resident problems.
+    bool spectral = false;
+    fpm_spectral_params spectral_params{};
+    std::vector<SpectralJob> spectral_jobs;
+    std::vector<fpm_spectral_result_desc> spectral_results;
+    std::unique_ptr<SpectralBatch> spectral_batch;
+    std::vector<cudaStream_t> streams;
+    cudaEvent_t done = nullptr;
+    std::mutex mu;
+    bool finished = false;
+    Status status;
+    fpm_run_stats stats{};
+    ~fpm_job() {
+        if (done) cudaEventSynchronize(done);
+        for (cudaStream_t s : streams) cudaStreamSynchronize(s);
+        // Buffers free on the job's streams before those are destroyed.
+        runs.clear();
+        spectral_batch.reset();
+        spectral_jobs.clear();
+        for (cudaStream_t s : streams) cudaStreamDestroy(s);
+        if (done) cudaEventDestroy(done);
+    }
+};
+
+namespace {
+
+Status job_done_event(fpm_job* job);
+Status create_job_streams(fpm_job* job, size_t count);
+
+// fpm_run_batch without the wait: the buckets run on the job's own streams
+// (jobs of one context overlap) and the results are copied as they finish.
+Status submit_batch(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                    fpm_result_desc* results, std::unique_ptr<fpm_job>& out) {
+    FPM_TRY(validate_params(a));
+    auto job = std::make_unique<fpm_job>();
+    job->ctx = ctx;
+    job->params = *a;
+    job->results = results;
+    FPM_TRY(build_buckets(ctx, count, problems, nullptr, job->buckets));
+    FPM_TRY(create_job_streams(job.get(), job->buckets.size()));
+    const size_t nstreams = job->streams.size();
+    for (size_t k = 0; k < job->buckets.size(); ++k) {
+        cudaStream_t s = job->streams[k % nstreams];
+        job->runs.push_back(std::make_unique<BucketRun>());
+        FPM_TRY(run_bucket(ctx, job->buckets[k], &job->params, s, *job->runs.back()));
+    }
+    FPM_TRY(job_done_event(job.get()));
+    for (auto& b : job->buckets)
+        for (fpm_problem* p : b.problems) p->busy = job.get();
+    out = std::move(job);
+    return Status::ok();
+}
+
+// Records the job's completion event behind every one of its streams.
+Status job_done_event(fpm_job* job) {
+    const size_t nstreams = job->streams.size();
+    for (size_t k = 1; k < nstreams; ++k) {
+        cudaEvent_t e;
+        FPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        const cudaError_t r1 = cudaEventRecord(e, job->streams[k]);
+        const cudaError_t r2 = r1 == cudaSuccess ? cudaStreamWaitEvent(job->streams[0], e, 0) : r1;
+        cudaEventDestroy(e);
+        FPM_CUDA(r2);
+    }
+    FPM_CUDA(cudaEventCreateWithFlags(&job->done, cudaEventDisableTiming));
+    FPM_CUDA(cudaEventRecord(job->done, job->streams[0]));
+    return Status::ok();
+}
+
+Status create_job_streams(fpm_job* job, size_t count) {
+    FPM_CUDA(cudaSetDevice(job->ctx->device));
+    for (size_t k = 0; k < std::max<size_t>(1, std::min<size_t>(count, fpm_context::kStreams)); ++k) {
+        cudaStream_t s;
+        FPM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        job->streams.push_back(s);
+    }
+    return Status::ok();
+}
+
+// fpm_spectral_run_batch without the wait.
+Status submit_spectral(fpm_context* ctx, int count, const fpm_spectral_model_desc* models,
+                       const fpm_measurement_desc* measurements, const fpm_spectral_params* a,
+                       fpm_spectral_result_desc* results, std::unique_ptr<fpm_job>& out) {
+    if (count <= 0 || !models || !measurements || !results || !a)
+        return Status::make(FPM_ERR_INVALID_PARAMETER, "a positive problem count and its arrays are required");
+    auto job = std::make_unique<fpm_job>();
+    job->ctx = ctx;
+    job->spectral = true;
+    job->spectral_params = *a;
+    job->spectral_jobs = std::vector<SpectralJob>(count);
+    job->spectral_results.assign(results, results + count);
+    for (int i = 0; i < count; ++i) {
+        Status st = spectral_prepare(job->spectral_jobs[i], &models[i], &measurements[i], &job->spectral_params,
+                                     nullptr, nullptr, nullptr, 0);
+        if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+    }
+    std::map<int, int> sizes;
+    for (auto& j : job->spectral_jobs) sizes[j.N] = 1;
+    FPM_TRY(create_job_streams(job.get(), sizes.size()));
+    job->spectral_batch = std::make_unique<SpectralBatch>();
+    FPM_TRY(spectral_queue(ctx, job->spectral_jobs, &job->spectral_params, job->spectral_results, job->streams, false,
+                           *job->spectral_batch));
+    FPM_TRY(job_done_event(job.get()));
+    out = std::move(job);
+    return Status::ok();
+}
+
+// Runs once, after the job's completion event: status words, objectives
+// and statistics; the problems' buffers return to a context stream and the
+// problems become usable again.
+// Result downloads go to pageable caller memory, which makes a copy wait
+// for its stream; they are therefore queued here, after the device work,
+// and waited for at once.
+Status collect_job(fpm_job* j) {
+    cudaStream_t s = j->streams[0];
+    if (j->spectral) {
+        for (size_t i = 0; i < j->spectral_jobs.size(); ++i)
+            FPM_TRY(spectral_queue_collect(j->ctx, j->spectral_jobs[i], &j->spectral_params, s,
+                                           j->spectral_results[i].objects, j->spectral_results[i].object_spectra,
+                                           j->spectral_batch->launches));
+    } else {
+        for (auto& b : j->buckets)
+            for (size_t t = 0; t < b.problems.size(); ++t)
+                FPM_TRY(queue_collect(b.problems[t], &j->params, j->results ? &j->results[b.indices[t]] : nullptr, s));
+    }
+    FPM_CUDA(cudaStreamSynchronize(s));
+    FPM_CUDA(cudaGetLastError());
+    if (j->spectral)
+        return spectral_finish(j->spectral_jobs, &j->spectral_params, j->spectral_results, *j->spectral_batch, j->stats);
+    for (auto& b : j->buckets)
+        for (size_t t = 0; t < b.problems.size(); ++t) {
+            Status s2 = finish_collect(b.problems[t], &j->params, j->results ? &j->results[b.indices[t]] : nullptr);
+            if (s2) return Status::make(s2.code, "problem %d: %s", b.indices[t], s2.message.c_str());
+        }
+    return compute_stats(j->buckets, j->runs, j->stats);
+}
+
+void finish_job(fpm_job* j) {
+    std::lock_guard<std::mutex> lock(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    j->status = collect_job(j);
+    for (auto& b : j->buckets)
+        for (fpm_problem* p : b.problems) {
+            for (DeviceBuffer* buf : run_buffers(p)) buf->bind(j->ctx->pool, j->ctx->streams[0]);
+            p->busy = nullptr;
+        }
+    j->finished = true;
+}
 }  // namespace
 
 namespace fpm {
@@ -2478,6 +2686,8 @@ int32_t fpm_problem_destroy(fpm_problem* problem) {
     if (!problem) return FPM_OK;
     fpm_context* ctx = problem->ctx;
     std::lock_guard<std::mutex> lock(ctx->mu);
+    if (problem->busy)
+        return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "the problem is in use by a submitted job"));
     cudaSetDevice(ctx->device);
     delete problem;
     return FPM_OK;
@@ -2593,6 +2803,83 @@ int32_t fpm_spectral_forward(fpm_context* ctx, const fpm_spectral_model_desc* mo
         return Status::ok();
     };
     return finish(ctx, body());
+}
+
+int32_t fpm_run_batch_submit(fpm_context* ctx, int32_t count, fpm_problem* const* problems,
+                             const fpm_algorithm_params* params, fpm_result_desc* results, fpm_job** job) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    if (!job) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "job is null"));
+    *job = nullptr;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    std::unique_ptr<fpm_job> made;
+    Status st = submit_batch(ctx, count, problems, params, results, made);
+    if (!st) *job = made.release();
+    return finish(ctx, st);
+}
+
+int32_t fpm_spectral_run_batch_submit(fpm_context* ctx, int32_t count, const fpm_spectral_model_desc* models,
+                                      const fpm_measurement_desc* measurements, const fpm_spectral_params* params,
+                                      fpm_spectral_result_desc* results, fpm_job** job) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    if (!job) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "job is null"));
+    *job = nullptr;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    std::unique_ptr<fpm_job> made;
+    Status st = submit_spectral(ctx, count, models, measurements, params, results, made);
+    if (!st) *job = made.release();
+    return finish(ctx, st);
+}
+
+int32_t fpm_job_poll(fpm_job* job, int32_t* done) {
+    if (!job || !done) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(job->mu);
+    if (!job->finished) {
+        const cudaError_t q = cudaEventQuery(job->done);
+        if (q == cudaErrorNotReady) {
+            *done = 0;
+            return FPM_OK;
+        }
+        if (q != cudaSuccess) {
+            job->status = Status::make(FPM_ERR_CUDA, "CUDA error %s (%s)", cudaGetErrorName(q), cudaGetErrorString(q));
+            job->finished = true;
+        } else {
+            finish_job(job);
+        }
+    }
+    *done = 1;
+    return job->status ? finish(job->ctx, job->status) : FPM_OK;
+}
+
+int32_t fpm_job_wait(fpm_job* job) {
+    if (!job) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "job is null"));
+    {
+        std::lock_guard<std::mutex> lock(job->mu);
+        if (!job->finished) {
+            const cudaError_t e = cudaEventSynchronize(job->done);
+            if (e != cudaSuccess) {
+                job->status = Status::make(FPM_ERR_CUDA, "CUDA error %s (%s)", cudaGetErrorName(e), cudaGetErrorString(e));
+                job->finished = true;
+            } else {
+                finish_job(job);
+            }
+        }
+    }
+    return job->status ? finish(job->ctx, job->status) : FPM_OK;
+}
+
+int32_t fpm_job_stats(fpm_job* job, fpm_run_stats* stats) {
+    if (!job || !stats) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(job->mu);
+    if (!job->finished) return finish(job->ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "the job has not finished"));
+    *stats = job->stats;
+    return FPM_OK;
+}
+
+int32_t fpm_job_destroy(fpm_job* job) {
+    if (!job) return FPM_OK;
+    fpm_job_wait(job);
+    delete job;
+    return FPM_OK;
 }
 
 int32_t fpm_last_run_stats(const fpm_context* ctx, fpm_run_stats* stats) {

@@ -22,12 +22,12 @@ from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
 from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjection, Epry, Fpie, GradientDescent, Mpie,
                              ReconstructionProblem,
-                             ReconstructionResult, RuntimeInfo, last_run_stats, run_batch)
+                             ReconstructionResult, RuntimeInfo, Job, last_run_stats, run_batch, submit_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
 from .spectral import (SpectralAcquisitionPlan, SpectralAlternatingProjection, SpectralChannel, SpectralFrame,
                        SpectralGeometry, SpectralImagePlaneModel, SpectralMixingDiagnostics,
-                       SpectralReconstructionCheckpoint, SpectralReconstructionProblem, SpectralReconstructionResult,
-                       compile_spectral_model)
+                       SpectralJob, SpectralReconstructionCheckpoint, SpectralReconstructionProblem,
+                       SpectralReconstructionResult, compile_spectral_model)
 
 
 def fft2(values, *, inverse: bool = False):
@@ -56,5 +56,5 @@ __all__ = [
     "ReconstructionCheckpoint", "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo",
     "SimulationResult",
     "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
-    "run_batch", "simulate", "suggest_reconstruction_shape",
+    "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob",
 ]

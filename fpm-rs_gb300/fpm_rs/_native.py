@@ -25,6 +25,7 @@ EXPORTED = (
     "fpm_fft2", "fpm_forward_stack", "fpm_simulate_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
     "fpm_spectral_run", "fpm_spectral_run_batch", "fpm_spectral_forward",
+    "fpm_run_batch_submit", "fpm_spectral_run_batch_submit", "fpm_job_poll", "fpm_job_wait", "fpm_job_stats", "fpm_job_destroy",
 )
 
 

@@ -98,9 +98,9 @@ class ReconstructionProblem:
         return self._handle
 
     def release(self) -> None:
-        """Frees the problem's device buffers."""
+        """Frees the problem's device buffers (refused while a submitted job uses them)."""
         if self._handle is not None:
-            N.library().fpm_problem_destroy(self._handle)
+            N.check(N.library().fpm_problem_destroy(self._handle), N.context().handle)
             self._handle = None
 
     def __del__(self):
@@ -419,6 +419,104 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
             result.metadata["problem_name"] = p.name
         out.append(result)
     return out
+
+
+class Job:
+    """A batch queued on the device by submit_batch; its problems stay
+    reserved until the job has finished (fpm_run_batch_submit, fpm_job_poll,
+    fpm_job_wait)."""
+
+    def __init__(self, handle, algorithm, problems, params, arrays, results, submitted):
+        self._handle = handle
+        self._algorithm = algorithm
+        self._problems = problems
+        self._params = params
+        self._arrays = arrays
+        self._results = results  # the result descriptors the device writes through
+        self._submitted = submitted
+        self._finished_at = None
+        self._out = None
+
+    def done(self) -> bool:
+        """True once the device work and the result copies have finished."""
+        if self._out is not None:
+            return True
+        flag = C.c_int32(0)
+        N.check(N.library().fpm_job_poll(self._handle, C.byref(flag)), N.context().handle)
+        if flag.value:
+            self._collect()
+        return bool(flag.value)
+
+    def wait(self) -> list:
+        """Blocks until the job has finished and returns one ReconstructionResult per problem."""
+        if self._out is None:
+            N.check(N.library().fpm_job_wait(self._handle), N.context().handle)
+            self._collect()
+        return self._out
+
+    @property
+    def finished_at(self):
+        """time.perf_counter() when done() or wait() first saw the job finished."""
+        return self._finished_at
+
+    def stats(self) -> dict:
+        """Device statistics of the finished job (as last_run_stats)."""
+        self.wait()
+        st = N.RunStats()
+        N.check(N.library().fpm_job_stats(self._handle, C.byref(st)), N.context().handle)
+        out = {name: getattr(st, name) for name, _ in N.RunStats._fields_[:6]}
+        out["buckets"] = [(st.bucket_size[k], st.bucket_tiles[k], st.bucket_end_ms[k]) for k in range(st.buckets)]
+        return out
+
+    def _collect(self) -> None:
+        self._finished_at = time.perf_counter()
+        elapsed = self._finished_at - self._submitted
+        out = []
+        for p, a in zip(self._problems, self._arrays):
+            trace = [(it + 1, float(a["objectives"][it]), elapsed) for it in range(self._params.iterations)]
+            result = ReconstructionResult(
+                object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
+                pupil_support=p.model.pupil_support, trace=trace,
+                runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
+                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background)
+            if p.name is not None:
+                result.metadata["problem_name"] = p.name
+            out.append(result)
+        self._out = out
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_job_destroy(handle)
+            self._handle = None
+
+
+def submit_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> Job:
+    """Queues run_batch on the device and returns at once; Job.done() polls
+    and Job.wait() returns the results. For serving loops: several jobs of
+    one context run side by side."""
+    problems = list(problems)
+    params = algorithm._params(schedule)
+    upload(problems)
+    handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
+    results = (N.ResultDesc * len(problems))()
+    arrays = []
+    for i, p in enumerate(problems):
+        mh, mw = p.reconstruction_shape
+        h, w = p.image_shape
+        a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
+                 pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)))
+        results[i].object = N.ptr(a["object"], C.c_double)
+        results[i].object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
+        results[i].pupil = N.ptr(a["pupil"], C.c_double)
+        results[i].objectives = N.ptr(a["objectives"], C.c_double)
+        arrays.append(a)
+    ctx = N.context()
+    handle = C.c_void_p()
+    submitted = time.perf_counter()
+    N.check(N.library().fpm_run_batch_submit(ctx.handle, len(problems), handles, C.byref(params), results,
+                                             C.byref(handle)), ctx.handle)
+    return Job(handle, algorithm, problems, params, arrays, results, submitted)
 
 
 def _state_arrays(problem, algorithm, iterations):

@@ -558,14 +558,8 @@ class SpectralAlternatingProjection:
         return dict(object_step=float(self.object_step), batch_size=int(self.batch_size), epsilon=float(self.epsilon),
                     loss_type=self.loss_type)
 
-    def run_many(self, *, problems) -> list:
-        """Independent problems in one device call (fpm_spectral_run_batch):
-        one engine launch per tile size, one thread-block cluster per problem,
-        acquisition order and measured-amplitude initialisation. Each result
-        equals the problem's own run()."""
-        problems = list(problems)
-        if not problems:
-            return []
+    def _batch(self, problems):
+        """Descriptors, result arrays and their keep-alive list for a batch call."""
         params = self._params()
         keep = []
         models = (N.SpectralModelDesc * len(problems))()
@@ -588,11 +582,9 @@ class SpectralAlternatingProjection:
             outs[i].object_spectra = N.ptr(a["spectra"], C.c_double)
             outs[i].objectives = N.ptr(a["objectives"], C.c_double)
             arrays.append(a)
-        ctx = N.context()
-        started = time.perf_counter()
-        N.check(N.library().fpm_spectral_run_batch(ctx.handle, len(problems), models, meas, C.byref(params), outs),
-                ctx.handle)
-        elapsed = time.perf_counter() - started
+        return params, models, meas, outs, arrays, keep
+
+    def _results(self, problems, arrays, elapsed) -> list:
         results = []
         for p, a in zip(problems, arrays):
             model = p.model
@@ -605,6 +597,36 @@ class SpectralAlternatingProjection:
                 completed_iterations=int(self.iterations),
                 runtime=dict(elapsed_seconds=elapsed, algorithm="SpectralAlternatingProjection")))
         return results
+
+    def run_many(self, *, problems) -> list:
+        """Independent problems in one device call (fpm_spectral_run_batch):
+        one engine launch per tile size, one thread-block cluster per problem,
+        acquisition order and measured-amplitude initialisation. Each result
+        equals the problem's own run()."""
+        problems = list(problems)
+        if not problems:
+            return []
+        params, models, meas, outs, arrays, keep = self._batch(problems)
+        ctx = N.context()
+        started = time.perf_counter()
+        N.check(N.library().fpm_spectral_run_batch(ctx.handle, len(problems), models, meas, C.byref(params), outs),
+                ctx.handle)
+        return self._results(problems, arrays, time.perf_counter() - started)
+
+    def submit_many(self, *, problems) -> "SpectralJob":
+        """run_many without the wait (fpm_spectral_run_batch_submit): the
+        uploads are queued and the call returns; SpectralJob.done() polls and
+        SpectralJob.wait() returns the results."""
+        problems = list(problems)
+        if not problems:
+            raise InvalidParameterError("submit_many needs at least one problem")
+        params, models, meas, outs, arrays, keep = self._batch(problems)
+        ctx = N.context()
+        handle = C.c_void_p()
+        started = time.perf_counter()
+        N.check(N.library().fpm_spectral_run_batch_submit(ctx.handle, len(problems), models, meas, C.byref(params),
+                                                          outs, C.byref(handle)), ctx.handle)
+        return SpectralJob(handle, self, problems, arrays, outs, started)
 
     def run(self, *, problem: SpectralReconstructionProblem, initial_objects=None, frame_order=None, seed=None,
             resume=None, checkpoint_directory=None, checkpoint_every=1) -> SpectralReconstructionResult:
@@ -692,3 +714,47 @@ class SpectralAlternatingProjection:
             object_coupling=model.object_coupling, _objects=objects[index], _spectra=spectra[index], _pupils=pupils,
             trace=trace, completed_iterations=total, checkpoint=checkpoint,
             runtime=dict(elapsed_seconds=elapsed0 + time.perf_counter() - started, algorithm="SpectralAlternatingProjection"))
+
+
+class SpectralJob:
+    """Spectral requests queued by SpectralAlternatingProjection.submit_many."""
+
+    def __init__(self, handle, solver, problems, arrays, outs, submitted):
+        self._handle = handle
+        self._solver = solver
+        self._problems = problems
+        self._arrays = arrays
+        self._outs = outs  # the result descriptors the device writes through
+        self._submitted = submitted
+        self._finished_at = None
+        self._out = None
+
+    def done(self) -> bool:
+        if self._out is not None:
+            return True
+        flag = C.c_int32(0)
+        N.check(N.library().fpm_job_poll(self._handle, C.byref(flag)), N.context().handle)
+        if flag.value:
+            self._collect()
+        return bool(flag.value)
+
+    def wait(self) -> list:
+        if self._out is None:
+            N.check(N.library().fpm_job_wait(self._handle), N.context().handle)
+            self._collect()
+        return self._out
+
+    @property
+    def finished_at(self):
+        """time.perf_counter() when done() or wait() first saw the job finished."""
+        return self._finished_at
+
+    def _collect(self) -> None:
+        self._finished_at = time.perf_counter()
+        self._out = self._solver._results(self._problems, self._arrays, self._finished_at - self._submitted)
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_job_destroy(handle)
+            self._handle = None

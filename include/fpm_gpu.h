@@ -30,6 +30,7 @@
  *                                  fpm_spectral_run_batch (many requests, one launch per tile size)
  *   SpectralImagePlaneModel::forward_intensity
  *                                  src/model/spectral.rs:400-446 -> fpm_spectral_forward
+ *   (new) serving ................ fpm_run_batch_submit + fpm_job_poll / fpm_job_wait
  *   (new) batched tiles .......... fpm_run_batch (many independent problems, one launch per tile size),
  *                                  fpm_run_batch_host (host inputs, copies overlapped with the runs)
  *   Error / FpmError ............. src/error.rs:12, python/src/errors.rs:17-50 -> FPM_ERR_* + fpm_last_error
@@ -71,6 +72,7 @@ enum {
 
 typedef struct fpm_context fpm_context;
 typedef struct fpm_problem fpm_problem;
+typedef struct fpm_job fpm_job;
 
 /* Microscope optics (src/experiment/optics.rs:44-68). */
 typedef struct {
@@ -298,6 +300,7 @@ typedef struct {
 
 int32_t fpm_last_run_stats(const fpm_context *ctx, fpm_run_stats *stats);
 
+
 /* ------------------------------------------------- narrowband spectral AP */
 /* ObjectCoupling (src/model/spectral.rs:21-30). */
 enum { FPM_COUPLING_INDEPENDENT = 0, FPM_COUPLING_SHARED_COMPLEX = 1 };
@@ -366,6 +369,32 @@ int32_t fpm_spectral_run_batch(fpm_context *ctx, int32_t count, const fpm_spectr
  * objects' centred spectra: gain * sum(weight * local intensity) + background. */
 int32_t fpm_spectral_forward(fpm_context *ctx, const fpm_spectral_model_desc *model, const double *spectra,
                              double *intensities);
+
+/* ------------------------------------------------------------ serving */
+/* fpm_run_batch without the wait, for serving loops: the work is queued on
+ * the job's own streams (jobs of one context overlap) and the call returns.
+ * Until the job has finished, its problems are reserved (other calls and
+ * fpm_problem_destroy refuse them) and `results` and its arrays must stay
+ * valid; `params` is copied. */
+int32_t fpm_run_batch_submit(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
+                             const fpm_algorithm_params *params, fpm_result_desc *results, fpm_job **job);
+/* fpm_spectral_run_batch without the wait: measurement uploads and the
+ * initial objects are queued before the call returns, so the descriptors
+ * and their arrays need to outlive the call only; `results` must stay valid
+ * until the job has finished. */
+int32_t fpm_spectral_run_batch_submit(fpm_context *ctx, int32_t count, const fpm_spectral_model_desc *models,
+                                      const fpm_measurement_desc *measurements, const fpm_spectral_params *params,
+                                      fpm_spectral_result_desc *results, fpm_job **job);
+/* Non-blocking: *done = 1 once the device work has finished; the call that
+ * first sees it downloads the results (a short wait on the finished work)
+ * and fills the objectives, then returns the job's status. */
+int32_t fpm_job_poll(fpm_job *job, int32_t *done);
+/* Blocks until the job has finished; returns its status. */
+int32_t fpm_job_wait(fpm_job *job);
+/* Device statistics of a finished job (as fpm_last_run_stats). */
+int32_t fpm_job_stats(fpm_job *job, fpm_run_stats *stats);
+/* Waits for the job if needed and frees it. */
+int32_t fpm_job_destroy(fpm_job *job);
 
 #ifdef __cplusplus
 }
