@@ -162,6 +162,35 @@ def test_mpie_epry_pupil_config(fpm):
             assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
 
 
+def test_config2_full_iteration_count(fpm):
+    """BASELINE config 2 at its full 50 iterations: mPIE and EPRY with pupil
+    recovery, 13x13 LEDs, 128x128 frames (M=336), Zernike true pupil (seed
+    11), Poisson 5e3. Object (and EPRY pupil) NRMSE <= 1e-4 vs FP64."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 13, 128, seed=1, photons=5e3, pupil_seed=11)
+    oproblem = oracle.Problem(omodel, data, gains=gains)
+    with ThreadPoolExecutor(max_workers=2) as pool:
+        futures = {name: pool.submit(oracle.run, oproblem, name, iterations=50) for name in ("mpie", "epry")}
+        problem = fpm.ReconstructionProblem(data, model)
+        got = {"mpie": fpm.Mpie(iterations=50).run(problem), "epry": fpm.Epry(iterations=50).run(problem)}
+        expected = {name: f.result() for name, f in futures.items()}
+    for name in ("mpie", "epry"):
+        assert oracle.complex_nrmse(expected[name]["object"], got[name].object) <= NRMSE, name
+        _objective_close([t[1] for t in got[name].trace], expected[name]["objectives"])
+    assert oracle.complex_nrmse(expected["epry"]["pupil"], got["epry"].recovered_pupil) <= NRMSE
+
+
+def test_config1_full_iteration_count(fpm):
+    """BASELINE config 1 at its full 100 GD iterations: 256x256 frames,
+    15x15 LEDs (M=729), Poisson 1e4 at the bright-field peak, seed 7."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 15, 256, seed=7, photons=1e4)
+    result, expected = _run_both(fpm, fpm.GradientDescent(iterations=100), "gd", dict(iterations=100), model, omodel,
+                                 data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
 def test_gradient_descent_full_tile(fpm):
     """Wirtinger GD on one 256x256 tile with 15x15 LEDs (M=729), Poisson 1e4, 2 iterations."""
     model, omodel, data, truth, gains = helpers.simulated(fpm, 15, 256, seed=7, photons=1e4)
