@@ -525,7 +525,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
         }
         const int steps = truncating ? 2 * T.frame_count : spectral ? T.step_count : T.frame_count;
-        for (int step = 0; step < steps; ++step) {
+        const int step_begin = P.frame_end > 0 ? P.frame_begin : 0;
+        const int step_end = P.frame_end > 0 ? min(P.frame_end, steps) : steps;
+        for (int step = step_begin; step < step_end; ++step) {
             // Truncating: batch k covers steps [2kB, 2kB + 2b): b statistics
             // steps, then the b update steps of the same frames.
             int idx = step;
@@ -1112,7 +1114,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         if (tid == 0) {
             double total = 0.0;
             for (int w = 0; w < K::WARPS; ++w) total += dred[w];
-            T.partials[(size_t)it * C + c] = total;
+            double* slot = T.partials + (size_t)it * C + c;
+            *slot = P.accumulate ? *slot + total : total;
         }
         __syncthreads();
     }

@@ -83,6 +83,7 @@ __global__ void shift_to_state_kernel(double2* const* scratch, float2* const* ob
     const long long total = (long long)m * ms;
     const double2* src = scratch[tile];
     float2* o = object[tile];
+    if (!o) return;  // a tile left out of this pass
     float2* a = anchor ? anchor[tile] : nullptr;
     float2* v = velocity ? velocity[tile] : nullptr;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
@@ -382,6 +383,109 @@ __global__ void __launch_bounds__(kGaugeThreads) gauge_kernel(const GaugeTile* t
 
 cudaError_t launch_gauge(const GaugeTile* tiles, int count, int n, int m, cudaStream_t s) {
     gauge_kernel<<<count, kGaugeThreads, 0, s>>>(tiles, n, m);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- GD regularisers
+
+__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double znorm2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+// Normalised forward differences of pixel (r, c) for the smoothed TV: the
+// horizontal and vertical differences over sqrt(|dh|^2 + |dv|^2 + eps^2),
+// each zero where the neighbour is outside the grid.
+__device__ __forceinline__ void tv_terms(const double2* __restrict__ v, int m, int r, int c, double eps2, double2& qh,
+                                         double2& qv) {
+    const double2 x = v[(long long)r * m + c];
+    const bool has_h = c + 1 < m, has_v = r + 1 < m;
+    const double2 dh = has_h ? zsub(v[(long long)r * m + c + 1], x) : make_double2(0.0, 0.0);
+    const double2 dv = has_v ? zsub(v[(long long)(r + 1) * m + c], x) : make_double2(0.0, 0.0);
+    const double inv = 1.0 / sqrt((has_h ? znorm2(dh) : 0.0) + (has_v ? znorm2(dv) : 0.0) + eps2);
+    qh = make_double2(dh.x * inv, dh.y * inv);
+    qv = make_double2(dv.x * inv, dv.y * inv);
+}
+
+// apply_complex_tv_step (src/algorithms/regularization.rs:5-48) as a
+// gather: the gradient at p is -(qh(p) + qv(p)) + qh(left) + qv(above).
+__global__ void object_tv_kernel(const RegularTile* tiles, int m, double epsilon) {
+    const RegularTile& T = tiles[blockIdx.y];
+    const double eps2 = epsilon * epsilon;
+    const long long total = (long long)m * m;
+    bool bad = false;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / m), c = (int)(e % m);
+        double2 qh, qv, g;
+        tv_terms(T.src, m, r, c, eps2, qh, qv);
+        g = make_double2(-(qh.x + qv.x), -(qh.y + qv.y));
+        if (c >= 1) {
+            tv_terms(T.src, m, r, c - 1, eps2, qh, qv);
+            g.x += qh.x;
+            g.y += qh.y;
+        }
+        if (r >= 1) {
+            tv_terms(T.src, m, r - 1, c, eps2, qh, qv);
+            g.x += qv.x;
+            g.y += qv.y;
+        }
+        const double2 x = T.src[e];
+        const double2 y = make_double2(x.x - T.weight * g.x, x.y - T.weight * g.y);
+        bad |= !isfinite(y.x) || !isfinite(y.y);
+        T.dst[e] = y;
+    }
+    if (bad) atomicOr(T.status, 128);
+}
+
+cudaError_t launch_object_tv(const RegularTile* tiles, int count, int m, double epsilon, cudaStream_t s) {
+    const long long total = (long long)m * m;
+    const int blocks = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+    object_tv_kernel<<<dim3(blocks, count), 256, 0, s>>>(tiles, m, epsilon);
+    return cudaGetLastError();
+}
+
+// apply_quadratic_smoothing_step (src/algorithms/regularization.rs:50-80)
+// into the scratch, then the support, then back into the pupil.
+__global__ void pupil_smoothing_kernel(const RegularTile* tiles, int n, int constrain) {
+    const RegularTile& T = tiles[blockIdx.y];
+    const long long total = (long long)n * n;
+    bool bad = false;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / n), c = (int)(e % n);
+        const float2 xf = T.pupil[e];
+        const double2 x = make_double2(xf.x, xf.y);
+        // The reference's scatter sums to grad = -2 * sum over the grid
+        // neighbours of (neighbour - x).
+        double2 g = make_double2(0.0, 0.0);
+        auto add = [&](long long q) {
+            const float2 yf = T.pupil[q];
+            g.x -= 2.0 * ((double)yf.x - x.x);
+            g.y -= 2.0 * ((double)yf.y - x.y);
+        };
+        if (c + 1 < n) add(e + 1);
+        if (r + 1 < n) add(e + n);
+        if (c >= 1) add(e - 1);
+        if (r >= 1) add(e - n);
+        double2 y = make_double2(x.x - T.weight * g.x, x.y - T.weight * g.y);
+        bad |= !isfinite(y.x) || !isfinite(y.y);
+        if (constrain && T.support[e] == 0) y = make_double2(0.0, 0.0);
+        T.pupil_scratch[e] = make_float2((float)y.x, (float)y.y);
+    }
+    if (bad) atomicOr(T.status, 128);
+}
+
+__global__ void pupil_copy_kernel(const RegularTile* tiles, int n) {
+    const RegularTile& T = tiles[blockIdx.y];
+    const long long total = (long long)n * n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+        T.pupil[e] = T.pupil_scratch[e];
+}
+
+cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, int constrain, cudaStream_t s) {
+    const long long total = (long long)n * n;
+    const int blocks = (int)((total + 255) / 256 < 256 ? (total + 255) / 256 : 256);
+    pupil_smoothing_kernel<<<dim3(blocks, count), 256, 0, s>>>(tiles, n, constrain);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    pupil_copy_kernel<<<dim3(blocks, count), 256, 0, s>>>(tiles, n);
     return cudaGetLastError();
 }
 

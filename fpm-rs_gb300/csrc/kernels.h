@@ -66,7 +66,8 @@ struct TileDesc {
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event
     int* status;               // bits: 1 non-finite momentum, 4 no valid data, 8 gauge, 16 truncation statistic,
-                               // 32 adaptive pass objective, 64 non-finite recovered pupil
+                               // 32 adaptive pass objective, 64 non-finite recovered pupil, 128 non-finite
+                               // regulariser step
     int M, frame_count;
     float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
@@ -112,6 +113,10 @@ struct EngineParams {
     int gd_batch;              // gradient descent frames per mini-batch (1: update after every frame)
     float trunc_threshold;     // gradient descent Poisson truncation threshold (0: off)
     double progress_threshold, reduction_factor, minimum_step;  // adaptive AP controller
+    // With frame_end > 0 a launch walks order positions [frame_begin,
+    // frame_end) of its one pass (one GD batch between regulariser steps),
+    // adding its objective partials to the pass's when `accumulate`.
+    int frame_begin, frame_end, accumulate;
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.
@@ -198,6 +203,23 @@ struct GaugeTile {
     int row_exact, col_exact;  // every source offset is integer on that axis
 };
 cudaError_t launch_gauge(const GaugeTile* tiles, int count, int n, int m, cudaStream_t s);
+
+// GD regularisers between per-batch engine launches (src/algorithms/
+// regularization.rs:5-80), FP64. Object TV: dst = src - weight * grad TV_eps
+// on natural-order M x M objects. Pupil smoothing: dst = pupil - weight *
+// grad |D pupil|^2 on the N x N state pupil, then the support when
+// `constrain`; status bit 128 marks a non-finite result.
+struct RegularTile {
+    const double2* src;
+    double2* dst;
+    float2* pupil;
+    float2* pupil_scratch;
+    const uint8_t* support;
+    double weight;
+    int* status;
+};
+cudaError_t launch_object_tv(const RegularTile* tiles, int count, int m, double epsilon, cudaStream_t s);
+cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, int constrain, cudaStream_t s);
 
 // Context accessors for entry points that live outside runtime.cpp.
 void set_context_error(fpm_context* ctx, const char* message);

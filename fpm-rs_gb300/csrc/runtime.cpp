@@ -216,7 +216,7 @@ struct fpm_problem {
     DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
-        pupil_gradient;
+        pupil_gradient, tv_scratch, pupil_scratch;
     fpm_job* busy = nullptr;  // the submitted job that owns the problem until it finishes
 };
 
@@ -829,7 +829,19 @@ Status validate_params(const fpm_algorithm_params* a) {
             return Status::make(FPM_ERR_UNSUPPORTED,
                                 "gradient descent with both pupil recovery and Poisson truncation is not implemented "
                                 "on the GB300 device path");
-        // GradientDescent::validate (src/algorithms/gradient_descent.rs:319-331).
+        // GradientDescent::validate (src/algorithms/gradient_descent.rs:319-383).
+        if (!std::isfinite(a->object_tv_weight) || a->object_tv_weight < 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "object_tv_weight must be finite and non-negative");
+        if (a->object_tv_weight > 0.0 && (!std::isfinite(a->object_tv_epsilon) || a->object_tv_epsilon <= 0.0))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "object_tv_epsilon must be finite and positive");
+        if (!std::isfinite(a->pupil_smoothing_weight) || a->pupil_smoothing_weight < 0.0)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_smoothing_weight must be finite and non-negative");
+        if (a->pupil_smoothing_weight > 0.0 && !a->recover_pupil)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_smoothing_weight requires recover_pupil");
+        if ((a->object_tv_weight > 0.0 || a->pupil_smoothing_weight > 0.0) && a->poisson_truncation)
+            return Status::make(FPM_ERR_UNSUPPORTED,
+                                "gradient descent regularisers with Poisson truncation are not implemented on the "
+                                "GB300 device path");
         if (a->poisson_truncation) {
             if (!std::isfinite(a->poisson_truncation_threshold) || a->poisson_truncation_threshold <= 0.0)
                 return Status::make(FPM_ERR_INVALID_PARAMETER,
@@ -888,11 +900,13 @@ Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) 
 // A problem's per-run buffers: bound to the stream of the run that uses them.
 std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
     return {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-            &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient};
+            &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient, &p->tv_scratch,
+            &p->pupil_scratch};
 }
 
 struct BucketRun {
-    DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial;
+    DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
+        tv_ptrs, tv_objects, tv_table, smooth_table;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
     cudaEvent_t first = nullptr, last = nullptr;
     int launches = 0;
@@ -915,6 +929,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     // and after every iteration (Runner::run, src/reconstruction/runner.rs:122,220).
     const bool canonical = (epry && a->recover_pupil) || gd_pupil;
     const bool gd_batched = a->algorithm == FPM_ALG_GD && a->batch_size > 1;
+    // GD regularisers run between per-batch engine launches.
+    const bool tv = a->algorithm == FPM_ALG_GD && a->object_tv_weight > 0.0;
+    const bool smoothing = gd_pupil && a->pupil_smoothing_weight > 0.0;
+    const bool regularised = tv || smoothing;
     const int iters = a->iterations;
     const bool resumed = !b.resume.empty();
     const int it0 = resumed ? b.resume[0]->completed_iterations : 0;
@@ -942,6 +960,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(p->pupil_gradient.ensure(sizeof(float2) * n2));
             FPM_CUDA(cudaMemsetAsync(p->pupil_gradient.ptr, 0, sizeof(float2) * n2, s));
         }
+        if (tv) FPM_TRY(p->tv_scratch.ensure(sizeof(double2) * (size_t)M * M));
+        if (smoothing) FPM_TRY(p->pupil_scratch.ensure(sizeof(float2) * n2));
         if (mpie) {
             FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
@@ -1069,7 +1089,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             br.bytes += 48.0 * (double)M * (double)M * (double)((long long)effective * iters / a->momentum_interval);
     }
     for (DeviceBuffer* buf : {&br.tiles, &br.init, &br.gauge, &br.scratch_ptrs, &br.object_ptrs, &br.anchor_ptrs,
-                              &br.velocity_ptrs, &br.avg, &br.init_partial})
+                              &br.velocity_ptrs, &br.avg, &br.init_partial, &br.tv_ptrs, &br.tv_objects,
+                              &br.tv_table, &br.smooth_table})
         buf->bind(ctx->pool, s);
     FPM_CUDA(cudaEventCreate(&br.first));
     FPM_CUDA(cudaEventCreate(&br.last));
@@ -1120,7 +1141,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.eps = (float)a->epsilon;
     ep.object_step = (float)a->object_step;
     ep.pupil_step = (float)a->pupil_step;
-    ep.constrain_pupil = a->constrain_pupil_support ? 1 : 0;
+    // With pupil smoothing the support is imposed after the smoothing step.
+    ep.constrain_pupil = a->constrain_pupil_support && !smoothing ? 1 : 0;
     ep.momentum = mpie ? 1 : 0;
     ep.interval = a->momentum_interval;
     ep.friction = (float)a->momentum_friction;
@@ -1146,7 +1168,71 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         br.launches += 1;
         return Status::ok();
     };
-    if (iters > it0) {
+    if (iters > it0 && regularised) {
+        // One launch per GD batch (order positions [b B, (b + 1) B)), then the
+        // regularisers scaled by each tile's batch share of its frames; a tile
+        // whose frames are exhausted keeps its state.
+        const int B = a->batch_size;
+        int fmax = 0;
+        for (fpm_problem* p : b.problems) fmax = std::max(fmax, p->frames);
+        const int nb = (fmax + B - 1) / B;
+        std::vector<fpm::RegularTile> tv_table, smooth_table;
+        std::vector<double2*> tv_ptrs(count);
+        std::vector<float2*> tv_objects((size_t)nb * count);
+        for (int k = 0; k < nb; ++k)
+            for (int t = 0; t < count; ++t) {
+                fpm_problem* p = b.problems[t];
+                const int in_batch = std::max(0, std::min((k + 1) * B, p->frames) - k * B);
+                const double fraction = (double)in_batch / (double)p->frames;
+                fpm::RegularTile r{};
+                r.src = p->scratch64.as<double2>();
+                r.dst = tv ? p->tv_scratch.as<double2>() : nullptr;
+                r.pupil = p->pupil_state.as<float2>();
+                r.pupil_scratch = smoothing ? p->pupil_scratch.as<float2>() : nullptr;
+                r.support = p->support_d.as<uint8_t>();
+                r.status = p->status.as<int>();
+                r.weight = a->object_tv_weight * fraction;
+                tv_table.push_back(r);
+                r.weight = a->pupil_smoothing_weight * fraction;
+                smooth_table.push_back(r);
+                tv_objects[(size_t)k * count + t] = in_batch > 0 ? p->object.as<float2>() : nullptr;
+                if (k == 0) tv_ptrs[t] = tv ? p->tv_scratch.as<double2>() : nullptr;
+            }
+        FPM_TRY(upload_array(br.tv_table, tv_table, s));
+        FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
+        FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
+        FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
+        for (int it = it0; it < iters; ++it) {
+            for (int k = 0; k < nb; ++k) {
+                ep.frame_begin = k * B;
+                ep.frame_end = (k + 1) * B;
+                ep.accumulate = k > 0 ? 1 : 0;
+                FPM_TRY(engine(it, it + 1));
+                if (tv) {
+                    // apply_object_tv (src/algorithms/gradient_descent.rs:1125-1165) in FP64.
+                    FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(br.object_ptrs.ptr),
+                                                          br.scratch_ptrs.as<double2*>(), count, M, s));
+                    FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, true, s));
+                    FPM_CUDA(fpm::launch_object_tv(br.tv_table.as<fpm::RegularTile>() + (size_t)k * count, count, M,
+                                                   a->object_tv_epsilon, s));
+                    FPM_TRY(fft2_device(ctx, br.tv_ptrs.as<double2*>(), count, M, M, false, s));
+                    FPM_CUDA(fpm::launch_shift_to_state(br.tv_ptrs.as<double2*>(),
+                                                        br.tv_objects.as<float2*>() + (size_t)k * count, nullptr,
+                                                        nullptr, count, M, s));
+                    br.launches += 7;
+                }
+                if (smoothing) {
+                    FPM_CUDA(fpm::launch_pupil_smoothing(br.smooth_table.as<fpm::RegularTile>() + (size_t)k * count,
+                                                         count, N, a->constrain_pupil_support ? 1 : 0, s));
+                    br.launches += 2;
+                }
+            }
+            if (canonical) {
+                FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
+                br.launches += 1;
+            }
+        }
+    } else if (iters > it0) {
         if (epry || canonical) {
             for (int it = it0; it < iters; ++it) {
                 FPM_TRY(engine(it, it + 1));
@@ -1251,6 +1337,7 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 16) return Status::make(FPM_ERR_NUMERICAL, "Poisson truncation statistic is non-finite");
     if (status & 32) return Status::make(FPM_ERR_NUMERICAL, "adaptive alternating projection produced an invalid pass objective");
     if (status & 64) return Status::make(FPM_ERR_NUMERICAL, "pupil update produced a non-finite value");
+    if (status & 128) return Status::make(FPM_ERR_NUMERICAL, "regularization produced a non-finite value");
     if (!r) return Status::ok();
     const int C = fpm::engine_ctas(p->n);
     if (r->objectives) fill_objectives(p, a, r->objectives);

@@ -74,6 +74,7 @@ class AlgorithmParams(C.Structure):
         ("recover_frame_gains", C.c_int32), ("recover_background", C.c_int32),
         ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
         ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
+        ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
     ]
 
 

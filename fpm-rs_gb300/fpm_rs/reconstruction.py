@@ -310,9 +310,9 @@ class GradientDescent(_Algorithm):
         self.pupil_step, self.constrain_pupil_support = pupil_step, constrain_pupil_support
         self.object_tv, self.pupil_smoothing = object_tv, pupil_smoothing
         self.parallel_workers = parallel_workers
-        if recover_illumination or object_tv or pupil_smoothing:
-            raise UnsupportedError(
-                "illumination recovery and object/pupil regularisation are not implemented on the GB300 device path")
+        self.object_tv_epsilon = object_tv_epsilon
+        if recover_illumination:
+            raise UnsupportedError("illumination recovery is not implemented on the GB300 device path")
 
     def _params(self, schedule):
         p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
@@ -323,6 +323,9 @@ class GradientDescent(_Algorithm):
         p.recover_pupil = int(bool(self.recover_pupil))
         p.pupil_step = float(self.pupil_step)
         p.constrain_pupil_support = int(bool(self.constrain_pupil_support))
+        p.object_tv_weight = float(self.object_tv)
+        p.object_tv_epsilon = float(self.object_tv_epsilon)
+        p.pupil_smoothing_weight = float(self.pupil_smoothing)
         return p
 
 

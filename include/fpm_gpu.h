@@ -136,6 +136,12 @@ typedef struct {
      * reduction_factor, not below minimum_object_step, after a pass whose
      * relative objective progress is at most progress_threshold. */
     double progress_threshold, reduction_factor, minimum_object_step;
+    /* GD regularisers at every batch end, scaled by the batch's share of the
+     * frames (src/algorithms/gradient_descent.rs:643-660): an isotropic TV
+     * step on the real-space object (weight 0: off; epsilon finite and > 0
+     * when on) and, with pupil recovery, a quadratic smoothing step on the
+     * pupil before its support is imposed. */
+    double object_tv_weight, object_tv_epsilon, pupil_smoothing_weight;
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */

@@ -1062,7 +1062,86 @@ typedef struct {
     int recover;
     double step;
     int constrain;
+    double tv_weight, tv_epsilon;  /* object TV regulariser (0: off) */
+    double smoothing;              /* pupil quadratic smoothing (0: off) */
 } gd_pupil_config;
+
+/* apply_complex_tv_step (src/algorithms/regularization.rs:5-48): one step of
+ * the smoothed isotropic TV gradient, accumulated in the reference's order. */
+static int32_t complex_tv_step(cplx *values, int h, int w, double weight, double epsilon) {
+    if (weight == 0.0 || h <= 0 || w <= 0) return ORC_OK;
+    size_t n = (size_t)h * w;
+    cplx *gradient = (cplx *)calloc(n, sizeof(cplx));
+    for (int row = 0; row < h; ++row)
+        for (int col = 0; col < w; ++col) {
+            size_t px = (size_t)row * w + col;
+            int has_h = col + 1 < w, has_v = row + 1 < h;
+            cplx dh = has_h ? c_sub(values[px + 1], values[px]) : cx(0.0, 0.0);
+            cplx dv = has_v ? c_sub(values[px + w], values[px]) : cx(0.0, 0.0);
+            double norm = sqrt((has_h ? c_norm_sqr(dh) : 0.0) + (has_v ? c_norm_sqr(dv) : 0.0) + epsilon * epsilon);
+            if (has_h) {
+                cplx q = c_divr(dh, norm);
+                gradient[px] = c_sub(gradient[px], q);
+                gradient[px + 1] = c_add(gradient[px + 1], q);
+            }
+            if (has_v) {
+                cplx q = c_divr(dv, norm);
+                gradient[px] = c_sub(gradient[px], q);
+                gradient[px + w] = c_add(gradient[px + w], q);
+            }
+        }
+    int32_t st = ORC_OK;
+    for (size_t i = 0; i < n; ++i) {
+        values[i] = c_sub(values[i], c_scale(gradient[i], weight));
+        if (!isfinite(values[i].re) || !isfinite(values[i].im)) st = ORC_NUMERICAL;
+    }
+    free(gradient);
+    return st ? fail(ORC_NUMERICAL, "regularization produced a non-finite value") : ORC_OK;
+}
+
+/* apply_quadratic_smoothing_step (src/algorithms/regularization.rs:50-80). */
+static int32_t quadratic_smoothing_step(cplx *values, int h, int w, double weight) {
+    if (weight == 0.0 || h <= 0 || w <= 0) return ORC_OK;
+    size_t n = (size_t)h * w;
+    cplx *gradient = (cplx *)calloc(n, sizeof(cplx));
+    for (int row = 0; row < h; ++row)
+        for (int col = 0; col < w; ++col) {
+            size_t px = (size_t)row * w + col;
+            if (col + 1 < w) {
+                cplx d = c_sub(values[px + 1], values[px]);
+                gradient[px] = c_sub(gradient[px], c_scale(d, 2.0));
+                gradient[px + 1] = c_add(gradient[px + 1], c_scale(d, 2.0));
+            }
+            if (row + 1 < h) {
+                cplx d = c_sub(values[px + w], values[px]);
+                gradient[px] = c_sub(gradient[px], c_scale(d, 2.0));
+                gradient[px + w] = c_add(gradient[px + w], c_scale(d, 2.0));
+            }
+        }
+    int32_t st = ORC_OK;
+    for (size_t i = 0; i < n; ++i) {
+        values[i] = c_sub(values[i], c_scale(gradient[i], weight));
+        if (!isfinite(values[i].re) || !isfinite(values[i].im)) st = ORC_NUMERICAL;
+    }
+    free(gradient);
+    return st ? fail(ORC_NUMERICAL, "regularization produced a non-finite value") : ORC_OK;
+}
+
+/* apply_object_tv (src/algorithms/gradient_descent.rs:1125-1165): the TV
+ * step on the real-space object, through ifftshift, inverse FFT, forward FFT
+ * and fftshift of the centred spectrum. */
+static int32_t object_tv(orc_state *s, double weight, double epsilon) {
+    cplx *field = (cplx *)malloc(sizeof(cplx) * s->n_high);
+    ifftshift_c(s->object, field, s->mh, s->mw);
+    fft2_c(field, s->mh, s->mw, 1);
+    int32_t st = complex_tv_step(field, s->mh, s->mw, weight, epsilon);
+    if (!st) {
+        fft2_c(field, s->mh, s->mw, 0);
+        fftshift_c(field, s->object, s->mh, s->mw);
+    }
+    free(field);
+    return st;
+}
 
 static int32_t gradient_step(orc_state *s, const int *frames, int count, double object_step, double epsilon,
                              int loss, double truncation_threshold, const gd_pupil_config *pupil_cfg,
@@ -1145,6 +1224,17 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
                     return fail(ORC_NUMERICAL, "pupil update produced a non-finite value");
             }
         }
+    }
+    /* Regularisers at the batch end, scaled by the batch's share of the
+     * frames (src/algorithms/gradient_descent.rs:643-660). */
+    double batch_fraction = (double)count / (double)s->frames;
+    if (pupil_cfg && pupil_cfg->tv_weight > 0.0) {
+        int32_t st = object_tv(s, batch_fraction * pupil_cfg->tv_weight, pupil_cfg->tv_epsilon);
+        if (st) return st;
+    }
+    if (recover_pupil && pupil_cfg->smoothing > 0.0) {
+        int32_t st = quadratic_smoothing_step(s->pupil, s->h, s->w, batch_fraction * pupil_cfg->smoothing);
+        if (st) return st;
     }
     if (recover_pupil && pupil_cfg->constrain) {
         const uint8_t *support = s->p->support;
@@ -1472,7 +1562,9 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
             int count = p->frames - start < prm->batch_size ? p->frames - start : prm->batch_size;
             if (prm->algorithm == ORC_ALG_GD)
             {
-                const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil};
+                const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil,
+                                            prm->object_tv_weight, prm->object_tv_epsilon,
+                                            prm->pupil_smoothing_weight};
                 st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type,
                                    prm->poisson_truncation_threshold, &pc, &summary);
             }
@@ -1894,4 +1986,12 @@ int32_t orc_spectral_forward(const orc_spectral_problem *p, const double *spectr
     }
     free(exit);
     return st;
+}
+
+int32_t orc_complex_tv_step(double *values, int32_t h, int32_t w, double weight, double epsilon) {
+    return complex_tv_step((cplx *)values, h, w, weight, epsilon);
+}
+
+int32_t orc_quadratic_smoothing_step(double *values, int32_t h, int32_t w, double weight) {
+    return quadratic_smoothing_step((cplx *)values, h, w, weight);
 }

@@ -95,6 +95,8 @@ typedef struct {
     double background_step, background_min, background_max;
     double poisson_truncation_threshold;   /* GD: 0 disables the truncation gate */
     double progress_threshold, reduction_factor, minimum_object_step;  /* adaptive AP controller */
+    double object_tv_weight, object_tv_epsilon;   /* GD object TV regulariser (weight 0: off) */
+    double pupil_smoothing_weight;                /* GD pupil quadratic smoothing (0: off) */
 } orc_params;
 
 /* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */
@@ -146,6 +148,11 @@ int32_t orc_run_many(int32_t count, const orc_problem *problems, const orc_param
                      orc_output *outputs, int32_t workers);
 
 double orc_complex_nrmse(const double *reference, const double *candidate, int64_t len);
+
+/* apply_complex_tv_step / apply_quadratic_smoothing_step
+ * (src/algorithms/regularization.rs:5-80) on h*w complex values, in place. */
+int32_t orc_complex_tv_step(double *values, int32_t h, int32_t w, double weight, double epsilon);
+int32_t orc_quadratic_smoothing_step(double *values, int32_t h, int32_t w, double weight);
 
 /* Narrowband spectral problem (src/model/spectral.rs:46-54,
  * src/experiment/spectral.rs:44-70): channel kernels on one common grid and a

@@ -97,6 +97,7 @@ class _Params(C.Structure):
         ("background_min", C.c_double), ("background_max", C.c_double),
         ("poisson_truncation_threshold", C.c_double),
         ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
+        ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
     ]
 
 
@@ -367,7 +368,8 @@ def params(algorithm: str, **kw) -> _Params:
                recover_pupil=False, constrain_pupil=True, pupil_step=0.1, recover_gains=False,
                gain_step=0.2, gain_min=1e-6, gain_max=1e6, recover_background=False,
                background_step=0.2, background_min=0.0, background_max=1e12, poisson_truncation_threshold=0.0,
-               progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001)
+               progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001, object_tv_weight=0.0,
+               object_tv_epsilon=1e-6, pupil_smoothing_weight=0.0)
     cfg.update(DEFAULTS[algorithm])
     cfg.update(kw)
     p = _Params()
@@ -379,7 +381,8 @@ def params(algorithm: str, **kw) -> _Params:
     for name in ("object_step", "epsilon", "stability", "momentum_friction", "momentum_feedback",
                  "pupil_step", "gain_step", "gain_min", "gain_max", "background_step",
                  "background_min", "background_max", "poisson_truncation_threshold", "progress_threshold",
-                 "reduction_factor", "minimum_object_step"):
+                 "reduction_factor", "minimum_object_step", "object_tv_weight", "object_tv_epsilon",
+                 "pupil_smoothing_weight"):
         setattr(p, name, float(cfg[name]))
     p.momentum_interval = int(cfg["momentum_interval"])
     p.recover_pupil = int(bool(cfg["recover_pupil"]))
@@ -540,3 +543,16 @@ def spectral_run(problem: SpectralProblem, *, iterations=50, object_step=1.0, ep
                                   _ptr(objectives, C.c_double)))
     objects = np.stack([state_object(s) for s in spectra])
     return dict(spectra=spectra, objects=objects, objectives=objectives)
+
+
+def complex_tv_step(values, weight: float, epsilon: float) -> np.ndarray:
+    out = _c128(values).copy()
+    _check(lib().orc_complex_tv_step(_ptr(out, C.c_double), out.shape[0], out.shape[1], C.c_double(weight),
+                                     C.c_double(epsilon)))
+    return out
+
+
+def quadratic_smoothing_step(values, weight: float) -> np.ndarray:
+    out = _c128(values).copy()
+    _check(lib().orc_quadratic_smoothing_step(_ptr(out, C.c_double), out.shape[0], out.shape[1], C.c_double(weight)))
+    return out

@@ -516,3 +516,45 @@ def test_gradient_descent_pupil_recovery(fpm, n, side, batch):
     _objective_close([t[1] for t in result.trace], expected["objectives"])
     plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "gd", iterations=4, batch_size=batch)
     assert oracle.complex_nrmse(plain["pupil"], expected["pupil"]) > 2 * NRMSE  # the pupil did move
+
+
+@pytest.mark.parametrize("n,side,batch", [(32, 5, 1), (64, 3, 4), (128, 3, 9)])
+def test_gradient_descent_object_tv(fpm, n, side, batch):
+    """GD with the object TV regulariser at every batch end
+    (src/algorithms/gradient_descent.rs:643-651, regularization.rs:5-48)."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=31, photons=1e4)
+    kw = dict(iterations=3, batch_size=batch, object_tv_weight=0.05, object_tv_epsilon=1e-6)
+    algo = fpm.GradientDescent(iterations=3, batch_size=batch, object_tv=0.05, object_tv_epsilon=1e-6)
+    result, expected = _run_both(fpm, algo, "gd", kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+    plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "gd", iterations=3, batch_size=batch)
+    assert oracle.complex_nrmse(plain["object"], expected["object"]) > 10 * NRMSE  # the regulariser acted
+
+
+@pytest.mark.parametrize("n,side,batch", [(32, 5, 1), (64, 3, 4)])
+def test_gradient_descent_pupil_smoothing(fpm, n, side, batch):
+    """GD pupil recovery with quadratic pupil smoothing before the support
+    (src/algorithms/gradient_descent.rs:653-663, regularization.rs:50-80)."""
+    model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=32, photons=1e4, pupil_seed=5)
+    kw = dict(iterations=3, batch_size=batch, recover_pupil=True, pupil_step=0.05, pupil_smoothing_weight=0.5)
+    algo = fpm.GradientDescent(iterations=3, batch_size=batch, recover_pupil=True, pupil_step=0.05,
+                               pupil_smoothing=0.5)
+    result, expected = _run_both(fpm, algo, "gd", kw, model, omodel, data, gains=gains)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
+    assert np.all(result.recovered_pupil[model.pupil_support == 0] == 0)
+    plain = oracle.run(oracle.Problem(omodel, data, gains=gains), "gd", iterations=3, batch_size=batch,
+                       recover_pupil=True, pupil_step=0.05)
+    assert oracle.complex_nrmse(plain["pupil"], expected["pupil"]) > 10 * NRMSE  # the smoothing acted
+
+
+def test_regulariser_validation(fpm):
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 3, 32, seed=33)
+    problem = fpm.ReconstructionProblem(data, model)
+    for bad in (dict(object_tv=-1.0), dict(object_tv=0.1, object_tv_epsilon=0.0), dict(pupil_smoothing=0.1)):
+        with pytest.raises(fpm.FpmError):
+            fpm.GradientDescent(iterations=1, **bad).run(problem)
+    with pytest.raises(fpm.UnsupportedError):
+        fpm.GradientDescent(iterations=1, object_tv=0.1, loss_type="poisson_nll",
+                            poisson_truncation_threshold=25.0).run(problem)

@@ -126,8 +126,7 @@ def test_unsupported_options_fail_before_device_work(fpm):
         fpm.AlternatingProjection(iterations=1).run(problem, callbacks=[object()])
     with pytest.raises(fpm.UnsupportedError):
         fpm.GradientDescent(recover_illumination=True)
-    with pytest.raises(fpm.UnsupportedError):
-        fpm.GradientDescent(object_tv=0.1)
+    fpm.GradientDescent(object_tv=0.1, recover_pupil=True, pupil_smoothing=0.02)  # device regularisers
     with pytest.raises(ValueError):
         fpm.Mpie(loss_type="l1")
 

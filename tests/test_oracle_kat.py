@@ -274,3 +274,34 @@ def test_gd_pupil_recovery_moves_the_pupil_inside_its_support():
     assert np.all(out["pupil"][support == 0] == 0)
     energy = np.sum(np.abs(out["pupil"][support != 0]) ** 2)
     assert abs(energy - np.sum(support)) <= 1e-9 * energy
+
+
+def test_regulariser_known_answers(oracle_module):
+    # apply_complex_tv_step / apply_quadratic_smoothing_step
+    # (src/algorithms/regularization.rs:5-80) on a 1x2 array, closed form.
+    a, b, w, eps = 1.0 + 0.5j, -0.25 + 2.0j, 0.3, 0.1
+    d = b - a
+    norm = np.sqrt(abs(d) ** 2 + eps ** 2)
+    got = oracle_module.complex_tv_step(np.array([[a, b]]), w, eps)
+    np.testing.assert_allclose(got[0], [a + w * d / norm, b - w * d / norm], rtol=0, atol=1e-15)
+    got = oracle_module.quadratic_smoothing_step(np.array([[a, b]]), w)
+    np.testing.assert_allclose(got[0], [a + 2 * w * d, b - 2 * w * d], rtol=0, atol=1e-15)
+    # Zero weight is the identity; the single-column case has vertical terms only.
+    x = np.array([[a], [b]])
+    np.testing.assert_array_equal(oracle_module.complex_tv_step(x, 0.0, eps), x)
+    got = oracle_module.complex_tv_step(x, w, eps)
+    np.testing.assert_allclose(got[:, 0], [a + w * d / norm, b - w * d / norm], rtol=0, atol=1e-15)
+
+
+def test_regularisers_reduce_variation_and_roughness(oracle_module):
+    # tests/reconstruction_tests.rs:2513-2600: a checkerboard object and pupil.
+    rows, cols = np.indices((16, 16))
+    sign = np.where((rows + cols) % 2 == 0, 1.0, -1.0)
+    obj = (1.0 + 0.15 * sign) * np.exp(1j * 0.2 * sign)
+
+    def variation(v):
+        return np.abs(np.diff(v, axis=1)).sum() + np.abs(np.diff(v, axis=0)).sum()
+
+    assert variation(oracle_module.complex_tv_step(obj, 0.002, 1e-6)) < variation(obj)
+    pupil = np.exp(1j * 0.35 * sign)
+    assert variation(oracle_module.quadratic_smoothing_step(pupil, 0.02)) < variation(pupil)
