@@ -1995,3 +1995,65 @@ int32_t orc_complex_tv_step(double *values, int32_t h, int32_t w, double weight,
 int32_t orc_quadratic_smoothing_step(double *values, int32_t h, int32_t w, double weight) {
     return quadratic_smoothing_step((cplx *)values, h, w, weight);
 }
+
+/* One GradientDescent::step (src/algorithms/gradient_descent.rs:405-671)
+ * over the batch `frames`, from the given centred spectrum and pupil; the
+ * state after the step is copied out. */
+int32_t orc_gd_batch_step(const orc_problem *p, const orc_params *prm, const double *spectrum, const double *pupil,
+                          const int32_t *frames, int32_t count, double *spectrum_out, double *pupil_out) {
+    orc_state s;
+    int32_t st = state_init(&s, p);
+    if (st) {
+        state_free(&s);
+        return st;
+    }
+    for (int32_t k = 0; k < count; ++k)
+        if (frames[k] < 0 || frames[k] >= p->frames) {
+            state_free(&s);
+            return fail(ORC_FRAME_OUT_OF_RANGE, "frame %d is out of range", frames[k]);
+        }
+    memcpy(s.object, spectrum, sizeof(cplx) * s.n_high);
+    memcpy(s.pupil, pupil, sizeof(cplx) * s.n_low);
+    const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil, prm->object_tv_weight,
+                                prm->object_tv_epsilon, prm->pupil_smoothing_weight};
+    step_summary summary = {0.0, 0.0};
+    st = gradient_step(&s, (const int *)frames, count, prm->object_step, prm->epsilon, prm->loss_type, 0.0, &pc,
+                       &summary);
+    if (!st) {
+        memcpy(spectrum_out, s.object, sizeof(cplx) * s.n_high);
+        memcpy(pupil_out, s.pupil, sizeof(cplx) * s.n_low);
+    }
+    state_free(&s);
+    return st;
+}
+
+/* The mean point loss of one frame over its unmasked pixels, for the
+ * prediction gain * |psi|^2 + background (objective.rs:14-46 on the frame's
+ * forward intensity). */
+int32_t orc_frame_loss(const orc_problem *p, const double *spectrum, const double *pupil, int32_t frame, int32_t loss,
+                       double *out) {
+    orc_state s;
+    int32_t st = state_init(&s, p);
+    if (st) {
+        state_free(&s);
+        return st;
+    }
+    memcpy(s.object, spectrum, sizeof(cplx) * s.n_high);
+    memcpy(s.pupil, pupil, sizeof(cplx) * s.n_low);
+    st = source_field(&s, frame);
+    if (!st) {
+        const double *measured = p->data + (size_t)frame * s.n_low;
+        const uint8_t *mask = frame_mask(p, frame);
+        double sum = 0.0;
+        long valid = 0;
+        for (size_t i = 0; i < s.n_low; ++i) {
+            if (mask && mask[i] == 0) continue;
+            double predicted = model_gain(p, frame) * c_norm_sqr(s.field[i]) + model_background(p, frame, i);
+            sum += point_loss(predicted, measured[i], loss);
+            ++valid;
+        }
+        *out = valid ? sum / (double)valid : NAN;
+    }
+    state_free(&s);
+    return st;
+}

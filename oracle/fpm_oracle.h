@@ -149,6 +149,15 @@ int32_t orc_run_many(int32_t count, const orc_problem *problems, const orc_param
 
 double orc_complex_nrmse(const double *reference, const double *candidate, int64_t len);
 
+/* One GradientDescent::step over the batch `frames` from the given centred
+ * spectrum (mh*mw) and pupil (h*w); writes the stepped state. */
+int32_t orc_gd_batch_step(const orc_problem *problem, const orc_params *params, const double *spectrum,
+                          const double *pupil, const int32_t *frames, int32_t count, double *spectrum_out,
+                          double *pupil_out);
+/* Mean point loss of one frame over its unmasked pixels (objective.rs:14-46). */
+int32_t orc_frame_loss(const orc_problem *problem, const double *spectrum, const double *pupil, int32_t frame,
+                       int32_t loss, double *out);
+
 /* apply_complex_tv_step / apply_quadratic_smoothing_step
  * (src/algorithms/regularization.rs:5-80) on h*w complex values, in place. */
 int32_t orc_complex_tv_step(double *values, int32_t h, int32_t w, double weight, double epsilon);

@@ -556,3 +556,24 @@ def quadratic_smoothing_step(values, weight: float) -> np.ndarray:
     out = _c128(values).copy()
     _check(lib().orc_quadratic_smoothing_step(_ptr(out, C.c_double), out.shape[0], out.shape[1], C.c_double(weight)))
     return out
+
+
+def gd_batch_step(problem: Problem, spectrum, pupil, frames, **kw):
+    """One gradient-descent step over the batch `frames` from the given state."""
+    prm = params("gd", **kw)
+    st = problem.struct()
+    s_in, p_in = _c128(spectrum), _c128(pupil)
+    s_out, p_out = np.zeros_like(s_in), np.zeros_like(p_in)
+    f = np.ascontiguousarray(frames, np.int32)
+    _check(lib().orc_gd_batch_step(C.byref(st), C.byref(prm), _ptr(s_in, C.c_double), _ptr(p_in, C.c_double),
+                                   _ptr(f, C.c_int32), f.size, _ptr(s_out, C.c_double), _ptr(p_out, C.c_double)))
+    return s_out, p_out
+
+
+def frame_loss(problem: Problem, spectrum, pupil, frame: int, loss_type: str) -> float:
+    st = problem.struct()
+    out = C.c_double()
+    s_in, p_in = _c128(spectrum), _c128(pupil)
+    _check(lib().orc_frame_loss(C.byref(st), _ptr(s_in, C.c_double), _ptr(p_in, C.c_double), int(frame),
+                                LOSSES[loss_type], C.byref(out)))
+    return out.value

@@ -305,3 +305,85 @@ def test_regularisers_reduce_variation_and_roughness(oracle_module):
     assert variation(oracle_module.complex_tv_step(obj, 0.002, 1e-6)) < variation(obj)
     pupil = np.exp(1j * 0.35 * sign)
     assert variation(oracle_module.quadratic_smoothing_step(pupil, 0.02)) < variation(pupil)
+
+
+def _direct_model():
+    # tests/common/mod.rs:49-81: 8x8 detector, 16x16 grid, unit pupil, five
+    # integer crops at (4 + row, 4 + column) for (column, row) shifts.
+    shifts = [(-3, 0), (0, -3), (0, 0), (0, 3), (3, 0)]
+    return dict(h=8, w=8, mh=16, mw=16, start_row=np.array([4 + r for c, r in shifts], np.int64),
+                start_col=np.array([4 + c for c, r in shifts], np.int64), off_row=np.zeros(5), off_col=np.zeros(5),
+                pupil=np.ones((8, 8), np.complex128), support=np.ones((8, 8), np.uint8))
+
+
+def _direction(length, scale):
+    i = np.arange(length)
+    return scale * ((i % 13) / 13.0 - 0.5) + 1j * scale * ((i % 17) / 17.0 - 0.5)
+
+
+@pytest.mark.parametrize("loss", ["amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude"])
+def test_gradient_descent_gradients_match_finite_differences(oracle_module, loss):
+    # tests/reconstruction_tests.rs:2189-2300: object and pupil gradients of
+    # one GD step against central differences of the masked frame loss, 2e-5.
+    o = oracle_module
+    model = _direct_model()
+    rng = np.random.default_rng(4)
+    truth = np.exp(1j * 0.3 * rng.standard_normal((16, 16))) * (0.8 + 0.2 * rng.random((16, 16)))
+    data = o.forward_stack(o.Problem(model, None), o.object_spectrum(truth))
+    mask = np.ones((8, 8), np.uint8)
+    mask.ravel()[::5] = 0
+    problem = o.Problem(model, data, masks=np.broadcast_to(mask, data.shape).copy())
+    idx = np.arange(256).reshape(16, 16)
+    start = truth * (0.78 + 0.03 * (idx % 7) / 7.0) * np.exp(1j * 0.08 * ((idx % 11) / 11.0 - 0.5))
+    spectrum = o.object_spectrum(start)
+    pupil = model["pupil"]
+    frame, eps = 2, 1e-10
+    after, pupil_after = o.gd_batch_step(problem, spectrum, pupil, [frame], object_step=1.0, loss_type=loss,
+                                         recover_pupil=True, pupil_step=1.0, constrain_pupil=False)
+    d_obj = _direction(256, 0.07).reshape(16, 16)
+    d_pup = _direction(64, 0.05).reshape(8, 8)
+
+    def check(gradient, direction, perturb):
+        analytical = 2.0 * np.sum((np.conj(gradient) * direction).real)
+        h = 1e-6
+        numerical = (perturb(h) - perturb(-h)) / (2 * h)
+        scale = max(abs(analytical), abs(numerical), 1e-10)
+        assert abs(analytical - numerical) <= 2e-5 * scale, (loss, analytical, numerical)
+
+    obj_den = max(np.max(np.abs(pupil) ** 2), eps) + eps
+    check((spectrum - after) * obj_den, d_obj,
+          lambda t: o.frame_loss(problem, spectrum + t * d_obj, pupil, frame, loss))
+    patch = o.extract_patch(spectrum, (model["start_row"][frame], model["start_col"][frame]), (8, 8))
+    pup_den = max(np.max(np.abs(patch) ** 2), eps) + eps
+    check((pupil - pupil_after) * pup_den, d_pup,
+          lambda t: o.frame_loss(problem, spectrum, pupil + t * d_pup, frame, loss))
+
+
+def test_gradient_minibatch_is_the_mean_of_frame_gradients(oracle_module):
+    # tests/reconstruction_tests.rs:1802-1854: a two-frame batch moves the
+    # object by the mean of the two single-frame moves (1e-12).
+    o = oracle_module
+    model = _direct_model()
+    rng = np.random.default_rng(5)
+    truth = np.exp(1j * 0.3 * rng.standard_normal((16, 16)))
+    data = o.forward_stack(o.Problem(model, None), o.object_spectrum(truth))
+    problem = o.Problem(model, data)
+    start = o.object_spectrum(truth * 0.9)
+    pupil = model["pupil"]
+    firsts = [o.gd_batch_step(problem, start, pupil, [f], object_step=0.3)[0] for f in (0, 1)]
+    batched = o.gd_batch_step(problem, start, pupil, [0, 1], object_step=0.3)[0]
+    expected = start + ((firsts[0] - start) + (firsts[1] - start)) / 2.0
+    np.testing.assert_allclose(batched, expected, rtol=0, atol=1e-12)
+
+
+def test_mpie_cadence_is_independent_of_batch_partitioning(oracle_module):
+    # tests/reconstruction_tests.rs:693-731: bitwise equal spectra and traces.
+    o = oracle_module
+    model = _direct_model()
+    truth = np.exp(1j * 0.3 * np.random.default_rng(6).standard_normal((16, 16)))
+    data = o.forward_stack(o.Problem(model, None), o.object_spectrum(truth))
+    problem = o.Problem(model, data)
+    single = o.run(problem, "mpie", iterations=4, momentum_interval=3, batch_size=1)
+    grouped = o.run(problem, "mpie", iterations=4, momentum_interval=3, batch_size=5)
+    np.testing.assert_array_equal(single["object_spectrum"], grouped["object_spectrum"])
+    np.testing.assert_array_equal(single["objectives"], grouped["objectives"])
