@@ -2057,3 +2057,23 @@ int32_t orc_frame_loss(const orc_problem *p, const double *spectrum, const doubl
     state_free(&s);
     return st;
 }
+
+/* canonicalize_object_pupil (src/algorithms/gauge.rs:20-73) applied to the
+ * given centred spectrum (mh*mw) and pupil (h*w), in place. */
+int32_t orc_canonicalize(const orc_problem *p, double *spectrum, double *pupil) {
+    orc_state s;
+    int32_t st = state_init(&s, p);
+    if (st) {
+        state_free(&s);
+        return st;
+    }
+    memcpy(s.object, spectrum, sizeof(cplx) * s.n_high);
+    memcpy(s.pupil, pupil, sizeof(cplx) * s.n_low);
+    st = canonicalize_gauge(&s);
+    if (!st) {
+        memcpy(spectrum, s.object, sizeof(cplx) * s.n_high);
+        memcpy(pupil, s.pupil, sizeof(cplx) * s.n_low);
+    }
+    state_free(&s);
+    return st;
+}

@@ -154,6 +154,8 @@ double orc_complex_nrmse(const double *reference, const double *candidate, int64
 int32_t orc_gd_batch_step(const orc_problem *problem, const orc_params *params, const double *spectrum,
                           const double *pupil, const int32_t *frames, int32_t count, double *spectrum_out,
                           double *pupil_out);
+/* canonicalize_object_pupil (src/algorithms/gauge.rs:20-73) in place. */
+int32_t orc_canonicalize(const orc_problem *problem, double *spectrum, double *pupil);
 /* Mean point loss of one frame over its unmasked pixels (objective.rs:14-46). */
 int32_t orc_frame_loss(const orc_problem *problem, const double *spectrum, const double *pupil, int32_t frame,
                        int32_t loss, double *out);

@@ -577,3 +577,11 @@ def frame_loss(problem: Problem, spectrum, pupil, frame: int, loss_type: str) ->
     _check(lib().orc_frame_loss(C.byref(st), _ptr(s_in, C.c_double), _ptr(p_in, C.c_double), int(frame),
                                 LOSSES[loss_type], C.byref(out)))
     return out.value
+
+
+def canonicalize(problem: Problem, spectrum, pupil):
+    """The object/pupil gauge canonicalisation of the given state (copies)."""
+    st = problem.struct()
+    s_io, p_io = _c128(spectrum).copy(), _c128(pupil).copy()
+    _check(lib().orc_canonicalize(C.byref(st), _ptr(s_io, C.c_double), _ptr(p_io, C.c_double)))
+    return s_io, p_io

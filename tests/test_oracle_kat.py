@@ -387,3 +387,31 @@ def test_mpie_cadence_is_independent_of_batch_partitioning(oracle_module):
     grouped = o.run(problem, "mpie", iterations=4, momentum_interval=3, batch_size=5)
     np.testing.assert_array_equal(single["object_spectrum"], grouped["object_spectrum"])
     np.testing.assert_array_equal(single["objectives"], grouped["objectives"])
+
+
+def test_gauge_keeps_predictions_and_is_idempotent(oracle_module):
+    # src/algorithms/gauge.rs:435-496: integer crops, a perturbed state;
+    # canonicalisation leaves every prediction unchanged (2e-12), and a second
+    # pass changes nothing; invalid fields are numerical errors.
+    o = oracle_module
+    model = _direct_model()
+    rng = np.random.default_rng(8)
+    truth = np.exp(1j * 0.3 * rng.standard_normal((16, 16)))
+    data = o.forward_stack(o.Problem(model, None), o.object_spectrum(truth))
+    problem = o.Problem(model, data)
+    rows, cols = np.indices((8, 8))
+    pupil = 1.7 * np.exp(1j * (0.4 + 0.17 * rows - 0.23 * cols))
+    spectrum = o.object_spectrum(truth) * 0.6 * np.exp(-0.9j)
+    before = o.forward_stack(o.Problem(dict(model, pupil=pupil), None), spectrum)
+    canon_s, canon_p = o.canonicalize(problem, spectrum, pupil)
+    after = o.forward_stack(o.Problem(dict(model, pupil=canon_p), None), canon_s)
+    assert np.max(np.abs(after - before)) <= 2e-12 * np.max(np.abs(before))
+    again_s, again_p = o.canonicalize(problem, canon_s, canon_p)
+    np.testing.assert_array_equal(again_s, canon_s)
+    np.testing.assert_array_equal(again_p, canon_p)
+    with pytest.raises(o.OracleError):
+        o.canonicalize(problem, spectrum, np.zeros_like(pupil))
+    bad = spectrum.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(o.OracleError):
+        o.canonicalize(problem, bad, pupil)
