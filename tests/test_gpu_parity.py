@@ -558,3 +558,36 @@ def test_regulariser_validation(fpm):
     with pytest.raises(fpm.UnsupportedError):
         fpm.GradientDescent(iterations=1, object_tv=0.1, loss_type="poisson_nll",
                             poisson_truncation_threshold=25.0).run(problem)
+
+
+def test_empty_batch_zero_iterations_and_large_grid(fpm):
+    """Edge cases: an empty batch, zero iterations (the measured-amplitude
+    initial object, src/reconstruction/state.rs:280-355), and 64-point tiles
+    on an exact 1024 x 1024 grid (crops far from the grid edges)."""
+    assert fpm.run_batch(fpm.Mpie(iterations=2), []) == []
+    model, omodel, data, truth, gains = helpers.simulated(fpm, 5, 32, seed=41, photons=1e4)
+    result, expected = _run_both(fpm, fpm.AlternatingProjection(iterations=0), "ap", dict(iterations=0), model,
+                                 omodel, data, gains=gains)
+    assert result.trace == []
+    assert oracle.complex_nrmse(expected["object"], result.object) <= 1e-6
+    big, obig = helpers.planar_model(fpm, 5, 64, shape_policy=(1024, 1024))
+    assert big.reconstruction_shape == (1024, 1024)
+    obj = W.smooth_random_object((1024, 1024), 42)
+    intensity = oracle.forward_stack(oracle.Problem(obig, None), oracle.object_spectrum(obj), workers=8)
+    result, expected = _run_both(fpm, fpm.Mpie(iterations=2), "mpie", dict(iterations=2), big, obig, intensity)
+    assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
+    _objective_close([t[1] for t in result.trace], expected["objectives"])
+
+
+def test_ragged_batch_of_all_tile_sizes(fpm):
+    """One batch mixing every tile size and LED count equals each tile's own run, bitwise."""
+    specs = [(3, 32, 51), (5, 64, 52), (3, 128, 53), (3, 256, 54), (5, 32, 55)]
+    problems = []
+    for side, n, seed in specs:
+        model, omodel, data, truth, gains = helpers.simulated(fpm, side, n, seed=seed, photons=1e4)
+        problems.append(fpm.ReconstructionProblem(data, model))
+    algo = fpm.Mpie(iterations=2)
+    batch = fpm.run_batch(algo, problems)
+    for p, got in zip(problems, batch):
+        alone = algo.run(p)
+        np.testing.assert_array_equal(alone.object_spectrum, got.object_spectrum)
