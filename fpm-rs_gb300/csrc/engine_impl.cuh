@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             // Spectral update steps start from the stored mode field: no
             // inverse transform; the object stencil for P8 and a changed
             // channel's pupil rows arrive asynchronously behind P4-P6.
-            const bool spectral_update = spectral && sp.update != 0;
+            const bool spectral_update = spectral && sp.update == 1;  // update only: no staging or inverse
             float2* const obj = spectral ? T.object + (size_t)sp.object * M * ostride : T.object;
             if constexpr (spectral) {
                 if (sp.channel != slab_channel) {
@@ -715,6 +715,11 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 float2* const slot = T.mode_fields + (size_t)sp.slot * N * N + mbase;
                 float* const pred = T.prediction + mbase;
                 const int pq = phys<K>(q4);
+                // The exposure's last mode evaluates and updates in one step
+                // (kind 2): the prediction is then complete and the staged
+                // stencil is still the current object. Its psi goes through
+                // the scratch like the others (registers are the limit).
+                const bool merged = sp.update == 2;
                 if (!spectral_update) {
                     // Evaluation: psi_k, and prediction += w_k |psi_k|^2.
                     if constexpr (R == 32) column_inverse_split<K>(fld, pq, h4, tw, v);
@@ -726,8 +731,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         if (sp.slot > 0) pk += __ldcg(pred + (size_t)k * mstride);
                         __stcg(pred + (size_t)k * mstride, pk);
                     }
-                    __syncthreads();
-                    continue;
+                    if (!merged) {
+                        __syncthreads();
+                        continue;
+                    }
                 }
                 // Update: psi' - psi with the exposure's shared amplitude
                 // ratio sqrt(target / prediction); masked pixels keep psi and

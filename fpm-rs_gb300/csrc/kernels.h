@@ -27,14 +27,16 @@ struct FrameParam {
 // One virtual step of narrowband spectral AP (src/algorithms/spectral.rs:
 // 182-271). An exposure with K coherent modes takes K evaluation steps (the
 // detector field of mode k from the pre-exposure objects into scratch slot k,
-// its weighted intensity into the prediction) and then K update steps (the
+// its weighted intensity into the prediction) and then the K updates (the
 // shared amplitude ratio, forward transform and local-denominator correction
-// into the mode's stored object).
+// into the mode's stored object), last mode first: the last evaluation step
+// also updates its own mode, so an exposure takes 2K - 1 steps. The update
+// order changes only the summation order into a shared object.
 struct SpectralStep {
     FrameParam frame;     // the mode's crop and bilinear weights
     int exposure;         // measurement frame
     int object, channel;  // stored object and channel pupil
-    int update;           // 0: evaluate, 1: update
+    int update;           // 0: evaluate, 1: update, 2: evaluate and update (the exposure's last mode)
     int slot;             // mode position within the exposure
     int first_update;     // 1 on the exposure's first update step, which adds its loss
     float mode_weight;    // effective intensity weight of the mode

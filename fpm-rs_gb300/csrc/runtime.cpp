@@ -1858,29 +1858,33 @@ Status spectral_prepare(SpectralJob& j, const fpm_spectral_model_desc* sm, const
             for (size_t i = 0; i < n2; ++i) valid += ms->masks[(size_t)e * n2 + i] != 0;
         }
         j.weight_total += fw;
-        for (int phase = 0; phase < 2; ++phase)
-            for (int k = 0; k < count; ++k) {
-                const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
-                fpm::SpectralStep st{};
-                const int mode = source_offset[c] + l;
-                st.frame = j.params[mode];
-                st.exposure = e;
-                st.object = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : c;
-                st.channel = c;
-                st.update = phase;
-                st.slot = k;
-                st.mode_weight = (float)wk[k];
-                st.update_scale = (float)(fw * (wk[k] / wsum));
-                st.gain = (float)gain;
-                st.background = (float)sm->exposure_background[e];
-                st.inv_weight_sum = (float)(1.0 / wsum);
-                st.first_update = phase == 1 && k == 0 ? 1 : 0;
-                st.loss_scale = fw / (double)valid;
-                j.steps.push_back(st);
-                // Algorithmic HBM bytes: stencil read (evaluation), object
-                // read-modify-write (update), measurement (+ mask) once.
-                j.bytes_per_pass += phase == 0 ? 8.0 * stencil[mode] : 16.0 * stencil[mode];
-            }
+        // Evaluations 0..K-1 (the last one also updates its mode), then the
+        // updates K-2..0.
+        std::vector<std::pair<int, int>> order;  // (mode position, step kind)
+        for (int k = 0; k < count; ++k) order.emplace_back(k, k == count - 1 ? 2 : 0);
+        for (int k = count - 2; k >= 0; --k) order.emplace_back(k, 1);
+        for (const auto& [k, kind] : order) {
+            const int c = sm->contribution_channel[first + k], l = sm->contribution_local_frame[first + k];
+            fpm::SpectralStep st{};
+            const int mode = source_offset[c] + l;
+            st.frame = j.params[mode];
+            st.exposure = e;
+            st.object = sm->object_coupling == FPM_COUPLING_SHARED_COMPLEX ? 0 : c;
+            st.channel = c;
+            st.update = kind;
+            st.slot = k;
+            st.mode_weight = (float)wk[k];
+            st.update_scale = (float)(fw * (wk[k] / wsum));
+            st.gain = (float)gain;
+            st.background = (float)sm->exposure_background[e];
+            st.inv_weight_sum = (float)(1.0 / wsum);
+            st.first_update = kind == 2 ? 1 : 0;
+            st.loss_scale = fw / (double)valid;
+            j.steps.push_back(st);
+            // Algorithmic HBM bytes: stencil read (evaluation), object
+            // read-modify-write (update), measurement (+ mask) once.
+            j.bytes_per_pass += (kind != 1 ? 8.0 : 0.0) * stencil[mode] + (kind != 0 ? 16.0 : 0.0) * stencil[mode];
+        }
         j.bytes_per_pass += 4.0 * (double)n2 + (ms->masks ? (double)n2 : 0.0);
     }
     if (!(j.weight_total > 0.0)) return Status::make(FPM_ERR_NUMERICAL, "spectral iteration has no positive frame weight");
