@@ -690,6 +690,12 @@ typedef struct {
     /* scratch */
     cplx *patch, *exit_spec, *field, *projected, *difference, *spectrum, *pupil_gradient, *gradient;
     double *prediction;
+    /* GD illumination recovery: per-source (row, column) offset corrections,
+     * per-source (gradient row, column, curvature row, column, weight) of the
+     * batch, and per-frame scratch. NULL when off. */
+    double *corr, *ill, *calref, *fd_plus, *fd_minus;
+    uint8_t *dgmask;
+    cplx *fd_patch, *fd_field;
 } orc_state;
 
 static double frame_weight(const orc_problem *p, int f) { return p->weights ? p->weights[f] : 1.0; }
@@ -722,6 +728,25 @@ static void state_free(orc_state *s) {
     free(s->pupil_gradient);
     free(s->gradient);
     free(s->prediction);
+    free(s->corr);
+    free(s->ill);
+    free(s->calref);
+    free(s->fd_plus);
+    free(s->fd_minus);
+    free(s->dgmask);
+    free(s->fd_patch);
+    free(s->fd_field);
+}
+
+static void illumination_alloc(orc_state *s) {
+    s->corr = (double *)calloc(2 * (size_t)s->frames, sizeof(double));
+    s->ill = (double *)calloc(5 * (size_t)s->frames, sizeof(double));
+    s->calref = (double *)calloc(s->n_low, sizeof(double));
+    s->fd_plus = (double *)calloc(s->n_low, sizeof(double));
+    s->fd_minus = (double *)calloc(s->n_low, sizeof(double));
+    s->dgmask = (uint8_t *)calloc(s->n_low, 1);
+    s->fd_patch = (cplx *)calloc(s->n_low, sizeof(cplx));
+    s->fd_field = (cplx *)calloc(s->n_low, sizeof(cplx));
 }
 
 /* ReconstructionProblem::validate (src/reconstruction/problem.rs:35-72) and
@@ -826,13 +851,21 @@ static int32_t state_init(orc_state *s, const orc_problem *p) {
 
 static double src_off_row(const orc_problem *p, int s) { return p->off_row ? p->off_row[s] : 0.0; }
 static double src_off_col(const orc_problem *p, int s) { return p->off_col ? p->off_col[s] : 0.0; }
+/* ReconstructionState::effective_source_offset (src/reconstruction/state.rs:
+ * 245-267): the compiled offset plus the recovered illumination correction. */
+static double eff_off_row(const orc_state *s, int src) {
+    return src_off_row(s->p, src) + (s->corr ? s->corr[2 * src] : 0.0);
+}
+static double eff_off_col(const orc_state *s, int src) {
+    return src_off_col(s->p, src) + (s->corr ? s->corr[2 * src + 1] : 0.0);
+}
 
 /* Patch, pupil, ifftshift and inverse FFT: the coherent detector field of one
  * source (src/algorithms/common.rs:94-131, gradient_descent.rs:1184-1213). */
 static int32_t source_field(orc_state *s, int source) {
     const orc_problem *p = s->p;
     int32_t st = extract_patch_c(s->object, s->mh, s->mw, (long)p->start_row[source], (long)p->start_col[source],
-                                 s->h, s->w, src_off_row(p, source), src_off_col(p, source), s->patch);
+                                 s->h, s->w, eff_off_row(s, source), eff_off_col(s, source), s->patch);
     if (st) return st;
     for (size_t i = 0; i < s->n_low; ++i) s->exit_spec[i] = c_mul(s->patch[i], s->pupil[i]);
     ifftshift_c(s->exit_spec, s->field, s->h, s->w);
@@ -1064,7 +1097,92 @@ typedef struct {
     int constrain;
     double tv_weight, tv_epsilon;  /* object TV regulariser (0: off) */
     double smoothing;              /* pupil quadratic smoothing (0: off) */
+    int illumination;              /* finite-difference source-offset recovery */
+    double illumination_step, illumination_distance, illumination_bounds;
 } gd_pupil_config;
+
+/* CropIndices::validate_subpixel_inside (src/model/crop.rs:105-113). */
+static int offset_valid(const orc_problem *p, int source, double orow, double ocol) {
+    axis_interp a;
+    return interpolation_axis((long)p->start_row[source], p->h, p->mh, orow, &a) == ORC_OK &&
+           interpolation_axis((long)p->start_col[source], p->w, p->mw, ocol, &a) == ORC_OK;
+}
+
+/* |field|^2 of one source at the given offsets (compute_source_field,
+ * src/algorithms/gradient_descent.rs:1184-1213). */
+static int32_t intensity_at(orc_state *s, int source, double orow, double ocol, double *out) {
+    const orc_problem *p = s->p;
+    int32_t st = extract_patch_c(s->object, s->mh, s->mw, (long)p->start_row[source], (long)p->start_col[source],
+                                 s->h, s->w, orow, ocol, s->fd_patch);
+    if (st) return st;
+    for (size_t i = 0; i < s->n_low; ++i) s->fd_patch[i] = c_mul(s->fd_patch[i], s->pupil[i]);
+    ifftshift_c(s->fd_patch, s->fd_field, s->h, s->w);
+    fft2_c(s->fd_field, s->h, s->w, 1);
+    for (size_t i = 0; i < s->n_low; ++i) out[i] = c_norm_sqr(s->fd_field[i]);
+    return ORC_OK;
+}
+
+/* descent_curvature (src/algorithms/gradient_descent.rs:1340-1360). */
+static double descent_curvature(double predicted, double factor, int loss, double epsilon) {
+    double mean = fmax(predicted, epsilon);
+    switch (loss) {
+    case ORC_LOSS_AMPLITUDE_MSE: return 0.5 / mean;
+    case ORC_LOSS_INTENSITY_MSE: return 2.0;
+    case ORC_LOSS_POISSON_NLL: return 1.0 / mean;
+    default: {
+        double clipped = factor * 2.0 * sqrt(mean);
+        return fabs(clipped) < 1.0 ? 0.25 / mean : epsilon;
+    }
+    }
+}
+
+/* illumination_axis_gradient (src/algorithms/gradient_descent.rs:1272-1338):
+ * central (or one-sided at the grid edge) differences of the frame's
+ * intensity along one offset axis, chained with the loss derivative and its
+ * Gauss-Newton curvature over the retained pixels. */
+static int32_t illumination_axis(orc_state *s, int source, double orow, double ocol, double drow, double dcol, int loss,
+                                 double epsilon, double *gradient, double *curvature) {
+    double distance = fabs(drow) + fabs(dcol);
+    int plus_valid = offset_valid(s->p, source, orow + drow, ocol + dcol);
+    int minus_valid = offset_valid(s->p, source, orow - drow, ocol - dcol);
+    *gradient = *curvature = 0.0;
+    if (!plus_valid && !minus_valid) return ORC_OK;
+    int32_t st = ORC_OK;
+    if (plus_valid) st = intensity_at(s, source, orow + drow, ocol + dcol, s->fd_plus);
+    if (!st && minus_valid) st = intensity_at(s, source, orow - drow, ocol - dcol, s->fd_minus);
+    if (st) return st;
+    for (size_t i = 0; i < s->n_low; ++i) {
+        if (!s->dgmask[i]) continue;
+        double derivative = plus_valid && minus_valid ? (s->fd_plus[i] - s->fd_minus[i]) / (2.0 * distance)
+                            : plus_valid            ? (s->fd_plus[i] - s->calref[i]) / distance
+                                                    : (s->calref[i] - s->fd_minus[i]) / distance;
+        double factor = s->projected[i].re, predicted = s->projected[i].im;
+        *gradient += factor * derivative;
+        *curvature += descent_curvature(predicted, factor, loss, epsilon) * derivative * derivative;
+    }
+    return ORC_OK;
+}
+
+/* apply_illumination_update (src/algorithms/gradient_descent.rs:1044-1089):
+ * a bounded Gauss-Newton step on each source's correction, kept only when
+ * the corrected crop stays inside the grid. */
+static int32_t illumination_update(orc_state *s, const gd_pupil_config *cfg, double epsilon) {
+    for (int src = 0; src < s->frames; ++src) {
+        const double *acc = s->ill + 5 * (size_t)src;
+        if (acc[4] == 0.0) continue;
+        if (!isfinite(acc[0]) || !isfinite(acc[1]) || !isfinite(acc[2]) || !isfinite(acc[3]) || acc[2] < 0.0 ||
+            acc[3] < 0.0)
+            return fail(ORC_NUMERICAL, "illumination gradient or curvature for source %d is invalid", src);
+        double b = cfg->illumination_bounds;
+        double cr = fmin(fmax(s->corr[2 * src] - cfg->illumination_step * acc[0] / (acc[2] + epsilon), -b), b);
+        double cc = fmin(fmax(s->corr[2 * src + 1] - cfg->illumination_step * acc[1] / (acc[3] + epsilon), -b), b);
+        if (offset_valid(s->p, src, src_off_row(s->p, src) + cr, src_off_col(s->p, src) + cc)) {
+            s->corr[2 * src] = cr;
+            s->corr[2 * src + 1] = cc;
+        }
+    }
+    return ORC_OK;
+}
 
 /* apply_complex_tv_step (src/algorithms/regularization.rs:5-48): one step of
  * the smoothed isotropic TV gradient, accumulated in the reference's order. */
@@ -1161,6 +1279,8 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
     memset(s->gradient, 0, sizeof(cplx) * s->n_high);
     const int recover_pupil = pupil_cfg && pupil_cfg->recover;
     if (recover_pupil) memset(s->pupil_gradient, 0, sizeof(cplx) * n);
+    const int illumination = pupil_cfg && pupil_cfg->illumination && s->corr;
+    if (illumination) memset(s->ill, 0, sizeof(double) * 5 * (size_t)s->frames);
     long active = 0;
     for (int b = 0; b < count; ++b) {
         int frame = frames[b];
@@ -1179,6 +1299,7 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
         for (size_t i = 0; i < n; ++i) {
             if (mask && mask[i] == 0) {
                 s->projected[i] = cx(0.0, 0.0);
+                if (illumination) s->dgmask[i] = 0;
                 continue;
             }
             ++valid;
@@ -1187,6 +1308,7 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
             double target = fmax((measured[i] - bg) / gain, 0.0);
             frame_loss += point_loss(intrinsic, target, loss);
             const int retained = !truncate || orc_truncation_accepts(intrinsic, target, scale);
+            if (illumination) s->dgmask[i] = (uint8_t)retained;
             s->projected[i] = cx(retained ? descent_factor(intrinsic, target, loss, epsilon) : 0.0, intrinsic);
         }
         if (valid == 0) return fail(ORC_INVALID_MEASUREMENTS, "frame %d has no unmasked pixels", frame);
@@ -1195,6 +1317,8 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
         summary->weight_sum += fw;
         /* The reference recomputes the same field here; the object has not
          * changed, so the field from above is reused. */
+        if (illumination)
+            for (size_t i = 0; i < n; ++i) s->calref[i] = c_norm_sqr(s->field[i]);
         for (size_t i = 0; i < n; ++i) s->field[i] = c_scale(s->field[i], 1.0 * s->projected[i].re);
         fft2_c(s->field, s->h, s->w, 0);
         fftshift_c(s->field, s->spectrum, s->h, s->w);
@@ -1210,8 +1334,22 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
         for (size_t i = 0; i < n; ++i)
             s->difference[i] = c_divr(c_mul(c_conj(s->pupil[i]), s->spectrum[i]), max_pupil + epsilon);
         st = insert_adjoint_c(s->gradient, s->mh, s->mw, (long)p->start_row[frame], (long)p->start_col[frame], s->h,
-                              s->w, src_off_row(p, frame), src_off_col(p, frame), s->difference, fw * valid_scale);
+                              s->w, eff_off_row(s, frame), eff_off_col(s, frame), s->difference, fw * valid_scale);
         if (st) return st;
+        if (illumination) {
+            /* illumination_gradient (src/algorithms/gradient_descent.rs:1236-1270). */
+            double orow = eff_off_row(s, frame), ocol = eff_off_col(s, frame), d = pupil_cfg->illumination_distance;
+            double gr, cr, gc, cc;
+            st = illumination_axis(s, frame, orow, ocol, d, 0.0, loss, epsilon, &gr, &cr);
+            if (!st) st = illumination_axis(s, frame, orow, ocol, 0.0, d, loss, epsilon, &gc, &cc);
+            if (st) return st;
+            double *acc = s->ill + 5 * (size_t)frame;
+            acc[0] += fw * (gr / (double)valid);
+            acc[1] += fw * (gc / (double)valid);
+            acc[2] += fw * (cr / (double)valid);
+            acc[3] += fw * (cc / (double)valid);
+            acc[4] += fw;
+        }
     }
     if (active > 0) {
         double step = object_step / (double)active;
@@ -1241,6 +1379,7 @@ static int32_t gradient_step(orc_state *s, const int *frames, int count, double 
         for (size_t i = 0; i < n; ++i)
             if (support[i] == 0) s->pupil[i] = cx(0.0, 0.0);
     }
+    if (illumination) return illumination_update(s, pupil_cfg, epsilon);
     return ORC_OK;
 }
 
@@ -1564,7 +1703,10 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
             {
                 const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil,
                                             prm->object_tv_weight, prm->object_tv_epsilon,
-                                            prm->pupil_smoothing_weight};
+                                            prm->pupil_smoothing_weight, prm->recover_illumination,
+                                            prm->illumination_step, prm->illumination_finite_difference,
+                                            prm->illumination_bounds};
+                if (prm->recover_illumination && !s.corr) illumination_alloc(&s);
                 st = gradient_step(&s, order + start, count, prm->object_step, prm->epsilon, prm->loss_type,
                                    prm->poisson_truncation_threshold, &pc, &summary);
             }
@@ -1583,6 +1725,9 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
             ifftshift_c(s.object, (cplx *)out->object, s.mh, s.mw);
             fft2_c((cplx *)out->object, s.mh, s.mw, 1);
         }
+        if (out->illumination_corrections)
+            for (size_t i = 0; i < 2 * (size_t)s.frames; ++i)
+                out->illumination_corrections[i] = s.corr ? s.corr[i] : 0.0;
     }
     state_free(&s);
     return out->status = st;
@@ -2000,7 +2145,8 @@ int32_t orc_quadratic_smoothing_step(double *values, int32_t h, int32_t w, doubl
  * over the batch `frames`, from the given centred spectrum and pupil; the
  * state after the step is copied out. */
 int32_t orc_gd_batch_step(const orc_problem *p, const orc_params *prm, const double *spectrum, const double *pupil,
-                          const int32_t *frames, int32_t count, double *spectrum_out, double *pupil_out) {
+                          const int32_t *frames, int32_t count, double *spectrum_out, double *pupil_out,
+                          double *illumination_gradient_out) {
     orc_state s;
     int32_t st = state_init(&s, p);
     if (st) {
@@ -2015,13 +2161,21 @@ int32_t orc_gd_batch_step(const orc_problem *p, const orc_params *prm, const dou
     memcpy(s.object, spectrum, sizeof(cplx) * s.n_high);
     memcpy(s.pupil, pupil, sizeof(cplx) * s.n_low);
     const gd_pupil_config pc = {prm->recover_pupil, prm->pupil_step, prm->constrain_pupil, prm->object_tv_weight,
-                                prm->object_tv_epsilon, prm->pupil_smoothing_weight};
+                                prm->object_tv_epsilon, prm->pupil_smoothing_weight, prm->recover_illumination,
+                                prm->illumination_step, prm->illumination_finite_difference,
+                                prm->illumination_bounds};
+    if (prm->recover_illumination) illumination_alloc(&s);
     step_summary summary = {0.0, 0.0};
     st = gradient_step(&s, (const int *)frames, count, prm->object_step, prm->epsilon, prm->loss_type, 0.0, &pc,
                        &summary);
     if (!st) {
         memcpy(spectrum_out, s.object, sizeof(cplx) * s.n_high);
         memcpy(pupil_out, s.pupil, sizeof(cplx) * s.n_low);
+        if (illumination_gradient_out)
+            for (int src = 0; src < s.frames; ++src) {
+                illumination_gradient_out[2 * src] = s.ill ? s.ill[5 * (size_t)src] : 0.0;
+                illumination_gradient_out[2 * src + 1] = s.ill ? s.ill[5 * (size_t)src + 1] : 0.0;
+            }
     }
     state_free(&s);
     return st;

@@ -97,6 +97,8 @@ typedef struct {
     double progress_threshold, reduction_factor, minimum_object_step;  /* adaptive AP controller */
     double object_tv_weight, object_tv_epsilon;   /* GD object TV regulariser (weight 0: off) */
     double pupil_smoothing_weight;                /* GD pupil quadratic smoothing (0: off) */
+    int32_t recover_illumination;                 /* GD finite-difference source-offset recovery */
+    double illumination_step, illumination_finite_difference, illumination_bounds;
 } orc_params;
 
 /* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */
@@ -108,6 +110,7 @@ typedef struct {
     double *objectives;       /* iterations */
     double *object;           /* optional mh*mw complex real-space object */
     int32_t status;
+    double *illumination_corrections;  /* optional frames*2 (row, column) recovered offset corrections */
 } orc_output;
 
 const char *orc_last_error(void);
@@ -153,7 +156,7 @@ double orc_complex_nrmse(const double *reference, const double *candidate, int64
  * spectrum (mh*mw) and pupil (h*w); writes the stepped state. */
 int32_t orc_gd_batch_step(const orc_problem *problem, const orc_params *params, const double *spectrum,
                           const double *pupil, const int32_t *frames, int32_t count, double *spectrum_out,
-                          double *pupil_out);
+                          double *pupil_out, double *illumination_gradient_out);
 /* canonicalize_object_pupil (src/algorithms/gauge.rs:20-73) in place. */
 int32_t orc_canonicalize(const orc_problem *problem, double *spectrum, double *pupil);
 /* Mean point loss of one frame over its unmasked pixels (objective.rs:14-46). */

@@ -98,6 +98,8 @@ class _Params(C.Structure):
         ("poisson_truncation_threshold", C.c_double),
         ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
         ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
+        ("recover_illumination", C.c_int32), ("illumination_step", C.c_double),
+        ("illumination_finite_difference", C.c_double), ("illumination_bounds", C.c_double),
     ]
 
 
@@ -106,6 +108,7 @@ class _Output(C.Structure):
         ("object_spectrum", C.POINTER(C.c_double)), ("pupil", C.POINTER(C.c_double)),
         ("objectives", C.POINTER(C.c_double)), ("object", C.POINTER(C.c_double)),
         ("status", C.c_int32),
+        ("illumination_corrections", C.POINTER(C.c_double)),
     ]
 
 
@@ -369,7 +372,8 @@ def params(algorithm: str, **kw) -> _Params:
                gain_step=0.2, gain_min=1e-6, gain_max=1e6, recover_background=False,
                background_step=0.2, background_min=0.0, background_max=1e12, poisson_truncation_threshold=0.0,
                progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001, object_tv_weight=0.0,
-               object_tv_epsilon=1e-6, pupil_smoothing_weight=0.0)
+               object_tv_epsilon=1e-6, pupil_smoothing_weight=0.0, recover_illumination=False,
+               illumination_step=0.1, illumination_finite_difference=0.05, illumination_bounds=1.0)
     cfg.update(DEFAULTS[algorithm])
     cfg.update(kw)
     p = _Params()
@@ -382,13 +386,15 @@ def params(algorithm: str, **kw) -> _Params:
                  "pupil_step", "gain_step", "gain_min", "gain_max", "background_step",
                  "background_min", "background_max", "poisson_truncation_threshold", "progress_threshold",
                  "reduction_factor", "minimum_object_step", "object_tv_weight", "object_tv_epsilon",
-                 "pupil_smoothing_weight"):
+                 "pupil_smoothing_weight", "illumination_step", "illumination_finite_difference",
+                 "illumination_bounds"):
         setattr(p, name, float(cfg[name]))
     p.momentum_interval = int(cfg["momentum_interval"])
     p.recover_pupil = int(bool(cfg["recover_pupil"]))
     p.constrain_pupil = int(bool(cfg["constrain_pupil"]))
     p.recover_gains = int(bool(cfg["recover_gains"]))
     p.recover_background = int(bool(cfg["recover_background"]))
+    p.recover_illumination = int(bool(cfg["recover_illumination"]))
     return p
 
 
@@ -399,12 +405,14 @@ def _outputs(problem: Problem, prm: _Params):
         pupil=np.zeros((m["h"], m["w"]), np.complex128),
         objectives=np.zeros(prm.iterations),
         object=np.zeros((m["mh"], m["mw"]), np.complex128),
+        illumination_corrections=np.zeros((len(m["start_row"]), 2)),
     )
     out = _Output()
     out.object_spectrum = _ptr(arrays["object_spectrum"], C.c_double)
     out.pupil = _ptr(arrays["pupil"], C.c_double)
     out.objectives = _ptr(arrays["objectives"], C.c_double)
     out.object = _ptr(arrays["object"], C.c_double)
+    out.illumination_corrections = _ptr(arrays["illumination_corrections"], C.c_double)
     return out, arrays
 
 
@@ -558,16 +566,20 @@ def quadratic_smoothing_step(values, weight: float) -> np.ndarray:
     return out
 
 
-def gd_batch_step(problem: Problem, spectrum, pupil, frames, **kw):
-    """One gradient-descent step over the batch `frames` from the given state."""
+def gd_batch_step(problem: Problem, spectrum, pupil, frames, illumination_gradient: bool = False, **kw):
+    """One gradient-descent step over the batch `frames` from the given state.
+    With illumination_gradient, also returns the batch's per-source (row,
+    column) source-offset gradient (recover_illumination must be set)."""
     prm = params("gd", **kw)
     st = problem.struct()
     s_in, p_in = _c128(spectrum), _c128(pupil)
     s_out, p_out = np.zeros_like(s_in), np.zeros_like(p_in)
+    ill = np.zeros((len(problem.model["start_row"]), 2))
     f = np.ascontiguousarray(frames, np.int32)
     _check(lib().orc_gd_batch_step(C.byref(st), C.byref(prm), _ptr(s_in, C.c_double), _ptr(p_in, C.c_double),
-                                   _ptr(f, C.c_int32), f.size, _ptr(s_out, C.c_double), _ptr(p_out, C.c_double)))
-    return s_out, p_out
+                                   _ptr(f, C.c_int32), f.size, _ptr(s_out, C.c_double), _ptr(p_out, C.c_double),
+                                   _ptr(ill, C.c_double)))
+    return (s_out, p_out, ill) if illumination_gradient else (s_out, p_out)
 
 
 def frame_loss(problem: Problem, spectrum, pupil, frame: int, loss_type: str) -> float:

@@ -376,6 +376,70 @@ def test_gradient_minibatch_is_the_mean_of_frame_gradients(oracle_module):
     np.testing.assert_allclose(batched, expected, rtol=0, atol=1e-12)
 
 
+@pytest.mark.parametrize("loss", ["amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude"])
+def test_illumination_gradients_match_direct_loss_differences(oracle_module, loss):
+    # tests/reconstruction_tests.rs:2300-2374: the source-offset gradient of
+    # one GD step on frame 2 (every sixth pixel masked, a perturbed start)
+    # against central differences of the masked frame loss at offsets +-d on
+    # each axis, 5e-3 relative.
+    o = oracle_module
+    model = _direct_model()
+    rng = np.random.default_rng(9)
+    truth = np.exp(1j * 0.3 * rng.standard_normal((16, 16))) * (0.8 + 0.2 * rng.random((16, 16)))
+    data = o.forward_stack(o.Problem(model, None), o.object_spectrum(truth))
+    mask = (np.arange(64) % 6 != 1).astype(np.uint8).reshape(8, 8)
+    masks = np.broadcast_to(mask, data.shape).copy()
+    problem = o.Problem(model, data, masks=masks)
+    idx = np.arange(256).reshape(16, 16)
+    spectrum = o.object_spectrum(truth * 0.82 * np.exp(1j * 0.04 * (idx % 9) / 9.0))
+    pupil = model["pupil"]
+    frame, d = 2, 1e-4
+    _, _, gradient = o.gd_batch_step(problem, spectrum, pupil, [frame], illumination_gradient=True,
+                                     object_step=1e-12, loss_type=loss, recover_illumination=True,
+                                     illumination_step=1e-12, illumination_finite_difference=d)
+
+    def shifted_loss(drow, dcol):
+        m = dict(model, off_row=model["off_row"].copy(), off_col=model["off_col"].copy())
+        m["off_row"][frame] += drow
+        m["off_col"][frame] += dcol
+        return o.frame_loss(o.Problem(m, data, masks=masks), spectrum, pupil, frame, loss)
+
+    for axis, (drow, dcol) in enumerate([(d, 0.0), (0.0, d)]):
+        numerical = (shifted_loss(drow, dcol) - shifted_loss(-drow, -dcol)) / (2 * d)
+        analytical = gradient[frame, axis]
+        scale = max(abs(analytical), abs(numerical), 1e-10)
+        assert abs(analytical - numerical) <= 5e-3 * scale, (loss, axis, analytical, numerical)
+    assert np.all(gradient[[0, 1, 3, 4]] == 0.0)
+
+
+def test_illumination_update_honours_bounds_and_the_grid(oracle_module):
+    # GradientDescent::apply_illumination_update (src/algorithms/
+    # gradient_descent.rs:1044-1089): each step is clamped to the correction
+    # bound and kept only while the corrected crop stays inside the grid
+    # (CropIndices::validate_subpixel_inside, src/model/crop.rs:105-113).
+    o = oracle_module
+    model = _direct_model()
+    rng = np.random.default_rng(10)
+    truth = np.exp(1j * 0.4 * rng.standard_normal((16, 16))) * (0.7 + 0.3 * rng.random((16, 16)))
+    shifted = dict(model, off_row=model["off_row"].copy(), off_col=model["off_col"].copy())
+    shifted["off_row"][1], shifted["off_col"][1] = 0.3, -0.2
+    data = o.forward_stack(o.Problem(shifted, None), o.object_spectrum(truth))
+    out = o.run(o.Problem(model, data), "gd", iterations=20, recover_illumination=True, illumination_step=0.5,
+                illumination_bounds=0.1)
+    corr = out["illumination_corrections"]
+    # The displaced source saturates at the bound on the side of its displacement.
+    np.testing.assert_array_equal(corr[1], [0.1, -0.1])
+    assert np.all(np.abs(corr) <= 0.1)
+    # Crops touching the grid edge (rows 0 and 8, columns 0 and 8 of a
+    # 16-point grid with 8-point frames) only move inward.
+    edge = dict(model, start_row=np.array([0, 4, 4, 4, 8]), start_col=np.array([4, 0, 4, 8, 4]))
+    data = o.forward_stack(o.Problem(edge, None), o.object_spectrum(truth)) * 1.1
+    corr = o.run(o.Problem(edge, data), "gd", iterations=20, recover_illumination=True, illumination_step=1.0,
+                 illumination_bounds=0.5)["illumination_corrections"]
+    assert corr[0, 0] >= 0.0 and corr[4, 0] <= 0.0 and corr[1, 1] >= 0.0 and corr[3, 1] <= 0.0, corr
+    assert np.abs(corr).max() > 0.05
+
+
 def test_mpie_cadence_is_independent_of_batch_partitioning(oracle_module):
     # tests/reconstruction_tests.rs:693-731: bitwise equal spectra and traces.
     o = oracle_module
