@@ -489,4 +489,47 @@ cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, i
     return cudaGetLastError();
 }
 
+// apply_illumination_update (src/algorithms/gradient_descent.rs:1044-1089),
+// one thread per task of the batch: the frame's gradient and curvature are
+// its CTA partials (fixed order) times weight / unmasked pixels; a bounded
+// Gauss-Newton step is kept only while the corrected stencil stays inside the
+// grid, and then the frame's stencil fields follow it.
+__global__ void illumination_update_kernel(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
+                                           int n, int ctas, double step, double bound, double epsilon) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const IlluminationTask task = tasks[t];
+    const IlluminationTile& T = tiles[task.tile];
+    if (task.position >= T.frame_count) return;
+    const int f = T.order ? T.order[task.position] : task.position;
+    FrameParam fp = T.params[f];
+    if (fp.weight == 0.f || fp.loss_scale == 0.0) return;
+    double sum[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = 0; c < ctas; ++c)
+        for (int a = 0; a < 4; ++a) sum[a] += T.partials[((size_t)f * ctas + c) * 4 + a];
+    for (int a = 0; a < 4; ++a) sum[a] *= fp.loss_scale;
+    if (!isfinite(sum[0]) || !isfinite(sum[1]) || !isfinite(sum[2]) || !isfinite(sum[3]) || sum[2] < 0.0 ||
+        sum[3] < 0.0) {
+        atomicOr(T.status, 256);
+        return;
+    }
+    const double cr = fmin(fmax(T.correction[2 * f] - step * sum[0] / (sum[2] + epsilon), -bound), bound);
+    const double cc = fmin(fmax(T.correction[2 * f + 1] - step * sum[1] / (sum[3] + epsilon), -bound), bound);
+    if (offset_frame_param(T.start[2 * f], T.start[2 * f + 1], T.offset[2 * f] + cr, T.offset[2 * f + 1] + cc, n,
+                           T.M, fp)) {
+        T.correction[2 * f] = cr;
+        T.correction[2 * f + 1] = cc;
+        T.params[f] = fp;
+    }
+}
+
+cudaError_t launch_illumination_update(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
+                                       int n, int ctas, double step, double bound, double epsilon,
+                                       cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    illumination_update_kernel<<<(count + 127) / 128, 128, 0, s>>>(tiles, tasks, count, n, ctas, step, bound,
+                                                                   epsilon);
+    return cudaGetLastError();
+}
+
 }  // namespace fpm

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 struct fpm_context;
@@ -222,6 +223,87 @@ struct RegularTile {
 };
 cudaError_t launch_object_tv(const RegularTile* tiles, int count, int m, double epsilon, cudaStream_t s);
 cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, int constrain, cudaStream_t s);
+
+// GD illumination recovery (src/algorithms/gradient_descent.rs:1044-1089,
+// 1236-1368). Per tile: the run's own copy of the frame constants, whose
+// stencil fields follow the recovered offsets, the compiled crop starts and
+// offsets, and the (row, column) corrections in FP64.
+struct IlluminationTile {
+    const float2* object;      // M x (M + M % 2) centred spectrum (state)
+    const float2* pupil;       // N*N state pupil
+    const float* meas;         // engine layout, as TileDesc::meas
+    const uint8_t* masks;      // engine layout, or null
+    const float* background;   // engine layout, or null
+    long long background_stride;
+    FrameParam* params;        // [frame_count], rewritten by the update
+    const int* order;          // [frame_count] schedule, or null
+    const long long* start;    // [frame_count][2] crop start (row, column)
+    const double* offset;      // [frame_count][2] compiled subpixel offset
+    double* correction;        // [frame_count][2] recovered correction
+    double* partials;          // [frame_count][C][4] per-CTA (gradient row, column, curvature row, column)
+    int* status;               // bit 256: non-finite illumination gradient or curvature
+    int M, frame_count, amplitude;
+};
+// One gradient evaluation: order position `position` of tile `tile`.
+struct IlluminationTask {
+    int tile, position;
+};
+struct IlluminationParams {
+    const IlluminationTile* tiles;
+    const IlluminationTask* tasks;
+    double distance, epsilon;
+    int loss;
+};
+// One axis of interpolation_axis (src/model/crop.rs:266-313) in FP64: the
+// lower start and the upper fraction; false when the stencil leaves [0, m).
+__host__ __device__ inline bool offset_axis(long long start, int n, int m, double offset, long long& lower,
+                                            double& fraction) {
+    if (!(fabs(offset) <= 1.7976931348623157e308)) return false;
+    const double nearest = round(offset);
+    double integer_offset;
+    if (fabs(offset - nearest) <= 1e-12) {
+        integer_offset = nearest;
+        fraction = 0.0;
+    } else {
+        integer_offset = floor(offset);
+        fraction = offset - integer_offset;
+    }
+    lower = start + (long long)integer_offset;
+    const long long end = lower + n;
+    return lower >= 0 && end <= m && !(fraction > 0.0 && end >= m);
+}
+
+// Stencil of a crop at a subpixel offset (CropIndices::validate_subpixel_inside
+// and interpolation_axis, src/model/crop.rs:105-113, 266-313), the same
+// arithmetic as the host's frame constants; false when it leaves the M x M
+// grid. Keeps the frame's weight, gain and scale fields.
+__host__ __device__ inline bool offset_frame_param(long long start_row, long long start_col, double off_row,
+                                                   double off_col, int n, int m, FrameParam& fp) {
+    long long lr, lc;
+    double fr, fc;
+    if (!offset_axis(start_row, n, m, off_row, lr, fr) || !offset_axis(start_col, n, m, off_col, lc, fc)) return false;
+    if (fabs(off_row) <= 1e-12 && fabs(off_col) <= 1e-12) {
+        fp.lower_row = (int)start_row;
+        fp.lower_col = (int)start_col;
+        fp.has_upper_row = fp.has_upper_col = 0;
+        fp.w00 = 1.f;
+        fp.w01 = fp.w10 = fp.w11 = 0.f;
+        return true;
+    }
+    fp.lower_row = (int)lr;
+    fp.lower_col = (int)lc;
+    fp.has_upper_row = fr > 0.0 ? 1 : 0;
+    fp.has_upper_col = fc > 0.0 ? 1 : 0;
+    fp.w00 = (float)((1.0 - fr) * (1.0 - fc));
+    fp.w01 = (float)((1.0 - fr) * fc);
+    fp.w10 = (float)(fr * (1.0 - fc));
+    fp.w11 = (float)(fr * fc);
+    return true;
+}
+cudaError_t launch_illumination_gradient(int n, const IlluminationParams& p, int tasks, cudaStream_t s);
+cudaError_t launch_illumination_update(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
+                                       int n, int ctas, double step, double bound, double epsilon,
+                                       cudaStream_t s);
 
 // Context accessors for entry points that live outside runtime.cpp.
 void set_context_error(fpm_context* ctx, const char* message);

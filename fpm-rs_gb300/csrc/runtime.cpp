@@ -217,6 +217,9 @@ struct fpm_problem {
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
         pupil_gradient, tv_scratch, pupil_scratch;
+    // GD illumination recovery: the run's frame constants, crop starts and
+    // offsets, corrections and per-CTA gradient partials.
+    DeviceBuffer ill_params, ill_start, ill_offset, ill_correction, ill_partials;
     fpm_job* busy = nullptr;  // the submitted job that owns the problem until it finishes
 };
 
@@ -842,6 +845,21 @@ Status validate_params(const fpm_algorithm_params* a) {
             return Status::make(FPM_ERR_UNSUPPORTED,
                                 "gradient descent regularisers with Poisson truncation are not implemented on the "
                                 "GB300 device path");
+        if (a->recover_illumination) {
+            const struct {
+                double v;
+                const char* name;
+            } ill[3] = {{a->illumination_step, "illumination_step"},
+                        {a->illumination_finite_difference, "illumination_finite_difference"},
+                        {a->maximum_illumination_correction, "maximum_illumination_correction"}};
+            for (const auto& v : ill)
+                if (!std::isfinite(v.v) || v.v <= 0.0)
+                    return Status::make(FPM_ERR_INVALID_PARAMETER, "%s must be finite and positive", v.name);
+            if (a->recover_pupil || a->poisson_truncation)
+                return Status::make(FPM_ERR_UNSUPPORTED,
+                                    "illumination recovery with pupil recovery or Poisson truncation is not "
+                                    "implemented on the GB300 device path");
+        }
         if (a->poisson_truncation) {
             if (!std::isfinite(a->poisson_truncation_threshold) || a->poisson_truncation_threshold <= 0.0)
                 return Status::make(FPM_ERR_INVALID_PARAMETER,
@@ -899,14 +917,15 @@ Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) 
 
 // A problem's per-run buffers: bound to the stream of the run that uses them.
 std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
-    return {&p->object, &p->pupil_state, &p->partials, &p->counter, &p->status, &p->scratch64,
-            &p->velocity, &p->anchor, &p->order, &p->gradient, &p->pupil_gradient, &p->tv_scratch,
-            &p->pupil_scratch};
+    return {&p->object,     &p->pupil_state,   &p->partials,       &p->counter,    &p->status,
+            &p->scratch64,  &p->velocity,      &p->anchor,         &p->order,      &p->gradient,
+            &p->pupil_gradient, &p->tv_scratch, &p->pupil_scratch, &p->ill_params, &p->ill_start,
+            &p->ill_offset, &p->ill_correction, &p->ill_partials};
 }
 
 struct BucketRun {
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
-        tv_ptrs, tv_objects, tv_table, smooth_table;
+        tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
     cudaEvent_t first = nullptr, last = nullptr;
     int launches = 0;
@@ -932,13 +951,17 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     // GD regularisers run between per-batch engine launches.
     const bool tv = a->algorithm == FPM_ALG_GD && a->object_tv_weight > 0.0;
     const bool smoothing = gd_pupil && a->pupil_smoothing_weight > 0.0;
-    const bool regularised = tv || smoothing;
+    // Illumination recovery: a finite-difference gradient launch before and a
+    // correction update after each GD batch's engine launch.
+    const bool illum = a->algorithm == FPM_ALG_GD && a->recover_illumination;
+    const bool regularised = tv || smoothing || illum;
     const int iters = a->iterations;
     const bool resumed = !b.resume.empty();
     const int it0 = resumed ? b.resume[0]->completed_iterations : 0;
     std::vector<fpm::TileDesc> tiles(count);
     std::vector<fpm::InitTile> inits(count);
     std::vector<fpm::GaugeTile> gauges(count);
+    std::vector<fpm::IlluminationTile> ill_tiles(illum ? count : 0);
     std::vector<double2*> scratch(count);
     std::vector<float2*> objects(count), anchors(count), velocities(count);
     float max_pupil_power = 0.f;
@@ -1026,6 +1049,45 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.background_stride = p->background_stride;
         T.params = p->frame_params.as<fpm::FrameParam>();
         T.order = order_dev;
+        if (illum) {
+            // The run's own frame constants follow the recovered offsets; the
+            // problem's resident ones stay as compiled.
+            const int F = p->frames;
+            FPM_TRY(p->ill_params.ensure(sizeof(fpm::FrameParam) * F));
+            FPM_CUDA(cudaMemcpyAsync(p->ill_params.ptr, p->frame_params.ptr, sizeof(fpm::FrameParam) * F,
+                                     cudaMemcpyDeviceToDevice, s));
+            std::vector<long long> start(2 * (size_t)F);
+            std::vector<double> offset(2 * (size_t)F);
+            for (int f = 0; f < F; ++f) {
+                start[2 * f] = p->start_row[f];
+                start[2 * f + 1] = p->start_col[f];
+                offset[2 * f] = p->off_row[f];
+                offset[2 * f + 1] = p->off_col[f];
+            }
+            FPM_TRY(upload_array(p->ill_start, start, s));
+            FPM_TRY(upload_array(p->ill_offset, offset, s));
+            FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
+            FPM_CUDA(cudaMemsetAsync(p->ill_correction.ptr, 0, sizeof(double) * 2 * F, s));
+            FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * (size_t)C * F));
+            T.params = p->ill_params.as<fpm::FrameParam>();
+            fpm::IlluminationTile& L = ill_tiles[t];
+            L.object = T.object;
+            L.pupil = T.pupil;
+            L.meas = T.meas;
+            L.masks = T.masks;
+            L.background = T.background;
+            L.background_stride = T.background_stride;
+            L.params = p->ill_params.as<fpm::FrameParam>();
+            L.order = order_dev;
+            L.start = p->ill_start.as<long long>();
+            L.offset = p->ill_offset.as<double>();
+            L.correction = p->ill_correction.as<double>();
+            L.partials = p->ill_partials.as<double>();
+            L.status = p->status.as<int>();
+            L.M = M;
+            L.frame_count = F;
+            L.amplitude = T.amplitude;
+        }
         T.velocity = mpie ? p->velocity.as<float2>() : nullptr;
         T.anchor = mpie ? p->anchor.as<float2>() : nullptr;
         T.gradient = gd_batched ? p->gradient.as<float2>() : nullptr;
@@ -1090,7 +1152,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     }
     for (DeviceBuffer* buf : {&br.tiles, &br.init, &br.gauge, &br.scratch_ptrs, &br.object_ptrs, &br.anchor_ptrs,
                               &br.velocity_ptrs, &br.avg, &br.init_partial, &br.tv_ptrs, &br.tv_objects,
-                              &br.tv_table, &br.smooth_table})
+                              &br.tv_table, &br.smooth_table, &br.ill_tiles, &br.ill_tasks})
         buf->bind(ctx->pool, s);
     FPM_CUDA(cudaEventCreate(&br.first));
     FPM_CUDA(cudaEventCreate(&br.last));
@@ -1202,12 +1264,41 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
         FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
         FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
+        // Illumination tasks of batch k: [k * count * B, (k + 1) * count * B).
+        fpm::IlluminationParams ip{};
+        if (illum) {
+            std::vector<fpm::IlluminationTask> tasks;
+            tasks.reserve((size_t)nb * count * B);
+            for (int k = 0; k < nb; ++k)
+                for (int t = 0; t < count; ++t)
+                    for (int j = 0; j < B; ++j) tasks.push_back({t, k * B + j});
+            FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
+            FPM_TRY(upload_array(br.ill_tasks, tasks, s));
+            ip.tiles = br.ill_tiles.as<fpm::IlluminationTile>();
+            ip.distance = a->illumination_finite_difference;
+            ip.epsilon = a->epsilon;
+            ip.loss = a->loss_type;
+        }
+        const int batch_tasks = count * B;
         for (int it = it0; it < iters; ++it) {
             for (int k = 0; k < nb; ++k) {
                 ep.frame_begin = k * B;
                 ep.frame_end = (k + 1) * B;
                 ep.accumulate = k > 0 ? 1 : 0;
+                if (illum) {
+                    // illumination_gradient from the batch-start object and
+                    // pupil (src/algorithms/gradient_descent.rs:590-613).
+                    ip.tasks = br.ill_tasks.as<fpm::IlluminationTask>() + (size_t)k * batch_tasks;
+                    FPM_CUDA(fpm::launch_illumination_gradient(N, ip, batch_tasks, s));
+                    br.launches += 1;
+                }
                 FPM_TRY(engine(it, it + 1));
+                if (illum) {
+                    FPM_CUDA(fpm::launch_illumination_update(br.ill_tiles.as<fpm::IlluminationTile>(), ip.tasks,
+                                                             batch_tasks, N, C, a->illumination_step,
+                                                             a->maximum_illumination_correction, a->epsilon, s));
+                    br.launches += 1;
+                }
                 if (tv) {
                     // apply_object_tv (src/algorithms/gradient_descent.rs:1125-1165) in FP64.
                     FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(br.object_ptrs.ptr),
@@ -1280,6 +1371,9 @@ Status queue_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_d
         FPM_CUDA(cudaMemcpyAsync(p->host_partials.data(), p->partials.ptr, sizeof(double) * p->host_partials.size(),
                                  cudaMemcpyDeviceToHost, s));
     }
+    if (r->illumination_corrections && a->algorithm == FPM_ALG_GD && a->recover_illumination)
+        FPM_CUDA(cudaMemcpyAsync(r->illumination_corrections, p->ill_correction.ptr, sizeof(double) * 2 * p->frames,
+                                 cudaMemcpyDeviceToHost, s));
     return Status::ok();
 }
 
@@ -1338,6 +1432,7 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 32) return Status::make(FPM_ERR_NUMERICAL, "adaptive alternating projection produced an invalid pass objective");
     if (status & 64) return Status::make(FPM_ERR_NUMERICAL, "pupil update produced a non-finite value");
     if (status & 128) return Status::make(FPM_ERR_NUMERICAL, "regularization produced a non-finite value");
+    if (status & 256) return Status::make(FPM_ERR_NUMERICAL, "illumination gradient or curvature is invalid");
     if (!r) return Status::ok();
     const int C = fpm::engine_ctas(p->n);
     if (r->objectives) fill_objectives(p, a, r->objectives);
@@ -1409,6 +1504,9 @@ Status validate_resume(int count, fpm_problem* const* problems, const fpm_algori
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     if (resume && a->algorithm == FPM_ALG_ADAPTIVE_AP)
         return Status::make(FPM_ERR_UNSUPPORTED, "adaptive alternating projection does not resume on the GB300 device path");
+    if ((resume || capture) && a->algorithm == FPM_ALG_GD && a->recover_illumination)
+        return Status::make(FPM_ERR_UNSUPPORTED,
+                            "illumination recovery does not checkpoint or resume on the GB300 device path");
     for (int i = 0; i < count && resume; ++i) {
         const fpm_state_desc& r = resume[i];
         const fpm_problem* p = problems[i];

@@ -75,6 +75,8 @@ class AlgorithmParams(C.Structure):
         ("poisson_truncation", C.c_int32), ("poisson_truncation_threshold", C.c_double),
         ("progress_threshold", C.c_double), ("reduction_factor", C.c_double), ("minimum_object_step", C.c_double),
         ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
+        ("recover_illumination", C.c_int32), ("illumination_step", C.c_double),
+        ("illumination_finite_difference", C.c_double), ("maximum_illumination_correction", C.c_double),
     ]
 
 
@@ -122,6 +124,7 @@ class ResultDesc(C.Structure):
         ("object", C.POINTER(C.c_double)), ("object_spectrum", C.POINTER(C.c_double)),
         ("pupil", C.POINTER(C.c_double)), ("objectives", C.POINTER(C.c_double)),
         ("completed_iterations", C.c_int32),
+        ("illumination_corrections", C.POINTER(C.c_double)),
     ]
 
 

@@ -311,8 +311,17 @@ class GradientDescent(_Algorithm):
         self.object_tv, self.pupil_smoothing = object_tv, pupil_smoothing
         self.parallel_workers = parallel_workers
         self.object_tv_epsilon = object_tv_epsilon
-        if recover_illumination:
-            raise UnsupportedError("illumination recovery is not implemented on the GB300 device path")
+        self.illumination_step = illumination_step
+        self.illumination_finite_difference = illumination_finite_difference
+        self.illumination_bounds = illumination_bounds
+        # GradientDescent::validate (src/algorithms/gradient_descent.rs:333-355).
+        for name in ("illumination_step", "illumination_finite_difference", "illumination_bounds"):
+            value = getattr(self, name)
+            if not (isinstance(value, (int, float)) and math.isfinite(value) and value > 0):
+                raise InvalidParameterError(f"{name} must be finite and positive")
+        if recover_illumination and (recover_pupil or poisson_truncation_threshold is not None):
+            raise UnsupportedError("illumination recovery with pupil recovery or Poisson truncation is not "
+                                   "implemented on the GB300 device path")
 
     def _params(self, schedule):
         p = _base_params(self, schedule, self.iterations, self.object_step, self.batch_size, self.epsilon,
@@ -326,6 +335,10 @@ class GradientDescent(_Algorithm):
         p.object_tv_weight = float(self.object_tv)
         p.object_tv_epsilon = float(self.object_tv_epsilon)
         p.pupil_smoothing_weight = float(self.pupil_smoothing)
+        p.recover_illumination = int(bool(self.recover_illumination))
+        p.illumination_step = float(self.illumination_step)
+        p.illumination_finite_difference = float(self.illumination_finite_difference)
+        p.maximum_illumination_correction = float(self.illumination_bounds)
         return p
 
 
@@ -352,6 +365,22 @@ def upload(problems) -> None:
     for p, h in zip(pending, handles):
         p._handle = C.c_void_p(h)
         p._ctx = ctx
+
+
+def _result_arrays(problem, params, desc) -> dict:
+    """Host arrays of one problem's results, bound into its ResultDesc."""
+    mh, mw = problem.reconstruction_shape
+    h, w = problem.image_shape
+    a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
+             pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)),
+             illumination=np.zeros((problem.model.source_count, 2)) if params.recover_illumination else None)
+    desc.object = N.ptr(a["object"], C.c_double)
+    desc.object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
+    desc.pupil = N.ptr(a["pupil"], C.c_double)
+    desc.objectives = N.ptr(a["objectives"], C.c_double)
+    if a["illumination"] is not None:
+        desc.illumination_corrections = N.ptr(a["illumination"], C.c_double)
+    return a
 
 
 def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=None, schedule="sequential",
@@ -382,16 +411,7 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
     results = (N.ResultDesc * len(problems))()
     arrays = []
     if download:
-        for i, p in enumerate(problems):
-            mh, mw = p.reconstruction_shape
-            h, w = p.image_shape
-            a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
-                     pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)))
-            results[i].object = N.ptr(a["object"], C.c_double)
-            results[i].object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
-            results[i].pupil = N.ptr(a["pupil"], C.c_double)
-            results[i].objectives = N.ptr(a["objectives"], C.c_double)
-            arrays.append(a)
+        arrays = [_result_arrays(p, params, results[i]) for i, p in enumerate(problems)]
     start = time.perf_counter()
     if host_path:
         descs = [p._descriptors() for p in problems]
@@ -417,7 +437,8 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
             object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
             pupil_support=p.model.pupil_support, trace=trace,
             runtime=RuntimeInfo(elapsed, params.iterations, False, algorithm._name),
-            recovered_frame_gains=gains, recovered_background=p.model._background)
+            recovered_frame_gains=gains, recovered_background=p.model._background,
+            calibrated_illumination=a["illumination"])
         if p.name is not None:
             result.metadata["problem_name"] = p.name
         out.append(result)
@@ -481,7 +502,8 @@ class Job:
                 object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
                 pupil_support=p.model.pupil_support, trace=trace,
                 runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
-                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background)
+                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                calibrated_illumination=a["illumination"])
             if p.name is not None:
                 result.metadata["problem_name"] = p.name
             out.append(result)
@@ -504,16 +526,7 @@ def submit_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> J
     handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
     results = (N.ResultDesc * len(problems))()
     arrays = []
-    for i, p in enumerate(problems):
-        mh, mw = p.reconstruction_shape
-        h, w = p.image_shape
-        a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
-                 pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)))
-        results[i].object = N.ptr(a["object"], C.c_double)
-        results[i].object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
-        results[i].pupil = N.ptr(a["pupil"], C.c_double)
-        results[i].objectives = N.ptr(a["objectives"], C.c_double)
-        arrays.append(a)
+    arrays = [_result_arrays(p, params, results[i]) for i, p in enumerate(problems)]
     ctx = N.context()
     handle = C.c_void_p()
     submitted = time.perf_counter()

@@ -142,6 +142,16 @@ typedef struct {
      * when on) and, with pupil recovery, a quadratic smoothing step on the
      * pupil before its support is imposed. */
     double object_tv_weight, object_tv_epsilon, pupil_smoothing_weight;
+    /* GD illumination recovery (GradientDescent::recover_illumination,
+     * src/algorithms/gradient_descent.rs:146-153, 1044-1089, 1236-1368): per
+     * source, a Gauss-Newton step of illumination_step on finite differences
+     * at +-illumination_finite_difference subpixels, clamped to
+     * +-maximum_illumination_correction and kept only while the corrected crop
+     * stays inside the grid. The three values are validated (finite and
+     * positive) when recover_illumination is set. Not combined with pupil
+     * recovery, Poisson truncation or resumed runs on the device path. */
+    int32_t recover_illumination;
+    double illumination_step, illumination_finite_difference, maximum_illumination_correction;
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */
@@ -151,6 +161,10 @@ typedef struct {
     double *pupil;           /* complex128 [h*w] recovered pupil */
     double *objectives;      /* [iterations] weighted mean objective per iteration */
     int32_t completed_iterations;
+    /* [sources*2] recovered (row, column) illumination corrections
+     * (ReconstructionResult::calibrated_illumination, src/reconstruction/
+     * result.rs:94); written only by runs with recover_illumination. */
+    double *illumination_corrections;
 } fpm_result_desc;
 
 /* ------------------------------------------------------------------ context */

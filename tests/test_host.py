@@ -125,7 +125,10 @@ def test_unsupported_options_fail_before_device_work(fpm):
     with pytest.raises(fpm.UnsupportedError):
         fpm.AlternatingProjection(iterations=1).run(problem, callbacks=[object()])
     with pytest.raises(fpm.UnsupportedError):
-        fpm.GradientDescent(recover_illumination=True)
+        fpm.GradientDescent(recover_illumination=True, recover_pupil=True)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.GradientDescent(recover_illumination=True, illumination_step=0.0)
+    fpm.GradientDescent(recover_illumination=True, object_tv=0.1)  # device illumination recovery
     fpm.GradientDescent(object_tv=0.1, recover_pupil=True, pupil_smoothing=0.02)  # device regularisers
     with pytest.raises(ValueError):
         fpm.Mpie(loss_type="l1")
