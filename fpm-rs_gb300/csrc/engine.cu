@@ -37,11 +37,6 @@ cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t 
 
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s) { FPM_DISPATCH(forward(p, s)) }
 
-cudaError_t launch_illumination_gradient(int n, const IlluminationParams& p, int tasks, cudaStream_t s) {
-    if (tasks <= 0) return cudaSuccess;
-    FPM_DISPATCH(illumination(p, tasks, s))
-}
-
 cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s) {
     FPM_DISPATCH(permute_f64(src, dst, frames, s))
 }

@@ -1194,156 +1194,6 @@ FPM_DEVICE int perm_index(int y, int x) {
     return (c * K::R + m) * K::N + K::NB * ka + kb;
 }
 
-// descent_curvature (src/algorithms/gradient_descent.rs:1340-1360) in FP32.
-FPM_DEVICE float descent_curvature(float predicted, float factor, int loss, float eps) {
-    const float mean = fmaxf(predicted, eps);
-    switch (loss) {
-        case 0: return 0.5f / mean;
-        case 1: return 2.f;
-        case 2: return 1.f / mean;
-        default: return fabsf(factor * 2.f * sqrtf(mean)) < 1.f ? 0.25f / mean : eps;
-    }
-}
-
-// Source-offset gradient of gradient descent with illumination recovery
-// (illumination_gradient and illumination_axis_gradient, src/algorithms/
-// gradient_descent.rs:1236-1338). Cluster t takes task t: the frame at one
-// order position of one tile, from the batch-start object and pupil. It
-// evaluates the frame's intensity at its current offset (evaluation 0: the
-// loss derivative and the retained pixels, as in the engine's gradient step)
-// and at +-d along rows (1, 2) and columns (3, 4), skipping displaced
-// stencils that leave the grid, and stores per CTA the retained-pixel sums of
-// factor * dI/do and curvature * (dI/do)^2 for each axis. Every thread keeps
-// its own 16 pixels across the evaluations; the thread-to-pixel map is that
-// of forward_kernel.
-template <int N_>
-// Register cap as the engine's, so a 16-CTA cluster fits 8 SMs.
-__global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) illumination_kernel(const IlluminationParams P) {
-    using K = Cfg<N_>;
-    constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[K::WARPS][4];
-    float2* field = reinterpret_cast<float2*>(smem_raw);
-    float2* fld = field + K::RS;
-    float2* osm = field + K::FIELD;
-    float2* pslab = osm + K::STAGE;
-    float2* tw = pslab + K::PSLAB;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int c = C == 1 ? 0 : (int)(blockIdx.x % C);
-    const int i_lo = C == 1 ? 0 : c * R;
-    const IlluminationTask task = P.tasks[blockIdx.x / C];
-    const IlluminationTile& T = P.tiles[task.tile];
-    // Uniform across the cluster: no CTA has touched a peer yet.
-    if (task.position >= T.frame_count) return;
-    const int f = T.order ? T.order[task.position] : task.position;
-    const FrameParam base = T.params[f];
-    if (base.weight == 0.f) return;
-    const long long ostride = T.M + (T.M & 1);
-    for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
-    load_pupil_slab<K>(pslab, T.pupil, c);
-
-    // Displaced stencils: offset = compiled + correction +- d on one axis.
-    const double orow = T.offset[2 * f] + T.correction[2 * f];
-    const double ocol = T.offset[2 * f + 1] + T.correction[2 * f + 1];
-    const long long srow = T.start[2 * f], scol = T.start[2 * f + 1];
-    FrameParam disp[4];
-    bool ok[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        disp[e] = base;
-        const double sign = (e & 1) ? -P.distance : P.distance;
-        ok[e] = offset_frame_param(srow, scol, e < 2 ? orow + sign : orow, e < 2 ? ocol : ocol + sign, N, T.M,
-                                   disp[e]);
-    }
-
-    const int q = R == 32 ? (warp << 4) | (lane & 15) : tid, h = R == 32 ? lane >> 4 : 0;
-    const int x = q / NB + NA * (q % NB);
-    const size_t frame_base = (size_t)f * N * N;
-    float factor[16], pred[16], plus[16];
-    unsigned kept = 0u;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const float inv_gain = 1.f / base.gain;
-    const float eps = (float)P.epsilon;
-    const float inv_d = (float)(1.0 / P.distance), inv_2d = (float)(0.5 / P.distance);
-    for (int e = 0; e < 5; ++e) {
-        if (e > 0 && !ok[e - 1]) continue;  // uniform: every thread computed the same flags
-        const FrameParam& fp = e == 0 ? base : disp[e - 1];
-        stage_object<K>(osm, T.object, T.M, ostride, fp, i_lo, 0, N - 1);
-        __syncthreads();
-        float amax = 0.f, bmax = 0.f;
-        rows_inverse<K, false>(fld, osm + (fp.lower_col & 1), tw, pslab, fp, c, i_lo, 0, N - 1, amax, bmax);
-        cluster_barrier<K>();
-        if constexpr (C > 1) {
-            columns_cross_inverse<K>(fld, tw, c, 0, N - 1);
-            cluster_barrier<K>();
-        }
-        float2 v[16];
-        if constexpr (R == 32) column_inverse_split<K>(fld, phys<K>(q), h, tw, v);
-        else column_inverse_local<K>(fld, phys<K>(q), v);
-        if (e == 0) {
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                const int y = c + C * (R == 32 ? h + 2 * k : k);
-                const int idx = perm_index<K>(y, x);
-                const float m = __ldg(T.meas + frame_base + idx);
-                bool valid;
-                float target;
-                if (T.amplitude) {
-                    valid = m >= 0.f;
-                    target = m * m;
-                } else {
-                    valid = !T.masks || T.masks[frame_base + idx] != 0;
-                    const float bg = T.background ? __ldg(T.background + (size_t)f * T.background_stride + idx) : 0.f;
-                    target = fmaxf((m - bg) * inv_gain, 0.f);
-                }
-                const float intrinsic = cnorm2(v[k]);
-                pred[k] = intrinsic;
-                factor[k] = valid ? descent_factor<-1>(intrinsic, target, P.loss, eps) : 0.f;
-                kept |= valid ? 1u << k : 0u;
-            }
-        } else if (e == 1 || e == 3) {
-#pragma unroll
-            for (int k = 0; k < 16; ++k) plus[k] = cnorm2(v[k]);
-            // Without a valid minus stencil the derivative is one-sided now.
-            if (!ok[e]) {
-                const int a = e == 1 ? 0 : 1;
-#pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    if (!((kept >> k) & 1u)) continue;
-                    const float d = (plus[k] - pred[k]) * inv_d;
-                    acc[a] += (double)(factor[k] * d);
-                    acc[2 + a] += (double)(descent_curvature(pred[k], factor[k], P.loss, eps) * d * d);
-                }
-            }
-        } else {
-            const int a = e == 2 ? 0 : 1;
-            const bool two = ok[e - 2];
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                if (!((kept >> k) & 1u)) continue;
-                const float minus = cnorm2(v[k]);
-                const float d = two ? (plus[k] - minus) * inv_2d : (pred[k] - minus) * inv_d;
-                acc[a] += (double)(factor[k] * d);
-                acc[2 + a] += (double)(descent_curvature(pred[k], factor[k], P.loss, eps) * d * d);
-            }
-        }
-        // The next evaluation rewrites the stage and the field.
-        cluster_barrier<K>();
-    }
-    // Per-CTA sums in a fixed order: warps, then thread 0 over warps.
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const double s = warp_sum(acc[a]);
-        if (lane == 0) red[warp][a] = s;
-    }
-    __syncthreads();
-    if (tid < 4) {
-        double total = 0.0;
-        for (int w = 0; w < K::WARPS; ++w) total += red[w][tid];
-        T.partials[((size_t)f * C + c) * 4 + tid] = total;
-    }
-}
-
 template <int N_>
 __global__ void permute_f64_kernel(const double* __restrict__ src, float* __restrict__ dst, long long frames) {
     using K = Cfg<N_>;
@@ -1534,10 +1384,6 @@ struct EngineEntry {
 
     static cudaError_t forward(const ForwardParams& p, cudaStream_t s) {
         return launch_cluster<N_>(forward_kernel<N_>, p, p.frame_count, s);
-    }
-
-    static cudaError_t illumination(const IlluminationParams& p, int tasks, cudaStream_t s) {
-        return launch_cluster<N_>(illumination_kernel<N_>, p, tasks, s);
     }
 
     static cudaError_t permute_f64(const double* src, float* dst, long long frames, cudaStream_t s) {

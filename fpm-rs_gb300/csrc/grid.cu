@@ -489,25 +489,198 @@ cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, i
     return cudaGetLastError();
 }
 
+// ------------------------------------------------ illumination recovery
+
+// Natural detector (y, x) -> engine layout index of an n x n frame (the
+// frame engine's CTA-row and digit permutation).
+__device__ int engine_index(int n, int y, int x) {
+    const int r = n >= 128 ? 16 : 32, c = n / r, na = n >= 128 ? 16 : 8, nb = n / na;
+    return ((y % c) * r + y / c) * n + nb * (x % na) + x / na;
+}
+
+__device__ bool task_frame(const IlluminationTile& T, const IlluminationTask& task, int& f) {
+    if (task.position >= T.frame_count) return false;
+    f = T.order ? T.order[task.position] : task.position;
+    return T.params[f].weight != 0.f;
+}
+
+// compute_source_field (src/algorithms/gradient_descent.rs:1184-1213) for
+// evaluation e of a task: the bilinear FP64 patch of the state at the
+// offset (compiled + correction, +-d on one axis for e > 0) times the
+// pupil, ifftshifted into the inverse FFT's input. blockIdx.y = task * 5 + e.
+__global__ void illumination_fields_kernel(const IlluminationParams P) {
+    const int task_index = blockIdx.y / 5, e = blockIdx.y % 5;
+    const IlluminationTask task = P.tasks[task_index];
+    const IlluminationTile& T = P.tiles[task.tile];
+    const int n = P.n;
+    double2* out = P.fields + (size_t)blockIdx.y * n * n;
+    int f = 0;
+    bool ok = task_frame(T, task, f);
+    long long lr = 0, lc = 0;
+    double fr = 0.0, fc = 0.0;
+    if (ok) {
+        const double d = (e == 2 || e == 4) ? -P.distance : P.distance;
+        const double orow = T.offset[2 * f] + T.correction[2 * f] + (e == 1 || e == 2 ? d : 0.0);
+        const double ocol = T.offset[2 * f + 1] + T.correction[2 * f + 1] + (e >= 3 ? d : 0.0);
+        ok = offset_axis(T.start[2 * f], n, T.M, orow, lr, fr) && offset_axis(T.start[2 * f + 1], n, T.M, ocol, lc, fc);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.valid[blockIdx.y] = ok ? 1 : 0;
+    if (!ok) {
+        // Skipped evaluation: a defined (zero) field through the FFT.
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n * n; p += gridDim.x * blockDim.x)
+            out[p] = make_double2(0.0, 0.0);
+        return;
+    }
+    const long long ostride = T.M + (T.M & 1);
+    const int half = n / 2;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n * n; p += gridDim.x * blockDim.x) {
+        const int i = p / n, j = p % n;  // centred patch coordinates
+        const float2* row0 = T.object + (lr + i) * ostride + lc + j;
+        const float2 a = row0[0];
+        double re = (1.0 - fr) * (1.0 - fc) * a.x, im = (1.0 - fr) * (1.0 - fc) * a.y;
+        if (fc > 0.0) {
+            const float2 b = row0[1];
+            re += (1.0 - fr) * fc * b.x;
+            im += (1.0 - fr) * fc * b.y;
+        }
+        if (fr > 0.0) {
+            const float2 c = row0[ostride];
+            re += fr * (1.0 - fc) * c.x;
+            im += fr * (1.0 - fc) * c.y;
+            if (fc > 0.0) {
+                const float2 g = row0[ostride + 1];
+                re += fr * fc * g.x;
+                im += fr * fc * g.y;
+            }
+        }
+        const float2 pu = T.pupil[p];
+        const double2 v = make_double2(re * pu.x - im * pu.y, re * pu.y + im * pu.x);
+        out[(size_t)((i + half) % n) * n + (j + half) % n] = v;
+    }
+}
+
+cudaError_t launch_illumination_fields(const IlluminationParams& p, int tasks, cudaStream_t s) {
+    if (tasks <= 0) return cudaSuccess;
+    const int blocks = (p.n * p.n + 255) / 256 < 64 ? (p.n * p.n + 255) / 256 : 64;
+    illumination_fields_kernel<<<dim3(blocks, tasks * 5), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// descent_factor and descent_curvature (src/algorithms/gradient_descent.rs:
+// 1167-1178, 1340-1360) in FP64.
+__device__ double gd_factor(double predicted, double measured, int loss, double eps) {
+    switch (loss) {
+        case 0: return 1.0 - sqrt(fmax(measured, 0.0)) / sqrt(fmax(predicted, eps));
+        case 1: return 2.0 * (predicted - measured);
+        case 2: return 1.0 - fmax(measured, 0.0) / fmax(predicted, eps);
+        default: {
+            const double pa = sqrt(fmax(predicted, eps));
+            return fmin(fmax(pa - sqrt(fmax(measured, 0.0)), -1.0), 1.0) / (2.0 * pa);
+        }
+    }
+}
+
+__device__ double gd_curvature(double predicted, double factor, int loss, double eps) {
+    const double mean = fmax(predicted, eps);
+    switch (loss) {
+        case 0: return 0.5 / mean;
+        case 1: return 2.0;
+        case 2: return 1.0 / mean;
+        default: return fabs(factor * 2.0 * sqrt(mean)) < 1.0 ? 0.25 / mean : eps;
+    }
+}
+
+// illumination_axis_gradient (src/algorithms/gradient_descent.rs:1272-1338):
+// one block per task; over the pixels the gradient step retains (unmasked,
+// no truncation), the loss derivative at the current offset times central
+// (or, at the grid edge, one-sided) differences of the intensity, and the
+// Gauss-Newton curvature times their squares, per axis, summed in a fixed
+// order into the frame's partials.
+constexpr int kIllumReduceThreads = 256;
+
+__global__ void __launch_bounds__(kIllumReduceThreads) illumination_reduce_kernel(const IlluminationParams P) {
+    __shared__ double red[kIllumReduceThreads / 32][4];
+    const IlluminationTask task = P.tasks[blockIdx.x];
+    const IlluminationTile& T = P.tiles[task.tile];
+    int f = 0;
+    if (!task_frame(T, task, f)) return;
+    const int n = P.n;
+    const size_t n2 = (size_t)n * n;
+    const int* valid = P.valid + (size_t)blockIdx.x * 5;
+    const double2* field = P.fields + (size_t)blockIdx.x * 5 * n2;
+    const bool ok[5] = {valid[0] != 0, valid[1] != 0, valid[2] != 0, valid[3] != 0, valid[4] != 0};
+    if (!ok[0]) return;  // the current stencil is always inside the grid
+    const double gain = (double)T.params[f].gain;
+    const double d = P.distance;
+    const size_t frame_base = (size_t)f * n2;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int p = threadIdx.x; p < n * n; p += blockDim.x) {
+        const int idx = engine_index(n, p / n, p % n);
+        const double m = (double)T.meas[frame_base + idx];
+        bool keep;
+        double target;
+        if (T.amplitude) {
+            keep = m >= 0.0;
+            target = m * m;
+        } else {
+            keep = !T.masks || T.masks[frame_base + idx] != 0;
+            const double bg = T.background ? (double)T.background[(size_t)f * T.background_stride + idx] : 0.0;
+            target = fmax((m - bg) / gain, 0.0);
+        }
+        if (!keep) continue;
+        const double2 f0 = field[p];
+        const double pred = f0.x * f0.x + f0.y * f0.y;
+        const double factor = gd_factor(pred, target, P.loss, P.epsilon);
+        const double curv = gd_curvature(pred, factor, P.loss, P.epsilon);
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            const bool plus = ok[1 + 2 * a], minus = ok[2 + 2 * a];
+            if (!plus && !minus) continue;
+            const double2 fp = field[(size_t)(1 + 2 * a) * n2 + p];
+            const double2 fm = field[(size_t)(2 + 2 * a) * n2 + p];
+            const double ip = fp.x * fp.x + fp.y * fp.y, im = fm.x * fm.x + fm.y * fm.y;
+            const double der = plus && minus ? (ip - im) / (2.0 * d) : plus ? (ip - pred) / d : (pred - im) / d;
+            acc[a] += factor * der;
+            acc[2 + a] += curv * der * der;
+        }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        double v = acc[a];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][a] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double total = 0.0;
+        for (int w = 0; w < kIllumReduceThreads / 32; ++w) total += red[w][threadIdx.x];
+        T.partials[(size_t)f * 4 + threadIdx.x] = total;
+    }
+}
+
+cudaError_t launch_illumination_reduce(const IlluminationParams& p, int tasks, cudaStream_t s) {
+    if (tasks <= 0) return cudaSuccess;
+    illumination_reduce_kernel<<<tasks, kIllumReduceThreads, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 // apply_illumination_update (src/algorithms/gradient_descent.rs:1044-1089),
-// one thread per task of the batch: the frame's gradient and curvature are
-// its CTA partials (fixed order) times weight / unmasked pixels; a bounded
-// Gauss-Newton step is kept only while the corrected stencil stays inside the
-// grid, and then the frame's stencil fields follow it.
+// one thread per task of the batch: the frame's sums times weight / unmasked
+// pixels, a bounded Gauss-Newton step kept only while the corrected stencil
+// stays inside the grid, and then the frame's stencil fields follow it.
 __global__ void illumination_update_kernel(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
-                                           int n, int ctas, double step, double bound, double epsilon) {
+                                           int n, double step, double bound, double epsilon) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const IlluminationTask task = tasks[t];
     const IlluminationTile& T = tiles[task.tile];
-    if (task.position >= T.frame_count) return;
-    const int f = T.order ? T.order[task.position] : task.position;
+    int f = 0;
+    if (!task_frame(T, task, f)) return;
     FrameParam fp = T.params[f];
-    if (fp.weight == 0.f || fp.loss_scale == 0.0) return;
-    double sum[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int c = 0; c < ctas; ++c)
-        for (int a = 0; a < 4; ++a) sum[a] += T.partials[((size_t)f * ctas + c) * 4 + a];
-    for (int a = 0; a < 4; ++a) sum[a] *= fp.loss_scale;
+    if (fp.loss_scale == 0.0) return;
+    double sum[4];
+    for (int a = 0; a < 4; ++a) sum[a] = T.partials[(size_t)f * 4 + a] * fp.loss_scale;
     if (!isfinite(sum[0]) || !isfinite(sum[1]) || !isfinite(sum[2]) || !isfinite(sum[3]) || sum[2] < 0.0 ||
         sum[3] < 0.0) {
         atomicOr(T.status, 256);
@@ -524,11 +697,9 @@ __global__ void illumination_update_kernel(const IlluminationTile* tiles, const 
 }
 
 cudaError_t launch_illumination_update(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
-                                       int n, int ctas, double step, double bound, double epsilon,
-                                       cudaStream_t s) {
+                                       int n, double step, double bound, double epsilon, cudaStream_t s) {
     if (count <= 0) return cudaSuccess;
-    illumination_update_kernel<<<(count + 127) / 128, 128, 0, s>>>(tiles, tasks, count, n, ctas, step, bound,
-                                                                   epsilon);
+    illumination_update_kernel<<<(count + 127) / 128, 128, 0, s>>>(tiles, tasks, count, n, step, bound, epsilon);
     return cudaGetLastError();
 }
 

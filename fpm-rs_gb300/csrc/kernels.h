@@ -230,7 +230,7 @@ cudaError_t launch_pupil_smoothing(const RegularTile* tiles, int count, int n, i
 // offsets, and the (row, column) corrections in FP64.
 struct IlluminationTile {
     const float2* object;      // M x (M + M % 2) centred spectrum (state)
-    const float2* pupil;       // N*N state pupil
+    const float2* pupil;       // N*N centred state pupil
     const float* meas;         // engine layout, as TileDesc::meas
     const uint8_t* masks;      // engine layout, or null
     const float* background;   // engine layout, or null
@@ -240,7 +240,7 @@ struct IlluminationTile {
     const long long* start;    // [frame_count][2] crop start (row, column)
     const double* offset;      // [frame_count][2] compiled subpixel offset
     double* correction;        // [frame_count][2] recovered correction
-    double* partials;          // [frame_count][C][4] per-CTA (gradient row, column, curvature row, column)
+    double* partials;          // [frame_count][4] (gradient row, column, curvature row, column) sums
     int* status;               // bit 256: non-finite illumination gradient or curvature
     int M, frame_count, amplitude;
 };
@@ -248,12 +248,23 @@ struct IlluminationTile {
 struct IlluminationTask {
     int tile, position;
 };
+// Finite differences of one chunk of tasks in FP64: per task five N x N
+// fields (the current offset, then +-d on rows and on columns), each the
+// ifftshifted patch x pupil before and the detector field after the
+// inverse FFT; `valid` flags the evaluations whose stencil is inside the grid.
 struct IlluminationParams {
     const IlluminationTile* tiles;
     const IlluminationTask* tasks;
+    double2* fields;           // [tasks][5][N*N]
+    int* valid;                // [tasks][5]
     double distance, epsilon;
-    int loss;
+    int loss, n;
 };
+cudaError_t launch_illumination_fields(const IlluminationParams& p, int tasks, cudaStream_t s);
+cudaError_t launch_illumination_reduce(const IlluminationParams& p, int tasks, cudaStream_t s);
+cudaError_t launch_illumination_update(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
+                                       int n, double step, double bound, double epsilon, cudaStream_t s);
+
 // One axis of interpolation_axis (src/model/crop.rs:266-313) in FP64: the
 // lower start and the upper fraction; false when the stencil leaves [0, m).
 __host__ __device__ inline bool offset_axis(long long start, int n, int m, double offset, long long& lower,
@@ -300,10 +311,6 @@ __host__ __device__ inline bool offset_frame_param(long long start_row, long lon
     fp.w11 = (float)(fr * fc);
     return true;
 }
-cudaError_t launch_illumination_gradient(int n, const IlluminationParams& p, int tasks, cudaStream_t s);
-cudaError_t launch_illumination_update(const IlluminationTile* tiles, const IlluminationTask* tasks, int count,
-                                       int n, int ctas, double step, double bound, double epsilon,
-                                       cudaStream_t s);
 
 // Context accessors for entry points that live outside runtime.cpp.
 void set_context_error(fpm_context* ctx, const char* message);

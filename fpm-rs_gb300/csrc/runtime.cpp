@@ -925,7 +925,7 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
 
 struct BucketRun {
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
-        tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks;
+        tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks, ill_fields, ill_valid, ill_ptrs;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
     cudaEvent_t first = nullptr, last = nullptr;
     int launches = 0;
@@ -1068,7 +1068,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(upload_array(p->ill_offset, offset, s));
             FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
             FPM_CUDA(cudaMemsetAsync(p->ill_correction.ptr, 0, sizeof(double) * 2 * F, s));
-            FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * (size_t)C * F));
+            FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
             fpm::IlluminationTile& L = ill_tiles[t];
             L.object = T.object;
@@ -1152,7 +1152,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     }
     for (DeviceBuffer* buf : {&br.tiles, &br.init, &br.gauge, &br.scratch_ptrs, &br.object_ptrs, &br.anchor_ptrs,
                               &br.velocity_ptrs, &br.avg, &br.init_partial, &br.tv_ptrs, &br.tv_objects,
-                              &br.tv_table, &br.smooth_table, &br.ill_tiles, &br.ill_tasks})
+                              &br.tv_table, &br.smooth_table, &br.ill_tiles, &br.ill_tasks, &br.ill_fields,
+                              &br.ill_valid, &br.ill_ptrs})
         buf->bind(ctx->pool, s);
     FPM_CUDA(cudaEventCreate(&br.first));
     FPM_CUDA(cudaEventCreate(&br.last));
@@ -1264,8 +1265,13 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
         FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
         FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
-        // Illumination tasks of batch k: [k * count * B, (k + 1) * count * B).
+        // Illumination tasks of batch k: [k * count * B, (k + 1) * count * B),
+        // evaluated in chunks of at most `chunk` tasks (5 FP64 N x N fields
+        // each, about 256 MB at most).
         fpm::IlluminationParams ip{};
+        const int batch_tasks = count * B;
+        const size_t field_bytes = sizeof(double2) * 5 * (size_t)N * N;
+        const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch_tasks, (256u << 20) / field_bytes));
         if (illum) {
             std::vector<fpm::IlluminationTask> tasks;
             tasks.reserve((size_t)nb * count * B);
@@ -1274,28 +1280,39 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                     for (int j = 0; j < B; ++j) tasks.push_back({t, k * B + j});
             FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
             FPM_TRY(upload_array(br.ill_tasks, tasks, s));
+            FPM_TRY(br.ill_fields.ensure(field_bytes * chunk));
+            FPM_TRY(br.ill_valid.ensure(sizeof(int) * 5 * (size_t)chunk));
+            std::vector<double2*> ptrs((size_t)5 * chunk);
+            for (size_t i = 0; i < ptrs.size(); ++i) ptrs[i] = br.ill_fields.as<double2>() + i * (size_t)N * N;
+            FPM_TRY(upload_array(br.ill_ptrs, ptrs, s));
             ip.tiles = br.ill_tiles.as<fpm::IlluminationTile>();
+            ip.fields = br.ill_fields.as<double2>();
+            ip.valid = br.ill_valid.as<int>();
             ip.distance = a->illumination_finite_difference;
             ip.epsilon = a->epsilon;
             ip.loss = a->loss_type;
+            ip.n = N;
         }
-        const int batch_tasks = count * B;
         for (int it = it0; it < iters; ++it) {
             for (int k = 0; k < nb; ++k) {
                 ep.frame_begin = k * B;
                 ep.frame_end = (k + 1) * B;
                 ep.accumulate = k > 0 ? 1 : 0;
-                if (illum) {
-                    // illumination_gradient from the batch-start object and
-                    // pupil (src/algorithms/gradient_descent.rs:590-613).
-                    ip.tasks = br.ill_tasks.as<fpm::IlluminationTask>() + (size_t)k * batch_tasks;
-                    FPM_CUDA(fpm::launch_illumination_gradient(N, ip, batch_tasks, s));
-                    br.launches += 1;
+                const fpm::IlluminationTask* batch = br.ill_tasks.as<fpm::IlluminationTask>() + (size_t)k * batch_tasks;
+                // illumination_gradient from the batch-start object and pupil
+                // (src/algorithms/gradient_descent.rs:590-613), FP64.
+                for (int c0 = 0; illum && c0 < batch_tasks; c0 += chunk) {
+                    const int n_tasks = std::min(chunk, batch_tasks - c0);
+                    ip.tasks = batch + c0;
+                    FPM_CUDA(fpm::launch_illumination_fields(ip, n_tasks, s));
+                    FPM_TRY(fft2_device(ctx, br.ill_ptrs.as<double2*>(), 5 * n_tasks, N, N, true, s));
+                    FPM_CUDA(fpm::launch_illumination_reduce(ip, n_tasks, s));
+                    br.launches += 4;
                 }
                 FPM_TRY(engine(it, it + 1));
                 if (illum) {
-                    FPM_CUDA(fpm::launch_illumination_update(br.ill_tiles.as<fpm::IlluminationTile>(), ip.tasks,
-                                                             batch_tasks, N, C, a->illumination_step,
+                    FPM_CUDA(fpm::launch_illumination_update(br.ill_tiles.as<fpm::IlluminationTile>(), batch,
+                                                             batch_tasks, N, a->illumination_step,
                                                              a->maximum_illumination_correction, a->epsilon, s));
                     br.launches += 1;
                 }
