@@ -22,6 +22,15 @@ with fixed per-wavelength pupils, one exposure per LED with all three
 wavelengths lit, Poisson counts at 1e4 photons, SpectralAlternatingProjection
 (50 passes), reconstructed together by fpm_spectral_run_batch.
 
+  python bench.py --workload illumination [--tiles T]
+
+times gradient descent with illumination (source-offset) recovery
+(GradientDescent defaults: batch 1, step 0.1, finite difference 0.05
+subpixels, bound 1.0; 10 iterations) on T tiles (default 32) of the tile
+workload above, with the centre LED displaced by (0.3, -0.2) subpixels in
+the simulation: per GD batch, five FP64 forward evaluations of the frame,
+the engine step and the on-device offset update.
+
   python bench.py --workload serving [--requests R]
 
 serves the request stream itself: Poisson arrivals at 200 requests/s (seed
@@ -74,9 +83,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--tiles", type=int, default=1024)
+    ap.add_argument("--tiles", type=int, default=None, help="1024 (tiles) or 32 (illumination) when omitted")
     ap.add_argument("--iterations", type=int, default=None, help="30 (tiles) or 50 (spectral) when omitted")
-    ap.add_argument("--workload", choices=("tiles", "spectral", "serving"), default="tiles")
+    ap.add_argument("--workload", choices=("tiles", "spectral", "serving", "illumination"), default="tiles")
     ap.add_argument("--requests", type=int, default=64, help="spectral requests per step")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
@@ -828,9 +837,136 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+# -------------------------------------------------------- illumination
+
+def run_illumination(args):
+    dist = Dist()
+    os.environ.setdefault("FPM_DEVICE", str(dist.local))
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    import fpm_rs as fpm
+    import oracle
+
+    iterations = args.iterations or 10
+    count = args.tiles or 32
+    models = build_models(fpm)
+    sizes = tile_sizes(count, args.seed + 7)
+    seed_base = 1_000_000 * dist.rank + 70_000
+    gen = torch.Generator(device="cuda")
+    host = []
+    for i, n in enumerate(sizes):
+        model = models[n]
+        centre = model.frame_count // 2
+        offsets = np.array(model.subpixel_offsets, dtype=np.float64)
+        offsets[centre] += (0.3, -0.2)
+        shifted = model._replace(offset_row=offsets[:, 0].copy(), offset_col=offsets[:, 1].copy())
+        obj = W.smooth_random_object(model.reconstruction_shape, seed_base + i)
+        intensity = fpm.forward_intensities(shifted, obj)
+        scale = PHOTONS / float(intensity.max())
+        gen.manual_seed(seed_base + i)
+        rate = torch.from_numpy(intensity).to("cuda").mul_(scale).clamp_(min=0.0)
+        counts = torch.poisson(rate, generator=gen).cpu().numpy()
+        host.append((fpm.MeasurementStack(counts), model._replace(frame_gains=np.full(model.frame_count, scale))))
+    problems = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
+    algo = fpm.GradientDescent(iterations=iterations, recover_illumination=True)
+    for _ in range(args.warmup):
+        fpm.run_batch(algo, problems, download=False)
+    clocks = ClockSampler(dist.local)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks.start()
+    device_ms = 0.0
+    launches = 0
+    for _ in range(args.steps):
+        fpm.run_batch(algo, problems, download=False)
+        st = fpm.last_run_stats()
+        device_ms += st["run_ms"]
+        launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    dist.barrier()
+    clock_info = clocks.stop()
+    step_ms = dist.max(device_ms / args.steps)
+    total = dist.sum(len(problems))
+    # e2e: host float64 inputs uploaded and results downloaded every step.
+    for p in problems:
+        p.release()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        fresh = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
+        results = fpm.run_batch(algo, fresh)
+        for p in fresh:
+            p.release()
+    wall_s = dist.max((time.perf_counter() - wall0) / args.steps)
+    h2d = sum(stack._data.nbytes for stack, _ in host)
+    d2h = sum(m.reconstruction_shape[0] * m.reconstruction_shape[1] * 32 + m.frame_count * 16 for _, m in host)
+
+    # Parity spot check: the smallest tile against the FP64 oracle.
+    check = min(range(len(sizes)), key=lambda i: sizes[i])
+    stack, model = host[check]
+    omodel = oracle.compile_model(W.OPTICS, model.k_vectors[:, 0], model.k_vectors[:, 1], model.image_shape)
+    expected = oracle.run(oracle.Problem(omodel, stack._data, gains=model.frame_gains), "gd", iterations=iterations,
+                          recover_illumination=True)
+    nrmse = oracle.complex_nrmse(expected["object"], results[check].object)
+    corr_err = float(np.abs(results[check].calibrated_illumination - expected["illumination_corrections"]).max())
+    centre = model.frame_count // 2
+
+    baseline = None
+    if dist.rank == 0:
+        from concurrent.futures import ThreadPoolExecutor
+
+        sample = [next(i for i, n in enumerate(sizes) if n == size) for size in SIZES if size in sizes]
+
+        def timed(i):
+            stack, model = host[i]
+            om = oracle.compile_model(W.OPTICS, model.k_vectors[:, 0], model.k_vectors[:, 1], model.image_shape)
+            t = time.perf_counter()
+            oracle.run(oracle.Problem(om, stack._data, gains=model.frame_gains), "gd", iterations=1,
+                       recover_illumination=True)
+            return time.perf_counter() - t
+
+        cores = os.cpu_count() or 1
+        with ThreadPoolExecutor(max_workers=cores) as pool:
+            per = dict(zip([sizes[i] for i in sample], pool.map(timed, sample)))
+        mean_tile_s = statistics.mean(per[n] * iterations for n in sizes)
+        baseline = {"value": cores / mean_tile_s, "unit": "tiles/s", "cores": cores, "kind": "port",
+                    "sample": (f"{len(sample)} tiles (one per N), 1 of {iterations} iterations each, FP64 oracle, one "
+                               f"tile per thread; tiles/s = cores / mean tile time scaled to {iterations} "
+                               f"iterations and this run's size mix ({sum(per.values()):.1f} CPU-s measured)")}
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": "GD illumination-recovery tiles/s (FP32 engine, FP64 finite differences)",
+        "value": total / (step_ms / 1e3),
+        "unit": "tiles/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64 state, f64 finite differences",
+        "data": "synthetic (seeded objects, GPU forward model with the centre LED displaced, Poisson counts)",
+        "config": {
+            "workload": (f"{count} tiles per GPU, N~U{{32,64,128,256}} (seed {args.seed + 7}), 15x15 LEDs, Poisson "
+                         f"{PHOTONS:g}, GradientDescent(recover_illumination=True) defaults, {iterations} iterations"),
+            "tile_sizes": {str(n): sizes.count(n) for n in SIZES},
+            "timing": "device span from the inputs being resident to the last result, CUDA events",
+        },
+        "cpu_baseline": baseline,
+        "e2e": {"value": total / wall_s, "unit": "tiles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches // max(1, args.steps),
+        "clocks": clock_info,
+        "parity": {"tile_n": sizes[check], "object_nrmse_vs_fp64": nrmse, "max_correction_error": corr_err,
+                   "centre_correction": [float(v) for v in results[check].calibrated_illumination[centre]]},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.workload in ("serving", "spectral") and args.impl == "reference":
+    if args.workload in ("serving", "spectral", "illumination") and args.impl == "reference":
         # These secondary workloads report their CPU baseline inside their own line.
         if dist_env()[0] == 0:
             print(json.dumps({"impl": "reference", "unavailable": f"the {args.workload} workload is measured against "
@@ -838,13 +974,17 @@ def main():
         return
     if args.workload == "serving":
         run_serving(args)
+    elif args.workload == "illumination":
+        run_illumination(args)
     elif args.workload == "spectral":
         run_spectral(args)
     elif args.impl == "reference":
         args.iterations = args.iterations or 30
+        args.tiles = args.tiles or 1024
         run_reference(args)
     else:
         args.iterations = args.iterations or 30
+        args.tiles = args.tiles or 1024
         run_ours(args)
 
 
