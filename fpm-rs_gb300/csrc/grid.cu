@@ -591,30 +591,34 @@ __device__ double gd_curvature(double predicted, double factor, int loss, double
 }
 
 // illumination_axis_gradient (src/algorithms/gradient_descent.rs:1272-1338):
-// one block per task; over the pixels the gradient step retains (unmasked,
-// no truncation), the loss derivative at the current offset times central
-// (or, at the grid edge, one-sided) differences of the intensity, and the
-// Gauss-Newton curvature times their squares, per axis, summed in a fixed
-// order into the frame's partials.
+// block (b, task) takes pixel slice b of the task's frame; over the pixels
+// the gradient step retains (unmasked, no truncation), the loss derivative at
+// the current offset times central (or, at the grid edge, one-sided)
+// differences of the intensity, and the Gauss-Newton curvature times their
+// squares, per axis, summed in a fixed order into the slice's partials.
 constexpr int kIllumReduceThreads = 256;
 
 __global__ void __launch_bounds__(kIllumReduceThreads) illumination_reduce_kernel(const IlluminationParams P) {
     __shared__ double red[kIllumReduceThreads / 32][4];
-    const IlluminationTask task = P.tasks[blockIdx.x];
+    const IlluminationTask task = P.tasks[blockIdx.y];
     const IlluminationTile& T = P.tiles[task.tile];
     int f = 0;
     if (!task_frame(T, task, f)) return;
     const int n = P.n;
     const size_t n2 = (size_t)n * n;
-    const int* valid = P.valid + (size_t)blockIdx.x * 5;
-    const double2* field = P.fields + (size_t)blockIdx.x * 5 * n2;
+    const int* valid = P.valid + (size_t)blockIdx.y * 5;
+    const double2* field = P.fields + (size_t)blockIdx.y * 5 * n2;
+    const int slice = (int)((n2 + kIlluminationBlocks - 1) / kIlluminationBlocks);
+    const int p_begin = blockIdx.x * slice, p_end = min((int)n2, p_begin + slice);
     const bool ok[5] = {valid[0] != 0, valid[1] != 0, valid[2] != 0, valid[3] != 0, valid[4] != 0};
-    if (!ok[0]) return;  // the current stencil is always inside the grid
+    // The current stencil is always inside the grid; were it not, the slice
+    // would add nothing.
+    const int p_stop = ok[0] ? p_end : p_begin;
     const double gain = (double)T.params[f].gain;
     const double d = P.distance;
     const size_t frame_base = (size_t)f * n2;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int p = threadIdx.x; p < n * n; p += blockDim.x) {
+    for (int p = p_begin + threadIdx.x; p < p_stop; p += blockDim.x) {
         const int idx = engine_index(n, p / n, p % n);
         const double m = (double)T.meas[frame_base + idx];
         bool keep;
@@ -655,13 +659,13 @@ __global__ void __launch_bounds__(kIllumReduceThreads) illumination_reduce_kerne
     if (threadIdx.x < 4) {
         double total = 0.0;
         for (int w = 0; w < kIllumReduceThreads / 32; ++w) total += red[w][threadIdx.x];
-        T.partials[(size_t)f * 4 + threadIdx.x] = total;
+        T.partials[((size_t)f * kIlluminationBlocks + blockIdx.x) * 4 + threadIdx.x] = total;
     }
 }
 
 cudaError_t launch_illumination_reduce(const IlluminationParams& p, int tasks, cudaStream_t s) {
     if (tasks <= 0) return cudaSuccess;
-    illumination_reduce_kernel<<<tasks, kIllumReduceThreads, 0, s>>>(p);
+    illumination_reduce_kernel<<<dim3(kIlluminationBlocks, tasks), kIllumReduceThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -679,8 +683,10 @@ __global__ void illumination_update_kernel(const IlluminationTile* tiles, const 
     if (!task_frame(T, task, f)) return;
     FrameParam fp = T.params[f];
     if (fp.loss_scale == 0.0) return;
-    double sum[4];
-    for (int a = 0; a < 4; ++a) sum[a] = T.partials[(size_t)f * 4 + a] * fp.loss_scale;
+    double sum[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < kIlluminationBlocks; ++b)
+        for (int a = 0; a < 4; ++a) sum[a] += T.partials[((size_t)f * kIlluminationBlocks + b) * 4 + a];
+    for (int a = 0; a < 4; ++a) sum[a] *= fp.loss_scale;
     if (!isfinite(sum[0]) || !isfinite(sum[1]) || !isfinite(sum[2]) || !isfinite(sum[3]) || sum[2] < 0.0 ||
         sum[3] < 0.0) {
         atomicOr(T.status, 256);

@@ -240,10 +240,13 @@ struct IlluminationTile {
     const long long* start;    // [frame_count][2] crop start (row, column)
     const double* offset;      // [frame_count][2] compiled subpixel offset
     double* correction;        // [frame_count][2] recovered correction
-    double* partials;          // [frame_count][4] (gradient row, column, curvature row, column) sums
+    double* partials;          // [frame_count][kIlluminationBlocks][4] (gradient row, column, curvature row, column)
     int* status;               // bit 256: non-finite illumination gradient or curvature
     int M, frame_count, amplitude;
 };
+// Pixel slices (blocks) per task of the finite-difference reduction; the
+// update sums their partials in a fixed order.
+constexpr int kIlluminationBlocks = 32;
 // One gradient evaluation: order position `position` of tile `tile`.
 struct IlluminationTask {
     int tile, position;

@@ -1068,7 +1068,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(upload_array(p->ill_offset, offset, s));
             FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
             FPM_CUDA(cudaMemsetAsync(p->ill_correction.ptr, 0, sizeof(double) * 2 * F, s));
-            FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * (size_t)F));
+            FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * fpm::kIlluminationBlocks * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
             fpm::IlluminationTile& L = ill_tiles[t];
             L.object = T.object;
