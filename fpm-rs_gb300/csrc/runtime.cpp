@@ -1054,8 +1054,25 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             // problem's resident ones stay as compiled.
             const int F = p->frames;
             FPM_TRY(p->ill_params.ensure(sizeof(fpm::FrameParam) * F));
-            FPM_CUDA(cudaMemcpyAsync(p->ill_params.ptr, p->frame_params.ptr, sizeof(fpm::FrameParam) * F,
-                                     cudaMemcpyDeviceToDevice, s));
+            FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
+            const double* saved = resumed ? b.resume[t]->illumination_corrections : nullptr;
+            if (saved) {
+                // A checkpoint's corrections and the stencils they imply.
+                std::vector<fpm::FrameParam> prm(p->params);
+                for (int f = 0; f < F; ++f)
+                    if (!fpm::offset_frame_param(p->start_row[f], p->start_col[f], p->off_row[f] + saved[2 * f],
+                                                 p->off_col[f] + saved[2 * f + 1], N, M, prm[f]))
+                        return Status::make(FPM_ERR_INVALID_PARAMETER,
+                                            "checkpoint illumination correction of source %d moves its crop outside "
+                                            "the reconstruction grid", f);
+                FPM_TRY(upload_array(p->ill_params, prm, s));
+                FPM_CUDA(cudaMemcpyAsync(p->ill_correction.ptr, saved, sizeof(double) * 2 * F,
+                                         cudaMemcpyHostToDevice, s));
+            } else {
+                FPM_CUDA(cudaMemcpyAsync(p->ill_params.ptr, p->frame_params.ptr, sizeof(fpm::FrameParam) * F,
+                                         cudaMemcpyDeviceToDevice, s));
+                FPM_CUDA(cudaMemsetAsync(p->ill_correction.ptr, 0, sizeof(double) * 2 * F, s));
+            }
             std::vector<long long> start(2 * (size_t)F);
             std::vector<double> offset(2 * (size_t)F);
             for (int f = 0; f < F; ++f) {
@@ -1066,8 +1083,6 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             }
             FPM_TRY(upload_array(p->ill_start, start, s));
             FPM_TRY(upload_array(p->ill_offset, offset, s));
-            FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
-            FPM_CUDA(cudaMemsetAsync(p->ill_correction.ptr, 0, sizeof(double) * 2 * F, s));
             FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * fpm::kIlluminationBlocks * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
             fpm::IlluminationTile& L = ill_tiles[t];
@@ -1431,6 +1446,9 @@ Status queue_capture(fpm_problem* p, const fpm_algorithm_params* a, fpm_state_de
         FPM_CUDA(cudaMemcpyAsync(p->host_partials.data(), p->partials.ptr, sizeof(double) * p->host_partials.size(),
                                  cudaMemcpyDeviceToHost, s));
     }
+    if (cap->illumination_corrections && a->algorithm == FPM_ALG_GD && a->recover_illumination)
+        FPM_CUDA(cudaMemcpyAsync(cap->illumination_corrections, p->ill_correction.ptr, sizeof(double) * 2 * p->frames,
+                                 cudaMemcpyDeviceToHost, s));
     return Status::ok();
 }
 
@@ -1521,9 +1539,6 @@ Status validate_resume(int count, fpm_problem* const* problems, const fpm_algori
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     if (resume && a->algorithm == FPM_ALG_ADAPTIVE_AP)
         return Status::make(FPM_ERR_UNSUPPORTED, "adaptive alternating projection does not resume on the GB300 device path");
-    if ((resume || capture) && a->algorithm == FPM_ALG_GD && a->recover_illumination)
-        return Status::make(FPM_ERR_UNSUPPORTED,
-                            "illumination recovery does not checkpoint or resume on the GB300 device path");
     for (int i = 0; i < count && resume; ++i) {
         const fpm_state_desc& r = resume[i];
         const fpm_problem* p = problems[i];
@@ -1545,8 +1560,10 @@ Status validate_resume(int count, fpm_problem* const* problems, const fpm_algori
                 if (!std::isfinite(v[k])) return false;
             return true;
         };
+        const bool illum = a->algorithm == FPM_ALG_GD && a->recover_illumination;
         if (!finite(r.object_spectrum, m2) || !finite(r.pupil, n2) ||
-            (mpie && (!finite(r.velocity, m2) || !finite(r.anchor, m2))))
+            (mpie && (!finite(r.velocity, m2) || !finite(r.anchor, m2))) ||
+            (illum && r.illumination_corrections && !finite(r.illumination_corrections, (size_t)p->frames)))
             return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d: checkpoint holds non-finite values", i);
     }
     for (int i = 0; i < count && capture; ++i) {

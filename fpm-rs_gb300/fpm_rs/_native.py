@@ -96,6 +96,7 @@ class StateDesc(C.Structure):
         ("object_spectrum", C.POINTER(C.c_double)), ("pupil", C.POINTER(C.c_double)),
         ("velocity", C.POINTER(C.c_double)), ("anchor", C.POINTER(C.c_double)),
         ("objectives", C.POINTER(C.c_double)),
+        ("illumination_corrections", C.POINTER(C.c_double)),
     ]
 
 

@@ -3,8 +3,8 @@
 Mirrors ReconstructionCheckpoint (src/reconstruction/checkpoint.rs:38-146)
 and CheckpointEvery (src/callbacks/checkpoint.rs:8-39). The state held is
 what this device path keeps between iterations: the centred object
-spectrum, the pupil, the mPIE velocity, anchor and momentum counter, and
-the objective trace. The device works in complex64, so the complex128
+spectrum, the pupil, the mPIE velocity, anchor and momentum counter, the
+gradient-descent illumination corrections, and the objective trace. The device works in complex64, so the complex128
 arrays stored here restore it exactly and a resumed run reproduces the
 uninterrupted one bit for bit.
 
@@ -58,6 +58,7 @@ class ReconstructionCheckpoint:
     momentum_counter: int = 0
     objectives: list = field(default_factory=list)
     format_version: int = FORMAT_VERSION
+    illumination_corrections: np.ndarray | None = None  # (sources, 2) row/column, or None
 
     def save(self, path) -> None:
         """Atomically serialize this checkpoint (write to a temporary file, then rename)."""
@@ -72,6 +73,8 @@ class ReconstructionCheckpoint:
                 "Mpie": {"velocity": _encode(self.velocity), "anchor": _encode(self.anchor),
                          "momentum_counter": int(self.momentum_counter)}},
             "trace": [float(v) for v in self.objectives],
+            "illumination_corrections": None if self.illumination_corrections is None else [
+                [float(r), float(c)] for r, c in np.asarray(self.illumination_corrections, np.float64)],
         }
         fd, tmp = tempfile.mkstemp(dir=path.parent, prefix=path.name, suffix=".tmp")
         try:
@@ -103,6 +106,8 @@ class ReconstructionCheckpoint:
             momentum_counter=int(mpie["momentum_counter"]) if mpie else 0,
             objectives=[float(v) for v in doc.get("trace", [])],
             format_version=version,
+            illumination_corrections=None if doc.get("illumination_corrections") is None else np.asarray(
+                doc["illumination_corrections"], np.float64).reshape(-1, 2),
         )
         if len(cp.objectives) != cp.completed_iterations:
             raise InvalidParameterError("checkpoint trace length differs from its completed iterations")

@@ -535,6 +535,10 @@ def submit_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> J
     return Job(handle, algorithm, problems, params, arrays, results, submitted)
 
 
+def _recovers_illumination(algorithm) -> bool:
+    return isinstance(algorithm, GradientDescent) and bool(algorithm.recover_illumination)
+
+
 def _state_arrays(problem, algorithm, iterations):
     mh, mw = problem.reconstruction_shape
     h, w = problem.image_shape
@@ -542,7 +546,9 @@ def _state_arrays(problem, algorithm, iterations):
     return dict(object_spectrum=np.zeros((mh, mw), np.complex128), pupil=np.zeros((h, w), np.complex128),
                 velocity=np.zeros((mh, mw), np.complex128) if mpie else None,
                 anchor=np.zeros((mh, mw), np.complex128) if mpie else None,
-                objectives=np.zeros(max(int(iterations), 1)))
+                objectives=np.zeros(max(int(iterations), 1)),
+                illumination=np.zeros((problem.model.source_count, 2)) if _recovers_illumination(algorithm)
+                else None)
 
 
 def _state_desc(arrays, completed, counter):
@@ -551,6 +557,8 @@ def _state_desc(arrays, completed, counter):
     d.momentum_counter = int(counter)
     for name in ("object_spectrum", "pupil", "velocity", "anchor", "objectives"):
         setattr(d, name, N.ptr(arrays[name], C.c_double))
+    if arrays.get("illumination") is not None:
+        d.illumination_corrections = N.ptr(arrays["illumination"], C.c_double)
     return d
 
 
@@ -565,11 +573,16 @@ def _checkpoint_arrays(cp: ReconstructionCheckpoint, problem, algorithm):
     mpie = isinstance(algorithm, Mpie)
     if mpie and (cp.velocity is None or cp.anchor is None):
         raise InvalidParameterError("an mPIE checkpoint needs its velocity and anchor")
+    illumination = None
+    if _recovers_illumination(algorithm) and cp.illumination_corrections is not None:
+        illumination = np.ascontiguousarray(cp.illumination_corrections, np.float64)
+        if illumination.shape != (problem.model.source_count, 2):
+            raise InvalidShapeError("checkpoint illumination corrections do not match the source count")
     arrays = dict(object_spectrum=np.ascontiguousarray(cp.object_spectrum, np.complex128),
                   pupil=np.ascontiguousarray(cp.pupil, np.complex128),
                   velocity=np.ascontiguousarray(cp.velocity, np.complex128) if mpie else None,
                   anchor=np.ascontiguousarray(cp.anchor, np.complex128) if mpie else None,
-                  objectives=np.asarray(cp.objectives + [0.0], np.float64))
+                  objectives=np.asarray(cp.objectives + [0.0], np.float64), illumination=illumination)
     return arrays
 
 
@@ -607,14 +620,7 @@ def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, downlo
         last = end == ends[-1]
         if last and download:
             results = (N.ResultDesc * len(problems))()
-            for i, p in enumerate(problems):
-                mh, mw = p.reconstruction_shape
-                h, w = p.image_shape
-                a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
-                         pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(end, 1)))
-                for name in ("object", "object_spectrum", "pupil", "objectives"):
-                    setattr(results[i], name, N.ptr(a[name], C.c_double))
-                result_arrays.append(a)
+            result_arrays = [_result_arrays(p, params, results[i]) for i, p in enumerate(problems)]
         t0 = time.perf_counter()
         N.check(N.library().fpm_run_batch_resumable(ctx.handle, len(problems), handles, C.byref(params), resume,
                                                     results, capture), ctx.handle)
@@ -622,7 +628,8 @@ def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, downlo
         checkpoints = [ReconstructionCheckpoint(
             completed_iterations=end, algorithm=algorithm._name, object_spectrum=a["object_spectrum"],
             pupil=a["pupil"], velocity=a["velocity"], anchor=a["anchor"],
-            momentum_counter=capture[i].momentum_counter, objectives=[float(v) for v in a["objectives"][:end]])
+            momentum_counter=capture[i].momentum_counter, objectives=[float(v) for v in a["objectives"][:end]],
+            illumination_corrections=None if a["illumination"] is None else a["illumination"].copy())
             for i, a in enumerate(captured)]
         for cb in callbacks:
             if end % cb.every == 0 and end > start:
@@ -640,7 +647,8 @@ def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, downlo
             object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
             pupil_support=p.model.pupil_support, trace=trace,
             runtime=RuntimeInfo(elapsed_total, total, False, algorithm._name),
-            recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background))
+            recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+            calibrated_illumination=a["illumination"]))
     return out
 
 

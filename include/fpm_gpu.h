@@ -278,6 +278,10 @@ typedef struct {
     double *velocity;               /* mPIE: mh*mw complex, else NULL */
     double *anchor;                 /* mPIE: mh*mw complex, else NULL */
     double *objectives;             /* one objective per completed iteration (the trace) */
+    /* GD illumination recovery: sources*2 (row, column) corrections
+     * (ReconstructionCheckpoint::illumination_corrections, src/reconstruction/
+     * checkpoint.rs:44), or NULL (none recovered yet: zeros on resume). */
+    double *illumination_corrections;
 } fpm_state_desc;
 
 /* fpm_run_batch that can start from saved state and save state at the end.

@@ -181,6 +181,13 @@ def test_checkpoint_json_round_trip(fpm, tmp_path):
     for name in ("object_spectrum", "pupil", "velocity", "anchor"):
         assert np.array_equal(getattr(back, name), getattr(cp, name)), name
     assert back.objectives == [3.0, 2.0, 1.5]
+    assert back.illumination_corrections is None
+    # Gradient-descent illumination corrections (checkpoint.rs:44) round-trip exactly.
+    corr = rng.standard_normal((9, 2)) * 0.3
+    gd = fpm.ReconstructionCheckpoint(completed_iterations=1, algorithm="GradientDescent", object_spectrum=obj,
+                                      pupil=pupil, objectives=[1.0], illumination_corrections=corr)
+    gd.save(tmp_path / "gd.json")
+    assert np.array_equal(fpm.ReconstructionCheckpoint.load(tmp_path / "gd.json").illumination_corrections, corr)
     with pytest.raises(fpm.InvalidParameterError):
         fpm.CheckpointEvery(0, tmp_path)
     assert fpm.CheckpointEvery(2, tmp_path).path_for(2).name == "checkpoint_00002.json"
