@@ -60,10 +60,87 @@ __global__ void fft_lines_kernel(double2* const* arrays, int n, long long stride
         base[(long long)k * stride] = make_double2(a[k].x * scale, a[k].y * scale);
 }
 
+// Power-of-two lengths: the same Stockham autosort with radix-4
+// butterflies (after one radix-2 stage when log2 n is odd), one thread per
+// butterfly and index arithmetic by shifts and masks. With span = 4 ns, the
+// outputs q of input group j are X_q = sum_r t_r w_4^(r q), where
+// t_r = a[j + r n/4] w_span^(r (j mod ns)) and w_span^k = roots[k n / span].
+__global__ void fft_lines_pow2_kernel(double2* const* arrays, int n, int log2n, long long stride, long long dist,
+                                      const double2* __restrict__ roots, int inverse, double scale) {
+    extern __shared__ double2 zsm[];
+    double2* a = zsm;
+    double2* b = zsm + n;
+    double2* base = arrays[blockIdx.y] + (long long)blockIdx.x * dist;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a[k] = base[(long long)k * stride];
+    __syncthreads();
+    int ls = 0;  // log2 of the completed sub-transform length ns
+    if (log2n & 1) {
+        const int half = n >> 1;
+        for (int j = threadIdx.x; j < half; j += blockDim.x) {
+            const double2 x0 = a[j], x1 = a[j + half];
+            b[2 * j] = make_double2(x0.x + x1.x, x0.y + x1.y);
+            b[2 * j + 1] = make_double2(x0.x - x1.x, x0.y - x1.y);
+        }
+        __syncthreads();
+        double2* t = a;
+        a = b;
+        b = t;
+        ls = 1;
+    }
+    const int quarter = n >> 2;
+    for (; ls < log2n; ls += 2) {
+        const int ns = 1 << ls;
+        const int tw_shift = log2n - ls - 2;
+        for (int j = threadIdx.x; j < quarter; j += blockDim.x) {
+            const int jm = j & (ns - 1);
+            double2 t0 = a[j], t1 = a[j + quarter], t2 = a[j + 2 * quarter], t3 = a[j + 3 * quarter];
+            if (jm) {
+                double2 w1 = roots[jm << tw_shift], w2 = roots[(2 * jm) << tw_shift], w3 = roots[(3 * jm) << tw_shift];
+                if (inverse) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w3.y = -w3.y;
+                }
+                t1 = zmul(t1, w1);
+                t2 = zmul(t2, w2);
+                t3 = zmul(t3, w3);
+            }
+            const double2 s02 = make_double2(t0.x + t2.x, t0.y + t2.y), d02 = make_double2(t0.x - t2.x, t0.y - t2.y);
+            const double2 s13 = make_double2(t1.x + t3.x, t1.y + t3.y), d13 = make_double2(t1.x - t3.x, t1.y - t3.y);
+            // w_4 = -i forward, +i inverse: X1 = d02 + w_4 d13, X3 = d02 - w_4 d13.
+            const double2 wd = inverse ? make_double2(-d13.y, d13.x) : make_double2(d13.y, -d13.x);
+            const int o = ((j >> ls) << (ls + 2)) + jm;
+            b[o] = make_double2(s02.x + s13.x, s02.y + s13.y);
+            b[o + ns] = make_double2(d02.x + wd.x, d02.y + wd.y);
+            b[o + 2 * ns] = make_double2(s02.x - s13.x, s02.y - s13.y);
+            b[o + 3 * ns] = make_double2(d02.x - wd.x, d02.y - wd.y);
+        }
+        __syncthreads();
+        double2* t = a;
+        a = b;
+        b = t;
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        base[(long long)k * stride] = make_double2(a[k].x * scale, a[k].y * scale);
+}
+
 cudaError_t launch_fft_lines(double2* const* arrays, int count, int n, long long stride, long long dist, int lines,
                              int inverse, const double2* roots, const int* factors, int nfactors, double scale,
                              cudaStream_t s) {
     const size_t smem = sizeof(double2) * 2 * (size_t)n;
+    if (n >= 4 && (n & (n - 1)) == 0) {
+        int log2n = 0;
+        while ((1 << log2n) < n) ++log2n;
+        if (smem > 48 * 1024) {
+            cudaError_t e =
+                cudaFuncSetAttribute(fft_lines_pow2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        const int threads = n / 4 < 32 ? 32 : (n / 4 > 256 ? 256 : n / 4);
+        fft_lines_pow2_kernel<<<dim3(lines, count), threads, smem, s>>>(arrays, n, log2n, stride, dist, roots, inverse,
+                                                                        scale);
+        return cudaGetLastError();
+    }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(fft_lines_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
