@@ -162,10 +162,10 @@ def test_mpie_epry_pupil_config(fpm):
             assert oracle.complex_nrmse(expected["pupil"], result.recovered_pupil) <= NRMSE
 
 
-def test_config2_full_iteration_count(fpm):
-    """BASELINE config 2 at its full 50 iterations: mPIE and EPRY with pupil
-    recovery, 13x13 LEDs, 128x128 frames (M=336), Zernike true pupil (seed
-    11), Poisson 5e3. Object (and EPRY pupil) NRMSE <= 1e-4 vs FP64."""
+def test_mpie_epry_pupil_recovery_128_full_50_iterations(fpm):
+    """The pupil-recovery workload at its full 50 iterations: mPIE and EPRY
+    with pupil recovery, 13x13 LEDs, 128x128 frames (M=336), Zernike true
+    pupil (seed 11), Poisson 5e3. Object (and EPRY pupil) NRMSE <= 1e-4 vs FP64."""
     from concurrent.futures import ThreadPoolExecutor
 
     model, omodel, data, truth, gains = helpers.simulated(fpm, 13, 128, seed=1, photons=5e3, pupil_seed=11)
@@ -181,8 +181,8 @@ def test_config2_full_iteration_count(fpm):
     assert oracle.complex_nrmse(expected["epry"]["pupil"], got["epry"].recovered_pupil) <= NRMSE
 
 
-def test_config1_full_iteration_count(fpm):
-    """BASELINE config 1 at its full 100 GD iterations: 256x256 frames,
+def test_gradient_descent_256_full_100_iterations(fpm):
+    """The 256-point GD workload at its full 100 iterations: 256x256 frames,
     15x15 LEDs (M=729), Poisson 1e4 at the bright-field peak, seed 7."""
     model, omodel, data, truth, gains = helpers.simulated(fpm, 15, 256, seed=7, photons=1e4)
     result, expected = _run_both(fpm, fpm.GradientDescent(iterations=100), "gd", dict(iterations=100), model, omodel,
