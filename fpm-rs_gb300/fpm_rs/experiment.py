@@ -142,7 +142,7 @@ class PlanarLEDArray:
         self.reference_index = (float(reference_index[0]), float(reference_index[1]))
         self.pose = pose
         if position_offsets_m is not None and np.any(np.asarray(position_offsets_m) != 0.0):
-            raise UnsupportedError("position_offsets_m is not supported by this build")
+            raise UnsupportedError("position_offsets_m is not supported on the GB300 device path")
         if self.shape[0] <= 0 or self.shape[1] <= 0:
             raise InvalidParameterError("shape rows and columns must be non-zero")
 
@@ -248,7 +248,7 @@ class Illumination:
     def __init__(self, geometry, *, calibration=None, acquisition=None):
         if calibration is not None or acquisition is not None:
             raise UnsupportedError(
-                "source calibration and multiplexed acquisition plans are not supported by this build")
+                "source calibration and multiplexed acquisition plans are not supported on the GB300 device path")
         self.geometry = geometry
 
     def resolve(self, optics: Optics) -> ResolvedSources:

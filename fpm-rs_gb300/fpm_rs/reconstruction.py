@@ -163,7 +163,7 @@ class _Algorithm:
     def _schedule(self, schedule: str) -> int:
         if schedule == "random":
             raise UnsupportedError(
-                "the random schedule depends on the reference's ChaCha12 stream and is not supported by this build")
+                "the random schedule depends on the reference's ChaCha12 stream and is not supported on the GB300 device path")
         if schedule not in _SCHEDULES:
             raise ValueError("schedule must be sequential, brightfield_first, spiral_out, random, or snr_weighted")
         return _SCHEDULES[schedule]

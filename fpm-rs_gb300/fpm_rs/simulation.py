@@ -102,7 +102,7 @@ def simulate(true_model: ImagePlaneModel, object, *, reconstruction_model=None, 
              illumination_errors=None, seed: int = 0) -> SimulationResult:
     """Simulate an image-plane FPM acquisition (Simulator::simulate)."""
     if illumination_errors is not None:
-        raise UnsupportedError("illumination acquisition errors are not supported by this build")
+        raise UnsupportedError("illumination acquisition errors are not supported on the GB300 device path")
     field = getattr(object, "field", object)
     field = N.c128(field)
     recon = reconstruction_model if reconstruction_model is not None else true_model

@@ -47,12 +47,12 @@ class SpectralChannel:
     """Fixed narrowband optics and the channel's local acquisition
     (src/experiment/spectral.rs:11-26). Source calibration and local
     multiplexing are expressed through the compiled channel's frame gains;
-    this build accepts only unit calibration and the all-sources plan here."""
+    the GB300 device path accepts only unit calibration and the all-sources plan here."""
 
     def __init__(self, *, channel_id, optics: Optics, calibration=None, acquisition=None):
         if calibration is not None or acquisition is not None:
             raise UnsupportedError(
-                "source calibration and local acquisition plans are not supported by this build; "
+                "source calibration and local acquisition plans are not supported on the GB300 device path; "
                 "set frame gains on compiled channels with SpectralImagePlaneModel.from_compiled_channels")
         self._channel_id = str(channel_id)
         self.optics = optics
@@ -637,7 +637,7 @@ class SpectralAlternatingProjection:
             raise ValueError("frame_order and seed are mutually exclusive")
         if seed is not None:
             raise UnsupportedError(
-                "the random spectral schedule depends on the reference's ChaCha12 stream and is not supported by this build")
+                "the random spectral schedule depends on the reference's ChaCha12 stream and is not supported on the GB300 device path")
         params = self._params()
         if int(checkpoint_every) <= 0 or (checkpoint_directory is not None and not str(checkpoint_directory)):
             raise InvalidParameterError("checkpoint_options: interval must be positive and directory nonempty")
