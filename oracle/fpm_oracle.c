@@ -2146,7 +2146,7 @@ int32_t orc_quadratic_smoothing_step(double *values, int32_t h, int32_t w, doubl
  * state after the step is copied out. */
 int32_t orc_gd_batch_step(const orc_problem *p, const orc_params *prm, const double *spectrum, const double *pupil,
                           const int32_t *frames, int32_t count, double *spectrum_out, double *pupil_out,
-                          double *illumination_gradient_out) {
+                          double *illumination_gradient_out, double *corrections_inout) {
     orc_state s;
     int32_t st = state_init(&s, p);
     if (st) {
@@ -2164,13 +2164,17 @@ int32_t orc_gd_batch_step(const orc_problem *p, const orc_params *prm, const dou
                                 prm->object_tv_epsilon, prm->pupil_smoothing_weight, prm->recover_illumination,
                                 prm->illumination_step, prm->illumination_finite_difference,
                                 prm->illumination_bounds};
-    if (prm->recover_illumination) illumination_alloc(&s);
+    if (prm->recover_illumination) {
+        illumination_alloc(&s);
+        if (corrections_inout) memcpy(s.corr, corrections_inout, sizeof(double) * 2 * (size_t)s.frames);
+    }
     step_summary summary = {0.0, 0.0};
     st = gradient_step(&s, (const int *)frames, count, prm->object_step, prm->epsilon, prm->loss_type, 0.0, &pc,
                        &summary);
     if (!st) {
         memcpy(spectrum_out, s.object, sizeof(cplx) * s.n_high);
         memcpy(pupil_out, s.pupil, sizeof(cplx) * s.n_low);
+        if (corrections_inout && s.corr) memcpy(corrections_inout, s.corr, sizeof(double) * 2 * (size_t)s.frames);
         if (illumination_gradient_out)
             for (int src = 0; src < s.frames; ++src) {
                 illumination_gradient_out[2 * src] = s.ill ? s.ill[5 * (size_t)src] : 0.0;

@@ -156,7 +156,7 @@ double orc_complex_nrmse(const double *reference, const double *candidate, int64
  * spectrum (mh*mw) and pupil (h*w); writes the stepped state. */
 int32_t orc_gd_batch_step(const orc_problem *problem, const orc_params *params, const double *spectrum,
                           const double *pupil, const int32_t *frames, int32_t count, double *spectrum_out,
-                          double *pupil_out, double *illumination_gradient_out);
+                          double *pupil_out, double *illumination_gradient_out, double *corrections_inout);
 /* canonicalize_object_pupil (src/algorithms/gauge.rs:20-73) in place. */
 int32_t orc_canonicalize(const orc_problem *problem, double *spectrum, double *pupil);
 /* Mean point loss of one frame over its unmasked pixels (objective.rs:14-46). */

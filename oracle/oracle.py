@@ -566,19 +566,25 @@ def quadratic_smoothing_step(values, weight: float) -> np.ndarray:
     return out
 
 
-def gd_batch_step(problem: Problem, spectrum, pupil, frames, illumination_gradient: bool = False, **kw):
+def gd_batch_step(problem: Problem, spectrum, pupil, frames, illumination_gradient: bool = False, corrections=None,
+                  **kw):
     """One gradient-descent step over the batch `frames` from the given state.
     With illumination_gradient, also returns the batch's per-source (row,
-    column) source-offset gradient (recover_illumination must be set)."""
+    column) source-offset gradient (recover_illumination must be set).
+    `corrections` (sources x 2 float64, updated in place) carries the
+    illumination corrections into and out of the step."""
     prm = params("gd", **kw)
     st = problem.struct()
     s_in, p_in = _c128(spectrum), _c128(pupil)
     s_out, p_out = np.zeros_like(s_in), np.zeros_like(p_in)
     ill = np.zeros((len(problem.model["start_row"]), 2))
+    if corrections is not None and (corrections.dtype != np.float64 or not corrections.flags.c_contiguous or
+                                    corrections.shape != ill.shape):
+        raise ValueError("corrections must be a C-contiguous float64 (sources, 2) array")
     f = np.ascontiguousarray(frames, np.int32)
     _check(lib().orc_gd_batch_step(C.byref(st), C.byref(prm), _ptr(s_in, C.c_double), _ptr(p_in, C.c_double),
                                    _ptr(f, C.c_int32), f.size, _ptr(s_out, C.c_double), _ptr(p_out, C.c_double),
-                                   _ptr(ill, C.c_double)))
+                                   _ptr(ill, C.c_double), _ptr(corrections, C.c_double)))
     return (s_out, p_out, ill) if illumination_gradient else (s_out, p_out)
 
 

@@ -479,3 +479,58 @@ def test_gauge_keeps_predictions_and_is_idempotent(oracle_module):
     bad[0, 0] = np.nan
     with pytest.raises(o.OracleError):
         o.canonicalize(problem, bad, pupil)
+
+
+def _mixed_test_pattern(shape):
+    # SyntheticObject::mixed_test_pattern (src/simulation/synthetic_object.rs:
+    # 275-298): an absorbing bar and disc on a Gaussian phase bump plus a sine.
+    rows, cols = np.indices(shape, dtype=np.float64)
+    y, x = rows - (shape[0] - 1) / 2.0, cols - (shape[1] - 1) / 2.0
+    scale = float(min(shape))
+    radius = np.hypot(x, y)
+    absorbing = ((np.abs(x) < 0.12 * scale) & (np.abs(y) < 0.35 * scale)) | (radius < 0.12 * scale)
+    amplitude = np.where(absorbing, 0.45, 1.0)
+    phase = 0.8 * np.exp(-radius * radius / (0.08 * scale * scale)) + 0.25 * np.sin(2 * np.pi * x / scale)
+    return amplitude * np.exp(1j * phase)
+
+
+def _offset_problem(o, offsets):
+    model = _direct_model()
+    truth = _mixed_test_pattern((16, 16))
+    true_model = dict(model, off_row=np.array([r for r, c in offsets]), off_col=np.array([c for r, c in offsets]))
+    data = o.forward_stack(o.Problem(true_model, None), o.object_spectrum(truth))
+    return model, truth, o.Problem(model, data)
+
+
+def test_gradient_recovers_known_source_offsets_with_fixed_object(oracle_module):
+    # tests/reconstruction_tests.rs:1322-1371: from the true object with a
+    # negligible object step, 8 full-batch steps halve the offset error.
+    o = oracle_module
+    offsets = [(0.20, -0.15), (-0.18, 0.22), (0.16, 0.12), (-0.20, -0.14), (0.14, -0.20)]
+    model, truth, problem = _offset_problem(o, offsets)
+    spectrum, pupil = o.object_spectrum(truth), model["pupil"]
+    corrections = np.zeros((5, 2))
+    for _ in range(8):
+        spectrum, pupil = o.gd_batch_step(problem, spectrum, pupil, range(5), corrections=corrections,
+                                          object_step=1e-10, recover_illumination=True, illumination_step=0.5,
+                                          illumination_finite_difference=0.02, illumination_bounds=0.75)
+    initial = sum(r * r + c * c for r, c in offsets)
+    final = float(np.sum((corrections - np.array(offsets)) ** 2))
+    assert final < 0.5 * initial, (initial, final, corrections)
+
+
+def test_joint_illumination_calibration_reduces_model_mismatch(oracle_module):
+    # tests/reconstruction_tests.rs:1373-1427: every source displaced by
+    # (0.22, -0.18); full-batch GD for 20 iterations with recovery reaches a
+    # lower objective than without, and the offset error falls.
+    o = oracle_module
+    offsets = [(0.22, -0.18)] * 5
+    model, truth, problem = _offset_problem(o, offsets)
+    kw = dict(iterations=20, object_step=0.3, batch_size=5)
+    plain = o.run(problem, "gd", **kw)
+    calibrated = o.run(problem, "gd", recover_illumination=True, illumination_step=0.05,
+                       illumination_finite_difference=0.02, illumination_bounds=0.75, **kw)
+    assert calibrated["objectives"][-1] < plain["objectives"][-1]
+    initial = sum(r * r + c * c for r, c in offsets)
+    final = float(np.sum((calibrated["illumination_corrections"] - np.array(offsets)) ** 2))
+    assert final < initial, (initial, final)
