@@ -1427,9 +1427,10 @@ static int32_t canonicalize_gauge(orc_state *s) {
     if (support_count == 0) return fail(ORC_INVALID_MODEL, "compiled reference pupil support is empty");
     double tol = 64.0 * 2.220446049250313e-16 * (double)support_count;
     int row_exact = 1, col_exact = 1;
+    /* The effective offsets, recovered illumination corrections included (gauge.rs:48-52). */
     for (int src = 0; src < s->frames; ++src) {
-        row_exact &= offset_is_zero(src_off_row(p, src), 0.0);
-        col_exact &= offset_is_zero(0.0, src_off_col(p, src));
+        row_exact &= offset_is_zero(eff_off_row(s, src), 0.0);
+        col_exact &= offset_is_zero(0.0, eff_off_col(s, src));
     }
     double row_slope = row_exact ? relative_phase_slope(s, 1, tol) : 0.0;
     double col_slope = col_exact ? relative_phase_slope(s, 0, tol) : 0.0;

@@ -128,6 +128,11 @@ def test_unsupported_options_fail_before_device_work(fpm):
         fpm.GradientDescent(recover_illumination=True, recover_pupil=True)
     with pytest.raises(fpm.InvalidParameterError):
         fpm.GradientDescent(recover_illumination=True, illumination_step=0.0)
+    # tests/reconstruction_tests.rs:2882-2887: a zero finite difference is invalid.
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.GradientDescent(recover_illumination=True, illumination_finite_difference=0.0)
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.GradientDescent(illumination_bounds=float("nan"))
     fpm.GradientDescent(recover_illumination=True, object_tv=0.1)  # device illumination recovery
     fpm.GradientDescent(object_tv=0.1, recover_pupil=True, pupil_smoothing=0.02)  # device regularisers
     with pytest.raises(ValueError):
