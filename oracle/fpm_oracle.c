@@ -1729,6 +1729,10 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         if (out->illumination_corrections)
             for (size_t i = 0; i < 2 * (size_t)s.frames; ++i)
                 out->illumination_corrections[i] = s.corr ? s.corr[i] : 0.0;
+        if (out->frame_gains) memcpy(out->frame_gains, s.gains, sizeof(double) * (size_t)s.frames);
+        if (out->background)
+            for (size_t i = 0; i < (size_t)s.frames * s.n_low; ++i)
+                out->background[i] = s.background ? s.background[i] : 0.0;
     }
     state_free(&s);
     return out->status = st;

@@ -111,6 +111,8 @@ typedef struct {
     double *object;           /* optional mh*mw complex real-space object */
     int32_t status;
     double *illumination_corrections;  /* optional frames*2 (row, column) recovered offset corrections */
+    double *frame_gains;               /* optional frames: the state's (recovered) frame gains */
+    double *background;                /* optional frames*h*w: the state's (recovered) background, 0 when none */
 } orc_output;
 
 const char *orc_last_error(void);

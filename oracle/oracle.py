@@ -109,6 +109,7 @@ class _Output(C.Structure):
         ("objectives", C.POINTER(C.c_double)), ("object", C.POINTER(C.c_double)),
         ("status", C.c_int32),
         ("illumination_corrections", C.POINTER(C.c_double)),
+        ("frame_gains", C.POINTER(C.c_double)), ("background", C.POINTER(C.c_double)),
     ]
 
 
@@ -406,6 +407,8 @@ def _outputs(problem: Problem, prm: _Params):
         objectives=np.zeros(prm.iterations),
         object=np.zeros((m["mh"], m["mw"]), np.complex128),
         illumination_corrections=np.zeros((len(m["start_row"]), 2)),
+        frame_gains=np.zeros(len(m["start_row"])),
+        background=np.zeros((len(m["start_row"]), m["h"], m["w"])),
     )
     out = _Output()
     out.object_spectrum = _ptr(arrays["object_spectrum"], C.c_double)
@@ -413,6 +416,8 @@ def _outputs(problem: Problem, prm: _Params):
     out.objectives = _ptr(arrays["objectives"], C.c_double)
     out.object = _ptr(arrays["object"], C.c_double)
     out.illumination_corrections = _ptr(arrays["illumination_corrections"], C.c_double)
+    out.frame_gains = _ptr(arrays["frame_gains"], C.c_double)
+    out.background = _ptr(arrays["background"], C.c_double)
     return out, arrays
 
 

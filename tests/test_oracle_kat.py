@@ -534,3 +534,43 @@ def test_joint_illumination_calibration_reduces_model_mismatch(oracle_module):
     initial = sum(r * r + c * c for r, c in offsets)
     final = float(np.sum((calibrated["illumination_corrections"] - np.array(offsets)) ** 2))
     assert final < initial, (initial, final)
+
+
+def _gain_error(reference, candidate):
+    # compare_frame_gains (src/metrics/model.rs:130-161): relative L2 error
+    # after one global positive scale.
+    reference, candidate = np.asarray(reference), np.asarray(candidate)
+    alignment = np.dot(candidate, reference) / max(np.dot(candidate, candidate), np.finfo(float).eps)
+    return math.sqrt(np.sum((alignment * candidate - reference) ** 2) / max(np.dot(reference, reference),
+                                                                          np.finfo(float).eps))
+
+
+def test_epry_recovers_relative_frame_gain_mismatch(oracle_module):
+    # tests/reconstruction_tests.rs:3037-3079: a constant object (amplitude 2)
+    # seen with frame gains (0.5, 1, 1.5, 2, 0.75); two EPRY passes with gain
+    # recovery (step 1) cut the scale-aligned gain error tenfold.
+    o = oracle_module
+    model = _direct_model()
+    true_gains = np.array([0.5, 1.0, 1.5, 2.0, 0.75])
+    data = o.forward_stack(o.Problem(model, None, gains=true_gains), o.object_spectrum(np.full((16, 16), 2.0 + 0j)))
+    out = o.run(o.Problem(model, data), "epry", iterations=2, object_step=1e-6, recover_pupil=False,
+                recover_gains=True, gain_step=1.0)
+    mean = true_gains.mean()
+    initial = math.sqrt(np.sum((mean - true_gains) ** 2) / np.sum(true_gains ** 2))
+    assert _gain_error(true_gains, out["frame_gains"]) < 0.1 * initial
+
+
+def test_epry_recovers_relative_per_frame_background(oracle_module):
+    # tests/reconstruction_tests.rs:3081-3123: per-frame constant backgrounds
+    # (0, 1, 2, 3, 0.5); one EPRY pass with background recovery (step 1,
+    # bounds [-10, 10]) recovers them up to a common offset, 1e-8.
+    o = oracle_module
+    model = _direct_model()
+    true_bg = np.array([0.0, 1.0, 2.0, 3.0, 0.5])
+    background = np.repeat(true_bg, 64).reshape(5, 8, 8)
+    data = o.forward_stack(o.Problem(model, None, background=background),
+                           o.object_spectrum(np.full((16, 16), 2.0 + 0j)))
+    out = o.run(o.Problem(model, data), "epry", iterations=1, object_step=1e-6, recover_pupil=False,
+                recover_background=True, background_step=1.0, background_min=-10.0, background_max=10.0)
+    means = out["background"].reshape(5, -1).mean(axis=1)
+    np.testing.assert_allclose(means - means.mean(), true_bg - true_bg.mean(), rtol=0, atol=1e-8)
