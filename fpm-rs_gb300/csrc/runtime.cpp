@@ -1469,7 +1469,6 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 128) return Status::make(FPM_ERR_NUMERICAL, "regularization produced a non-finite value");
     if (status & 256) return Status::make(FPM_ERR_NUMERICAL, "illumination gradient or curvature is invalid");
     if (!r) return Status::ok();
-    const int C = fpm::engine_ctas(p->n);
     if (r->objectives) fill_objectives(p, a, r->objectives);
     r->completed_iterations = a->iterations;
     return Status::ok();

@@ -189,7 +189,7 @@ int32_t fpm_suggest_shape(const fpm_optics *optics, int32_t sources, const doubl
 /* Compiles k-vectors into crops, fractional offsets and the circular pupil.
  * Caller allocates start_row/start_col/offset_row/offset_col [sources],
  * pupil [2*h*w] and support [h*w]. For FPM_SHAPE_EXACT the shape is read from
- * *recon_height/*recon_width; otherwise it is written there. */
+ * the values recon_height and recon_width point to; otherwise it is written there. */
 int32_t fpm_compile_model(const fpm_optics *optics, int32_t sources, const double *kx, const double *ky,
                           int32_t image_height, int32_t image_width, int32_t policy, int32_t *recon_height,
                           int32_t *recon_width, int64_t *start_row, int64_t *start_col, double *offset_row,
