@@ -1280,19 +1280,22 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
         FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
         FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
-        // Illumination tasks of batch k: [k * count * B, (k + 1) * count * B),
+        // Illumination tasks of batch k: [k * batch_tasks, (k + 1) * batch_tasks),
         // evaluated in chunks of at most `chunk` tasks (5 FP64 N x N fields
-        // each, about 256 MB at most).
+        // each, about 256 MB at most). Positions past the longest tile never
+        // hold a frame, so a batch larger than every tile needs only fmax
+        // tasks per tile.
         fpm::IlluminationParams ip{};
-        const int batch_tasks = count * B;
+        const int task_b = std::min(B, fmax);
+        const int batch_tasks = count * task_b;
         const size_t field_bytes = sizeof(double2) * 5 * (size_t)N * N;
         const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch_tasks, (256u << 20) / field_bytes));
         if (illum) {
             std::vector<fpm::IlluminationTask> tasks;
-            tasks.reserve((size_t)nb * count * B);
+            tasks.reserve((size_t)nb * batch_tasks);
             for (int k = 0; k < nb; ++k)
                 for (int t = 0; t < count; ++t)
-                    for (int j = 0; j < B; ++j) tasks.push_back({t, k * B + j});
+                    for (int j = 0; j < task_b; ++j) tasks.push_back({t, k * B + j});
             FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
             FPM_TRY(upload_array(br.ill_tasks, tasks, s));
             FPM_TRY(br.ill_fields.ensure(field_bytes * chunk));
