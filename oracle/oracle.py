@@ -408,7 +408,8 @@ def _outputs(problem: Problem, prm: _Params):
         object=np.zeros((m["mh"], m["mw"]), np.complex128),
         illumination_corrections=np.zeros((len(m["start_row"]), 2)),
         frame_gains=np.zeros(len(m["start_row"])),
-        background=np.zeros((len(m["start_row"]), m["h"], m["w"])),
+        # The recovered background only when recovered (frames x h x w).
+        background=np.zeros((len(m["start_row"]), m["h"], m["w"])) if prm.recover_background else None,
     )
     out = _Output()
     out.object_spectrum = _ptr(arrays["object_spectrum"], C.c_double)
