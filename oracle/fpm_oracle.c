@@ -1623,6 +1623,9 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
         state_free(&s);
         return out->status = st;
     }
+    /* A given start state replaces the measured-amplitude initialisation
+     * (ReconstructionState::from_object, src/reconstruction/state.rs:357-383). */
+    if (prm->initial_spectrum) memcpy(s.object, prm->initial_spectrum, sizeof(cplx) * s.n_high);
     update_config cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.object_step = prm->object_step;

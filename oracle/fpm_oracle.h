@@ -99,6 +99,7 @@ typedef struct {
     double pupil_smoothing_weight;                /* GD pupil quadratic smoothing (0: off) */
     int32_t recover_illumination;                 /* GD finite-difference source-offset recovery */
     double illumination_step, illumination_finite_difference, illumination_bounds;
+    const double *initial_spectrum;               /* optional mh*mw complex start state (ReconstructionState::from_object) */
 } orc_params;
 
 /* truncation_accepts (src/algorithms/gradient_descent.rs:1180-1182). */

@@ -100,6 +100,7 @@ class _Params(C.Structure):
         ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
         ("recover_illumination", C.c_int32), ("illumination_step", C.c_double),
         ("illumination_finite_difference", C.c_double), ("illumination_bounds", C.c_double),
+        ("initial_spectrum", C.POINTER(C.c_double)),
     ]
 
 
@@ -422,8 +423,12 @@ def _outputs(problem: Problem, prm: _Params):
     return out, arrays
 
 
-def run(problem: Problem, algorithm: str, **kw) -> dict:
+def run(problem: Problem, algorithm: str, initial_spectrum=None, **kw) -> dict:
+    """orc_run; `initial_spectrum` (centred mh x mw) replaces the default start."""
     prm = params(algorithm, **kw)
+    init = None if initial_spectrum is None else _c128(initial_spectrum)
+    if init is not None:
+        prm.initial_spectrum = _ptr(init, C.c_double)
     st = problem.struct()
     out, arrays = _outputs(problem, prm)
     _check(lib().orc_run(C.byref(st), C.byref(prm), C.byref(out)))

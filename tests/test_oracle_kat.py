@@ -661,3 +661,29 @@ def test_forward_stack_is_independent_of_worker_count(oracle_module):
     spectrum = ((idx % 17) / 13.0 + 1j * (idx % 11) / 9.0).reshape(16, 16)
     serial = o.forward_stack(o.Problem(model, None), spectrum, workers=1)
     np.testing.assert_array_equal(o.forward_stack(o.Problem(model, None), spectrum, workers=3), serial)
+
+
+def test_amplitude_gradient_loss_decreases_on_single_source_data(oracle_module):
+    # tests/reconstruction_tests.rs:1263-1281
+    o = oracle_module
+    model, data = _ideal_direct(o)
+    out = o.run(o.Problem(model, data), "gd", iterations=8, object_step=0.5)
+    assert out["objectives"][-1] < out["objectives"][0]
+
+
+def test_truncated_poisson_gradient_rejects_outliers_and_improves_object_error(oracle_module):
+    # tests/reconstruction_tests.rs:2061-2137: each frame's brightest pixel
+    # scaled by 100; from a perturbed truth, 8 full-batch Poisson GD steps
+    # (0.08) with the truncation gate at 25 end closer to the truth than
+    # without it.
+    o = oracle_module
+    truth = _mixed_test_pattern((16, 16))
+    model, data = _ideal_direct(o, truth)
+    flat = data.reshape(5, -1)
+    flat[np.arange(5), flat.argmax(axis=1)] *= 100.0
+    idx = np.arange(256).reshape(16, 16)
+    start = o.object_spectrum(truth * 0.82 * np.exp(1j * 0.12 * (idx % 13) / 13.0))
+    kw = dict(iterations=8, object_step=0.08, batch_size=5, loss_type="poisson_nll", initial_spectrum=start)
+    plain = o.run(o.Problem(model, data), "gd", **kw)
+    gated = o.run(o.Problem(model, data), "gd", poisson_truncation_threshold=25.0, **kw)
+    assert o.complex_nrmse(truth, gated["object"]) < o.complex_nrmse(truth, plain["object"])
