@@ -1699,6 +1699,7 @@ int32_t orc_run(const orc_problem *p, const orc_params *prm, orc_output *out) {
             }
             previous_objective = last_objective;
         }
+        if (out->object_steps) out->object_steps[it] = cfg.object_step;
         st = schedule_order(p, prm->schedule, order);
         step_summary summary = {0.0, 0.0};
         for (int start = 0; start < p->frames && !st; start += prm->batch_size) {

@@ -114,6 +114,7 @@ typedef struct {
     double *illumination_corrections;  /* optional frames*2 (row, column) recovered offset corrections */
     double *frame_gains;               /* optional frames: the state's (recovered) frame gains */
     double *background;                /* optional frames*h*w: the state's (recovered) background, 0 when none */
+    double *object_steps;              /* optional [iterations]: the object step each pass used (adaptive AP trace) */
 } orc_output;
 
 const char *orc_last_error(void);

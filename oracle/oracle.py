@@ -111,6 +111,7 @@ class _Output(C.Structure):
         ("status", C.c_int32),
         ("illumination_corrections", C.POINTER(C.c_double)),
         ("frame_gains", C.POINTER(C.c_double)), ("background", C.POINTER(C.c_double)),
+        ("object_steps", C.POINTER(C.c_double)),
     ]
 
 
@@ -409,6 +410,7 @@ def _outputs(problem: Problem, prm: _Params):
         object=np.zeros((m["mh"], m["mw"]), np.complex128),
         illumination_corrections=np.zeros((len(m["start_row"]), 2)),
         frame_gains=np.zeros(len(m["start_row"])),
+        object_steps=np.zeros(max(prm.iterations, 1)),
         # The recovered background only when recovered (frames x h x w).
         background=np.zeros((len(m["start_row"]), m["h"], m["w"])) if prm.recover_background else None,
     )
@@ -419,6 +421,7 @@ def _outputs(problem: Problem, prm: _Params):
     out.object = _ptr(arrays["object"], C.c_double)
     out.illumination_corrections = _ptr(arrays["illumination_corrections"], C.c_double)
     out.frame_gains = _ptr(arrays["frame_gains"], C.c_double)
+    out.object_steps = _ptr(arrays["object_steps"], C.c_double)
     out.background = _ptr(arrays["background"], C.c_double)
     return out, arrays
 

@@ -687,3 +687,24 @@ def test_truncated_poisson_gradient_rejects_outliers_and_improves_object_error(o
     plain = o.run(o.Problem(model, data), "gd", **kw)
     gated = o.run(o.Problem(model, data), "gd", poisson_truncation_threshold=25.0, **kw)
     assert o.complex_nrmse(truth, gated["object"]) < o.complex_nrmse(truth, plain["object"])
+
+
+def test_adaptive_projection_matches_fixed_step_until_feedback_has_two_objectives(oracle_module):
+    # tests/reconstruction_tests.rs:103-125: two passes at 0.7 equal AP at
+    # 0.7 bitwise, with the step trace (0.7, 0.7).
+    o = oracle_module
+    model, data = _ideal_direct(o)
+    fixed = o.run(o.Problem(model, data), "ap", iterations=2, object_step=0.7)
+    adaptive = o.run(o.Problem(model, data), "adaptive_ap", iterations=2, object_step=0.7)
+    np.testing.assert_array_equal(adaptive["object_spectrum"], fixed["object_spectrum"])
+    assert list(adaptive["object_steps"]) == [0.7, 0.7]
+
+
+def test_adaptive_projection_reduces_the_step_to_its_floor(oracle_module):
+    # tests/reconstruction_tests.rs:127-149: threshold 1 - eps, factor 0.5,
+    # floor 0.2: steps (1, 1, 0.5, 0.25, 0.2, 0.2).
+    o = oracle_module
+    model, data = _ideal_direct(o)
+    out = o.run(o.Problem(model, data), "adaptive_ap", iterations=6, progress_threshold=1.0 - np.finfo(float).eps,
+                reduction_factor=0.5, minimum_object_step=0.2)
+    assert list(out["object_steps"]) == [1.0, 1.0, 0.5, 0.25, 0.2, 0.2]
