@@ -729,3 +729,32 @@ def test_mpie_accelerates_the_same_rpie_base_on_strong_phase_data(oracle_module)
     target = 5.4e-5
     reached = [next((i for i, v in enumerate(t) if v < target), None) for t in (mpie, fpie)]
     assert reached[0] is not None and (reached[1] is None or reached[0] < reached[1]), reached
+
+
+def _pupil_phase_rmse(recovered, truth, support):
+    # pupil_phase_rmse (tests/reconstruction_tests.rs:3128-3149): phase RMSE
+    # on the support after removing the global phase.
+    inside = support != 0
+    correction = np.exp(-1j * np.angle(np.sum(recovered[inside] * np.conj(truth[inside]))))
+    diff = np.mod(np.angle(recovered[inside] * correction) - np.angle(truth[inside]) + np.pi, 2 * np.pi) - np.pi
+    return math.sqrt(np.mean(diff * diff))
+
+
+def test_epry_reduces_known_pupil_phase_error(oracle_module):
+    # tests/reconstruction_tests.rs:2922-3010: data through a pupil with
+    # -24 um defocus and astigmatism 0.2 (3x3 LEDs, 16x16 frames, exact
+    # 32x32 grid, phase disk radius 8 and 0.9 rad); 40 EPRY passes (pupil
+    # step 0.05) from the unaberrated pupil lower the pupil phase error.
+    o = oracle_module
+    kx, ky = o.planar_kvectors(W.OPTICS, (3, 3), W.PITCH, (1.0, 1.0), (0.0, 0.0, W.Z))
+    assumed = o.compile_model(W.OPTICS, kx, ky, (16, 16), (32, 32))
+    true_optics = dict(W.OPTICS, defocus_distance=-24e-6, pupil_aberration=dict(astigmatism=0.2))
+    true = o.compile_model(true_optics, kx, ky, (16, 16), (32, 32))
+    rows, cols = np.indices((32, 32))
+    disk = np.hypot(rows - 15.5, cols - 15.5) <= 8.0
+    obj = np.exp(1j * np.where(disk, 0.9, 0.0))  # SyntheticObject::phase_disk (synthetic_object.rs:156-180)
+    data = o.forward_stack(o.Problem(true, None), o.object_spectrum(obj))
+    out = o.run(o.Problem(assumed, data), "epry", iterations=40, pupil_step=0.05)
+    initial = _pupil_phase_rmse(assumed["pupil"], true["pupil"], true["support"])
+    recovered = _pupil_phase_rmse(out["pupil"], true["pupil"], true["support"])
+    assert recovered < initial, (initial, recovered)
