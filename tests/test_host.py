@@ -92,6 +92,23 @@ def test_optics_validation(fpm):
         fpm.Optics(532e-9, 1.2, 40.0, 6.5e-6)  # NA above the medium index
 
 
+def test_coherent_sampling_is_strict_at_the_nyquist_boundary(fpm):
+    # tests/geometry_tests.rs:26-65: pitch 4 / 2 equals 1 / (2 * 0.25) exactly;
+    # the boundary itself is refused with the reference's wording, one ulp
+    # below passes and one ulp above is refused.
+    import math
+
+    assert abs(fpm.Optics(532e-9, 0.1, 4.0, 6.5e-6).object_pixel_size - 1.625e-6) <= 1e-18
+    with pytest.raises(fpm.InvalidParameterError) as info:
+        fpm.Optics(1.0, 0.25, 2.0, 4.0)
+    message = str(info.value)
+    assert "strictly less" in message and "camera_pixel_size / magnification" in message
+    assert "wavelength_vacuum_m / (2 * objective_na)" in message
+    fpm.Optics(1.0, 0.25, 2.0, math.nextafter(4.0, 0.0))
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.Optics(1.0, 0.25, 2.0, math.nextafter(4.0, 5.0))
+
+
 def test_measurement_and_problem_validation(fpm):
     model = fpm.compile_model(fpm.Optics(**W.OPTICS), fpm.Illumination(fpm.PlanarLEDArray(
         (3, 3), W.PITCH, (1.0, 1.0), fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))), (32, 32))
