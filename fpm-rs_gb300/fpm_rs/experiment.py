@@ -238,7 +238,13 @@ class KVectorList:
         return self._k.copy()
 
     def resolve(self, optics: Optics) -> ResolvedSources:
+        """validate_k_vectors (src/experiment/illumination.rs:873-890): every
+        vector must propagate at the illumination wavenumber."""
         optics._validate()
+        k = 2.0 * math.pi * optics.illumination_refractive_index / optics.wavelength_vacuum_m
+        if np.any(np.hypot(self._k[:, 0], self._k[:, 1]) > k * (1.0 + 128.0 * np.finfo(np.float64).eps)):
+            raise InvalidParameterError("k_vectors: vectors must be finite and propagating at the configured vacuum "
+                                        "wavelength and illumination refractive index")
         return ResolvedSources(self._k)
 
 

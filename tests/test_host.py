@@ -213,3 +213,17 @@ def test_checkpoint_json_round_trip(fpm, tmp_path):
     with pytest.raises(fpm.InvalidParameterError):
         fpm.CheckpointEvery(0, tmp_path)
     assert fpm.CheckpointEvery(2, tmp_path).path_for(2).name == "checkpoint_00002.json"
+
+
+def test_direction_and_kvector_resolution_use_the_illumination_index(fpm):
+    # tests/geometry_tests.rs:335-358: k scales with the illumination index;
+    # explicit k-vectors resolve unchanged and must propagate.
+    directions = fpm.DirectionList.from_direction_cosines(values=[[0.25, -0.5]])
+    air = directions.resolve(fpm.Optics(532e-9, 0.1, 4.0, 6.5e-6))
+    glass_optics = fpm.Optics(532e-9, 0.1, 4.0, 6.5e-6, illumination_refractive_index=1.5)
+    glass = directions.resolve(glass_optics)
+    assert abs(glass.k_vectors[0, 0] - 1.5 * air.k_vectors[0, 0]) <= 1e-9
+    assert np.array_equal(fpm.KVectorList(air.k_vectors).resolve(glass_optics).k_vectors, air.k_vectors)
+    k_glass = 2 * np.pi * 1.5 / 532e-9
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.KVectorList([[k_glass * 1.01, 0.0]]).resolve(glass_optics)
