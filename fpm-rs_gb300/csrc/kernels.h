@@ -6,6 +6,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 struct fpm_context;
 
 namespace fpm {
@@ -318,5 +320,7 @@ __host__ __device__ inline bool offset_frame_param(long long start_row, long lon
 // Context accessors for entry points that live outside runtime.cpp.
 void set_context_error(fpm_context* ctx, const char* message);
 void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream);
+// The context's own lock, held by every entry point that uses its streams or error text.
+std::mutex& context_mutex(fpm_context* ctx);
 
 }  // namespace fpm

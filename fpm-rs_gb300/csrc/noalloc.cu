@@ -11,13 +11,18 @@
 //
 // The array holds kNoAllocMaxValues complex128 values (9 MiB) plus twiddle and
 // factor tables; every GPU that loads this library keeps it until the process
-// exits. All calls in the process share it and it keeps the last call's
+// exits. Under CUDA's default lazy module loading the array is committed on
+// the device by the first call there (its cudaGetSymbolAddress), with eager
+// loading when the module loads: callers that budget device memory should make
+// one call during their set-up so that those 9 MiB are taken before the budget
+// is. All calls in the process share the array and it keeps the last call's
 // contents; each call overwrites every element it reads, so nothing needs
 // clearing. Calls that overlapped on the GPU would race on the array, so this
-// entry point takes a process-wide lock and synchronises before returning.
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current; make that first call
-// before any stream capture.
+// entry point takes a process-wide lock (then the context's own lock, the
+// order every caller keeps) and leaves nothing queued on the array when it
+// returns, on success or error. The first call on each device looks up the
+// array's device address with cudaGetSymbolAddress while that device is
+// current; make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -72,13 +77,20 @@ void fill_roots(int n, double* out) {
 extern "C" int32_t fpm_fft2_noalloc(fpm_context* ctx, double* values, int32_t height, int32_t width, int32_t inverse) {
     std::lock_guard<std::mutex> lock(g_noalloc_lock);
     char text[512];
+    if (!ctx) {
+        fpm::set_context_error(nullptr, "fpm_fft2_noalloc: context must be non-null");
+        return FPM_ERR_INVALID_PARAMETER;
+    }
+    // The context's streams and error text belong to whichever entry point
+    // holds its lock; this one takes it after the array's lock.
+    std::lock_guard<std::mutex> context_lock(fpm::context_mutex(ctx));
     auto error = [&](int32_t code) {
         fpm::set_context_error(ctx, text);
         return code;
     };
-    if (!ctx || !values) {
-        std::snprintf(text, sizeof text, "fpm_fft2_noalloc: context and values must be non-null");
-        return ctx ? error(FPM_ERR_INVALID_PARAMETER) : FPM_ERR_INVALID_PARAMETER;
+    if (!values) {
+        std::snprintf(text, sizeof text, "fpm_fft2_noalloc: values must be non-null");
+        return error(FPM_ERR_INVALID_PARAMETER);
     }
     if (height <= 0 || width <= 0) {
         std::snprintf(text, sizeof text, "fpm_fft2_noalloc: FFT dimensions must be non-zero, got (%d, %d)", height,
@@ -95,9 +107,13 @@ extern "C" int32_t fpm_fft2_noalloc(fpm_context* ctx, double* values, int32_t he
     int device = 0;
     cudaStream_t s = nullptr;
     fpm::context_device_stream(ctx, &device, &s);
+    // Once a copy or kernel is queued, an error return first waits for the
+    // stream, so no work on the shared array outlives the lock.
+    bool queued = false;
     auto cuda = [&](cudaError_t e, const char* what) {
         std::snprintf(text, sizeof text, "fpm_fft2_noalloc: %s failed: %s (%s)", what, cudaGetErrorName(e),
                       cudaGetErrorString(e));
+        if (queued) (void)cudaStreamSynchronize(s);
         return error(FPM_ERR_CUDA);
     };
     cudaError_t e = cudaSetDevice(device);
@@ -142,6 +158,7 @@ extern "C" int32_t fpm_fft2_noalloc(fpm_context* ctx, double* values, int32_t he
     };
     for (const Copy& c : copies) {
         e = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, s);
+        queued = true;
         if (e != cudaSuccess) return cuda(e, "cudaMemcpyAsync (host to device)");
     }
     // Rows, then columns; the forward transform is scaled by 1/(h*w), as

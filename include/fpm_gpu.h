@@ -169,6 +169,8 @@ typedef struct {
 
 /* ------------------------------------------------------------------ context */
 int32_t fpm_create(fpm_context **ctx, int32_t device);
+/* Problems and jobs refer to their context: destroy them (waiting for jobs)
+ * before the context. */
 int32_t fpm_destroy(fpm_context *ctx);
 /* Copies the last error message of this context (NUL-terminated, truncated). */
 int32_t fpm_last_error(const fpm_context *ctx, char *buffer, size_t length);
@@ -208,7 +210,9 @@ int32_t fpm_fft2(fpm_context *ctx, double *values, int32_t height, int32_t width
  * return FPM_ERR_INVALID_SHAPE) that each GPU holds until the process exits.
  * Calls are serialised by a process-wide lock because they share that array.
  * The first call on a device looks up the array's address; make it before any
- * stream capture. */
+ * stream capture. That first call (or the module load, where modules load
+ * eagerly) also commits the array's 9 MiB on the device: callers that budget
+ * device memory should make one call during their set-up. */
 int32_t fpm_fft2_noalloc(fpm_context *ctx, double *values, int32_t height, int32_t width, int32_t inverse);
 
 /* Forward intensity stack [sources*h*w] of a complex128 object [mh*mw]
