@@ -604,7 +604,17 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 prefetch_step(&s_steps[(vstep + 1) & 1], T.steps, next);
             } else {
                 const int f0 = T.order ? T.order[idx] : idx;
-                if (tid == 0) s_frame = T.params[f0];
+                if (tid == 0) {
+                    s_frame = T.params[f0];
+                    // The next frame's measurement rows of this CTA go to L2
+                    // now, so that its P4 loads do not wait on HBM.
+                    if (!truncating && idx + 1 < T.frame_count) {
+                        const int f1 = T.order ? T.order[idx + 1] : idx + 1;
+                        const size_t off = (size_t)f1 * N * N + (size_t)c * R * N;
+                        prefetch_l2(T.meas + off, R * N * sizeof(float));
+                        if (T.masks) prefetch_l2(T.masks + off, R * N);
+                    }
+                }
                 __syncthreads();
             }
             const SpectralStep& sp = s_steps[vstep & 1];
@@ -826,6 +836,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         const float r = rsqrtf(fmaxf(intrinsic, 1.17549435e-38f));
                         const float s_amp = intrinsic * r;
                         if constexpr (projection) {
+                            // The forward transform takes psi' - psi, so P7 reads
+                            // Psi' - P * patch directly; masked pixels keep psi.
                             if (a >= 0.f) {
                                 if constexpr (LOSS == 0) {
                                     const float d = s_amp - a;
@@ -833,7 +845,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                                 } else {
                                     frame_loss += point_loss<LOSS>(gain * intrinsic, gain * a * a, P.loss);
                                 }
-                                v[k] = intrinsic > P.eps ? cscale(v[k], a * r) : make_float2(a, 0.f);
+                                v[k] = intrinsic > P.eps ? cscale(v[k], fmaf(a, r, -1.f))
+                                                         : make_float2(a - v[k].x, -v[k].y);
+                            } else {
+                                v[k] = make_float2(0.f, 0.f);
                             }
                         } else {
                             if (a < 0.f) {
@@ -863,8 +878,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     if constexpr (projection) {
                         if (!masked) {
                             frame_loss += point_loss<LOSS>(fmaf(gain, intrinsic, bg), meas, P.loss);
-                            v[k] = intrinsic > P.eps ? cscale(v[k], sqrtf(target) * rsqrtf(intrinsic))
-                                                     : make_float2(sqrtf(target), 0.f);
+                            v[k] = intrinsic > P.eps ? cscale(v[k], fmaf(sqrtf(target), rsqrtf(intrinsic), -1.f))
+                                                     : make_float2(sqrtf(target) - v[k].x, -v[k].y);
+                        } else {
+                            v[k] = make_float2(0.f, 0.f);
                         }
                     } else {
                         if (masked) {
@@ -917,8 +934,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             __syncthreads();
 
             // P7: row FFT step A', fftshift, correction U (+ EPRY pupil update).
+            // P4 transformed psi' - psi, so psi below is already Psi' - P * patch
+            // (src/algorithms/common.rs:186-196); the patch itself is needed only
+            // by the pupil updates.
             {
-                float2 ureg[K::T1][NA];
                 const float inv_n2 = 1.0f / (float)(N * N);
                 const float max_p2 = epry || gd_pupil ? fmaxf(frame_max_pup, P.eps) : T.max_pupil_power;
                 // Pupil gradient weight w * (N^2 / valid) / (max |patch|^2 + eps).
@@ -927,32 +946,18 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 const float inv_global = 1.0f / (max_p2 + P.eps);
                 const float pupil_scale =
                     epry ? fp.weight * P.pupil_step / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
-#pragma unroll
-                for (int t = 0; t < K::T1; ++t) {
-                    const int task = tid + t * K::THREADS;
-                    const int l = task / NB, jb = task % NB;
-                    const int i = centred_row<K>(c, l);
-                    if (i < row_lo || i > row_hi) {
-#pragma unroll
-                        for (int ja = 0; ja < NA; ++ja) ureg[t][ja] = make_float2(0.f, 0.f);
-                        continue;
-                    }
-                    float2 v[NA];
-#pragma unroll
-                    for (int ka = 0; ka < NA; ++ka) v[ka] = fld[l * K::RS + phys<K>(NB * ka + jb)];
-                    dft_reg<NA, false>(v);
+                // U of one task (row l, column class jb) into v, from the row's
+                // transform in v: pixels j = (NB * ja + jb + N / 2) mod N.
+                auto correction = [&](float2 (&v)[NA], int i, int jb) {
                     const int il = i - i_lo;
 #pragma unroll
                     for (int ja = 0; ja < NA; ++ja) {
                         const int j = (NB * ja + jb + N / 2) & (N - 1);
                         const float2 psi = cscale(v[ja], inv_n2);
-                        // Spectral update steps transform psi' - psi, so psi is already the difference.
-                        const float2 pt = spectral ? make_float2(0.f, 0.f) : patch_at(ostage, K::ORS, il, j, fp);
                         float2* pp = pslab + il * N + j;
                         const float2 pv = *pp;
                         float2 u;
                         if constexpr (projection) {
-                            const float2 d = spectral ? psi : csub(psi, cmul(pt, pv));
                             const float pw = cnorm2(pv);
                             float inv_den;
                             if constexpr (ALG == kAlgLocal || ALG == kAlgLocalAdaptive || spectral)
@@ -961,37 +966,82 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                                 inv_den = 1.0f / ((1.f - P.alpha) * pw + P.alpha * max_p2 + P.eps);
                             else
                                 inv_den = inv_global;
-                            u = cscale(cmulc(d, pv), inv_den);
+                            u = cscale(cmulc(psi, pv), inv_den);
                             if constexpr (epry) {
-                                float2 np = cfma(pupil_scale, cmulc(d, pt), pv);
+                                const float2 pt = patch_at(ostage, K::ORS, il, j, fp);
+                                float2 np = cfma(pupil_scale, cmulc(psi, pt), pv);
                                 if (P.constrain_pupil && T.support[i * N + j] == 0) np = make_float2(0.f, 0.f);
                                 *pp = np;
                             }
                         } else {
                             u = cscale(cmulc(psi, pv), inv_global);
                             if constexpr (gd_pupil) {
+                                const float2 pt = patch_at(ostage, K::ORS, il, j, fp);
                                 float2* g = T.pupil_gradient + (size_t)i * N + j;
                                 __stcg(g, cfma(pupil_grad_scale, cmulc(psi, pt), __ldcg(g)));
                             }
                         }
-                        ureg[t][ja] = u;
+                        v[ja] = u;
                     }
-                }
-                __syncthreads();
-                float2* next_halo = nullptr;
+                };
                 if constexpr (C > 1) {
-                    if (c < C - 1) next_halo = cg::this_cluster().map_shared_rank(field, c + 1);
-                }
+                    // Each row's NB tasks sit in one warp (32 % NB == 0) and
+                    // centred row i is local row l, so U overwrites the row
+                    // in place once the warp has read it.
+                    static_assert(32 % NB == 0, "a warp holds whole rows");
+                    float2* next_halo = c < C - 1 ? cg::this_cluster().map_shared_rank(field, c + 1) : nullptr;
+#pragma unroll 1
+                    for (int t = 0; t < K::T1; ++t) {
+                        const int task = tid + t * K::THREADS;
+                        const int l = task / NB, jb = task % NB;
+                        const int i = centred_row<K>(c, l);
+                        const bool live = i >= row_lo && i <= row_hi;
+                        float2 v[NA];
 #pragma unroll
-                for (int t = 0; t < K::T1; ++t) {
-                    const int task = tid + t * K::THREADS;
-                    const int l = task / NB, jb = task % NB;
-                    const int urow = centred_row<K>(c, l) - i_lo;
+                        for (int ka = 0; ka < NA; ++ka)
+                            v[ka] = live ? fld[l * K::RS + phys<K>(NB * ka + jb)] : make_float2(0.f, 0.f);
+                        __syncwarp();
+                        if (live) {
+                            dft_reg<NA, false>(v);
+                            correction(v, i, jb);
+                        }
 #pragma unroll
-                    for (int ja = 0; ja < NA; ++ja) {
-                        const int j = (NB * ja + jb + N / 2) & (N - 1);
-                        fld[urow * K::RS + j] = ureg[t][ja];
-                        if (C > 1 && urow == R - 1 && next_halo) next_halo[j] = ureg[t][ja];
+                        for (int ja = 0; ja < NA; ++ja) {
+                            const int j = (NB * ja + jb + N / 2) & (N - 1);
+                            fld[l * K::RS + j] = v[ja];
+                            if (l == R - 1 && next_halo) next_halo[j] = v[ja];
+                        }
+                    }
+                } else {
+                    // One CTA: fftshift moves U to the row N / 2 away, which
+                    // another warp reads, so U waits in registers.
+                    float2 ureg[K::T1][NA];
+#pragma unroll
+                    for (int t = 0; t < K::T1; ++t) {
+                        const int task = tid + t * K::THREADS;
+                        const int l = task / NB, jb = task % NB;
+                        const int i = centred_row<K>(c, l);
+                        if (i < row_lo || i > row_hi) {
+#pragma unroll
+                            for (int ja = 0; ja < NA; ++ja) ureg[t][ja] = make_float2(0.f, 0.f);
+                            continue;
+                        }
+#pragma unroll
+                        for (int ka = 0; ka < NA; ++ka) ureg[t][ka] = fld[l * K::RS + phys<K>(NB * ka + jb)];
+                        dft_reg<NA, false>(ureg[t]);
+                        correction(ureg[t], i, jb);
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int t = 0; t < K::T1; ++t) {
+                        const int task = tid + t * K::THREADS;
+                        const int l = task / NB, jb = task % NB;
+                        const int urow = centred_row<K>(c, l) - i_lo;
+#pragma unroll
+                        for (int ja = 0; ja < NA; ++ja) {
+                            const int j = (NB * ja + jb + N / 2) & (N - 1);
+                            fld[urow * K::RS + j] = ureg[t][ja];
+                        }
                     }
                 }
             }

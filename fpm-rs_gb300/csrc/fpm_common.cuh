@@ -117,6 +117,12 @@ FPM_DEVICE void cp_async16(void* smem, const void* gmem, int src_bytes) {
 
 FPM_DEVICE void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2: one
+// instruction for a whole block that a later phase reads.
+FPM_DEVICE void prefetch_l2(const void* gmem, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
+
 // Distributed shared memory: the cluster-shared address of `local` (a shared
 // memory location of this CTA) in CTA `rank`, and 8-byte accesses to it.
 FPM_DEVICE unsigned dsmem_address(const void* local, int rank) {
