@@ -8,9 +8,11 @@ GPU is available.
 
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
 import threading
+import weakref
 
 import numpy as np
 
@@ -196,12 +198,43 @@ class Context:
 
     def __del__(self):
         try:
-            self.close()
+            if not _closed:
+                self.close()
         except Exception:
             pass
 
 
 _context: Context | None = None
+
+# Objects that hold device handles of the process context (problems, submitted
+# jobs). At interpreter exit they are released before the context is
+# destroyed: jobs first (each waits for its device work), then problems, and
+# handles released after that are left alone.
+_owners: "weakref.WeakSet" = weakref.WeakSet()
+_closed = False
+
+
+def own(obj) -> None:
+    _owners.add(obj)
+
+
+def closed() -> bool:
+    return _closed
+
+
+def _shutdown() -> None:
+    global _closed
+    for obj in sorted(list(_owners), key=lambda o: getattr(o, "_release_order", 1)):
+        try:
+            obj._release_native()
+        except Exception:
+            pass
+    if _context is not None:
+        _context.close()
+    _closed = True
+
+
+atexit.register(_shutdown)
 
 
 def context() -> Context:

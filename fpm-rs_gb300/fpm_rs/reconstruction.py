@@ -95,13 +95,19 @@ class ReconstructionProblem:
                     ctx.handle)
             self._handle = handle
             self._ctx = ctx
+            N.own(self)
         return self._handle
 
     def release(self) -> None:
         """Frees the problem's device buffers (refused while a submitted job uses them)."""
-        if self._handle is not None:
+        if self._handle is not None and not N.closed():
             N.check(N.library().fpm_problem_destroy(self._handle), N.context().handle)
-            self._handle = None
+        self._handle = None
+
+    _release_order = 1
+
+    def _release_native(self) -> None:
+        self.release()
 
     def __del__(self):
         try:
@@ -460,6 +466,16 @@ class Job:
         self._submitted = submitted
         self._finished_at = None
         self._out = None
+        N.own(self)
+
+    _release_order = 0
+
+    def _release_native(self) -> None:
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_job_wait(handle)
+            N.library().fpm_job_destroy(handle)
+            self._handle = None
 
     def done(self) -> bool:
         """True once the device work and the result copies have finished."""
@@ -511,9 +527,9 @@ class Job:
 
     def __del__(self):
         handle = getattr(self, "_handle", None)
-        if handle:
+        if handle and not N.closed():
             N.library().fpm_job_destroy(handle)
-            self._handle = None
+        self._handle = None
 
 
 def submit_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> Job:

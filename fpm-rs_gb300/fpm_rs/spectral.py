@@ -728,6 +728,16 @@ class SpectralJob:
         self._submitted = submitted
         self._finished_at = None
         self._out = None
+        N.own(self)
+
+    _release_order = 0
+
+    def _release_native(self) -> None:
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_job_wait(handle)
+            N.library().fpm_job_destroy(handle)
+            self._handle = None
 
     def done(self) -> bool:
         if self._out is not None:
@@ -755,6 +765,6 @@ class SpectralJob:
 
     def __del__(self):
         handle = getattr(self, "_handle", None)
-        if handle:
+        if handle and not N.closed():
             N.library().fpm_job_destroy(handle)
-            self._handle = None
+        self._handle = None
