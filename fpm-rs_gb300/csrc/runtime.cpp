@@ -2487,6 +2487,8 @@ void context_device_stream(fpm_context* ctx, int* device, cudaStream_t* stream) 
     *stream = ctx->streams[0];
 }
 
+std::mutex& context_mutex(fpm_context* ctx) { return ctx->mu; }
+
 }  // namespace fpm
 
 // ====================================================================== ABI
