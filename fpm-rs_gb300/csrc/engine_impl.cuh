@@ -287,6 +287,135 @@ FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c, int row_l
     }
 }
 
+// Push exchange (cluster tiles). After P2 the row values travel to the CTA
+// that owns their cross-CTA column step: CTA o owns local rows
+// [o * ROWS, o * ROWS + ROWS) of every CTA (ROWS = R / C), received into
+// its buffer `rbuf` at ((sender * ROWS + m) * N + q) with st.async, each
+// store completing its bytes on the owner's receive mbarrier. The owner's
+// radix-C results go straight into the field rows of the CTAs that hold
+// them, completing on their row mbarrier. No CTA reads another's shared
+// memory, and a CTA waits only for the bytes it consumes.
+
+// P1 (as rows_inverse), a cluster arrival once this CTA's stencil is read
+// (peers then reuse that slab as their receive buffer), P2 in registers, the
+// matching wait, and the push of the live rows.
+template <class K>
+FPM_DEVICE void rows_inverse_push(float2* __restrict__ fld, float2* __restrict__ rbuf, unsigned long long* recv_bar,
+                                  const float2* __restrict__ ostage, const float2* __restrict__ tw,
+                                  const float2* __restrict__ pslab, const FrameParam& fp, int c, int i_lo, int row_lo,
+                                  int row_hi) {
+    constexpr int N = K::N, NA = K::NA, NB = K::NB, ROWS = K::R / K::C;
+#pragma unroll 1
+    for (int t = 0; t < K::T1; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int l = task / NB, nb = task % NB;
+        const int i = centred_row<K>(c, l);
+        if (i < row_lo || i > row_hi) continue;
+        const int il = i - i_lo;
+        float2 v[NA];
+#pragma unroll
+        for (int na = 0; na < NA; ++na) {
+            const int j = (NB * na + nb + N / 2) & (N - 1);
+            v[na] = cmul(patch_at(ostage, K::ORS, il, j, fp), pslab[il * N + j]);
+        }
+        dft_reg<NA, true>(v);
+        float2* row = fld + l * K::RS;
+#pragma unroll
+        for (int ka = 0; ka < NA; ++ka) row[phys<K>(NB * ka + nb)] = twiddle_smem<true>(v[ka], tw, nb * ka * K::TW);
+    }
+    __syncthreads();
+    cluster_arrive();
+    float2 v[K::T2][NB];
+    bool live[K::T2];
+#pragma unroll
+    for (int t = 0; t < K::T2; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int l = task / NA, ka = task % NA;
+        const int i = centred_row<K>(c, l);
+        live[t] = i >= row_lo && i <= row_hi;
+        const float2* g = fld + l * K::RS + ka * (NB + 1);
+#pragma unroll
+        for (int kb = 0; kb < NB; ++kb) v[t][kb] = live[t] ? g[kb] : make_float2(0.f, 0.f);
+        dft_reg<NB, true>(v[t]);
+    }
+    cluster_wait();
+#pragma unroll
+    for (int t = 0; t < K::T2; ++t) {
+        if (!live[t]) continue;
+        const int task = threadIdx.x + t * K::THREADS;
+        const int l = task / NA, ka = task % NA;
+        const int o = l / ROWS, m = l % ROWS;
+        float2* dst = rbuf + (c * ROWS + m) * N + NB * ka;
+        if (o == c) {
+#pragma unroll
+            for (int kb = 0; kb < NB; ++kb) dst[kb] = v[t][kb];
+        } else {
+            const unsigned rd = dsmem_address(dst, o), rb = dsmem_address(recv_bar, o);
+#pragma unroll
+            for (int kb = 0; kb < NB; ++kb) st_async(rd + 8u * kb, v[t][kb], rb);
+        }
+    }
+}
+
+// P3, push form: this CTA's rows of every CTA from rbuf (zeros for rows the
+// pupil leaves empty), the radix-C inverse step, results to their CTAs.
+template <class K>
+FPM_DEVICE void columns_cross_inverse_push(float2* __restrict__ fld, const float2* __restrict__ rbuf,
+                                           unsigned long long* rows_bar, const float2* __restrict__ tw, int c,
+                                           int row_lo, int row_hi) {
+    constexpr int C = K::C, N = K::N, ROWS = K::R / C;
+#pragma unroll 1
+    for (int t = 0; t < K::TX; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int mrow = task / N, q = task % N;
+        const int l = c * ROWS + mrow;
+        float2 v[C];
+#pragma unroll
+        for (int nc = 0; nc < C; ++nc) {
+            // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * R + l.
+            const int x = nc ^ (C / 2);
+            const int i = x * K::R + l;
+            v[nc] = i >= row_lo && i <= row_hi ? rbuf[(x * ROWS + mrow) * N + q] : make_float2(0.f, 0.f);
+        }
+        dft_reg<C, true>(v);
+        const int off = l * K::RS + phys<K>(q);
+#pragma unroll
+        for (int k1 = 0; k1 < C; ++k1) {
+            const float2 val = twiddle_smem<true>(v[k1], tw, l * k1 * K::TW);
+            if (k1 == c) fld[off] = val;
+            else st_async(dsmem_address(fld + off, k1), val, dsmem_address(rows_bar, k1));
+        }
+    }
+}
+
+// P5, push form: column values of this CTA's rows from every CTA (rbuf), the
+// radix-C forward step, and each output block to the CTA holding its natural
+// rows when the pupil reaches them.
+template <class K>
+FPM_DEVICE void columns_cross_forward_push(float2* __restrict__ fld, const float2* __restrict__ rbuf,
+                                           unsigned long long* rows_bar, int c, int row_lo, int row_hi) {
+    constexpr int C = K::C, N = K::N, ROWS = K::R / C;
+#pragma unroll 1
+    for (int t = 0; t < K::TX; ++t) {
+        const int task = threadIdx.x + t * K::THREADS;
+        const int mrow = task / N, q = task % N;
+        const int l = c * ROWS + mrow;
+        float2 v[C];
+#pragma unroll
+        for (int k1 = 0; k1 < C; ++k1) v[k1] = rbuf[(k1 * ROWS + mrow) * N + q];
+        dft_reg<C, false>(v);
+        const int off = l * K::RS + phys<K>(q);
+#pragma unroll
+        for (int j1 = 0; j1 < C; ++j1) {
+            const int target = j1 ^ (C / 2);
+            const int i = target * K::R + l;
+            if (i < row_lo || i > row_hi) continue;
+            if (target == c) fld[off] = v[j1];
+            else st_async(dsmem_address(fld + off, target), v[j1], dsmem_address(rows_bar, target));
+        }
+    }
+}
+
 // P4 column transforms with two threads per column: lanes l and l ^ 16 of a
 // warp share column position q; half h = lane / 16 holds local rows
 // n2 and n2 + 16 for n2 in [8h, 8h + 8). The 32-point transform is split as
@@ -319,9 +448,8 @@ FPM_DEVICE void column_inverse_split(const float2* __restrict__ fld, int pq, int
 // Forward, the dual: z[k] holds x'[h + 2k]; writes natural rows n2 and n2 + 16
 // for n2 in [8h, 8h + 8), each times w_N^(-c * row) when the cluster splits
 // the column (C > 1).
-template <class K>
-FPM_DEVICE void column_forward_split(float2* __restrict__ fld, int pq, int h, int c, const float2* __restrict__ tw,
-                                     float2 (&z)[16]) {
+template <class K, class Emit>
+FPM_DEVICE void column_forward_split(int h, int c, const float2* __restrict__ tw, float2 (&z)[16], Emit emit) {
     dft_reg<16, false>(z);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -335,8 +463,8 @@ FPM_DEVICE void column_forward_split(float2* __restrict__ fld, int pq, int h, in
             lo = twiddle_smem<false>(lo, tw, c * row * K::TW);
             hi = twiddle_smem<false>(hi, tw, c * (row + 16) * K::TW);
         }
-        fld[row * K::RS + pq] = lo;
-        fld[(row + 16) * K::RS + pq] = hi;
+        emit(row, lo);
+        emit(row + 16, hi);
     }
 }
 
@@ -351,12 +479,11 @@ FPM_DEVICE void column_inverse_local(const float2* __restrict__ fld, int pq, flo
     dft_reg<16, true>(z);
 }
 
-template <class K>
-FPM_DEVICE void column_forward_local(float2* __restrict__ fld, int pq, int c, const float2* __restrict__ tw,
-                                     float2 (&z)[16]) {
+template <class K, class Emit>
+FPM_DEVICE void column_forward_local(int c, const float2* __restrict__ tw, float2 (&z)[16], Emit emit) {
     dft_reg<16, false>(z);
 #pragma unroll
-    for (int b = 0; b < 16; ++b) fld[b * K::RS + pq] = K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b];
+    for (int b = 0; b < 16; ++b) emit(b, K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b]);
 }
 
 // End of a gradient-descent mini-batch (src/algorithms/gradient_descent.rs:
@@ -457,6 +584,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     // their shared-memory budget.
     __shared__ __align__(16) unsigned char s_desc[ALG == kAlgSpectral ? 2 * sizeof(SpectralStep) : sizeof(FrameParam)];
     FrameParam& s_frame = *reinterpret_cast<FrameParam*>(s_desc);
+    // The next frame's descriptor, copied asynchronously one frame ahead.
+    __shared__ __align__(16) FrameParam s_next;
+    static_assert(sizeof(FrameParam) % 8 == 0, "FrameParam is copied in 8-byte pieces");
+    int next_ready = -1;  // thread 0: order position whose descriptor s_next holds
     SpectralStep* const s_steps = reinterpret_cast<SpectralStep*>(s_desc);
     if (tid == 0) s_tile = P.tiles[tile];
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
@@ -503,6 +634,58 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     double ada_step = P.object_step;
     double ada_previous = 0.0;
     bool ada_has_previous = false;
+    // Push exchange for cluster tiles of every family except EPRY with pupil
+    // recovery, GD with pupil recovery and spectral AP (their P7 reads the
+    // staged stencil) and truncated GD (its statistics steps stop after P4).
+    // Two cluster barriers remain per frame: after P1, overlapped with P2,
+    // and at the frame end. mbarriers: 0 receive buffer (reusing the stencil
+    // slab), 1 field rows, 2 halo row.
+    constexpr bool push = C > 1 && !(epry || gd_pupil || spectral || truncating);
+    constexpr int ROWS = R / C;
+    constexpr unsigned kDenseBytes = (unsigned)((C - 1) * ROWS * N * sizeof(float2));
+    __shared__ __align__(8) unsigned long long s_mbar[3];
+    __shared__ unsigned s_bytes[2];  // expected bytes: P3 input, P5 output
+    __shared__ int s_sync_failed;
+    float2* const rbuf = osm;
+    unsigned ph_recv = 0, ph_rows = 0, ph_halo = 0;
+    if constexpr (push) {
+        if (tid == 0) {
+            // Rows arrive only where the pupil reaches (the rest are zero).
+            unsigned b3 = 0, a5 = 0;
+            for (int x = 0; x < C; ++x) {
+                if (x == c) continue;
+                for (int m = 0; m < ROWS; ++m) {
+                    const int i3 = x * R + c * ROWS + m, i5 = c * R + x * ROWS + m;
+                    if (i3 >= row_lo && i3 <= row_hi) b3 += N * sizeof(float2);
+                    if (i5 >= row_lo && i5 <= row_hi) a5 += N * sizeof(float2);
+                }
+            }
+            s_bytes[0] = b3;
+            s_bytes[1] = a5;
+            s_sync_failed = 0;
+            for (int k = 0; k < 3; ++k) mbar_init(&s_mbar[k], 1);
+            fence_mbar_init_cluster();
+            mbar_arrive_expect_tx(&s_mbar[0], b3);
+            mbar_arrive_expect_tx(&s_mbar[1], kDenseBytes);
+            if (c > 0) mbar_arrive_expect_tx(&s_mbar[2], N * sizeof(float2));
+        }
+    }
+    // One exchange step on mbarrier k: every thread waits (bounded) for the
+    // current phase, the block synchronises, and only then thread 0 arms the
+    // next phase with `next_bytes`. Arming after every thread has seen the
+    // completion matters: a phase that expects no bytes completes as it is
+    // armed, and a thread still polling the previous phase would then see
+    // its parity again. A timeout sets status bit 512; the CTA then skips
+    // its later waits and arms nothing more, so the launch still ends.
+    auto exchange = [&](int k, unsigned& parity, unsigned next_bytes) {
+        if (!s_sync_failed && !mbar_wait(&s_mbar[k], parity)) {
+            s_sync_failed = 1;
+            atomicOr(T.status, 512);
+        }
+        parity ^= 1u;
+        __syncthreads();
+        if (tid == 0 && !s_sync_failed) mbar_arrive_expect_tx(&s_mbar[k], next_bytes);
+    };
     __syncthreads();
 
     for (int it = P.it_begin; it < P.it_end; ++it) {
@@ -603,13 +786,24 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 const int next = step + 1 < steps ? step + 1 : 0;
                 prefetch_step(&s_steps[(vstep + 1) & 1], T.steps, next);
             } else {
-                const int f0 = T.order ? T.order[idx] : idx;
+                const int f0 = T.order ? __ldg(T.order + idx) : idx;
                 if (tid == 0) {
-                    s_frame = T.params[f0];
-                    // The next frame's measurement rows of this CTA go to L2
-                    // now, so that its P4 loads do not wait on HBM.
-                    if (!truncating && idx + 1 < T.frame_count) {
-                        const int f1 = T.order ? T.order[idx + 1] : idx + 1;
+                    if (next_ready == idx) {
+                        cp_async_wait_all();
+                        s_frame = s_next;
+                    } else {
+                        s_frame = T.params[f0];
+                    }
+                    // The next frame's descriptor comes in behind this frame,
+                    // and its measurement rows of this CTA go to L2 now, so
+                    // that its P4 loads do not wait on HBM.
+                    if (!truncating && idx + 1 < step_end) {
+                        const int f1 = T.order ? __ldg(T.order + idx + 1) : idx + 1;
+#pragma unroll
+                        for (int k = 0; k < (int)(sizeof(FrameParam) / 8); ++k)
+                            cp_async8(reinterpret_cast<char*>(&s_next) + 8 * k,
+                                      reinterpret_cast<const char*>(T.params + f1) + 8 * k);
+                        next_ready = idx + 1;
                         const size_t off = (size_t)f1 * N * N + (size_t)c * R * N;
                         prefetch_l2(T.meas + off, R * N * sizeof(float));
                         if (T.masks) prefetch_l2(T.masks + off, R * N);
@@ -662,9 +856,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P1, P2
             float max_obj = 0.f, max_pup = 0.f;
-            if (!spectral_update)
+            if constexpr (push) {
+                rows_inverse_push<K>(fld, rbuf, &s_mbar[0], ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi);
+            } else if (!spectral_update) {
                 rows_inverse<K, epry || gd_pupil>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj,
                                                   max_pup);
+            }
             if constexpr (epry || gd_pupil) {
                 max_obj = warp_max(max_obj);
                 max_pup = warp_max(max_pup);
@@ -683,7 +880,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     fred[2 * K::WARPS + 1] = b;
                 }
             }
-            if (!spectral_update) cluster_barrier<K>();
+            if constexpr (!push) {
+                if (!spectral_update) cluster_barrier<K>();
+            }
 
             float frame_max_obj = 0.f, frame_max_pup = 0.f;
             if constexpr (epry || gd_pupil) {
@@ -702,7 +901,11 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
 
             // P3
-            if constexpr (C > 1) {
+            if constexpr (push) {
+                __syncthreads();                       // this CTA's own rows in rbuf
+                exchange(0, ph_recv, kDenseBytes);     // P3 input; next: P5 input
+                columns_cross_inverse_push<K>(fld, rbuf, &s_mbar[1], tw, c, row_lo, row_hi);
+            } else if constexpr (C > 1) {
                 if (!spectral_update) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
             }
             // P4 ownership. R = 32: column position q4, half h4, slot k =
@@ -713,7 +916,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             const int mbase = (c * R + h4) * N + q4;
             constexpr int mstride = R == 32 ? 2 * N : N;
 
-            if constexpr (C > 1) {
+            if constexpr (push) {
+                __syncthreads();                       // this CTA's own P3 results
+                exchange(1, ph_rows, s_bytes[1]);      // P3 output; next: P5 output
+            } else if constexpr (C > 1) {
                 if (!spectral_update) cluster_barrier<K>();
             }
 
@@ -770,8 +976,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     else
                         v[k] = make_float2(sqrtf(target * sp.inv_weight_sum) - psi.x, -psi.y);
                 }
-                if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
-                else column_forward_local<K>(fld, pq, c, tw, v);
+                auto to_field = [&](int row, float2 x) { fld[row * K::RS + pq] = x; };
+                if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_field);
+                else column_forward_local<K>(c, tw, v, to_field);
                 if (first) loss_acc += (double)frame_loss * sp.loss_scale;
             } else {
             // P4: column inverse FFT, projection, column forward FFT.
@@ -895,8 +1102,21 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                 }
                 if (!stats) {
-                    if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
-                    else column_forward_local<K>(fld, pq, c, tw, v);
+                    if constexpr (push) {
+                        // Row `row` of this column goes to the CTA owning its cross step.
+                        auto to_owner = [&](int row, float2 x) {
+                            const int o = row / ROWS, m = row % ROWS;
+                            float2* dst = rbuf + (c * ROWS + m) * N + q4;
+                            if (o == c) *dst = x;
+                            else st_async(dsmem_address(dst, o), x, dsmem_address(&s_mbar[0], o));
+                        };
+                        if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_owner);
+                        else column_forward_local<K>(c, tw, v, to_owner);
+                    } else {
+                        auto to_field = [&](int row, float2 x) { fld[row * K::RS + pq] = x; };
+                        if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_field);
+                        else column_forward_local<K>(c, tw, v, to_field);
+                    }
                     loss_acc += (double)frame_loss * fp.loss_scale;
                 }
             }
@@ -905,12 +1125,21 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 __syncthreads();
                 continue;
             }
-            cluster_barrier<K>();
-
-            // P5
-            if constexpr (C > 1) {
-                columns_cross_forward<K>(fld, c, row_lo, row_hi);
+            if constexpr (push) {
+                // P5 input rows from every CTA, then the results into the field rows.
+                __syncthreads();
+                exchange(0, ph_recv, s_bytes[0]);      // P5 input; next: the next frame's P3 input
+                columns_cross_forward_push<K>(fld, rbuf, &s_mbar[1], c, row_lo, row_hi);
+                __syncthreads();
+                exchange(1, ph_rows, kDenseBytes);     // P5 output; next: the next frame's P3 output
+            } else {
                 cluster_barrier<K>();
+
+                // P5
+                if constexpr (C > 1) {
+                    columns_cross_forward<K>(fld, c, row_lo, row_hi);
+                    cluster_barrier<K>();
+                }
             }
 
             // P6: row FFT step C' with twiddles.
@@ -989,7 +1218,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     // centred row i is local row l, so U overwrites the row
                     // in place once the warp has read it.
                     static_assert(32 % NB == 0, "a warp holds whole rows");
-                    float2* next_halo = c < C - 1 ? cg::this_cluster().map_shared_rank(field, c + 1) : nullptr;
+                    float2* next_halo = !push && c < C - 1 ? cg::this_cluster().map_shared_rank(field, c + 1) : nullptr;
 #pragma unroll 1
                     for (int t = 0; t < K::T1; ++t) {
                         const int task = tid + t * K::THREADS;
@@ -1009,7 +1238,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         for (int ja = 0; ja < NA; ++ja) {
                             const int j = (NB * ja + jb + N / 2) & (N - 1);
                             fld[l * K::RS + j] = v[ja];
-                            if (l == R - 1 && next_halo) next_halo[j] = v[ja];
+                            if constexpr (push) {
+                                if (l == R - 1 && c < C - 1)
+                                    st_async(dsmem_address(field + j, c + 1), v[ja], dsmem_address(&s_mbar[2], c + 1));
+                            } else {
+                                if (l == R - 1 && next_halo) next_halo[j] = v[ja];
+                            }
                         }
                     }
                 } else {
@@ -1045,7 +1279,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                 }
             }
-            cluster_barrier<K>();
+            if constexpr (push) {
+                __syncthreads();  // U rows of this CTA
+                if (c > 0) exchange(2, ph_halo, N * sizeof(float2));  // the halo row from CTA c - 1
+            } else {
+                cluster_barrier<K>();
+            }
 
             // P8: exact bilinear adjoint scatter of scale * U into the object.
             {
@@ -1084,7 +1323,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
                         acc = cfma(fp.w11, d1, acc);
-                        const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
+                        // Push families reuse the stencil slab for received rows,
+                        // so they read the current object from L2.
+                        const float2 base = j < cols8 ? (gd_batched || push ? __ldcg(grow + j) : srow[j]) : z;
                         out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
 #pragma unroll
@@ -1184,6 +1425,11 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         }
     }
     if (P.momentum && c == 0 && tid == 0) *T.counter = counter;
+    if constexpr (push) {
+        // After a timed-out exchange, stores that peers issued may still be
+        // on their way into this CTA's shared memory: let them land first.
+        if (s_sync_failed) linger_ns(1000000ull);
+    }
     // Peers must not exit while their shared memory may still be addressed.
     cluster_barrier<K>();
 }

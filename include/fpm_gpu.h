@@ -57,7 +57,7 @@ enum {
     FPM_ERR_NUMERICAL = 7,            /* Error::Numerical */
     FPM_ERR_UNSUPPORTED = 8,          /* Error::Unsupported */
     FPM_ERR_CUDA = 9,                 /* a CUDA runtime call failed */
-    FPM_ERR_TIMEOUT = 10              /* reserved: a bounded device wait expired */
+    FPM_ERR_TIMEOUT = 10              /* a bounded device wait expired (frame-engine exchange) */
 };
 
 enum { FPM_SHAPE_EXACT = 0, FPM_SHAPE_MINIMUM = 1, FPM_SHAPE_SMOOTH = 2, FPM_SHAPE_POWER_OF_TWO = 3 };
@@ -169,8 +169,8 @@ typedef struct {
 
 /* ------------------------------------------------------------------ context */
 int32_t fpm_create(fpm_context **ctx, int32_t device);
-/* Problems and jobs refer to their context: destroy them (waiting for jobs)
- * before the context. */
+/* Problems, jobs and plans refer to their context: destroy them (waiting for
+ * jobs) before the context. */
 int32_t fpm_destroy(fpm_context *ctx);
 /* Copies the last error message of this context (NUL-terminated, truncated). */
 int32_t fpm_last_error(const fpm_context *ctx, char *buffer, size_t length);
