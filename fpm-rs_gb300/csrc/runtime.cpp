@@ -221,6 +221,7 @@ struct fpm_problem {
     // offsets, corrections and per-CTA gradient partials.
     DeviceBuffer ill_params, ill_start, ill_offset, ill_correction, ill_partials;
     fpm_job* busy = nullptr;  // the submitted job that owns the problem until it finishes
+    fpm_plan* plan = nullptr;  // the captured run plan that holds the problem until destroyed
 };
 
 namespace {
@@ -930,6 +931,10 @@ struct BucketRun {
     cudaEvent_t first = nullptr, last = nullptr;
     int launches = 0;
     double bytes = 0.0;
+    // A run is prepared (host work, buffers, uploads of its tables) and
+    // launched (device work only). Captured run plans do the two apart: the
+    // preparation once, the launch inside a CUDA graph capture.
+    bool prepare = true, launch = true;
     ~BucketRun() {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (first) cudaEventDestroy(first);
@@ -977,11 +982,11 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(p->scratch64.ensure(sizeof(double2) * (size_t)M * M));
         if (gd_batched) {
             FPM_TRY(p->gradient.ensure(sizeof(float2) * (size_t)M * ms));
-            FPM_CUDA(cudaMemsetAsync(p->gradient.ptr, 0, sizeof(float2) * (size_t)M * ms, s));
+            if (br.launch) FPM_CUDA(cudaMemsetAsync(p->gradient.ptr, 0, sizeof(float2) * (size_t)M * ms, s));
         }
         if (gd_pupil) {
             FPM_TRY(p->pupil_gradient.ensure(sizeof(float2) * n2));
-            FPM_CUDA(cudaMemsetAsync(p->pupil_gradient.ptr, 0, sizeof(float2) * n2, s));
+            if (br.launch) FPM_CUDA(cudaMemsetAsync(p->pupil_gradient.ptr, 0, sizeof(float2) * n2, s));
         }
         if (tv) FPM_TRY(p->tv_scratch.ensure(sizeof(double2) * (size_t)M * M));
         if (smoothing) FPM_TRY(p->pupil_scratch.ensure(sizeof(float2) * n2));
@@ -989,7 +994,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(p->velocity.ensure(sizeof(float2) * (size_t)M * ms));
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
         }
-        FPM_CUDA(cudaMemsetAsync(p->status.ptr, 0, sizeof(int), s));
+        if (br.launch) FPM_CUDA(cudaMemsetAsync(p->status.ptr, 0, sizeof(int), s));
         p->it0 = it0;
         p->resume_objectives.clear();
         if (resumed) {
@@ -1011,13 +1016,13 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 FPM_CUDA(fpm::launch_narrow(wide, M, M, grids[g].dst->as<float2>(), ms, s));
             }
             br.launches += mpie ? 4 : 2;
-        } else {
+        } else if (br.launch) {
             FPM_CUDA(cudaMemsetAsync(p->counter.ptr, 0, sizeof(int), s));
             FPM_CUDA(cudaMemcpyAsync(p->pupil_state.ptr, p->pupil_model.ptr, sizeof(float2) * n2, cudaMemcpyDeviceToDevice, s));
         }
         const int* order_dev = nullptr;
         if (a->schedule != FPM_SCHEDULE_SEQUENTIAL) {
-            FPM_TRY(upload_array(p->order, schedule_order(p, a->schedule), s));
+            if (br.prepare) FPM_TRY(upload_array(p->order, schedule_order(p, a->schedule), s));
             order_dev = p->order.as<int>();
         }
         // max(max |P|^2, eps) of the compiled pupil, FP64.
@@ -1056,7 +1061,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(p->ill_params.ensure(sizeof(fpm::FrameParam) * F));
             FPM_TRY(p->ill_correction.ensure(sizeof(double) * 2 * F));
             const double* saved = resumed ? b.resume[t]->illumination_corrections : nullptr;
-            if (saved) {
+            if (!br.launch) {
+                // Prepared only: the run copies its frame constants when launched.
+            } else if (saved) {
                 // A checkpoint's corrections and the stencils they imply.
                 std::vector<fpm::FrameParam> prm(p->params);
                 for (int f = 0; f < F; ++f)
@@ -1081,8 +1088,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 offset[2 * f] = p->off_row[f];
                 offset[2 * f + 1] = p->off_col[f];
             }
-            FPM_TRY(upload_array(p->ill_start, start, s));
-            FPM_TRY(upload_array(p->ill_offset, offset, s));
+            if (br.prepare) {
+                FPM_TRY(upload_array(p->ill_start, start, s));
+                FPM_TRY(upload_array(p->ill_offset, offset, s));
+            }
             FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * fpm::kIlluminationBlocks * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
             fpm::IlluminationTile& L = ill_tiles[t];
@@ -1135,7 +1144,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         objects[t] = T.object;
         anchors[t] = T.anchor;
         velocities[t] = T.velocity;
-        // Algorithmic bytes of the engine for this tile.
+        // Algorithmic bytes of the engine for this tile (counted when prepared).
+        if (!br.prepare) continue;
         double frame_bytes = 0.0;
         int effective = 0;
         for (int f = 0; f < p->frames; ++f) {
@@ -1170,23 +1180,30 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                               &br.tv_table, &br.smooth_table, &br.ill_tiles, &br.ill_tasks, &br.ill_fields,
                               &br.ill_valid, &br.ill_ptrs})
         buf->bind(ctx->pool, s);
-    FPM_CUDA(cudaEventCreate(&br.first));
-    FPM_CUDA(cudaEventCreate(&br.last));
-    FPM_CUDA(cudaEventRecord(br.first, s));
-    FPM_TRY(upload_array(br.tiles, tiles, s));
-    FPM_TRY(upload_array(br.init, inits, s));
-    FPM_TRY(upload_array(br.gauge, gauges, s));
-    FPM_TRY(upload_array(br.scratch_ptrs, scratch, s));
-    FPM_TRY(upload_array(br.object_ptrs, objects, s));
-    FPM_TRY(upload_array(br.anchor_ptrs, anchors, s));
-    FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
+    if (!br.first) FPM_CUDA(cudaEventCreate(&br.first));
+    if (!br.last) FPM_CUDA(cudaEventCreate(&br.last));
+    if (br.prepare) {
+        FPM_TRY(upload_array(br.tiles, tiles, s));
+        FPM_TRY(upload_array(br.init, inits, s));
+        FPM_TRY(upload_array(br.gauge, gauges, s));
+        FPM_TRY(upload_array(br.scratch_ptrs, scratch, s));
+        FPM_TRY(upload_array(br.object_ptrs, objects, s));
+        FPM_TRY(upload_array(br.anchor_ptrs, anchors, s));
+        FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
+        // The line FFT plans of both grids exist before any launch (a plan's
+        // creation synchronises, which a graph capture cannot).
+        FftPlan* plan = nullptr;
+        FPM_TRY(get_plan(ctx, M, plan));
+        FPM_TRY(get_plan(ctx, N, plan));
+    }
+    if (br.launch) FPM_CUDA(cudaEventRecord(br.first, s));
 
     // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift;
     // one launch pair for all tiles of the bucket. A resumed run has restored
     // its state above. Pupil-recovering runs canonicalise either way.
-    if (!resumed) {
-        FPM_TRY(br.avg.ensure(sizeof(double) * (size_t)N * N * count));
-        FPM_TRY(br.init_partial.ensure(sizeof(double) * 2 * (size_t)fpm::init_chunks(N) * count));
+    FPM_TRY(br.avg.ensure(sizeof(double) * (size_t)N * N * count));
+    FPM_TRY(br.init_partial.ensure(sizeof(double) * 2 * (size_t)fpm::init_chunks(N) * count));
+    if (!resumed && br.launch) {
         FPM_CUDA(fpm::launch_init_mean(N, M, br.init.as<fpm::InitTile>(), count, br.avg.as<double>(),
                                        br.init_partial.as<double>(), s));
         br.launches += 2;
@@ -1196,7 +1213,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                                             mpie ? br.velocity_ptrs.as<float2*>() : nullptr, count, M, s));
         br.launches += 3;
     }
-    if (canonical) {
+    if (canonical && br.launch) {
         FPM_CUDA(fpm::launch_gauge(br.gauge.as<fpm::GaugeTile>(), count, N, M, s));
         br.launches += 1;
     }
@@ -1276,10 +1293,12 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 tv_objects[(size_t)k * count + t] = in_batch > 0 ? p->object.as<float2>() : nullptr;
                 if (k == 0) tv_ptrs[t] = tv ? p->tv_scratch.as<double2>() : nullptr;
             }
-        FPM_TRY(upload_array(br.tv_table, tv_table, s));
-        FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
-        FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
-        FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
+        if (br.prepare) {
+            FPM_TRY(upload_array(br.tv_table, tv_table, s));
+            FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
+            FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
+            FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
+        }
         // Illumination tasks of batch k: [k * batch_tasks, (k + 1) * batch_tasks),
         // evaluated in chunks of at most `chunk` tasks (5 FP64 N x N fields
         // each, about 256 MB at most). Positions past the longest tile never
@@ -1296,13 +1315,15 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             for (int k = 0; k < nb; ++k)
                 for (int t = 0; t < count; ++t)
                     for (int j = 0; j < task_b; ++j) tasks.push_back({t, k * B + j});
-            FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
-            FPM_TRY(upload_array(br.ill_tasks, tasks, s));
             FPM_TRY(br.ill_fields.ensure(field_bytes * chunk));
             FPM_TRY(br.ill_valid.ensure(sizeof(int) * 5 * (size_t)chunk));
-            std::vector<double2*> ptrs((size_t)5 * chunk);
-            for (size_t i = 0; i < ptrs.size(); ++i) ptrs[i] = br.ill_fields.as<double2>() + i * (size_t)N * N;
-            FPM_TRY(upload_array(br.ill_ptrs, ptrs, s));
+            if (br.prepare) {
+                FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
+                FPM_TRY(upload_array(br.ill_tasks, tasks, s));
+                std::vector<double2*> ptrs((size_t)5 * chunk);
+                for (size_t i = 0; i < ptrs.size(); ++i) ptrs[i] = br.ill_fields.as<double2>() + i * (size_t)N * N;
+                FPM_TRY(upload_array(br.ill_ptrs, ptrs, s));
+            }
             ip.tiles = br.ill_tiles.as<fpm::IlluminationTile>();
             ip.fields = br.ill_fields.as<double2>();
             ip.valid = br.ill_valid.as<int>();
@@ -1311,7 +1332,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             ip.loss = a->loss_type;
             ip.n = N;
         }
-        for (int it = it0; it < iters; ++it) {
+        for (int it = it0; it < iters && br.launch; ++it) {
             for (int k = 0; k < nb; ++k) {
                 ep.frame_begin = k * B;
                 ep.frame_end = (k + 1) * B;
@@ -1358,7 +1379,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 br.launches += 1;
             }
         }
-    } else if (iters > it0) {
+    } else if (iters > it0 && br.launch) {
         if (epry || canonical) {
             for (int it = it0; it < iters; ++it) {
                 FPM_TRY(engine(it, it + 1));
@@ -1371,6 +1392,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(engine(it0, iters));
         }
     }
+    if (!br.launch) return Status::ok();
     // Finalise: ifftshift, inverse FFT (FP64) into scratch.
     FPM_CUDA(fpm::launch_state_to_natural(reinterpret_cast<const float2* const*>(br.object_ptrs.ptr),
                                           br.scratch_ptrs.as<double2*>(), count, M, s));
@@ -1594,6 +1616,7 @@ Status build_buckets(fpm_context* ctx, int count, fpm_problem* const* problems, 
         fpm_problem* p = problems[i];
         if (!p || p->ctx != ctx) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d does not belong to this context", i);
         if (p->busy) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d is in use by a submitted job", i);
+        if (p->plan) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem %d is held by a captured run plan", i);
         auto it = std::find_if(buckets.begin(), buckets.end(), [&](const Bucket& b) { return b.n == p->n && b.m == p->m; });
         if (it == buckets.end()) {
             buckets.push_back(Bucket{p->n, p->m, {}, {}});
@@ -2478,6 +2501,93 @@ void finish_job(fpm_job* j) {
 }
 }  // namespace
 
+// A captured run plan: the device work of one run_batch over resident
+// problems (initialisation, frame engine, per-iteration gauge, regulariser
+// and illumination steps, finalisation, for every tile size on its own
+// stream) recorded once as a CUDA graph and replayed as one launch. Each
+// replay starts from the problems' initial state, exactly as a fresh run.
+struct fpm_plan {
+    fpm_context* ctx = nullptr;
+    fpm_algorithm_params params{};
+    std::vector<Bucket> buckets;
+    std::vector<std::unique_ptr<BucketRun>> runs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int streams = 0;
+    ~fpm_plan() {
+        if (ctx)
+            for (int k = 0; k < streams; ++k) cudaStreamSynchronize(ctx->streams[k]);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto& b : buckets)
+            for (fpm_problem* p : b.problems) p->plan = nullptr;
+        runs.clear();  // buffers free on their streams
+    }
+};
+
+namespace {
+
+Status plan_create(fpm_context* ctx, int count, fpm_problem* const* problems, const fpm_algorithm_params* a,
+                   std::unique_ptr<fpm_plan>& out) {
+    FPM_TRY(validate_params(a));
+    auto plan = std::make_unique<fpm_plan>();
+    plan->ctx = ctx;
+    plan->params = *a;
+    FPM_TRY(build_buckets(ctx, count, problems, nullptr, plan->buckets));
+    const int ns = (int)std::min<size_t>(plan->buckets.size(), fpm_context::kStreams);
+    plan->streams = ns;
+    // Host preparation: buffers, descriptor tables and FFT plans.
+    for (size_t k = 0; k < plan->buckets.size(); ++k) {
+        plan->runs.push_back(std::make_unique<BucketRun>());
+        BucketRun& br = *plan->runs.back();
+        br.launch = false;
+        FPM_TRY(run_bucket(ctx, plan->buckets[k], &plan->params, ctx->streams[k % fpm_context::kStreams], br));
+    }
+    for (int k = 0; k < ns; ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k]));
+    // Capture: the first stream forks to the others and joins them at the end.
+    cudaStream_t s0 = ctx->streams[0];
+    FPM_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
+    std::vector<cudaEvent_t> marks;
+    auto captured = [&]() -> Status {
+        cudaEvent_t fork;
+        FPM_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        marks.push_back(fork);
+        FPM_CUDA(cudaEventRecord(fork, s0));
+        for (int k = 1; k < ns; ++k) FPM_CUDA(cudaStreamWaitEvent(ctx->streams[k], fork, 0));
+        for (size_t k = 0; k < plan->buckets.size(); ++k) {
+            BucketRun& br = *plan->runs[k];
+            br.prepare = false;
+            br.launch = true;
+            FPM_TRY(run_bucket(ctx, plan->buckets[k], &plan->params, ctx->streams[k % fpm_context::kStreams], br));
+        }
+        for (int k = 1; k < ns; ++k) {
+            cudaEvent_t join;
+            FPM_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+            marks.push_back(join);
+            FPM_CUDA(cudaEventRecord(join, ctx->streams[k]));
+            FPM_CUDA(cudaStreamWaitEvent(s0, join, 0));
+        }
+        return Status::ok();
+    };
+    Status st = captured();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(s0, &graph);
+    for (cudaEvent_t e : marks) cudaEventDestroy(e);
+    if (st) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    FPM_CUDA(end);
+    plan->graph = graph;
+    FPM_CUDA(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
+    for (auto& b : plan->buckets)
+        for (fpm_problem* p : b.problems) p->plan = plan.get();
+    out = std::move(plan);
+    return Status::ok();
+}
+
+}  // namespace
+
 namespace fpm {
 
 void set_context_error(fpm_context* ctx, const char* message) {
@@ -2918,6 +3028,8 @@ int32_t fpm_problem_destroy(fpm_problem* problem) {
     std::lock_guard<std::mutex> lock(ctx->mu);
     if (problem->busy)
         return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "the problem is in use by a submitted job"));
+    if (problem->plan)
+        return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "the problem is held by a captured run plan"));
     cudaSetDevice(ctx->device);
     delete problem;
     return FPM_OK;
@@ -3119,3 +3231,79 @@ int32_t fpm_last_run_stats(const fpm_context* ctx, fpm_run_stats* stats) {
 }
 
 }  // extern "C"
+
+int32_t fpm_plan_create(fpm_context* ctx, int32_t count, fpm_problem* const* problems,
+                        const fpm_algorithm_params* params, fpm_plan** out) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        if (!out || !params || (count > 0 && !problems))
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "problems, params and the output pointer must be non-null");
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        std::unique_ptr<fpm_plan> plan;
+        FPM_TRY(plan_create(ctx, count, problems, params, plan));
+        *out = plan.release();
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_plan_launch(fpm_plan* plan) {
+    if (!plan) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "plan is null"));
+    fpm_context* ctx = plan->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        FPM_CUDA(cudaGraphLaunch(plan->exec, ctx->streams[0]));
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_plan_wait(fpm_plan* plan) {
+    if (!plan) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "plan is null"));
+    fpm_context* ctx = plan->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->streams[0];
+        for (auto& b : plan->buckets)
+            for (fpm_problem* p : b.problems) FPM_TRY(queue_collect(p, &plan->params, nullptr, s));
+        FPM_CUDA(cudaStreamSynchronize(s));
+        FPM_CUDA(cudaGetLastError());
+        FPM_TRY(compute_stats(plan->buckets, plan->runs, ctx->stats));
+        for (auto& b : plan->buckets)
+            for (fpm_problem* p : b.problems) FPM_TRY(finish_collect(p, &plan->params, nullptr));
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_plan_collect(fpm_plan* plan, fpm_result_desc* results) {
+    if (!plan) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "plan is null"));
+    fpm_context* ctx = plan->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        if (!results) return Status::make(FPM_ERR_INVALID_PARAMETER, "results is null");
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->streams[0];
+        for (auto& b : plan->buckets)
+            for (size_t t = 0; t < b.problems.size(); ++t)
+                FPM_TRY(queue_collect(b.problems[t], &plan->params, &results[b.indices[t]], s));
+        FPM_CUDA(cudaStreamSynchronize(s));
+        for (auto& b : plan->buckets)
+            for (size_t t = 0; t < b.problems.size(); ++t)
+                FPM_TRY(finish_collect(b.problems[t], &plan->params, &results[b.indices[t]]));
+        return Status::ok();
+    };
+    return finish(ctx, body());
+}
+
+int32_t fpm_plan_destroy(fpm_plan* plan) {
+    if (!plan) return FPM_OK;
+    fpm_context* ctx = plan->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    delete plan;
+    return FPM_OK;
+}

@@ -22,7 +22,8 @@ from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
 from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjection, Epry, Fpie, GradientDescent, Mpie,
                              ReconstructionProblem,
-                             ReconstructionResult, RuntimeInfo, Job, last_run_stats, run_batch, submit_batch)
+                             ReconstructionResult, RunPlan, RuntimeInfo, Job, capture_batch, last_run_stats, run_batch,
+                             submit_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
 from .spectral import (SpectralAcquisitionPlan, SpectralAlternatingProjection, SpectralChannel, SpectralFrame,
                        SpectralGeometry, SpectralImagePlaneModel, SpectralMixingDiagnostics,
@@ -56,5 +57,6 @@ __all__ = [
     "ReconstructionCheckpoint", "ReconstructionProblem", "ReconstructionResult", "ResolvedSources", "RuntimeInfo",
     "SimulationResult",
     "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
-    "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob",
+    "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob", "RunPlan",
+    "capture_batch",
 ]

@@ -28,6 +28,7 @@ EXPORTED = (
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
     "fpm_spectral_run", "fpm_spectral_run_batch", "fpm_spectral_forward",
     "fpm_run_batch_submit", "fpm_spectral_run_batch_submit", "fpm_job_poll", "fpm_job_wait", "fpm_job_stats", "fpm_job_destroy",
+    "fpm_plan_create", "fpm_plan_launch", "fpm_plan_wait", "fpm_plan_collect", "fpm_plan_destroy",
 )
 
 

@@ -551,6 +551,87 @@ def submit_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> J
     return Job(handle, algorithm, problems, params, arrays, results, submitted)
 
 
+class RunPlan:
+    """run_batch over fixed problems, captured once as a CUDA graph
+    (fpm_plan_create) and replayed as a single launch per run. Each replay
+    starts from the problems' initial state, as a fresh run does; the
+    problems stay held by the plan until close()."""
+
+    _release_order = 0
+
+    def __init__(self, handle, algorithm, problems, params):
+        self._handle = handle
+        self._algorithm = algorithm
+        self._problems = problems
+        self._params = params
+        N.own(self)
+
+    def launch(self) -> None:
+        """Queues one replay and returns."""
+        N.check(N.library().fpm_plan_launch(self._handle), N.context().handle)
+
+    def wait(self) -> None:
+        """Waits for the queued replays; last_run_stats() then describes the last one."""
+        N.check(N.library().fpm_plan_wait(self._handle), N.context().handle)
+
+    def run(self) -> None:
+        self.launch()
+        self.wait()
+
+    def results(self) -> list:
+        """The last replay's results, one ReconstructionResult per problem."""
+        results = (N.ResultDesc * len(self._problems))()
+        arrays = [_result_arrays(p, self._params, results[i]) for i, p in enumerate(self._problems)]
+        start = time.perf_counter()
+        N.check(N.library().fpm_plan_collect(self._handle, results), N.context().handle)
+        elapsed = time.perf_counter() - start
+        out = []
+        for p, a in zip(self._problems, arrays):
+            trace = [(it + 1, float(a["objectives"][it]), elapsed) for it in range(self._params.iterations)]
+            result = ReconstructionResult(
+                object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
+                pupil_support=p.model.pupil_support, trace=trace,
+                runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
+                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                calibrated_illumination=a["illumination"])
+            if p.name is not None:
+                result.metadata["problem_name"] = p.name
+            out.append(result)
+        return out
+
+    def _release_native(self) -> None:
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_plan_destroy(handle)
+            self._handle = None
+
+    def close(self) -> None:
+        """Frees the graph; the problems are free for other runs again."""
+        if getattr(self, "_handle", None) and not N.closed():
+            N.check(N.library().fpm_plan_destroy(self._handle), N.context().handle)
+        self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def capture_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> RunPlan:
+    """Captures run_batch(algorithm, problems) as a CUDA graph for repeated
+    replays (RunPlan.launch / wait / results)."""
+    problems = list(problems)
+    params = algorithm._params(schedule)
+    upload(problems)
+    handles = (C.c_void_p * len(problems))(*[p.device_handle() for p in problems])
+    ctx = N.context()
+    handle = C.c_void_p()
+    N.check(N.library().fpm_plan_create(ctx.handle, len(problems), handles, C.byref(params), C.byref(handle)),
+            ctx.handle)
+    return RunPlan(handle, algorithm, problems, params)
+
+
 def _recovers_illumination(algorithm) -> bool:
     return isinstance(algorithm, GradientDescent) and bool(algorithm.recover_illumination)
 

@@ -73,6 +73,7 @@ enum {
 typedef struct fpm_context fpm_context;
 typedef struct fpm_problem fpm_problem;
 typedef struct fpm_job fpm_job;
+typedef struct fpm_plan fpm_plan;
 
 /* Microscope optics (src/experiment/optics.rs:44-68). */
 typedef struct {
@@ -423,6 +424,29 @@ int32_t fpm_job_wait(fpm_job *job);
 int32_t fpm_job_stats(fpm_job *job, fpm_run_stats *stats);
 /* Waits for the job if needed and frees it. */
 int32_t fpm_job_destroy(fpm_job *job);
+
+/* ----------------------------------------------------- captured run plans */
+/* Runner::run over a batch (src/reconstruction/runner.rs:76-285) recorded
+ * once as a CUDA graph: the device work of fpm_run_batch for these problems
+ * and parameters (initialisation, frame engine, per-iteration gauge,
+ * regulariser and illumination steps, finalisation; every tile size on its
+ * own stream) becomes one graph launch. Each replay starts from the problems'
+ * initial state, exactly as a fresh fpm_run_batch, and leaves its results on
+ * the device. The problems are held by the plan until fpm_plan_destroy
+ * (other runs and fpm_problem_destroy refuse them); resumed runs are not
+ * captured. */
+int32_t fpm_plan_create(fpm_context *ctx, int32_t count, fpm_problem *const *problems,
+                        const fpm_algorithm_params *params, fpm_plan **plan);
+/* Queues one replay on the context's first stream and returns. */
+int32_t fpm_plan_launch(fpm_plan *plan);
+/* Waits for the replays queued so far, checks every problem's device status
+ * and records the last replay's statistics (fpm_last_run_stats). */
+int32_t fpm_plan_wait(fpm_plan *plan);
+/* Downloads the last replay's results, as fpm_run_batch fills `results`
+ * (indexed like the plan's problems). */
+int32_t fpm_plan_collect(fpm_plan *plan, fpm_result_desc *results);
+/* Waits for queued replays and frees the plan; its problems are free again. */
+int32_t fpm_plan_destroy(fpm_plan *plan);
 
 #ifdef __cplusplus
 }
