@@ -287,18 +287,24 @@ FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c, int row_l
     }
 }
 
-// Push exchange (cluster tiles). After P2 the row values travel to the CTA
-// that owns their cross-CTA column step: CTA o owns local rows
-// [o * ROWS, o * ROWS + ROWS) of every CTA (ROWS = R / C), received into
-// its buffer `rbuf` at ((sender * ROWS + m) * N + q) with st.async, each
-// store completing its bytes on the owner's receive mbarrier. The owner's
-// radix-C results go straight into the field rows of the CTAs that hold
-// them, completing on their row mbarrier. No CTA reads another's shared
-// memory, and a CTA waits only for the bytes it consumes.
-
-// P1 (as rows_inverse), a cluster arrival once this CTA's stencil is read
-// (peers then reuse that slab as their receive buffer), P2 in registers, the
-// matching wait, and the push of the live rows.
+// Push exchange (256-point tiles, 16-CTA clusters). After P2 the rows
+// travel to the CTA that owns their cross-CTA column step: CTA o owns local
+// row o of every CTA (ROWS = R / C = 1), received into its buffer `rbuf`
+// (padded rows, stride RS, the stencil slab's space) at row `sender`. Each
+// row is one bulk copy of RS complex values into the peer's shared memory,
+// completing its bytes on the peer's receive mbarrier; the owner's radix-C
+// results go back the same way into the field rows of the CTAs that hold
+// them, completing on their row mbarrier. Results bound for another CTA are
+// first written in place over the rows they were computed from, so every
+// copy reads whole contiguous rows. No CTA reads another's shared memory and
+// a CTA waits only for the rows it consumes. A copy's source is never
+// rewritten before its receiver has it: each later write to it follows,
+// through the exchange chain, the receiver's wait.
+// P1 (as rows_inverse), then: peers may reuse their stencil slab as receive
+// buffer once this CTA has read its own, so the cluster arrival comes right
+// after P1; P2 runs in place meanwhile (rows owned by this CTA go straight
+// into its own rbuf), and after the matching wait each live row is copied
+// to its owner.
 template <class K>
 FPM_DEVICE void rows_inverse_push(float2* __restrict__ fld, float2* __restrict__ rbuf, unsigned long long* recv_bar,
                                   const float2* __restrict__ ostage, const float2* __restrict__ tw,
@@ -324,43 +330,39 @@ FPM_DEVICE void rows_inverse_push(float2* __restrict__ fld, float2* __restrict__
         for (int ka = 0; ka < NA; ++ka) row[phys<K>(NB * ka + nb)] = twiddle_smem<true>(v[ka], tw, nb * ka * K::TW);
     }
     __syncthreads();
+    fence_proxy_async_smem();  // this CTA's writes before the copies peers will make into it
     cluster_arrive();
-    float2 v[K::T2][NB];
-    bool live[K::T2];
-#pragma unroll
+#pragma unroll 1
     for (int t = 0; t < K::T2; ++t) {
         const int task = threadIdx.x + t * K::THREADS;
         const int l = task / NA, ka = task % NA;
         const int i = centred_row<K>(c, l);
-        live[t] = i >= row_lo && i <= row_hi;
+        if (i < row_lo || i > row_hi) continue;
         const float2* g = fld + l * K::RS + ka * (NB + 1);
+        float2 v[NB];
 #pragma unroll
-        for (int kb = 0; kb < NB; ++kb) v[t][kb] = live[t] ? g[kb] : make_float2(0.f, 0.f);
-        dft_reg<NB, true>(v[t]);
+        for (int kb = 0; kb < NB; ++kb) v[kb] = g[kb];
+        dft_reg<NB, true>(v);
+        float2* out = l / ROWS == c ? rbuf + (c * ROWS + l % ROWS) * K::RS + ka * (NB + 1) : fld + l * K::RS + ka * (NB + 1);
+#pragma unroll
+        for (int kb = 0; kb < NB; ++kb) out[kb] = v[kb];
     }
+    fence_proxy_async_smem();
+    __syncthreads();
     cluster_wait();
-#pragma unroll
-    for (int t = 0; t < K::T2; ++t) {
-        if (!live[t]) continue;
-        const int task = threadIdx.x + t * K::THREADS;
-        const int l = task / NA, ka = task % NA;
-        const int o = l / ROWS, m = l % ROWS;
-        float2* dst = rbuf + (c * ROWS + m) * N + NB * ka;
-        if (o == c) {
-#pragma unroll
-            for (int kb = 0; kb < NB; ++kb) dst[kb] = v[t][kb];
-        } else {
-            const unsigned rd = dsmem_address(dst, o), rb = dsmem_address(recv_bar, o);
-#pragma unroll
-            for (int kb = 0; kb < NB; ++kb) st_async(rd + 8u * kb, v[t][kb], rb);
-        }
+    if (threadIdx.x < K::R) {
+        const int l = threadIdx.x, o = l / ROWS, i = centred_row<K>(c, l);
+        if (o != c && i >= row_lo && i <= row_hi)
+            bulk_copy_to_peer(dsmem_address(rbuf + (c * ROWS + l % ROWS) * K::RS, o), fld + l * K::RS,
+                              K::RS * sizeof(float2), dsmem_address(recv_bar, o));
     }
 }
 
 // P3, push form: this CTA's rows of every CTA from rbuf (zeros for rows the
-// pupil leaves empty), the radix-C inverse step, results to their CTAs.
+// pupil leaves empty), the radix-C inverse step, then each result row to
+// the CTA that holds it.
 template <class K>
-FPM_DEVICE void columns_cross_inverse_push(float2* __restrict__ fld, const float2* __restrict__ rbuf,
+FPM_DEVICE void columns_cross_inverse_push(float2* __restrict__ fld, float2* __restrict__ rbuf,
                                            unsigned long long* rows_bar, const float2* __restrict__ tw, int c,
                                            int row_lo, int row_hi) {
     constexpr int C = K::C, N = K::N, ROWS = K::R / C;
@@ -368,51 +370,66 @@ FPM_DEVICE void columns_cross_inverse_push(float2* __restrict__ fld, const float
     for (int t = 0; t < K::TX; ++t) {
         const int task = threadIdx.x + t * K::THREADS;
         const int mrow = task / N, q = task % N;
-        const int l = c * ROWS + mrow;
+        const int l = c * ROWS + mrow, pq = phys<K>(q);
         float2 v[C];
 #pragma unroll
         for (int nc = 0; nc < C; ++nc) {
             // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * R + l.
             const int x = nc ^ (C / 2);
             const int i = x * K::R + l;
-            v[nc] = i >= row_lo && i <= row_hi ? rbuf[(x * ROWS + mrow) * N + q] : make_float2(0.f, 0.f);
+            v[nc] = i >= row_lo && i <= row_hi ? rbuf[(x * ROWS + mrow) * K::RS + pq] : make_float2(0.f, 0.f);
         }
         dft_reg<C, true>(v);
-        const int off = l * K::RS + phys<K>(q);
 #pragma unroll
         for (int k1 = 0; k1 < C; ++k1) {
             const float2 val = twiddle_smem<true>(v[k1], tw, l * k1 * K::TW);
-            if (k1 == c) fld[off] = val;
-            else st_async(dsmem_address(fld + off, k1), val, dsmem_address(rows_bar, k1));
+            if (k1 == c) fld[l * K::RS + pq] = val;
+            else rbuf[(k1 * ROWS + mrow) * K::RS + pq] = val;
         }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x < C * ROWS) {
+        const int k1 = threadIdx.x / ROWS, mrow = threadIdx.x % ROWS;
+        if (k1 != c)
+            bulk_copy_to_peer(dsmem_address(fld + (c * ROWS + mrow) * K::RS, k1), rbuf + (k1 * ROWS + mrow) * K::RS,
+                              K::RS * sizeof(float2), dsmem_address(rows_bar, k1));
     }
 }
 
 // P5, push form: column values of this CTA's rows from every CTA (rbuf), the
-// radix-C forward step, and each output block to the CTA holding its natural
+// radix-C forward step, and each output row to the CTA holding its natural
 // rows when the pupil reaches them.
 template <class K>
-FPM_DEVICE void columns_cross_forward_push(float2* __restrict__ fld, const float2* __restrict__ rbuf,
+FPM_DEVICE void columns_cross_forward_push(float2* __restrict__ fld, float2* __restrict__ rbuf,
                                            unsigned long long* rows_bar, int c, int row_lo, int row_hi) {
     constexpr int C = K::C, N = K::N, ROWS = K::R / C;
 #pragma unroll 1
     for (int t = 0; t < K::TX; ++t) {
         const int task = threadIdx.x + t * K::THREADS;
         const int mrow = task / N, q = task % N;
-        const int l = c * ROWS + mrow;
+        const int l = c * ROWS + mrow, pq = phys<K>(q);
         float2 v[C];
 #pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) v[k1] = rbuf[(k1 * ROWS + mrow) * N + q];
+        for (int k1 = 0; k1 < C; ++k1) v[k1] = rbuf[(k1 * ROWS + mrow) * K::RS + pq];
         dft_reg<C, false>(v);
-        const int off = l * K::RS + phys<K>(q);
 #pragma unroll
         for (int j1 = 0; j1 < C; ++j1) {
             const int target = j1 ^ (C / 2);
             const int i = target * K::R + l;
             if (i < row_lo || i > row_hi) continue;
-            if (target == c) fld[off] = v[j1];
-            else st_async(dsmem_address(fld + off, target), v[j1], dsmem_address(rows_bar, target));
+            if (target == c) fld[l * K::RS + pq] = v[j1];
+            else rbuf[(j1 * ROWS + mrow) * K::RS + pq] = v[j1];
         }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x < C * ROWS) {
+        const int j1 = threadIdx.x / ROWS, mrow = threadIdx.x % ROWS;
+        const int target = j1 ^ (C / 2), l = c * ROWS + mrow, i = target * K::R + l;
+        if (target != c && i >= row_lo && i <= row_hi)
+            bulk_copy_to_peer(dsmem_address(fld + l * K::RS, target), rbuf + (j1 * ROWS + mrow) * K::RS,
+                              K::RS * sizeof(float2), dsmem_address(rows_bar, target));
     }
 }
 
@@ -593,6 +610,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
     __syncthreads();
     const TileDesc& T = s_tile;
+    const float eps = (float)P.eps;  // epsilon in the per-pixel FP32 arithmetic
     const int M = T.M;
     const long long ostride = M + (M & 1);
     const int i_lo = C == 1 ? 0 : c * R;
@@ -634,15 +652,19 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     double ada_step = P.object_step;
     double ada_previous = 0.0;
     bool ada_has_previous = false;
-    // Push exchange for cluster tiles of every family except EPRY with pupil
-    // recovery, GD with pupil recovery and spectral AP (their P7 reads the
-    // staged stencil) and truncated GD (its statistics steps stop after P4).
-    // Two cluster barriers remain per frame: after P1, overlapped with P2,
-    // and at the frame end. mbarriers: 0 receive buffer (reusing the stencil
-    // slab), 1 field rows, 2 halo row.
-    constexpr bool push = C > 1 && !(epry || gd_pupil || spectral || truncating);
+    // Push exchange for 256-point tiles of every family except EPRY with
+    // pupil recovery, GD with pupil recovery and spectral AP (their P7 reads
+    // the staged stencil) and truncated GD (its statistics steps stop after
+    // P4); smaller tiles keep the pull exchange, whose padded receive rows
+    // would not fit their stencil slab. Two cluster barriers remain per
+    // frame: after P1, overlapped with P2, and at the frame end. mbarriers:
+    // 0 receive buffer (reusing the stencil slab), 1 field rows, 2 halo row.
+    constexpr bool push = C == 16 && !(epry || gd_pupil || spectral || truncating);
     constexpr int ROWS = R / C;
-    constexpr unsigned kDenseBytes = (unsigned)((C - 1) * ROWS * N * sizeof(float2));
+    constexpr unsigned kRowBytes = (unsigned)(K::RS * sizeof(float2));  // one padded row, one bulk copy
+    constexpr unsigned kDenseBytes = (unsigned)((C - 1) * ROWS) * kRowBytes;
+    static_assert(!push || (K::R * K::RS <= K::STAGE && kRowBytes % 16 == 0 && (K::FIELD * 8) % 16 == 0),
+                  "padded receive rows fit the stencil slab, 16-byte aligned");
     __shared__ __align__(8) unsigned long long s_mbar[3];
     __shared__ unsigned s_bytes[2];  // expected bytes: P3 input, P5 output
     __shared__ int s_sync_failed;
@@ -656,8 +678,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 if (x == c) continue;
                 for (int m = 0; m < ROWS; ++m) {
                     const int i3 = x * R + c * ROWS + m, i5 = c * R + x * ROWS + m;
-                    if (i3 >= row_lo && i3 <= row_hi) b3 += N * sizeof(float2);
-                    if (i5 >= row_lo && i5 <= row_hi) a5 += N * sizeof(float2);
+                    if (i3 >= row_lo && i3 <= row_hi) b3 += kRowBytes;
+                    if (i5 >= row_lo && i5 <= row_hi) a5 += kRowBytes;
                 }
             }
             s_bytes[0] = b3;
@@ -667,7 +689,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             fence_mbar_init_cluster();
             mbar_arrive_expect_tx(&s_mbar[0], b3);
             mbar_arrive_expect_tx(&s_mbar[1], kDenseBytes);
-            if (c > 0) mbar_arrive_expect_tx(&s_mbar[2], N * sizeof(float2));
+            if (c > 0) mbar_arrive_expect_tx(&s_mbar[2], kRowBytes);
         }
     }
     // One exchange step on mbarrier k: every thread waits (bounded) for the
@@ -834,12 +856,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 __syncthreads();
                 if constexpr (gd_pupil) {
                     if (batch_boundary) {
-                        if (pupil_active > 0) gd_pupil_apply<K>(T, pslab, P, c, P.pupil_step / (float)pupil_active);
+                        if (pupil_active > 0) gd_pupil_apply<K>(T, pslab, P, c, (float)(P.pupil_step / pupil_active));
                         pupil_active = 0;
                     }
                 }
                 if (batch_end) {
-                    if (batch_active > 0) gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
+                    if (batch_active > 0) gd_batch_apply<K>(T, (float)(P.object_step / batch_active), c);
                     batch_active = 0;
                     cluster_barrier<K>();
                 }
@@ -971,7 +993,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                     if (first) frame_loss += point_loss<LOSS>(fmaf(gain, pk, bg), meas, P.loss);
                     const float target = fmaxf((meas - bg) * inv_gain, 0.f);
-                    if (pk > P.eps)
+                    if (pk > eps)
                         v[k] = cscale(psi, sqrtf(target / pk) - 1.f);
                     else
                         v[k] = make_float2(sqrtf(target * sp.inv_weight_sum) - psi.x, -psi.y);
@@ -1052,7 +1074,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                                 } else {
                                     frame_loss += point_loss<LOSS>(gain * intrinsic, gain * a * a, P.loss);
                                 }
-                                v[k] = intrinsic > P.eps ? cscale(v[k], fmaf(a, r, -1.f))
+                                v[k] = intrinsic > eps ? cscale(v[k], fmaf(a, r, -1.f))
                                                          : make_float2(a - v[k].x, -v[k].y);
                             } else {
                                 v[k] = make_float2(0.f, 0.f);
@@ -1063,12 +1085,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                             } else if constexpr (LOSS == 0) {
                                 const float d = s_amp - a;
                                 frame_loss = fmaf(d, d, frame_loss);
-                                v[k] = cscale(v[k], 1.f - a * rsqrtf(fmaxf(intrinsic, P.eps)));
+                                v[k] = cscale(v[k], 1.f - a * rsqrtf(fmaxf(intrinsic, eps)));
                             } else {
                                 const float target = a * a;
                                 frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
                                 const bool kept = !truncating || fabsf(target - intrinsic) <= trunc_scale * sqrtf(intrinsic);
-                                v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, P.eps) : 0.f);
+                                v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, eps) : 0.f);
                             }
                         }
                     }
@@ -1085,7 +1107,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     if constexpr (projection) {
                         if (!masked) {
                             frame_loss += point_loss<LOSS>(fmaf(gain, intrinsic, bg), meas, P.loss);
-                            v[k] = intrinsic > P.eps ? cscale(v[k], fmaf(sqrtf(target), rsqrtf(intrinsic), -1.f))
+                            v[k] = intrinsic > eps ? cscale(v[k], fmaf(sqrtf(target), rsqrtf(intrinsic), -1.f))
                                                      : make_float2(sqrtf(target) - v[k].x, -v[k].y);
                         } else {
                             v[k] = make_float2(0.f, 0.f);
@@ -1096,7 +1118,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         } else {
                             frame_loss += point_loss<LOSS>(intrinsic, target, P.loss);
                             const bool kept = !truncating || fabsf(target - intrinsic) <= trunc_scale * sqrtf(intrinsic);
-                            v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, P.eps) : 0.f);
+                            v[k] = cscale(v[k], kept ? descent_factor<LOSS>(intrinsic, target, P.loss, eps) : 0.f);
                         }
                     }
                     }
@@ -1104,11 +1126,11 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 if (!stats) {
                     if constexpr (push) {
                         // Row `row` of this column goes to the CTA owning its cross step.
+                        // Rows this CTA owns go to its own rbuf; the others stay in
+                        // place and are copied to their owners below.
                         auto to_owner = [&](int row, float2 x) {
-                            const int o = row / ROWS, m = row % ROWS;
-                            float2* dst = rbuf + (c * ROWS + m) * N + q4;
-                            if (o == c) *dst = x;
-                            else st_async(dsmem_address(dst, o), x, dsmem_address(&s_mbar[0], o));
+                            if (row / ROWS == c) rbuf[(c * ROWS + row % ROWS) * K::RS + pq] = x;
+                            else fld[row * K::RS + pq] = x;
                         };
                         if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_owner);
                         else column_forward_local<K>(c, tw, v, to_owner);
@@ -1126,8 +1148,13 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 continue;
             }
             if constexpr (push) {
-                // P5 input rows from every CTA, then the results into the field rows.
+                // P4 rows owned by other CTAs go to them; then P5's input rows
+                // from every CTA, and its results into the field rows.
+                fence_proxy_async_smem();
                 __syncthreads();
+                if (tid < R && tid / ROWS != c)
+                    bulk_copy_to_peer(dsmem_address(rbuf + (c * ROWS + tid % ROWS) * K::RS, tid / ROWS),
+                                      fld + tid * K::RS, kRowBytes, dsmem_address(&s_mbar[0], tid / ROWS));
                 exchange(0, ph_recv, s_bytes[0]);      // P5 input; next: the next frame's P3 input
                 columns_cross_forward_push<K>(fld, rbuf, &s_mbar[1], c, row_lo, row_hi);
                 __syncthreads();
@@ -1168,13 +1195,16 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             // by the pupil updates.
             {
                 const float inv_n2 = 1.0f / (float)(N * N);
-                const float max_p2 = epry || gd_pupil ? fmaxf(frame_max_pup, P.eps) : T.max_pupil_power;
+                // The frame's scalars in FP64, each rounded once.
+                const double max_p2 =
+                    epry || gd_pupil ? (double)fmaxf(frame_max_pup, eps) : T.max_pupil_power;
+                const double obj_den = (double)fmaxf(frame_max_obj, eps) + P.eps;
                 // Pupil gradient weight w * (N^2 / valid) / (max |patch|^2 + eps).
-                const float pupil_grad_scale =
-                    gd_pupil ? fp.weight * fp.valid_scale / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
-                const float inv_global = 1.0f / (max_p2 + P.eps);
-                const float pupil_scale =
-                    epry ? fp.weight * P.pupil_step / (fmaxf(frame_max_obj, P.eps) + P.eps) : 0.f;
+                const float pupil_grad_scale = gd_pupil ? (float)((double)fp.weight * fp.valid_scale / obj_den) : 0.f;
+                const float inv_global = (float)(1.0 / (max_p2 + P.eps));
+                const float pupil_scale = epry ? (float)((double)fp.weight * P.pupil_step / obj_den) : 0.f;
+                // rPIE: 1 / ((1 - alpha) |P|^2 + alpha max|P|^2 + eps) = 1 / (rpie_a |P|^2 + rpie_b).
+                const float rpie_a = (float)(1.0 - P.alpha), rpie_b = (float)(P.alpha * max_p2 + P.eps);
                 // U of one task (row l, column class jb) into v, from the row's
                 // transform in v: pixels j = (NB * ja + jb + N / 2) mod N.
                 auto correction = [&](float2 (&v)[NA], int i, int jb) {
@@ -1190,9 +1220,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                             const float pw = cnorm2(pv);
                             float inv_den;
                             if constexpr (ALG == kAlgLocal || ALG == kAlgLocalAdaptive || spectral)
-                                inv_den = 1.0f / (pw + P.eps);
+                                inv_den = 1.0f / (pw + eps);
                             else if constexpr (ALG == kAlgRpie)
-                                inv_den = 1.0f / ((1.f - P.alpha) * pw + P.alpha * max_p2 + P.eps);
+                                inv_den = 1.0f / fmaf(rpie_a, pw, rpie_b);
                             else
                                 inv_den = inv_global;
                             u = cscale(cmulc(psi, pv), inv_den);
@@ -1238,10 +1268,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         for (int ja = 0; ja < NA; ++ja) {
                             const int j = (NB * ja + jb + N / 2) & (N - 1);
                             fld[l * K::RS + j] = v[ja];
-                            if constexpr (push) {
-                                if (l == R - 1 && c < C - 1)
-                                    st_async(dsmem_address(field + j, c + 1), v[ja], dsmem_address(&s_mbar[2], c + 1));
-                            } else {
+                            if constexpr (!push) {
                                 if (l == R - 1 && next_halo) next_halo[j] = v[ja];
                             }
                         }
@@ -1280,8 +1307,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 }
             }
             if constexpr (push) {
-                __syncthreads();  // U rows of this CTA
-                if (c > 0) exchange(2, ph_halo, N * sizeof(float2));  // the halo row from CTA c - 1
+                fence_proxy_async_smem();
+                __syncthreads();  // U rows of this CTA; its last row is the next CTA's halo
+                if (tid == 0 && c < C - 1)
+                    bulk_copy_to_peer(dsmem_address(field, c + 1), fld + (R - 1) * K::RS, kRowBytes,
+                                      dsmem_address(&s_mbar[2], c + 1));
+                if (c > 0) exchange(2, ph_halo, kRowBytes);  // the halo row from CTA c - 1
             } else {
                 cluster_barrier<K>();
             }
@@ -1291,10 +1322,10 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // Projection: O += w * step * adj(U). Gradient descent: O -= step *
                 // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
                 // (N^2 / valid) * adj(U).
-                const float scale = spectral     ? sp.update_scale * P.object_step
-                                    : projection ? fp.weight * (adaptive ? (float)ada_step : P.object_step)
+                const float scale = spectral     ? (float)((double)sp.update_scale * P.object_step)
+                                    : projection ? (float)((double)fp.weight * (adaptive ? ada_step : P.object_step))
                                     : gd_batched ? fp.weight * fp.valid_scale
-                                                 : -P.object_step * fp.weight * fp.valid_scale;
+                                                 : (float)(-P.object_step * (double)fp.weight * fp.valid_scale);
                 // Spectral updates stage the current object at the step start: an
                 // earlier mode of the same exposure may have changed it.
                 float2* target = gd_batched ? T.gradient : obj;
@@ -1339,12 +1370,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             if constexpr (gd_pupil) {
                 if (batch_boundary) {
-                    gd_pupil_apply<K>(T, pslab, P, c, P.pupil_step / (float)pupil_active);
+                    gd_pupil_apply<K>(T, pslab, P, c, (float)(P.pupil_step / pupil_active));
                     pupil_active = 0;
                 }
             }
             if (batch_end) {
-                gd_batch_apply<K>(T, P.object_step / (float)batch_active, c);
+                gd_batch_apply<K>(T, (float)(P.object_step / batch_active), c);
                 batch_active = 0;
                 cluster_barrier<K>();
             }

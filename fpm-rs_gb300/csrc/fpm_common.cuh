@@ -149,7 +149,7 @@ FPM_DEVICE void dsmem_store(unsigned address, float2 v) {
 }
 
 // ---------------------------------------------------------------- mbarriers
-// A CTA's receive buffers are filled by its peers with st.async, each store
+// A CTA's receive buffers are filled by its peers with bulk copies, each
 // completing its bytes on the receiving CTA's own mbarrier; the receiver arms
 // each phase with the bytes it expects (arrival count 1) and waits on the
 // phase parity. Waits are bounded in time: after kMbarWaitNs the wait gives
@@ -207,13 +207,18 @@ FPM_DEVICE bool mbar_wait(unsigned long long* bar, unsigned parity) {
     }
 }
 
-// 8-byte store into a peer CTA's shared memory (cluster address `remote`)
-// that completes 8 bytes on the peer's mbarrier at cluster address `bar`.
-FPM_DEVICE void st_async(unsigned remote, float2 v, unsigned bar) {
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];\n" ::"r"(remote),
-                 "f"(v.x), "f"(v.y), "r"(bar)
+// Bulk copy of `bytes` (a multiple of 16, both ends 16-byte aligned) from
+// this CTA's shared memory into a peer's (cluster address `dst`), completing
+// the bytes on the peer's mbarrier at cluster address `bar`.
+FPM_DEVICE void bulk_copy_to_peer(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "r"(smem_u32(src)), "r"(bytes), "r"(bar)
                  : "memory");
 }
+
+// Orders this thread's earlier shared-memory writes before later bulk
+// copies (the async proxy) that read or overwrite them.
+FPM_DEVICE void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
 // Split cluster barrier: arrive (releasing this thread's prior writes) now,
 // wait (acquiring the others') later, with independent work in between.

@@ -74,7 +74,7 @@ struct TileDesc {
                                // 32 adaptive pass objective, 64 non-finite recovered pupil, 128 non-finite
                                // regulariser step
     int M, frame_count;
-    float max_pupil_power;     // max(max |P|^2, eps) for fixed-pupil algorithms
+    double max_pupil_power;    // max(max |P|^2, eps) for fixed-pupil algorithms, FP64
     int amplitude;             // 1: meas holds sqrt(max(I / gain, 0)), -1 where masked; no masks or background
     double weight_sum;         // sum of frame weights: the objective's denominator
     // Centred pupil rows [row_lo, row_hi] that hold a non-zero pupil value.
@@ -109,7 +109,9 @@ enum EngineAlg {
 struct EngineParams {
     const TileDesc* tiles;
     int alg;
-    float alpha, eps, object_step, pupil_step;
+    // Step sizes, the rPIE blend and epsilon in FP64: per-frame scales and
+    // denominator constants are formed in FP64 and rounded once to float.
+    double alpha, eps, object_step, pupil_step;
     int constrain_pupil;
     int momentum, interval;
     float friction, feedback;

@@ -969,7 +969,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     std::vector<fpm::IlluminationTile> ill_tiles(illum ? count : 0);
     std::vector<double2*> scratch(count);
     std::vector<float2*> objects(count), anchors(count), velocities(count);
-    float max_pupil_power = 0.f;
+    double max_pupil_power = 0.0;
     for (int t = 0; t < count; ++t) {
         fpm_problem* p = b.problems[t];
         const size_t n2 = (size_t)N * N;
@@ -1030,7 +1030,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         for (size_t i = 0; i < n2; ++i)
             mp = std::max(mp, p->pupil[2 * i] * p->pupil[2 * i] + p->pupil[2 * i + 1] * p->pupil[2 * i + 1]);
         mp = std::max(mp, a->epsilon);
-        max_pupil_power = (float)mp;
+        max_pupil_power = mp;
         fpm::TileDesc& T = tiles[t];
         T.object = p->object.as<float2>();
         T.pupil = p->pupil_state.as<float2>();
@@ -1232,10 +1232,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                                              : fpm::kAlgGradient;
             break;
     }
-    ep.alpha = (float)a->stability;
-    ep.eps = (float)a->epsilon;
-    ep.object_step = (float)a->object_step;
-    ep.pupil_step = (float)a->pupil_step;
+    ep.alpha = a->stability;
+    ep.eps = a->epsilon;
+    ep.object_step = a->object_step;
+    ep.pupil_step = a->pupil_step;
     // With pupil smoothing the support is imposed after the smoothing step.
     ep.constrain_pupil = a->constrain_pupil_support && !smoothing ? 1 : 0;
     ep.momentum = mpie ? 1 : 0;
@@ -2131,7 +2131,7 @@ fpm::TileDesc spectral_tile(const SpectralJob& j) {
     T.status = j.status.as<int>();
     T.M = j.M;
     T.frame_count = j.E;
-    T.max_pupil_power = 1.f;
+    T.max_pupil_power = 1.0;
     T.weight_sum = j.weight_total;
     T.row_lo = 0;
     T.row_hi = j.N - 1;
@@ -2145,8 +2145,8 @@ fpm::TileDesc spectral_tile(const SpectralJob& j) {
 fpm::EngineParams spectral_engine_params(const fpm_spectral_params* a, int completed) {
     fpm::EngineParams ep{};
     ep.alg = fpm::kAlgSpectral;
-    ep.eps = (float)a->epsilon;
-    ep.object_step = (float)a->object_step;
+    ep.eps = a->epsilon;
+    ep.object_step = a->object_step;
     ep.loss = a->loss_type;
     ep.gd_batch = 1;
     ep.it_begin = completed;
