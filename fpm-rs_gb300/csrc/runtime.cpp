@@ -935,6 +935,12 @@ struct BucketRun {
     // launched (device work only). Captured run plans do the two apart: the
     // preparation once, the launch inside a CUDA graph capture.
     bool prepare = true, launch = true;
+    bool captured = false;  // launched inside a stream capture: timing events become graph nodes
+    cudaError_t record(cudaEvent_t e, cudaStream_t s) const {
+        // Inside a capture a plain record only orders streams; an external
+        // record is a node that records the event at each replay.
+        return captured ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+    }
     ~BucketRun() {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (first) cudaEventDestroy(first);
@@ -1196,7 +1202,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(get_plan(ctx, M, plan));
         FPM_TRY(get_plan(ctx, N, plan));
     }
-    if (br.launch) FPM_CUDA(cudaEventRecord(br.first, s));
+    if (br.launch) FPM_CUDA(br.record(br.first, s));
 
     // Initial object: mean amplitude, upsample, forward FFT (FP64), fftshift;
     // one launch pair for all tiles of the bucket. A resumed run has restored
@@ -1257,9 +1263,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         br.events.push_back(e1);
         ep.it_begin = it0;
         ep.it_end = it1;
-        FPM_CUDA(cudaEventRecord(e0, s));
+        FPM_CUDA(br.record(e0, s));
         FPM_CUDA(fpm::launch_engine(N, ep, count, s));
-        FPM_CUDA(cudaEventRecord(e1, s));
+        FPM_CUDA(br.record(e1, s));
         br.launches += 1;
         return Status::ok();
     };
@@ -1398,7 +1404,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                                           br.scratch_ptrs.as<double2*>(), count, M, s));
     FPM_TRY(fft2_device(ctx, br.scratch_ptrs.as<double2*>(), count, M, M, true, s));
     br.launches += 3;
-    FPM_CUDA(cudaEventRecord(br.last, s));
+    FPM_CUDA(br.record(br.last, s));
     return Status::ok();
 }
 
@@ -2558,6 +2564,7 @@ Status plan_create(fpm_context* ctx, int count, fpm_problem* const* problems, co
             BucketRun& br = *plan->runs[k];
             br.prepare = false;
             br.launch = true;
+            br.captured = true;
             FPM_TRY(run_bucket(ctx, plan->buckets[k], &plan->params, ctx->streams[k % fpm_context::kStreams], br));
         }
         for (int k = 1; k < ns; ++k) {
