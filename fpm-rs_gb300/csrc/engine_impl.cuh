@@ -287,152 +287,6 @@ FPM_DEVICE void columns_cross_forward(float2* __restrict__ fld, int c, int row_l
     }
 }
 
-// Push exchange (256-point tiles, 16-CTA clusters). After P2 the rows
-// travel to the CTA that owns their cross-CTA column step: CTA o owns local
-// row o of every CTA (ROWS = R / C = 1), received into its buffer `rbuf`
-// (padded rows, stride RS, the stencil slab's space) at row `sender`. Each
-// row is one bulk copy of RS complex values into the peer's shared memory,
-// completing its bytes on the peer's receive mbarrier; the owner's radix-C
-// results go back the same way into the field rows of the CTAs that hold
-// them, completing on their row mbarrier. Results bound for another CTA are
-// first written in place over the rows they were computed from, so every
-// copy reads whole contiguous rows. No CTA reads another's shared memory and
-// a CTA waits only for the rows it consumes. A copy's source is never
-// rewritten before its receiver has it: each later write to it follows,
-// through the exchange chain, the receiver's wait.
-// P1 (as rows_inverse), then: peers may reuse their stencil slab as receive
-// buffer once this CTA has read its own, so the cluster arrival comes right
-// after P1; P2 runs in place meanwhile (rows owned by this CTA go straight
-// into its own rbuf), and after the matching wait each live row is copied
-// to its owner.
-template <class K>
-FPM_DEVICE void rows_inverse_push(float2* __restrict__ fld, float2* __restrict__ rbuf, unsigned long long* recv_bar,
-                                  const float2* __restrict__ ostage, const float2* __restrict__ tw,
-                                  const float2* __restrict__ pslab, const FrameParam& fp, int c, int i_lo, int row_lo,
-                                  int row_hi) {
-    constexpr int N = K::N, NA = K::NA, NB = K::NB, ROWS = K::R / K::C;
-#pragma unroll 1
-    for (int t = 0; t < K::T1; ++t) {
-        const int task = threadIdx.x + t * K::THREADS;
-        const int l = task / NB, nb = task % NB;
-        const int i = centred_row<K>(c, l);
-        if (i < row_lo || i > row_hi) continue;
-        const int il = i - i_lo;
-        float2 v[NA];
-#pragma unroll
-        for (int na = 0; na < NA; ++na) {
-            const int j = (NB * na + nb + N / 2) & (N - 1);
-            v[na] = cmul(patch_at(ostage, K::ORS, il, j, fp), pslab[il * N + j]);
-        }
-        dft_reg<NA, true>(v);
-        float2* row = fld + l * K::RS;
-#pragma unroll
-        for (int ka = 0; ka < NA; ++ka) row[phys<K>(NB * ka + nb)] = twiddle_smem<true>(v[ka], tw, nb * ka * K::TW);
-    }
-    __syncthreads();
-    fence_proxy_async_smem();  // this CTA's writes before the copies peers will make into it
-    cluster_arrive();
-#pragma unroll 1
-    for (int t = 0; t < K::T2; ++t) {
-        const int task = threadIdx.x + t * K::THREADS;
-        const int l = task / NA, ka = task % NA;
-        const int i = centred_row<K>(c, l);
-        if (i < row_lo || i > row_hi) continue;
-        const float2* g = fld + l * K::RS + ka * (NB + 1);
-        float2 v[NB];
-#pragma unroll
-        for (int kb = 0; kb < NB; ++kb) v[kb] = g[kb];
-        dft_reg<NB, true>(v);
-        float2* out = l / ROWS == c ? rbuf + (c * ROWS + l % ROWS) * K::RS + ka * (NB + 1) : fld + l * K::RS + ka * (NB + 1);
-#pragma unroll
-        for (int kb = 0; kb < NB; ++kb) out[kb] = v[kb];
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    cluster_wait();
-    if (threadIdx.x < K::R) {
-        const int l = threadIdx.x, o = l / ROWS, i = centred_row<K>(c, l);
-        if (o != c && i >= row_lo && i <= row_hi)
-            bulk_copy_to_peer(dsmem_address(rbuf + (c * ROWS + l % ROWS) * K::RS, o), fld + l * K::RS,
-                              K::RS * sizeof(float2), dsmem_address(recv_bar, o));
-    }
-}
-
-// P3, push form: this CTA's rows of every CTA from rbuf (zeros for rows the
-// pupil leaves empty), the radix-C inverse step, then each result row to
-// the CTA that holds it.
-template <class K>
-FPM_DEVICE void columns_cross_inverse_push(float2* __restrict__ fld, float2* __restrict__ rbuf,
-                                           unsigned long long* rows_bar, const float2* __restrict__ tw, int c,
-                                           int row_lo, int row_hi) {
-    constexpr int C = K::C, N = K::N, ROWS = K::R / C;
-#pragma unroll 1
-    for (int t = 0; t < K::TX; ++t) {
-        const int task = threadIdx.x + t * K::THREADS;
-        const int mrow = task / N, q = task % N;
-        const int l = c * ROWS + mrow, pq = phys<K>(q);
-        float2 v[C];
-#pragma unroll
-        for (int nc = 0; nc < C; ++nc) {
-            // Natural block nc lives in CTA nc ^ (C / 2) as centred rows (nc ^ (C / 2)) * R + l.
-            const int x = nc ^ (C / 2);
-            const int i = x * K::R + l;
-            v[nc] = i >= row_lo && i <= row_hi ? rbuf[(x * ROWS + mrow) * K::RS + pq] : make_float2(0.f, 0.f);
-        }
-        dft_reg<C, true>(v);
-#pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) {
-            const float2 val = twiddle_smem<true>(v[k1], tw, l * k1 * K::TW);
-            if (k1 == c) fld[l * K::RS + pq] = val;
-            else rbuf[(k1 * ROWS + mrow) * K::RS + pq] = val;
-        }
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x < C * ROWS) {
-        const int k1 = threadIdx.x / ROWS, mrow = threadIdx.x % ROWS;
-        if (k1 != c)
-            bulk_copy_to_peer(dsmem_address(fld + (c * ROWS + mrow) * K::RS, k1), rbuf + (k1 * ROWS + mrow) * K::RS,
-                              K::RS * sizeof(float2), dsmem_address(rows_bar, k1));
-    }
-}
-
-// P5, push form: column values of this CTA's rows from every CTA (rbuf), the
-// radix-C forward step, and each output row to the CTA holding its natural
-// rows when the pupil reaches them.
-template <class K>
-FPM_DEVICE void columns_cross_forward_push(float2* __restrict__ fld, float2* __restrict__ rbuf,
-                                           unsigned long long* rows_bar, int c, int row_lo, int row_hi) {
-    constexpr int C = K::C, N = K::N, ROWS = K::R / C;
-#pragma unroll 1
-    for (int t = 0; t < K::TX; ++t) {
-        const int task = threadIdx.x + t * K::THREADS;
-        const int mrow = task / N, q = task % N;
-        const int l = c * ROWS + mrow, pq = phys<K>(q);
-        float2 v[C];
-#pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) v[k1] = rbuf[(k1 * ROWS + mrow) * K::RS + pq];
-        dft_reg<C, false>(v);
-#pragma unroll
-        for (int j1 = 0; j1 < C; ++j1) {
-            const int target = j1 ^ (C / 2);
-            const int i = target * K::R + l;
-            if (i < row_lo || i > row_hi) continue;
-            if (target == c) fld[l * K::RS + pq] = v[j1];
-            else rbuf[(j1 * ROWS + mrow) * K::RS + pq] = v[j1];
-        }
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x < C * ROWS) {
-        const int j1 = threadIdx.x / ROWS, mrow = threadIdx.x % ROWS;
-        const int target = j1 ^ (C / 2), l = c * ROWS + mrow, i = target * K::R + l;
-        if (target != c && i >= row_lo && i <= row_hi)
-            bulk_copy_to_peer(dsmem_address(fld + l * K::RS, target), rbuf + (j1 * ROWS + mrow) * K::RS,
-                              K::RS * sizeof(float2), dsmem_address(rows_bar, target));
-    }
-}
-
 // P4 column transforms with two threads per column: lanes l and l ^ 16 of a
 // warp share column position q; half h = lane / 16 holds local rows
 // n2 and n2 + 16 for n2 in [8h, 8h + 8). The 32-point transform is split as
@@ -465,8 +319,9 @@ FPM_DEVICE void column_inverse_split(const float2* __restrict__ fld, int pq, int
 // Forward, the dual: z[k] holds x'[h + 2k]; writes natural rows n2 and n2 + 16
 // for n2 in [8h, 8h + 8), each times w_N^(-c * row) when the cluster splits
 // the column (C > 1).
-template <class K, class Emit>
-FPM_DEVICE void column_forward_split(int h, int c, const float2* __restrict__ tw, float2 (&z)[16], Emit emit) {
+template <class K>
+FPM_DEVICE void column_forward_split(float2* __restrict__ fld, int pq, int h, int c, const float2* __restrict__ tw,
+                                     float2 (&z)[16]) {
     dft_reg<16, false>(z);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -480,8 +335,8 @@ FPM_DEVICE void column_forward_split(int h, int c, const float2* __restrict__ tw
             lo = twiddle_smem<false>(lo, tw, c * row * K::TW);
             hi = twiddle_smem<false>(hi, tw, c * (row + 16) * K::TW);
         }
-        emit(row, lo);
-        emit(row + 16, hi);
+        fld[row * K::RS + pq] = lo;
+        fld[(row + 16) * K::RS + pq] = hi;
     }
 }
 
@@ -496,11 +351,12 @@ FPM_DEVICE void column_inverse_local(const float2* __restrict__ fld, int pq, flo
     dft_reg<16, true>(z);
 }
 
-template <class K, class Emit>
-FPM_DEVICE void column_forward_local(int c, const float2* __restrict__ tw, float2 (&z)[16], Emit emit) {
+template <class K>
+FPM_DEVICE void column_forward_local(float2* __restrict__ fld, int pq, int c, const float2* __restrict__ tw,
+                                     float2 (&z)[16]) {
     dft_reg<16, false>(z);
 #pragma unroll
-    for (int b = 0; b < 16; ++b) emit(b, K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b]);
+    for (int b = 0; b < 16; ++b) fld[b * K::RS + pq] = K::C > 1 ? twiddle_smem<false>(z[b], tw, c * b * K::TW) : z[b];
 }
 
 // End of a gradient-descent mini-batch (src/algorithms/gradient_descent.rs:
@@ -652,62 +508,6 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     double ada_step = P.object_step;
     double ada_previous = 0.0;
     bool ada_has_previous = false;
-    // Push exchange for 256-point tiles of every family except EPRY with
-    // pupil recovery, GD with pupil recovery and spectral AP (their P7 reads
-    // the staged stencil) and truncated GD (its statistics steps stop after
-    // P4); smaller tiles keep the pull exchange, whose padded receive rows
-    // would not fit their stencil slab. Two cluster barriers remain per
-    // frame: after P1, overlapped with P2, and at the frame end. mbarriers:
-    // 0 receive buffer (reusing the stencil slab), 1 field rows, 2 halo row.
-    constexpr bool push = C == 16 && !(epry || gd_pupil || spectral || truncating);
-    constexpr int ROWS = R / C;
-    constexpr unsigned kRowBytes = (unsigned)(K::RS * sizeof(float2));  // one padded row, one bulk copy
-    constexpr unsigned kDenseBytes = (unsigned)((C - 1) * ROWS) * kRowBytes;
-    static_assert(!push || (K::R * K::RS <= K::STAGE && kRowBytes % 16 == 0 && (K::FIELD * 8) % 16 == 0),
-                  "padded receive rows fit the stencil slab, 16-byte aligned");
-    __shared__ __align__(8) unsigned long long s_mbar[3];
-    __shared__ unsigned s_bytes[2];  // expected bytes: P3 input, P5 output
-    __shared__ int s_sync_failed;
-    float2* const rbuf = osm;
-    unsigned ph_recv = 0, ph_rows = 0, ph_halo = 0;
-    if constexpr (push) {
-        if (tid == 0) {
-            // Rows arrive only where the pupil reaches (the rest are zero).
-            unsigned b3 = 0, a5 = 0;
-            for (int x = 0; x < C; ++x) {
-                if (x == c) continue;
-                for (int m = 0; m < ROWS; ++m) {
-                    const int i3 = x * R + c * ROWS + m, i5 = c * R + x * ROWS + m;
-                    if (i3 >= row_lo && i3 <= row_hi) b3 += kRowBytes;
-                    if (i5 >= row_lo && i5 <= row_hi) a5 += kRowBytes;
-                }
-            }
-            s_bytes[0] = b3;
-            s_bytes[1] = a5;
-            s_sync_failed = 0;
-            for (int k = 0; k < 3; ++k) mbar_init(&s_mbar[k], 1);
-            fence_mbar_init_cluster();
-            mbar_arrive_expect_tx(&s_mbar[0], b3);
-            mbar_arrive_expect_tx(&s_mbar[1], kDenseBytes);
-            if (c > 0) mbar_arrive_expect_tx(&s_mbar[2], kRowBytes);
-        }
-    }
-    // One exchange step on mbarrier k: every thread waits (bounded) for the
-    // current phase, the block synchronises, and only then thread 0 arms the
-    // next phase with `next_bytes`. Arming after every thread has seen the
-    // completion matters: a phase that expects no bytes completes as it is
-    // armed, and a thread still polling the previous phase would then see
-    // its parity again. A timeout sets status bit 512; the CTA then skips
-    // its later waits and arms nothing more, so the launch still ends.
-    auto exchange = [&](int k, unsigned& parity, unsigned next_bytes) {
-        if (!s_sync_failed && !mbar_wait(&s_mbar[k], parity)) {
-            s_sync_failed = 1;
-            atomicOr(T.status, 512);
-        }
-        parity ^= 1u;
-        __syncthreads();
-        if (tid == 0 && !s_sync_failed) mbar_arrive_expect_tx(&s_mbar[k], next_bytes);
-    };
     __syncthreads();
 
     for (int it = P.it_begin; it < P.it_end; ++it) {
@@ -878,12 +678,9 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
 
             // P1, P2
             float max_obj = 0.f, max_pup = 0.f;
-            if constexpr (push) {
-                rows_inverse_push<K>(fld, rbuf, &s_mbar[0], ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi);
-            } else if (!spectral_update) {
+            if (!spectral_update)
                 rows_inverse<K, epry || gd_pupil>(fld, ostage, tw, pslab, fp, c, i_lo, row_lo, row_hi, max_obj,
                                                   max_pup);
-            }
             if constexpr (epry || gd_pupil) {
                 max_obj = warp_max(max_obj);
                 max_pup = warp_max(max_pup);
@@ -902,9 +699,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     fred[2 * K::WARPS + 1] = b;
                 }
             }
-            if constexpr (!push) {
-                if (!spectral_update) cluster_barrier<K>();
-            }
+            if (!spectral_update) cluster_barrier<K>();
 
             float frame_max_obj = 0.f, frame_max_pup = 0.f;
             if constexpr (epry || gd_pupil) {
@@ -923,11 +718,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             }
 
             // P3
-            if constexpr (push) {
-                __syncthreads();                       // this CTA's own rows in rbuf
-                exchange(0, ph_recv, kDenseBytes);     // P3 input; next: P5 input
-                columns_cross_inverse_push<K>(fld, rbuf, &s_mbar[1], tw, c, row_lo, row_hi);
-            } else if constexpr (C > 1) {
+            if constexpr (C > 1) {
                 if (!spectral_update) columns_cross_inverse<K>(fld, tw, c, row_lo, row_hi);
             }
             // P4 ownership. R = 32: column position q4, half h4, slot k =
@@ -938,10 +729,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             const int mbase = (c * R + h4) * N + q4;
             constexpr int mstride = R == 32 ? 2 * N : N;
 
-            if constexpr (push) {
-                __syncthreads();                       // this CTA's own P3 results
-                exchange(1, ph_rows, s_bytes[1]);      // P3 output; next: P5 output
-            } else if constexpr (C > 1) {
+            if constexpr (C > 1) {
                 if (!spectral_update) cluster_barrier<K>();
             }
 
@@ -998,9 +786,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     else
                         v[k] = make_float2(sqrtf(target * sp.inv_weight_sum) - psi.x, -psi.y);
                 }
-                auto to_field = [&](int row, float2 x) { fld[row * K::RS + pq] = x; };
-                if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_field);
-                else column_forward_local<K>(c, tw, v, to_field);
+                if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
+                else column_forward_local<K>(fld, pq, c, tw, v);
                 if (first) loss_acc += (double)frame_loss * sp.loss_scale;
             } else {
             // P4: column inverse FFT, projection, column forward FFT.
@@ -1124,21 +911,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                 }
                 if (!stats) {
-                    if constexpr (push) {
-                        // Row `row` of this column goes to the CTA owning its cross step.
-                        // Rows this CTA owns go to its own rbuf; the others stay in
-                        // place and are copied to their owners below.
-                        auto to_owner = [&](int row, float2 x) {
-                            if (row / ROWS == c) rbuf[(c * ROWS + row % ROWS) * K::RS + pq] = x;
-                            else fld[row * K::RS + pq] = x;
-                        };
-                        if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_owner);
-                        else column_forward_local<K>(c, tw, v, to_owner);
-                    } else {
-                        auto to_field = [&](int row, float2 x) { fld[row * K::RS + pq] = x; };
-                        if constexpr (R == 32) column_forward_split<K>(h4, c, tw, v, to_field);
-                        else column_forward_local<K>(c, tw, v, to_field);
-                    }
+                    if constexpr (R == 32) column_forward_split<K>(fld, pq, h4, c, tw, v);
+                    else column_forward_local<K>(fld, pq, c, tw, v);
                     loss_acc += (double)frame_loss * fp.loss_scale;
                 }
             }
@@ -1147,26 +921,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 __syncthreads();
                 continue;
             }
-            if constexpr (push) {
-                // P4 rows owned by other CTAs go to them; then P5's input rows
-                // from every CTA, and its results into the field rows.
-                fence_proxy_async_smem();
-                __syncthreads();
-                if (tid < R && tid / ROWS != c)
-                    bulk_copy_to_peer(dsmem_address(rbuf + (c * ROWS + tid % ROWS) * K::RS, tid / ROWS),
-                                      fld + tid * K::RS, kRowBytes, dsmem_address(&s_mbar[0], tid / ROWS));
-                exchange(0, ph_recv, s_bytes[0]);      // P5 input; next: the next frame's P3 input
-                columns_cross_forward_push<K>(fld, rbuf, &s_mbar[1], c, row_lo, row_hi);
-                __syncthreads();
-                exchange(1, ph_rows, kDenseBytes);     // P5 output; next: the next frame's P3 output
-            } else {
-                cluster_barrier<K>();
+            cluster_barrier<K>();
 
-                // P5
-                if constexpr (C > 1) {
-                    columns_cross_forward<K>(fld, c, row_lo, row_hi);
-                    cluster_barrier<K>();
-                }
+            // P5
+            if constexpr (C > 1) {
+                columns_cross_forward<K>(fld, c, row_lo, row_hi);
+                cluster_barrier<K>();
             }
 
             // P6: row FFT step C' with twiddles.
@@ -1248,7 +1008,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     // centred row i is local row l, so U overwrites the row
                     // in place once the warp has read it.
                     static_assert(32 % NB == 0, "a warp holds whole rows");
-                    float2* next_halo = !push && c < C - 1 ? cg::this_cluster().map_shared_rank(field, c + 1) : nullptr;
+                    float2* next_halo = c < C - 1 ? cg::this_cluster().map_shared_rank(field, c + 1) : nullptr;
 #pragma unroll 1
                     for (int t = 0; t < K::T1; ++t) {
                         const int task = tid + t * K::THREADS;
@@ -1268,9 +1028,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         for (int ja = 0; ja < NA; ++ja) {
                             const int j = (NB * ja + jb + N / 2) & (N - 1);
                             fld[l * K::RS + j] = v[ja];
-                            if constexpr (!push) {
-                                if (l == R - 1 && next_halo) next_halo[j] = v[ja];
-                            }
+                            if (l == R - 1 && next_halo) next_halo[j] = v[ja];
                         }
                     }
                 } else {
@@ -1306,16 +1064,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     }
                 }
             }
-            if constexpr (push) {
-                fence_proxy_async_smem();
-                __syncthreads();  // U rows of this CTA; its last row is the next CTA's halo
-                if (tid == 0 && c < C - 1)
-                    bulk_copy_to_peer(dsmem_address(field, c + 1), fld + (R - 1) * K::RS, kRowBytes,
-                                      dsmem_address(&s_mbar[2], c + 1));
-                if (c > 0) exchange(2, ph_halo, kRowBytes);  // the halo row from CTA c - 1
-            } else {
-                cluster_barrier<K>();
-            }
+            cluster_barrier<K>();
 
             // P8: exact bilinear adjoint scatter of scale * U into the object.
             {
@@ -1354,9 +1103,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
                         acc = cfma(fp.w11, d1, acc);
-                        // Push families reuse the stencil slab for received rows,
-                        // so they read the current object from L2.
-                        const float2 base = j < cols8 ? (gd_batched || push ? __ldcg(grow + j) : srow[j]) : z;
+                        const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
                         out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
 #pragma unroll
@@ -1456,11 +1203,6 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         }
     }
     if (P.momentum && c == 0 && tid == 0) *T.counter = counter;
-    if constexpr (push) {
-        // After a timed-out exchange, stores that peers issued may still be
-        // on their way into this CTA's shared memory: let them land first.
-        if (s_sync_failed) linger_ns(1000000ull);
-    }
     // Peers must not exit while their shared memory may still be addressed.
     cluster_barrier<K>();
 }

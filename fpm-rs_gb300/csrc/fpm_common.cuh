@@ -147,80 +147,3 @@ FPM_DEVICE float2 dsmem_load(unsigned address) {
 FPM_DEVICE void dsmem_store(unsigned address, float2 v) {
     asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(address), "f"(v.x), "f"(v.y) : "memory");
 }
-
-// ---------------------------------------------------------------- mbarriers
-// A CTA's receive buffers are filled by its peers with bulk copies, each
-// completing its bytes on the receiving CTA's own mbarrier; the receiver arms
-// each phase with the bytes it expects (arrival count 1) and waits on the
-// phase parity. Waits are bounded in time: after kMbarWaitNs the wait gives
-// up and reports it, so a lost store can never hang the kernel.
-FPM_DEVICE unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-    return t;
-}
-
-// Spins for about `ns` nanoseconds.
-FPM_DEVICE void linger_ns(unsigned long long ns) {
-    const unsigned long long t0 = global_ns();
-    while (global_ns() - t0 < ns) {
-    }
-}
-
-constexpr unsigned long long kMbarWaitNs = 2000000000ull;  // 2 s
-
-FPM_DEVICE unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-FPM_DEVICE void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-// Makes the initialised mbarriers visible to the cluster's other CTAs.
-FPM_DEVICE void fence_mbar_init_cluster() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
-
-// The receiver's own arrival for the current phase, with the bytes its peers will complete.
-FPM_DEVICE void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// True once the phase with parity `parity` has completed; false when about
-// kMbarWaitNs have passed first. Peers' stores become visible with the
-// completion (acquire at cluster scope).
-FPM_DEVICE bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    const unsigned a = smem_u32(bar);
-    unsigned long long t0 = 0;
-    for (unsigned k = 0;; ++k) {
-        unsigned done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((k & 255u) == 0) {
-            const unsigned long long t = global_ns();
-            if (k == 0) t0 = t;
-            else if (t - t0 > kMbarWaitNs) return false;
-        }
-    }
-}
-
-// Bulk copy of `bytes` (a multiple of 16, both ends 16-byte aligned) from
-// this CTA's shared memory into a peer's (cluster address `dst`), completing
-// the bytes on the peer's mbarrier at cluster address `bar`.
-FPM_DEVICE void bulk_copy_to_peer(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
-    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
-                 "r"(smem_u32(src)), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-
-// Orders this thread's earlier shared-memory writes before later bulk
-// copies (the async proxy) that read or overwrite them.
-FPM_DEVICE void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-
-// Split cluster barrier: arrive (releasing this thread's prior writes) now,
-// wait (acquiring the others') later, with independent work in between.
-FPM_DEVICE void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
-FPM_DEVICE void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }

@@ -1499,9 +1499,6 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 64) return Status::make(FPM_ERR_NUMERICAL, "pupil update produced a non-finite value");
     if (status & 128) return Status::make(FPM_ERR_NUMERICAL, "regularization produced a non-finite value");
     if (status & 256) return Status::make(FPM_ERR_NUMERICAL, "illumination gradient or curvature is invalid");
-    if (status & 512)
-        return Status::make(FPM_ERR_TIMEOUT, "a frame-engine exchange between the CTAs of a cluster did not complete "
-                                             "within its bounded wait");
     if (!r) return Status::ok();
     if (r->objectives) fill_objectives(p, a, r->objectives);
     r->completed_iterations = a->iterations;

@@ -57,7 +57,7 @@ enum {
     FPM_ERR_NUMERICAL = 7,            /* Error::Numerical */
     FPM_ERR_UNSUPPORTED = 8,          /* Error::Unsupported */
     FPM_ERR_CUDA = 9,                 /* a CUDA runtime call failed */
-    FPM_ERR_TIMEOUT = 10              /* a bounded device wait expired (frame-engine exchange) */
+    FPM_ERR_TIMEOUT = 10              /* reserved: a bounded device wait expired */
 };
 
 enum { FPM_SHAPE_EXACT = 0, FPM_SHAPE_MINIMUM = 1, FPM_SHAPE_SMOOTH = 2, FPM_SHAPE_POWER_OF_TWO = 3 };
