@@ -15,14 +15,14 @@ import numpy as _np
 from . import _native
 from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasurementsError, InvalidModelError,
                      InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
-                     UnsupportedError)
+                     ServerBusyError, UnsupportedError)
 from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
 from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjection, Epry, Fpie, GradientDescent, Mpie,
                              ReconstructionProblem,
-                             ReconstructionResult, RunPlan, RuntimeInfo, Job, capture_batch, last_run_stats, run_batch,
+                             ReconstructionResult, Request, RunPlan, RuntimeInfo, Job, Server, capture_batch, last_run_stats, run_batch,
                              submit_batch)
 from .simulation import MeasurementStack, SimulationResult, forward_intensities, simulate
 from .spectral import (SpectralAcquisitionPlan, SpectralAlternatingProjection, SpectralChannel, SpectralFrame,
@@ -58,5 +58,5 @@ __all__ = [
     "SimulationResult",
     "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
     "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob", "RunPlan",
-    "capture_batch",
+    "capture_batch", "Server", "Request", "ServerBusyError",
 ]

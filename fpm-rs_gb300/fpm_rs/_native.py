@@ -29,6 +29,8 @@ EXPORTED = (
     "fpm_spectral_run", "fpm_spectral_run_batch", "fpm_spectral_forward",
     "fpm_run_batch_submit", "fpm_spectral_run_batch_submit", "fpm_job_poll", "fpm_job_wait", "fpm_job_stats", "fpm_job_destroy",
     "fpm_plan_create", "fpm_plan_launch", "fpm_plan_wait", "fpm_plan_collect", "fpm_plan_destroy",
+    "fpm_server_create", "fpm_server_submit", "fpm_server_poll", "fpm_server_wait", "fpm_server_stats_get",
+    "fpm_server_destroy",
 )
 
 
@@ -139,6 +141,23 @@ class RunStats(C.Structure):
         ("buckets", C.c_int32), ("bucket_size", C.c_int32 * 8), ("bucket_tiles", C.c_int32 * 8),
         ("bucket_end_ms", C.c_double * 8),
     ]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_batch", C.c_int32), ("batch_window_ms", C.c_double),
+                ("max_queue", C.c_int64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("submit_ms", C.c_double), ("admit_ms", C.c_double), ("start_ms", C.c_double),
+                ("done_ms", C.c_double), ("footprint_bytes", C.c_int64), ("status", C.c_int32),
+                ("message", C.c_char * 256)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
+                ("rejected", C.c_int64), ("batches", C.c_int64), ("in_use_bytes", C.c_int64),
+                ("peak_bytes", C.c_int64), ("waiting", C.c_int64), ("in_flight_batches", C.c_int64)]
 
 
 _lib = None

@@ -43,6 +43,10 @@ class DeviceError(FpmError):
     """A CUDA runtime call failed or no suitable GPU is present."""
 
 
+class ServerBusyError(FpmError):
+    """The serving loop's queue is full; the request was not taken."""
+
+
 _BY_STATUS = {
     1: InvalidShapeError,
     2: InvalidParameterError,
@@ -54,6 +58,7 @@ _BY_STATUS = {
     8: UnsupportedError,
     9: DeviceError,
     10: DeviceError,
+    11: ServerBusyError,
 }
 
 

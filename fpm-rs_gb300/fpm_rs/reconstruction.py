@@ -632,6 +632,123 @@ def capture_batch(algorithm: _Algorithm, problems, *, schedule="sequential") -> 
     return RunPlan(handle, algorithm, problems, params)
 
 
+class Request:
+    """One request of a Server: done() polls, wait() returns its
+    ReconstructionResult; info() gives its timeline (ms since the server
+    started: submitted, admitted, started on the device, done)."""
+
+    def __init__(self, server, rid, problem, algorithm, params, arrays, desc, keep):
+        self._server = server
+        self._id = rid
+        self._problem = problem
+        self._algorithm = algorithm
+        self._params = params
+        self._arrays = arrays
+        self._desc = desc
+        self._keep = keep  # host inputs the device reads until the request finishes
+        self._result = None
+        self._info = None
+
+    def done(self) -> bool:
+        if self._result is not None:
+            return True
+        flag = C.c_int32(0)
+        N.check(N.library().fpm_server_poll(self._server._handle, C.c_uint64(self._id), C.byref(flag)),
+                N.context().handle)
+        return bool(flag.value)
+
+    def wait(self):
+        if self._result is None:
+            info = N.RequestInfo()
+            status = N.library().fpm_server_wait(self._server._handle, C.c_uint64(self._id), C.byref(info))
+            self._info = info
+            self._keep = None
+            N.check(status, N.context().handle)
+            a, p = self._arrays, self._problem
+            elapsed = (info.done_ms - info.submit_ms) / 1e3
+            trace = [(it + 1, float(a["objectives"][it]), elapsed) for it in range(self._params.iterations)]
+            self._result = ReconstructionResult(
+                object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
+                pupil_support=p.model.pupil_support, trace=trace,
+                runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
+                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                calibrated_illumination=a["illumination"])
+            if p.name is not None:
+                self._result.metadata["problem_name"] = p.name
+        return self._result
+
+    def info(self) -> dict:
+        """Timeline of a finished request (wait() first)."""
+        self.wait()
+        i = self._info
+        return {"submit_ms": i.submit_ms, "admit_ms": i.admit_ms, "start_ms": i.start_ms, "done_ms": i.done_ms,
+                "latency_ms": i.done_ms - i.submit_ms, "footprint_bytes": i.footprint_bytes}
+
+
+class Server:
+    """The serving loop of libfpm_gpu (fpm_server_*): requests submitted from
+    any thread are admitted by device footprint against an HBM budget as
+    earlier work finishes, batched with others of the same algorithm that
+    arrive within the batching window, and run while other batches are on
+    the GPU. Each result equals a run of that request alone."""
+
+    def __init__(self, *, hbm_budget_gb: float = 150.0, max_batch: int = 16, batch_window_ms: float = 2.0,
+                 max_queue: int = 0):
+        cfg = N.ServerConfig()
+        cfg.hbm_budget_bytes = int(hbm_budget_gb * 1e9)
+        cfg.max_batch = int(max_batch)
+        cfg.batch_window_ms = float(batch_window_ms)
+        cfg.max_queue = int(max_queue)
+        ctx = N.context()
+        handle = C.c_void_p()
+        N.check(N.library().fpm_server_create(ctx.handle, C.byref(cfg), C.byref(handle)), ctx.handle)
+        self._handle = handle
+        N.own(self)
+
+    def submit(self, algorithm: _Algorithm, problem: ReconstructionProblem, *, schedule="sequential") -> Request:
+        """Queues `algorithm.run(problem)` and returns at once."""
+        params = algorithm._params(schedule)
+        desc, meas, keep = problem._descriptors()
+        result = N.ResultDesc()
+        arrays = _result_arrays(problem, params, result)
+        rid = C.c_uint64()
+        N.check(N.library().fpm_server_submit(self._handle, C.byref(desc), C.byref(meas), C.byref(params),
+                                              C.byref(result), C.byref(rid)), N.context().handle)
+        return Request(self, rid.value, problem, algorithm, params, arrays, (desc, meas, result),
+                       (keep, problem.measurements))
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.library().fpm_server_stats_get(self._handle, C.byref(st)), N.context().handle)
+        return {name: getattr(st, name) for name, _ in N.ServerStats._fields_}
+
+    _release_order = 0
+
+    def _release_native(self) -> None:
+        handle = getattr(self, "_handle", None)
+        if handle:
+            N.library().fpm_server_destroy(handle)
+            self._handle = None
+
+    def close(self) -> None:
+        """Finishes every queued and running request, then stops the loop."""
+        if getattr(self, "_handle", None) and not N.closed():
+            N.library().fpm_server_destroy(self._handle)
+        self._handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _recovers_illumination(algorithm) -> bool:
     return isinstance(algorithm, GradientDescent) and bool(algorithm.recover_illumination)
 

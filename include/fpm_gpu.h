@@ -57,7 +57,8 @@ enum {
     FPM_ERR_NUMERICAL = 7,            /* Error::Numerical */
     FPM_ERR_UNSUPPORTED = 8,          /* Error::Unsupported */
     FPM_ERR_CUDA = 9,                 /* a CUDA runtime call failed */
-    FPM_ERR_TIMEOUT = 10              /* reserved: a bounded device wait expired */
+    FPM_ERR_TIMEOUT = 10,             /* reserved: a bounded device wait expired */
+    FPM_ERR_QUEUE_FULL = 11           /* serving: the server's queue is full, the request was not taken */
 };
 
 enum { FPM_SHAPE_EXACT = 0, FPM_SHAPE_MINIMUM = 1, FPM_SHAPE_SMOOTH = 2, FPM_SHAPE_POWER_OF_TWO = 3 };
@@ -74,6 +75,7 @@ typedef struct fpm_context fpm_context;
 typedef struct fpm_problem fpm_problem;
 typedef struct fpm_job fpm_job;
 typedef struct fpm_plan fpm_plan;
+typedef struct fpm_server fpm_server;
 
 /* Microscope optics (src/experiment/optics.rs:44-68). */
 typedef struct {
@@ -447,6 +449,51 @@ int32_t fpm_plan_wait(fpm_plan *plan);
 int32_t fpm_plan_collect(fpm_plan *plan, fpm_result_desc *results);
 /* Waits for queued replays and frees the plan; its problems are free again. */
 int32_t fpm_plan_destroy(fpm_plan *plan);
+
+/* ------------------------------------------------------- serving loop */
+/* A request loop over one context: the work run_algorithm
+ * (python/src/reconstruction.rs:1107-1141) does for one caller, served to
+ * many with continuous batching. A dispatcher thread admits waiting
+ * requests in arrival order while their device footprint fits the budget
+ * beside the work in flight, sends requests of equal parameters that arrive
+ * within the batching window as one submitted batch, and admits more as
+ * batches finish, so new requests overlap the ones on the GPU. Each
+ * result is the one a run of that request alone gives. */
+typedef struct {
+    int64_t hbm_budget_bytes; /* admitted requests' device footprint at most this; 0: no limit */
+    int32_t max_batch;        /* requests of equal parameters per submitted batch, >= 1 */
+    double batch_window_ms;   /* how long the oldest waiting request waits for batch-mates */
+    int64_t max_queue;        /* waiting requests at most this (more get FPM_ERR_QUEUE_FULL); 0: no limit */
+} fpm_server_config;
+
+/* One request's times (host clock, ms since the server's creation),
+ * footprint and outcome. */
+typedef struct {
+    double submit_ms, admit_ms, start_ms, done_ms;
+    int64_t footprint_bytes;
+    int32_t status;
+    char message[256];
+} fpm_request_info;
+
+typedef struct {
+    int64_t submitted, admitted, completed, rejected, batches;
+    int64_t in_use_bytes, peak_bytes, waiting, in_flight_batches;
+} fpm_server_stats;
+
+int32_t fpm_server_create(fpm_context *ctx, const fpm_server_config *config, fpm_server **server);
+/* Queues one request and returns its id. The descriptors are copied; the
+ * arrays they point to (inputs and the result arrays) must stay valid until
+ * fpm_server_wait returns for this request. */
+int32_t fpm_server_submit(fpm_server *server, const fpm_model_desc *model, const fpm_measurement_desc *measurements,
+                          const fpm_algorithm_params *params, fpm_result_desc *result, uint64_t *request);
+/* Non-blocking: *done = 1 once the request's results are in its arrays. */
+int32_t fpm_server_poll(fpm_server *server, uint64_t request, int32_t *done);
+/* Blocks until the request has finished, fills `info` (may be NULL), forgets
+ * the request and returns its status. */
+int32_t fpm_server_wait(fpm_server *server, uint64_t request, fpm_request_info *info);
+int32_t fpm_server_stats_get(fpm_server *server, fpm_server_stats *stats);
+/* Finishes every queued and running request, then stops the dispatcher. */
+int32_t fpm_server_destroy(fpm_server *server);
 
 #ifdef __cplusplus
 }

@@ -34,6 +34,7 @@ use std::os::raw::c_char;
 pub enum FpmContext {}
 pub enum FpmProblem {}
 pub enum FpmPlan {}
+pub enum FpmServer {}
 #[link(name = "fpm_gpu")]
 extern "C" {
     pub fn fpm_create(ctx: *mut *mut FpmContext, device: i32) -> i32;
@@ -94,6 +95,13 @@ extern "C" {
     pub fn fpm_plan_wait(plan: *mut FpmPlan) -> i32;
     pub fn fpm_plan_collect(plan: *mut FpmPlan, r: *mut FpmResultDesc) -> i32;
     pub fn fpm_plan_destroy(plan: *mut FpmPlan) -> i32;
+    pub fn fpm_server_create(ctx: *mut FpmContext, config: *const FpmServerConfig, server: *mut *mut FpmServer) -> i32;
+    pub fn fpm_server_submit(server: *mut FpmServer, model: *const FpmModelDesc, m: *const FpmMeasurementDesc,
+        a: *const FpmAlgorithmParams, r: *mut FpmResultDesc, request: *mut u64) -> i32;
+    pub fn fpm_server_poll(server: *mut FpmServer, request: u64, done: *mut i32) -> i32;
+    pub fn fpm_server_wait(server: *mut FpmServer, request: u64, info: *mut FpmRequestInfo) -> i32;
+    pub fn fpm_server_stats_get(server: *mut FpmServer, stats: *mut FpmServerStats) -> i32;
+    pub fn fpm_server_destroy(server: *mut FpmServer) -> i32;
 }
 #[repr(C)] pub struct FpmJob { _opaque: [u8; 0] }
 #[repr(C)] pub struct FpmRunStats { pub kernel_launches: i32, pub engine_launches: i32, pub run_ms: f64,
@@ -114,3 +122,9 @@ extern "C" {
     pub offset_counts: f64, pub read_noise_electrons: f64, pub dark_current_electrons: f64,
     pub shot_noise: i32, pub quantize: i32, pub maximum_count: f64, pub pixel_sensitivity: *const f64,
     pub bad_pixels: *const i64, pub bad_pixel_count: i64, pub bad_pixel_value: f64 }
+#[repr(C)] pub struct FpmServerConfig { pub hbm_budget_bytes: i64, pub max_batch: i32, pub batch_window_ms: f64,
+    pub max_queue: i64 }
+#[repr(C)] pub struct FpmRequestInfo { pub submit_ms: f64, pub admit_ms: f64, pub start_ms: f64, pub done_ms: f64,
+    pub footprint_bytes: i64, pub status: i32, pub message: [c_char; 256] }
+#[repr(C)] pub struct FpmServerStats { pub submitted: i64, pub admitted: i64, pub completed: i64, pub rejected: i64,
+    pub batches: i64, pub in_use_bytes: i64, pub peak_bytes: i64, pub waiting: i64, pub in_flight_batches: i64 }

@@ -21,6 +21,7 @@ C_NAMES = {
     "AlgorithmParams": "fpm_algorithm_params", "CameraDesc": "fpm_camera_desc", "StateDesc": "fpm_state_desc",
     "SpectralModelDesc": "fpm_spectral_model_desc", "SpectralParams": "fpm_spectral_params",
     "SpectralResultDesc": "fpm_spectral_result_desc", "ResultDesc": "fpm_result_desc", "RunStats": "fpm_run_stats",
+    "ServerConfig": "fpm_server_config", "RequestInfo": "fpm_request_info", "ServerStats": "fpm_server_stats",
 }
 
 
