@@ -370,8 +370,17 @@ FPM_DEVICE void gd_batch_apply(const TileDesc& T, float step, int c) {
     const long long end = begin + per < total ? begin + per : total;
     float4* O4 = reinterpret_cast<float4*>(T.object);
     float4* G4 = reinterpret_cast<float4*>(T.gradient);
+    float4* E4 = reinterpret_cast<float4*>(T.gradient_err);  // compensated: G's rounding error
     for (long long e = begin + threadIdx.x; e < end; e += K::THREADS) {
-        const float4 g = __ldcg(G4 + e);
+        float4 g = __ldcg(G4 + e);
+        if (E4) {
+            const float4 err = __ldcg(E4 + e);
+            g.x -= err.x;
+            g.y -= err.y;
+            g.z -= err.z;
+            g.w -= err.w;
+            __stcg(E4 + e, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
         float4 o = __ldcg(O4 + e);
         o.x = fmaf(-step, g.x, o.x);
         o.y = fmaf(-step, g.y, o.y);
@@ -1078,6 +1087,7 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                 // Spectral updates stage the current object at the step start: an
                 // earlier mode of the same exposure may have changed it.
                 float2* target = gd_batched ? T.gradient : obj;
+                float2* const comp_err = spectral ? nullptr : gd_batched ? T.gradient_err : T.object_err;
                 const int rows8 = C == 1 ? N + fp.has_upper_row : R + (c == C - 1 ? fp.has_upper_row : 0);
                 const int cols8 = N + fp.has_upper_col;
                 constexpr int PER = (N + 1 + 31) / 32;
@@ -1090,10 +1100,8 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                     const float2* u1 = u0 - K::RS;  // r == 0: the halo row
                     const float2* srow = ostage + r * K::ORS;
                     float2* grow = target + (long long)(fp.lower_row + i) * ostride + fp.lower_col;
-                    float2 out[PER];
-#pragma unroll
-                    for (int t = 0; t < PER; ++t) {
-                        const int j = lane + 32 * t;
+                    // The bilinear adjoint of U at stencil column j.
+                    auto adjoint = [&](int j) {
                         const float2 z = make_float2(0.f, 0.f);
                         const float2 a = has0 && j < N ? u0[j] : z;
                         const float2 b = has0 && j >= 1 && j <= N ? u0[j - 1] : z;
@@ -1102,7 +1110,30 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
                         float2 acc = cscale(a, fp.w00);
                         acc = cfma(fp.w01, b, acc);
                         acc = cfma(fp.w10, d0, acc);
-                        acc = cfma(fp.w11, d1, acc);
+                        return cfma(fp.w11, d1, acc);
+                    };
+                    if (comp_err) {
+                        // Kahan: add scale * acc minus the carried error and keep
+                        // the new error (what the rounded sum lost), cell by cell.
+                        float2* erow = comp_err + (grow - target);
+#pragma unroll 1
+                        for (int j = lane; j < cols8; j += 32) {
+                            const float2 acc = adjoint(j);
+                            const float2 base = gd_batched ? __ldcg(grow + j) : srow[j];
+                            const float2 e = __ldcg(erow + j);
+                            const float2 y = make_float2(fmaf(scale, acc.x, -e.x), fmaf(scale, acc.y, -e.y));
+                            const float2 sum = cadd(base, y);
+                            __stcg(grow + j, sum);
+                            __stcg(erow + j, make_float2((sum.x - base.x) - y.x, (sum.y - base.y) - y.y));
+                        }
+                        continue;
+                    }
+                    float2 out[PER];
+#pragma unroll
+                    for (int t = 0; t < PER; ++t) {
+                        const int j = lane + 32 * t;
+                        const float2 z = make_float2(0.f, 0.f);
+                        const float2 acc = adjoint(j);
                         const float2 base = j < cols8 ? (gd_batched ? __ldcg(grow + j) : srow[j]) : z;
                         out[t] = j < cols8 ? cfma(scale, acc, base) : z;
                     }
@@ -1203,6 +1234,28 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         }
     }
     if (P.momentum && c == 0 && tid == 0) *T.counter = counter;
+    if (!spectral && T.object_err) {
+        // Compensated accumulation: the carried error goes back into the
+        // object at the end of the launch (every frame's P8 is done), so
+        // whatever reads the state next sees O - E; the error restarts at zero.
+        cluster_barrier<K>();
+        const long long total = (long long)M * ostride / 2;
+        const long long per = (total + C - 1) / C;
+        const long long begin = c * per;
+        const long long end = begin + per < total ? begin + per : total;
+        float4* O4 = reinterpret_cast<float4*>(T.object);
+        float4* E4 = reinterpret_cast<float4*>(T.object_err);
+        for (long long e = begin + tid; e < end; e += K::THREADS) {
+            const float4 err = __ldcg(E4 + e);
+            float4 o = __ldcg(O4 + e);
+            o.x -= err.x;
+            o.y -= err.y;
+            o.z -= err.z;
+            o.w -= err.w;
+            __stcg(O4 + e, o);
+            __stcg(E4 + e, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
+    }
     // Peers must not exit while their shared memory may still be addressed.
     cluster_barrier<K>();
 }

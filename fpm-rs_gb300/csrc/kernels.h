@@ -67,6 +67,11 @@ struct TileDesc {
     float2* velocity;          // mPIE, M*M
     float2* anchor;            // mPIE, M*M
     float2* gradient;          // mini-batch gradient descent: M*M accumulator, zero between batches
+    // Compensated accumulation (null when off): the running rounding error of
+    // the object (or, with mini-batches, of the gradient accumulator) under
+    // Kahan summation of the frame updates, M*M complex64, zero at the start.
+    float2* object_err;
+    float2* gradient_err;
     float2* pupil_gradient;    // gradient descent with pupil recovery: N*N accumulator, zero between batches
     double* partials;          // [iterations * cluster] objective partial sums
     int* counter;              // mPIE effective frames since the last event

@@ -216,6 +216,7 @@ struct fpm_problem {
     DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
+        object_err, gradient_err,
         pupil_gradient, tv_scratch, pupil_scratch;
     // GD illumination recovery: the run's frame constants, crop starts and
     // offsets, corrections and per-CTA gradient partials.
@@ -921,7 +922,7 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
     return {&p->object,     &p->pupil_state,   &p->partials,       &p->counter,    &p->status,
             &p->scratch64,  &p->velocity,      &p->anchor,         &p->order,      &p->gradient,
             &p->pupil_gradient, &p->tv_scratch, &p->pupil_scratch, &p->ill_params, &p->ill_start,
-            &p->ill_offset, &p->ill_correction, &p->ill_partials};
+            &p->ill_offset, &p->ill_correction, &p->ill_partials, &p->object_err, &p->gradient_err};
 }
 
 struct BucketRun {
@@ -959,6 +960,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     // and after every iteration (Runner::run, src/reconstruction/runner.rs:122,220).
     const bool canonical = (epry && a->recover_pupil) || gd_pupil;
     const bool gd_batched = a->algorithm == FPM_ALG_GD && a->batch_size > 1;
+    // Kahan summation of the frame updates into the object (or the mini-batch gradient).
+    const bool compensated = a->compensated_accumulation != 0;
     // GD regularisers run between per-batch engine launches.
     const bool tv = a->algorithm == FPM_ALG_GD && a->object_tv_weight > 0.0;
     const bool smoothing = gd_pupil && a->pupil_smoothing_weight > 0.0;
@@ -993,6 +996,11 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         if (gd_pupil) {
             FPM_TRY(p->pupil_gradient.ensure(sizeof(float2) * n2));
             if (br.launch) FPM_CUDA(cudaMemsetAsync(p->pupil_gradient.ptr, 0, sizeof(float2) * n2, s));
+        }
+        if (compensated) {
+            DeviceBuffer& e = gd_batched ? p->gradient_err : p->object_err;
+            FPM_TRY(e.ensure(sizeof(float2) * (size_t)M * ms));
+            if (br.launch) FPM_CUDA(cudaMemsetAsync(e.ptr, 0, sizeof(float2) * (size_t)M * ms, s));
         }
         if (tv) FPM_TRY(p->tv_scratch.ensure(sizeof(double2) * (size_t)M * M));
         if (smoothing) FPM_TRY(p->pupil_scratch.ensure(sizeof(float2) * n2));
@@ -1121,6 +1129,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.velocity = mpie ? p->velocity.as<float2>() : nullptr;
         T.anchor = mpie ? p->anchor.as<float2>() : nullptr;
         T.gradient = gd_batched ? p->gradient.as<float2>() : nullptr;
+        T.object_err = compensated && !gd_batched ? p->object_err.as<float2>() : nullptr;
+        T.gradient_err = compensated && gd_batched ? p->gradient_err.as<float2>() : nullptr;
         T.pupil_gradient = gd_pupil ? p->pupil_gradient.as<float2>() : nullptr;
         T.partials = p->partials.as<double>();
         T.counter = p->counter.as<int>();
@@ -1161,6 +1171,13 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                            (canonical ? 16.0 * (double)n2 : 0.0);
         }
         br.bytes += frame_bytes * iters;
+        if (compensated) {
+            // The error term's read and write beside every stencil update.
+            double err = 0.0;
+            for (int f = 0; f < p->frames; ++f)
+                if (p->params[f].weight != 0.f) err += 16.0 * p->stencil_cells[f];
+            br.bytes += err * iters;
+        }
         if (a->algorithm == FPM_ALG_GD && a->poisson_truncation) {
             // Forward-only statistics pass: stencil read and measurement per frame,
             // and |O|^2 of the grid per batch.

@@ -82,6 +82,7 @@ class AlgorithmParams(C.Structure):
         ("object_tv_weight", C.c_double), ("object_tv_epsilon", C.c_double), ("pupil_smoothing_weight", C.c_double),
         ("recover_illumination", C.c_int32), ("illumination_step", C.c_double),
         ("illumination_finite_difference", C.c_double), ("maximum_illumination_correction", C.c_double),
+        ("compensated_accumulation", C.c_int32),
     ]
 
 

@@ -174,6 +174,14 @@ class _Algorithm:
             raise ValueError("schedule must be sequential, brightfield_first, spiral_out, random, or snr_weighted")
         return _SCHEDULES[schedule]
 
+    _compensated = False
+
+    def compensated(self, enabled: bool = True):
+        """Accumulates the per-frame updates into the complex64 object (or the
+        mini-batch gradient) with compensated (Kahan) summation; returns self."""
+        self._compensated = bool(enabled)
+        return self
+
     def run(self, problem: ReconstructionProblem, *, callbacks=None, resume_from=None, schedule="sequential",
             schedule_seed=0) -> ReconstructionResult:
         """Run the reconstruction on the GPU and return host results."""
@@ -190,6 +198,7 @@ def _base_params(alg: _Algorithm, schedule: str, iterations, object_step, batch_
     p.object_step = float(object_step)
     p.epsilon = float(epsilon)
     p.constrain_pupil_support = 1
+    p.compensated_accumulation = int(alg._compensated)
     return p
 
 

@@ -155,6 +155,12 @@ typedef struct {
      * recovery, Poisson truncation or resumed runs on the device path. */
     int32_t recover_illumination;
     double illumination_step, illumination_finite_difference, maximum_illumination_correction;
+    /* Compensated (Kahan) summation of the per-frame updates into the
+     * complex64 object spectrum, or into the mini-batch gradient: each grid
+     * cell carries its rounding error, folded back at the end of every
+     * launch. Costs one more complex64 read and write per stencil cell. 0:
+     * plain FP32 accumulation. */
+    int32_t compensated_accumulation;
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */

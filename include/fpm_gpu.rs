@@ -27,7 +27,8 @@ use std::os::raw::c_char;
     pub poisson_truncation_threshold: f64, pub progress_threshold: f64, pub reduction_factor: f64,
     pub minimum_object_step: f64, pub object_tv_weight: f64, pub object_tv_epsilon: f64,
     pub pupil_smoothing_weight: f64, pub recover_illumination: i32, pub illumination_step: f64,
-    pub illumination_finite_difference: f64, pub maximum_illumination_correction: f64 }
+    pub illumination_finite_difference: f64, pub maximum_illumination_correction: f64,
+    pub compensated_accumulation: i32 }
 #[repr(C)] pub struct FpmResultDesc { pub object: *mut f64, pub object_spectrum: *mut f64,
     pub pupil: *mut f64, pub objectives: *mut f64, pub completed_iterations: i32,
     pub illumination_corrections: *mut f64 }

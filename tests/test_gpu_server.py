@@ -63,7 +63,10 @@ def test_budget_admits_one_request_at_a_time(fpm):
     problems = [_problem(fpm, 5, 64, 41 + k) for k in range(3)]
     algo = fpm.Mpie(iterations=3)
     solo = [fpm.run_batch(algo, [fpm.ReconstructionProblem(p.measurements, p.model)])[0] for p in problems]
-    with fpm.Server(hbm_budget_gb=0.004, max_batch=8, batch_window_ms=0.0) as server:  # one 64-point request is about 2.8 MB
+    with fpm.Server() as server:
+        footprint = server.submit(algo, problems[0]).info()["footprint_bytes"]
+    budget = 1.5 * footprint  # room for one of these requests at a time
+    with fpm.Server(hbm_budget_gb=budget / 1e9, max_batch=8, batch_window_ms=0.0) as server:
         requests = [server.submit(algo, p) for p in problems]
         results = [r.wait() for r in requests]
         infos = sorted((r.info() for r in requests), key=lambda i: i["admit_ms"])
@@ -72,7 +75,7 @@ def test_budget_admits_one_request_at_a_time(fpm):
         _same(got, want)
     for prev, nxt in zip(infos, infos[1:]):
         assert nxt["admit_ms"] >= prev["done_ms"]
-    assert peak <= 0.004e9
+    assert footprint <= peak <= budget
 
 
 def test_full_queue_sheds_and_oversized_requests_are_refused(fpm):
