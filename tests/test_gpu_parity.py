@@ -174,11 +174,14 @@ def test_mpie_epry_pupil_recovery_128_full_50_iterations(fpm):
         futures = {name: pool.submit(oracle.run, oproblem, name, iterations=50) for name in ("mpie", "epry")}
         problem = fpm.ReconstructionProblem(data, model)
         got = {"mpie": fpm.Mpie(iterations=50).run(problem), "epry": fpm.Epry(iterations=50).run(problem)}
+        compensated = {"mpie": fpm.Mpie(iterations=50).compensated().run(problem),
+                       "epry": fpm.Epry(iterations=50).compensated().run(problem)}
         expected = {name: f.result() for name, f in futures.items()}
-    for name in ("mpie", "epry"):
-        assert oracle.complex_nrmse(expected[name]["object"], got[name].object) <= NRMSE, name
-        _objective_close([t[1] for t in got[name].trace], expected[name]["objectives"])
-    assert oracle.complex_nrmse(expected["epry"]["pupil"], got["epry"].recovered_pupil) <= NRMSE
+    for runs in (got, compensated):
+        for name in ("mpie", "epry"):
+            assert oracle.complex_nrmse(expected[name]["object"], runs[name].object) <= NRMSE, name
+            _objective_close([t[1] for t in runs[name].trace], expected[name]["objectives"])
+        assert oracle.complex_nrmse(expected["epry"]["pupil"], runs["epry"].recovered_pupil) <= NRMSE
 
 
 def test_gradient_descent_256_full_100_iterations(fpm):
@@ -189,6 +192,10 @@ def test_gradient_descent_256_full_100_iterations(fpm):
                                  data, gains=gains)
     assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE
     _objective_close([t[1] for t in result.trace], expected["objectives"])
+    # The same run with compensated accumulation of the frame updates.
+    compensated = fpm.GradientDescent(iterations=100).compensated().run(fpm.ReconstructionProblem(data, model))
+    assert oracle.complex_nrmse(expected["object"], compensated.object) <= NRMSE
+    _objective_close([t[1] for t in compensated.trace], expected["objectives"])
 
 
 def test_gradient_descent_full_tile(fpm):
@@ -217,6 +224,10 @@ def test_gradient_descent_mini_batches(fpm, n, side, batch):
                                      omodel, data, gains=gains, weights=weights)
         assert oracle.complex_nrmse(expected["object"], result.object) <= NRMSE, loss
         _objective_close([t[1] for t in result.trace], expected["objectives"])
+        # Compensated accumulation of the batch gradient gives the same answer.
+        problem = fpm.ReconstructionProblem(data, model, frame_weights=weights)
+        compensated = fpm.GradientDescent(iterations=3, batch_size=batch, loss_type=loss).compensated().run(problem)
+        assert oracle.complex_nrmse(expected["object"], compensated.object) <= NRMSE, loss
 
 
 @pytest.mark.parametrize("n,side,batch,threshold", [(32, 5, 5, 25.0), (64, 3, 1, 2.0), (128, 3, 9, 4.0)])
