@@ -22,6 +22,16 @@ int engine_ctas(int n) {
     }
 }
 
+int engine_rows(int n) {
+    switch (n) {
+        case 32: return Cfg<32>::R;
+        case 64: return Cfg<64>::R;
+        case 128: return Cfg<128>::R;
+        case 256: return Cfg<256>::R;
+        default: return 0;
+    }
+}
+
 int init_chunks(int n) { return (n * n + kInitBlock - 1) / kInitBlock; }
 
 #define FPM_DISPATCH(call)                       \

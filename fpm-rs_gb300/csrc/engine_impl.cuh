@@ -446,13 +446,22 @@ template <int N_, int ALG, int LOSS>
 __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_kernel(const EngineParams P) {
     using K = Cfg<N_>;
     constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* field = reinterpret_cast<float2*>(smem_raw);
     float2* fld = field + K::RS;  // FFT rows 0..31; raw row 0 is the U halo
     float2* osm = field + K::FIELD;
     float2* pslab = osm + K::STAGE;
     float2* tw = pslab + K::PSLAB;
     double* dred = reinterpret_cast<double*>(tw + 256);
+    // TMA staging of the stencil: 256-point tiles of the fixed-pupil
+    // families (the pupil-recovering ones are at their register limit),
+    // whose staging slab starts 128-byte aligned.
+    constexpr bool tma_capable = N_ == 256 && ALG != kAlgSpectral && ALG != kAlgEpry && ALG != kAlgGradientPupil &&
+                                 (K::FIELD * 8) % 128 == 0;
+    constexpr unsigned kStageBytes = (unsigned)(K::STAGE * sizeof(float2));
+    __shared__ __align__(8) unsigned long long s_tma_bar;
+    __shared__ int s_tma_failed;
+    unsigned tma_phase = 0;
     double* tred = dred + K::WARPS;  // this CTA's truncation partials (residual, weight, |O|^2)
     float* fred = reinterpret_cast<float*>(dred + K::WARPS + 4);
 
@@ -471,10 +480,17 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     static_assert(sizeof(FrameParam) % 8 == 0, "FrameParam is copied in 8-byte pieces");
     int next_ready = -1;  // thread 0: order position whose descriptor s_next holds
     SpectralStep* const s_steps = reinterpret_cast<SpectralStep*>(s_desc);
-    if (tid == 0) s_tile = P.tiles[tile];
+    if (tid == 0) {
+        s_tile = P.tiles[tile];
+        if (tma_capable) {
+            s_tma_failed = 0;
+            mbar_init(&s_tma_bar, 1);
+        }
+    }
     for (int k = tid; k < 256; k += K::THREADS) tw[k] = c_tw256[k];
     __syncthreads();
     const TileDesc& T = s_tile;
+    const bool use_tma = tma_capable && T.omap != nullptr && (smem_u32(osm) & 127u) == 0;
     const float eps = (float)P.eps;  // epsilon in the per-pixel FP32 arithmetic
     const int M = T.M;
     const long long ostride = M + (M & 1);
@@ -680,7 +696,25 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             if (gd_pupil && !stats) ++pupil_active;
 
             // S0
-            if (!spectral_update) stage_object<K>(osm, obj, M, ostride, fp, i_lo, row_lo, row_hi);
+            if (use_tma && !s_tma_failed) {
+                // One bulk tensor load of the (R + 1) x (N + 2) stencil from an
+                // even column (pair c0 / 2); rows and pairs past the grid read
+                // as zeros. CTAs the pupil leaves empty stage nothing.
+                const int r_begin = max(row_lo - i_lo, 0), r_end = min(row_hi + 1 - i_lo, R);
+                if (r_begin <= r_end) {
+                    if (tid == 0) {
+                        mbar_arrive_expect_tx(&s_tma_bar, kStageBytes);
+                        tma_load_3d(osm, T.omap, 0, (fp.lower_col & ~1) >> 1, fp.lower_row + i_lo, &s_tma_bar);
+                    }
+                    if (!mbar_wait(&s_tma_bar, tma_phase)) {
+                        s_tma_failed = 1;
+                        atomicOr(T.status, 512);
+                    }
+                    tma_phase ^= 1u;
+                }
+            } else if (!spectral_update) {
+                stage_object<K>(osm, obj, M, ostride, fp, i_lo, row_lo, row_hi);
+            }
             if (!spectral) __syncthreads();
             if (spectral && !spectral_update) __syncthreads();
             const float2* ostage = osm + (fp.lower_col & 1);
@@ -1234,6 +1268,12 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
         }
     }
     if (P.momentum && c == 0 && tid == 0) *T.counter = counter;
+    if (use_tma && s_tma_failed) {
+        // A stencil load that timed out may still land: let it, before exit.
+        const unsigned long long t0 = global_ns();
+        while (global_ns() - t0 < 1000000ull) {
+        }
+    }
     if (!spectral && T.object_err) {
         // Compensated accumulation: the carried error goes back into the
         // object at the end of the launch (every frame's P8 is done), so

@@ -147,3 +147,62 @@ FPM_DEVICE float2 dsmem_load(unsigned address) {
 FPM_DEVICE void dsmem_store(unsigned address, float2 v) {
     asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(address), "f"(v.x), "f"(v.y) : "memory");
 }
+
+// ------------------------------------------------------------ TMA staging
+// A bulk tensor load completes its bytes on an mbarrier of this CTA; the
+// threads wait on the phase parity, bounded in time so that a load that
+// never lands cannot hang the kernel.
+FPM_DEVICE unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+constexpr unsigned long long kMbarWaitNs = 2000000000ull;  // 2 s
+
+FPM_DEVICE unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+FPM_DEVICE void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+FPM_DEVICE void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// True once the phase with parity `parity` has completed; false when about
+// kMbarWaitNs have passed first.
+FPM_DEVICE bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    unsigned long long t0 = 0;
+    for (unsigned k = 0;; ++k) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((k & 255u) == 0) {
+            const unsigned long long t = global_ns();
+            if (k == 0) t0 = t;
+            else if (t - t0 > kMbarWaitNs) return false;
+        }
+    }
+}
+
+// 3-D tiled bulk tensor load (box of the tensor map at coordinates x, y, z,
+// innermost first) into this CTA's shared memory, completing on `bar`.
+// Global data written earlier by other threads through ordinary stores is
+// ordered before the load by the fence.
+FPM_DEVICE void tma_load_3d(void* smem, const void* tmap, int x, int y, int z, unsigned long long* bar) {
+    asm volatile("fence.proxy.async.global;\n" ::: "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}

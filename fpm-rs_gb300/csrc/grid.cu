@@ -232,11 +232,17 @@ cudaError_t launch_widen(const float2* src, long long src_stride, int rows, int 
 // (checkpoint restore: the values were widened from complex64, so this is exact).
 __global__ void narrow_kernel(const double2* __restrict__ src, int rows, int cols, float2* __restrict__ dst,
                               long long dst_stride) {
-    const long long total = (long long)rows * cols;
+    // Every destination element, pad columns (c >= cols) set to zero: the
+    // stencil staging reads whole column pairs.
+    const long long total = (long long)rows * dst_stride;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const long long r = e / cols, c = e % cols;
-        const double2 v = src[e];
-        dst[r * dst_stride + c] = make_float2((float)v.x, (float)v.y);
+        const long long r = e / dst_stride, c = e % dst_stride;
+        float2 out = make_float2(0.f, 0.f);
+        if (c < cols) {
+            const double2 v = src[r * cols + c];
+            out = make_float2((float)v.x, (float)v.y);
+        }
+        dst[e] = out;
     }
 }
 

@@ -63,6 +63,9 @@ struct TileDesc {
     const float* background;   // engine-permuted, or null
     long long background_stride;  // floats between frames (0: one shared image)
     const FrameParam* params;  // [frame_count]
+    // Tensor map of `object` for TMA staging of the stencil (256-point tiles;
+    // viewed as [M rows][MS / 2 column pairs][4 floats]), or null.
+    const void* omap;
     const int* order;          // [frame_count] schedule, or null for sequential
     float2* velocity;          // mPIE, M*M
     float2* anchor;            // mPIE, M*M
@@ -145,6 +148,8 @@ struct ForwardParams {
 bool engine_supported(int n);
 // CTAs in the thread-block cluster that reconstructs one n x n tile.
 int engine_ctas(int n);
+// Field rows per CTA of an n x n tile (the stencil box is engine_rows(n) + 1 rows).
+int engine_rows(int n);
 cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t s);
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
 

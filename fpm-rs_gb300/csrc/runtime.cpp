@@ -4,6 +4,7 @@
 // canonicalise (EPRY), iterate the schedule, canonicalise per iteration,
 // record the weighted mean objective, and build the result. Every numerical
 // step runs on the GPU; there is no host fallback.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -903,6 +904,42 @@ std::vector<int> schedule_order(const fpm_problem* p, int schedule) {
     return order;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// to the driver library); null when unavailable.
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+    static const EncodeTiled fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (EncodeTiled) nullptr;
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+// The stencil staging map of an M x MS complex64 object spectrum: viewed as
+// [M rows][MS / 2 column pairs][4 floats], so every box starts at an aligned
+// innermost coordinate (0) and a pair index (even column / 2); the box is
+// (rows) x (n / 2 + 1 pairs) x 4, the (rows) x (n + 2) stencil slab.
+bool encode_stencil_map(CUtensorMap* map, float2* object, int m, int n, int rows) {
+    const EncodeTiled fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t ms = (cuuint64_t)(m + (m & 1));
+    const cuuint64_t dims[3] = {4, ms / 2, (cuuint64_t)m};
+    const cuuint64_t strides[2] = {16, ms * sizeof(float2)};
+    const cuuint32_t box[3] = {4, (cuuint32_t)(n / 2 + 1), (cuuint32_t)rows};
+    const cuuint32_t unit[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, object, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct Bucket {
     int n, m;
     std::vector<fpm_problem*> problems;
@@ -926,6 +963,7 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
 }
 
 struct BucketRun {
+    DeviceBuffer tmaps;  // per tile: the object spectrum's tensor map for TMA stencil staging
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
         tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks, ill_fields, ill_valid, ill_ptrs;
     std::vector<cudaEvent_t> events;  // (start, end) pairs around engine launches
@@ -973,6 +1011,13 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     const bool resumed = !b.resume.empty();
     const int it0 = resumed ? b.resume[0]->completed_iterations : 0;
     std::vector<fpm::TileDesc> tiles(count);
+    // 256-point tiles stage their stencils with TMA, through one tensor map per tile.
+    const bool tma = N == 256;
+    std::vector<CUtensorMap> maps(tma ? count : 0);
+    if (tma) {
+        br.tmaps.bind(ctx->pool, s);
+        FPM_TRY(br.tmaps.ensure(sizeof(CUtensorMap) * (size_t)count));
+    }
     std::vector<fpm::InitTile> inits(count);
     std::vector<fpm::GaugeTile> gauges(count);
     std::vector<fpm::IlluminationTile> ill_tiles(illum ? count : 0);
@@ -1067,6 +1112,9 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.background = p->has_background ? p->background.as<float>() : nullptr;
         T.background_stride = p->background_stride;
         T.params = p->frame_params.as<fpm::FrameParam>();
+        T.omap = nullptr;
+        if (tma && encode_stencil_map(&maps[t], p->object.as<float2>(), M, N, fpm::engine_rows(N) + 1))
+            T.omap = br.tmaps.as<CUtensorMap>() + t;
         T.order = order_dev;
         if (illum) {
             // The run's own frame constants follow the recovered offsets; the
@@ -1206,6 +1254,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     if (!br.first) FPM_CUDA(cudaEventCreate(&br.first));
     if (!br.last) FPM_CUDA(cudaEventCreate(&br.last));
     if (br.prepare) {
+        if (tma) FPM_TRY(upload_array(br.tmaps, maps, s));
         FPM_TRY(upload_array(br.tiles, tiles, s));
         FPM_TRY(upload_array(br.init, inits, s));
         FPM_TRY(upload_array(br.gauge, gauges, s));
@@ -1516,6 +1565,8 @@ Status finish_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_
     if (status & 64) return Status::make(FPM_ERR_NUMERICAL, "pupil update produced a non-finite value");
     if (status & 128) return Status::make(FPM_ERR_NUMERICAL, "regularization produced a non-finite value");
     if (status & 256) return Status::make(FPM_ERR_NUMERICAL, "illumination gradient or curvature is invalid");
+    if (status & 512)
+        return Status::make(FPM_ERR_TIMEOUT, "a frame-engine stencil load (TMA) did not complete within its bounded wait");
     if (!r) return Status::ok();
     if (r->objectives) fill_objectives(p, a, r->objectives);
     r->completed_iterations = a->iterations;

@@ -57,7 +57,7 @@ enum {
     FPM_ERR_NUMERICAL = 7,            /* Error::Numerical */
     FPM_ERR_UNSUPPORTED = 8,          /* Error::Unsupported */
     FPM_ERR_CUDA = 9,                 /* a CUDA runtime call failed */
-    FPM_ERR_TIMEOUT = 10,             /* reserved: a bounded device wait expired */
+    FPM_ERR_TIMEOUT = 10,             /* a bounded device wait expired (frame-engine stencil load) */
     FPM_ERR_QUEUE_FULL = 11           /* serving: the server's queue is full, the request was not taken */
 };
 
