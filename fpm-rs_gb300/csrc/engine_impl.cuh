@@ -1305,7 +1305,7 @@ template <int N_>
 __global__ void __launch_bounds__(Cfg<N_>::THREADS) forward_kernel(const ForwardParams P) {
     using K = Cfg<N_>;
     constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* field = reinterpret_cast<float2*>(smem_raw);
     float2* fld = field + K::RS;
     float2* osm = field + K::FIELD;
@@ -1356,38 +1356,67 @@ FPM_DEVICE int perm_index(int y, int x) {
     return (c * K::R + m) * K::N + K::NB * ka + kb;
 }
 
+// Natural column x of engine-layout position t within a row: positions
+// NB * ka + kb hold columns ka + NA * kb.
+template <class K>
+FPM_DEVICE int layout_column(int t) {
+    return t / K::NB + K::NA * (t % K::NB);
+}
+
+// Natural -> engine layout, one row per block (blockDim.x == N): the row is
+// read and written contiguously; the column shuffle goes through shared
+// memory. Row `row` of frame f is natural row y; its engine row starts at
+// (c * R + m) * N with y = c + C * m.
+template <class K>
+FPM_DEVICE long long layout_row_base(long long f, int y) {
+    return f * K::N * K::N + (long long)((y % K::C) * K::R + y / K::C) * K::N;
+}
+
 template <int N_>
-__global__ void permute_f64_kernel(const double* __restrict__ src, float* __restrict__ dst, long long frames) {
+__global__ void __launch_bounds__(N_) permute_f64_kernel(const double* __restrict__ src, float* __restrict__ dst,
+                                                         long long frames) {
     using K = Cfg<N_>;
-    const long long total = frames * K::N * K::N;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const long long f = e / (K::N * K::N);
-        const int p = (int)(e % (K::N * K::N));
-        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = (float)src[e];
+    __shared__ float row[N_];
+    for (long long r = blockIdx.x; r < frames * K::N; r += gridDim.x) {
+        const long long f = r / K::N;
+        const int y = (int)(r % K::N), t = threadIdx.x;
+        row[t] = (float)src[r * K::N + t];
+        __syncthreads();
+        dst[layout_row_base<K>(f, y) + t] = row[layout_column<K>(t)];
+        __syncthreads();
     }
 }
 
 template <int N_>
-__global__ void permute_amplitude_kernel(const double* __restrict__ src, const uint8_t* __restrict__ masks,
-                                         const double* __restrict__ gains, float* __restrict__ dst, long long frames) {
+__global__ void __launch_bounds__(N_) permute_amplitude_kernel(const double* __restrict__ src,
+                                                               const uint8_t* __restrict__ masks,
+                                                               const double* __restrict__ gains,
+                                                               float* __restrict__ dst, long long frames) {
     using K = Cfg<N_>;
-    const long long total = frames * K::N * K::N;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const long long f = e / (K::N * K::N);
-        const int p = (int)(e % (K::N * K::N));
-        const float a = (masks && masks[e] == 0) ? -1.0f : (float)sqrt(fmax(src[e] / gains[f], 0.0));
-        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = a;
+    __shared__ float row[N_];
+    for (long long r = blockIdx.x; r < frames * K::N; r += gridDim.x) {
+        const long long f = r / K::N;
+        const int y = (int)(r % K::N), t = threadIdx.x;
+        const long long e = r * K::N + t;
+        row[t] = (masks && masks[e] == 0) ? -1.0f : (float)sqrt(fmax(src[e] / gains[f], 0.0));
+        __syncthreads();
+        dst[layout_row_base<K>(f, y) + t] = row[layout_column<K>(t)];
+        __syncthreads();
     }
 }
 
 template <int N_>
-__global__ void permute_u8_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, long long frames) {
+__global__ void __launch_bounds__(N_) permute_u8_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                                                        long long frames) {
     using K = Cfg<N_>;
-    const long long total = frames * K::N * K::N;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const long long f = e / (K::N * K::N);
-        const int p = (int)(e % (K::N * K::N));
-        dst[f * K::N * K::N + perm_index<K>(p / K::N, p % K::N)] = src[e];
+    __shared__ uint8_t row[N_];
+    for (long long r = blockIdx.x; r < frames * K::N; r += gridDim.x) {
+        const long long f = r / K::N;
+        const int y = (int)(r % K::N), t = threadIdx.x;
+        row[t] = src[r * K::N + t];
+        __syncthreads();
+        dst[layout_row_base<K>(f, y) + t] = row[layout_column<K>(t)];
+        __syncthreads();
     }
 }
 
@@ -1403,11 +1432,14 @@ __global__ void init_mean_kernel(const InitTile* __restrict__ tiles, double* __r
     constexpr int N = K::N;
     const InitTile T = tiles[blockIdx.y];
     const int chunks = gridDim.x;
-    const int p = blockIdx.x * kInitBlock + threadIdx.x;  // natural pixel
+    // Threads walk the engine layout (coalesced reads of every frame); each
+    // writes its natural pixel's mean.
+    const int idx = blockIdx.x * kInitBlock + threadIdx.x;
     __shared__ double s_amp[kInitBlock / 32], s_w[kInitBlock / 32];
     double sum = 0.0, wsum = 0.0;
-    if (p < N * N) {
-        const int idx = perm_index<K>(p / N, p % N);
+    if (idx < N * N) {
+        const int erow = idx / N, c = erow / K::R, m = erow % K::R;
+        const int p = (c + K::C * m) * N + layout_column<K>(idx % N);  // natural pixel
         for (int f = 0; f < T.frames_count; ++f) {
             const FrameParam fp = T.params[f];
             if (fp.weight == 0.0f) continue;
@@ -1548,25 +1580,28 @@ struct EngineEntry {
         return launch_cluster<N_>(forward_kernel<N_>, p, p.frame_count, s);
     }
 
+    // One block of N threads per frame row (grid-strided over the rows).
+    static int permute_blocks(long long frames) {
+        const long long rows = frames * N_;
+        return (int)(rows < 65536 ? rows : 65536);
+    }
+
     static cudaError_t permute_f64(const double* src, float* dst, long long frames, cudaStream_t s) {
-        const long long total = frames * N_ * N_;
-        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
-        permute_f64_kernel<N_><<<blocks, 256, 0, s>>>(src, dst, frames);
+        if (frames <= 0) return cudaSuccess;
+        permute_f64_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, dst, frames);
         return cudaGetLastError();
     }
 
     static cudaError_t permute_u8(const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s) {
-        const long long total = frames * N_ * N_;
-        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
-        permute_u8_kernel<N_><<<blocks, 256, 0, s>>>(src, dst, frames);
+        if (frames <= 0) return cudaSuccess;
+        permute_u8_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, dst, frames);
         return cudaGetLastError();
     }
 
     static cudaError_t permute_amplitude(const double* src, const uint8_t* masks, const double* gains, float* dst,
                                          long long frames, cudaStream_t s) {
-        const long long total = frames * N_ * N_;
-        const int blocks = (int)((total + 255) / 256 < 65536 ? (total + 255) / 256 : 65536);
-        permute_amplitude_kernel<N_><<<blocks, 256, 0, s>>>(src, masks, gains, dst, frames);
+        if (frames <= 0) return cudaSuccess;
+        permute_amplitude_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, masks, gains, dst, frames);
         return cudaGetLastError();
     }
 
