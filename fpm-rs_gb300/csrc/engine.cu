@@ -47,6 +47,8 @@ cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t 
 
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s) { FPM_DISPATCH(forward(p, s)) }
 
+cudaError_t engine_max_active_clusters(int n, int* count) { FPM_DISPATCH(max_active_clusters(count)) }
+
 cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s) {
     FPM_DISPATCH(permute_f64(src, dst, frames, s))
 }

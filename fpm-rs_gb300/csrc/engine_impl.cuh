@@ -442,8 +442,9 @@ FPM_DEVICE void prefetch_step(SpectralStep* slot, const SpectralStep* steps, int
                    reinterpret_cast<const char*>(steps + step) + 16 * threadIdx.x, 16);
 }
 
+// One tile's whole launch (iterations [it_begin, it_end)) by one cluster.
 template <int N_, int ALG, int LOSS>
-__global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_kernel(const EngineParams P) {
+FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
     using K = Cfg<N_>;
     constexpr int N = K::N, R = K::R, C = K::C, NA = K::NA, NB = K::NB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -466,7 +467,6 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
     float* fred = reinterpret_cast<float*>(dred + K::WARPS + 4);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tile = blockIdx.x / C;
     const int c = C == 1 ? 0 : (int)(blockIdx.x % C);
     // Tile and frame descriptors live in shared memory, not registers.
     __shared__ TileDesc s_tile;
@@ -1296,8 +1296,20 @@ __global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_
             __stcg(E4 + e, make_float4(0.f, 0.f, 0.f, 0.f));
         }
     }
-    // Peers must not exit while their shared memory may still be addressed.
+    // Peers must not exit, nor take their next tile, while their shared
+    // memory may still be addressed.
     cluster_barrier<K>();
+    if (tma_capable && tid == 0) mbar_inval(&s_tma_bar);  // initialised again by the next tile
+}
+
+// Persistent frame engine: the launch has G clusters (G <= the tile count,
+// chosen per tile size); cluster k reconstructs tiles k, k + G, k + 2G, ...
+// of the launch, each as engine_tile.
+template <int N_, int ALG, int LOSS>
+__global__ void __launch_bounds__(Cfg<N_>::THREADS, Cfg<N_>::MIN_BLOCKS) engine_kernel(const EngineParams P) {
+    const int clusters = (int)(gridDim.x / Cfg<N_>::C);
+    for (int tile = (int)(blockIdx.x / Cfg<N_>::C); tile < P.tile_count; tile += clusters)
+        engine_tile<N_, ALG, LOSS>(P, tile);
 }
 
 // Forward model (simulate): cluster f computes frame f's intensity.
@@ -1574,6 +1586,31 @@ struct EngineEntry {
             case kAlgSpectral: return engine_alg<kAlgSpectral>(p, tiles, s);
             default: return cudaErrorInvalidValue;
         }
+    }
+
+    // Clusters of the frame engine that can be resident at once on the
+    // current device (every family shares the shape and the register cap).
+    static cudaError_t max_active_clusters(int* count) {
+        using K = Cfg<N_>;
+        auto kernel = engine_kernel<N_, kAlgRpie, 0>;
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        if constexpr (K::C > 8) {
+            e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e != cudaSuccess) return e;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(K::C);
+        cfg.blockDim = dim3(K::THREADS);
+        cfg.dynamicSmemBytes = K::SMEM_BYTES;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = K::C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaOccupancyMaxActiveClusters(count, kernel, &cfg);
     }
 
     static cudaError_t forward(const ForwardParams& p, cudaStream_t s) {

@@ -167,6 +167,10 @@ FPM_DEVICE void mbar_init(unsigned long long* bar, unsigned count) {
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
+FPM_DEVICE void mbar_inval(unsigned long long* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
 FPM_DEVICE void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");

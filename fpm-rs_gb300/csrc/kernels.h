@@ -116,6 +116,7 @@ enum EngineAlg {
 
 struct EngineParams {
     const TileDesc* tiles;
+    int tile_count;            // tiles of the launch (its clusters walk them, see engine_kernel)
     int alg;
     // Step sizes, the rPIE blend and epsilon in FP64: per-frame scales and
     // denominator constants are formed in FP64 and rounded once to float.
@@ -150,7 +151,9 @@ bool engine_supported(int n);
 int engine_ctas(int n);
 // Field rows per CTA of an n x n tile (the stencil box is engine_rows(n) + 1 rows).
 int engine_rows(int n);
-cudaError_t launch_engine(int n, const EngineParams& p, int tiles, cudaStream_t s);
+// `clusters` clusters walk p.tile_count tiles (clusters <= p.tile_count).
+cudaError_t launch_engine(int n, const EngineParams& p, int clusters, cudaStream_t s);
+cudaError_t engine_max_active_clusters(int n, int* count);
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
 
 // Permutes natural-order frames [frames][N][N] into the engine layout.

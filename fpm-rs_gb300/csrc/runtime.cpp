@@ -190,6 +190,9 @@ struct fpm_context {
     cudaMemPool_t pool = nullptr;  // problem buffers: stream-ordered, memory kept for reuse
     cudaStream_t upload = nullptr, download = nullptr;  // host-input batches: copies beside compute
     fpm_run_stats stats = {};
+    // Clusters of a frame-engine launch per tile size (index log2(n) - 5; 0:
+    // one cluster per tile); with fewer, each cluster walks several tiles.
+    int engine_grid[4] = {0, 0, 0, 0};
 };
 
 struct fpm_problem {
@@ -987,6 +990,15 @@ struct BucketRun {
     }
 };
 
+int engine_grid_slot(int n) { return n == 32 ? 0 : n == 64 ? 1 : n == 128 ? 2 : n == 256 ? 3 : -1; }
+
+// Clusters of an engine launch over `tiles` tiles of size n.
+int engine_clusters(const fpm_context* ctx, int n, int tiles) {
+    const int k = engine_grid_slot(n);
+    const int g = k >= 0 ? ctx->engine_grid[k] : 0;
+    return g > 0 && g < tiles ? g : tiles;
+}
+
 Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cudaStream_t s, BucketRun& br) {
     const int N = b.n, M = b.m, count = (int)b.problems.size();
     const int C = fpm::engine_ctas(N);
@@ -1292,6 +1304,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
 
     fpm::EngineParams ep{};
     ep.tiles = br.tiles.as<fpm::TileDesc>();
+    ep.tile_count = count;
     switch (a->algorithm) {
         case FPM_ALG_AP: ep.alg = fpm::kAlgLocal; break;
         case FPM_ALG_ADAPTIVE_AP: ep.alg = fpm::kAlgLocalAdaptive; break;
@@ -1330,7 +1343,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         ep.it_begin = it0;
         ep.it_end = it1;
         FPM_CUDA(br.record(e0, s));
-        FPM_CUDA(fpm::launch_engine(N, ep, count, s));
+        FPM_CUDA(fpm::launch_engine(N, ep, engine_clusters(ctx, N, count), s));
         FPM_CUDA(br.record(e1, s));
         br.launches += 1;
         return Status::ok();
@@ -2318,13 +2331,14 @@ Status spectral_queue(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fp
         FPM_TRY(upload_array(*b.tile_bufs.back(), tiles, s));
         fpm::EngineParams ep = spectral_engine_params(a, completed);
         ep.tiles = b.tile_bufs.back()->as<fpm::TileDesc>();
+        ep.tile_count = (int)tiles.size();
         cudaEvent_t e0, e1, done;
         FPM_TRY(b.event(e0));
         FPM_TRY(b.event(e1));
         FPM_TRY(b.event(done));
         FPM_CUDA(cudaEventRecord(e0, s));
         if (a->iterations > completed) {
-            FPM_CUDA(fpm::launch_engine(N, ep, (int)tiles.size(), s));
+            FPM_CUDA(fpm::launch_engine(N, ep, engine_clusters(ctx, N, (int)tiles.size()), s));
             ++b.launches;
             b.st.engine_launches += 1;
         }
@@ -3378,4 +3392,28 @@ int32_t fpm_plan_destroy(fpm_plan* plan) {
     cudaSetDevice(ctx->device);
     delete plan;
     return FPM_OK;
+}
+
+int32_t fpm_set_engine_grid(fpm_context* ctx, int32_t n, int32_t clusters) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const int k = engine_grid_slot(n);
+    if (k < 0) return finish(ctx, Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n));
+    if (clusters < 0) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "clusters must be non-negative"));
+    ctx->engine_grid[k] = clusters;
+    return FPM_OK;
+}
+
+int32_t fpm_engine_max_clusters(fpm_context* ctx, int32_t n, int32_t* clusters) {
+    if (!ctx || !clusters) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto body = [&]() -> Status {
+        FPM_CUDA(cudaSetDevice(ctx->device));
+        int count = 0;
+        if (engine_grid_slot(n) < 0) return Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n);
+        FPM_CUDA(fpm::engine_max_active_clusters(n, &count));
+        *clusters = count;
+        return Status::ok();
+    };
+    return finish(ctx, body());
 }

@@ -12,7 +12,7 @@ import ctypes as _C
 
 import numpy as _np
 
-from . import _native
+from . import _native, tuning
 from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasurementsError, InvalidModelError,
                      InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
                      ServerBusyError, UnsupportedError)

@@ -30,7 +30,7 @@ EXPORTED = (
     "fpm_run_batch_submit", "fpm_spectral_run_batch_submit", "fpm_job_poll", "fpm_job_wait", "fpm_job_stats", "fpm_job_destroy",
     "fpm_plan_create", "fpm_plan_launch", "fpm_plan_wait", "fpm_plan_collect", "fpm_plan_destroy",
     "fpm_server_create", "fpm_server_submit", "fpm_server_poll", "fpm_server_wait", "fpm_server_stats_get",
-    "fpm_server_destroy",
+    "fpm_server_destroy", "fpm_set_engine_grid", "fpm_engine_max_clusters",
 )
 
 
@@ -263,8 +263,25 @@ def context() -> Context:
     if _context is None:
         with _lock:
             if _context is None:
-                _context = Context(int(os.environ.get("FPM_DEVICE", "0")))
+                ctx = Context(int(os.environ.get("FPM_DEVICE", "0")))
+                _apply_tuning(ctx)
+                _context = ctx
     return _context
+
+
+def _apply_tuning(ctx: "Context") -> None:
+    """The committed frame-engine launch grids (tuning.json), if any."""
+    import json
+
+    try:
+        with open(os.path.join(PACKAGE_ROOT, "tuning.json")) as handle:
+            grid = json.load(handle).get("grid", {})
+    except (OSError, ValueError):
+        return
+    for n in (32, 64, 128, 256):
+        clusters = int(grid.get(str(n), 0))
+        if clusters:
+            check(ctx._lib.fpm_set_engine_grid(ctx.handle, n, clusters), ctx.handle)
 
 
 def c128(a) -> np.ndarray:

@@ -1,0 +1,93 @@
+"""Autotuner of the frame-engine launch grids.
+
+Each tile size's engine launch runs G thread-block clusters that walk the
+launch's tiles (fpm_set_engine_grid); G = 0 gives every tile its own
+cluster, and the hardware scheduler then shares the device between the tile
+sizes of a batch as clusters finish. Smaller persistent grids instead fix
+how many clusters of each size are resident at once. `autotune` times a
+workload under a set of candidate grids, keeps the fastest, and `save`
+writes the table that every new context applies (tuning.json next to the
+package).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import time
+
+from . import _native as N
+
+TABLE_PATH = os.path.join(N.PACKAGE_ROOT, "tuning.json")
+SIZES = (32, 64, 128, 256)
+
+
+def max_clusters(n: int) -> int:
+    """Clusters of an n x n tile's frame engine that fit on the device at once."""
+    ctx = N.context()
+    out = C.c_int32()
+    N.check(N.library().fpm_engine_max_clusters(ctx.handle, int(n), C.byref(out)), ctx.handle)
+    return out.value
+
+
+def set_engine_grid(n: int, clusters: int) -> None:
+    ctx = N.context()
+    N.check(N.library().fpm_set_engine_grid(ctx.handle, int(n), int(clusters)), ctx.handle)
+
+
+def apply(grid: dict) -> None:
+    """Applies {tile size: clusters} (0: one cluster per tile) to the context."""
+    for n in SIZES:
+        set_engine_grid(n, int(grid.get(str(n), grid.get(n, 0))))
+
+
+def load(path: str = TABLE_PATH) -> dict | None:
+    try:
+        with open(path) as handle:
+            return json.load(handle)
+    except (OSError, ValueError):
+        return None
+
+
+def candidates(sizes) -> list:
+    """Grids to try: one cluster per tile; every size at its residency
+    limit; and the largest size at its limit with the others at a quarter
+    or a half of theirs (so that they run beside it rather than after it)."""
+    limit = {n: max_clusters(n) for n in sizes}
+    largest = max(sizes)
+    out = [{str(n): 0 for n in sizes}, {str(n): limit[n] for n in sizes}]
+    for share in (0.25, 0.5):
+        grid = {str(n): max(1, int(limit[n] * share)) for n in sizes}
+        grid[str(largest)] = limit[largest]
+        out.append(grid)
+    return out
+
+
+def autotune(algorithm, problems, *, grids=None, repeats: int = 2) -> dict:
+    """Times run_batch(algorithm, problems) (results left on the device)
+    under each candidate grid and returns the table of the fastest, with
+    every measurement."""
+    from .reconstruction import last_run_stats, run_batch
+
+    sizes = sorted({p.image_shape[0] for p in problems})
+    grids = grids or candidates(sizes)
+    measured = []
+    for grid in grids:
+        apply(grid)
+        run_batch(algorithm, problems, download=False)  # warm-up under this grid
+        times = []
+        for _ in range(repeats):
+            run_batch(algorithm, problems, download=False)
+            times.append(last_run_stats()["run_ms"])
+        measured.append({"grid": grid, "run_ms": min(times)})
+    best = min(measured, key=lambda m: m["run_ms"])
+    apply(best["grid"])
+    return {"grid": best["grid"], "measured": measured, "tiles": len(problems),
+            "algorithm": type(algorithm).__name__, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+
+
+def save(table: dict, path: str = TABLE_PATH) -> None:
+    with open(path, "w") as handle:
+        json.dump(table, handle, indent=1)
+        handle.write("\n")

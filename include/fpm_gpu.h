@@ -456,6 +456,15 @@ int32_t fpm_plan_collect(fpm_plan *plan, fpm_result_desc *results);
 /* Waits for queued replays and frees the plan; its problems are free again. */
 int32_t fpm_plan_destroy(fpm_plan *plan);
 
+/* -------------------------------------------------- frame-engine launches */
+/* A frame-engine launch of one tile size runs `clusters` thread-block
+ * clusters that walk the launch's tiles (cluster k takes tiles k, k + G, ...);
+ * 0 (the default) gives every tile its own cluster. Autotuners set it per
+ * tile size n in {32, 64, 128, 256}. */
+int32_t fpm_set_engine_grid(fpm_context *ctx, int32_t n, int32_t clusters);
+/* Clusters of an n x n tile's frame engine that fit on the device at once. */
+int32_t fpm_engine_max_clusters(fpm_context *ctx, int32_t n, int32_t *clusters);
+
 /* ------------------------------------------------------- serving loop */
 /* A request loop over one context: the work run_algorithm
  * (python/src/reconstruction.rs:1107-1141) does for one caller, served to

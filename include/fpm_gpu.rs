@@ -96,6 +96,8 @@ extern "C" {
     pub fn fpm_plan_wait(plan: *mut FpmPlan) -> i32;
     pub fn fpm_plan_collect(plan: *mut FpmPlan, r: *mut FpmResultDesc) -> i32;
     pub fn fpm_plan_destroy(plan: *mut FpmPlan) -> i32;
+    pub fn fpm_set_engine_grid(ctx: *mut FpmContext, n: i32, clusters: i32) -> i32;
+    pub fn fpm_engine_max_clusters(ctx: *mut FpmContext, n: i32, clusters: *mut i32) -> i32;
     pub fn fpm_server_create(ctx: *mut FpmContext, config: *const FpmServerConfig, server: *mut *mut FpmServer) -> i32;
     pub fn fpm_server_submit(server: *mut FpmServer, model: *const FpmModelDesc, m: *const FpmMeasurementDesc,
         a: *const FpmAlgorithmParams, r: *mut FpmResultDesc, request: *mut u64) -> i32;
