@@ -434,6 +434,9 @@ def run_ours(args):
                   f"{sum(225 * n * n * 4 for n in sizes) / 1e9:.1f} GB per GPU vs 129 MB L2",
             "timing": "device span of each batch from CUDA events on the library's streams",
             "setup_s": round(setup_s, 1),
+            "engine_shapes": {"32": "1 CTA x 32 rows", "64": "2-CTA cluster x 32 rows",
+                              "128": "8-CTA cluster x 16 rows", "256": "16-CTA cluster x 16 rows, TMA stencil staging"},
+            "engine_grid": (fpm.tuning.load() or {}).get("grid", "one cluster per tile (no tuning table)"),
         },
         "roofline": {
             "bound": "hbm",
