@@ -19,6 +19,8 @@ from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasure
 from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
+from .callbacks import (Callback, CsvLogger, IterationCallback, ProgressLogger, SaveImageEvery, SavePupilEvery,
+                        SaveResidualsEvery, StepContext, StopOnPlateau)
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
 from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjection, Epry, Fpie, GradientDescent, Mpie,
                              ReconstructionProblem,
@@ -58,5 +60,6 @@ __all__ = [
     "SimulationResult",
     "UnsupportedError", "compile_camera_model", "compile_model", "fft2", "forward_intensities", "last_run_stats",
     "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob", "RunPlan",
-    "capture_batch", "Server", "Request", "ServerBusyError",
+    "capture_batch", "Server", "Request", "ServerBusyError", "Callback", "CsvLogger", "IterationCallback",
+    "ProgressLogger", "SaveImageEvery", "SavePupilEvery", "SaveResidualsEvery", "StepContext", "StopOnPlateau",
 ]

@@ -22,6 +22,7 @@ from pathlib import Path
 
 import numpy as np
 
+from .callbacks import Callback, _interval, _next_multiple
 from .errors import InvalidParameterError
 
 FORMAT_VERSION = 2
@@ -114,15 +115,25 @@ class ReconstructionCheckpoint:
         return cp
 
 
-class CheckpointEvery:
+class CheckpointEvery(Callback):
     """Saves a checkpoint every `every` completed iterations into `directory`
-    as checkpoint_<iteration, 5 digits>.json (src/callbacks/checkpoint.rs:8-39)."""
+    as checkpoint_<iteration, 5 digits>.json; a zero interval becomes one
+    (src/callbacks/checkpoint.rs:8-39)."""
 
     def __init__(self, every: int, directory):
-        if int(every) <= 0:
-            raise InvalidParameterError("checkpoint interval must be greater than zero")
-        self.every = int(every)
+        self.every = _interval(every)
         self.directory = Path(directory)
 
     def path_for(self, iteration: int) -> Path:
         return self.directory / f"checkpoint_{iteration:05d}.json"
+
+    def _next_state(self, current: int) -> int:
+        return _next_multiple(current, self.every)
+
+    def on_start(self, context) -> None:
+        self.directory.mkdir(parents=True, exist_ok=True)
+
+    def on_iteration_end(self, context) -> bool:
+        if context.iteration % self.every == 0:
+            context.checkpoint().save(self.path_for(context.iteration))
+        return False

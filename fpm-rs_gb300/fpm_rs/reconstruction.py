@@ -18,7 +18,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native as N
-from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
+from .callbacks import Callback, StepContext, plan_segment
+from .checkpoint import ReconstructionCheckpoint
 from .errors import (InvalidMeasurementsError, InvalidModelError, InvalidParameterError, InvalidShapeError,
                      UnsupportedError)
 from .model import ImagePlaneModel
@@ -409,8 +410,8 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
     """
     callbacks = list(callbacks or [])
     for cb in callbacks:
-        if not isinstance(cb, CheckpointEvery):
-            raise UnsupportedError("the GB300 device path supports the CheckpointEvery callback only")
+        if not isinstance(cb, Callback):
+            raise TypeError("unsupported callback object")
     problems = list(problems)
     if callbacks or resume_from is not None:
         return _run_resumable(algorithm, problems, callbacks, resume_from, schedule, download)
@@ -809,11 +810,64 @@ def _checkpoint_arrays(cp: ReconstructionCheckpoint, problem, algorithm):
     return arrays
 
 
+class _SegmentState:
+    """The state a device segment ended at: captured arrays, the device's
+    results, and derived views for callbacks (computed on first use)."""
+
+    def __init__(self, problem, algorithm, captured, counter, end, results):
+        self.problem = problem
+        self.algorithm = algorithm
+        self.arrays = captured
+        self.counter = counter
+        self.end = end
+        self.results = results
+
+    def object(self) -> np.ndarray:
+        return self.results["object"]
+
+    def checkpoint(self) -> ReconstructionCheckpoint:
+        a = self.arrays
+        return ReconstructionCheckpoint(
+            completed_iterations=self.end, algorithm=self.algorithm._name, object_spectrum=a["object_spectrum"],
+            pupil=a["pupil"], velocity=a["velocity"], anchor=a["anchor"], momentum_counter=self.counter,
+            objectives=[float(v) for v in a["objectives"][:self.end]],
+            illumination_corrections=None if a["illumination"] is None else a["illumination"].copy())
+
+    def residual_images(self) -> np.ndarray:
+        """Forward intensities of the current object, pupil and illumination
+        corrections minus the measurements, zero at masked pixels
+        (src/reconstruction/runner.rs:435-454 and 335-395)."""
+        from .simulation import forward_intensities
+
+        model = self.problem.model
+        changes = dict(pupil=np.ascontiguousarray(self.arrays["pupil"], np.complex128))
+        if self.arrays["illumination"] is not None:
+            corrections = self.arrays["illumination"]
+            changes.update(offset_row=model._offset_row + corrections[:, 0],
+                           offset_col=model._offset_col + corrections[:, 1])
+        predicted = forward_intensities(model._replace(**changes), self.object())
+        measured = self.problem.measurements._data.reshape(predicted.shape)
+        residual = predicted - measured
+        masks = self.problem.measurements._masks
+        if masks is not None:
+            residual[~masks.reshape(predicted.shape).astype(bool)] = 0.0
+        return residual
+
+
+_SPECULATION = 16
+
+
 def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, download):
-    """Runs in segments through fpm_run_batch_resumable: from a checkpoint,
-    and/or stopping at every CheckpointEvery boundary to save the state."""
+    """Runs in device segments through fpm_run_batch_resumable: from a
+    checkpoint, and/or with host callbacks at iteration boundaries.
+
+    Segments end where a callback needs the state (plan_segment); hooks that
+    read only objectives are replayed after each segment in iteration order.
+    A stop request inside a segment re-runs the segment from its starting
+    state to the stopping iteration (src/reconstruction/runner.rs:76-285).
+    """
     if callbacks and len(problems) != 1:
-        raise UnsupportedError("CheckpointEvery is supported for single-problem runs")
+        raise UnsupportedError("callbacks are supported for single-problem runs")
     if resume_from is not None and not isinstance(resume_from, (list, tuple)):
         resume_from = [resume_from]
     if resume_from is not None and len(resume_from) != len(problems):
@@ -826,52 +880,80 @@ def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, downlo
     keep = []
     resume = None
     start = 0
+    trace = []
     if resume_from is not None:
         arrays = [_checkpoint_arrays(cp, p, algorithm) for cp, p in zip(resume_from, problems)]
         keep.append(arrays)
         start = resume_from[0].completed_iterations
         resume = (N.StateDesc * len(problems))(
             *[_state_desc(a, cp.completed_iterations, cp.momentum_counter) for a, cp in zip(arrays, resume_from)])
-    ends = sorted({k for cb in callbacks for k in range(start + 1, total) if k % cb.every == 0} | {total})
-    result_arrays = []
-    results = None
-    elapsed_total = 0.0
-    for end in ends:
+        trace = [(it + 1, float(v), 0.0) for it, v in enumerate(resume_from[0].objectives)]
+    name = problems[0].name
+    context = lambda iteration, objective, state=None: StepContext(  # noqa: E731
+        iteration=iteration, objective=objective, trace=trace, problem_name=name, algorithm=algorithm._name,
+        _state=state)
+    for cb in callbacks:
+        cb.on_start(context(start, None))
+
+    def segment(end):
         params.iterations = end
         captured = [_state_arrays(p, algorithm, end) for p in problems]
         capture = (N.StateDesc * len(problems))(*[_state_desc(a, 0, 0) for a in captured])
-        last = end == ends[-1]
-        if last and download:
-            results = (N.ResultDesc * len(problems))()
-            result_arrays = [_result_arrays(p, params, results[i]) for i, p in enumerate(problems)]
+        results = (N.ResultDesc * len(problems))()
+        result_arrays = [_result_arrays(p, params, results[i]) for i, p in enumerate(problems)]
         t0 = time.perf_counter()
         N.check(N.library().fpm_run_batch_resumable(ctx.handle, len(problems), handles, C.byref(params), resume,
                                                     results, capture), ctx.handle)
-        elapsed_total += time.perf_counter() - t0
-        checkpoints = [ReconstructionCheckpoint(
-            completed_iterations=end, algorithm=algorithm._name, object_spectrum=a["object_spectrum"],
-            pupil=a["pupil"], velocity=a["velocity"], anchor=a["anchor"],
-            momentum_counter=capture[i].momentum_counter, objectives=[float(v) for v in a["objectives"][:end]],
-            illumination_corrections=None if a["illumination"] is None else a["illumination"].copy())
-            for i, a in enumerate(captured)]
-        for cb in callbacks:
-            if end % cb.every == 0 and end > start:
-                cb.directory.mkdir(parents=True, exist_ok=True)
-                checkpoints[0].save(cb.path_for(end))
-        keep.append(captured)
-        resume = (N.StateDesc * len(problems))(
-            *[_state_desc(a, end, capture[i].momentum_counter) for i, a in enumerate(captured)])
-    if not download:
-        return [None] * len(problems)
-    out = []
-    for p, a in zip(problems, result_arrays):
-        trace = [(it + 1, float(a["objectives"][it]), elapsed_total) for it in range(total)]
-        out.append(ReconstructionResult(
+        seconds = time.perf_counter() - t0
+        states = [_SegmentState(p, algorithm, captured[i], capture[i].momentum_counter, end, result_arrays[i])
+                  for i, p in enumerate(problems)]
+        return states, seconds
+
+    current = start
+    elapsed = trace[-1][2] if trace else 0.0
+    stopped = False
+    while True:
+        end = plan_segment(callbacks, current, total, _SPECULATION)
+        states, seconds = segment(end)
+        stop_at = None
+        objectives = states[0].arrays["objectives"]
+        for it in range(current + 1, end + 1):
+            trace.append((it, float(objectives[it - 1]), elapsed + seconds * (it - current) / (end - current)))
+            step = context(it, float(objectives[it - 1]), states[0] if it == end else None)
+            requested = False
+            for cb in callbacks:
+                requested |= bool(cb.on_iteration_end(step))
+            if requested:
+                stop_at = it
+                break
+        elapsed += seconds
+        if stop_at is not None:
+            stopped = True
+            if stop_at < end:
+                states, seconds = segment(stop_at)
+                elapsed += seconds
+            end = stop_at
+        if stopped or end >= total:
+            break
+        keep.append(states)
+        resume = (N.StateDesc * len(problems))(*[_state_desc(st.arrays, end, st.counter) for st in states])
+        current = end
+    out = [] if download else [None] * len(problems)
+    for p, st in zip(problems, states if download else []):
+        a = st.results
+        records = trace if len(problems) == 1 else [(it + 1, float(a["objectives"][it]), elapsed)
+                                                    for it in range(end)]
+        result = ReconstructionResult(
             object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
-            pupil_support=p.model.pupil_support, trace=trace,
-            runtime=RuntimeInfo(elapsed_total, total, False, algorithm._name),
+            pupil_support=p.model.pupil_support, trace=list(records),
+            runtime=RuntimeInfo(elapsed, end, stopped, algorithm._name),
             recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
-            calibrated_illumination=a["illumination"]))
+            calibrated_illumination=a["illumination"])
+        if p.name is not None:
+            result.metadata["problem_name"] = p.name
+        out.append(result)
+    for cb in callbacks:
+        cb.on_finish(out[0])
     return out
 
 

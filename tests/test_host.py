@@ -139,7 +139,8 @@ def test_unsupported_options_fail_before_device_work(fpm):
         fpm.AlternatingProjection(iterations=1).run(problem, schedule="random")
     with pytest.raises(ValueError):
         fpm.AlternatingProjection(iterations=1).run(problem, schedule="spiral")
-    with pytest.raises(fpm.UnsupportedError):
+    # python/src/reconstruction.rs:1074-1078: other objects are a TypeError.
+    with pytest.raises(TypeError):
         fpm.AlternatingProjection(iterations=1).run(problem, callbacks=[object()])
     with pytest.raises(fpm.UnsupportedError):
         fpm.GradientDescent(recover_illumination=True, recover_pupil=True)
@@ -210,8 +211,10 @@ def test_checkpoint_json_round_trip(fpm, tmp_path):
                                       pupil=pupil, objectives=[1.0], illumination_corrections=corr)
     gd.save(tmp_path / "gd.json")
     assert np.array_equal(fpm.ReconstructionCheckpoint.load(tmp_path / "gd.json").illumination_corrections, corr)
-    with pytest.raises(fpm.InvalidParameterError):
-        fpm.CheckpointEvery(0, tmp_path)
+    # python/src/reconstruction.rs:839-848: a zero interval becomes one.
+    assert fpm.CheckpointEvery(0, tmp_path).every == 1
+    with pytest.raises(OverflowError):
+        fpm.CheckpointEvery(-1, tmp_path)
     assert fpm.CheckpointEvery(2, tmp_path).path_for(2).name == "checkpoint_00002.json"
 
 
