@@ -90,6 +90,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
     ap.add_argument("--cpu-sample-iterations", type=int, default=1)
+    ap.add_argument("--engine-256", choices=("auto", "single", "cluster"), default="auto",
+                    help="frame-engine shape of 256-point tiles (auto: single CTA for large launches)")
     return ap.parse_args()
 
 
@@ -289,6 +291,8 @@ def run_ours(args):
     import fpm_rs as fpm
     import oracle
 
+    fpm.tuning.set_engine_shape(256, {"auto": fpm.tuning.AUTO, "single": fpm.tuning.SINGLE_CTA,
+                                      "cluster": fpm.tuning.CLUSTER}[args.engine_256])
     models = build_models(fpm)
     sizes = tile_sizes(args.tiles, args.seed)
     seed_base = 1_000_000 * dist.rank + 10_000
@@ -325,8 +329,10 @@ def run_ours(args):
         engine_span += st["engine_span_ms"]
         engine_sum += st["engine_ms_sum"]
         engine_launches += st["engine_launches"]
+        bucket_end = {}
         for n, count, end_ms in st["buckets"]:
             latencies += [end_ms] * count
+            bucket_end[str(n)] = round(end_ms, 1)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     dist.barrier()
@@ -435,7 +441,12 @@ def run_ours(args):
             "timing": "device span of each batch from CUDA events on the library's streams",
             "setup_s": round(setup_s, 1),
             "engine_shapes": {"32": "1 CTA x 32 rows", "64": "2-CTA cluster x 32 rows",
-                              "128": "8-CTA cluster x 16 rows", "256": "16-CTA cluster x 16 rows, TMA stencil staging"},
+                              "128": "8-CTA cluster x 16 rows",
+                              "256": {"auto": "single 512-thread CTA per tile, field scratch in L2, when a launch "
+                                              "holds >= 2/3 of the resident CTAs; else 16-CTA cluster x 16 rows, "
+                                              "TMA stencil staging",
+                                      "single": "single 512-thread CTA per tile, field scratch in L2",
+                                      "cluster": "16-CTA cluster x 16 rows, TMA stencil staging"}[args.engine_256]},
             "engine_grid": (fpm.tuning.load() or {}).get("grid", "one cluster per tile (no tuning table)"),
         },
         "roofline": {
@@ -459,6 +470,7 @@ def run_ours(args):
                 "seconds_per_step": e2e_s},
         "gpu_launches": launches // max(1, args.steps),
         "clocks": clock_info,
+        "size_done_ms": bucket_end,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                        "definition": "batch start to the tile's results ready on the device"},
         "nrmse_vs_fp64": {"tiles_checked": len(nrmse), "tile_sizes": checked_sizes,

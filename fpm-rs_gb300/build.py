@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfpm_gpu.so")
 SOURCES = ["engine_n256.cu", "engine_n256_gd.cu", "engine_n128.cu", "engine_n128_gd.cu", "engine_n64.cu",
-           "engine_n64_gd.cu", "engine_n32.cu", "engine_n32_gd.cu", "engine.cu", "grid.cu", "camera.cu", "noalloc.cu", "runtime.cpp", "server.cpp"]
+           "engine_n64_gd.cu", "engine_n32.cu", "engine_n32_gd.cu", "engine.cu", "engine_l2.cu", "grid.cu", "camera.cu", "noalloc.cu", "runtime.cpp", "server.cpp"]
 HEADERS = ["fpm_common.cuh", "kernels.h", "twiddle256.cuh", "engine_impl.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

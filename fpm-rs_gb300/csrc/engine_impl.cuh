@@ -491,7 +491,7 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
     __syncthreads();
     const TileDesc& T = s_tile;
     const bool use_tma = tma_capable && T.omap != nullptr && (smem_u32(osm) & 127u) == 0;
-    const float eps = (float)P.eps;  // epsilon in the per-pixel FP32 arithmetic
+    const float eps = opaque((float)P.eps);  // epsilon in the per-pixel FP32 arithmetic
     const int M = T.M;
     const long long ostride = M + (M & 1);
     const int i_lo = C == 1 ? 0 : c * R;
@@ -1003,11 +1003,12 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
                     epry || gd_pupil ? (double)fmaxf(frame_max_pup, eps) : T.max_pupil_power;
                 const double obj_den = (double)fmaxf(frame_max_obj, eps) + P.eps;
                 // Pupil gradient weight w * (N^2 / valid) / (max |patch|^2 + eps).
-                const float pupil_grad_scale = gd_pupil ? (float)((double)fp.weight * fp.valid_scale / obj_den) : 0.f;
-                const float inv_global = (float)(1.0 / (max_p2 + P.eps));
-                const float pupil_scale = epry ? (float)((double)fp.weight * P.pupil_step / obj_den) : 0.f;
+                const float pupil_grad_scale =
+                    opaque(gd_pupil ? (float)((double)fp.weight * fp.valid_scale / obj_den) : 0.f);
+                const float inv_global = opaque((float)(1.0 / (max_p2 + P.eps)));
+                const float pupil_scale = opaque(epry ? (float)((double)fp.weight * P.pupil_step / obj_den) : 0.f);
                 // rPIE: 1 / ((1 - alpha) |P|^2 + alpha max|P|^2 + eps) = 1 / (rpie_a |P|^2 + rpie_b).
-                const float rpie_a = (float)(1.0 - P.alpha), rpie_b = (float)(P.alpha * max_p2 + P.eps);
+                const float rpie_a = opaque((float)(1.0 - P.alpha)), rpie_b = opaque((float)(P.alpha * max_p2 + P.eps));
                 // U of one task (row l, column class jb) into v, from the row's
                 // transform in v: pixels j = (NB * ja + jb + N / 2) mod N.
                 auto correction = [&](float2 (&v)[NA], int i, int jb) {
@@ -1114,10 +1115,10 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
                 // Projection: O += w * step * adj(U). Gradient descent: O -= step *
                 // w * (N^2 / valid) * adj(U), or with mini-batches G += w *
                 // (N^2 / valid) * adj(U).
-                const float scale = spectral     ? (float)((double)sp.update_scale * P.object_step)
-                                    : projection ? (float)((double)fp.weight * (adaptive ? ada_step : P.object_step))
-                                    : gd_batched ? fp.weight * fp.valid_scale
-                                                 : (float)(-P.object_step * (double)fp.weight * fp.valid_scale);
+                const float scale = opaque(spectral     ? (float)((double)sp.update_scale * P.object_step)
+                                           : projection ? (float)((double)fp.weight * (adaptive ? ada_step : P.object_step))
+                                           : gd_batched ? fp.weight * fp.valid_scale
+                                                        : (float)(-P.object_step * (double)fp.weight * fp.valid_scale));
                 // Spectral updates stage the current object at the step start: an
                 // earlier mode of the same exposure may have changed it.
                 float2* target = gd_batched ? T.gradient : obj;

@@ -94,6 +94,15 @@ FPM_DEVICE void dft_reg(float2 (&v)[L]) {
     }
 }
 
+// A float the compiler must keep (in a register, or spilled) rather than
+// recompute: values derived from FP64 kernel parameters would otherwise be
+// re-derived at each use inside the pixel loops, and every conversion from
+// FP64 occupies the FP64 pipe, which is narrow on GB300.
+FPM_DEVICE float opaque(float x) {
+    asm volatile("" : "+f"(x));
+    return x;
+}
+
 // Block-wide reductions used once per frame or iteration.
 FPM_DEVICE float warp_max(float v) {
 #pragma unroll

@@ -90,6 +90,10 @@ struct TileDesc {
     // correction U there is zero, so the engine skips those rows (EPRY,
     // whose pupil evolves, uses the full range).
     int row_lo, row_hi;
+    // Unit pupil: per centred row the column interval [x, y] where the pupil
+    // is exactly 1 (0 elsewhere; empty rows hold x > y), or null when the
+    // pupil has any other value. Read by the single-CTA engine.
+    const int2* pupil_span;
     // Spectral AP: objects are consecutive M x (M + M % 2) grids from
     // `object`, channel pupils consecutive N x N grids from `pupil`.
     const SpectralStep* steps;  // [step_count] per pass
@@ -133,6 +137,10 @@ struct EngineParams {
     // frame_end) of its one pass (one GD batch between regulariser steps),
     // adding its objective partials to the pass's when `accumulate`.
     int frame_begin, frame_end, accumulate;
+    // Single-CTA engine: per-CTA field scratch, [launch CTAs][N * N], and
+    // whether every tile has a unit pupil (TileDesc::pupil_span set).
+    float2* field_scratch;
+    int unit_pupils;
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.
@@ -155,6 +163,15 @@ int engine_rows(int n);
 cudaError_t launch_engine(int n, const EngineParams& p, int clusters, cudaStream_t s);
 cudaError_t engine_max_active_clusters(int n, int* count);
 cudaError_t launch_forward(int n, const ForwardParams& p, cudaStream_t s);
+
+// Single-CTA frame engine (engine_l2.cu): one 512-thread CTA per tile, the
+// field through a per-CTA scratch of engine_l2_scratch_bytes(n) bytes in
+// p.field_scratch; 256-point tiles of the fixed-pupil projection families
+// with amplitude-form measurements.
+bool engine_l2_supported(int n, int alg);
+size_t engine_l2_scratch_bytes(int n);
+cudaError_t launch_engine_l2(int n, const EngineParams& p, int ctas, cudaStream_t s);
+cudaError_t engine_l2_max_active_ctas(int n, int* count);
 
 // Permutes natural-order frames [frames][N][N] into the engine layout.
 cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s);

@@ -193,6 +193,11 @@ struct fpm_context {
     // Clusters of a frame-engine launch per tile size (index log2(n) - 5; 0:
     // one cluster per tile); with fewer, each cluster walks several tiles.
     int engine_grid[4] = {0, 0, 0, 0};
+    // Frame-engine shape per tile size (FPM_ENGINE_CLUSTER, _SINGLE_CTA or
+    // _AUTO).
+    int engine_shape[4] = {FPM_ENGINE_CLUSTER, FPM_ENGINE_CLUSTER, FPM_ENGINE_CLUSTER, FPM_ENGINE_AUTO};
+    // CTAs of a single-CTA engine launch per tile size (0: as many as fit at once).
+    int engine_ctas[4] = {0, 0, 0, 0};
 };
 
 struct fpm_problem {
@@ -204,6 +209,8 @@ struct fpm_problem {
     std::vector<double> pupil;  // complex128 interleaved
     std::vector<double> upload_gains;  // host sources of asynchronous uploads
     std::vector<float2> pupil_f32;
+    std::vector<int2> pupil_spans;  // host source of pupil_span
+    bool unit_pupil = false;  // pupil_f32 is exactly 1 on one column interval per row and 0 elsewhere
     int host_status = 0;                // result downloads
     std::vector<double> host_partials;
     int it0 = 0;                        // first iteration of the last run (resumed runs start later)
@@ -217,7 +224,7 @@ struct fpm_problem {
     bool row_exact = true, col_exact = true;
     double weight_sum = 0.0;
     // resident device data
-    DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model;
+    DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model, pupil_span;
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
         object_err, gradient_err,
@@ -684,7 +691,7 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     const int N = p->n, F = p->frames;
     const size_t n2 = (size_t)N * N;
     for (DeviceBuffer* b : {&p->meas, &p->masks, &p->background, &p->frame_params, &p->support_d, &p->pupil_ref,
-                            &p->pupil_model})
+                            &p->pupil_model, &p->pupil_span})
         b->bind(ctx->pool, s);
     DeviceBuffer staging, mask_staging, gain_staging;
     for (DeviceBuffer* b : {&staging, &mask_staging, &gain_staging}) b->bind(ctx->pool, s);
@@ -737,6 +744,32 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)p->pupil[2 * i], (float)p->pupil[2 * i + 1]);
     FPM_TRY(p->pupil_model.ensure(n2 * sizeof(float2)));
     FPM_CUDA(cudaMemcpyAsync(p->pupil_model.ptr, pf.data(), n2 * sizeof(float2), cudaMemcpyHostToDevice, s));
+    // Unit pupil: every value exactly 0 or 1 (FP32), the ones of each row on
+    // one column interval. The single-CTA engine then reads the intervals
+    // instead of the pupil; P * patch and U come out the same.
+    std::vector<int2>& spans = p->pupil_spans;
+    spans.assign(N, make_int2(0, -1));
+    p->unit_pupil = true;
+    for (int i = 0; i < N && p->unit_pupil; ++i) {
+        int lo = N, hi = -1, ones = 0;
+        for (int j = 0; j < N; ++j) {
+            const float2 v = pf[(size_t)i * N + j];
+            if (v.x == 0.f && v.y == 0.f) continue;
+            if (v.x != 1.f || v.y != 0.f) {
+                p->unit_pupil = false;
+                break;
+            }
+            lo = std::min(lo, j);
+            hi = std::max(hi, j);
+            ++ones;
+        }
+        if (ones > 0 && ones != hi - lo + 1) p->unit_pupil = false;
+        if (ones > 0) spans[i] = make_int2(lo, hi);
+    }
+    if (p->unit_pupil) {
+        FPM_TRY(p->pupil_span.ensure(N * sizeof(int2)));
+        FPM_CUDA(cudaMemcpyAsync(p->pupil_span.ptr, spans.data(), N * sizeof(int2), cudaMemcpyHostToDevice, s));
+    }
     return Status::ok();
 }
 
@@ -966,6 +999,7 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
 }
 
 struct BucketRun {
+    DeviceBuffer field_scratch;  // single-CTA engine: per-CTA field scratch
     DeviceBuffer tmaps;  // per tile: the object spectrum's tensor map for TMA stencil staging
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
         tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks, ill_fields, ill_valid, ill_ptrs;
@@ -992,11 +1026,44 @@ struct BucketRun {
 
 int engine_grid_slot(int n) { return n == 32 ? 0 : n == 64 ? 1 : n == 128 ? 2 : n == 256 ? 3 : -1; }
 
+// Whether a launch of `tiles` tiles of size n takes the single-CTA engine
+// (alg: its family; `eligible`: measurements and options it takes). AUTO
+// picks it once the launch holds at least two thirds of the CTAs that fit
+// at once: a lone tile then runs about seven times longer on one CTA than
+// on a 16-CTA cluster, while a full device of single CTAs has the higher
+// throughput.
+Status single_cta_engine(const fpm_context* ctx, int n, int alg, bool eligible, int tiles, bool* single,
+                         int* resident) {
+    *single = false;
+    *resident = 0;
+    const int k = engine_grid_slot(n);
+    if (k < 0 || ctx->engine_shape[k] == FPM_ENGINE_CLUSTER || !eligible || !fpm::engine_l2_supported(n, alg))
+        return Status::ok();
+    FPM_CUDA(fpm::engine_l2_max_active_ctas(n, resident));
+    *single = ctx->engine_shape[k] == FPM_ENGINE_SINGLE_CTA || 3 * tiles >= 2 * *resident;
+    return Status::ok();
+}
+
 // Clusters of an engine launch over `tiles` tiles of size n.
 int engine_clusters(const fpm_context* ctx, int n, int tiles) {
     const int k = engine_grid_slot(n);
     const int g = k >= 0 ? ctx->engine_grid[k] : 0;
     return g > 0 && g < tiles ? g : tiles;
+}
+
+// The frame-engine family of an algorithm's parameters.
+int engine_family(const fpm_algorithm_params* a) {
+    switch (a->algorithm) {
+        case FPM_ALG_AP: return fpm::kAlgLocal;
+        case FPM_ALG_ADAPTIVE_AP: return fpm::kAlgLocalAdaptive;
+        case FPM_ALG_FPIE:
+        case FPM_ALG_MPIE: return fpm::kAlgRpie;
+        case FPM_ALG_EPRY: return a->recover_pupil ? fpm::kAlgEpry : fpm::kAlgGlobal;
+        default:
+            return a->recover_pupil       ? fpm::kAlgGradientPupil
+                   : a->poisson_truncation ? fpm::kAlgGradientTruncated
+                                           : fpm::kAlgGradient;
+    }
 }
 
 Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cudaStream_t s, BucketRun& br) {
@@ -1120,6 +1187,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                     T.row_hi = std::max(T.row_hi, i);
                 }
             }
+        // A resumed run's pupil comes from its checkpoint, not the compiled model.
+        T.pupil_span = p->unit_pupil && !resumed ? p->pupil_span.as<int2>() : nullptr;
         T.masks = p->has_masks && !p->amplitude ? p->masks.as<uint8_t>() : nullptr;
         T.background = p->has_background ? p->background.as<float>() : nullptr;
         T.background_stride = p->background_stride;
@@ -1305,18 +1374,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     fpm::EngineParams ep{};
     ep.tiles = br.tiles.as<fpm::TileDesc>();
     ep.tile_count = count;
-    switch (a->algorithm) {
-        case FPM_ALG_AP: ep.alg = fpm::kAlgLocal; break;
-        case FPM_ALG_ADAPTIVE_AP: ep.alg = fpm::kAlgLocalAdaptive; break;
-        case FPM_ALG_FPIE:
-        case FPM_ALG_MPIE: ep.alg = fpm::kAlgRpie; break;
-        case FPM_ALG_EPRY: ep.alg = canonical ? fpm::kAlgEpry : fpm::kAlgGlobal; break;
-        default:
-            ep.alg = a->recover_pupil       ? fpm::kAlgGradientPupil
-                     : a->poisson_truncation ? fpm::kAlgGradientTruncated
-                                             : fpm::kAlgGradient;
-            break;
-    }
+    ep.alg = engine_family(a);
     ep.alpha = a->stability;
     ep.eps = a->epsilon;
     ep.object_step = a->object_step;
@@ -1334,6 +1392,24 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.minimum_step = a->minimum_object_step;
     ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
     ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
+    // The single-CTA engine takes 256-point tiles of the fixed-pupil
+    // projection families with amplitude-form measurements and plain
+    // accumulation; other runs use the cluster engine.
+    bool all_amplitude = true;
+    for (fpm_problem* p : b.problems) all_amplitude = all_amplitude && p->amplitude;
+    bool single = false;
+    int resident = 0;
+    FPM_TRY(single_cta_engine(ctx, N, ep.alg, all_amplitude && !compensated && !regularised, count, &single, &resident));
+    int units = engine_clusters(ctx, N, count);
+    if (single) {
+        const int want = ctx->engine_ctas[engine_grid_slot(N)];
+        units = std::max(1, std::min(count, want > 0 ? want : resident));
+        br.field_scratch.bind(ctx->pool, s);
+        FPM_TRY(br.field_scratch.ensure(fpm::engine_l2_scratch_bytes(N) * (size_t)units));
+        ep.field_scratch = br.field_scratch.as<float2>();
+        ep.unit_pupils = 1;
+        for (const fpm::TileDesc& T : tiles) ep.unit_pupils &= T.pupil_span != nullptr ? 1 : 0;
+    }
     auto engine = [&](int it0, int it1) -> Status {
         cudaEvent_t e0, e1;
         FPM_CUDA(cudaEventCreate(&e0));
@@ -1343,7 +1419,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         ep.it_begin = it0;
         ep.it_end = it1;
         FPM_CUDA(br.record(e0, s));
-        FPM_CUDA(fpm::launch_engine(N, ep, engine_clusters(ctx, N, count), s));
+        if (single) FPM_CUDA(fpm::launch_engine_l2(N, ep, units, s));
+        else FPM_CUDA(fpm::launch_engine(N, ep, units, s));
         FPM_CUDA(br.record(e1, s));
         br.launches += 1;
         return Status::ok();
@@ -1778,15 +1855,31 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
     std::stable_sort(groups.begin(), groups.end(), [](const auto& x, const auto& y) { return x.first.first > y.first.first; });
     std::vector<Bucket> chunks;
     for (const auto& g : groups) {
-        size_t acc = 0;
+        // Sizes whose engine picks its shape by the launch's tile count
+        // keep enough tiles per chunk for the single-CTA engine.
+        size_t min_tiles = 1;
+        {
+            bool single = false;
+            int resident = 0;
+            const bool amplitude = mds[g.second[0]].background == nullptr;
+            FPM_TRY(single_cta_engine(ctx, g.first.first, engine_family(a), amplitude && !a->compensated_accumulation,
+                                      (int)g.second.size(), &single, &resident));
+            if (single) {
+                const size_t parts = std::max<size_t>(1, g.second.size() / std::max(1, (2 * resident + 2) / 3));
+                min_tiles = (g.second.size() + parts - 1) / parts;
+            }
+        }
+        size_t acc = 0, tiles = 0;
         for (int i : g.second) {
             if (chunks.empty() || chunks.back().n != g.first.first || chunks.back().m != g.first.second ||
-                acc + bytes[i] > kChunkBytes) {
+                (acc + bytes[i] > kChunkBytes && tiles >= min_tiles)) {
                 chunks.push_back(Bucket{g.first.first, g.first.second, {}, {}});
                 acc = 0;
+                tiles = 0;
             }
             chunks.back().indices.push_back(i);
             acc += bytes[i];
+            ++tiles;
         }
     }
     std::vector<std::unique_ptr<BucketRun>> runs;
@@ -3404,14 +3497,40 @@ int32_t fpm_set_engine_grid(fpm_context* ctx, int32_t n, int32_t clusters) {
     return FPM_OK;
 }
 
+int32_t fpm_set_engine_ctas(fpm_context* ctx, int32_t n, int32_t ctas) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const int k = engine_grid_slot(n);
+    if (k < 0) return finish(ctx, Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n));
+    if (ctas < 0) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "ctas must be non-negative"));
+    ctx->engine_ctas[k] = ctas;
+    return FPM_OK;
+}
+
+int32_t fpm_set_engine_shape(fpm_context* ctx, int32_t n, int32_t shape) {
+    if (!ctx) return finish(nullptr, Status::make(FPM_ERR_INVALID_PARAMETER, "context is null"));
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const int k = engine_grid_slot(n);
+    if (k < 0) return finish(ctx, Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n));
+    if (shape != FPM_ENGINE_CLUSTER && shape != FPM_ENGINE_SINGLE_CTA && shape != FPM_ENGINE_AUTO)
+        return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "engine shape must be FPM_ENGINE_CLUSTER, "
+                                                                   "FPM_ENGINE_SINGLE_CTA or FPM_ENGINE_AUTO"));
+    if (shape != FPM_ENGINE_CLUSTER && n != 256)
+        return finish(ctx, Status::make(FPM_ERR_UNSUPPORTED, "the single-CTA engine takes 256-point tiles only"));
+    ctx->engine_shape[k] = shape;
+    return FPM_OK;
+}
+
 int32_t fpm_engine_max_clusters(fpm_context* ctx, int32_t n, int32_t* clusters) {
     if (!ctx || !clusters) return finish(ctx, Status::make(FPM_ERR_INVALID_PARAMETER, "null argument"));
     std::lock_guard<std::mutex> lock(ctx->mu);
     auto body = [&]() -> Status {
         FPM_CUDA(cudaSetDevice(ctx->device));
         int count = 0;
-        if (engine_grid_slot(n) < 0) return Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n);
-        FPM_CUDA(fpm::engine_max_active_clusters(n, &count));
+        const int k = engine_grid_slot(n);
+        if (k < 0) return Status::make(FPM_ERR_UNSUPPORTED, "tile size %d has no frame engine", n);
+        if (ctx->engine_shape[k] != FPM_ENGINE_CLUSTER) FPM_CUDA(fpm::engine_l2_max_active_ctas(n, &count));
+        else FPM_CUDA(fpm::engine_max_active_clusters(n, &count));
         *clusters = count;
         return Status::ok();
     };

@@ -30,7 +30,8 @@ EXPORTED = (
     "fpm_run_batch_submit", "fpm_spectral_run_batch_submit", "fpm_job_poll", "fpm_job_wait", "fpm_job_stats", "fpm_job_destroy",
     "fpm_plan_create", "fpm_plan_launch", "fpm_plan_wait", "fpm_plan_collect", "fpm_plan_destroy",
     "fpm_server_create", "fpm_server_submit", "fpm_server_poll", "fpm_server_wait", "fpm_server_stats_get",
-    "fpm_server_destroy", "fpm_set_engine_grid", "fpm_engine_max_clusters",
+    "fpm_server_destroy", "fpm_set_engine_grid", "fpm_engine_max_clusters", "fpm_set_engine_shape",
+    "fpm_set_engine_ctas",
 )
 
 
@@ -270,14 +271,19 @@ def context() -> Context:
 
 
 def _apply_tuning(ctx: "Context") -> None:
-    """The committed frame-engine launch grids (tuning.json), if any."""
+    """The committed frame-engine shapes and launch grids (tuning.json), if any."""
     import json
 
     try:
         with open(os.path.join(PACKAGE_ROOT, "tuning.json")) as handle:
-            grid = json.load(handle).get("grid", {})
+            table = json.load(handle)
     except (OSError, ValueError):
         return
+    grid = table.get("grid", {})
+    for n, shape in table.get("shape", {}).items():
+        check(ctx._lib.fpm_set_engine_shape(ctx.handle, int(n), int(shape)), ctx.handle)
+    for n, ctas in table.get("ctas", {}).items():
+        check(ctx._lib.fpm_set_engine_ctas(ctx.handle, int(n), int(ctas)), ctx.handle)
     for n in (32, 64, 128, 256):
         clusters = int(grid.get(str(n), 0))
         if clusters:

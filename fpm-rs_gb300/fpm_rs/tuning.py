@@ -36,10 +36,32 @@ def set_engine_grid(n: int, clusters: int) -> None:
     N.check(N.library().fpm_set_engine_grid(ctx.handle, int(n), int(clusters)), ctx.handle)
 
 
-def apply(grid: dict) -> None:
-    """Applies {tile size: clusters} (0: one cluster per tile) to the context."""
+CLUSTER, SINGLE_CTA, AUTO = 0, 1, 2  # FPM_ENGINE_CLUSTER, FPM_ENGINE_SINGLE_CTA, FPM_ENGINE_AUTO
+
+
+def set_engine_shape(n: int, shape: int) -> None:
+    """Selects the cluster engine (0), the single-CTA engine (1, 256-point
+    tiles) or the choice by launch size (2, the default for 256) for size n."""
+    ctx = N.context()
+    N.check(N.library().fpm_set_engine_shape(ctx.handle, int(n), int(shape)), ctx.handle)
+
+
+def set_engine_ctas(n: int, ctas: int) -> None:
+    """CTAs of a single-CTA engine launch of size n (0: as many as fit at once)."""
+    ctx = N.context()
+    N.check(N.library().fpm_set_engine_ctas(ctx.handle, int(n), int(ctas)), ctx.handle)
+
+
+def apply(grid: dict, shape: dict | None = None, ctas: dict | None = None) -> None:
+    """Applies {tile size: engine shape}, {tile size: clusters} of cluster
+    launches and {tile size: CTAs} of single-CTA launches (0: the default)
+    to the context."""
+    for n, sh in (shape or {}).items():
+        set_engine_shape(int(n), int(sh))
     for n in SIZES:
         set_engine_grid(n, int(grid.get(str(n), grid.get(n, 0))))
+    for n, c in (ctas or {}).items():
+        set_engine_ctas(int(n), int(c))
 
 
 def load(path: str = TABLE_PATH) -> dict | None:

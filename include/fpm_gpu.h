@@ -462,8 +462,27 @@ int32_t fpm_plan_destroy(fpm_plan *plan);
  * 0 (the default) gives every tile its own cluster. Autotuners set it per
  * tile size n in {32, 64, 128, 256}. */
 int32_t fpm_set_engine_grid(fpm_context *ctx, int32_t n, int32_t clusters);
-/* Clusters of an n x n tile's frame engine that fit on the device at once. */
+/* Clusters of an n x n tile's frame engine that fit on the device at once
+ * (CTAs when the tile size's shape is FPM_ENGINE_SINGLE_CTA or _AUTO). */
 int32_t fpm_engine_max_clusters(fpm_context *ctx, int32_t n, int32_t *clusters);
+/* Frame-engine shape of a tile size. FPM_ENGINE_CLUSTER splits a tile over
+ * a thread-block cluster (rows across CTAs, exchanges through distributed
+ * shared memory). FPM_ENGINE_SINGLE_CTA gives a tile one 512-thread CTA
+ * whose 2-D transforms pass through a per-CTA field scratch held in L2
+ * (256-point tiles of AP, FPIE, mPIE and EPRY without pupil recovery, with
+ * measurements that have no background and plain accumulation; other runs
+ * keep the cluster engine): a higher throughput over many tiles, a longer
+ * time for one. FPM_ENGINE_AUTO takes the single-CTA engine for launches of
+ * at least two thirds of the CTAs that fit at once, else the cluster
+ * engine. Default: AUTO for n = 256, the cluster engine for the other
+ * sizes. Both shapes compute the update of src/algorithms/common.rs:57-306
+ * with the same arithmetic per value; fpm_set_engine_grid applies to
+ * cluster launches, fpm_set_engine_ctas to single-CTA launches. */
+enum { FPM_ENGINE_CLUSTER = 0, FPM_ENGINE_SINGLE_CTA = 1, FPM_ENGINE_AUTO = 2 };
+int32_t fpm_set_engine_shape(fpm_context *ctx, int32_t n, int32_t shape);
+/* CTAs of a single-CTA engine launch of tile size n, which walk the
+ * launch's tiles as the clusters do (0, the default: as many as fit at once). */
+int32_t fpm_set_engine_ctas(fpm_context *ctx, int32_t n, int32_t ctas);
 
 /* ------------------------------------------------------- serving loop */
 /* A request loop over one context: the work run_algorithm

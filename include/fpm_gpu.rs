@@ -98,6 +98,8 @@ extern "C" {
     pub fn fpm_plan_destroy(plan: *mut FpmPlan) -> i32;
     pub fn fpm_set_engine_grid(ctx: *mut FpmContext, n: i32, clusters: i32) -> i32;
     pub fn fpm_engine_max_clusters(ctx: *mut FpmContext, n: i32, clusters: *mut i32) -> i32;
+    pub fn fpm_set_engine_shape(ctx: *mut FpmContext, n: i32, shape: i32) -> i32;
+    pub fn fpm_set_engine_ctas(ctx: *mut FpmContext, n: i32, ctas: i32) -> i32;
     pub fn fpm_server_create(ctx: *mut FpmContext, config: *const FpmServerConfig, server: *mut *mut FpmServer) -> i32;
     pub fn fpm_server_submit(server: *mut FpmServer, model: *const FpmModelDesc, m: *const FpmMeasurementDesc,
         a: *const FpmAlgorithmParams, r: *mut FpmResultDesc, request: *mut u64) -> i32;
