@@ -90,6 +90,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
     ap.add_argument("--cpu-sample-iterations", type=int, default=1)
+    ap.add_argument("--tune", action="store_true",
+                    help="run the launch-table autotuner on the tile workload, write tuning.json and exit")
     ap.add_argument("--engine-256", choices=("auto", "single", "cluster"), default="auto",
                     help="frame-engine shape of 256-point tiles (auto: single CTA for large launches)")
     return ap.parse_args()
@@ -306,6 +308,16 @@ def run_ours(args):
         p.device_handle()
     setup_s = time.perf_counter() - t0
     algo = fpm.Mpie(iterations=args.iterations)
+    if args.tune:
+        # Launch table for this workload: every candidate timed on the
+        # resident problems, the fastest written where contexts load it.
+        table = fpm.tuning.autotune(algo, problems)
+        if dist.rank == 0:
+            fpm.tuning.save(table)
+            print(json.dumps({"tuned": table["grid"], "ctas": table["ctas"],
+                              "measured": [(m["grid"], m["ctas"], round(m["run_ms"], 1)) for m in table["measured"]]}),
+                  flush=True)
+        return
 
     # value: device-resident inputs, results left on the device.
     for _ in range(args.warmup):
@@ -448,6 +460,7 @@ def run_ours(args):
                                       "single": "single 512-thread CTA per tile, field scratch in L2",
                                       "cluster": "16-CTA cluster x 16 rows, TMA stencil staging"}[args.engine_256]},
             "engine_grid": (fpm.tuning.load() or {}).get("grid", "one cluster per tile (no tuning table)"),
+            "engine_ctas": (fpm.tuning.load() or {}).get("ctas", {}),
         },
         "roofline": {
             "bound": "hbm",

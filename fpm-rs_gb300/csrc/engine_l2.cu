@@ -31,9 +31,14 @@ namespace fpm {
 namespace {
 
 constexpr int kL2N = 256;
+// 512 threads per CTA, one CTA per SM (128 registers per thread). Two
+// 256-thread CTAs per SM (kL2Threads = 256, 16-position blocks in phase B)
+// measured the same SM time per tile and a slower tile mix on GB300.
 constexpr int kL2Threads = 512;
+constexpr int kL2PerSm = 512 / kL2Threads;     // resident CTAs per SM (registers: 128 per thread)
 constexpr int kL2Warps = kL2Threads / 32;
-constexpr int kL2Stage = 16 * 16 * 32;         // one column-stage buffer: [16][16][32 positions]
+constexpr int kL2Pos = kL2Threads / 16;        // phase B: positions per block (one thread per digit and position)
+constexpr int kL2Stage = 16 * 16 * kL2Pos;     // one column-stage buffer: [16][16][positions]
 constexpr int kL2Tp = 17;                      // transpose row stride (float2): conflict-free rows and columns
 constexpr int kL2HalfBuf = 16 * kL2Tp;         // one half-warp's 16 x 16 transpose buffer
 constexpr int kL2Slot = 16 * kL2Tp;            // one ring row: N = 256 values of U, or a transpose
@@ -44,13 +49,13 @@ constexpr int kL2CtaOfN = Cfg<kL2N>::C;        // objective partial slots per it
 constexpr int kL2Rings = kL2Warps * 3 * kL2Slot;
 static_assert(kL2Slot >= kL2N, "a ring row holds a row of U");
 constexpr int kL2Region = 2 * kL2Stage > kL2Rings ? 2 * kL2Stage : kL2Rings;
-static_assert(32 * kL2HalfBuf <= kL2Region, "phase A transposes fit the work region");
+static_assert(2 * kL2Warps * kL2HalfBuf <= kL2Region, "phase A transposes fit the work region");
 // tw[256] + work region + pupil spans [N] + per-warp FP64 partials.
 constexpr int kL2SmemBytes = (256 + kL2Region) * 8 + kL2N * 8 + kL2Warps * 8;
 
 // Preferred shared-memory carveout (percent of the 228 KB maximum): the
-// dynamic and static shared memory plus the 1 KB reserved per CTA.
-constexpr int kL2Carveout = ((kL2SmemBytes + 1024 + 1024) * 100 + 228 * 1024 - 1) / (228 * 1024);
+// resident CTAs' dynamic and static shared memory plus the 1 KB reserved per CTA.
+constexpr int kL2Carveout = (kL2PerSm * (kL2SmemBytes + 1024 + 1024) * 100 + 228 * 1024 - 1) / (228 * 1024);
 
 // Element (r, c) of a 16 x 16 transpose buffer.
 FPM_DEVICE constexpr int tpos(int r, int c) { return r * kL2Tp + c; }
@@ -245,35 +250,37 @@ FPM_DEVICE void engine_l2_tile(const EngineParams& P, const int tile) {
             }
             __syncthreads();
 
-            // B: columns, 32 positions t at a time. Stage 1: warp = natural
-            // row low digit l, register = high digit; stage 2: warp = k1,
-            // register m = spatial row k1 + 16 m (the engine layout's row
-            // 16 k1 + m); the forward transform mirrors it.
+            // B: columns, kL2Pos positions t at a time; thread (d, pos) with
+            // d = tid / kL2Pos. Stage 1: d = natural row low digit l,
+            // register = high digit; stage 2: d = k1, register m = spatial
+            // row k1 + 16 m (the engine layout's row 16 k1 + m); the forward
+            // transform mirrors it.
             {
                 const float gain = fp.gain;
                 float frame_loss = 0.f;
+                const int d = tid / kL2Pos, pos = tid % kL2Pos;
 #pragma unroll 1
-                for (int blk = 0; blk < N / 32; ++blk) {
-                    const int t = 32 * blk + lane;
+                for (int blk = 0; blk < N / kL2Pos; ++blk) {
+                    const int t = kL2Pos * blk + pos;
                     float mreg[16];
                     {
-                        const float* mrow = T.meas + (size_t)f * N * N + (size_t)(16 * warp) * N + t;
+                        const float* mrow = T.meas + (size_t)f * N * N + (size_t)(16 * d) * N + t;
 #pragma unroll
                         for (int m = 0; m < 16; ++m) mreg[m] = __ldcs(mrow + (size_t)m * N);
                     }
                     float2 v[16];
 #pragma unroll
                     for (int nc = 0; nc < 16; ++nc) {
-                        const int i = (16 * nc + warp + N / 2) & (N - 1);
+                        const int i = (16 * nc + d + N / 2) & (N - 1);
                         v[nc] = i >= row_lo && i <= row_hi ? G[(size_t)i * N + t] : make_float2(0.f, 0.f);
                     }
                     dft_reg<16, true>(v);
 #pragma unroll
                     for (int k1 = 0; k1 < 16; ++k1)
-                        S[(k1 * 16 + warp) * 32 + lane] = twiddle_smem<true>(v[k1], tw, warp * k1);
+                        S[(k1 * 16 + d) * kL2Pos + pos] = twiddle_smem<true>(v[k1], tw, d * k1);
                     __syncthreads();
 #pragma unroll
-                    for (int l = 0; l < 16; ++l) v[l] = S[(warp * 16 + l) * 32 + lane];
+                    for (int l = 0; l < 16; ++l) v[l] = S[(d * 16 + l) * kL2Pos + pos];
                     dft_reg<16, true>(v);
                     // Amplitude projection: the forward transform takes psi' - psi
                     // (masked pixels contribute zero).
@@ -285,8 +292,8 @@ FPM_DEVICE void engine_l2_tile(const EngineParams& P, const int tile) {
                         const float s_amp = intrinsic * r;
                         if (a >= 0.f) {
                             if constexpr (LOSS == 0) {
-                                const float d = s_amp - a;
-                                frame_loss = fmaf(d, d, frame_loss);
+                                const float dd = s_amp - a;
+                                frame_loss = fmaf(dd, dd, frame_loss);
                             } else {
                                 frame_loss += point_loss<LOSS>(gain * intrinsic, gain * a * a, P.loss);
                             }
@@ -298,14 +305,14 @@ FPM_DEVICE void engine_l2_tile(const EngineParams& P, const int tile) {
                     dft_reg<16, false>(v);
 #pragma unroll
                     for (int b = 0; b < 16; ++b)
-                        S2[(b * 16 + warp) * 32 + lane] = twiddle_smem<false>(v[b], tw, warp * b);
+                        S2[(b * 16 + d) * kL2Pos + pos] = twiddle_smem<false>(v[b], tw, d * b);
                     __syncthreads();
 #pragma unroll
-                    for (int k1 = 0; k1 < 16; ++k1) v[k1] = S2[(warp * 16 + k1) * 32 + lane];
+                    for (int k1 = 0; k1 < 16; ++k1) v[k1] = S2[(d * 16 + k1) * kL2Pos + pos];
                     dft_reg<16, false>(v);
 #pragma unroll
                     for (int j1 = 0; j1 < 16; ++j1) {
-                        const int i = (16 * j1 + warp + N / 2) & (N - 1);
+                        const int i = (16 * j1 + d + N / 2) & (N - 1);
                         if (i >= row_lo && i <= row_hi) G[(size_t)i * N + t] = v[j1];
                     }
                 }
@@ -457,7 +464,7 @@ FPM_DEVICE void engine_l2_tile(const EngineParams& P, const int tile) {
 }
 
 template <int ALG, int LOSS, bool UNIT>
-__global__ void __launch_bounds__(kL2Threads, 1) engine_l2_kernel(const EngineParams P) {
+__global__ void __launch_bounds__(kL2Threads, kL2PerSm) engine_l2_kernel(const EngineParams P) {
     for (int tile = blockIdx.x; tile < P.tile_count; tile += gridDim.x) engine_l2_tile<ALG, LOSS, UNIT>(P, tile);
 }
 
