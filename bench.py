@@ -70,11 +70,14 @@ SIZES = (32, 64, 128, 256)
 LED_SIDE = 15
 PHOTONS = 1e4
 L2_BYTES = 129 * 1024 * 1024
-# Measured DRAM bytes (read + write) of engine_kernel per tile and mPIE
+# Measured DRAM bytes (read + write) of the frame engine per tile and mPIE
 # iteration, by tile size: ncu dram__bytes_read.sum + dram__bytes_write.sum
-# of the four engine launches of a 64-tile run (profiles/engine_dram_traffic_64tiles.txt).
+# of the cluster-engine launches of a 64-tile run
+# (profiles/engine_dram_traffic_64tiles.txt) and, for 256-point tiles, of
+# the single-CTA engine that the 1024-tile run uses for them
+# (profiles/engine_l2_256_full_13tiles.txt: 3.197 GB for 13 tile-iterations).
 # roofline.traffic scales them by this run's tile counts and iterations.
-DRAM_BYTES_PER_TILE_ITERATION = {256: 244.23e6, 128: 23.32e6, 64: 0.827e6, 32: 0.040e6}
+DRAM_BYTES_PER_TILE_ITERATION = {256: 245.9e6, 128: 23.32e6, 64: 0.827e6, 32: 0.040e6}
 
 
 def parse():
