@@ -57,6 +57,10 @@ cudaError_t launch_permute_u8(int n, const uint8_t* src, uint8_t* dst, long long
     FPM_DISPATCH(permute_u8(src, dst, frames, s))
 }
 
+cudaError_t launch_unpermute_f32_to_f64(int n, const float* src, double* dst, long long frames, cudaStream_t s) {
+    FPM_DISPATCH(unpermute_f64(src, dst, frames, s))
+}
+
 cudaError_t launch_permute_amplitude(int n, const double* src, const uint8_t* masks, const double* gains, float* dst,
                                      long long frames, cudaStream_t s) {
     FPM_DISPATCH(permute_amplitude(src, masks, gains, dst, frames, s))

@@ -442,6 +442,42 @@ FPM_DEVICE void prefetch_step(SpectralStep* slot, const SpectralStep* steps, int
                    reinterpret_cast<const char*>(steps + step) + 16 * threadIdx.x, 16);
 }
 
+// Sum of two FP64 values over every thread of the cluster, in a fixed order
+// (warps, then CTAs by rank), identical in every CTA. `dred` holds a value
+// per warp and `tred` this CTA's two totals; the closing barrier keeps them
+// until every CTA has read them.
+template <class K>
+FPM_DEVICE void cluster_sum2(double& a, double& b, double* dred, double* tred) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double part[2] = {a, b};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const double w = warp_sum(part[q]);
+        __syncthreads();
+        if (lane == 0) dred[warp] = w;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int ww = 0; ww < K::WARPS; ++ww) t += dred[ww];
+            tred[q] = t;
+        }
+    }
+    cluster_barrier<K>();
+    if constexpr (K::C == 1) {
+        a = tred[0];
+        b = tred[1];
+    } else {
+        cg::cluster_group cluster = cg::this_cluster();
+        a = b = 0.0;
+        for (int r = 0; r < K::C; ++r) {
+            const double* pr = cluster.map_shared_rank(tred, r);
+            a += pr[0];
+            b += pr[1];
+        }
+    }
+    cluster_barrier<K>();
+}
+
 // One tile's whole launch (iterations [it_begin, it_end)) by one cluster.
 template <int N_, int ALG, int LOSS>
 FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
@@ -457,7 +493,8 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
     // TMA staging of the stencil: 256-point tiles of the fixed-pupil
     // families (the pupil-recovering ones are at their register limit),
     // whose staging slab starts 128-byte aligned.
-    constexpr bool tma_capable = N_ == 256 && ALG != kAlgSpectral && ALG != kAlgEpry && ALG != kAlgGradientPupil &&
+    constexpr bool tma_capable = N_ == 256 && ALG != kAlgSpectral && ALG != kAlgEpry && ALG != kAlgEpryCal &&
+                                 ALG != kAlgGlobalCal && ALG != kAlgGradientPupil &&
                                  (K::FIELD * 8) % 128 == 0;
     constexpr unsigned kStageBytes = (unsigned)(K::STAGE * sizeof(float2));
     __shared__ __align__(8) unsigned long long s_tma_bar;
@@ -499,7 +536,9 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
     constexpr bool projection = !gradient;
     // Families whose pupil evolves during the launch: per-frame maxima, all rows.
     constexpr bool gd_pupil = ALG == kAlgGradientPupil;
-    constexpr bool epry = ALG == kAlgEpry;
+    constexpr bool epry = ALG == kAlgEpry || ALG == kAlgEpryCal;
+    // EPRY with frame-gain / background recovery (either pupil mode).
+    constexpr bool calibrating = ALG == kAlgEpryCal || ALG == kAlgGlobalCal;
     // Narrowband spectral AP: per-mode channel pupils and stored objects.
     constexpr bool spectral = ALG == kAlgSpectral;
     // Rows of psi that can be non-zero (all rows when the pupil evolves or
@@ -837,7 +876,7 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
             {
                 const float* brow =
                     T.background ? T.background + (size_t)f * T.background_stride + mbase : nullptr;
-                const float gain = fp.gain, inv_gain = 1.0f / fp.gain;
+                float gain = fp.gain, inv_gain = 1.0f / fp.gain;
                 const int pq = phys<K>(q4);
                 float2 v[16];
                 if constexpr (R == 32) column_inverse_split<K>(fld, pq, h4, tw, v);
@@ -854,6 +893,71 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
                         mbits = 0u;
 #pragma unroll
                         for (int k = 0; k < 16; ++k) mbits |= (T.masks[off + (size_t)k * mstride] != 0 ? 1u : 0u) << k;
+                    }
+                }
+                // EPRY frame-gain and background recovery (update_gain and
+                // update_background, src/algorithms/common.rs:390-489): the
+                // frame's gain moves toward sum p (y - b)+ / sum p^2 and its
+                // background by the mean residual y - g p - b, from the
+                // prediction p = |psi|^2 before the projection; both are
+                // summed over the cluster in FP64 and the projection below
+                // uses the new values. The amplitude form holds
+                // a = sqrt(max(y / g0, 0)); its intensities are g0 a^2.
+                bool recovered = false;
+                float bgv[16];
+                if constexpr (calibrating) {
+                    {
+                        recovered = true;
+                        if (T.amplitude) {
+                            mbits = 0u;
+#pragma unroll
+                            for (int k = 0; k < 16; ++k) {
+                                const float a = mreg[k];
+                                if (a >= 0.f) mbits |= 1u << k;
+                                mreg[k] = a >= 0.f ? fp.gain * (a * a) : 0.f;
+                            }
+                        }
+                        const TileRecovery rs = P.recovery[tile];
+                        float* const bstate = rs.bg_state ? rs.bg_state + (size_t)f * N * N + mbase : nullptr;
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) bgv[k] = bstate ? bstate[k * mstride] : 0.f;
+                        double g = rs.gain_state[f];
+                        if (P.recover_gains) {
+                            double num = 0.0, den = 0.0;
+#pragma unroll
+                            for (int k = 0; k < 16; ++k) {
+                                if (((mbits >> k) & 1u) == 0u) continue;
+                                const double pk = (double)cnorm2(v[k]);
+                                num += pk * fmax((double)mreg[k] - (double)bgv[k], 0.0);
+                                den += pk * pk;
+                            }
+                            cluster_sum2<K>(num, den, dred, tred);
+                            if (den > P.eps) {
+                                const double est = fmin(fmax(num / den, P.gain_min), P.gain_max);
+                                g = fmin(fmax((1.0 - P.gain_step) * g + P.gain_step * est, P.gain_min), P.gain_max);
+                                if (c == 0 && tid == 0) rs.gain_state[f] = g;
+                            }
+                        }
+                        if (P.recover_background) {
+                            double res = 0.0, cnt = 0.0;
+#pragma unroll
+                            for (int k = 0; k < 16; ++k) {
+                                if (((mbits >> k) & 1u) == 0u) continue;
+                                res += (double)mreg[k] - g * (double)cnorm2(v[k]) - (double)bgv[k];
+                                cnt += 1.0;
+                            }
+                            cluster_sum2<K>(res, cnt, dred, tred);
+                            if (cnt > 0.0) {
+                                const double corr = P.background_step * res / cnt;
+#pragma unroll
+                                for (int k = 0; k < 16; ++k) {
+                                    bgv[k] = (float)fmin(fmax((double)bgv[k] + corr, P.background_min), P.background_max);
+                                    bstate[k * mstride] = bgv[k];
+                                }
+                            }
+                        }
+                        gain = (float)g;
+                        inv_gain = 1.0f / gain;
                     }
                 }
                 if constexpr (truncating) {
@@ -885,7 +989,7 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
                 float frame_loss = 0.f;
                 if (stats) {
                     // Forward-only statistics step: nothing to write back.
-                } else if (T.amplitude) {
+                } else if (T.amplitude && !recovered) {
                     // a = sqrt(max(I / g, 0)), -1 where masked; with no
                     // background, I = g a^2 exactly as the reference uses it.
 #pragma unroll
@@ -931,7 +1035,7 @@ FPM_DEVICE void engine_tile(const EngineParams& P, const int tile) {
                     for (int k = 0; k < 16; ++k) {
                         const float meas = mreg[k];
                     const bool masked = ((mbits >> k) & 1u) == 0u;
-                    const float bg = brow ? __ldg(brow + k * mstride) : 0.f;
+                    const float bg = recovered ? bgv[k] : brow ? __ldg(brow + k * mstride) : 0.f;
                     const float intrinsic = cnorm2(v[k]);
                     const float target = fmaxf((meas - bg) * inv_gain, 0.f);
                     if constexpr (projection) {
@@ -1418,6 +1522,20 @@ __global__ void __launch_bounds__(N_) permute_amplitude_kernel(const double* __r
     }
 }
 
+// Engine layout -> natural order, widened to FP64: the inverse of
+// permute_f64_kernel (engine position t of a row holds natural column
+// layout_column(t)).
+template <int N_>
+__global__ void __launch_bounds__(N_) unpermute_f64_kernel(const float* __restrict__ src, double* __restrict__ dst,
+                                                           long long frames) {
+    using K = Cfg<N_>;
+    for (long long r = blockIdx.x; r < frames * K::N; r += gridDim.x) {
+        const long long f = r / K::N;
+        const int y = (int)(r % K::N), t = threadIdx.x;
+        dst[r * K::N + layout_column<K>(t)] = (double)src[layout_row_base<K>(f, y) + t];
+    }
+}
+
 template <int N_>
 __global__ void __launch_bounds__(N_) permute_u8_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
                                                         long long frames) {
@@ -1565,7 +1683,9 @@ cudaError_t launch_engine_alg(const EngineParams& p, int tiles, cudaStream_t s) 
                                                                           cudaStream_t);               \
     SPEC template cudaError_t launch_engine_alg<N, kAlgLocalAdaptive>(const EngineParams&, int, cudaStream_t); \
     SPEC template cudaError_t launch_engine_alg<N, kAlgGradientPupil>(const EngineParams&, int, cudaStream_t); \
-    SPEC template cudaError_t launch_engine_alg<N, kAlgSpectral>(const EngineParams&, int, cudaStream_t);
+    SPEC template cudaError_t launch_engine_alg<N, kAlgSpectral>(const EngineParams&, int, cudaStream_t);    \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgGlobalCal>(const EngineParams&, int, cudaStream_t);   \
+    SPEC template cudaError_t launch_engine_alg<N, kAlgEpryCal>(const EngineParams&, int, cudaStream_t);
 
 template <int N_>
 struct EngineEntry {
@@ -1580,6 +1700,8 @@ struct EngineEntry {
             case kAlgRpie: return engine_alg<kAlgRpie>(p, tiles, s);
             case kAlgGlobal: return engine_alg<kAlgGlobal>(p, tiles, s);
             case kAlgEpry: return engine_alg<kAlgEpry>(p, tiles, s);
+            case kAlgGlobalCal: return engine_alg<kAlgGlobalCal>(p, tiles, s);
+            case kAlgEpryCal: return engine_alg<kAlgEpryCal>(p, tiles, s);
             case kAlgGradient: return engine_alg<kAlgGradient>(p, tiles, s);
             case kAlgGradientTruncated: return engine_alg<kAlgGradientTruncated>(p, tiles, s);
             case kAlgLocalAdaptive: return engine_alg<kAlgLocalAdaptive>(p, tiles, s);
@@ -1627,6 +1749,12 @@ struct EngineEntry {
     static cudaError_t permute_f64(const double* src, float* dst, long long frames, cudaStream_t s) {
         if (frames <= 0) return cudaSuccess;
         permute_f64_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, dst, frames);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t unpermute_f64(const float* src, double* dst, long long frames, cudaStream_t s) {
+        if (frames <= 0) return cudaSuccess;
+        unpermute_f64_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, dst, frames);
         return cudaGetLastError();
     }
 

@@ -102,6 +102,14 @@ struct TileDesc {
     float* prediction;          // N*N weighted intensity sum, engine layout
 };
 
+// EPRY frame-gain and background recovery state of one tile: gains
+// [frames] and backgrounds [frames][N * N] (engine layout). Kept apart from
+// TileDesc, which every CTA holds in shared memory.
+struct TileRecovery {
+    double* gain_state;
+    float* bg_state;
+};
+
 // Frame-engine kernel families, fixed at compile time so each instantiation
 // carries only its own update code: AP (local |P|^2 denominator), FPIE/mPIE
 // (rPIE blend), EPRY without and with pupil recovery (global max |P|^2), and
@@ -116,6 +124,8 @@ enum EngineAlg {
     kAlgLocalAdaptive = 6,      // AP with the adaptive step controller
     kAlgGradientPupil = 7,      // gradient descent with pupil recovery
     kAlgSpectral = 8,           // narrowband spectral AP over multi-mode exposures
+    kAlgGlobalCal = 9,          // EPRY (fixed pupil) with frame-gain / background recovery
+    kAlgEpryCal = 10,           // EPRY with pupil and frame-gain / background recovery
 };
 
 struct EngineParams {
@@ -141,6 +151,11 @@ struct EngineParams {
     // whether every tile has a unit pupil (TileDesc::pupil_span set).
     float2* field_scratch;
     int unit_pupils;
+    // EPRY frame-gain and background recovery (src/algorithms/common.rs:390-489):
+    // per-tile state (indexed like tiles), or null.
+    const TileRecovery* recovery;
+    int recover_gains, recover_background;
+    double gain_step, gain_min, gain_max, background_step, background_min, background_max;
 };
 
 // Forward-model (simulate) parameters: one model, cluster per frame.
@@ -176,6 +191,8 @@ cudaError_t engine_l2_max_active_ctas(int n, int* count);
 // Permutes natural-order frames [frames][N][N] into the engine layout.
 cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long long frames, cudaStream_t s);
 cudaError_t launch_permute_u8(int n, const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s);
+// Engine layout -> natural-order frames [frames][N][N], widened to FP64.
+cudaError_t launch_unpermute_f32_to_f64(int n, const float* src, double* dst, long long frames, cudaStream_t s);
 // Amplitude form: dst = sqrt(max(src / gain[f], 0)) in FP64, rounded once to
 // float, or -1 where masks (natural order, may be null) is zero.
 cudaError_t launch_permute_amplitude(int n, const double* src, const uint8_t* masks, const double* gains, float* dst,

@@ -224,7 +224,8 @@ struct fpm_problem {
     bool row_exact = true, col_exact = true;
     double weight_sum = 0.0;
     // resident device data
-    DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model, pupil_span;
+    DeviceBuffer meas, masks, background, frame_params, support_d, pupil_ref, pupil_model, pupil_span, gains_d;
+    std::vector<double> state_gains;  // host source of gains_d: the model gains (1 where not positive)
     // run state
     DeviceBuffer object, pupil_state, velocity, anchor, partials, counter, status, scratch64, order, gradient,
         object_err, gradient_err,
@@ -232,6 +233,10 @@ struct fpm_problem {
     // GD illumination recovery: the run's frame constants, crop starts and
     // offsets, corrections and per-CTA gradient partials.
     DeviceBuffer ill_params, ill_start, ill_offset, ill_correction, ill_partials;
+    // EPRY frame-gain and background recovery: state gains [frames], state
+    // backgrounds [frames][N * N] (engine layout), and their natural-order
+    // FP64 copy for downloads.
+    DeviceBuffer gain_state, bg_state, bg_natural;
     fpm_job* busy = nullptr;  // the submitted job that owns the problem until it finishes
     fpm_plan* plan = nullptr;  // the captured run plan that holds the problem until destroyed
 };
@@ -691,7 +696,7 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     const int N = p->n, F = p->frames;
     const size_t n2 = (size_t)N * N;
     for (DeviceBuffer* b : {&p->meas, &p->masks, &p->background, &p->frame_params, &p->support_d, &p->pupil_ref,
-                            &p->pupil_model, &p->pupil_span})
+                            &p->pupil_model, &p->pupil_span, &p->gains_d})
         b->bind(ctx->pool, s);
     DeviceBuffer staging, mask_staging, gain_staging;
     for (DeviceBuffer* b : {&staging, &mask_staging, &gain_staging}) b->bind(ctx->pool, s);
@@ -733,6 +738,10 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
                                  cudaMemcpyHostToDevice, s));
         FPM_CUDA(fpm::launch_permute_f64_to_f32(N, bg_staging.as<double>(), p->background.as<float>(), bg_frames, s));
     }
+    p->state_gains.resize(F);
+    for (int f = 0; f < F; ++f) p->state_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
+    FPM_TRY(p->gains_d.ensure(F * sizeof(double)));
+    FPM_CUDA(cudaMemcpyAsync(p->gains_d.ptr, p->state_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
     FPM_TRY(p->frame_params.ensure(sizeof(fpm::FrameParam) * F));
     FPM_CUDA(cudaMemcpyAsync(p->frame_params.ptr, p->params.data(), sizeof(fpm::FrameParam) * F, cudaMemcpyHostToDevice, s));
     FPM_TRY(p->support_d.ensure(n2));
@@ -848,9 +857,21 @@ Status validate_params(const fpm_algorithm_params* a) {
     if (a->algorithm == FPM_ALG_EPRY) {
         if (!std::isfinite(a->pupil_step) || a->pupil_step < 0.0)
             return Status::make(FPM_ERR_INVALID_PARAMETER, "pupil_step must be finite and non-negative");
-        if (a->recover_frame_gains || a->recover_background)
-            return Status::make(FPM_ERR_UNSUPPORTED,
-                                "EPRY frame-gain and background recovery are not implemented on the GB300 device path");
+        // Epry::validate (src/algorithms/epry.rs:206-236), for the recoveries requested.
+        if (a->recover_frame_gains) {
+            if (!std::isfinite(a->gain_step) || a->gain_step < 0.0 || a->gain_step > 1.0)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "gain_step must be finite and between zero and one");
+            if (!std::isfinite(a->gain_min) || !std::isfinite(a->gain_max) || a->gain_min <= 0.0 ||
+                a->gain_max <= a->gain_min)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "gain_bounds must be finite, positive, and strictly increasing");
+        }
+        if (a->recover_background) {
+            if (!std::isfinite(a->background_step) || a->background_step < 0.0 || a->background_step > 1.0)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "background_step must be finite and between zero and one");
+            if (!std::isfinite(a->background_min) || !std::isfinite(a->background_max) ||
+                a->background_max <= a->background_min)
+                return Status::make(FPM_ERR_INVALID_PARAMETER, "background_bounds must be finite and strictly increasing");
+        }
     }
     if (a->algorithm == FPM_ALG_ADAPTIVE_AP) {
         // AdaptiveAlternatingProjection::validate (src/algorithms/adaptive_alternating_projection.rs:350-403).
@@ -995,11 +1016,13 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
     return {&p->object,     &p->pupil_state,   &p->partials,       &p->counter,    &p->status,
             &p->scratch64,  &p->velocity,      &p->anchor,         &p->order,      &p->gradient,
             &p->pupil_gradient, &p->tv_scratch, &p->pupil_scratch, &p->ill_params, &p->ill_start,
-            &p->ill_offset, &p->ill_correction, &p->ill_partials, &p->object_err, &p->gradient_err};
+            &p->ill_offset, &p->ill_correction, &p->ill_partials, &p->object_err, &p->gradient_err,
+            &p->gain_state, &p->bg_state, &p->bg_natural};
 }
 
 struct BucketRun {
     DeviceBuffer field_scratch;  // single-CTA engine: per-CTA field scratch
+    DeviceBuffer recovery;       // EPRY gain / background recovery: per-tile state pointers
     DeviceBuffer tmaps;  // per tile: the object spectrum's tensor map for TMA stencil staging
     DeviceBuffer tiles, init, gauge, scratch_ptrs, object_ptrs, anchor_ptrs, velocity_ptrs, avg, init_partial,
         tv_ptrs, tv_objects, tv_table, smooth_table, ill_tiles, ill_tasks, ill_fields, ill_valid, ill_ptrs;
@@ -1058,7 +1081,10 @@ int engine_family(const fpm_algorithm_params* a) {
         case FPM_ALG_ADAPTIVE_AP: return fpm::kAlgLocalAdaptive;
         case FPM_ALG_FPIE:
         case FPM_ALG_MPIE: return fpm::kAlgRpie;
-        case FPM_ALG_EPRY: return a->recover_pupil ? fpm::kAlgEpry : fpm::kAlgGlobal;
+        case FPM_ALG_EPRY:
+            if (a->recover_frame_gains || a->recover_background)
+                return a->recover_pupil ? fpm::kAlgEpryCal : fpm::kAlgGlobalCal;
+            return a->recover_pupil ? fpm::kAlgEpry : fpm::kAlgGlobal;
         default:
             return a->recover_pupil       ? fpm::kAlgGradientPupil
                    : a->poisson_truncation ? fpm::kAlgGradientTruncated
@@ -1084,6 +1110,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     const bool smoothing = gd_pupil && a->pupil_smoothing_weight > 0.0;
     // Illumination recovery: a finite-difference gradient launch before and a
     // correction update after each GD batch's engine launch.
+    // EPRY frame-gain / background recovery: state gains and backgrounds on the device.
+    const bool recover_gb = epry && (a->recover_frame_gains || a->recover_background);
     const bool illum = a->algorithm == FPM_ALG_GD && a->recover_illumination;
     const bool regularised = tv || smoothing || illum;
     const int iters = a->iterations;
@@ -1098,6 +1126,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         FPM_TRY(br.tmaps.ensure(sizeof(CUtensorMap) * (size_t)count));
     }
     std::vector<fpm::InitTile> inits(count);
+    std::vector<fpm::TileRecovery> recovery(count);
     std::vector<fpm::GaugeTile> gauges(count);
     std::vector<fpm::IlluminationTile> ill_tiles(illum ? count : 0);
     std::vector<double2*> scratch(count);
@@ -1133,6 +1162,27 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(p->anchor.ensure(sizeof(float2) * (size_t)M * ms));
         }
         if (br.launch) FPM_CUDA(cudaMemsetAsync(p->status.ptr, 0, sizeof(int), s));
+        if (recover_gb) {
+            // State gains start at the model's; state backgrounds at the
+            // model's (one shared image or one per frame) or zero.
+            const int F = p->frames;
+            const size_t n2f = (size_t)N * N;
+            FPM_TRY(p->gain_state.ensure(sizeof(double) * F));
+            FPM_TRY(p->bg_state.ensure(sizeof(float) * n2f * F));
+            if (br.launch) {
+                FPM_CUDA(cudaMemcpyAsync(p->gain_state.ptr, p->gains_d.ptr, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
+                if (!p->has_background) {
+                    FPM_CUDA(cudaMemsetAsync(p->bg_state.ptr, 0, sizeof(float) * n2f * F, s));
+                } else if (p->background_stride == 0) {
+                    for (int f = 0; f < F; ++f)
+                        FPM_CUDA(cudaMemcpyAsync(p->bg_state.as<float>() + (size_t)f * n2f, p->background.ptr,
+                                                 sizeof(float) * n2f, cudaMemcpyDeviceToDevice, s));
+                } else {
+                    FPM_CUDA(cudaMemcpyAsync(p->bg_state.ptr, p->background.ptr, sizeof(float) * n2f * F,
+                                             cudaMemcpyDeviceToDevice, s));
+                }
+            }
+        }
         p->it0 = it0;
         p->resume_objectives.clear();
         if (resumed) {
@@ -1261,6 +1311,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         T.object_err = compensated && !gd_batched ? p->object_err.as<float2>() : nullptr;
         T.gradient_err = compensated && gd_batched ? p->gradient_err.as<float2>() : nullptr;
         T.pupil_gradient = gd_pupil ? p->pupil_gradient.as<float2>() : nullptr;
+        recovery[t] = {recover_gb ? p->gain_state.as<double>() : nullptr, recover_gb ? p->bg_state.as<float>() : nullptr};
         T.partials = p->partials.as<double>();
         T.counter = p->counter.as<int>();
         T.status = p->status.as<int>();
@@ -1330,7 +1381,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     for (DeviceBuffer* buf : {&br.tiles, &br.init, &br.gauge, &br.scratch_ptrs, &br.object_ptrs, &br.anchor_ptrs,
                               &br.velocity_ptrs, &br.avg, &br.init_partial, &br.tv_ptrs, &br.tv_objects,
                               &br.tv_table, &br.smooth_table, &br.ill_tiles, &br.ill_tasks, &br.ill_fields,
-                              &br.ill_valid, &br.ill_ptrs})
+                              &br.ill_valid, &br.ill_ptrs, &br.recovery})
         buf->bind(ctx->pool, s);
     if (!br.first) FPM_CUDA(cudaEventCreate(&br.first));
     if (!br.last) FPM_CUDA(cudaEventCreate(&br.last));
@@ -1392,6 +1443,18 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.minimum_step = a->minimum_object_step;
     ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
     ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
+    if (recover_gb) {
+        if (br.prepare) FPM_TRY(upload_array(br.recovery, recovery, s));
+        ep.recovery = br.recovery.as<fpm::TileRecovery>();
+    }
+    ep.recover_gains = recover_gb && a->recover_frame_gains ? 1 : 0;
+    ep.recover_background = recover_gb && a->recover_background ? 1 : 0;
+    ep.gain_step = a->gain_step;
+    ep.gain_min = a->gain_min;
+    ep.gain_max = a->gain_max;
+    ep.background_step = a->background_step;
+    ep.background_min = a->background_min;
+    ep.background_max = a->background_max;
     // The single-CTA engine takes 256-point tiles of the fixed-pupil
     // projection families with amplitude-form measurements and plain
     // accumulation; other runs use the cluster engine.
@@ -1399,7 +1462,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     for (fpm_problem* p : b.problems) all_amplitude = all_amplitude && p->amplitude;
     bool single = false;
     int resident = 0;
-    FPM_TRY(single_cta_engine(ctx, N, ep.alg, all_amplitude && !compensated && !regularised, count, &single, &resident));
+    FPM_TRY(single_cta_engine(ctx, N, ep.alg, all_amplitude && !compensated && !regularised && !recover_gb, count,
+                              &single, &resident));
     int units = engine_clusters(ctx, N, count);
     if (single) {
         const int want = ctx->engine_ctas[engine_grid_slot(N)];
@@ -1593,6 +1657,17 @@ Status queue_collect(fpm_problem* p, const fpm_algorithm_params* a, fpm_result_d
     if (r->illumination_corrections && a->algorithm == FPM_ALG_GD && a->recover_illumination)
         FPM_CUDA(cudaMemcpyAsync(r->illumination_corrections, p->ill_correction.ptr, sizeof(double) * 2 * p->frames,
                                  cudaMemcpyDeviceToHost, s));
+    if (a->algorithm == FPM_ALG_EPRY && (a->recover_frame_gains || a->recover_background)) {
+        if (r->frame_gains)
+            FPM_CUDA(cudaMemcpyAsync(r->frame_gains, p->gain_state.ptr, sizeof(double) * p->frames, cudaMemcpyDeviceToHost, s));
+        if (r->background) {
+            const size_t count = (size_t)N * N * p->frames;
+            p->bg_natural.bind(p->ctx->pool, s);
+            FPM_TRY(p->bg_natural.ensure(sizeof(double) * count));
+            FPM_CUDA(fpm::launch_unpermute_f32_to_f64(N, p->bg_state.as<float>(), p->bg_natural.as<double>(), p->frames, s));
+            FPM_CUDA(cudaMemcpyAsync(r->background, p->bg_natural.ptr, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
+        }
+    }
     return Status::ok();
 }
 
@@ -1727,6 +1802,9 @@ Status validate_resume(int count, fpm_problem* const* problems, const fpm_algori
     const bool mpie = a->algorithm == FPM_ALG_MPIE;
     if (resume && a->algorithm == FPM_ALG_ADAPTIVE_AP)
         return Status::make(FPM_ERR_UNSUPPORTED, "adaptive alternating projection does not resume on the GB300 device path");
+    if (resume && a->algorithm == FPM_ALG_EPRY && (a->recover_frame_gains || a->recover_background))
+        return Status::make(FPM_ERR_UNSUPPORTED,
+                            "EPRY runs that recover frame gains or backgrounds do not resume on the GB300 device path");
     for (int i = 0; i < count && resume; ++i) {
         const fpm_state_desc& r = resume[i];
         const fpm_problem* p = problems[i];
@@ -1862,8 +1940,10 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
             bool single = false;
             int resident = 0;
             const bool amplitude = mds[g.second[0]].background == nullptr;
-            FPM_TRY(single_cta_engine(ctx, g.first.first, engine_family(a), amplitude && !a->compensated_accumulation,
-                                      (int)g.second.size(), &single, &resident));
+            const bool recovery = a->algorithm == FPM_ALG_EPRY && (a->recover_frame_gains || a->recover_background);
+            FPM_TRY(single_cta_engine(ctx, g.first.first, engine_family(a),
+                                      amplitude && !a->compensated_accumulation && !recovery, (int)g.second.size(),
+                                      &single, &resident));
             if (single) {
                 const size_t parts = std::max<size_t>(1, g.second.size() / std::max(1, (2 * resident + 2) / 3));
                 min_tiles = (g.second.size() + parts - 1) / parts;

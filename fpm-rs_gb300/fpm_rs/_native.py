@@ -84,6 +84,8 @@ class AlgorithmParams(C.Structure):
         ("recover_illumination", C.c_int32), ("illumination_step", C.c_double),
         ("illumination_finite_difference", C.c_double), ("maximum_illumination_correction", C.c_double),
         ("compensated_accumulation", C.c_int32),
+        ("gain_step", C.c_double), ("gain_min", C.c_double), ("gain_max", C.c_double),
+        ("background_step", C.c_double), ("background_min", C.c_double), ("background_max", C.c_double),
     ]
 
 
@@ -133,6 +135,7 @@ class ResultDesc(C.Structure):
         ("pupil", C.POINTER(C.c_double)), ("objectives", C.POINTER(C.c_double)),
         ("completed_iterations", C.c_int32),
         ("illumination_corrections", C.POINTER(C.c_double)),
+        ("frame_gains", C.POINTER(C.c_double)), ("background", C.POINTER(C.c_double)),
     ]
 
 

@@ -306,6 +306,10 @@ class Epry(_Algorithm):
         p.constrain_pupil_support = int(bool(self.constrain_pupil_support))
         p.recover_frame_gains = int(bool(self.recover_frame_gains))
         p.recover_background = int(bool(self.recover_background))
+        p.gain_step = float(self.gain_step)
+        p.gain_min, p.gain_max = (float(v) for v in self.gain_bounds)
+        p.background_step = float(self.background_step)
+        p.background_min, p.background_max = (float(v) for v in self.background_bounds)
         return p
 
 
@@ -387,16 +391,34 @@ def _result_arrays(problem, params, desc) -> dict:
     """Host arrays of one problem's results, bound into its ResultDesc."""
     mh, mw = problem.reconstruction_shape
     h, w = problem.image_shape
+    frames = problem.model.source_count
+    # EPRY frame-gain / background recovery returns the recovered state.
+    recovering = params.algorithm == _ALG["epry"] and (params.recover_frame_gains or params.recover_background)
     a = dict(object=np.zeros((mh, mw), np.complex128), object_spectrum=np.zeros((mh, mw), np.complex128),
              pupil=np.zeros((h, w), np.complex128), objectives=np.zeros(max(params.iterations, 1)),
-             illumination=np.zeros((problem.model.source_count, 2)) if params.recover_illumination else None)
+             illumination=np.zeros((frames, 2)) if params.recover_illumination else None,
+             gains=np.zeros(frames) if recovering else None,
+             background=np.zeros((frames, h, w)) if recovering else None)
     desc.object = N.ptr(a["object"], C.c_double)
     desc.object_spectrum = N.ptr(a["object_spectrum"], C.c_double)
     desc.pupil = N.ptr(a["pupil"], C.c_double)
     desc.objectives = N.ptr(a["objectives"], C.c_double)
     if a["illumination"] is not None:
         desc.illumination_corrections = N.ptr(a["illumination"], C.c_double)
+    if a["gains"] is not None:
+        desc.frame_gains = N.ptr(a["gains"], C.c_double)
+        desc.background = N.ptr(a["background"], C.c_double)
     return a
+
+
+def _recovered_gains(problem, arrays):
+    """Frame gains of a result: the recovered ones, else the model's."""
+    return arrays["gains"] if arrays.get("gains") is not None else problem.model.frame_gains
+
+
+def _recovered_background(problem, arrays):
+    """Background of a result: the recovered [frames, h, w] stack, else the model's."""
+    return arrays["background"] if arrays.get("background") is not None else problem.model._background
 
 
 def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=None, schedule="sequential",
@@ -448,12 +470,11 @@ def run_batch(algorithm: _Algorithm, problems, *, callbacks=None, resume_from=No
     out = []
     for p, a in zip(problems, arrays):
         trace = [(it + 1, float(a["objectives"][it]), elapsed) for it in range(params.iterations)]
-        gains = p.model.frame_gains
         result = ReconstructionResult(
             object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
             pupil_support=p.model.pupil_support, trace=trace,
             runtime=RuntimeInfo(elapsed, params.iterations, False, algorithm._name),
-            recovered_frame_gains=gains, recovered_background=p.model._background,
+            recovered_frame_gains=_recovered_gains(p, a), recovered_background=_recovered_background(p, a),
             calibrated_illumination=a["illumination"])
         if p.name is not None:
             result.metadata["problem_name"] = p.name
@@ -528,7 +549,7 @@ class Job:
                 object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
                 pupil_support=p.model.pupil_support, trace=trace,
                 runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
-                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                recovered_frame_gains=_recovered_gains(p, a), recovered_background=_recovered_background(p, a),
                 calibrated_illumination=a["illumination"])
             if p.name is not None:
                 result.metadata["problem_name"] = p.name
@@ -602,7 +623,7 @@ class RunPlan:
                 object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
                 pupil_support=p.model.pupil_support, trace=trace,
                 runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
-                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                recovered_frame_gains=_recovered_gains(p, a), recovered_background=_recovered_background(p, a),
                 calibrated_illumination=a["illumination"])
             if p.name is not None:
                 result.metadata["problem_name"] = p.name
@@ -681,7 +702,7 @@ class Request:
                 object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
                 pupil_support=p.model.pupil_support, trace=trace,
                 runtime=RuntimeInfo(elapsed, self._params.iterations, False, self._algorithm._name),
-                recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+                recovered_frame_gains=_recovered_gains(p, a), recovered_background=_recovered_background(p, a),
                 calibrated_illumination=a["illumination"])
             if p.name is not None:
                 self._result.metadata["problem_name"] = p.name
@@ -947,7 +968,7 @@ def _run_resumable(algorithm, problems, callbacks, resume_from, schedule, downlo
             object=a["object"], object_spectrum=a["object_spectrum"], recovered_pupil=a["pupil"],
             pupil_support=p.model.pupil_support, trace=list(records),
             runtime=RuntimeInfo(elapsed, end, stopped, algorithm._name),
-            recovered_frame_gains=p.model.frame_gains, recovered_background=p.model._background,
+            recovered_frame_gains=_recovered_gains(p, a), recovered_background=_recovered_background(p, a),
             calibrated_illumination=a["illumination"])
         if p.name is not None:
             result.metadata["problem_name"] = p.name

@@ -131,8 +131,8 @@ typedef struct {
     int32_t recover_pupil;       /* EPRY */
     int32_t constrain_pupil_support;
     double pupil_step;
-    int32_t recover_frame_gains; /* EPRY extension (unsupported on the device path) */
-    int32_t recover_background;  /* EPRY extension (unsupported on the device path) */
+    int32_t recover_frame_gains; /* EPRY: per-frame gain recovery (gain_step, gain_min, gain_max below) */
+    int32_t recover_background;  /* EPRY: per-frame background recovery (background_step, _min, _max below) */
     int32_t poisson_truncation;  /* GD: nonzero enables the Poisson truncation gate */
     double poisson_truncation_threshold; /* GD: the gate's threshold (finite, positive; Poisson NLL only) */
     /* Adaptive AP (object_step is the initial step): the step is multiplied by
@@ -161,6 +161,19 @@ typedef struct {
      * launch. Costs one more complex64 read and write per stencil cell. 0:
      * plain FP32 accumulation. */
     int32_t compensated_accumulation;
+    /* EPRY frame-gain and background recovery (update_gain and
+     * update_background, src/algorithms/common.rs:390-489; Epry::validate,
+     * src/algorithms/epry.rs:206-236). Each frame's gain moves by gain_step
+     * toward sum p (y - b)+ / sum p^2 (clamped to [gain_min, gain_max]), then
+     * its background by background_step times the mean residual y - g p - b
+     * (clamped to [background_min, background_max]), before the projection
+     * uses them. Steps in [0, 1]; gain bounds finite, positive, increasing;
+     * background bounds finite, increasing. Validated only when the matching
+     * recovery is set; not combined with resumed runs. Amplitude-form
+     * problems (no model background) read their intensities as g0 a^2 from
+     * the stored a = sqrt(max(y / g0, 0)). */
+    double gain_step, gain_min, gain_max;
+    double background_step, background_min, background_max;
 } fpm_algorithm_params;
 
 /* Result buffers; any pointer may be NULL. */
@@ -174,6 +187,11 @@ typedef struct {
      * (ReconstructionResult::calibrated_illumination, src/reconstruction/
      * result.rs:94); written only by runs with recover_illumination. */
     double *illumination_corrections;
+    /* EPRY runs that recover them: [sources] frame gains and
+     * [sources*h*w] backgrounds (ReconstructionResult::recovered_frame_gains
+     * and recovered_background). */
+    double *frame_gains;
+    double *background;
 } fpm_result_desc;
 
 /* ------------------------------------------------------------------ context */

@@ -28,10 +28,11 @@ use std::os::raw::c_char;
     pub minimum_object_step: f64, pub object_tv_weight: f64, pub object_tv_epsilon: f64,
     pub pupil_smoothing_weight: f64, pub recover_illumination: i32, pub illumination_step: f64,
     pub illumination_finite_difference: f64, pub maximum_illumination_correction: f64,
-    pub compensated_accumulation: i32 }
+    pub compensated_accumulation: i32, pub gain_step: f64, pub gain_min: f64, pub gain_max: f64,
+    pub background_step: f64, pub background_min: f64, pub background_max: f64 }
 #[repr(C)] pub struct FpmResultDesc { pub object: *mut f64, pub object_spectrum: *mut f64,
     pub pupil: *mut f64, pub objectives: *mut f64, pub completed_iterations: i32,
-    pub illumination_corrections: *mut f64 }
+    pub illumination_corrections: *mut f64, pub frame_gains: *mut f64, pub background: *mut f64 }
 pub enum FpmContext {}
 pub enum FpmProblem {}
 pub enum FpmPlan {}
