@@ -138,6 +138,19 @@ class Dist:
         self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
         return float(t.item())
 
+    def gather(self, obj) -> list:
+        """Every rank's `obj`, in rank order (host objects; never on the data path)."""
+        if self.world == 1:
+            return [obj]
+        out = [None] * self.world
+        self.td.all_gather_object(out, obj)
+        return out
+
+
+def rank_seed_base(rank: int) -> int:
+    """First tile seed of a rank: ranks draw disjoint tiles of the same size mix."""
+    return 1_000_000 * rank + 10_000
+
 
 def tile_sizes(count: int, seed: int):
     rng = np.random.default_rng(seed)
@@ -300,7 +313,7 @@ def run_ours(args):
                                       "cluster": fpm.tuning.CLUSTER}[args.engine_256])
     models = build_models(fpm)
     sizes = tile_sizes(args.tiles, args.seed)
-    seed_base = 1_000_000 * dist.rank + 10_000
+    seed_base = rank_seed_base(dist.rank)
     t0 = time.perf_counter()
     tiles = generate_tiles(fpm, models, sizes, seed_base)
     # Host inputs as a user holds them: one MeasurementStack and model per tile.
