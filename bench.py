@@ -388,9 +388,17 @@ def run_ours(args):
         p.release()
     problems = None
 
+    e2e_parts = {"call_s": 0.0, "device_span_s": 0.0}
+
     def e2e_step():
         fresh = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
+        c0 = time.perf_counter()
         out = fpm.run_batch(algo, fresh)
+        e2e_parts["call_s"] += time.perf_counter() - c0
+        st = fpm.last_run_stats()
+        e2e_parts["device_span_s"] += st["run_ms"] / 1e3
+        for key in ("host_first_launch_ms", "host_scan_ms", "host_upload_ms", "host_call_ms"):
+            e2e_parts[key] = e2e_parts.get(key, 0.0) + st[key] / 1e3
         for p in fresh:
             p.release()
         return out
@@ -398,6 +406,8 @@ def run_ours(args):
     e2e_step()
     torch.cuda.synchronize()
     dist.barrier()
+    e2e_parts.update(call_s=0.0, device_span_s=0.0, host_first_launch_ms=0.0, host_scan_ms=0.0, host_upload_ms=0.0,
+                     host_call_ms=0.0)
     e0 = time.perf_counter()
     e2e_steps = max(1, args.steps)
     for _ in range(e2e_steps):
@@ -496,7 +506,11 @@ def run_ours(args):
         },
         "cpu_baseline": baseline,
         "e2e": {"value": e2e_value, "unit": "tiles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "seconds_per_step": e2e_s},
+                "seconds_per_step": e2e_s,
+                "run_batch_call_s": round(e2e_parts["call_s"] / e2e_steps, 3),
+                "device_span_s": round(e2e_parts["device_span_s"] / e2e_steps, 3),
+                "host_s": {k.replace("host_", "").replace("_ms", ""): round(e2e_parts[k] / e2e_steps, 3)
+                           for k in ("host_first_launch_ms", "host_scan_ms", "host_upload_ms", "host_call_ms")}},
         "gpu_launches": launches // max(1, args.steps),
         "clocks": clock_info,
         "size_done_ms": bucket_end,

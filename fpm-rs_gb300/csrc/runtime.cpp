@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <chrono>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -179,6 +180,30 @@ struct FftPlan {
 
 }  // namespace
 
+// Pinned staging for host->device copies of caller (pageable) memory: host
+// threads fill one slot while the copy engine drains the others. Pageable
+// copies go through the driver's own staging on the calling thread alone.
+struct PinnedRing {
+    static constexpr int kSlots = 4;
+    static constexpr size_t kSlotBytes = size_t(64) << 20;
+    void* slot[kSlots] = {};
+    // Per slot, the last copy from it on each stream that used it.
+    std::vector<std::pair<cudaStream_t, cudaEvent_t>> pending[kSlots];
+    std::vector<cudaEvent_t> spare;
+    int cur = 0;      // slot being filled
+    size_t used = 0;  // bytes of it handed out (256-byte granules)
+    ~PinnedRing() {
+        for (int k = 0; k < kSlots; ++k) {
+            for (auto& pe : pending[k]) {
+                cudaEventSynchronize(pe.second);
+                cudaEventDestroy(pe.second);
+            }
+            if (slot[k]) cudaFreeHost(slot[k]);
+        }
+        for (cudaEvent_t e : spare) cudaEventDestroy(e);
+    }
+};
+
 struct fpm_context {
     int device = 0;
     static constexpr int kStreams = 4;
@@ -198,6 +223,7 @@ struct fpm_context {
     int engine_shape[4] = {FPM_ENGINE_CLUSTER, FPM_ENGINE_CLUSTER, FPM_ENGINE_CLUSTER, FPM_ENGINE_AUTO};
     // CTAs of a single-CTA engine launch per tile size (0: as many as fit at once).
     int engine_ctas[4] = {0, 0, 0, 0};
+    std::unique_ptr<PinnedRing> pinned;  // created by the first large upload
 };
 
 struct fpm_problem {
@@ -242,6 +268,66 @@ struct fpm_problem {
 };
 
 namespace {
+
+// Host -> device copy of `bytes` of pageable memory on stream s, through
+// the context's pinned ring. A copy straight from pageable memory first
+// waits for all earlier work on its stream, so the host would stall behind
+// the device at every small table; here each copy takes the next free
+// stretch of the current slot, large ones in 64 MB pieces copied by the host
+// worker pool, and a slot is reused once its last copy has left it. The
+// caller holds the context.
+Status upload_pageable(fpm_context* ctx, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return Status::ok();
+    if (!ctx->pinned) {
+        auto ring = std::make_unique<PinnedRing>();
+        for (int k = 0; k < PinnedRing::kSlots; ++k)
+            FPM_CUDA(cudaHostAlloc(&ring->slot[k], PinnedRing::kSlotBytes, cudaHostAllocDefault));
+        ctx->pinned = std::move(ring);
+    }
+    PinnedRing& R = *ctx->pinned;
+    constexpr size_t kPiece = size_t(1) << 20;
+    for (size_t off = 0; off < bytes;) {
+        size_t len = std::min(bytes - off, PinnedRing::kSlotBytes);
+        if (R.used + len > PinnedRing::kSlotBytes) {
+            R.cur = (R.cur + 1) % PinnedRing::kSlots;
+            R.used = 0;
+            // The slot's earlier copies, on whichever streams, have left it.
+            for (auto& pe : R.pending[R.cur]) {
+                FPM_CUDA(cudaEventSynchronize(pe.second));
+                R.spare.push_back(pe.second);
+            }
+            R.pending[R.cur].clear();
+        }
+        char* at = static_cast<char*>(R.slot[R.cur]) + R.used;
+        const char* from = static_cast<const char*>(src) + off;
+        if (len <= kPiece) {
+            std::memcpy(at, from, len);
+        } else {
+            HostPool::get().run((long long)((len + kPiece - 1) / kPiece), [&](long long q) {
+                const size_t o = (size_t)q * kPiece;
+                std::memcpy(at + o, from + o, std::min(kPiece, len - o));
+            });
+        }
+        FPM_CUDA(cudaMemcpyAsync(static_cast<char*>(dst) + off, at, len, cudaMemcpyHostToDevice, s));
+        auto& pend = R.pending[R.cur];
+        auto it = std::find_if(pend.begin(), pend.end(), [&](const auto& pe) { return pe.first == s; });
+        if (it == pend.end()) {
+            cudaEvent_t e = nullptr;
+            if (!R.spare.empty()) {
+                e = R.spare.back();
+                R.spare.pop_back();
+            } else {
+                FPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            }
+            pend.emplace_back(s, e);
+            it = pend.end() - 1;
+        }
+        FPM_CUDA(cudaEventRecord(it->second, s));  // a stream's copies complete in order
+        R.used += (len + 255) & ~size_t(255);
+        off += len;
+    }
+    return Status::ok();
+}
 
 Status set_error(fpm_context* ctx, Status s) {
     if (ctx) ctx->error = s.message;
@@ -707,15 +793,15 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     const size_t total = n2 * F;
     FPM_TRY(staging.ensure(total * sizeof(double)));
     FPM_TRY(p->meas.ensure(total * sizeof(float)));
-    FPM_CUDA(cudaMemcpyAsync(staging.ptr, ms->measurements, total * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, staging.ptr, ms->measurements, total * sizeof(double), s));
     if (p->amplitude) {
         p->upload_gains.resize(F);
         for (int f = 0; f < F; ++f) p->upload_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
         FPM_TRY(gain_staging.ensure(F * sizeof(double)));
-        FPM_CUDA(cudaMemcpyAsync(gain_staging.ptr, p->upload_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
+        FPM_TRY(upload_pageable(ctx, gain_staging.ptr, p->upload_gains.data(), F * sizeof(double), s));
         if (ms->masks) {
             FPM_TRY(mask_staging.ensure(total));
-            FPM_CUDA(cudaMemcpyAsync(mask_staging.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+            FPM_TRY(upload_pageable(ctx, mask_staging.ptr, ms->masks, total, s));
         }
         FPM_CUDA(fpm::launch_permute_amplitude(N, staging.as<double>(), ms->masks ? mask_staging.as<uint8_t>() : nullptr,
                                                gain_staging.as<double>(), p->meas.as<float>(), F, s));
@@ -724,7 +810,7 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
         if (ms->masks) {
             FPM_TRY(p->masks.ensure(total));
             FPM_TRY(mask_staging.ensure(total));
-            FPM_CUDA(cudaMemcpyAsync(mask_staging.ptr, ms->masks, total, cudaMemcpyHostToDevice, s));
+            FPM_TRY(upload_pageable(ctx, mask_staging.ptr, ms->masks, total, s));
             FPM_CUDA(fpm::launch_permute_u8(N, mask_staging.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
         }
     }
@@ -734,25 +820,24 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
         bg_staging.bind(ctx->pool, s);
         FPM_TRY(bg_staging.ensure((size_t)md->background_len * sizeof(double)));
         FPM_TRY(p->background.ensure((size_t)md->background_len * sizeof(float)));
-        FPM_CUDA(cudaMemcpyAsync(bg_staging.ptr, md->background, (size_t)md->background_len * sizeof(double),
-                                 cudaMemcpyHostToDevice, s));
+        FPM_TRY(upload_pageable(ctx, bg_staging.ptr, md->background, (size_t)md->background_len * sizeof(double), s));
         FPM_CUDA(fpm::launch_permute_f64_to_f32(N, bg_staging.as<double>(), p->background.as<float>(), bg_frames, s));
     }
     p->state_gains.resize(F);
     for (int f = 0; f < F; ++f) p->state_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
     FPM_TRY(p->gains_d.ensure(F * sizeof(double)));
-    FPM_CUDA(cudaMemcpyAsync(p->gains_d.ptr, p->state_gains.data(), F * sizeof(double), cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, p->gains_d.ptr, p->state_gains.data(), F * sizeof(double), s));
     FPM_TRY(p->frame_params.ensure(sizeof(fpm::FrameParam) * F));
-    FPM_CUDA(cudaMemcpyAsync(p->frame_params.ptr, p->params.data(), sizeof(fpm::FrameParam) * F, cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, p->frame_params.ptr, p->params.data(), sizeof(fpm::FrameParam) * F, s));
     FPM_TRY(p->support_d.ensure(n2));
-    FPM_CUDA(cudaMemcpyAsync(p->support_d.ptr, p->support.data(), n2, cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, p->support_d.ptr, p->support.data(), n2, s));
     FPM_TRY(p->pupil_ref.ensure(n2 * sizeof(double2)));
-    FPM_CUDA(cudaMemcpyAsync(p->pupil_ref.ptr, p->pupil.data(), n2 * sizeof(double2), cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, p->pupil_ref.ptr, p->pupil.data(), n2 * sizeof(double2), s));
     std::vector<float2>& pf = p->pupil_f32;
     pf.resize(n2);
     for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)p->pupil[2 * i], (float)p->pupil[2 * i + 1]);
     FPM_TRY(p->pupil_model.ensure(n2 * sizeof(float2)));
-    FPM_CUDA(cudaMemcpyAsync(p->pupil_model.ptr, pf.data(), n2 * sizeof(float2), cudaMemcpyHostToDevice, s));
+    FPM_TRY(upload_pageable(ctx, p->pupil_model.ptr, pf.data(), n2 * sizeof(float2), s));
     // Unit pupil: every value exactly 0 or 1 (FP32), the ones of each row on
     // one column interval. The single-CTA engine then reads the intervals
     // instead of the pupil; P * patch and U come out the same.
@@ -777,7 +862,7 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     }
     if (p->unit_pupil) {
         FPM_TRY(p->pupil_span.ensure(N * sizeof(int2)));
-        FPM_CUDA(cudaMemcpyAsync(p->pupil_span.ptr, spans.data(), N * sizeof(int2), cudaMemcpyHostToDevice, s));
+        FPM_TRY(upload_pageable(ctx, p->pupil_span.ptr, spans.data(), N * sizeof(int2), s));
     }
     return Status::ok();
 }
@@ -1005,9 +1090,9 @@ struct Bucket {
 };
 
 template <class T>
-Status upload_array(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
+Status upload_array(fpm_context* ctx, DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
     FPM_TRY(buf.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
-    if (!v.empty()) FPM_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    if (!v.empty()) FPM_TRY(upload_pageable(ctx, buf.ptr, v.data(), sizeof(T) * v.size(), s));
     return Status::ok();
 }
 
@@ -1210,7 +1295,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         }
         const int* order_dev = nullptr;
         if (a->schedule != FPM_SCHEDULE_SEQUENTIAL) {
-            if (br.prepare) FPM_TRY(upload_array(p->order, schedule_order(p, a->schedule), s));
+            if (br.prepare) FPM_TRY(upload_array(ctx, p->order, schedule_order(p, a->schedule), s));
             order_dev = p->order.as<int>();
         }
         // max(max |P|^2, eps) of the compiled pupil, FP64.
@@ -1265,7 +1350,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                         return Status::make(FPM_ERR_INVALID_PARAMETER,
                                             "checkpoint illumination correction of source %d moves its crop outside "
                                             "the reconstruction grid", f);
-                FPM_TRY(upload_array(p->ill_params, prm, s));
+                FPM_TRY(upload_array(ctx, p->ill_params, prm, s));
                 FPM_CUDA(cudaMemcpyAsync(p->ill_correction.ptr, saved, sizeof(double) * 2 * F,
                                          cudaMemcpyHostToDevice, s));
             } else {
@@ -1282,8 +1367,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 offset[2 * f + 1] = p->off_col[f];
             }
             if (br.prepare) {
-                FPM_TRY(upload_array(p->ill_start, start, s));
-                FPM_TRY(upload_array(p->ill_offset, offset, s));
+                FPM_TRY(upload_array(ctx, p->ill_start, start, s));
+                FPM_TRY(upload_array(ctx, p->ill_offset, offset, s));
             }
             FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * fpm::kIlluminationBlocks * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
@@ -1386,14 +1471,14 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     if (!br.first) FPM_CUDA(cudaEventCreate(&br.first));
     if (!br.last) FPM_CUDA(cudaEventCreate(&br.last));
     if (br.prepare) {
-        if (tma) FPM_TRY(upload_array(br.tmaps, maps, s));
-        FPM_TRY(upload_array(br.tiles, tiles, s));
-        FPM_TRY(upload_array(br.init, inits, s));
-        FPM_TRY(upload_array(br.gauge, gauges, s));
-        FPM_TRY(upload_array(br.scratch_ptrs, scratch, s));
-        FPM_TRY(upload_array(br.object_ptrs, objects, s));
-        FPM_TRY(upload_array(br.anchor_ptrs, anchors, s));
-        FPM_TRY(upload_array(br.velocity_ptrs, velocities, s));
+        if (tma) FPM_TRY(upload_array(ctx, br.tmaps, maps, s));
+        FPM_TRY(upload_array(ctx, br.tiles, tiles, s));
+        FPM_TRY(upload_array(ctx, br.init, inits, s));
+        FPM_TRY(upload_array(ctx, br.gauge, gauges, s));
+        FPM_TRY(upload_array(ctx, br.scratch_ptrs, scratch, s));
+        FPM_TRY(upload_array(ctx, br.object_ptrs, objects, s));
+        FPM_TRY(upload_array(ctx, br.anchor_ptrs, anchors, s));
+        FPM_TRY(upload_array(ctx, br.velocity_ptrs, velocities, s));
         // The line FFT plans of both grids exist before any launch (a plan's
         // creation synchronises, which a graph capture cannot).
         FftPlan* plan = nullptr;
@@ -1444,7 +1529,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
     ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
     if (recover_gb) {
-        if (br.prepare) FPM_TRY(upload_array(br.recovery, recovery, s));
+        if (br.prepare) FPM_TRY(upload_array(ctx, br.recovery, recovery, s));
         ep.recovery = br.recovery.as<fpm::TileRecovery>();
     }
     ep.recover_gains = recover_gb && a->recover_frame_gains ? 1 : 0;
@@ -1520,10 +1605,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 if (k == 0) tv_ptrs[t] = tv ? p->tv_scratch.as<double2>() : nullptr;
             }
         if (br.prepare) {
-            FPM_TRY(upload_array(br.tv_table, tv_table, s));
-            FPM_TRY(upload_array(br.smooth_table, smooth_table, s));
-            FPM_TRY(upload_array(br.tv_ptrs, tv_ptrs, s));
-            FPM_TRY(upload_array(br.tv_objects, tv_objects, s));
+            FPM_TRY(upload_array(ctx, br.tv_table, tv_table, s));
+            FPM_TRY(upload_array(ctx, br.smooth_table, smooth_table, s));
+            FPM_TRY(upload_array(ctx, br.tv_ptrs, tv_ptrs, s));
+            FPM_TRY(upload_array(ctx, br.tv_objects, tv_objects, s));
         }
         // Illumination tasks of batch k: [k * batch_tasks, (k + 1) * batch_tasks),
         // evaluated in chunks of at most `chunk` tasks (5 FP64 N x N fields
@@ -1544,11 +1629,11 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(br.ill_fields.ensure(field_bytes * chunk));
             FPM_TRY(br.ill_valid.ensure(sizeof(int) * 5 * (size_t)chunk));
             if (br.prepare) {
-                FPM_TRY(upload_array(br.ill_tiles, ill_tiles, s));
-                FPM_TRY(upload_array(br.ill_tasks, tasks, s));
+                FPM_TRY(upload_array(ctx, br.ill_tiles, ill_tiles, s));
+                FPM_TRY(upload_array(ctx, br.ill_tasks, tasks, s));
                 std::vector<double2*> ptrs((size_t)5 * chunk);
                 for (size_t i = 0; i < ptrs.size(); ++i) ptrs[i] = br.ill_fields.as<double2>() + i * (size_t)N * N;
-                FPM_TRY(upload_array(br.ill_ptrs, ptrs, s));
+                FPM_TRY(upload_array(ctx, br.ill_ptrs, ptrs, s));
             }
             ip.tiles = br.ill_tiles.as<fpm::IlluminationTile>();
             ip.fields = br.ill_fields.as<double2>();
@@ -1908,6 +1993,12 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
                       const fpm_algorithm_params* a, fpm_result_desc* results,
                       std::vector<std::unique_ptr<fpm_problem>>& made) {
     constexpr size_t kChunkBytes = size_t(1) << 31;
+    using clock = std::chrono::steady_clock;
+    const auto t_call = clock::now();
+    auto since = [](clock::time_point t0) {
+        return std::chrono::duration<double, std::milli>(clock::now() - t0).count();
+    };
+    double scan_ms = 0.0, upload_ms = 0.0, first_launch_ms = 0.0;
     FPM_TRY(validate_params(a));
     if (count < 0) return Status::make(FPM_ERR_INVALID_PARAMETER, "problem count must be non-negative");
     made.clear();
@@ -1934,8 +2025,11 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
     std::vector<Bucket> chunks;
     for (const auto& g : groups) {
         // Sizes whose engine picks its shape by the launch's tile count
-        // keep enough tiles per chunk for the single-CTA engine.
-        size_t min_tiles = 1;
+        // keep enough tiles per chunk for the single-CTA engine. The first
+        // chunk stays an ordinary one when the rest still fills such chunks:
+        // it runs on the cluster engine while the large chunks upload, so
+        // the device starts after one chunk's upload rather than a large one.
+        size_t min_tiles = 1, first_tiles = 0;
         {
             bool single = false;
             int resident = 0;
@@ -1945,18 +2039,31 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
                                       amplitude && !a->compensated_accumulation && !recovery, (int)g.second.size(),
                                       &single, &resident));
             if (single) {
-                const size_t parts = std::max<size_t>(1, g.second.size() / std::max(1, (2 * resident + 2) / 3));
-                min_tiles = (g.second.size() + parts - 1) / parts;
+                const size_t threshold = std::max(1, (2 * resident + 2) / 3);
+                size_t head = 0, head_bytes = 0;
+                for (int i : g.second) {
+                    if (head > 0 && head_bytes + bytes[i] > kChunkBytes) break;
+                    head_bytes += bytes[i];
+                    ++head;
+                }
+                const size_t rest = g.second.size() - head;
+                if (head < g.second.size() && rest >= threshold) first_tiles = head;
+                const size_t pool = first_tiles ? rest : g.second.size();
+                const size_t parts = std::max<size_t>(1, pool / threshold);
+                min_tiles = (pool + parts - 1) / parts;
             }
         }
-        size_t acc = 0, tiles = 0;
+        size_t acc = 0, tiles = 0, placed = 0;
         for (int i : g.second) {
+            const size_t need = first_tiles && placed < first_tiles ? first_tiles : min_tiles;
+            const bool head_done = first_tiles && placed == first_tiles;
             if (chunks.empty() || chunks.back().n != g.first.first || chunks.back().m != g.first.second ||
-                (acc + bytes[i] > kChunkBytes && tiles >= min_tiles)) {
+                head_done || (acc + bytes[i] > kChunkBytes && tiles >= need)) {
                 chunks.push_back(Bucket{g.first.first, g.first.second, {}, {}});
                 acc = 0;
                 tiles = 0;
             }
+            ++placed;
             chunks.back().indices.push_back(i);
             acc += bytes[i];
             ++tiles;
@@ -1971,16 +2078,20 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
         std::vector<int> owner(first.back());
         for (size_t t = 0; t < ch.indices.size(); ++t)
             for (long long q = first[t]; q < first[t + 1]; ++q) owner[q] = (int)t;
+        const auto t_scan = clock::now();
         HostPool::get().run(first.back(), [&](long long q) {
             const int i = ch.indices[owner[q]];
             scan_frame(&mds[i], &mss[i], (int)(q - first[owner[q]]), scans[q]);
         });
+        scan_ms += since(t_scan);
         for (size_t t = 0; t < ch.indices.size(); ++t) {
             const int i = ch.indices[t];
             Status st = check_scans(&mss[i], scans.data() + first[t]);
             if (!st) st = prepare_problem(ctx, &mds[i], &mss[i], scans.data() + first[t], made[i]);
             if (st) return Status::make(st.code, "problem %d: %s", i, st.message.c_str());
+            const auto t_up = clock::now();
             FPM_TRY(upload_problem(ctx, made[i].get(), &mds[i], &mss[i], ctx->upload));
+            upload_ms += since(t_up);
             ch.problems.push_back(made[i].get());
         }
         cudaEvent_t ready;
@@ -1992,6 +2103,7 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
         FPM_CUDA(wait);
         runs.push_back(std::make_unique<BucketRun>());
         FPM_TRY(run_bucket(ctx, ch, a, s, *runs.back()));
+        if (k == 0) first_launch_ms = since(t_call);
     }
     // Downloads on their own stream, each after its chunk's last kernel;
     // the last launched (smallest) chunks finish first.
@@ -2005,6 +2117,10 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
     FPM_CUDA(cudaStreamSynchronize(ctx->download));
     for (size_t k = 0; k < chunks.size(); ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
     FPM_TRY(record_stats(ctx, chunks, runs));
+    ctx->stats.host_first_launch_ms = first_launch_ms;
+    ctx->stats.host_scan_ms = scan_ms;
+    ctx->stats.host_upload_ms = upload_ms;
+    ctx->stats.host_call_ms = since(t_call);
     for (size_t k = 0; k < chunks.size(); ++k)
         for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
             const int idx = chunks[k].indices[t];
@@ -2343,8 +2459,8 @@ Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_para
         FPM_CUDA(fpm::launch_permute_u8(N, mask_staging.as<uint8_t>(), j.masks.as<uint8_t>(), E, s));
         ++launches;
     }
-    FPM_TRY(upload_array(j.d_pupils, j.pupils, s));
-    FPM_TRY(upload_array(j.d_steps, j.steps, s));
+    FPM_TRY(upload_array(ctx, j.d_pupils, j.pupils, s));
+    FPM_TRY(upload_array(ctx, j.d_steps, j.steps, s));
     FPM_TRY(j.object.ensure(sizeof(float2) * (size_t)M * j.ostride * j.objects));
     FPM_TRY(j.wide.ensure(sizeof(double2) * nm * j.objects));
     FPM_TRY(j.fields.ensure(sizeof(float2) * n2 * j.max_modes));
@@ -2359,8 +2475,8 @@ Status spectral_upload(fpm_context* ctx, SpectralJob& j, const fpm_spectral_para
         j.optr[o] = j.object.as<float2>() + (size_t)o * M * j.ostride;
         j.wptr[o] = j.wide.as<double2>() + (size_t)o * nm;
     }
-    FPM_TRY(upload_array(j.object_ptrs, j.optr, s));
-    FPM_TRY(upload_array(j.wide_ptrs, j.wptr, s));
+    FPM_TRY(upload_array(ctx, j.object_ptrs, j.optr, s));
+    FPM_TRY(upload_array(ctx, j.wide_ptrs, j.wptr, s));
     if (j.resume_spectra) {
         // Checkpoint spectra are the widened complex64 state: narrowing restores it exactly.
         FPM_CUDA(cudaMemcpyAsync(j.wide.ptr, j.resume_spectra, sizeof(double2) * nm * j.objects, cudaMemcpyHostToDevice, s));
@@ -2501,7 +2617,7 @@ Status spectral_queue(fpm_context* ctx, std::vector<SpectralJob>& jobs, const fp
         }
         b.tile_bufs.push_back(std::make_unique<DeviceBuffer>());
         b.tile_bufs.back()->bind(ctx->pool, s);
-        FPM_TRY(upload_array(*b.tile_bufs.back(), tiles, s));
+        FPM_TRY(upload_array(ctx, *b.tile_bufs.back(), tiles, s));
         fpm::EngineParams ep = spectral_engine_params(a, completed);
         ep.tiles = b.tile_bufs.back()->as<fpm::TileDesc>();
         ep.tile_count = (int)tiles.size();
@@ -2905,17 +3021,17 @@ Status forward_stack_device(fpm_context* ctx, const fpm_model_desc* md, const do
             params[f] = fp;
         }
         DeviceBuffer d_params, d_pupil, d_obj64, d_state, d_ptrs, d_ptrs2, d_bg;
-        FPM_TRY(upload_array(d_params, params, s));
+        FPM_TRY(upload_array(ctx, d_params, params, s));
         std::vector<float2> pf(n2);
         for (size_t i = 0; i < n2; ++i) pf[i] = make_float2((float)md->pupil[2 * i], (float)md->pupil[2 * i + 1]);
-        FPM_TRY(upload_array(d_pupil, pf, s));
+        FPM_TRY(upload_array(ctx, d_pupil, pf, s));
         FPM_TRY(d_obj64.ensure(sizeof(double2) * m2));
         FPM_CUDA(cudaMemcpyAsync(d_obj64.ptr, object, sizeof(double2) * m2, cudaMemcpyHostToDevice, s));
         FPM_TRY(d_state.ensure(sizeof(float2) * (size_t)M * ms));
         std::vector<double2*> p64 = {d_obj64.as<double2>()};
         std::vector<float2*> pst = {d_state.as<float2>()};
-        FPM_TRY(upload_array(d_ptrs, p64, s));
-        FPM_TRY(upload_array(d_ptrs2, pst, s));
+        FPM_TRY(upload_array(ctx, d_ptrs, p64, s));
+        FPM_TRY(upload_array(ctx, d_ptrs2, pst, s));
         if (centred) {
             FPM_CUDA(fpm::launch_narrow(d_obj64.as<double2>(), M, M, d_state.as<float2>(), ms, s));
         } else {
@@ -2929,7 +3045,7 @@ Status forward_stack_device(fpm_context* ctx, const fpm_model_desc* md, const do
         fwd.params = d_params.as<fpm::FrameParam>();
         if (md->background) {
             std::vector<float> bg(md->background, md->background + md->background_len);
-            FPM_TRY(upload_array(d_bg, bg, s));
+            FPM_TRY(upload_array(ctx, d_bg, bg, s));
             fwd.background = d_bg.as<float>();
             fwd.background_stride = md->background_len == (int64_t)n2 ? 0 : (long long)n2;
         }

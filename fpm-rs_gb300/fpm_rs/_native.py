@@ -145,6 +145,8 @@ class RunStats(C.Structure):
         ("engine_ms_sum", C.c_double), ("engine_span_ms", C.c_double), ("engine_bytes", C.c_double),
         ("buckets", C.c_int32), ("bucket_size", C.c_int32 * 8), ("bucket_tiles", C.c_int32 * 8),
         ("bucket_end_ms", C.c_double * 8),
+        ("host_first_launch_ms", C.c_double), ("host_scan_ms", C.c_double), ("host_upload_ms", C.c_double),
+        ("host_call_ms", C.c_double),
     ]
 
 

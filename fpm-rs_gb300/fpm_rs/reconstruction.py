@@ -990,5 +990,6 @@ def last_run_stats() -> dict:
     st = N.RunStats()
     N.check(N.library().fpm_last_run_stats(ctx.handle, C.byref(st)), ctx.handle)
     out = {name: getattr(st, name) for name, _ in N.RunStats._fields_[:6]}
+    out.update({name: getattr(st, name) for name, _ in N.RunStats._fields_[10:]})
     out["buckets"] = [(st.bucket_size[k], st.bucket_tiles[k], st.bucket_end_ms[k]) for k in range(st.buckets)]
     return out

@@ -351,6 +351,11 @@ typedef struct {
     int32_t bucket_size[8];    /* detector size N of each group */
     int32_t bucket_tiles[8];   /* tiles in each group */
     double bucket_end_ms[8];   /* run start to the group's results being ready */
+    /* fpm_run_batch_host only (0 otherwise), host wall times in ms from the
+     * call's start: until the first chunk's device work was queued, spent
+     * validating measurements, spent in measurement uploads, and the whole
+     * call. */
+    double host_first_launch_ms, host_scan_ms, host_upload_ms, host_call_ms;
 } fpm_run_stats;
 
 int32_t fpm_last_run_stats(const fpm_context *ctx, fpm_run_stats *stats);
