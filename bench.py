@@ -93,6 +93,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
     ap.add_argument("--cpu-sample-iterations", type=int, default=1)
+    ap.add_argument("--sizes", default=None,
+                    help="comma-separated tile sizes to keep from the drawn mix (per-size cost; default: all)")
     ap.add_argument("--tune", action="store_true",
                     help="run the launch-table autotuner on the tile workload, write tuning.json and exit")
     ap.add_argument("--engine-256", choices=("auto", "single", "cluster"), default="auto",
@@ -313,6 +315,9 @@ def run_ours(args):
                                       "cluster": fpm.tuning.CLUSTER}[args.engine_256])
     models = build_models(fpm)
     sizes = tile_sizes(args.tiles, args.seed)
+    if args.sizes:
+        keep = {int(x) for x in args.sizes.split(",")}
+        sizes = [n for n in sizes if n in keep]
     seed_base = rank_seed_base(dist.rank)
     t0 = time.perf_counter()
     tiles = generate_tiles(fpm, models, sizes, seed_base)
@@ -536,6 +541,9 @@ def run_reference(args):
     if rank != 0:
         return
     sizes = tile_sizes(args.tiles, args.seed)
+    if args.sizes:
+        keep = {int(x) for x in args.sizes.split(",")}
+        sizes = [n for n in sizes if n in keep]
     values = []
     last = None
     for step in range(args.warmup + args.steps):

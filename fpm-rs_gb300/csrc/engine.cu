@@ -32,6 +32,16 @@ int engine_rows(int n) {
     }
 }
 
+int engine_na(int n) {
+    switch (n) {
+        case 32: return Cfg<32>::NA;
+        case 64: return Cfg<64>::NA;
+        case 128: return Cfg<128>::NA;
+        case 256: return Cfg<256>::NA;
+        default: return 0;
+    }
+}
+
 int init_chunks(int n) { return (n * n + kInitBlock - 1) / kInitBlock; }
 
 #define FPM_DISPATCH(call)                       \

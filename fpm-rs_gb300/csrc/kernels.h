@@ -174,6 +174,10 @@ bool engine_supported(int n);
 int engine_ctas(int n);
 // Field rows per CTA of an n x n tile (the stencil box is engine_rows(n) + 1 rows).
 int engine_rows(int n);
+// Stage-1 radix NA of the engine's row transform for an n x n tile: engine
+// position t of a row holds natural column t / (n / NA) + NA * (t % (n / NA)),
+// and engine row (y % C) * R + y / C holds natural row y.
+int engine_na(int n);
 // `clusters` clusters walk p.tile_count tiles (clusters <= p.tile_count).
 cudaError_t launch_engine(int n, const EngineParams& p, int clusters, cudaStream_t s);
 cudaError_t engine_max_active_clusters(int n, int* count);

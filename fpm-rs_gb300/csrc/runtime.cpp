@@ -269,36 +269,72 @@ struct fpm_problem {
 
 namespace {
 
-// Host -> device copy of `bytes` of pageable memory on stream s, through
-// the context's pinned ring. A copy straight from pageable memory first
-// waits for all earlier work on its stream, so the host would stall behind
-// the device at every small table; here each copy takes the next free
-// stretch of the current slot, large ones in 64 MB pieces copied by the host
-// worker pool, and a slot is reused once its last copy has left it. The
-// caller holds the context.
-Status upload_pageable(fpm_context* ctx, void* dst, const void* src, size_t bytes, cudaStream_t s) {
-    if (bytes == 0) return Status::ok();
+// The context's pinned ring, created on first use.
+Status pinned_ring(fpm_context* ctx, PinnedRing** out) {
     if (!ctx->pinned) {
         auto ring = std::make_unique<PinnedRing>();
         for (int k = 0; k < PinnedRing::kSlots; ++k)
             FPM_CUDA(cudaHostAlloc(&ring->slot[k], PinnedRing::kSlotBytes, cudaHostAllocDefault));
         ctx->pinned = std::move(ring);
     }
-    PinnedRing& R = *ctx->pinned;
+    *out = ctx->pinned.get();
+    return Status::ok();
+}
+
+// `len` bytes (at most a slot) of the ring's current slot, moving to the
+// next slot, once the copies from it on every stream have finished, when
+// the current one is full.
+Status ring_take(PinnedRing& R, size_t len, char** at) {
+    if (R.used + len > PinnedRing::kSlotBytes) {
+        R.cur = (R.cur + 1) % PinnedRing::kSlots;
+        R.used = 0;
+        for (auto& pe : R.pending[R.cur]) {
+            FPM_CUDA(cudaEventSynchronize(pe.second));
+            R.spare.push_back(pe.second);
+        }
+        R.pending[R.cur].clear();
+    }
+    *at = static_cast<char*>(R.slot[R.cur]) + R.used;
+    R.used += (len + 255) & ~size_t(255);
+    return Status::ok();
+}
+
+// Queues the copy of `len` bytes at `at` (in the current slot) to `dst` on
+// stream s and records it against the slot.
+Status ring_copy(PinnedRing& R, void* dst, const char* at, size_t len, cudaStream_t s) {
+    FPM_CUDA(cudaMemcpyAsync(dst, at, len, cudaMemcpyHostToDevice, s));
+    auto& pend = R.pending[R.cur];
+    auto it = std::find_if(pend.begin(), pend.end(), [&](const auto& pe) { return pe.first == s; });
+    if (it == pend.end()) {
+        cudaEvent_t e = nullptr;
+        if (!R.spare.empty()) {
+            e = R.spare.back();
+            R.spare.pop_back();
+        } else {
+            FPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        pend.emplace_back(s, e);
+        it = pend.end() - 1;
+    }
+    FPM_CUDA(cudaEventRecord(it->second, s));  // a stream's copies complete in order
+    return Status::ok();
+}
+
+// Host -> device copy of `bytes` of pageable memory on stream s, through
+// the context's pinned ring. A copy straight from pageable memory first
+// waits for all earlier work on its stream, so the host would stall behind
+// the device at every small table; here each copy takes the next free
+// stretch of the current slot, large ones in 64 MB pieces copied by the host
+// worker pool. The caller holds the context.
+Status upload_pageable(fpm_context* ctx, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return Status::ok();
+    PinnedRing* ring = nullptr;
+    FPM_TRY(pinned_ring(ctx, &ring));
     constexpr size_t kPiece = size_t(1) << 20;
     for (size_t off = 0; off < bytes;) {
-        size_t len = std::min(bytes - off, PinnedRing::kSlotBytes);
-        if (R.used + len > PinnedRing::kSlotBytes) {
-            R.cur = (R.cur + 1) % PinnedRing::kSlots;
-            R.used = 0;
-            // The slot's earlier copies, on whichever streams, have left it.
-            for (auto& pe : R.pending[R.cur]) {
-                FPM_CUDA(cudaEventSynchronize(pe.second));
-                R.spare.push_back(pe.second);
-            }
-            R.pending[R.cur].clear();
-        }
-        char* at = static_cast<char*>(R.slot[R.cur]) + R.used;
+        const size_t len = std::min(bytes - off, PinnedRing::kSlotBytes);
+        char* at = nullptr;
+        FPM_TRY(ring_take(*ring, len, &at));
         const char* from = static_cast<const char*>(src) + off;
         if (len <= kPiece) {
             std::memcpy(at, from, len);
@@ -308,23 +344,35 @@ Status upload_pageable(fpm_context* ctx, void* dst, const void* src, size_t byte
                 std::memcpy(at + o, from + o, std::min(kPiece, len - o));
             });
         }
-        FPM_CUDA(cudaMemcpyAsync(static_cast<char*>(dst) + off, at, len, cudaMemcpyHostToDevice, s));
-        auto& pend = R.pending[R.cur];
-        auto it = std::find_if(pend.begin(), pend.end(), [&](const auto& pe) { return pe.first == s; });
-        if (it == pend.end()) {
-            cudaEvent_t e = nullptr;
-            if (!R.spare.empty()) {
-                e = R.spare.back();
-                R.spare.pop_back();
-            } else {
-                FPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-            }
-            pend.emplace_back(s, e);
-            it = pend.end() - 1;
-        }
-        FPM_CUDA(cudaEventRecord(it->second, s));  // a stream's copies complete in order
-        R.used += (len + 255) & ~size_t(255);
+        FPM_TRY(ring_copy(*ring, static_cast<char*>(dst) + off, at, len, s));
         off += len;
+    }
+    return Status::ok();
+}
+
+// Host -> device copy of `rows` rows of `row_bytes` each, produced on the
+// host straight into the pinned ring: fill(row, out) writes row `row` at
+// `out`, in parallel over the host worker pool. Nothing runs on the device
+// but the copies, so an upload never waits for an SM behind the persistent
+// engine launches. The caller holds the context.
+Status upload_rows(fpm_context* ctx, void* dst, long long rows, size_t row_bytes, cudaStream_t s,
+                   const std::function<void(long long, char*)>& fill) {
+    if (rows <= 0) return Status::ok();
+    PinnedRing* ring = nullptr;
+    FPM_TRY(pinned_ring(ctx, &ring));
+    const long long per_slot = std::max<long long>(1, (long long)(PinnedRing::kSlotBytes / row_bytes));
+    constexpr long long kRowsPerTask = 16;
+    for (long long r0 = 0; r0 < rows;) {
+        const long long n = std::min(per_slot, rows - r0);
+        const size_t len = (size_t)n * row_bytes;
+        char* at = nullptr;
+        FPM_TRY(ring_take(*ring, len, &at));
+        HostPool::get().run((n + kRowsPerTask - 1) / kRowsPerTask, [&](long long q) {
+            const long long a = q * kRowsPerTask, b = std::min(n, a + kRowsPerTask);
+            for (long long r = a; r < b; ++r) fill(r0 + r, at + (size_t)r * row_bytes);
+        });
+        FPM_TRY(ring_copy(*ring, static_cast<char*>(dst) + (size_t)r0 * row_bytes, at, len, s));
+        r0 += n;
     }
     return Status::ok();
 }
@@ -784,44 +832,63 @@ Status upload_problem(fpm_context* ctx, fpm_problem* p, const fpm_model_desc* md
     for (DeviceBuffer* b : {&p->meas, &p->masks, &p->background, &p->frame_params, &p->support_d, &p->pupil_ref,
                             &p->pupil_model, &p->pupil_span, &p->gains_d})
         b->bind(ctx->pool, s);
-    DeviceBuffer staging, mask_staging, gain_staging;
-    for (DeviceBuffer* b : {&staging, &mask_staging, &gain_staging}) b->bind(ctx->pool, s);
-    // Measurements: FP64 upload, permuted to the engine's FP32 layout. With no
-    // background the engine reads the amplitude form sqrt(max(I / g, 0))
-    // (computed in FP64, -1 on masked pixels): one float per pixel, no mask
-    // bytes, and no divide or square root in the frame loop.
+    // Measurements go to the engine's FP32 layout, converted and permuted on
+    // the host into the pinned ring (engine row e of a frame holds natural
+    // row e / R + C (e % R); its position t holds natural column
+    // t / NB + NA (t % NB)). With no background the engine reads the
+    // amplitude form sqrt(max(I / g, 0)) (-1 on masked pixels): one float
+    // per pixel, no mask bytes, and no divide or square root in the frame
+    // loop. Every upload path converts the same way, so results do not
+    // depend on how a problem was uploaded.
     const size_t total = n2 * F;
-    FPM_TRY(staging.ensure(total * sizeof(double)));
+    const int C = fpm::engine_ctas(N), R = fpm::engine_rows(N), NA = fpm::engine_na(N), NB = N / NA;
+    std::vector<int> column(N);
+    for (int t = 0; t < N; ++t) column[t] = t / NB + NA * (t % NB);
+    auto natural_row = [=](long long e) { return (int)(e / R) + C * (int)(e % R); };
     FPM_TRY(p->meas.ensure(total * sizeof(float)));
-    FPM_TRY(upload_pageable(ctx, staging.ptr, ms->measurements, total * sizeof(double), s));
     if (p->amplitude) {
         p->upload_gains.resize(F);
         for (int f = 0; f < F; ++f) p->upload_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
-        FPM_TRY(gain_staging.ensure(F * sizeof(double)));
-        FPM_TRY(upload_pageable(ctx, gain_staging.ptr, p->upload_gains.data(), F * sizeof(double), s));
-        if (ms->masks) {
-            FPM_TRY(mask_staging.ensure(total));
-            FPM_TRY(upload_pageable(ctx, mask_staging.ptr, ms->masks, total, s));
-        }
-        FPM_CUDA(fpm::launch_permute_amplitude(N, staging.as<double>(), ms->masks ? mask_staging.as<uint8_t>() : nullptr,
-                                               gain_staging.as<double>(), p->meas.as<float>(), F, s));
+        const double* gains = p->upload_gains.data();
+        FPM_TRY(upload_rows(ctx, p->meas.ptr, (long long)F * N, N * sizeof(float), s, [&](long long row, char* out) {
+            const long long f = row / N;
+            const size_t base = ((size_t)f * N + natural_row(row % N)) * N;
+            const double* in = ms->measurements + base;
+            const uint8_t* mk = ms->masks ? ms->masks + base : nullptr;
+            const double inv_g = 1.0 / gains[f];
+            // Natural column order first (contiguous, vectorised), then the
+            // permutation: I / g in FP64 (by the reciprocal), rounded to
+            // FP32, square root in FP32 (at most one ulp from rounding the
+            // FP64 root).
+            float a[256];
+            for (int x = 0; x < N; ++x) a[x] = std::sqrt(std::fmax((float)(in[x] * inv_g), 0.0f));
+            if (mk)
+                for (int x = 0; x < N; ++x) a[x] = mk[x] == 0 ? -1.0f : a[x];
+            float* o = reinterpret_cast<float*>(out);
+            for (int t = 0; t < N; ++t) o[t] = a[column[t]];
+        }));
     } else {
-        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, staging.as<double>(), p->meas.as<float>(), F, s));
+        FPM_TRY(upload_rows(ctx, p->meas.ptr, (long long)F * N, N * sizeof(float), s, [&](long long row, char* out) {
+            const double* in = ms->measurements + ((size_t)(row / N) * N + natural_row(row % N)) * N;
+            float* o = reinterpret_cast<float*>(out);
+            for (int t = 0; t < N; ++t) o[t] = (float)in[column[t]];
+        }));
         if (ms->masks) {
             FPM_TRY(p->masks.ensure(total));
-            FPM_TRY(mask_staging.ensure(total));
-            FPM_TRY(upload_pageable(ctx, mask_staging.ptr, ms->masks, total, s));
-            FPM_CUDA(fpm::launch_permute_u8(N, mask_staging.as<uint8_t>(), p->masks.as<uint8_t>(), F, s));
+            FPM_TRY(upload_rows(ctx, p->masks.ptr, (long long)F * N, N, s, [&](long long row, char* out) {
+                const uint8_t* in = ms->masks + ((size_t)(row / N) * N + natural_row(row % N)) * N;
+                for (int t = 0; t < N; ++t) out[t] = in[column[t]];
+            }));
         }
     }
     if (md->background) {
         const long long bg_frames = p->background_stride ? F : 1;
-        DeviceBuffer bg_staging;
-        bg_staging.bind(ctx->pool, s);
-        FPM_TRY(bg_staging.ensure((size_t)md->background_len * sizeof(double)));
         FPM_TRY(p->background.ensure((size_t)md->background_len * sizeof(float)));
-        FPM_TRY(upload_pageable(ctx, bg_staging.ptr, md->background, (size_t)md->background_len * sizeof(double), s));
-        FPM_CUDA(fpm::launch_permute_f64_to_f32(N, bg_staging.as<double>(), p->background.as<float>(), bg_frames, s));
+        FPM_TRY(upload_rows(ctx, p->background.ptr, bg_frames * N, N * sizeof(float), s, [&](long long row, char* out) {
+            const double* in = md->background + ((size_t)(row / N) * N + natural_row(row % N)) * N;
+            float* o = reinterpret_cast<float*>(out);
+            for (int t = 0; t < N; ++t) o[t] = (float)in[column[t]];
+        }));
     }
     p->state_gains.resize(F);
     for (int f = 0; f < F; ++f) p->state_gains[f] = p->gains[f] > 0.0 ? p->gains[f] : 1.0;
@@ -1089,10 +1156,47 @@ struct Bucket {
     std::vector<const fpm_state_desc*> resume;  // per problem, or empty for a fresh start
 };
 
+// Pinned host storage for a run's tables: copies from it are asynchronous
+// and do not wait for the work already queued on the run's stream (a copy
+// from pageable memory would), and it lives as long as the run.
+struct PinnedTables {
+    std::vector<std::pair<char*, size_t>> blocks;  // (block, bytes used of kBlock or more)
+    static constexpr size_t kBlock = size_t(1) << 20;
+    size_t capacity = 0;
+    ~PinnedTables() {
+        for (auto& b : blocks) cudaFreeHost(b.first);
+    }
+    Status take(size_t bytes, char** at) {
+        bytes = (bytes + 255) & ~size_t(255);
+        if (blocks.empty() || blocks.back().second + bytes > capacity) {
+            const size_t size = std::max(kBlock, bytes);
+            char* block = nullptr;
+            FPM_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&block), size, cudaHostAllocDefault));
+            blocks.emplace_back(block, 0);
+            capacity = size;
+        }
+        *at = blocks.back().first + blocks.back().second;
+        blocks.back().second += bytes;
+        return Status::ok();
+    }
+};
+
 template <class T>
 Status upload_array(fpm_context* ctx, DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
     FPM_TRY(buf.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
     if (!v.empty()) FPM_TRY(upload_pageable(ctx, buf.ptr, v.data(), sizeof(T) * v.size(), s));
+    return Status::ok();
+}
+
+// A run's table: staged in the run's own pinned storage and copied on its stream.
+template <class T>
+Status upload_table(PinnedTables& tables, DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
+    FPM_TRY(buf.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (v.empty()) return Status::ok();
+    char* at = nullptr;
+    FPM_TRY(tables.take(sizeof(T) * v.size(), &at));
+    std::memcpy(at, v.data(), sizeof(T) * v.size());
+    FPM_CUDA(cudaMemcpyAsync(buf.ptr, at, sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
     return Status::ok();
 }
 
@@ -1106,6 +1210,7 @@ std::vector<DeviceBuffer*> run_buffers(fpm_problem* p) {
 }
 
 struct BucketRun {
+    PinnedTables tables;         // host sources of the run's table uploads
     DeviceBuffer field_scratch;  // single-CTA engine: per-CTA field scratch
     DeviceBuffer recovery;       // EPRY gain / background recovery: per-tile state pointers
     DeviceBuffer tmaps;  // per tile: the object spectrum's tensor map for TMA stencil staging
@@ -1295,7 +1400,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
         }
         const int* order_dev = nullptr;
         if (a->schedule != FPM_SCHEDULE_SEQUENTIAL) {
-            if (br.prepare) FPM_TRY(upload_array(ctx, p->order, schedule_order(p, a->schedule), s));
+            if (br.prepare) FPM_TRY(upload_table(br.tables, p->order, schedule_order(p, a->schedule), s));
             order_dev = p->order.as<int>();
         }
         // max(max |P|^2, eps) of the compiled pupil, FP64.
@@ -1350,7 +1455,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                         return Status::make(FPM_ERR_INVALID_PARAMETER,
                                             "checkpoint illumination correction of source %d moves its crop outside "
                                             "the reconstruction grid", f);
-                FPM_TRY(upload_array(ctx, p->ill_params, prm, s));
+                FPM_TRY(upload_table(br.tables, p->ill_params, prm, s));
                 FPM_CUDA(cudaMemcpyAsync(p->ill_correction.ptr, saved, sizeof(double) * 2 * F,
                                          cudaMemcpyHostToDevice, s));
             } else {
@@ -1367,8 +1472,8 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 offset[2 * f + 1] = p->off_col[f];
             }
             if (br.prepare) {
-                FPM_TRY(upload_array(ctx, p->ill_start, start, s));
-                FPM_TRY(upload_array(ctx, p->ill_offset, offset, s));
+                FPM_TRY(upload_table(br.tables, p->ill_start, start, s));
+                FPM_TRY(upload_table(br.tables, p->ill_offset, offset, s));
             }
             FPM_TRY(p->ill_partials.ensure(sizeof(double) * 4 * fpm::kIlluminationBlocks * (size_t)F));
             T.params = p->ill_params.as<fpm::FrameParam>();
@@ -1471,14 +1576,14 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     if (!br.first) FPM_CUDA(cudaEventCreate(&br.first));
     if (!br.last) FPM_CUDA(cudaEventCreate(&br.last));
     if (br.prepare) {
-        if (tma) FPM_TRY(upload_array(ctx, br.tmaps, maps, s));
-        FPM_TRY(upload_array(ctx, br.tiles, tiles, s));
-        FPM_TRY(upload_array(ctx, br.init, inits, s));
-        FPM_TRY(upload_array(ctx, br.gauge, gauges, s));
-        FPM_TRY(upload_array(ctx, br.scratch_ptrs, scratch, s));
-        FPM_TRY(upload_array(ctx, br.object_ptrs, objects, s));
-        FPM_TRY(upload_array(ctx, br.anchor_ptrs, anchors, s));
-        FPM_TRY(upload_array(ctx, br.velocity_ptrs, velocities, s));
+        if (tma) FPM_TRY(upload_table(br.tables, br.tmaps, maps, s));
+        FPM_TRY(upload_table(br.tables, br.tiles, tiles, s));
+        FPM_TRY(upload_table(br.tables, br.init, inits, s));
+        FPM_TRY(upload_table(br.tables, br.gauge, gauges, s));
+        FPM_TRY(upload_table(br.tables, br.scratch_ptrs, scratch, s));
+        FPM_TRY(upload_table(br.tables, br.object_ptrs, objects, s));
+        FPM_TRY(upload_table(br.tables, br.anchor_ptrs, anchors, s));
+        FPM_TRY(upload_table(br.tables, br.velocity_ptrs, velocities, s));
         // The line FFT plans of both grids exist before any launch (a plan's
         // creation synchronises, which a graph capture cannot).
         FftPlan* plan = nullptr;
@@ -1529,7 +1634,7 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
     ep.gd_batch = a->algorithm == FPM_ALG_GD ? a->batch_size : 1;
     ep.trunc_threshold = a->algorithm == FPM_ALG_GD && a->poisson_truncation ? (float)a->poisson_truncation_threshold : 0.f;
     if (recover_gb) {
-        if (br.prepare) FPM_TRY(upload_array(ctx, br.recovery, recovery, s));
+        if (br.prepare) FPM_TRY(upload_table(br.tables, br.recovery, recovery, s));
         ep.recovery = br.recovery.as<fpm::TileRecovery>();
     }
     ep.recover_gains = recover_gb && a->recover_frame_gains ? 1 : 0;
@@ -1605,10 +1710,10 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
                 if (k == 0) tv_ptrs[t] = tv ? p->tv_scratch.as<double2>() : nullptr;
             }
         if (br.prepare) {
-            FPM_TRY(upload_array(ctx, br.tv_table, tv_table, s));
-            FPM_TRY(upload_array(ctx, br.smooth_table, smooth_table, s));
-            FPM_TRY(upload_array(ctx, br.tv_ptrs, tv_ptrs, s));
-            FPM_TRY(upload_array(ctx, br.tv_objects, tv_objects, s));
+            FPM_TRY(upload_table(br.tables, br.tv_table, tv_table, s));
+            FPM_TRY(upload_table(br.tables, br.smooth_table, smooth_table, s));
+            FPM_TRY(upload_table(br.tables, br.tv_ptrs, tv_ptrs, s));
+            FPM_TRY(upload_table(br.tables, br.tv_objects, tv_objects, s));
         }
         // Illumination tasks of batch k: [k * batch_tasks, (k + 1) * batch_tasks),
         // evaluated in chunks of at most `chunk` tasks (5 FP64 N x N fields
@@ -1629,11 +1734,11 @@ Status run_bucket(fpm_context* ctx, Bucket& b, const fpm_algorithm_params* a, cu
             FPM_TRY(br.ill_fields.ensure(field_bytes * chunk));
             FPM_TRY(br.ill_valid.ensure(sizeof(int) * 5 * (size_t)chunk));
             if (br.prepare) {
-                FPM_TRY(upload_array(ctx, br.ill_tiles, ill_tiles, s));
-                FPM_TRY(upload_array(ctx, br.ill_tasks, tasks, s));
+                FPM_TRY(upload_table(br.tables, br.ill_tiles, ill_tiles, s));
+                FPM_TRY(upload_table(br.tables, br.ill_tasks, tasks, s));
                 std::vector<double2*> ptrs((size_t)5 * chunk);
                 for (size_t i = 0; i < ptrs.size(); ++i) ptrs[i] = br.ill_fields.as<double2>() + i * (size_t)N * N;
-                FPM_TRY(upload_array(ctx, br.ill_ptrs, ptrs, s));
+                FPM_TRY(upload_table(br.tables, br.ill_ptrs, ptrs, s));
             }
             ip.tiles = br.ill_tiles.as<fpm::IlluminationTile>();
             ip.fields = br.ill_fields.as<double2>();
