@@ -71,11 +71,6 @@ cudaError_t launch_unpermute_f32_to_f64(int n, const float* src, double* dst, lo
     FPM_DISPATCH(unpermute_f64(src, dst, frames, s))
 }
 
-cudaError_t launch_permute_amplitude(int n, const double* src, const uint8_t* masks, const double* gains, float* dst,
-                                     long long frames, cudaStream_t s) {
-    FPM_DISPATCH(permute_amplitude(src, masks, gains, dst, frames, s))
-}
-
 cudaError_t launch_init_mean(int n, int m, const InitTile* tiles, int count, double* avg, double* partial,
                              cudaStream_t s) {
     FPM_DISPATCH(init(m, tiles, count, avg, partial, s))

@@ -1504,24 +1504,6 @@ __global__ void __launch_bounds__(N_) permute_f64_kernel(const double* __restric
     }
 }
 
-template <int N_>
-__global__ void __launch_bounds__(N_) permute_amplitude_kernel(const double* __restrict__ src,
-                                                               const uint8_t* __restrict__ masks,
-                                                               const double* __restrict__ gains,
-                                                               float* __restrict__ dst, long long frames) {
-    using K = Cfg<N_>;
-    __shared__ float row[N_];
-    for (long long r = blockIdx.x; r < frames * K::N; r += gridDim.x) {
-        const long long f = r / K::N;
-        const int y = (int)(r % K::N), t = threadIdx.x;
-        const long long e = r * K::N + t;
-        row[t] = (masks && masks[e] == 0) ? -1.0f : (float)sqrt(fmax(src[e] / gains[f], 0.0));
-        __syncthreads();
-        dst[layout_row_base<K>(f, y) + t] = row[layout_column<K>(t)];
-        __syncthreads();
-    }
-}
-
 // Engine layout -> natural order, widened to FP64: the inverse of
 // permute_f64_kernel (engine position t of a row holds natural column
 // layout_column(t)).
@@ -1761,13 +1743,6 @@ struct EngineEntry {
     static cudaError_t permute_u8(const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s) {
         if (frames <= 0) return cudaSuccess;
         permute_u8_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, dst, frames);
-        return cudaGetLastError();
-    }
-
-    static cudaError_t permute_amplitude(const double* src, const uint8_t* masks, const double* gains, float* dst,
-                                         long long frames, cudaStream_t s) {
-        if (frames <= 0) return cudaSuccess;
-        permute_amplitude_kernel<N_><<<permute_blocks(frames), N_, 0, s>>>(src, masks, gains, dst, frames);
         return cudaGetLastError();
     }
 

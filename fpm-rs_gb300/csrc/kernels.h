@@ -197,10 +197,6 @@ cudaError_t launch_permute_f64_to_f32(int n, const double* src, float* dst, long
 cudaError_t launch_permute_u8(int n, const uint8_t* src, uint8_t* dst, long long frames, cudaStream_t s);
 // Engine layout -> natural-order frames [frames][N][N], widened to FP64.
 cudaError_t launch_unpermute_f32_to_f64(int n, const float* src, double* dst, long long frames, cudaStream_t s);
-// Amplitude form: dst = sqrt(max(src / gain[f], 0)) in FP64, rounded once to
-// float, or -1 where masks (natural order, may be null) is zero.
-cudaError_t launch_permute_amplitude(int n, const double* src, const uint8_t* masks, const double* gains, float* dst,
-                                     long long frames, cudaStream_t s);
 
 // Initial object (ReconstructionState::initialize_with_backend,
 // src/reconstruction/state.rs:280-355) for a batch of tiles of one size:
