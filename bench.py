@@ -394,6 +394,7 @@ def run_ours(args):
     problems = None
 
     e2e_parts = {"call_s": 0.0, "device_span_s": 0.0}
+    e2e_latencies = []  # per tile: call start to its results on the host (ms)
 
     def e2e_step():
         fresh = [fpm.ReconstructionProblem(stack, model) for stack, model in host]
@@ -402,6 +403,8 @@ def run_ours(args):
         e2e_parts["call_s"] += time.perf_counter() - c0
         st = fpm.last_run_stats()
         e2e_parts["device_span_s"] += st["run_ms"] / 1e3
+        for tiles, done_ms in st["host_chunks"]:
+            e2e_latencies.extend([done_ms] * tiles)
         for key in ("host_first_launch_ms", "host_scan_ms", "host_upload_ms", "host_call_ms"):
             e2e_parts[key] = e2e_parts.get(key, 0.0) + st[key] / 1e3
         for p in fresh:
@@ -413,12 +416,14 @@ def run_ours(args):
     dist.barrier()
     e2e_parts.update(call_s=0.0, device_span_s=0.0, host_first_launch_ms=0.0, host_scan_ms=0.0, host_upload_ms=0.0,
                      host_call_ms=0.0)
+    e2e_latencies.clear()
     e0 = time.perf_counter()
     e2e_steps = max(1, args.steps)
     for _ in range(e2e_steps):
         results = e2e_step()
     torch.cuda.synchronize()
     e2e_s = dist.max((time.perf_counter() - e0) / e2e_steps)
+    e2e_lat = sorted(e2e_latencies)
     e2e_value = total_tiles / e2e_s
 
     # Parity spot check against the FP64 oracle: the first tile of every size
@@ -519,8 +524,13 @@ def run_ours(args):
         "gpu_launches": launches // max(1, args.steps),
         "clocks": clock_info,
         "size_done_ms": bucket_end,
-        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                       "definition": "batch start to the tile's results ready on the device"},
+        "latency_ms": {"p50": e2e_lat[len(e2e_lat) // 2] if e2e_lat else None,
+                       "p99": e2e_lat[min(len(e2e_lat) - 1, int(0.99 * len(e2e_lat)))] if e2e_lat else None,
+                       "definition": "solve latency through the public call with host inputs: call start to the "
+                                     "tile's results on the host (its chunk's validation, upload, reconstruction "
+                                     "and download), over every tile of the e2e steps"},
+        "device_latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                              "definition": "batch start to the tile's results ready on the device"},
         "nrmse_vs_fp64": {"tiles_checked": len(nrmse), "tile_sizes": checked_sizes,
                           "per_tile": nrmse, "max": max(nrmse) if nrmse else None, "threshold": 1e-4},
         "compensated_accumulation": {"tiles_per_s": total_tiles / (comp_ms / 1e3), "ms_per_step": comp_ms,

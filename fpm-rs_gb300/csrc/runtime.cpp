@@ -2210,22 +2210,41 @@ Status run_batch_host(fpm_context* ctx, int count, const fpm_model_desc* mds, co
         FPM_TRY(run_bucket(ctx, ch, a, s, *runs.back()));
         if (k == 0) first_launch_ms = since(t_call);
     }
-    // Downloads on their own stream, each after its chunk's last kernel;
-    // the last launched (smallest) chunks finish first.
-    for (size_t k = chunks.size(); k-- > 0;) {
-        FPM_CUDA(cudaStreamWaitEvent(ctx->download, runs[k]->last, 0));
-        for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
-            const int idx = chunks[k].indices[t];
-            FPM_TRY(queue_collect(chunks[k].problems[t], a, results ? &results[idx] : nullptr, ctx->download));
+    // Downloads on their own stream, chunk by chunk in the order the chunks
+    // finish (polled on each chunk's last event), so a chunk's results reach
+    // the host as soon as its own work is done; the time each arrives is its
+    // tiles' latency from the call's start.
+    std::vector<double> done_ms(chunks.size(), -1.0);
+    for (size_t left = chunks.size(); left > 0;) {
+        bool progressed = false;
+        for (size_t k = chunks.size(); k-- > 0;) {
+            if (done_ms[k] >= 0.0) continue;
+            const cudaError_t q = cudaEventQuery(runs[k]->last);
+            if (q == cudaErrorNotReady) continue;
+            FPM_CUDA(q);
+            FPM_CUDA(cudaStreamWaitEvent(ctx->download, runs[k]->last, 0));
+            for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
+                const int idx = chunks[k].indices[t];
+                FPM_TRY(queue_collect(chunks[k].problems[t], a, results ? &results[idx] : nullptr, ctx->download));
+            }
+            FPM_CUDA(cudaStreamSynchronize(ctx->download));
+            done_ms[k] = since(t_call);
+            --left;
+            progressed = true;
         }
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
-    FPM_CUDA(cudaStreamSynchronize(ctx->download));
     for (size_t k = 0; k < chunks.size(); ++k) FPM_CUDA(cudaStreamSynchronize(ctx->streams[k % fpm_context::kStreams]));
     FPM_TRY(record_stats(ctx, chunks, runs));
     ctx->stats.host_first_launch_ms = first_launch_ms;
     ctx->stats.host_scan_ms = scan_ms;
     ctx->stats.host_upload_ms = upload_ms;
     ctx->stats.host_call_ms = since(t_call);
+    ctx->stats.host_chunks = (int32_t)std::min<size_t>(chunks.size(), 16);
+    for (size_t k = 0; k < chunks.size() && k < 16; ++k) {
+        ctx->stats.host_done_ms[k] = done_ms[k];
+        ctx->stats.host_done_tiles[k] = (int32_t)chunks[k].problems.size();
+    }
     for (size_t k = 0; k < chunks.size(); ++k)
         for (size_t t = 0; t < chunks[k].problems.size(); ++t) {
             const int idx = chunks[k].indices[t];

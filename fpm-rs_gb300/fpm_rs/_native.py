@@ -147,6 +147,7 @@ class RunStats(C.Structure):
         ("bucket_end_ms", C.c_double * 8),
         ("host_first_launch_ms", C.c_double), ("host_scan_ms", C.c_double), ("host_upload_ms", C.c_double),
         ("host_call_ms", C.c_double),
+        ("host_chunks", C.c_int32), ("host_done_tiles", C.c_int32 * 16), ("host_done_ms", C.c_double * 16),
     ]
 
 

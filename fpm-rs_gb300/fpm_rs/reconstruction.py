@@ -990,6 +990,7 @@ def last_run_stats() -> dict:
     st = N.RunStats()
     N.check(N.library().fpm_last_run_stats(ctx.handle, C.byref(st)), ctx.handle)
     out = {name: getattr(st, name) for name, _ in N.RunStats._fields_[:6]}
-    out.update({name: getattr(st, name) for name, _ in N.RunStats._fields_[10:]})
+    out.update({name: getattr(st, name) for name, _ in N.RunStats._fields_[10:14]})
+    out["host_chunks"] = [(st.host_done_tiles[k], st.host_done_ms[k]) for k in range(st.host_chunks)]
     out["buckets"] = [(st.bucket_size[k], st.bucket_tiles[k], st.bucket_end_ms[k]) for k in range(st.buckets)]
     return out

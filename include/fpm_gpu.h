@@ -356,6 +356,11 @@ typedef struct {
      * validating measurements, spent in measurement uploads, and the whole
      * call. */
     double host_first_launch_ms, host_scan_ms, host_upload_ms, host_call_ms;
+    /* fpm_run_batch_host only: the call's chunks (at most 16 reported), each
+     * with its tile count and the time its results were on the host. */
+    int32_t host_chunks;
+    int32_t host_done_tiles[16];
+    double host_done_ms[16];
 } fpm_run_stats;
 
 int32_t fpm_last_run_stats(const fpm_context *ctx, fpm_run_stats *stats);

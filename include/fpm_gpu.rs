@@ -113,7 +113,8 @@ extern "C" {
 #[repr(C)] pub struct FpmRunStats { pub kernel_launches: i32, pub engine_launches: i32, pub run_ms: f64,
     pub engine_ms_sum: f64, pub engine_span_ms: f64, pub engine_bytes: f64, pub buckets: i32,
     pub bucket_size: [i32; 8], pub bucket_tiles: [i32; 8], pub bucket_end_ms: [f64; 8],
-    pub host_first_launch_ms: f64, pub host_scan_ms: f64, pub host_upload_ms: f64, pub host_call_ms: f64 }
+    pub host_first_launch_ms: f64, pub host_scan_ms: f64, pub host_upload_ms: f64, pub host_call_ms: f64,
+    pub host_chunks: i32, pub host_done_tiles: [i32; 16], pub host_done_ms: [f64; 16] }
 #[repr(C)] pub struct FpmSpectralModelDesc { pub channels: i32, pub channel_models: *const FpmModelDesc,
     pub object_coupling: i32, pub exposures: i32, pub contribution_offsets: *const i32,
     pub contribution_channel: *const i32, pub contribution_local_frame: *const i32,
