@@ -74,10 +74,11 @@ L2_BYTES = 129 * 1024 * 1024
 # iteration, by tile size: ncu dram__bytes_read.sum + dram__bytes_write.sum
 # of the cluster-engine launches of a 64-tile run
 # (profiles/engine_dram_traffic_64tiles.txt) and, for 256-point tiles, of
-# the single-CTA engine that the 1024-tile run uses for them
-# (profiles/engine_l2_256_full_13tiles.txt: 3.197 GB for 13 tile-iterations).
+# the single-CTA engine that the 1024-tile run uses for them, under load
+# (profiles/launches_mix700_single_cta.txt: 1116.5 GB for 1704
+# tile-iterations with about 150 CTAs resident; alone it moves 246 MB).
 # roofline.traffic scales them by this run's tile counts and iterations.
-DRAM_BYTES_PER_TILE_ITERATION = {256: 245.9e6, 128: 23.32e6, 64: 0.827e6, 32: 0.040e6}
+DRAM_BYTES_PER_TILE_ITERATION = {256: 655.2e6, 128: 23.32e6, 64: 0.827e6, 32: 0.040e6}
 
 
 def parse():
