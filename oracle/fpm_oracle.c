@@ -58,11 +58,13 @@ static int32_t fail(int32_t code, const char *fmt, ...) {
 
 /* --------------------------------------------------------------------- FFT */
 
-/* One cached 1-D plan: forward twiddles e^{-2 pi i t / n}. */
+/* One cached 1-D plan: forward twiddles e^{-2 pi i t / n} and their exact
+ * conjugates for the inverse direction. */
 typedef struct {
     int n;
     int pow2;
     cplx *tw;
+    cplx *twi;
     int *rev;
 } fft_plan;
 
@@ -76,12 +78,15 @@ static fft_plan *get_plan(int n) {
     fft_plan *p = &g_plans[g_plan_next];
     g_plan_next = (g_plan_next + 1) % PLAN_CACHE;
     free(p->tw);
+    free(p->twi);
     free(p->rev);
     p->n = n;
     p->tw = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+    p->twi = (cplx *)malloc(sizeof(cplx) * (size_t)n);
     for (int t = 0; t < n; ++t) {
         double angle = 2.0 * M_PI * (double)t / (double)n;
         p->tw[t] = cx(cos(angle), -sin(angle));
+        p->twi[t] = c_conj(p->tw[t]);
     }
     p->pow2 = (n & (n - 1)) == 0;
     p->rev = NULL;
@@ -144,50 +149,134 @@ static void dft_rec(const cplx *in, int stride, cplx *out, int n, const fft_plan
     }
 }
 
+/* Two doubles (re, im) as one GCC vector value: portable C (the vector
+ * extension, no target intrinsics), unaligned-safe loads and stores. */
+typedef double v2d __attribute__((vector_size(16)));
+typedef double v2d_u __attribute__((vector_size(16), aligned(8)));
+
+static inline v2d v_load(const cplx *p) { return *(const v2d_u *)p; }
+static inline void v_store(cplx *p, v2d v) { *(v2d_u *)p = v; }
+/* b * w with w = (wr, wi) and ws = (-wi, wr): (re wr + im (-wi), re wi +
+ * im wr), which rounds exactly like c_mul(b, w) since negation is exact. */
+static inline v2d v_mul(v2d b, v2d w, v2d ws) {
+    v2d re = {b[0], b[0]}, im = {b[1], b[1]};
+    return re * w + im * ws;
+}
+
+/* Power-of-two radix-2 decimation in time over `count` interleaved
+ * transforms: element i of transform c sits at v[i * count + c]. With
+ * count = 1 this is one contiguous transform; with count = w it transforms
+ * every column of an h x w row-major array at once, each butterfly combining
+ * two whole rows, so the inner loop runs over contiguous memory. Every
+ * transform sees the same operations in the same order for any count. */
+static void fft_pow2(cplx *v, size_t count, const fft_plan *plan, int inverse) {
+    int n = plan->n;
+    const cplx *tw = inverse ? plan->twi : plan->tw;
+    for (int i = 0; i < n; ++i) {
+        int r = plan->rev[i];
+        if (r <= i) continue;
+        cplx *a = v + (size_t)i * count, *b = v + (size_t)r * count;
+        for (size_t c = 0; c < count; ++c) {
+            cplx tmp = a[c];
+            a[c] = b[c];
+            b[c] = tmp;
+        }
+    }
+    int len = 2;
+    int bits = 0;
+    while ((1 << bits) < n) ++bits;
+    if (bits & 1) {
+        /* One lone stage (butterflies of width 2, twiddle w^0) leaves an
+         * even number of stages for the pairs below. */
+        v2d w = {tw[0].re, tw[0].im}, ws = {-tw[0].im, tw[0].re};
+        for (int start = 0; start < n; start += 2) {
+            cplx *a = v + (size_t)start * count, *b = a + count;
+            for (size_t c = 0; c < count; ++c) {
+                v2d x = v_load(a + c);
+                v2d y = v_mul(v_load(b + c), w, ws);
+                v_store(a + c, x + y);
+                v_store(b + c, x - y);
+            }
+        }
+        len = 4;
+    }
+    /* Stages len and 2 len together: for j < h = len / 2 the four points
+     * start + j + {0, h, 2h, 3h} meet only each other in both stages, so
+     * their four radix-2 butterflies run in registers, in the same order and
+     * with the same twiddles as two separate passes. */
+    for (; len <= n; len <<= 2) {
+        int h = len >> 1;
+        size_t step1 = (size_t)(n / len), step2 = step1 >> 1;
+        for (int start = 0; start < n; start += 2 * len) {
+            for (int j = 0; j < h; ++j) {
+                cplx t1 = tw[(size_t)j * step1], t2 = tw[(size_t)j * step2], t3 = tw[(size_t)(j + h) * step2];
+                v2d w1 = {t1.re, t1.im}, w1s = {-t1.im, t1.re};
+                v2d w2 = {t2.re, t2.im}, w2s = {-t2.im, t2.re};
+                v2d w3 = {t3.re, t3.im}, w3s = {-t3.im, t3.re};
+                cplx *p0 = v + (size_t)(start + j) * count;
+                cplx *p1 = p0 + (size_t)h * count, *p2 = p1 + (size_t)h * count, *p3 = p2 + (size_t)h * count;
+                for (size_t c = 0; c < count; ++c) {
+                    v2d x0 = v_load(p0 + c), x2 = v_load(p2 + c);
+                    v2d y1 = v_mul(v_load(p1 + c), w1, w1s), y3 = v_mul(v_load(p3 + c), w1, w1s);
+                    v2d a0 = x0 + y1, a1 = x0 - y1;
+                    v2d a2 = x2 + y3, a3 = x2 - y3;
+                    v2d z2 = v_mul(a2, w2, w2s), z3 = v_mul(a3, w3, w3s);
+                    v_store(p0 + c, a0 + z2);
+                    v_store(p2 + c, a0 - z2);
+                    v_store(p1 + c, a1 + z3);
+                    v_store(p3 + c, a1 - z3);
+                }
+            }
+        }
+    }
+}
+
 /* Unnormalised 1-D transform in place on contiguous values. */
 static void fft1(cplx *v, int n, int inverse, cplx *scratch) {
     if (n <= 1) return;
     fft_plan *plan = get_plan(n);
     if (plan->pow2) {
-        for (int i = 0; i < n; ++i) {
-            int r = plan->rev[i];
-            if (r > i) {
-                cplx tmp = v[i];
-                v[i] = v[r];
-                v[r] = tmp;
-            }
-        }
-        for (int len = 2; len <= n; len <<= 1) {
-            int half = len >> 1;
-            int step = n / len;
-            for (int start = 0; start < n; start += len) {
-                for (int j = 0; j < half; ++j) {
-                    cplx w = plan->tw[(size_t)j * step];
-                    if (inverse) w = c_conj(w);
-                    cplx a = v[start + j];
-                    cplx b = c_mul(v[start + j + half], w);
-                    v[start + j] = c_add(a, b);
-                    v[start + j + half] = c_sub(a, b);
-                }
-            }
-        }
+        fft_pow2(v, 1, plan, inverse);
         return;
     }
     memcpy(scratch, v, sizeof(cplx) * (size_t)n);
     dft_rec(scratch, 1, v, n, plan, inverse);
 }
 
+#define ROW_GROUP 8
+
 /* CpuBackend::fft2 (src/backend/cpu.rs:130-175): rows, then columns; the
- * forward transform is normalised by 1/(h*w) and the inverse is not. */
+ * forward transform is normalised by 1/(h*w) and the inverse is not. A
+ * power-of-two row length transforms ROW_GROUP rows at a time, interleaved
+ * in a small scratch slab; each row's arithmetic is the same as a one-row
+ * transform. */
 static void fft2_c(cplx *v, int h, int w, int inverse) {
     int longest = h > w ? h : w;
-    cplx *scratch = (cplx *)malloc(sizeof(cplx) * (size_t)longest * 2);
+    cplx *scratch = (cplx *)malloc(sizeof(cplx) * (size_t)longest * (2 + ROW_GROUP));
     cplx *column = scratch + longest;
-    for (int r = 0; r < h; ++r) fft1(v + (size_t)r * w, w, inverse, scratch);
-    for (int c = 0; c < w; ++c) {
-        for (int r = 0; r < h; ++r) column[r] = v[(size_t)r * w + c];
-        fft1(column, h, inverse, scratch);
-        for (int r = 0; r < h; ++r) v[(size_t)r * w + c] = column[r];
+    cplx *slab = column + longest;
+    fft_plan *row_plan = w > 1 ? get_plan(w) : NULL;
+    int r = 0;
+    if (row_plan && row_plan->pow2) {
+        for (; r + ROW_GROUP <= h; r += ROW_GROUP) {
+            const cplx *rows = v + (size_t)r * w;
+            for (int i = 0; i < w; ++i)
+                for (int g = 0; g < ROW_GROUP; ++g) slab[(size_t)i * ROW_GROUP + g] = rows[(size_t)g * w + i];
+            fft_pow2(slab, ROW_GROUP, row_plan, inverse);
+            for (int g = 0; g < ROW_GROUP; ++g)
+                for (int i = 0; i < w; ++i) v[(size_t)(r + g) * w + i] = slab[(size_t)i * ROW_GROUP + g];
+        }
+    }
+    for (; r < h; ++r) fft1(v + (size_t)r * w, w, inverse, scratch);
+    fft_plan *plan = h > 1 ? get_plan(h) : NULL;
+    if (plan && plan->pow2) {
+        fft_pow2(v, (size_t)w, plan, inverse);
+    } else {
+        for (int c = 0; c < w && h > 1; ++c) {
+            for (int r = 0; r < h; ++r) column[r] = v[(size_t)r * w + c];
+            fft1(column, h, inverse, scratch);
+            for (int r = 0; r < h; ++r) v[(size_t)r * w + c] = column[r];
+        }
     }
     if (!inverse) {
         double norm = (double)h * (double)w;

@@ -40,7 +40,11 @@ def test_fft_forward_inverse_round_trip():
     assert np.abs(back - original).max() <= 1e-10
 
 
-@pytest.mark.parametrize("shape", [(7, 9), (42, 42), (96, 96), (189, 189), (13, 17), (37, 1031)])
+@pytest.mark.parametrize("shape", [(7, 9), (42, 42), (96, 96), (189, 189), (13, 17), (37, 1031),
+                                   # power-of-two paths: even and odd exponents, groups of eight rows
+                                   # with a ragged tail, and either axis a power of two alone
+                                   (32, 32), (128, 128), (256, 256), (2, 512), (12, 64), (8, 96), (96, 8),
+                                   (1, 16), (16, 1)])
 def test_fft_matches_numpy_with_reference_normalisation(shape):
     # CpuBackend::fft2 (src/backend/cpu.rs:162-172): forward / N, inverse unscaled.
     rng = np.random.default_rng(1)
