@@ -111,44 +111,6 @@ static int smallest_factor(int n) {
     return n;
 }
 
-/* Mixed-radix decimation in time: out[k] = sum_j in[j*stride] w_n^{jk}. */
-static void dft_rec(const cplx *in, int stride, cplx *out, int n, const fft_plan *root,
-                    int inverse) {
-    if (n == 1) {
-        out[0] = in[0];
-        return;
-    }
-    int p = smallest_factor(n);
-    int m = n / p;
-    for (int r = 0; r < p; ++r) dft_rec(in + (size_t)r * stride, stride * p, out + (size_t)r * m, m, root, inverse);
-    int step = root->n / n;
-    cplx stack_t[16];
-    cplx *t = p <= 16 ? stack_t : (cplx *)malloc(sizeof(cplx) * (size_t)p);
-    cplx stack_y[16];
-    cplx *y = p <= 16 ? stack_y : (cplx *)malloc(sizeof(cplx) * (size_t)p);
-    for (int k = 0; k < m; ++k) {
-        for (int r = 0; r < p; ++r) {
-            cplx w = root->tw[(size_t)((long)r * k % n) * step];
-            if (inverse) w = c_conj(w);
-            t[r] = c_mul(out[(size_t)r * m + k], w);
-        }
-        for (int q = 0; q < p; ++q) {
-            cplx acc = cx(0.0, 0.0);
-            for (int r = 0; r < p; ++r) {
-                cplx w = root->tw[(size_t)((long)m * r * q % n) * step];
-                if (inverse) w = c_conj(w);
-                acc = c_add(acc, c_mul(t[r], w));
-            }
-            y[q] = acc;
-        }
-        for (int q = 0; q < p; ++q) out[(size_t)k + (size_t)m * q] = y[q];
-    }
-    if (p > 16) {
-        free(t);
-        free(y);
-    }
-}
-
 /* Two doubles (re, im) as one GCC vector value: portable C (the vector
  * extension, no target intrinsics), unaligned-safe loads and stores. */
 typedef double v2d __attribute__((vector_size(16)));
@@ -161,6 +123,55 @@ static inline void v_store(cplx *p, v2d v) { *(v2d_u *)p = v; }
 static inline v2d v_mul(v2d b, v2d w, v2d ws) {
     v2d re = {b[0], b[0]}, im = {b[1], b[1]};
     return re * w + im * ws;
+}
+
+/* Mixed-radix decimation in time over `count` interleaved transforms:
+ * out[k] = sum_j in[j istride] w_n^{jk}, where each element is a run of
+ * `count` values (one per transform) and out holds element k at k count.
+ * The p-point steps of every transform use the same operations in the same
+ * order for any count. t and y hold p count values each, for the largest
+ * prime p of n; a level uses them only after its sub-transforms return. */
+static void dft_multi(const cplx *in, size_t istride, cplx *out, int n, const fft_plan *root, int inverse,
+                      size_t count, cplx *t, cplx *y) {
+    if (n == 1) {
+        memcpy(out, in, sizeof(cplx) * count);
+        return;
+    }
+    int p = smallest_factor(n);
+    int m = n / p;
+    for (int r = 0; r < p; ++r)
+        dft_multi(in + (size_t)r * istride, istride * p, out + (size_t)r * m * count, m, root, inverse, count, t, y);
+    int step = root->n / n;
+    const cplx *tw = inverse ? root->twi : root->tw;
+    for (int k = 0; k < m; ++k) {
+        /* Twiddle w_n^{r k}: its exponent (r k mod n) advances by k per r. */
+        for (int r = 0, e = 0; r < p; ++r) {
+            cplx w = tw[(size_t)e * step];
+            v2d wv = {w.re, w.im}, ws = {-w.im, w.re};
+            const cplx *src = out + ((size_t)r * m + k) * count;
+            cplx *dst = t + (size_t)r * count;
+            for (size_t c = 0; c < count; ++c) v_store(dst + c, v_mul(v_load(src + c), wv, ws));
+            e += k;
+            if (e >= n) e -= n;
+        }
+        /* The size-p DFT: w_n^{m r q} = w_p^{r q}, exponent (m r q mod n)
+         * advancing by m q per r. */
+        for (int q = 0; q < p; ++q) {
+            cplx *acc = y + (size_t)q * count;
+            for (size_t c = 0; c < count; ++c) acc[c] = cx(0.0, 0.0);
+            int mq = (int)((long)m * q % n);
+            for (int r = 0, e = 0; r < p; ++r) {
+                cplx w = tw[(size_t)e * step];
+                v2d wv = {w.re, w.im}, ws = {-w.im, w.re};
+                const cplx *tr = t + (size_t)r * count;
+                for (size_t c = 0; c < count; ++c) v_store(acc + c, v_load(acc + c) + v_mul(v_load(tr + c), wv, ws));
+                e += mq;
+                if (e >= n) e -= n;
+            }
+        }
+        for (int q = 0; q < p; ++q)
+            memcpy(out + ((size_t)k + (size_t)m * q) * count, y + (size_t)q * count, sizeof(cplx) * count);
+    }
 }
 
 /* Power-of-two radix-2 decimation in time over `count` interleaved
@@ -231,58 +242,58 @@ static void fft_pow2(cplx *v, size_t count, const fft_plan *plan, int inverse) {
     }
 }
 
-/* Unnormalised 1-D transform in place on contiguous values. */
-static void fft1(cplx *v, int n, int inverse, cplx *scratch) {
-    if (n <= 1) return;
+static int largest_prime_factor(int n) {
+    int largest = 1;
+    while (n > 1) {
+        int p = smallest_factor(n);
+        largest = p;
+        n /= p;
+    }
+    return largest;
+}
+
+/* Unnormalised transforms of length n in place over `count` interleaved
+ * transforms (element i of transform c at v[i count + c]). */
+static void fft_lines(cplx *v, int n, size_t count, int inverse) {
+    if (n <= 1 || count == 0) return;
     fft_plan *plan = get_plan(n);
     if (plan->pow2) {
-        fft_pow2(v, 1, plan, inverse);
+        fft_pow2(v, count, plan, inverse);
         return;
     }
-    memcpy(scratch, v, sizeof(cplx) * (size_t)n);
-    dft_rec(scratch, 1, v, n, plan, inverse);
+    size_t p = (size_t)largest_prime_factor(n);
+    cplx *work = (cplx *)malloc(sizeof(cplx) * count * ((size_t)n + 2 * p));
+    memcpy(work, v, sizeof(cplx) * (size_t)n * count);
+    dft_multi(work, count, v, n, plan, inverse, count, work + (size_t)n * count, work + ((size_t)n + p) * count);
+    free(work);
 }
 
 #define ROW_GROUP 8
 
 /* CpuBackend::fft2 (src/backend/cpu.rs:130-175): rows, then columns; the
- * forward transform is normalised by 1/(h*w) and the inverse is not. A
- * power-of-two row length transforms ROW_GROUP rows at a time, interleaved
- * in a small scratch slab; each row's arithmetic is the same as a one-row
- * transform. */
+ * forward transform is normalised by 1/(h*w) and the inverse is not. Rows
+ * are transformed ROW_GROUP at a time, interleaved in a scratch slab, and
+ * columns all at once, a whole row per element; each row's and column's
+ * arithmetic is that of a transform on its own. */
 static void fft2_c(cplx *v, int h, int w, int inverse) {
-    int longest = h > w ? h : w;
-    cplx *scratch = (cplx *)malloc(sizeof(cplx) * (size_t)longest * (2 + ROW_GROUP));
-    cplx *column = scratch + longest;
-    cplx *slab = column + longest;
-    fft_plan *row_plan = w > 1 ? get_plan(w) : NULL;
-    int r = 0;
-    if (row_plan && row_plan->pow2) {
-        for (; r + ROW_GROUP <= h; r += ROW_GROUP) {
+    if (w > 1) {
+        cplx *slab = (cplx *)malloc(sizeof(cplx) * (size_t)w * ROW_GROUP);
+        for (int r = 0; r < h; r += ROW_GROUP) {
+            int g_count = h - r < ROW_GROUP ? h - r : ROW_GROUP;
             const cplx *rows = v + (size_t)r * w;
             for (int i = 0; i < w; ++i)
-                for (int g = 0; g < ROW_GROUP; ++g) slab[(size_t)i * ROW_GROUP + g] = rows[(size_t)g * w + i];
-            fft_pow2(slab, ROW_GROUP, row_plan, inverse);
-            for (int g = 0; g < ROW_GROUP; ++g)
-                for (int i = 0; i < w; ++i) v[(size_t)(r + g) * w + i] = slab[(size_t)i * ROW_GROUP + g];
+                for (int g = 0; g < g_count; ++g) slab[(size_t)i * g_count + g] = rows[(size_t)g * w + i];
+            fft_lines(slab, w, (size_t)g_count, inverse);
+            for (int g = 0; g < g_count; ++g)
+                for (int i = 0; i < w; ++i) v[(size_t)(r + g) * w + i] = slab[(size_t)i * g_count + g];
         }
+        free(slab);
     }
-    for (; r < h; ++r) fft1(v + (size_t)r * w, w, inverse, scratch);
-    fft_plan *plan = h > 1 ? get_plan(h) : NULL;
-    if (plan && plan->pow2) {
-        fft_pow2(v, (size_t)w, plan, inverse);
-    } else {
-        for (int c = 0; c < w && h > 1; ++c) {
-            for (int r = 0; r < h; ++r) column[r] = v[(size_t)r * w + c];
-            fft1(column, h, inverse, scratch);
-            for (int r = 0; r < h; ++r) v[(size_t)r * w + c] = column[r];
-        }
-    }
+    fft_lines(v, h, (size_t)w, inverse);
     if (!inverse) {
         double norm = (double)h * (double)w;
         for (size_t i = 0; i < (size_t)h * w; ++i) v[i] = c_divr(v[i], norm);
     }
-    free(scratch);
 }
 
 int32_t orc_fft2(double *values, int32_t h, int32_t w, int32_t inverse) {
