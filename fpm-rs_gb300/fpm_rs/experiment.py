@@ -2,7 +2,7 @@
 
 Mirrors the fpm_rs Python classes of the same names
 (python/fpm_rs/__init__.pyi: Optics 1411-1480, ArrayPose 1481-1511,
-PlanarLEDArray 1512-1560, KVectorList 1764-1780, Illumination 1871-1895,
+PlanarLEDArray 1512-1560, DirectionList 1716-1763, KVectorList 1764-1780, Illumination 1871-1895,
 CameraModel 1956-2006). Resolution to k-vectors runs in the native library.
 """
 
@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 from dataclasses import dataclass, field
+from fractions import Fraction
 
 import numpy as np
 
@@ -170,39 +171,124 @@ class PlanarLEDArray:
         return ResolvedSources(np.stack([kx, ky], axis=1))
 
 
+_DIRECTION_TOLERANCE = 128.0 * np.finfo(np.float64).eps
+
+
+def _pair_rows(values, width: int, name: str) -> list:
+    """The binding's array copy (python/src/config.rs:1109-1140): a (sources,
+    width) float64 array with at least one row, else ValueError."""
+    a = np.asarray(values, dtype=np.float64)
+    if a.ndim != 2 or a.shape[1] != width or a.shape[0] == 0:
+        raise ValueError(f"{name} must have shape (sources, {width})")
+    return [[float(x) for x in row] for row in a]
+
+
+def _mul_add(a: float, b: float, c: float) -> float:
+    """f64::mul_add: a * b + c with one rounding (exact rational arithmetic,
+    then the correctly rounded conversion)."""
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def _libm(f, x: float) -> float:
+    """A libm function that, like Rust's, maps a non-finite input to NaN
+    instead of raising."""
+    return f(x) if math.isfinite(x) else math.nan
+
+
+def _direction_vectors(vectors: list, normalize: bool) -> np.ndarray:
+    """DirectionList::from_vectors (src/experiment/illumination.rs:91-126)."""
+    out = []
+    for x, y, z in vectors:
+        if not (math.isfinite(x) and math.isfinite(y) and math.isfinite(z)):
+            raise InvalidParameterError("unit_vectors: components must be finite")
+        norm = float(np.hypot(np.hypot(x, y), z))
+        if not math.isfinite(norm) or norm <= 0.0:
+            raise InvalidParameterError("unit_vectors: vectors must have non-zero finite norm")
+        if normalize:
+            x, y, z = x / norm, y / norm, z / norm
+        elif abs(norm - 1.0) > _DIRECTION_TOLERANCE:
+            raise InvalidParameterError("unit_vectors: vectors must be normalized")
+        if z < -_DIRECTION_TOLERANCE:
+            raise InvalidParameterError("unit_vectors: directions must lie in the positive-z illumination hemisphere")
+        out.append([x, y, max(z, 0.0)])
+    return np.array(out, dtype=np.float64)
+
+
+def _transverse_directions(pairs: list, component) -> np.ndarray:
+    """from_transverse_components (src/experiment/illumination.rs:173-192):
+    (dx, dy) = component of each pair, z = sqrt(max(1 - (dx^2 + dy^2), 0))
+    with the magnitude formed by one fused multiply-add."""
+    vectors = []
+    for x, y in pairs:
+        if not (math.isfinite(x) and math.isfinite(y)):
+            raise InvalidParameterError("directions: components must be finite")
+        dx, dy = component(x), component(y)
+        squared = _mul_add(dx, dx, dy * dy)
+        if squared > 1.0 + _DIRECTION_TOLERANCE:
+            raise InvalidParameterError("directions: squared transverse direction magnitude cannot exceed one")
+        vectors.append([dx, dy, math.sqrt(max(1.0 - squared, 0.0))])
+    return _direction_vectors(vectors, False)
+
+
 class DirectionList:
     """Illumination propagation directions (src/experiment/illumination.rs:76-254),
     stored as unit vectors with non-negative z; resolves to k * (ux, uy)
-    with k = 2 pi n_illumination / wavelength."""
+    with k = 2 pi n_illumination / wavelength. Constructors and getters follow
+    python/src/config.rs:483-570."""
 
     def __init__(self, unit_vectors):
-        u = np.array(unit_vectors, dtype=np.float64)
-        if u.ndim != 2 or u.shape[1] != 3 or u.shape[0] == 0:
-            raise InvalidParameterError("unit_vectors: at least one (x, y, z) direction is required")
-        if not np.all(np.isfinite(u)):
-            raise InvalidParameterError("unit_vectors: components must be finite")
-        norm = np.sqrt(np.sum(u * u, axis=1))
-        if np.any(np.abs(norm - 1.0) > 128.0 * np.finfo(np.float64).eps):
-            raise InvalidParameterError("unit_vectors: vectors must be normalized")
-        if np.any(u[:, 2] < -128.0 * np.finfo(np.float64).eps):
-            raise InvalidParameterError("unit_vectors: directions must lie in the positive-z illumination hemisphere")
-        u[:, 2] = np.maximum(u[:, 2], 0.0)
-        self._u = u
+        self._u = _direction_vectors(_pair_rows(unit_vectors, 3, "unit_vectors"), False)
 
     @staticmethod
-    def from_unit_vectors(*, values) -> "DirectionList":
+    def _of(unit_vectors: np.ndarray) -> "DirectionList":
+        directions = DirectionList.__new__(DirectionList)
+        directions._u = unit_vectors
+        return directions
+
+    @staticmethod
+    def from_unit_vectors(values) -> "DirectionList":
         return DirectionList(values)
 
     @staticmethod
-    def from_direction_cosines(*, values) -> "DirectionList":
-        """Transverse direction cosines (dx, dy); z = sqrt(1 - dx^2 - dy^2)."""
-        d = np.asarray(values, dtype=np.float64).reshape(-1, 2)
-        if not np.all(np.isfinite(d)):
-            raise InvalidParameterError("directions: components must be finite")
-        t = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]
-        if np.any(t > 1.0 + 128.0 * np.finfo(np.float64).eps):
-            raise InvalidParameterError("directions: squared transverse direction magnitude cannot exceed one")
-        return DirectionList(np.stack([d[:, 0], d[:, 1], np.sqrt(np.maximum(1.0 - t, 0.0))], axis=1))
+    def from_vectors(values, *, normalize: bool = True) -> "DirectionList":
+        """Vectors of any non-zero length, each divided by its norm when
+        `normalize` (else they must already be unit length)."""
+        return DirectionList._of(_direction_vectors(_pair_rows(values, 3, "vectors"), bool(normalize)))
+
+    @staticmethod
+    def from_direction_cosines(values) -> "DirectionList":
+        """Transverse direction cosines (dx, dy)."""
+        return DirectionList._of(_transverse_directions(_pair_rows(values, 2, "directions"), lambda v: v))
+
+    @staticmethod
+    def from_component_angles_radians(values) -> "DirectionList":
+        """Independent component angles (theta_x, theta_y): (sin theta_x, sin theta_y)."""
+        return DirectionList._of(_transverse_directions(_pair_rows(values, 2, "directions"),
+                                                        lambda v: _libm(math.sin, v)))
+
+    @staticmethod
+    def from_component_angles_degrees(values) -> "DirectionList":
+        pairs = [[math.radians(x), math.radians(y)] for x, y in _pair_rows(values, 2, "directions")]
+        return DirectionList._of(_transverse_directions(pairs, lambda v: _libm(math.sin, v)))
+
+    @staticmethod
+    def from_polar_angles_radians(values) -> "DirectionList":
+        """Polar angle theta and azimuth phi: (sin theta cos phi, sin theta sin phi, cos theta)."""
+        return DirectionList._of(DirectionList._polar(_pair_rows(values, 2, "directions")))
+
+    @staticmethod
+    def from_polar_angles_degrees(values) -> "DirectionList":
+        pairs = [[math.radians(t), math.radians(f)] for t, f in _pair_rows(values, 2, "directions")]
+        return DirectionList._of(DirectionList._polar(pairs))
+
+    @staticmethod
+    def _polar(pairs: list) -> np.ndarray:
+        vectors = []
+        for theta, phi in pairs:
+            st, ct = _libm(math.sin, theta), _libm(math.cos, theta)
+            sp, cp = _libm(math.sin, phi), _libm(math.cos, phi)
+            vectors.append([st * cp, st * sp, ct])
+        return _direction_vectors(vectors, False)
 
     @property
     def source_count(self) -> int:
@@ -211,6 +297,29 @@ class DirectionList:
     @property
     def unit_vectors(self) -> np.ndarray:
         return self._u.copy()
+
+    @property
+    def direction_cosines(self) -> np.ndarray:
+        return self._u[:, :2].copy()
+
+    @property
+    def component_angles_rad(self) -> np.ndarray:
+        return np.array([[math.asin(x), math.asin(y)] for x, y, _ in self._u], dtype=np.float64).reshape(-1, 2)
+
+    @property
+    def component_angles_deg(self) -> np.ndarray:
+        return np.array([[math.degrees(x), math.degrees(y)] for x, y in self.component_angles_rad],
+                        dtype=np.float64).reshape(-1, 2)
+
+    @property
+    def polar_angles_rad(self) -> np.ndarray:
+        return np.array([[math.acos(min(max(z, -1.0), 1.0)), math.atan2(y, x)] for x, y, z in self._u],
+                        dtype=np.float64).reshape(-1, 2)
+
+    @property
+    def polar_angles_deg(self) -> np.ndarray:
+        return np.array([[math.degrees(t), math.degrees(f)] for t, f in self.polar_angles_rad],
+                        dtype=np.float64).reshape(-1, 2)
 
     def resolve(self, optics: Optics) -> ResolvedSources:
         optics._validate()

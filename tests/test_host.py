@@ -5,8 +5,10 @@ mapping, and unsupported options failing before any device work."""
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import re
+from fractions import Fraction
 
 import numpy as np
 import pytest
@@ -96,8 +98,6 @@ def test_coherent_sampling_is_strict_at_the_nyquist_boundary(fpm):
     # tests/geometry_tests.rs:26-65: pitch 4 / 2 equals 1 / (2 * 0.25) exactly;
     # the boundary itself is refused with the reference's wording, one ulp
     # below passes and one ulp above is refused.
-    import math
-
     assert abs(fpm.Optics(532e-9, 0.1, 4.0, 6.5e-6).object_pixel_size - 1.625e-6) <= 1e-18
     with pytest.raises(fpm.InvalidParameterError) as info:
         fpm.Optics(1.0, 0.25, 2.0, 4.0)
@@ -216,6 +216,67 @@ def test_checkpoint_json_round_trip(fpm, tmp_path):
     with pytest.raises(OverflowError):
         fpm.CheckpointEvery(-1, tmp_path)
     assert fpm.CheckpointEvery(2, tmp_path).path_for(2).name == "checkpoint_00002.json"
+
+
+def test_direction_constructors_and_accessors_round_trip(fpm):
+    # tests/geometry_tests.rs:309-333, with `values` positional as the
+    # binding takes it (python/src/config.rs:490-551).
+    cosines = [[0.1, -0.2], [0.0, 0.0]]
+    directions = fpm.DirectionList.from_direction_cosines(np.array(cosines))
+    assert np.abs(directions.direction_cosines - cosines).max() <= 1e-12
+    component = fpm.DirectionList.from_component_angles_degrees(np.array([[10.0, -5.0]]))
+    assert np.abs(component.component_angles_deg[0] - [10.0, -5.0]).max() <= 1e-12
+    polar = fpm.DirectionList.from_polar_angles_degrees(np.array([[30.0, 120.0]]))
+    assert np.abs(polar.polar_angles_deg[0] - [30.0, 120.0]).max() <= 1e-12
+    normalized = fpm.DirectionList.from_vectors(np.array([[0.0, 0.0, 2.0]]))
+    assert np.array_equal(normalized.unit_vectors, [[0.0, 0.0, 1.0]])
+    for bad in (lambda: fpm.DirectionList.from_unit_vectors(np.array([[0.0, 0.0, 2.0]])),
+                lambda: fpm.DirectionList.from_direction_cosines(np.array([[0.8, 0.8]])),
+                lambda: fpm.DirectionList.from_unit_vectors(np.array([[0.0, 0.0, -1.0]]))):
+        with pytest.raises(fpm.InvalidParameterError):
+            bad()
+
+
+def test_direction_list_angular_forms_shapes_and_arithmetic(fpm):
+    # python/tests/test_configuration.py:212-218.
+    polar = fpm.DirectionList.from_polar_angles_degrees(np.array([[0.0, 0.0], [30.0, 120.0]]))
+    np.testing.assert_allclose(polar.polar_angles_deg, [[0.0, 0.0], [30.0, 120.0]], atol=1e-12)
+    assert polar.source_count == 2 and polar.polar_angles_rad.shape == (2, 2)
+    # Component angles map through sin; polar angles through (sin t cos p, sin t sin p, cos t)
+    # (src/experiment/illumination.rs:133-171).
+    angles = np.array([[0.01, -0.02], [0.3, 0.1]])
+    component = fpm.DirectionList.from_component_angles_radians(angles)
+    assert np.array_equal(component.direction_cosines, np.vectorize(math.sin)(angles))
+    np.testing.assert_allclose(component.component_angles_rad, angles, atol=1e-15)
+    t, p = 0.4, -2.0
+    u = fpm.DirectionList.from_polar_angles_radians(np.array([[t, p]])).unit_vectors[0]
+    assert u.tolist() == [math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)]
+    # The transverse magnitude is one fused multiply-add (f64::mul_add), so
+    # z = sqrt(1 - (dx^2 + dy^2)) is rounded as the reference rounds it.
+    dx, dy = 0.1, 0.7
+    fused = float(Fraction(dx) * Fraction(dx) + Fraction(dy * dy))
+    z = fpm.DirectionList.from_direction_cosines(np.array([[dx, dy]])).unit_vectors[0, 2]
+    assert z == math.sqrt(1.0 - fused)
+    # Binding shape checks (python/src/config.rs:1109-1140) raise ValueError.
+    for bad in (lambda: fpm.DirectionList(np.zeros((2, 2))), lambda: fpm.DirectionList.from_vectors(np.zeros((1, 2))),
+                lambda: fpm.DirectionList.from_direction_cosines(np.zeros((0, 2)))):
+        with pytest.raises(ValueError):
+            bad()
+    # Without normalisation a vector must be unit length; a zero or non-finite one is refused either way.
+    for bad in (lambda: fpm.DirectionList.from_vectors(np.array([[0.0, 0.0, 2.0]]), normalize=False),
+                lambda: fpm.DirectionList.from_vectors(np.zeros((1, 3))),
+                lambda: fpm.DirectionList.from_polar_angles_radians(np.array([[np.inf, 0.0]]))):
+        with pytest.raises(fpm.InvalidParameterError):
+            bad()
+
+
+def test_component_angle_directions_compile(fpm):
+    # python/tests/test_configuration.py:97-103,168-175: two sources, two frames.
+    optics = fpm.Optics(532e-9, 0.10, 4.0, 6.5e-6)
+    illumination = fpm.Illumination(fpm.DirectionList.from_component_angles_radians(np.array([[0.0, 0.0],
+                                                                                             [0.01, -0.01]])))
+    model = fpm.compile_model(optics, illumination, (8, 8), (16, 16))
+    assert model.source_count == 2 and model.frame_count == 2
 
 
 def test_direction_and_kvector_resolution_use_the_illumination_index(fpm):
