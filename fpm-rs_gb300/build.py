@@ -22,8 +22,12 @@ SOURCES = ["engine_n256.cu", "engine_n256_gd.cu", "engine_n128.cu", "engine_n128
            "engine_n64_gd.cu", "engine_n32.cu", "engine_n32_gd.cu", "engine.cu", "engine_l2.cu", "grid.cu", "camera.cu", "noalloc.cu", "runtime.cpp", "server.cpp"]
 HEADERS = ["fpm_common.cuh", "kernels.h", "twiddle256.cuh", "engine_impl.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+# Host code is compiled without floating-point contraction: GCC would otherwise
+# fuse a * b + c into one rounding wherever the target has FMA (always on
+# aarch64), and the model compilation (pose rotation, k-vectors, crop offsets)
+# must round as the reference does, on every host architecture.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 
 def nvcc() -> str:
