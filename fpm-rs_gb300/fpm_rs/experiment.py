@@ -119,8 +119,14 @@ class ArrayPose:
 
 
 class ResolvedSources:
-    def __init__(self, k_vectors: np.ndarray):
+    """Resolved sources (src/experiment/illumination.rs:377-440): transverse
+    k-vectors, propagation unit vectors, and source positions for physical
+    geometries (None for direction and k-vector lists)."""
+
+    def __init__(self, k_vectors: np.ndarray, directions: np.ndarray, positions_m: np.ndarray | None = None):
         self._k = np.ascontiguousarray(k_vectors, dtype=np.float64)
+        self._directions = np.ascontiguousarray(directions, dtype=np.float64)
+        self._positions = None if positions_m is None else np.ascontiguousarray(positions_m, dtype=np.float64)
 
     @property
     def source_count(self) -> int:
@@ -129,6 +135,14 @@ class ResolvedSources:
     @property
     def k_vectors(self) -> np.ndarray:
         return self._k.copy()
+
+    @property
+    def directions(self) -> np.ndarray:
+        return self._directions.copy()
+
+    @property
+    def positions_m(self) -> np.ndarray | None:
+        return None if self._positions is None else self._positions.copy()
 
 
 class PlanarLEDArray:
@@ -146,6 +160,14 @@ class PlanarLEDArray:
             raise UnsupportedError("position_offsets_m is not supported on the GB300 device path")
         if self.shape[0] <= 0 or self.shape[1] <= 0:
             raise InvalidParameterError("shape rows and columns must be non-zero")
+        self._offsets = (np.zeros((0, 3)) if position_offsets_m is None
+                         else np.array(position_offsets_m, dtype=np.float64).reshape(-1, 3))
+
+    @property
+    def position_offsets_m(self) -> np.ndarray:
+        """Per-LED offsets (src/experiment/led_array.rs:202-204): empty unless
+        given; only zero offsets are accepted here."""
+        return self._offsets.copy()
 
     @property
     def source_count(self) -> int:
@@ -168,7 +190,30 @@ class PlanarLEDArray:
             C.byref(o), self.shape[0], self.shape[1], C.c_double(self.pitch_m[0]), C.c_double(self.pitch_m[1]),
             C.c_double(self.reference_index[0]), C.c_double(self.reference_index[1]),
             N.ptr(t, C.c_double), N.ptr(r, C.c_double), N.ptr(kx, C.c_double), N.ptr(ky, C.c_double)))
-        return ResolvedSources(np.stack([kx, ky], axis=1))
+        positions, directions = self._positions_and_directions()
+        return ResolvedSources(np.stack([kx, ky], axis=1), directions, positions)
+
+    def _positions_and_directions(self):
+        """LED positions and source-to-sample directions for the getters
+        (led_array.rs:292-313, illumination.rs:385-410): the native
+        compilation's operations, in its order and unfused, so k times a
+        direction reproduces its k-vector bit for bit."""
+        sx, cx = math.sin(self.pose.rotation_rad[0]), math.cos(self.pose.rotation_rad[0])
+        sy, cy = math.sin(self.pose.rotation_rad[1]), math.cos(self.pose.rotation_rad[1])
+        sz, cz = math.sin(self.pose.rotation_rad[2]), math.cos(self.pose.rotation_rad[2])
+        t = [float(v) for v in self.pose.translation_m]
+        positions, directions = [], []
+        for r in range(self.shape[0]):
+            for c in range(self.shape[1]):
+                p = ((c - self.reference_index[0]) * self.pitch_m[0], (r - self.reference_index[1]) * self.pitch_m[1], 0.0)
+                ax = (p[0], cx * p[1] - sx * p[2], sx * p[1] + cx * p[2])
+                ay = (cy * ax[0] + sy * ax[2], ax[1], -sy * ax[0] + cy * ax[2])
+                az = (cz * ay[0] - sz * ay[1], sz * ay[0] + cz * ay[1], ay[2])
+                pos = (az[0] + t[0], az[1] + t[1], az[2] + t[2])
+                norm = float(np.hypot(np.hypot(pos[0], pos[1]), pos[2]))
+                positions.append(pos)
+                directions.append((-pos[0] / norm, -pos[1] / norm, -pos[2] / norm))
+        return np.array(positions, dtype=np.float64), np.array(directions, dtype=np.float64)
 
 
 _DIRECTION_TOLERANCE = 128.0 * np.finfo(np.float64).eps
@@ -324,7 +369,7 @@ class DirectionList:
     def resolve(self, optics: Optics) -> ResolvedSources:
         optics._validate()
         k = 2.0 * math.pi * optics.illumination_refractive_index / optics.wavelength_vacuum_m
-        return ResolvedSources(np.stack([k * self._u[:, 0], k * self._u[:, 1]], axis=1))
+        return ResolvedSources(np.stack([k * self._u[:, 0], k * self._u[:, 1]], axis=1), self._u)
 
 
 class KVectorList:
@@ -354,7 +399,13 @@ class KVectorList:
         if np.any(np.hypot(self._k[:, 0], self._k[:, 1]) > k * (1.0 + 128.0 * np.finfo(np.float64).eps)):
             raise InvalidParameterError("k_vectors: vectors must be finite and propagating at the configured vacuum "
                                         "wavelength and illumination refractive index")
-        return ResolvedSources(self._k)
+        # KVectorList::resolve (src/experiment/illumination.rs:282-299): the
+        # direction of (kx, ky) at the illumination wavenumber.
+        directions = []
+        for kx, ky in self._k:
+            dx, dy = float(kx) / k, float(ky) / k
+            directions.append([dx, dy, math.sqrt(max(1.0 - _mul_add(dx, dx, dy * dy), 0.0))])
+        return ResolvedSources(self._k, np.array(directions, dtype=np.float64))
 
 
 class Illumination:
@@ -365,6 +416,10 @@ class Illumination:
             raise UnsupportedError(
                 "source calibration and multiplexed acquisition plans are not supported on the GB300 device path")
         self.geometry = geometry
+        # The unit calibration and the sequential all-sources plan, which are
+        # the only ones the device path takes, read as None.
+        self.calibration = None
+        self.acquisition = None
 
     def resolve(self, optics: Optics) -> ResolvedSources:
         return self.geometry.resolve(optics)

@@ -55,6 +55,10 @@ class MeasurementStack:
     def frame_count(self) -> int:
         return self._data.shape[0]
 
+    def __len__(self) -> int:
+        """The frame count (python/src/measurements.rs:118-120)."""
+        return self._data.shape[0]
+
     @property
     def image_shape(self):
         return self._data.shape[1:]

@@ -270,6 +270,32 @@ def test_direction_list_angular_forms_shapes_and_arithmetic(fpm):
             bad()
 
 
+def test_resolved_sources_directions_and_positions(fpm):
+    # ResolvedSources getters (python/src/config.rs:913-935): LED arrays carry
+    # positions and source-to-sample directions whose k-multiples are the
+    # compiled k-vectors bit for bit; direction and k-vector lists carry no
+    # positions (illumination.rs:240-299).
+    optics = fpm.Optics(**W.OPTICS)
+    pose = fpm.ArrayPose.from_translation_and_extrinsic_xyz_degrees((1e-3, -2e-3, -85e-3), (2.0, -1.0, 15.0))
+    array = fpm.PlanarLEDArray((5, 7), (4e-3, 3.5e-3), (3.2, 1.7), pose)
+    resolved = array.resolve(optics)
+    k = 2.0 * math.pi * optics.illumination_refractive_index / optics.wavelength_vacuum_m
+    assert resolved.positions_m.shape == (35, 3) and resolved.directions.shape == (35, 3)
+    assert np.array_equal(k * resolved.directions[:, :2], resolved.k_vectors)
+    assert np.allclose(np.linalg.norm(resolved.directions, axis=1), 1.0, atol=1e-15)
+    assert np.allclose(resolved.directions, -resolved.positions_m / np.linalg.norm(resolved.positions_m, axis=1)[:, None])
+    assert array.position_offsets_m.shape == (0, 3)
+    directions = fpm.DirectionList.from_direction_cosines(np.array([[0.25, -0.5]]))
+    from_directions = directions.resolve(optics)
+    assert from_directions.positions_m is None and np.array_equal(from_directions.directions, directions.unit_vectors)
+    from_k = fpm.KVectorList(from_directions.k_vectors).resolve(optics)
+    assert from_k.positions_m is None
+    assert np.abs(from_k.directions - directions.unit_vectors).max() <= 1e-15
+    illumination = fpm.Illumination(array)
+    assert illumination.geometry is array and illumination.calibration is None and illumination.acquisition is None
+    assert len(fpm.MeasurementStack(np.ones((9, 4, 4)))) == 9
+
+
 def test_component_angle_directions_compile(fpm):
     # python/tests/test_configuration.py:97-103,168-175: two sources, two frames.
     optics = fpm.Optics(532e-9, 0.10, 4.0, 6.5e-6)
