@@ -3306,6 +3306,46 @@ int32_t fpm_planar_led_kvectors(const fpm_optics* optics, int32_t rows, int32_t 
     return finish(nullptr, body());
 }
 
+// The objective's data term on host intensities (loss and point_loss,
+// src/algorithms/objective.rs:27-72): per-value losses summed in order in
+// FP64, then divided by the count. Amplitude, Poisson and Huber losses clamp
+// negative intensities to zero.
+int32_t fpm_intensity_loss(const double* predicted, const double* measured, int64_t count, int32_t loss_type,
+                           double* out) {
+    auto body = [&]() -> Status {
+        if (!predicted || !measured || !out) return Status::make(FPM_ERR_INVALID_PARAMETER, "null argument");
+        if (loss_type < FPM_LOSS_AMPLITUDE_MSE || loss_type > FPM_LOSS_HUBER_AMPLITUDE)
+            return Status::make(FPM_ERR_INVALID_PARAMETER, "unknown loss_type %d", loss_type);
+        if (count <= 0)
+            return Status::make(FPM_ERR_INVALID_SHAPE, "loss inputs have lengths %lld and %lld", (long long)count,
+                                (long long)count);
+        double sum = 0.0;
+        for (int64_t i = 0; i < count; ++i) {
+            const double p = predicted[i], m = measured[i];
+            if (!std::isfinite(p) || !std::isfinite(m))
+                return Status::make(FPM_ERR_NUMERICAL, "loss input contains a non-finite value");
+            double term;
+            if (loss_type == FPM_LOSS_INTENSITY_MSE) {
+                const double r = p - m;
+                term = r * r;
+            } else if (loss_type == FPM_LOSS_POISSON_NLL) {
+                const double mean = std::max(p, 1e-12);
+                term = mean - std::max(m, 0.0) * std::log(mean);
+            } else {
+                const double r = std::sqrt(std::max(p, 0.0)) - std::sqrt(std::max(m, 0.0));
+                if (loss_type == FPM_LOSS_AMPLITUDE_MSE)
+                    term = r * r;
+                else
+                    term = std::fabs(r) <= 1.0 ? 0.5 * r * r : std::fabs(r) - 0.5;
+            }
+            sum += term;
+        }
+        *out = sum / (double)count;
+        return Status::ok();
+    };
+    return finish(nullptr, body());
+}
+
 int32_t fpm_suggest_shape(const fpm_optics* optics, int32_t sources, const double* kx, const double* ky,
                           int32_t image_height, int32_t image_width, int32_t policy, int32_t* recon_height,
                           int32_t* recon_width) {

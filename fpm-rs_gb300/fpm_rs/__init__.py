@@ -19,6 +19,7 @@ from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasure
 from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedSources)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
+from .objective import intensity_loss
 from .callbacks import (Callback, CsvLogger, IterationCallback, ProgressLogger, SaveImageEvery, SavePupilEvery,
                         SaveResidualsEvery, StepContext, StopOnPlateau)
 from .checkpoint import CheckpointEvery, ReconstructionCheckpoint
@@ -62,4 +63,5 @@ __all__ = [
     "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob", "RunPlan",
     "capture_batch", "Server", "Request", "ServerBusyError", "Callback", "CsvLogger", "IterationCallback",
     "ProgressLogger", "SaveImageEvery", "SavePupilEvery", "SaveResidualsEvery", "StepContext", "StopOnPlateau",
+    "intensity_loss",
 ]

@@ -23,7 +23,7 @@ LIB_PATH = os.environ.get("FPM_GPU_LIBRARY", os.path.join(PACKAGE_ROOT, "libfpm_
 
 EXPORTED = (
     "fpm_create", "fpm_destroy", "fpm_last_error", "fpm_global_last_error",
-    "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model",
+    "fpm_planar_led_kvectors", "fpm_suggest_shape", "fpm_compile_model", "fpm_intensity_loss",
     "fpm_fft2", "fpm_forward_stack", "fpm_simulate_stack", "fpm_problem_create", "fpm_problem_create_batch", "fpm_problem_destroy",
     "fpm_run", "fpm_run_batch", "fpm_run_batch_host", "fpm_run_batch_resumable", "fpm_last_run_stats",
     "fpm_spectral_run", "fpm_spectral_run_batch", "fpm_spectral_forward",

@@ -215,6 +215,12 @@ int32_t fpm_planar_led_kvectors(const fpm_optics *optics, int32_t rows, int32_t 
 int32_t fpm_suggest_shape(const fpm_optics *optics, int32_t sources, const double *kx, const double *ky,
                           int32_t image_height, int32_t image_width, int32_t policy, int32_t *recon_height,
                           int32_t *recon_width);
+/* Mean loss (FPM_LOSS_*) between count > 0 finite predicted and measured
+ * intensities, summed in order in FP64 on the host: the objective's data term
+ * (src/algorithms/objective.rs:27-72), which the Python binding exposes as
+ * intensity_loss (python/src/metrics.rs:248-269). */
+int32_t fpm_intensity_loss(const double *predicted, const double *measured, int64_t count, int32_t loss_type,
+                           double *out);
 /* Compiles k-vectors into crops, fractional offsets and the circular pupil.
  * Caller allocates start_row/start_col/offset_row/offset_col [sources],
  * pupil [2*h*w] and support [h*w]. For FPM_SHAPE_EXACT the shape is read from

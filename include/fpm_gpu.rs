@@ -83,6 +83,8 @@ extern "C" {
         kx: *mut f64, ky: *mut f64) -> i32;
     pub fn fpm_suggest_shape(optics: *const FpmOptics, sources: i32, kx: *const f64, ky: *const f64,
         image_height: i32, image_width: i32, policy: i32, recon_height: *mut i32, recon_width: *mut i32) -> i32;
+    pub fn fpm_intensity_loss(predicted: *const f64, measured: *const f64, count: i64, loss_type: i32,
+        out: *mut f64) -> i32;
     pub fn fpm_compile_model(optics: *const FpmOptics, sources: i32, kx: *const f64, ky: *const f64,
         image_height: i32, image_width: i32, policy: i32, recon_height: *mut i32, recon_width: *mut i32,
         start_row: *mut i64, start_col: *mut i64, offset_row: *mut f64, offset_col: *mut f64, pupil: *mut f64,

@@ -317,3 +317,59 @@ def test_direction_and_kvector_resolution_use_the_illumination_index(fpm):
     k_glass = 2 * np.pi * 1.5 / 532e-9
     with pytest.raises(fpm.InvalidParameterError):
         fpm.KVectorList([[k_glass * 1.01, 0.0]]).resolve(glass_optics)
+
+
+LOSS_TYPES = ("amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude")
+
+
+def _loss_in_order(predicted, measured, loss_type):
+    """objective.rs:27-72 restated with NumPy per value and an in-order sum."""
+    p, m = predicted.ravel(), measured.ravel()
+    if loss_type == "intensity_mse":
+        terms = (p - m) * (p - m)
+    elif loss_type == "poisson_nll":
+        mean = np.maximum(p, 1e-12)
+        terms = mean - np.maximum(m, 0.0) * np.array([math.log(v) for v in mean])
+    else:
+        r = np.sqrt(np.maximum(p, 0.0)) - np.sqrt(np.maximum(m, 0.0))
+        terms = r * r if loss_type == "amplitude_mse" else np.where(np.abs(r) <= 1.0, 0.5 * r * r, np.abs(r) - 0.5)
+    return np.cumsum(np.concatenate(([0.0], terms)))[-1] / p.size
+
+
+def test_intensity_loss_known_values_and_errors(fpm):
+    # tests/diagnostics_tests.rs:33-64, through the binding's argument order
+    # intensity_loss(reference = measured, candidate = predicted).
+    measured, predicted = np.array([[1.0]]), np.array([[4.0]])
+    assert fpm.intensity_loss(measured, predicted, "amplitude_mse") == 1.0
+    assert fpm.intensity_loss(measured, predicted, "intensity_mse") == 9.0
+    assert fpm.intensity_loss(measured, predicted, "huber_amplitude") == 0.5
+    assert fpm.intensity_loss(measured, predicted, "poisson_nll") == 4.0 - math.log(4.0)
+    with pytest.raises(fpm.InvalidShapeError):
+        fpm.intensity_loss(np.zeros((0, 2)), np.zeros((0, 2)), "amplitude_mse")
+    with pytest.raises(ValueError):
+        fpm.intensity_loss(np.ones((1, 1)), np.ones((1, 2)), "amplitude_mse")
+    with pytest.raises(fpm.NumericalError):
+        fpm.intensity_loss(np.ones((1, 1)), np.array([[np.nan]]), "amplitude_mse")
+    with pytest.raises(ValueError):
+        fpm.intensity_loss(np.ones((1, 1)), np.ones((1, 1)), "l1")
+    # python/src/metrics.rs:256: only the value counts must agree.
+    assert fpm.intensity_loss(np.ones((1, 2)), np.full((2, 1), 4.0), "intensity_mse") == 9.0
+
+
+@pytest.mark.parametrize("loss_type", LOSS_TYPES)
+def test_intensity_loss_sums_in_order_and_matches_the_oracle_frame_loss(fpm, loss_type):
+    import helpers
+
+    rng = np.random.default_rng(5)
+    measured = rng.normal(4.0, 3.0, (64, 48))  # some negative values, which the clamps see
+    predicted = rng.normal(4.0, 3.0, (64, 48))
+    assert fpm.intensity_loss(measured, predicted, loss_type) == _loss_in_order(predicted, measured, loss_type)
+    # One frame of the forward model against its Poisson counts: the oracle's
+    # frame loss (ImagePlaneForwardModel::frame_loss, src/model/forward.rs:475-489).
+    model, omodel = helpers.planar_model(fpm, 3, 32)
+    spectrum = oracle.object_spectrum(W.smooth_random_object(model.reconstruction_shape, 9))
+    stack = oracle.forward_stack(oracle.Problem(omodel, None), spectrum)
+    counts = rng.poisson(stack * 50.0) / 50.0
+    want = oracle.frame_loss(oracle.Problem(omodel, counts), spectrum, omodel["pupil"], 4, loss_type)
+    got = fpm.intensity_loss(counts[4], stack[4], loss_type)
+    assert abs(got - want) <= 1e-12 * abs(want)
