@@ -112,9 +112,10 @@ static int smallest_factor(int n) {
 }
 
 /* Two doubles (re, im) as one GCC vector value: portable C (the vector
- * extension, no target intrinsics), unaligned-safe loads and stores. */
+ * extension, no target intrinsics). Loads and stores go through a type that
+ * may sit at 8-byte alignment and may alias the cplx values it reads. */
 typedef double v2d __attribute__((vector_size(16)));
-typedef double v2d_u __attribute__((vector_size(16), aligned(8)));
+typedef double v2d_u __attribute__((vector_size(16), aligned(8), may_alias));
 
 static inline v2d v_load(const cplx *p) { return *(const v2d_u *)p; }
 static inline void v_store(cplx *p, v2d v) { *(v2d_u *)p = v; }
