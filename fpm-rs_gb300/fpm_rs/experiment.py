@@ -408,6 +408,77 @@ class KVectorList:
         return ResolvedSources(self._k, np.array(directions, dtype=np.float64))
 
 
+class SourceContribution:
+    """One source's intensity weight within a frame (python/src/config.rs:694-722)."""
+
+    def __init__(self, source: int, intensity_weight: float):
+        self.source = int(source)
+        self.intensity_weight = float(intensity_weight)
+
+
+class ResolvedFrame:
+    """A frame's source contributions and gain (src/experiment/illumination.rs:764-775)."""
+
+    def __init__(self, contributions: list, gain: float):
+        self.contributions = list(contributions)
+        self.gain = float(gain)
+
+
+class ResolvedIllumination:
+    """Resolved sources plus the acquisition (src/experiment/illumination.rs:784-852).
+
+    The device path takes only the unit calibration and the sequential
+    all-sources plan, so frame f holds source f alone at unit weight, and
+    source powers and frame gains are one."""
+
+    def __init__(self, sources: ResolvedSources):
+        self._sources = sources
+
+    @property
+    def sources(self) -> ResolvedSources:
+        return self._sources
+
+    @property
+    def source_count(self) -> int:
+        return self._sources.source_count
+
+    @property
+    def frame_count(self) -> int:
+        return self._sources.source_count
+
+    @property
+    def is_multiplexed(self) -> bool:
+        return False
+
+    @property
+    def frames(self) -> list:
+        return [ResolvedFrame([SourceContribution(f, 1.0)], 1.0) for f in range(self.frame_count)]
+
+    @property
+    def source_power(self) -> np.ndarray:
+        return np.ones(self.source_count)
+
+    @property
+    def frame_gains(self) -> np.ndarray:
+        return np.ones(self.frame_count)
+
+    @property
+    def directions(self) -> np.ndarray:
+        return self._sources.directions
+
+    @property
+    def positions_m(self):
+        return self._sources.positions_m
+
+    @property
+    def k_vectors(self) -> np.ndarray:
+        return self._sources.k_vectors
+
+    @property
+    def dense_weights(self) -> np.ndarray:
+        return np.eye(self.frame_count, self.source_count)
+
+
 class Illumination:
     """Geometry plus (unit) calibration and the all-sources sequential acquisition."""
 
@@ -421,8 +492,8 @@ class Illumination:
         self.calibration = None
         self.acquisition = None
 
-    def resolve(self, optics: Optics) -> ResolvedSources:
-        return self.geometry.resolve(optics)
+    def resolve(self, optics: Optics) -> ResolvedIllumination:
+        return ResolvedIllumination(self.geometry.resolve(optics))
 
 
 @dataclass

@@ -294,6 +294,17 @@ def test_resolved_sources_directions_and_positions(fpm):
     illumination = fpm.Illumination(array)
     assert illumination.geometry is array and illumination.calibration is None and illumination.acquisition is None
     assert len(fpm.MeasurementStack(np.ones((9, 4, 4)))) == 9
+    # ResolvedIllumination (python/src/config.rs:968-1041, as
+    # python/tests/test_configuration.py:189-205 reads it) under the unit
+    # calibration and the sequential plan: frame f is source f at unit weight.
+    lit = fpm.Illumination(fpm.KVectorList(np.array([[0.0, 0.0], [1.0e4, 0.0]]))).resolve(optics)
+    assert lit.directions.shape == (2, 3) and lit.k_vectors.shape == (2, 2) and lit.positions_m is None
+    assert lit.source_count == 2 and lit.frame_count == 2 and not lit.is_multiplexed
+    assert np.array_equal(lit.source_power, [1.0, 1.0]) and np.array_equal(lit.frame_gains, [1.0, 1.0])
+    assert np.array_equal(lit.dense_weights, [[1.0, 0.0], [0.0, 1.0]])
+    assert [(c.source, c.intensity_weight) for f in lit.frames for c in f.contributions] == [(0, 1.0), (1, 1.0)]
+    assert np.array_equal(lit.sources.k_vectors, lit.k_vectors)
+    assert np.array_equal(illumination.resolve(optics).k_vectors, resolved.k_vectors)
 
 
 def test_component_angle_directions_compile(fpm):
