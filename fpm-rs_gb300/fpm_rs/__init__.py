@@ -17,7 +17,8 @@ from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasure
                      InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
                      ServerBusyError, UnsupportedError)
 from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
-                         PupilAberration, ResolvedFrame, ResolvedIllumination, ResolvedSources, SourceContribution)
+                         PupilAberration, ResolvedFrame, ResolvedIllumination, ResolvedSources, SourceContribution,
+                         SourcePositionList)
 from .model import ImagePlaneModel, compile_camera_model, compile_model, suggest_reconstruction_shape
 from .objective import intensity_loss
 from .callbacks import (Callback, CsvLogger, IterationCallback, ProgressLogger, SaveImageEvery, SavePupilEvery,
@@ -63,5 +64,5 @@ __all__ = [
     "run_batch", "simulate", "suggest_reconstruction_shape", "Job", "submit_batch", "SpectralJob", "RunPlan",
     "capture_batch", "Server", "Request", "ServerBusyError", "Callback", "CsvLogger", "IterationCallback",
     "ProgressLogger", "SaveImageEvery", "SavePupilEvery", "SaveResidualsEvery", "StepContext", "StopOnPlateau",
-    "intensity_loss", "ResolvedFrame", "ResolvedIllumination", "SourceContribution",
+    "intensity_loss", "ResolvedFrame", "ResolvedIllumination", "SourceContribution", "SourcePositionList",
 ]

@@ -209,11 +209,44 @@ class PlanarLEDArray:
                 ax = (p[0], cx * p[1] - sx * p[2], sx * p[1] + cx * p[2])
                 ay = (cy * ax[0] + sy * ax[2], ax[1], -sy * ax[0] + cy * ax[2])
                 az = (cz * ay[0] - sz * ay[1], sz * ay[0] + cz * ay[1], ay[2])
-                pos = (az[0] + t[0], az[1] + t[1], az[2] + t[2])
-                norm = float(np.hypot(np.hypot(pos[0], pos[1]), pos[2]))
-                positions.append(pos)
-                directions.append((-pos[0] / norm, -pos[1] / norm, -pos[2] / norm))
-        return np.array(positions, dtype=np.float64), np.array(directions, dtype=np.float64)
+                positions.append((az[0] + t[0], az[1] + t[1], az[2] + t[2]))
+        return np.array(positions, dtype=np.float64), _directions_from_positions(positions)
+
+
+def _directions_from_positions(positions) -> np.ndarray:
+    """Source-to-sample unit vectors -p / |p| (ResolvedSources::from_positions,
+    src/experiment/illumination.rs:385-410), |p| as hypot(hypot(x, y), z)."""
+    directions = []
+    for x, y, z in positions:
+        if not (math.isfinite(x) and math.isfinite(y) and math.isfinite(z)):
+            raise InvalidParameterError("positions_m: position components must be finite")
+        norm = float(np.hypot(np.hypot(x, y), z))
+        if not math.isfinite(norm) or norm <= 0.0:
+            raise InvalidParameterError("positions_m: no source may coincide with the sample origin")
+        directions.append((-x / norm, -y / norm, -z / norm))
+    return np.array(directions, dtype=np.float64)
+
+
+class SourcePositionList:
+    """Explicit source positions in sample coordinates, metres
+    (src/experiment/illumination.rs:45-72; python/src/config.rs:437-470)."""
+
+    def __init__(self, positions_m):
+        self._p = np.array(_pair_rows(positions_m, 3, "positions_m"), dtype=np.float64)
+
+    @property
+    def positions_m(self) -> np.ndarray:
+        return self._p.copy()
+
+    @property
+    def source_count(self) -> int:
+        return self._p.shape[0]
+
+    def resolve(self, optics: Optics) -> ResolvedSources:
+        optics._validate()
+        directions = _directions_from_positions([tuple(float(v) for v in row) for row in self._p])
+        k = 2.0 * math.pi * optics.illumination_refractive_index / optics.wavelength_vacuum_m
+        return ResolvedSources(np.stack([k * directions[:, 0], k * directions[:, 1]], axis=1), directions, self._p)
 
 
 _DIRECTION_TOLERANCE = 128.0 * np.finfo(np.float64).eps

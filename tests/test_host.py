@@ -307,6 +307,26 @@ def test_resolved_sources_directions_and_positions(fpm):
     assert np.array_equal(illumination.resolve(optics).k_vectors, resolved.k_vectors)
 
 
+def test_source_position_list(fpm):
+    # SourcePositionList (src/experiment/illumination.rs:45-72): the LED
+    # array's own positions resolve to its compiled k-vectors bit for bit,
+    # and python/tests/test_configuration.py:137-144 compiles two sources.
+    optics = fpm.Optics(532e-9, 0.10, 4.0, 6.5e-6)
+    pose = fpm.ArrayPose.from_translation_and_extrinsic_xyz_degrees((1e-3, -2e-3, -85e-3), (2.0, -1.0, 15.0))
+    array = fpm.PlanarLEDArray((5, 7), (4e-3, 3.5e-3), (3.2, 1.7), pose).resolve(optics)
+    listed = fpm.SourcePositionList(array.positions_m)
+    assert listed.source_count == 35 and np.array_equal(listed.positions_m, array.positions_m)
+    resolved = listed.resolve(optics)
+    assert np.array_equal(resolved.k_vectors, array.k_vectors) and np.array_equal(resolved.directions, array.directions)
+    model = fpm.compile_model(optics, fpm.Illumination(fpm.SourcePositionList(
+        np.array([[0.0, 0.0, -0.09], [0.001, 0.0, -0.09]]))), (8, 8), (16, 16))
+    assert model.source_count == 2 and model.frame_count == 2
+    with pytest.raises(fpm.InvalidParameterError):
+        fpm.SourcePositionList(np.zeros((1, 3))).resolve(optics)
+    with pytest.raises(ValueError):
+        fpm.SourcePositionList(np.zeros((0, 3)))
+
+
 def test_component_angle_directions_compile(fpm):
     # python/tests/test_configuration.py:97-103,168-175: two sources, two frames.
     optics = fpm.Optics(532e-9, 0.10, 4.0, 6.5e-6)
