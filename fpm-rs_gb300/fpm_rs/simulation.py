@@ -1,17 +1,19 @@
-"""Measurement stacks and acquisition simulation (src/simulation/simulator.rs:107-226).
+"""Measurement stacks, synthetic objects and acquisition simulation
+(src/simulation/simulator.rs:107-226, src/simulation/synthetic_object.rs).
 
 The forward stack (object FFT, crop, pupil, IFFT, |psi|^2 * gain + background)
-runs on the GPU; the camera's noise draws run on the host in frame order.
+and the camera model with its noise draws run in one device call.
 """
 
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
 from . import _native as N
-from .errors import InvalidMeasurementsError, InvalidShapeError, UnsupportedError
+from .errors import InvalidMeasurementsError, InvalidParameterError, InvalidShapeError, UnsupportedError
 from .experiment import CameraModel
 from .model import ImagePlaneModel, compile_camera_model
 
@@ -74,6 +76,220 @@ class MeasurementStack:
     @property
     def masks(self):
         return None if self._masks is None else self._masks.copy()
+
+
+def _polar(r: float, theta: float) -> complex:
+    """Complex64::from_polar: (r cos theta, r sin theta), libm cos and sin
+    (NaN for a non-finite angle, as in Rust)."""
+    if not math.isfinite(theta):
+        return complex(math.nan, math.nan)
+    return complex(r * math.cos(theta), r * math.sin(theta))
+
+
+def _object_shape(shape) -> tuple:
+    h, w = int(shape[0]), int(shape[1])
+    if h <= 0 or w <= 0:
+        raise InvalidShapeError(f"synthetic object dimensions must be non-zero, got ({h}, {w})")
+    return h, w
+
+
+def _real_2d(values, name: str) -> np.ndarray:
+    a = np.array(values, dtype=np.float64, order="C")
+    if a.ndim != 2:
+        raise TypeError(f"{name} must be a 2-D float64 array")
+    return a
+
+
+class SyntheticObject:
+    """High-resolution complex sample field used as simulation ground truth
+    (src/simulation/synthetic_object.rs:36-376; python/src/simulation.rs:25-180).
+
+    The deterministic targets follow the reference's arithmetic term by term
+    (libm hypot, atan2, sin, cos, exp), so their values match it bit for bit.
+    `random_phase`, `particle_field` and `biological_like` draw from NumPy's
+    PCG64 seeded with `seed`: the same distributions as the reference's
+    ChaCha12 stream, not the same values. Image files are not decoded here:
+    load the image as an array and use `amplitude_only` or
+    `from_amplitude_phase`."""
+
+    def __init__(self, field):
+        f = np.array(field, dtype=np.complex128, order="C")
+        if f.ndim != 2:
+            raise TypeError("field must be a 2-D complex128 array")
+        _object_shape(f.shape)
+        if not (np.all(np.isfinite(f.real)) and np.all(np.isfinite(f.imag))):
+            raise InvalidParameterError("field: values must have finite real and imaginary components")
+        self._field = f
+
+    @staticmethod
+    def _of(values: np.ndarray) -> "SyntheticObject":
+        obj = SyntheticObject.__new__(SyntheticObject)
+        obj._field = values
+        return obj
+
+    @staticmethod
+    def _build(shape, value) -> "SyntheticObject":
+        h, w = shape
+        out = np.empty((h, w), np.complex128)
+        for row in range(h):
+            for column in range(w):
+                out[row, column] = value(row, column)
+        return SyntheticObject._of(out)
+
+    @property
+    def field(self) -> np.ndarray:
+        return self._field.copy()
+
+    @property
+    def shape(self) -> tuple:
+        return tuple(self._field.shape)
+
+    @property
+    def label(self):
+        return None
+
+    @staticmethod
+    def constant(shape, amplitude: float = 1.0, phase: float = 0.0) -> "SyntheticObject":
+        shape = _object_shape(shape)
+        amplitude, phase = float(amplitude), float(phase)
+        if not math.isfinite(amplitude) or amplitude < 0.0:
+            raise InvalidParameterError("amplitude: must be finite and non-negative")
+        return SyntheticObject._of(np.full(shape, _polar(amplitude, phase), np.complex128))
+
+    @staticmethod
+    def amplitude_only(amplitude) -> "SyntheticObject":
+        a = _real_2d(amplitude, "amplitude")
+        _object_shape(a.shape)
+        if not np.all(np.isfinite(a)) or np.any(a < 0.0):
+            raise InvalidParameterError("amplitude: values must be finite and non-negative")
+        return SyntheticObject._of(a.astype(np.complex128))
+
+    @staticmethod
+    def phase_only(phase) -> "SyntheticObject":
+        p = _real_2d(phase, "phase")
+        _object_shape(p.shape)
+        if not np.all(np.isfinite(p)):
+            raise InvalidParameterError("phase: values must be finite")
+        return SyntheticObject._build(p.shape, lambda r, c: _polar(1.0, float(p[r, c])))
+
+    @staticmethod
+    def from_amplitude_phase(amplitude, phase) -> "SyntheticObject":
+        a, p = _real_2d(amplitude, "amplitude"), _real_2d(phase, "phase")
+        if a.shape != p.shape:
+            raise InvalidShapeError(f"amplitude {a.shape} and phase {p.shape} differ")
+        _object_shape(a.shape)
+        return SyntheticObject(SyntheticObject._build(a.shape, lambda r, c: _polar(float(a[r, c]), float(p[r, c])))._field)
+
+    @staticmethod
+    def from_amplitude_image(path) -> "SyntheticObject":
+        raise UnsupportedError("image decoding is not available here: load the image as an array and use "
+                               "SyntheticObject.amplitude_only")
+
+    @staticmethod
+    def from_amplitude_phase_images(amplitude_path, phase_path, phase_extent) -> "SyntheticObject":
+        raise UnsupportedError("image decoding is not available here: load the images as arrays and use "
+                               "SyntheticObject.from_amplitude_phase")
+
+    @staticmethod
+    def phase_disk(shape, radius_pixels: float, phase_shift: float) -> "SyntheticObject":
+        """Unit amplitude; phase `phase_shift` within `radius_pixels` of the centre (:156-180)."""
+        shape = _object_shape(shape)
+        radius_pixels, phase_shift = float(radius_pixels), float(phase_shift)
+        if not math.isfinite(radius_pixels) or radius_pixels <= 0.0 or not math.isfinite(phase_shift):
+            raise InvalidParameterError("phase disk: radius must be positive and phase must be finite")
+        c0, c1 = (shape[0] - 1) / 2.0, (shape[1] - 1) / 2.0
+        return SyntheticObject._build(shape, lambda r, c: _polar(
+            1.0, phase_shift if float(np.hypot(r - c0, c - c1)) <= radius_pixels else 0.0))
+
+    @staticmethod
+    def siemens_star(shape, spokes: int) -> "SyntheticObject":
+        """Binary amplitude (0.25 / 1) star of `spokes` spokes inside 0.46 of the smaller side (:183-209)."""
+        shape = _object_shape(shape)
+        spokes = int(spokes)
+        if spokes < 2:
+            raise InvalidParameterError("spokes: must be at least 2")
+        c0, c1 = (shape[0] - 1) / 2.0, (shape[1] - 1) / 2.0
+        maximum_radius = float(min(shape)) * 0.46
+
+        def value(r, c):
+            y, x = r - c0, c - c1
+            dark = float(np.hypot(x, y)) <= maximum_radius and math.sin(math.atan2(x, y) * float(spokes)) >= 0.0
+            return complex(0.25 if dark else 1.0, 0.0)
+
+        return SyntheticObject._build(shape, value)
+
+    @staticmethod
+    def resolution_target(shape) -> "SyntheticObject":
+        """Horizontal and vertical bar groups of periods 2, 3, 4, 6, 8 at amplitude 0.2 (:212-233)."""
+        h, w = _object_shape(shape)
+        out = np.ones((h, w), np.complex128)
+        groups = (2, 3, 4, 6, 8)
+        for group, period in enumerate(groups):
+            top, bottom = group * h // len(groups), (group + 1) * h // len(groups)
+            for row in range(top, bottom):
+                for column in range(w):
+                    dark = (column // period) % 2 == 0 if group % 2 == 0 else ((row - top) // period) % 2 == 0
+                    if dark:
+                        out[row, column] = 0.2
+        return SyntheticObject._of(out)
+
+    @staticmethod
+    def mixed_test_pattern(shape) -> "SyntheticObject":
+        """Amplitude bar and disk at 0.45 with a Gaussian plus sinusoidal phase (:275-299)."""
+        shape = _object_shape(shape)
+        c0, c1 = (shape[0] - 1) / 2.0, (shape[1] - 1) / 2.0
+        scale = float(min(shape))
+
+        def value(r, c):
+            y, x = r - c0, c - c1
+            radius = float(np.hypot(x, y))
+            inside = (abs(x) < 0.12 * scale and abs(y) < 0.35 * scale) or radius < 0.12 * scale
+            phase = 0.8 * math.exp(-radius * radius / (0.08 * scale * scale)) + 0.25 * math.sin(math.tau * x / scale)
+            return _polar(0.45 if inside else 1.0, phase)
+
+        return SyntheticObject._build(shape, value)
+
+    @staticmethod
+    def random_phase(shape, standard_deviation: float, seed: int) -> "SyntheticObject":
+        shape = _object_shape(shape)
+        sd = float(standard_deviation)
+        if not math.isfinite(sd) or sd < 0.0:
+            raise InvalidParameterError("standard_deviation: must be finite and non-negative")
+        if sd == 0.0:
+            return SyntheticObject._of(np.ones(shape, np.complex128))
+        phase = np.random.default_rng(int(seed)).normal(0.0, sd, shape)
+        return SyntheticObject._of(np.cos(phase) + 1j * np.sin(phase))
+
+    @staticmethod
+    def particle_field(shape, particles: int, seed: int) -> "SyntheticObject":
+        shape = _object_shape(shape)
+        out = np.ones(shape, np.complex128)
+        rng = np.random.default_rng(int(seed))
+        for _ in range(int(particles)):
+            out[rng.integers(0, shape[0]), rng.integers(0, shape[1])] = 0.1
+        return SyntheticObject._of(out)
+
+    @staticmethod
+    def biological_like(shape, features: int, seed: int) -> "SyntheticObject":
+        shape = _object_shape(shape)
+        if int(features) == 0:
+            raise InvalidParameterError("features: must be greater than zero")
+        rng = np.random.default_rng(int(seed))
+        minimum_size = float(min(shape))
+        lower = max(0.02 * minimum_size, 1.0)
+        upper = max(0.12 * minimum_size, lower + 0.1)
+        rows, cols = np.meshgrid(np.arange(shape[0], dtype=np.float64), np.arange(shape[1], dtype=np.float64),
+                                 indexing="ij")
+        phase = np.zeros(shape)
+        absorption = np.zeros(shape)
+        for _ in range(int(features)):
+            cr, cc = rng.uniform(0.0, shape[0]), rng.uniform(0.0, shape[1])
+            sigma, strength, absorb = rng.uniform(lower, upper), rng.uniform(-0.4, 1.0), rng.uniform(0.0, 0.25)
+            profile = np.exp(-((rows - cr) ** 2 + (cols - cc) ** 2) / (2.0 * sigma * sigma))
+            phase += strength * profile
+            absorption += absorb * profile
+        amplitude = np.maximum(1.0 - absorption, 0.1)
+        return SyntheticObject._of(amplitude * np.cos(phase) + 1j * amplitude * np.sin(phase))
 
 
 class SimulationResult:
