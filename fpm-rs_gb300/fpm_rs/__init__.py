@@ -28,7 +28,8 @@ from .reconstruction import (AdaptiveAlternatingProjection, AlternatingProjectio
                              ReconstructionProblem,
                              ReconstructionResult, Request, RunPlan, RuntimeInfo, Job, Server, capture_batch, last_run_stats, run_batch,
                              submit_batch)
-from .simulation import MeasurementStack, SimulationResult, SyntheticObject, forward_intensities, simulate
+from .simulation import (IlluminationAcquisitionErrors, MeasurementStack, SimulationResult, SyntheticObject,
+                         forward_intensities, simulate)
 from .spectral import (SpectralAcquisitionPlan, SpectralAlternatingProjection, SpectralChannel, SpectralFrame,
                        SpectralGeometry, SpectralImagePlaneModel, SpectralMixingDiagnostics,
                        SpectralJob, SpectralReconstructionCheckpoint, SpectralReconstructionProblem,
@@ -65,5 +66,5 @@ __all__ = [
     "capture_batch", "Server", "Request", "ServerBusyError", "Callback", "CsvLogger", "IterationCallback",
     "ProgressLogger", "SaveImageEvery", "SavePupilEvery", "SaveResidualsEvery", "StepContext", "StopOnPlateau",
     "intensity_loss", "ResolvedFrame", "ResolvedIllumination", "SourceContribution", "SourcePositionList",
-    "SyntheticObject",
+    "SyntheticObject", "IlluminationAcquisitionErrors",
 ]

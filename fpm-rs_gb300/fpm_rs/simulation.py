@@ -318,23 +318,110 @@ def forward_intensities(model: ImagePlaneModel, object_field) -> np.ndarray:
     return out
 
 
+class IlluminationAcquisitionErrors:
+    """Acquisition faults applied to the true model before simulation
+    (src/simulation/illumination_acquisition_errors.rs:8-50;
+    python/src/config.rs:1229-1258): relative Gaussian frame-gain variation,
+    frames whose illumination fails, and a source permutation."""
+
+    def __init__(self, *, frame_gain_relative_std: float = 0.0, missing_frames=(), source_permutation=None):
+        std = float(frame_gain_relative_std)
+        if not math.isfinite(std) or std < 0.0:
+            raise ValueError("frame_gain_relative_std must be finite and non-negative")
+        indices = [int(i) for i in missing_frames]
+        permutation = None if source_permutation is None else [int(i) for i in source_permutation]
+        if any(i < 0 for i in indices + (permutation or [])):
+            raise OverflowError("frame and source indices must be non-negative")
+        self.frame_gain_relative_std = std
+        self.missing_frames = indices
+        self.source_permutation = permutation
+
+
+def _apply_acquisition_errors(model: ImagePlaneModel, errors: IlluminationAcquisitionErrors,
+                              seed: int) -> ImagePlaneModel:
+    """apply_illumination_acquisition_errors (src/simulation/simulator.rs:230-330):
+    validation, then the source permutation of k-vectors, crops, offsets,
+    gains and per-frame backgrounds, then each frame gain times
+    max(N(1, std), 0.01). The draws come from NumPy's PCG64 seeded with
+    `seed`: the reference's distribution, not its ChaCha12 values."""
+    frames = model.frame_count
+    missing = sorted(errors.missing_frames)
+    if any(f >= frames for f in missing) or any(a == b for a, b in zip(missing, missing[1:])):
+        raise InvalidParameterError(f"missing_frames: must contain unique frame indices below {frames}")
+    permutation = errors.source_permutation
+    if permutation is not None and sorted(permutation) != list(range(model.source_count)):
+        raise InvalidParameterError(f"source_permutation: must be a permutation of 0..{model.source_count}")
+    changes = {}
+    gains = None if model._gains is None else model._gains.copy()
+    if permutation is not None:
+        order = np.asarray(permutation, dtype=np.int64)
+        changes.update(k_vectors=model._k[order], start_row=model._start_row[order], start_col=model._start_col[order],
+                       offset_row=model._offset_row[order], offset_col=model._offset_col[order])
+        if gains is not None:
+            gains = gains[order]
+        n = model.image_shape[0] * model.image_shape[1]
+        if model._background is not None and model._background.size == n * frames:
+            changes["background"] = model._background.reshape(frames, n)[order].ravel()
+    if errors.frame_gain_relative_std > 0.0:
+        if gains is None:
+            gains = np.ones(frames)
+        draws = np.random.default_rng(int(seed) & (2**64 - 1)).normal(1.0, errors.frame_gain_relative_std, frames)
+        gains = gains * np.maximum(draws, 0.01)
+    if gains is not None:
+        changes["frame_gains"] = gains
+    return model._replace(**changes) if changes else model
+
+
+def _frame_background(model: ImagePlaneModel, frame: int) -> np.ndarray:
+    """The background a frame's camera sees without illumination (zero when none)."""
+    h, w = model.image_shape
+    if model._background is None:
+        return np.zeros((h, w))
+    bg = model._background.ravel()
+    return (bg if bg.size == h * w else bg[frame * h * w:(frame + 1) * h * w]).reshape(h, w).copy()
+
+
+def _without_missing_illumination(model: ImagePlaneModel, missing) -> ImagePlaneModel:
+    """The model with zero gain on the missing frames: the forward stack then
+    gives 0 * |psi|^2 + background, the background the camera measures
+    (src/simulation/simulator.rs:168-180)."""
+    gains = np.ones(model.frame_count) if model._gains is None else model._gains.copy()
+    gains[list(missing)] = 0.0
+    return model._replace(frame_gains=gains)
+
+
 def simulate(true_model: ImagePlaneModel, object, *, reconstruction_model=None, camera: CameraModel | None = None,
              illumination_errors=None, seed: int = 0) -> SimulationResult:
     """Simulate an image-plane FPM acquisition (Simulator::simulate)."""
-    if illumination_errors is not None:
-        raise UnsupportedError("illumination acquisition errors are not supported on the GB300 device path")
     field = getattr(object, "field", object)
     field = N.c128(field)
     recon = reconstruction_model if reconstruction_model is not None else true_model
     if (recon.image_shape != true_model.image_shape or recon.reconstruction_shape != true_model.reconstruction_shape
             or recon.frame_count != true_model.frame_count):
         raise InvalidShapeError("true and reconstruction models must have matching image, object, and frame dimensions")
+    missing = []
+    if illumination_errors is not None:
+        if not isinstance(illumination_errors, IlluminationAcquisitionErrors):
+            raise TypeError("illumination_errors must be an IlluminationAcquisitionErrors object")
+        true_model = _apply_acquisition_errors(true_model, illumination_errors, seed)
+        missing = list(illumination_errors.missing_frames)
     if camera is None:
         data = forward_intensities(true_model, field)
+        for f in missing:
+            data[f] = _frame_background(true_model, f)
     else:
         recon = compile_camera_model(recon, camera)
-        data = _simulate_counts(true_model, field, camera, seed)
-    return SimulationResult(MeasurementStack(data), field.copy(), true_model, recon, camera is None, seed)
+        lit = _without_missing_illumination(true_model, missing) if missing else true_model
+        data = _simulate_counts(lit, field, camera, seed)
+    if missing:
+        weights = np.ones(true_model.frame_count)
+        weights[missing] = 0.0
+        stack = MeasurementStack(data, frame_weights=weights)
+    else:
+        stack = MeasurementStack(data)
+    result = SimulationResult(stack, field.copy(), true_model, recon, camera is None, seed)
+    result.missing_frames = missing
+    return result
 
 
 def _simulate_counts(model: ImagePlaneModel, field: np.ndarray, camera: CameraModel, seed: int) -> np.ndarray:
