@@ -381,15 +381,6 @@ def _frame_background(model: ImagePlaneModel, frame: int) -> np.ndarray:
     return (bg if bg.size == h * w else bg[frame * h * w:(frame + 1) * h * w]).reshape(h, w).copy()
 
 
-def _without_missing_illumination(model: ImagePlaneModel, missing) -> ImagePlaneModel:
-    """The model with zero gain on the missing frames: the forward stack then
-    gives 0 * |psi|^2 + background, the background the camera measures
-    (src/simulation/simulator.rs:168-180)."""
-    gains = np.ones(model.frame_count) if model._gains is None else model._gains.copy()
-    gains[list(missing)] = 0.0
-    return model._replace(frame_gains=gains)
-
-
 def simulate(true_model: ImagePlaneModel, object, *, reconstruction_model=None, camera: CameraModel | None = None,
              illumination_errors=None, seed: int = 0) -> SimulationResult:
     """Simulate an image-plane FPM acquisition (Simulator::simulate)."""
@@ -411,8 +402,15 @@ def simulate(true_model: ImagePlaneModel, object, *, reconstruction_model=None, 
             data[f] = _frame_background(true_model, f)
     else:
         recon = compile_camera_model(recon, camera)
-        lit = _without_missing_illumination(true_model, missing) if missing else true_model
-        data = _simulate_counts(lit, field, camera, seed)
+        data = _simulate_counts(true_model, field, camera, seed)
+        if missing:
+            # A failed source leaves only the background for the camera
+            # (src/simulation/simulator.rs:168-180). A zero object gives
+            # gain * 0 + background on every frame, and the camera's streams
+            # are keyed by (seed, frame, pixel), so the same seed draws each
+            # missing frame's noise as it would have in place.
+            dark = _simulate_counts(true_model, np.zeros_like(field), camera, seed)
+            data[missing] = dark[missing]
     if missing:
         weights = np.ones(true_model.frame_count)
         weights[missing] = 0.0

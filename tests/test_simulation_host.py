@@ -58,12 +58,8 @@ def test_frame_gain_variation_is_seeded_and_clamped(fpm, model):
 
 
 def test_missing_frames_see_only_the_background(fpm, model):
-    from fpm_rs.simulation import _frame_background, _without_missing_illumination
+    from fpm_rs.simulation import _frame_background
 
-    dark = _without_missing_illumination(model, [2, 5])
-    expected = model.frame_gains.copy()
-    expected[[2, 5]] = 0.0
-    assert np.array_equal(dark.frame_gains, expected)
     assert np.array_equal(_frame_background(model, 5).ravel(), model._background[5 * 1024:6 * 1024])
     assert np.array_equal(_frame_background(model._replace(background=None), 5), np.zeros((32, 32)))
     flat = np.linspace(0.0, 1.0, 1024)
