@@ -13,9 +13,9 @@ import ctypes as _C
 import numpy as _np
 
 from . import _native, tuning
-from .errors import (DeviceError, FpmError, FrameOutOfRangeError, InvalidMeasurementsError, InvalidModelError,
-                     InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
-                     ServerBusyError, UnsupportedError)
+from .errors import (DatasetError, DeviceError, FpmError, FpmIoError, FrameOutOfRangeError, InvalidMeasurementsError,
+                     InvalidModelError, InvalidParameterError, InvalidShapeError, LengthMismatchError, NumericalError,
+                     SerializationError, ServerBusyError, UnsupportedError)
 from .experiment import (ArrayPose, CameraModel, DirectionList, Illumination, KVectorList, Optics, PlanarLEDArray,
                          PupilAberration, ResolvedFrame, ResolvedIllumination, ResolvedSources, SourceContribution,
                          SourcePositionList)
@@ -66,5 +66,5 @@ __all__ = [
     "capture_batch", "Server", "Request", "ServerBusyError", "Callback", "CsvLogger", "IterationCallback",
     "ProgressLogger", "SaveImageEvery", "SavePupilEvery", "SaveResidualsEvery", "StepContext", "StopOnPlateau",
     "intensity_loss", "ResolvedFrame", "ResolvedIllumination", "SourceContribution", "SourcePositionList",
-    "SyntheticObject", "IlluminationAcquisitionErrors",
+    "SyntheticObject", "IlluminationAcquisitionErrors", "DatasetError", "FpmIoError", "SerializationError",
 ]

@@ -23,7 +23,7 @@ from pathlib import Path
 import numpy as np
 
 from .callbacks import Callback, _interval, _next_multiple
-from .errors import InvalidParameterError
+from .errors import InvalidParameterError, json_file_errors
 
 FORMAT_VERSION = 2
 
@@ -63,6 +63,10 @@ class ReconstructionCheckpoint:
 
     def save(self, path) -> None:
         """Atomically serialize this checkpoint (write to a temporary file, then rename)."""
+        with json_file_errors(path):
+            self._save(path)
+
+    def _save(self, path) -> None:
         path = Path(path)
         doc = {
             "format_version": self.format_version,
@@ -90,6 +94,11 @@ class ReconstructionCheckpoint:
     @staticmethod
     def load(path) -> "ReconstructionCheckpoint":
         """Read and validate a checkpoint file."""
+        with json_file_errors(path):
+            return ReconstructionCheckpoint._load(path)
+
+    @staticmethod
+    def _load(path) -> "ReconstructionCheckpoint":
         with open(path) as f:
             doc = json.load(f)
         version = int(doc.get("format_version", -1))

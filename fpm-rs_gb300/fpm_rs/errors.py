@@ -2,6 +2,10 @@
 
 from __future__ import annotations
 
+import contextlib
+import json
+import os
+
 
 class FpmError(Exception):
     """Base class for errors raised by the device backend."""
@@ -37,6 +41,31 @@ class NumericalError(FpmError):
 
 class UnsupportedError(FpmError):
     pass
+
+
+class DatasetError(FpmError):
+    pass
+
+
+class FpmIoError(FpmError):
+    """A file could not be read or written (Error::Io)."""
+
+
+class SerializationError(FpmError):
+    """A file's contents could not be decoded (Error::Serialization)."""
+
+
+@contextlib.contextmanager
+def json_file_errors(path):
+    """Maps failures of a JSON file operation as python/src/errors.rs:17-50
+    maps Error::Io and Error::Serialization: file-system errors become
+    FpmIoError, malformed or incomplete JSON becomes SerializationError."""
+    try:
+        yield
+    except OSError as error:
+        raise FpmIoError(f"{os.fspath(path)}: {error}") from error
+    except (json.JSONDecodeError, KeyError, TypeError, IndexError) as error:
+        raise SerializationError(f"{os.fspath(path)}: {error!r}") from error
 
 
 class DeviceError(FpmError):

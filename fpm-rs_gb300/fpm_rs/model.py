@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import _native as N
-from .errors import InvalidModelError, InvalidParameterError, InvalidShapeError
+from .errors import InvalidModelError, InvalidParameterError, InvalidShapeError, json_file_errors
 
 _POLICIES = {"minimum": 1, "smooth": 2, "power_of_two": 3}
 
@@ -152,6 +152,10 @@ class ImagePlaneModel:
 
     # -- persistence (ImagePlaneModel::save_json/load_json, src/model/image_plane_fpm.rs:117-134)
     def save_json(self, *, path) -> None:
+        with json_file_errors(path):
+            self._save_json(path)
+
+    def _save_json(self, path) -> None:
         doc = {
             "format": "fpm-gb300 image-plane model v1",
             "image_shape": list(self._image_shape),
@@ -173,6 +177,11 @@ class ImagePlaneModel:
 
     @staticmethod
     def load_json(*, path) -> "ImagePlaneModel":
+        with json_file_errors(path):
+            return ImagePlaneModel._load_json(path)
+
+    @staticmethod
+    def _load_json(path) -> "ImagePlaneModel":
         with open(os.fspath(path)) as handle:
             doc = json.load(handle)
         h, w = doc["image_shape"]

@@ -27,7 +27,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _native as N
-from .errors import InvalidMeasurementsError, InvalidParameterError, InvalidShapeError, UnsupportedError
+from .errors import InvalidMeasurementsError, InvalidParameterError, InvalidShapeError, UnsupportedError, json_file_errors
 from .experiment import KVectorList, Optics
 from .model import ImagePlaneModel, compile_model, suggest_reconstruction_shape
 from .simulation import MeasurementStack
@@ -462,6 +462,10 @@ class SpectralReconstructionCheckpoint:
 
     def save(self, path) -> None:
         """Atomic JSON write: a temporary file in the same directory, then a rename."""
+        with json_file_errors(path):
+            self._save(path)
+
+    def _save(self, path) -> None:
         path = Path(path)
         doc = dict(kind=self.kind, format_version=self.format_version, completed_iterations=self.completed_iterations,
                    elapsed_seconds=self.elapsed_seconds, spectra=[_encode(s) for s in self.spectra],
@@ -479,6 +483,11 @@ class SpectralReconstructionCheckpoint:
 
     @staticmethod
     def load(path) -> "SpectralReconstructionCheckpoint":
+        with json_file_errors(path):
+            return SpectralReconstructionCheckpoint._load(path)
+
+    @staticmethod
+    def _load(path) -> "SpectralReconstructionCheckpoint":
         with open(path) as f:
             doc = json.load(f)
         if doc.get("kind") != "spectral_alternating_projection" or int(doc.get("format_version", -1)) != FORMAT_VERSION:

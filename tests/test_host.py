@@ -404,3 +404,28 @@ def test_intensity_loss_sums_in_order_and_matches_the_oracle_frame_loss(fpm, los
     want = oracle.frame_loss(oracle.Problem(omodel, counts), spectrum, omodel["pupil"], 4, loss_type)
     got = fpm.intensity_loss(counts[4], stack[4], loss_type)
     assert abs(got - want) <= 1e-12 * abs(want)
+
+
+def test_file_errors_map_to_io_and_serialization_errors(fpm, tmp_path):
+    # python/src/errors.rs:17-50: Error::Io -> FpmIoError, Error::Serialization -> SerializationError.
+    model = fpm.compile_model(fpm.Optics(**W.OPTICS), fpm.Illumination(fpm.PlanarLEDArray(
+        (3, 3), W.PITCH, (1.0, 1.0), fpm.ArrayPose.from_translation((0.0, 0.0, W.Z)))), (32, 32))
+    model.save_json(path=tmp_path / "model.json")
+    loaded = fpm.ImagePlaneModel.load_json(path=tmp_path / "model.json")
+    assert np.array_equal(loaded.k_vectors, model.k_vectors) and np.array_equal(loaded.pupil, model.pupil)
+    (tmp_path / "bad.json").write_text("{not json")
+    (tmp_path / "partial.json").write_text("{}")
+    with pytest.raises(fpm.FpmIoError):
+        fpm.ImagePlaneModel.load_json(path=tmp_path / "missing.json")
+    with pytest.raises(fpm.SerializationError):
+        fpm.ImagePlaneModel.load_json(path=tmp_path / "bad.json")
+    with pytest.raises(fpm.SerializationError):
+        fpm.ImagePlaneModel.load_json(path=tmp_path / "partial.json")
+    with pytest.raises(fpm.FpmIoError):
+        model.save_json(path=tmp_path / "no" / "such" / "model.json")
+    for checkpoint in (fpm.ReconstructionCheckpoint, fpm.SpectralReconstructionCheckpoint):
+        with pytest.raises(fpm.FpmIoError):
+            checkpoint.load(tmp_path / "missing.json")
+        with pytest.raises(fpm.SerializationError):
+            checkpoint.load(tmp_path / "bad.json")
+    assert issubclass(fpm.FpmIoError, fpm.FpmError) and issubclass(fpm.DatasetError, fpm.FpmError)
