@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--workload", choices=("tiles", "spectral", "serving", "illumination"), default="tiles")
     ap.add_argument("--requests", type=int, default=64, help="spectral requests per step")
     ap.add_argument("--seed", type=int, default=3)
-    ap.add_argument("--cpu-sample-tiles", type=int, default=16, help="tiles in the bounded CPU baseline sample")
+    ap.add_argument("--cpu-sample-tiles", type=int, default=32, help="tiles in the bounded CPU baseline sample")
     ap.add_argument("--cpu-sample-iterations", type=int, default=1)
     ap.add_argument("--sizes", default=None,
                     help="comma-separated tile sizes to keep from the drawn mix (per-size cost; default: all)")
@@ -249,23 +249,40 @@ def peaks():
         return 6800.0, "fallback"
 
 
+_CPU_SAMPLES = {}
+
+
+def _cpu_sample(per_size, seed_base):
+    """The CPU baseline's sample problems, built once per process: equal tile
+    counts per size, as the workload's mix has them, in round-robin size
+    order so that the tiles running at once on the host threads are a mix of
+    sizes too, not one size's tiles competing for memory bandwidth."""
+    import oracle
+
+    key = (per_size, seed_base)
+    if key not in _CPU_SAMPLES:
+        oracle.build()
+        problems = []
+        for k in range(per_size):
+            for n in SIZES:
+                grid, ref = W.led_grid(LED_SIDE)
+                kx, ky = oracle.planar_kvectors(W.OPTICS, grid, W.PITCH, ref, (0.0, 0.0, W.Z))
+                model = oracle.compile_model(W.OPTICS, kx, ky, (n, n))
+                obj = W.smooth_random_object((model["mh"], model["mw"]), seed_base + 100000 + 10 * n + k)
+                intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(obj),
+                                                 workers=os.cpu_count() or 1)
+                counts, scale = W.poisson_counts(intensity, PHOTONS, seed_base + k)
+                problems.append(oracle.Problem(model, counts, gains=np.full(len(kx), scale)))
+        _CPU_SAMPLES[key] = problems
+    return _CPU_SAMPLES[key]
+
+
 def cpu_baseline(sizes, iterations, sample_tiles, sample_iterations, seed_base):
     """Times the FP64 oracle on a bounded sample of the workload with all host cores."""
     import oracle
 
-    oracle.build()
     per_size = max(1, sample_tiles // len(SIZES))
-    problems = []
-    for n in SIZES:
-        for k in range(per_size):
-            grid, ref = W.led_grid(LED_SIDE)
-            kx, ky = oracle.planar_kvectors(W.OPTICS, grid, W.PITCH, ref, (0.0, 0.0, W.Z))
-            model = oracle.compile_model(W.OPTICS, kx, ky, (n, n))
-            obj = W.smooth_random_object((model["mh"], model["mw"]), seed_base + 100000 + 10 * n + k)
-            intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(obj),
-                                             workers=os.cpu_count() or 1)
-            counts, scale = W.poisson_counts(intensity, PHOTONS, seed_base + k)
-            problems.append(oracle.Problem(model, counts, gains=np.full(len(kx), scale)))
+    problems = _cpu_sample(per_size, seed_base)
     cores = os.cpu_count() or 1
     from concurrent.futures import ThreadPoolExecutor
 
@@ -295,7 +312,7 @@ def cpu_baseline(sizes, iterations, sample_tiles, sample_iterations, seed_base):
     mean_tile_s = statistics.mean(full)
     tiles_per_s = cores / mean_tile_s
     measured = sum(t1 + t2 for t1, t2 in timings)
-    sample = (f"{len(problems)} tiles ({per_size} per N in {list(SIZES)}), each run for {k} and {k + 1} mPIE "
+    sample = (f"{len(problems)} tiles ({per_size} per N in {list(SIZES)}, sizes interleaved), each run for {k} and {k + 1} mPIE "
               f"iterations (FP64 oracle, one tile per thread on {cores} threads); a full {iterations}-iteration "
               f"tile = t({k}) + {iterations - k} x (t({k + 1}) - t({k})), so initialisation and finalisation count "
               f"once; tiles/s = cores / mean full-tile time ({measured:.1f} CPU-s measured)")
