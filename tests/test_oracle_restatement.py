@@ -1,0 +1,224 @@
+"""A second restatement of the projection algorithms, in NumPy and independent
+of the C oracle, written from the reference's Rust:
+
+- state initialisation: src/reconstruction/state.rs:280-349;
+- projection_update: src/algorithms/common.rs:57-306 (one source per frame);
+- mPIE momentum: common.rs:308-387 and src/algorithms/mpie.rs:152-164;
+- the crop and its exact adjoint: src/model/crop.rs:79-313;
+- the point loss: src/algorithms/objective.rs:47-72;
+- the per-pass objective: src/algorithms/metrics.rs:24-35;
+- the result object: src/reconstruction/result.rs:397-413.
+
+Each run's per-pass objectives and final object must agree with the oracle's
+to rounding. The two share no code: NumPy's FFT here, the oracle's own FFT
+there. So the oracle's reading of the reference, which the GPU parity tests
+rest on, is checked by a second reading over whole trajectories.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle
+import workloads as W
+
+EPS = 1e-10
+
+
+def _round_half_away(x: float) -> float:
+    return math.copysign(math.floor(abs(x) + 0.5), x)
+
+
+def _axis(start: int, length: int, offset: float):
+    """interpolation_axis (crop.rs:258-313): lower start, upper start and weights."""
+    nearest = _round_half_away(offset)
+    if abs(offset - nearest) <= 1e-12:
+        whole, fraction = nearest, 0.0
+    else:
+        whole = math.floor(offset)
+        fraction = offset - whole
+    lower = start + int(whole)
+    return lower, lower + (1 if fraction > 0.0 else 0), 1.0 - fraction, fraction
+
+
+def _stencil(model, source):
+    h, w = model["h"], model["w"]
+    sr, sc = int(model["start_row"][source]), int(model["start_col"][source])
+    orow, ocol = float(model["off_row"][source]), float(model["off_col"][source])
+    if abs(orow) <= 1e-12 and abs(ocol) <= 1e-12:
+        return [(sr, sc, 1.0)], h, w
+    lr, ur, lwr, uwr = _axis(sr, h, orow)
+    lc, uc, lwc, uwc = _axis(sc, w, ocol)
+    return [(lr, lc, lwr * lwc), (lr, uc, lwr * uwc), (ur, lc, uwr * lwc), (ur, uc, uwr * uwc)], h, w
+
+
+def _extract(spectrum, model, source):
+    taps, h, w = _stencil(model, source)
+    out = np.zeros((h, w), np.complex128)
+    for r, c, weight in taps:
+        out = out + spectrum[r:r + h, c:c + w] * weight
+    return out
+
+
+def _insert_adjoint(spectrum, model, source, update, scale):
+    taps, h, w = _stencil(model, source)
+    value = scale * update
+    for r, c, weight in taps:
+        spectrum[r:r + h, c:c + w] += value * weight
+
+
+def _point_loss(predicted, measured, loss):
+    if loss == "intensity_mse":
+        return (predicted - measured) ** 2
+    if loss == "poisson_nll":
+        mean = np.maximum(predicted, 1e-12)
+        return mean - np.maximum(measured, 0.0) * np.log(mean)
+    r = np.sqrt(np.maximum(predicted, 0.0)) - np.sqrt(np.maximum(measured, 0.0))
+    if loss == "amplitude_mse":
+        return r * r
+    return np.where(np.abs(r) <= 1.0, 0.5 * r * r, np.abs(r) - 0.5)
+
+
+def _fft_forward(x):
+    return np.fft.fft2(x) / x.size
+
+
+def _fft_inverse(x):
+    return np.fft.ifft2(x) * x.size
+
+
+def _initial_spectrum(model, data, gains, weights, masks, background):
+    h, w, mh, mw = model["h"], model["w"], model["mh"], model["mw"]
+    average = np.zeros((h, w))
+    weight = np.zeros((h, w))
+    total_amplitude = total_weight = 0.0
+    for f in range(data.shape[0]):
+        if weights[f] == 0.0:
+            continue
+        valid = np.ones((h, w), bool) if masks is None else masks[f] != 0
+        amplitude = np.sqrt(np.maximum((data[f] - background[f]) / gains[f], 0.0))
+        average[valid] += weights[f] * amplitude[valid]
+        weight[valid] += weights[f]
+        total_amplitude += float(np.sum(weights[f] * amplitude[valid]))
+        total_weight += weights[f] * int(valid.sum())
+    average = np.where(weight > 0.0, average / np.where(weight > 0.0, weight, 1.0), total_amplitude / total_weight)
+    rows = (np.arange(mh) * h) // mh
+    cols = (np.arange(mw) * w) // mw
+    obj = average[rows[:, None], cols[None, :]].astype(np.complex128)
+    return np.fft.fftshift(_fft_forward(obj))
+
+
+def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
+                 gains=None, background=None):
+    """AP / FPIE / mPIE with the reference defaults, sequential schedule, batch 1."""
+    frames = data.shape[0]
+    weights = np.ones(frames) if weights is None else np.asarray(weights, np.float64)
+    gains = np.ones(frames) if gains is None else np.asarray(gains, np.float64)
+    bg = np.zeros((frames, model["h"], model["w"])) if background is None else background
+    step, denominator, alpha, momentum = {
+        "ap": (1.0, "local", 0.0, False),
+        "fpie": (0.8, "rpie", 0.1, False),
+        "mpie": (0.2, "rpie", 0.05, True),
+    }[algorithm]
+    spectrum = _initial_spectrum(model, data, gains, weights, masks, bg)
+    pupil = np.asarray(model["pupil"], np.complex128)
+    velocity = np.zeros_like(spectrum)
+    anchor = spectrum.copy()
+    counter = 0
+    objectives = []
+    for _ in range(iterations):
+        objective_sum = weight_sum = 0.0
+        for f in range(frames):
+            fw = weights[f]
+            if fw == 0.0:
+                continue
+            patch = _extract(spectrum, model, f)
+            field = _fft_inverse(np.fft.ifftshift(patch * pupil))
+            intrinsic = np.abs(field) ** 2
+            valid = np.ones(intrinsic.shape, bool) if masks is None else masks[f] != 0
+            predicted = gains[f] * intrinsic + bg[f]
+            frame_loss = float(np.sum(_point_loss(predicted, data[f], loss)[valid]))
+            objective_sum += fw * (frame_loss / int(valid.sum()))
+            weight_sum += fw
+            target = np.maximum((data[f] - bg[f]) / gains[f], 0.0)
+            bright = intrinsic > EPS
+            ratio = np.sqrt(target / np.where(bright, intrinsic, 1.0))
+            difference = np.where(bright, field * ratio, np.sqrt(target) + 0j)
+            difference = np.where(valid, difference, field)
+            projected = np.fft.fftshift(_fft_forward(difference))
+            delta = projected - patch * pupil
+            power = np.abs(pupil) ** 2
+            maximum = max(float(power.max()), EPS)
+            den = power + EPS if denominator == "local" else (1.0 - alpha) * power + alpha * maximum + EPS
+            _insert_adjoint(spectrum, model, f, np.conj(pupil) * delta / den, fw * step)
+            if momentum:
+                counter += 1
+                if counter == 30:
+                    velocity = 0.9 * velocity + (spectrum - anchor)
+                    spectrum = spectrum + 0.9 * velocity
+                    anchor = spectrum.copy()
+                    counter = 0
+        objectives.append(objective_sum / weight_sum)
+    return dict(objectives=np.array(objectives), object_spectrum=spectrum,
+                object=_fft_inverse(np.fft.ifftshift(spectrum)))
+
+
+def _direct_model():
+    # tests/common/mod.rs:49-81: 8x8 detector, 16x16 grid, unit pupil, five integer crops.
+    shifts = [(-3, 0), (0, -3), (0, 0), (0, 3), (3, 0)]
+    return dict(h=8, w=8, mh=16, mw=16, start_row=np.array([4 + r for c, r in shifts], np.int64),
+                start_col=np.array([4 + c for c, r in shifts], np.int64), off_row=np.zeros(5), off_col=np.zeros(5),
+                pupil=np.ones((8, 8), np.complex128), support=np.ones((8, 8), np.uint8))
+
+
+def _compare(want, got, iterations):
+    assert np.allclose(got["objectives"], want["objectives"][:iterations], rtol=1e-9, atol=0.0)
+    scale = np.abs(want["object"]).max()
+    assert np.abs(got["object"] - want["object"]).max() <= 1e-9 * scale
+    assert np.abs(got["object_spectrum"] - want["object_spectrum"]).max() <= 1e-9 * np.abs(want["object_spectrum"]).max()
+
+
+@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie"])
+def test_direct_model_trajectories_agree(oracle_module, algorithm):
+    model = _direct_model()
+    rng = np.random.default_rng(21)
+    truth = np.exp(1j * 0.4 * rng.standard_normal((16, 16))) * (0.7 + 0.3 * rng.random((16, 16)))
+    data = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    iterations = 40 if algorithm == "mpie" else 6  # mPIE: 200 frame updates, six momentum events
+    want = oracle.run(oracle.Problem(model, data), algorithm, iterations=iterations)
+    _compare(want, restated_run(model, data, algorithm, iterations), iterations)
+
+
+@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie"])
+@pytest.mark.parametrize("loss", ["amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude"])
+def test_subpixel_masked_weighted_trajectories_agree(oracle_module, native_library, algorithm, loss):
+    """A compiled 5 x 5 planar tile (fractional crop offsets) with an
+    apodized, aberrated pupil (so |P|^2 varies and the local and rPIE
+    denominators differ), Poisson counts with gains and a per-frame
+    background, masked pixels and one zero-weight frame, under each loss."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    assert np.any(np.abs(model["off_row"]) > 1e-12) or np.any(np.abs(model["off_col"]) > 1e-12)
+    support = model["support"].astype(bool)
+    apodized = W.zernike_pupil(model["support"], 3) * np.where(support, 0.4 + 0.6 * np.random.default_rng(8).random(support.shape), 0.0)
+    model = dict(model, pupil=apodized)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 5)
+    intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    frames = intensity.shape[0]
+    rng = np.random.default_rng(6)
+    gains = rng.uniform(200.0, 400.0, frames)
+    background = rng.uniform(0.0, 3.0, (frames, 32, 32))
+    data = rng.poisson(intensity * gains[:, None, None]) + background
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = np.ones(frames)
+    weights[7] = 0.0
+    problem = oracle.Problem(model, data, gains=gains, background=background, masks=masks, weights=weights)
+    want = oracle.run(problem, algorithm, iterations=3, loss_type=loss)
+    got = restated_run(model, data, algorithm, 3, loss=loss, weights=weights, masks=masks, gains=gains,
+                       background=background)
+    _compare(want, got, 3)
