@@ -167,6 +167,64 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
                 object=_fft_inverse(np.fft.ifftshift(spectrum)))
 
 
+def _descent_factor(predicted, measured, loss):
+    """descent_factor (src/algorithms/gradient_descent.rs:1167-1178)."""
+    if loss == "amplitude_mse":
+        return 1.0 - np.sqrt(np.maximum(measured, 0.0)) / np.sqrt(np.maximum(predicted, EPS))
+    if loss == "intensity_mse":
+        return 2.0 * (predicted - measured)
+    if loss == "poisson_nll":
+        return 1.0 - np.maximum(measured, 0.0) / np.maximum(predicted, EPS)
+    amplitude = np.sqrt(np.maximum(predicted, EPS))
+    return np.clip(amplitude - np.sqrt(np.maximum(measured, 0.0)), -1.0, 1.0) / (2.0 * amplitude)
+
+
+def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", weights=None, masks=None,
+                gains=None, background=None, object_step=0.5):
+    """GradientDescent::step (gradient_descent.rs:405-671) without truncation,
+    pupil or illumination recovery, or regularisers: per batch, the frames'
+    Wirtinger gradients accumulate, each frame scaled by its weight times
+    N / (valid pixels), then the object takes one step of object_step over
+    the batch's active frame count. The loss compares |psi|^2 with
+    (I - background) / gain."""
+    frames = data.shape[0]
+    weights = np.ones(frames) if weights is None else np.asarray(weights, np.float64)
+    gains = np.ones(frames) if gains is None else np.asarray(gains, np.float64)
+    bg = np.zeros((frames, model["h"], model["w"])) if background is None else background
+    spectrum = _initial_spectrum(model, data, gains, weights, masks, bg)
+    pupil = np.asarray(model["pupil"], np.complex128)
+    n = model["h"] * model["w"]
+    objectives = []
+    for _ in range(iterations):
+        objective_sum = weight_sum = 0.0
+        for first in range(0, frames, batch_size):
+            maximum = max(float((np.abs(pupil) ** 2).max()), EPS)
+            gradient = np.zeros_like(spectrum)
+            active = 0
+            for f in range(first, min(first + batch_size, frames)):
+                fw = weights[f]
+                if fw == 0.0:
+                    continue
+                active += 1
+                patch = _extract(spectrum, model, f)
+                field = _fft_inverse(np.fft.ifftshift(patch * pupil))
+                intrinsic = np.maximum(np.abs(field) ** 2, 0.0)
+                valid = np.ones(intrinsic.shape, bool) if masks is None else masks[f] != 0
+                target = np.maximum((data[f] - bg[f]) / gains[f], 0.0)
+                frame_loss = float(np.sum(_point_loss(intrinsic, target, loss)[valid]))
+                objective_sum += fw * (frame_loss / int(valid.sum()))
+                weight_sum += fw
+                factor = np.where(valid, _descent_factor(intrinsic, target, loss), 0.0)
+                projected = np.fft.fftshift(_fft_forward(field * factor))
+                _insert_adjoint(gradient, model, f, np.conj(pupil) * projected / (maximum + EPS),
+                                fw * (n / int(valid.sum())))
+            if active > 0:
+                spectrum = spectrum - (object_step / active) * gradient
+        objectives.append(objective_sum / weight_sum)
+    return dict(objectives=np.array(objectives), object_spectrum=spectrum,
+                object=_fft_inverse(np.fft.ifftshift(spectrum)))
+
+
 def _direct_model():
     # tests/common/mod.rs:49-81: 8x8 detector, 16x16 grid, unit pupil, five integer crops.
     shifts = [(-3, 0), (0, -3), (0, 0), (0, 3), (3, 0)]
@@ -175,11 +233,11 @@ def _direct_model():
                 pupil=np.ones((8, 8), np.complex128), support=np.ones((8, 8), np.uint8))
 
 
-def _compare(want, got, iterations):
-    assert np.allclose(got["objectives"], want["objectives"][:iterations], rtol=1e-9, atol=0.0)
+def _compare(want, got, iterations, rtol=1e-9):
+    assert np.allclose(got["objectives"], want["objectives"][:iterations], rtol=rtol, atol=0.0)
     scale = np.abs(want["object"]).max()
-    assert np.abs(got["object"] - want["object"]).max() <= 1e-9 * scale
-    assert np.abs(got["object_spectrum"] - want["object_spectrum"]).max() <= 1e-9 * np.abs(want["object_spectrum"]).max()
+    assert np.abs(got["object"] - want["object"]).max() <= rtol * scale
+    assert np.abs(got["object_spectrum"] - want["object_spectrum"]).max() <= rtol * np.abs(want["object_spectrum"]).max()
 
 
 @pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie"])
@@ -222,3 +280,39 @@ def test_subpixel_masked_weighted_trajectories_agree(oracle_module, native_libra
     got = restated_run(model, data, algorithm, 3, loss=loss, weights=weights, masks=masks, gains=gains,
                        background=background)
     _compare(want, got, 3)
+
+
+@pytest.mark.parametrize("batch_size", [1, 4, 9])
+@pytest.mark.parametrize("loss", ["amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude"])
+def test_gradient_descent_trajectories_agree(oracle_module, native_library, batch_size, loss):
+    """Gradient descent on the same compiled tile, apodized pupil, gains,
+    background, masks and a zero-weight frame, in mini-batches. The Poisson
+    descent factor 1 - I / max(|psi|^2, eps) reaches about 1e8 on dark fringe
+    pixels, which magnifies last-bit differences between the two FFTs: with
+    one frame per step it is compared over two passes at 1e-5 (the
+    objectives still agree to 1e-9); every other case over three passes at
+    1e-9."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    support = model["support"].astype(bool)
+    model = dict(model, pupil=W.zernike_pupil(model["support"], 4)
+                 * np.where(support, 0.4 + 0.6 * np.random.default_rng(9).random(support.shape), 0.0))
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 6)
+    intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    frames = intensity.shape[0]
+    rng = np.random.default_rng(10)
+    gains = rng.uniform(200.0, 400.0, frames)
+    background = rng.uniform(0.0, 3.0, (frames, 32, 32))
+    data = rng.poisson(intensity * gains[:, None, None]) + background
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = np.ones(frames)
+    weights[3] = 0.0
+    problem = oracle.Problem(model, data, gains=gains, background=background, masks=masks, weights=weights)
+    sensitive = loss == "poisson_nll" and batch_size == 1
+    iterations = 2 if sensitive else 3
+    want = oracle.run(problem, "gd", iterations=iterations, loss_type=loss, batch_size=batch_size)
+    got = restated_gd(model, data, iterations, batch_size, loss=loss, weights=weights, masks=masks, gains=gains,
+                      background=background)
+    _compare(want, got, iterations, rtol=1e-5 if sensitive else 1e-9)
+    assert np.allclose(got["objectives"], want["objectives"], rtol=1e-9, atol=0.0)
