@@ -113,16 +113,19 @@ def _initial_spectrum(model, data, gains, weights, masks, background):
 
 
 def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
-                 gains=None, background=None):
-    """AP / FPIE / mPIE with the reference defaults, sequential schedule, batch 1."""
+                 gains=None, background=None, recover_gains=False, recover_background=False):
+    """AP / FPIE / mPIE / EPRY with a fixed pupil, with the reference defaults,
+    sequential schedule, batch 1; EPRY optionally recovers frame gains and
+    backgrounds (update_gain / update_background, common.rs:389-489)."""
     frames = data.shape[0]
     weights = np.ones(frames) if weights is None else np.asarray(weights, np.float64)
-    gains = np.ones(frames) if gains is None else np.asarray(gains, np.float64)
-    bg = np.zeros((frames, model["h"], model["w"])) if background is None else background
+    gains = np.ones(frames) if gains is None else np.array(gains, np.float64)
+    bg = np.zeros((frames, model["h"], model["w"])) if background is None else np.array(background, np.float64)
     step, denominator, alpha, momentum = {
         "ap": (1.0, "local", 0.0, False),
         "fpie": (0.8, "rpie", 0.1, False),
         "mpie": (0.2, "rpie", 0.05, True),
+        "epry": (0.8, "global", 0.0, False),
     }[algorithm]
     spectrum = _initial_spectrum(model, data, gains, weights, masks, bg)
     pupil = np.asarray(model["pupil"], np.complex128)
@@ -140,6 +143,15 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
             field = _fft_inverse(np.fft.ifftshift(patch * pupil))
             intrinsic = np.abs(field) ** 2
             valid = np.ones(intrinsic.shape, bool) if masks is None else masks[f] != 0
+            if recover_gains:
+                numerator = float(np.sum((intrinsic * np.maximum(data[f] - bg[f], 0.0))[valid]))
+                den_sum = float(np.sum((intrinsic * intrinsic)[valid]))
+                if den_sum > EPS:
+                    estimate = min(max(numerator / den_sum, 1e-6), 1e6)
+                    gains[f] = min(max(0.8 * gains[f] + 0.2 * estimate, 1e-6), 1e6)
+            if recover_background:
+                residual = float(np.sum((data[f] - gains[f] * intrinsic - bg[f])[valid]))
+                bg[f] = np.clip(bg[f] + 0.2 * residual / int(valid.sum()), 0.0, 1e12)
             predicted = gains[f] * intrinsic + bg[f]
             frame_loss = float(np.sum(_point_loss(predicted, data[f], loss)[valid]))
             objective_sum += fw * (frame_loss / int(valid.sum()))
@@ -153,7 +165,12 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
             delta = projected - patch * pupil
             power = np.abs(pupil) ** 2
             maximum = max(float(power.max()), EPS)
-            den = power + EPS if denominator == "local" else (1.0 - alpha) * power + alpha * maximum + EPS
+            if denominator == "local":
+                den = power + EPS
+            elif denominator == "global":
+                den = maximum + EPS
+            else:
+                den = (1.0 - alpha) * power + alpha * maximum + EPS
             _insert_adjoint(spectrum, model, f, np.conj(pupil) * delta / den, fw * step)
             if momentum:
                 counter += 1
@@ -164,7 +181,7 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
                     counter = 0
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
-                object=_fft_inverse(np.fft.ifftshift(spectrum)))
+                object=_fft_inverse(np.fft.ifftshift(spectrum)), frame_gains=gains, background=bg)
 
 
 def _descent_factor(predicted, measured, loss):
@@ -240,18 +257,21 @@ def _compare(want, got, iterations, rtol=1e-9):
     assert np.abs(got["object_spectrum"] - want["object_spectrum"]).max() <= rtol * np.abs(want["object_spectrum"]).max()
 
 
-@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie"])
+_ORACLE_OPTIONS = {"epry": dict(recover_pupil=False)}
+
+
+@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie", "epry"])
 def test_direct_model_trajectories_agree(oracle_module, algorithm):
     model = _direct_model()
     rng = np.random.default_rng(21)
     truth = np.exp(1j * 0.4 * rng.standard_normal((16, 16))) * (0.7 + 0.3 * rng.random((16, 16)))
     data = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
     iterations = 40 if algorithm == "mpie" else 6  # mPIE: 200 frame updates, six momentum events
-    want = oracle.run(oracle.Problem(model, data), algorithm, iterations=iterations)
+    want = oracle.run(oracle.Problem(model, data), algorithm, iterations=iterations, **_ORACLE_OPTIONS.get(algorithm, {}))
     _compare(want, restated_run(model, data, algorithm, iterations), iterations)
 
 
-@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie"])
+@pytest.mark.parametrize("algorithm", ["ap", "fpie", "mpie", "epry"])
 @pytest.mark.parametrize("loss", ["amplitude_mse", "intensity_mse", "poisson_nll", "huber_amplitude"])
 def test_subpixel_masked_weighted_trajectories_agree(oracle_module, native_library, algorithm, loss):
     """A compiled 5 x 5 planar tile (fractional crop offsets) with an
@@ -276,10 +296,42 @@ def test_subpixel_masked_weighted_trajectories_agree(oracle_module, native_libra
     weights = np.ones(frames)
     weights[7] = 0.0
     problem = oracle.Problem(model, data, gains=gains, background=background, masks=masks, weights=weights)
-    want = oracle.run(problem, algorithm, iterations=3, loss_type=loss)
+    want = oracle.run(problem, algorithm, iterations=3, loss_type=loss, **_ORACLE_OPTIONS.get(algorithm, {}))
     got = restated_run(model, data, algorithm, 3, loss=loss, weights=weights, masks=masks, gains=gains,
                        background=background)
     _compare(want, got, 3)
+
+
+@pytest.mark.parametrize("recover", ["gains", "background", "both"])
+def test_epry_gain_and_background_recovery_trajectories_agree(oracle_module, native_library, recover):
+    """EPRY with a fixed pupil recovering frame gains and per-frame
+    backgrounds that the model gets wrong, on the same compiled tile."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 7)
+    intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    frames = intensity.shape[0]
+    rng = np.random.default_rng(12)
+    true_gains = rng.uniform(200.0, 400.0, frames)
+    true_background = rng.uniform(2.0, 6.0, frames)[:, None, None] * np.ones((1, 32, 32))
+    data = rng.poisson(intensity * true_gains[:, None, None]) + true_background
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    model_gains = np.full(frames, 300.0)
+    model_background = np.full((frames, 32, 32), 4.0)
+    gains_on, background_on = recover in ("gains", "both"), recover in ("background", "both")
+    problem = oracle.Problem(model, data, gains=model_gains, background=model_background, masks=masks)
+    want = oracle.run(problem, "epry", iterations=3, recover_pupil=False, recover_gains=gains_on,
+                      recover_background=background_on)
+    got = restated_run(model, data, "epry", 3, masks=masks, gains=model_gains, background=model_background,
+                       recover_gains=gains_on, recover_background=background_on)
+    _compare(want, got, 3)
+    if gains_on:
+        assert np.allclose(got["frame_gains"], want["frame_gains"], rtol=1e-9, atol=0.0)
+        assert not np.allclose(got["frame_gains"], model_gains)
+    if background_on:
+        assert np.allclose(got["background"], want["background"], rtol=1e-9, atol=0.0)
+        assert not np.allclose(got["background"], model_background)
 
 
 @pytest.mark.parametrize("batch_size", [1, 4, 9])
