@@ -113,7 +113,7 @@ def _initial_spectrum(model, data, gains, weights, masks, background):
 
 
 def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
-                 gains=None, background=None, recover_gains=False, recover_background=False):
+                 gains=None, background=None, recover_gains=False, recover_background=False, order=None):
     """AP / FPIE / mPIE / EPRY with a fixed pupil, with the reference defaults,
     sequential schedule, batch 1; EPRY optionally recovers frame gains and
     backgrounds (update_gain / update_background, common.rs:389-489)."""
@@ -135,7 +135,7 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
     objectives = []
     for _ in range(iterations):
         objective_sum = weight_sum = 0.0
-        for f in range(frames):
+        for f in (range(frames) if order is None else order):
             fw = weights[f]
             if fw == 0.0:
                 continue
@@ -197,7 +197,7 @@ def _descent_factor(predicted, measured, loss):
 
 
 def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", weights=None, masks=None,
-                gains=None, background=None, object_step=0.5):
+                gains=None, background=None, object_step=0.5, order=None):
     """GradientDescent::step (gradient_descent.rs:405-671) without truncation,
     pupil or illumination recovery, or regularisers: per batch, the frames'
     Wirtinger gradients accumulate, each frame scaled by its weight times
@@ -214,11 +214,12 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
     objectives = []
     for _ in range(iterations):
         objective_sum = weight_sum = 0.0
+        sequence = list(range(frames)) if order is None else list(order)
         for first in range(0, frames, batch_size):
             maximum = max(float((np.abs(pupil) ** 2).max()), EPS)
             gradient = np.zeros_like(spectrum)
             active = 0
-            for f in range(first, min(first + batch_size, frames)):
+            for f in sequence[first:first + batch_size]:
                 fw = weights[f]
                 if fw == 0.0:
                     continue
@@ -240,6 +241,31 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
                 object=_fft_inverse(np.fft.ifftshift(spectrum)))
+
+
+def _schedule(name, model, data, weights, masks, background):
+    """FrameSchedule::order / order_for_problem (src/reconstruction/schedule.rs:35-131):
+    stable sorts by |k|, by |k| then azimuth in [0, 2 pi), or by descending
+    weight * sqrt(mean(max(I - background, 0))) over unmasked pixels with
+    ties in frame order and zero-weight frames last."""
+    frames = data.shape[0]
+    kx, ky = np.asarray(model["kx"], np.float64), np.asarray(model["ky"], np.float64)
+    radius = [float(np.hypot(kx[f], ky[f])) for f in range(frames)]
+    if name == "sequential":
+        return list(range(frames))
+    if name == "brightfield_first":
+        return sorted(range(frames), key=lambda f: radius[f])
+    if name == "spiral_out":
+        return sorted(range(frames), key=lambda f: (radius[f], math.atan2(ky[f], kx[f]) % math.tau))
+    scores = []
+    for f in range(frames):
+        valid = np.ones(data.shape[1:], bool) if masks is None else masks[f] != 0
+        if weights[f] == 0.0 or not valid.any():
+            scores.append(-math.inf)
+            continue
+        signal = float(np.sum(np.maximum(data[f] - background[f], 0.0)[valid]))
+        scores.append(weights[f] * math.sqrt(signal / int(valid.sum())))
+    return sorted(range(frames), key=lambda f: (-scores[f], f))
 
 
 def _direct_model():
@@ -368,3 +394,38 @@ def test_gradient_descent_trajectories_agree(oracle_module, native_library, batc
                       background=background)
     _compare(want, got, iterations, rtol=1e-5 if sensitive else 1e-9)
     assert np.allclose(got["objectives"], want["objectives"], rtol=1e-9, atol=0.0)
+
+
+@pytest.mark.parametrize("schedule", ["brightfield_first", "spiral_out", "snr_weighted"])
+def test_schedules_order_frames_as_the_reference(oracle_module, native_library, schedule):
+    """The same tile under each deterministic schedule, with mPIE (frame by
+    frame) and gradient descent (batches of four taken from the ordered
+    frames), against the oracle's runs."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 8)
+    intensity = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    frames = intensity.shape[0]
+    rng = np.random.default_rng(13)
+    gains = np.full(frames, 300.0)
+    background = rng.uniform(0.0, 3.0, (frames, 32, 32))
+    data = rng.poisson(intensity * gains[:, None, None]) + background
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = rng.uniform(0.5, 1.5, frames)
+    weights[11] = 0.0
+    # Frames 2 and 5 score alike, so the SNR order must break their tie by index.
+    data[5], masks[5], background[5], weights[5] = data[2], masks[2], background[2], weights[2]
+    order = _schedule(schedule, model, data, weights, masks, background)
+    assert sorted(order) == list(range(frames)) and order != list(range(frames))
+    if schedule == "snr_weighted":
+        assert order.index(2) + 1 == order.index(5) and order[-1] == 11
+    problem = oracle.Problem(model, data, gains=gains, background=background, masks=masks, weights=weights)
+    want = oracle.run(problem, "mpie", iterations=2, schedule=schedule)
+    got = restated_run(model, data, "mpie", 2, weights=weights, masks=masks, gains=gains, background=background,
+                       order=order)
+    _compare(want, got, 2)
+    want = oracle.run(problem, "gd", iterations=2, schedule=schedule, batch_size=4)
+    got = restated_gd(model, data, 2, 4, weights=weights, masks=masks, gains=gains, background=background,
+                      order=order)
+    _compare(want, got, 2)
