@@ -113,7 +113,8 @@ def _initial_spectrum(model, data, gains, weights, masks, background):
 
 
 def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
-                 gains=None, background=None, recover_gains=False, recover_background=False, order=None):
+                 gains=None, background=None, recover_gains=False, recover_background=False, order=None,
+                 initial_spectrum=None):
     """AP / FPIE / mPIE / EPRY with a fixed pupil, with the reference defaults,
     sequential schedule, batch 1; EPRY optionally recovers frame gains and
     backgrounds (update_gain / update_background, common.rs:389-489)."""
@@ -127,7 +128,8 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
         "mpie": (0.2, "rpie", 0.05, True),
         "epry": (0.8, "global", 0.0, False),
     }[algorithm]
-    spectrum = _initial_spectrum(model, data, gains, weights, masks, bg)
+    spectrum = (_initial_spectrum(model, data, gains, weights, masks, bg) if initial_spectrum is None
+                else np.array(initial_spectrum, np.complex128))
     pupil = np.asarray(model["pupil"], np.complex128)
     velocity = np.zeros_like(spectrum)
     anchor = spectrum.copy()
@@ -429,3 +431,149 @@ def test_schedules_order_frames_as_the_reference(oracle_module, native_library, 
     got = restated_gd(model, data, 2, 4, weights=weights, masks=masks, gains=gains, background=background,
                       order=order)
     _compare(want, got, 2)
+
+
+def restated_spectral(channels, frames, data, iterations, *, shared=False, weights=None, masks=None,
+                      loss="amplitude_mse", object_step=1.0, initial_spectra=None):
+    """Spectral alternating projection (src/algorithms/spectral.rs:182-271,
+    src/reconstruction/spectral.rs:127-230 and :271-331): each exposure's
+    modes are evaluated from the pre-exposure objects, share one projection
+    ratio against gain * sum_k w_k |psi_k|^2 + background, and each adds its
+    local-denominator update scaled by w_k / sum w."""
+    exposures = len(frames)
+    weights = np.ones(exposures) if weights is None else np.asarray(weights, np.float64)
+    count = 1 if shared else len(channels)
+    index = (lambda c: 0) if shared else (lambda c: c)
+    fg = [np.asarray(ch.get("frame_gains", np.ones(len(ch["start_row"]))), np.float64) for ch in channels]
+    h, w, mh, mw = channels[0]["h"], channels[0]["w"], channels[0]["mh"], channels[0]["mw"]
+    spectra = []
+    for o in range(count):
+        average, weight = np.zeros((h, w)), np.zeros((h, w))
+        total_amplitude = total_weight = 0.0
+        for e, (gain, background, contributions) in enumerate(frames):
+            if not any(index(c) == o for c, _, _ in contributions) or weights[e] == 0.0:
+                continue
+            g = sum(s * fg[c][l] for c, l, s in contributions) * gain
+            valid = np.ones((h, w), bool) if masks is None else masks[e] != 0
+            amplitude = np.sqrt(np.maximum((data[e] - background) / g, 0.0))
+            average[valid] += weights[e] * amplitude[valid]
+            weight[valid] += weights[e]
+            total_amplitude += float(np.sum(weights[e] * amplitude[valid]))
+            total_weight += weights[e] * int(valid.sum())
+        average = np.where(weight > 0.0, average / np.where(weight > 0.0, weight, 1.0), total_amplitude / total_weight)
+        obj = average[((np.arange(mh) * h) // mh)[:, None], ((np.arange(mw) * w) // mw)[None, :]].astype(np.complex128)
+        spectra.append(np.fft.fftshift(_fft_forward(obj)))
+    if initial_spectra is not None:
+        spectra = [np.array(x, np.complex128) for x in initial_spectra]
+    objectives = []
+    for _ in range(iterations):
+        objective_sum = weight_sum = 0.0
+        for e, (gain, background, contributions) in enumerate(frames):
+            fw = weights[e]
+            if fw == 0.0:
+                continue
+            separate = len(contributions) == 1
+            effective_gain = gain * (contributions[0][2] * fg[contributions[0][0]][contributions[0][1]] if separate else 1.0)
+            modes, predicted = [], np.zeros((h, w))
+            for c, l, s in contributions:
+                mode_weight = 1.0 if separate else s * fg[c][l]
+                exit_wave = _extract(spectra[index(c)], channels[c], l) * channels[c]["pupil"]
+                psi = _fft_inverse(np.fft.ifftshift(exit_wave))
+                predicted = predicted + mode_weight * np.abs(psi) ** 2
+                modes.append((c, l, mode_weight, psi, exit_wave))
+            mode_sum = sum(m[2] for m in modes)
+            valid = np.ones((h, w), bool) if masks is None else masks[e] != 0
+            loss_value = float(np.sum(_point_loss(effective_gain * predicted + background, data[e], loss)[valid]))
+            objective_sum += fw * (loss_value / int(valid.sum()))
+            weight_sum += fw
+            target = np.maximum((data[e] - background) / effective_gain, 0.0)
+            bright = predicted > EPS
+            ratio = np.sqrt(target / np.where(bright, predicted, 1.0))
+            dark = np.sqrt(target / mode_sum)
+            for c, l, mode_weight, psi, exit_wave in modes:
+                projected = np.where(valid, np.where(bright, psi * ratio, dark + 0j), psi)
+                centred = np.fft.fftshift(_fft_forward(projected))
+                pupil = channels[c]["pupil"]
+                update = np.conj(pupil) * (centred - exit_wave) / (np.abs(pupil) ** 2 + EPS)
+                _insert_adjoint(spectra[index(c)], channels[c], l, update, fw * object_step * (mode_weight / mode_sum))
+        objectives.append(objective_sum / weight_sum)
+    return dict(objectives=np.array(objectives), spectra=np.stack(spectra),
+                objects=np.stack([_fft_inverse(np.fft.ifftshift(s)) for s in spectra]))
+
+
+@pytest.mark.parametrize("plan", ["separate", "multiplexed_shared"])
+def test_spectral_trajectories_agree(oracle_module, plan):
+    """Three channels compiled on one grid: separate exposures with
+    independent objects, or every exposure mixing all three channels into
+    one shared object; frame and exposure gains, backgrounds, masks and a
+    zero-weight exposure."""
+    import spectral_cases as sc
+
+    gains = [np.random.default_rng(14 + c).uniform(0.8, 1.2, len(sc.DIRECTIONS)) for c in range(3)]
+    channels = [dict(ch, frame_gains=g) for ch, g in zip(sc.compile_channels(3, image_shape=(32, 32)), gains)]
+    shared = plan == "multiplexed_shared"
+    if shared:
+        frames = [(1.7, 0.3, [(c, l, 0.4 + 0.2 * c) for c in range(3)]) for l in range(len(sc.DIRECTIONS))]
+    else:
+        frames = [(1.0 + 0.1 * l, 0.2 * c, [(c, l, 1.0)]) for c in range(3) for l in range(len(sc.DIRECTIONS))]
+    truth = sc.truth_objects((channels[0]["mh"], channels[0]["mw"]), 1 if shared else 3)
+    problem = oracle.SpectralProblem(channels, frames, shared_object=shared)
+    intensity = oracle.spectral_forward(problem, sc.spectra_of(truth))
+    rng = np.random.default_rng(15)
+    data = rng.poisson(intensity * 500.0) / 500.0
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = np.ones(len(frames))
+    weights[1] = 0.0
+    want = oracle.spectral_run(oracle.SpectralProblem(channels, frames, data, shared_object=shared, weights=weights,
+                                                      masks=masks), iterations=4)
+    got = restated_spectral(channels, frames, data, 4, shared=shared, weights=weights, masks=masks)
+    assert np.allclose(got["objectives"], want["objectives"], rtol=1e-9, atol=0.0)
+    assert np.abs(got["spectra"] - want["spectra"]).max() <= 1e-9 * np.abs(want["spectra"]).max()
+    assert np.abs(got["objects"] - want["objects"]).max() <= 1e-9 * np.abs(want["objects"]).max()
+
+
+def _zero_stencil(spectrum, model, source):
+    """The spectrum with `source`'s whole crop stencil set to zero, so that
+    frame's field is exactly zero and every pixel takes the dark branch."""
+    out = np.array(spectrum, np.complex128)
+    taps, h, w = _stencil(model, source)
+    for r, c, _ in taps:
+        out[r:r + h, c:c + w] = 0.0
+    return out
+
+
+@pytest.mark.parametrize("algorithm", ["ap", "mpie"])
+def test_dark_frames_take_the_fallback_amplitude(oracle_module, native_library, algorithm):
+    """A start whose spectrum vanishes on frame 0's stencil: every pixel of
+    that frame is dark (|psi|^2 <= eps), so its projection is the fallback
+    sqrt(target) (common.rs:184-190) and its update is still non-zero."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 9)
+    spectrum = oracle.object_spectrum(truth)
+    data = oracle.forward_stack(oracle.Problem(model, None), spectrum)
+    start = _zero_stencil(spectrum, model, 0)
+    want = oracle.run(oracle.Problem(model, data), algorithm, iterations=2, initial_spectrum=start)
+    got = restated_run(model, data, algorithm, 2, initial_spectrum=start)
+    _compare(want, got, 2)
+
+
+def test_dark_spectral_exposure_takes_the_fallback_over_the_mode_weights(oracle_module):
+    """The same for a multiplexed exposure on a shared object: its fallback
+    amplitude is sqrt(target / sum of mode weights) (spectral.rs:221-225)."""
+    import spectral_cases as sc
+
+    channels = sc.compile_channels(3, image_shape=(32, 32))
+    frames = [(1.7, 0.3, [(c, l, 0.4 + 0.2 * c) for c in range(3)]) for l in range(len(sc.DIRECTIONS))]
+    truth = sc.truth_objects((channels[0]["mh"], channels[0]["mw"]), 1)
+    spectra = sc.spectra_of(truth)
+    data = oracle.spectral_forward(oracle.SpectralProblem(channels, frames, shared_object=True), spectra)
+    start = spectra[0]
+    for c in range(3):
+        start = _zero_stencil(start, channels[c], 0)
+    want = oracle.spectral_run(oracle.SpectralProblem(channels, frames, data, shared_object=True), iterations=2,
+                               initial_spectra=start[None])
+    got = restated_spectral(channels, frames, data, 2, shared=True, initial_spectra=start[None])
+    assert np.allclose(got["objectives"], want["objectives"], rtol=1e-9, atol=0.0)
+    assert np.abs(got["spectra"] - want["spectra"]).max() <= 1e-9 * np.abs(want["spectra"]).max()
