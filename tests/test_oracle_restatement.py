@@ -114,7 +114,7 @@ def _initial_spectrum(model, data, gains, weights, masks, background):
 
 def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
                  gains=None, background=None, recover_gains=False, recover_background=False, order=None,
-                 initial_spectrum=None):
+                 initial_spectrum=None, progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001):
     """AP / FPIE / mPIE / EPRY with a fixed pupil, with the reference defaults,
     sequential schedule, batch 1; EPRY optionally recovers frame gains and
     backgrounds (update_gain / update_background, common.rs:389-489)."""
@@ -127,6 +127,7 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
         "fpie": (0.8, "rpie", 0.1, False),
         "mpie": (0.2, "rpie", 0.05, True),
         "epry": (0.8, "global", 0.0, False),
+        "adaptive_ap": (1.0, "local", 0.0, False),
     }[algorithm]
     spectrum = (_initial_spectrum(model, data, gains, weights, masks, bg) if initial_spectrum is None
                 else np.array(initial_spectrum, np.complex128))
@@ -135,7 +136,14 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
     anchor = spectrum.copy()
     counter = 0
     objectives = []
-    for _ in range(iterations):
+    steps = []
+    for i in range(iterations):
+        if algorithm == "adaptive_ap" and i >= 2:
+            # AdaptiveAlternatingProjection::begin_iteration (adaptive_alternating_projection.rs:245-307).
+            progress = (objectives[-2] - objectives[-1]) / max(objectives[-2], EPS)
+            if progress <= progress_threshold:
+                step = max(step * reduction_factor, minimum_object_step)
+        steps.append(step)
         objective_sum = weight_sum = 0.0
         for f in (range(frames) if order is None else order):
             fw = weights[f]
@@ -183,7 +191,8 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
                     counter = 0
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
-                object=_fft_inverse(np.fft.ifftshift(spectrum)), frame_gains=gains, background=bg)
+                object=_fft_inverse(np.fft.ifftshift(spectrum)), frame_gains=gains, background=bg,
+                object_steps=np.array(steps))
 
 
 def _descent_factor(predicted, measured, loss):
@@ -577,3 +586,22 @@ def test_dark_spectral_exposure_takes_the_fallback_over_the_mode_weights(oracle_
     got = restated_spectral(channels, frames, data, 2, shared=True, initial_spectra=start[None])
     assert np.allclose(got["objectives"], want["objectives"], rtol=1e-9, atol=0.0)
     assert np.abs(got["spectra"] - want["spectra"]).max() <= 1e-9 * np.abs(want["spectra"]).max()
+
+
+def test_adaptive_ap_step_controller_trajectory_agrees(oracle_module, native_library):
+    """Adaptive AP with a threshold that most passes miss, so the step halves
+    down to its floor, on the compiled tile with an apodized pupil."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    support = model["support"].astype(bool)
+    model = dict(model, pupil=np.where(support, 0.5 + 0.5 * np.random.default_rng(16).random(support.shape), 0.0)
+                 + 0j)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 10)
+    data = oracle.forward_stack(oracle.Problem(model, None), oracle.object_spectrum(truth))
+    options = dict(progress_threshold=0.6, reduction_factor=0.5, minimum_object_step=0.2)
+    want = oracle.run(oracle.Problem(model, data), "adaptive_ap", iterations=8, **options)
+    got = restated_run(model, data, "adaptive_ap", 8, **options)
+    _compare(want, got, 8)
+    assert np.array_equal(got["object_steps"], want["object_steps"][:8])
+    assert list(got["object_steps"]) == [1.0, 1.0, 1.0, 1.0, 0.5, 0.25, 0.2, 0.2]
