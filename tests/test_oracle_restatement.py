@@ -208,50 +208,91 @@ def _descent_factor(predicted, measured, loss):
 
 
 def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", weights=None, masks=None,
-                gains=None, background=None, object_step=0.5, order=None):
+                gains=None, background=None, object_step=0.5, order=None, recover_pupil=False, pupil_step=0.05,
+                truncation_threshold=None, canonicalize=None):
     """GradientDescent::step (gradient_descent.rs:405-671) without truncation,
     pupil or illumination recovery, or regularisers: per batch, the frames'
     Wirtinger gradients accumulate, each frame scaled by its weight times
     N / (valid pixels), then the object takes one step of object_step over
     the batch's active frame count. The loss compares |psi|^2 with
-    (I - background) / gain."""
+    (I - background) / gain. Optionally the pupil descends too (its gradient
+    over max |patch|^2, stepped after the batch, then the support applied),
+    and Poisson truncation (compute_truncation_statistics, :701-791) drops
+    pixels with |target - prediction| > scale * sqrt(prediction) from the
+    gradient, the scale taken from the pre-batch state. With pupil recovery
+    the runner canonicalises object and pupil after initialisation and after
+    every pass (src/reconstruction/runner.rs:122,220); `canonicalize` is that
+    gauge (src/algorithms/gauge.rs), which this file does not restate."""
     frames = data.shape[0]
     weights = np.ones(frames) if weights is None else np.asarray(weights, np.float64)
     gains = np.ones(frames) if gains is None else np.asarray(gains, np.float64)
     bg = np.zeros((frames, model["h"], model["w"])) if background is None else background
     spectrum = _initial_spectrum(model, data, gains, weights, masks, bg)
-    pupil = np.asarray(model["pupil"], np.complex128)
+    pupil = np.array(model["pupil"], np.complex128)
+    support = np.asarray(model["support"]) != 0
     n = model["h"] * model["w"]
     objectives = []
+    rejected = 0
+    if recover_pupil and canonicalize is not None:
+        spectrum, pupil = canonicalize(spectrum, pupil)
+
+    def frame_terms(f):
+        patch = _extract(spectrum, model, f)
+        field = _fft_inverse(np.fft.ifftshift(patch * pupil))
+        valid = np.ones(field.shape, bool) if masks is None else masks[f] != 0
+        target = np.maximum((data[f] - bg[f]) / gains[f], 0.0)
+        return patch, field, np.maximum(np.abs(field) ** 2, 0.0), valid, target
     for _ in range(iterations):
         objective_sum = weight_sum = 0.0
         sequence = list(range(frames)) if order is None else list(order)
         for first in range(0, frames, batch_size):
+            batch = [f for f in sequence[first:first + batch_size]]
+            scale = None
+            if truncation_threshold is not None:
+                residual = weight_total = 0.0
+                for f in batch:
+                    if weights[f] == 0.0:
+                        continue
+                    _, _, intrinsic, valid, target = frame_terms(f)
+                    residual += float(np.sum(weights[f] * np.abs(target - intrinsic)[valid]))
+                    weight_total += weights[f] * int(valid.sum())
+                rms = max(float(np.sqrt(np.sum(np.abs(spectrum) ** 2))), math.sqrt(EPS))
+                scale = truncation_threshold * (residual / weight_total if weight_total > 0.0 else 0.0) / rms
             maximum = max(float((np.abs(pupil) ** 2).max()), EPS)
             gradient = np.zeros_like(spectrum)
+            pupil_gradient = np.zeros_like(pupil)
             active = 0
-            for f in sequence[first:first + batch_size]:
+            for f in batch:
                 fw = weights[f]
                 if fw == 0.0:
                     continue
                 active += 1
-                patch = _extract(spectrum, model, f)
-                field = _fft_inverse(np.fft.ifftshift(patch * pupil))
-                intrinsic = np.maximum(np.abs(field) ** 2, 0.0)
-                valid = np.ones(intrinsic.shape, bool) if masks is None else masks[f] != 0
-                target = np.maximum((data[f] - bg[f]) / gains[f], 0.0)
+                patch, field, intrinsic, valid, target = frame_terms(f)
                 frame_loss = float(np.sum(_point_loss(intrinsic, target, loss)[valid]))
                 objective_sum += fw * (frame_loss / int(valid.sum()))
                 weight_sum += fw
-                factor = np.where(valid, _descent_factor(intrinsic, target, loss), 0.0)
+                kept = valid
+                if scale is not None:
+                    kept = valid & (np.abs(target - intrinsic) <= scale * np.sqrt(intrinsic))
+                    rejected += int(np.sum(valid & ~kept))
+                factor = np.where(kept, _descent_factor(intrinsic, target, loss), 0.0)
                 projected = np.fft.fftshift(_fft_forward(field * factor))
-                _insert_adjoint(gradient, model, f, np.conj(pupil) * projected / (maximum + EPS),
-                                fw * (n / int(valid.sum())))
+                valid_scale = n / int(valid.sum())
+                if recover_pupil:
+                    object_power = max(float((np.abs(patch) ** 2).max()), EPS)
+                    pupil_gradient += fw * valid_scale * np.conj(patch) * projected / (object_power + EPS)
+                _insert_adjoint(gradient, model, f, np.conj(pupil) * projected / (maximum + EPS), fw * valid_scale)
             if active > 0:
                 spectrum = spectrum - (object_step / active) * gradient
+                if recover_pupil:
+                    pupil = pupil - (pupil_step / active) * pupil_gradient
+            if recover_pupil:
+                pupil = np.where(support, pupil, 0.0)
+        if recover_pupil and canonicalize is not None:
+            spectrum, pupil = canonicalize(spectrum, pupil)
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
-                object=_fft_inverse(np.fft.ifftshift(spectrum)))
+                object=_fft_inverse(np.fft.ifftshift(spectrum)), pupil=pupil, rejected=rejected)
 
 
 def _schedule(name, model, data, weights, masks, background):
@@ -605,3 +646,33 @@ def test_adaptive_ap_step_controller_trajectory_agrees(oracle_module, native_lib
     _compare(want, got, 8)
     assert np.array_equal(got["object_steps"], want["object_steps"][:8])
     assert list(got["object_steps"]) == [1.0, 1.0, 1.0, 1.0, 0.5, 0.25, 0.2, 0.2]
+
+
+@pytest.mark.parametrize("variant", ["pupil_recovery", "poisson_truncation"])
+def test_gradient_descent_pupil_recovery_and_truncation_agree(oracle_module, native_library, variant):
+    """GD recovering an aberrated pupil inside its support, and GD under the
+    Poisson loss with truncation that rejects outliers planted in the data,
+    in batches of four with masked pixels, against the oracle."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    true_pupil = W.zernike_pupil(model["support"], 5)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 11)
+    intensity = oracle.forward_stack(oracle.Problem(dict(model, pupil=true_pupil), None), oracle.object_spectrum(truth))
+    rng = np.random.default_rng(17)
+    data = rng.poisson(intensity * 300.0) / 300.0
+    data.reshape(data.shape[0], -1)[:, ::97] *= 20.0  # outliers
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    kw = (dict(recover_pupil=True, pupil_step=0.05) if variant == "pupil_recovery"
+          else dict(loss="poisson_nll", truncation_threshold=3.0))
+    oracle_kw = (dict(recover_pupil=True, pupil_step=0.05) if variant == "pupil_recovery"
+                 else dict(loss_type="poisson_nll", poisson_truncation_threshold=3.0))
+    want = oracle.run(oracle.Problem(model, data, masks=masks), "gd", iterations=3, batch_size=4, **oracle_kw)
+    gauge = lambda spectrum, pupil: oracle.canonicalize(oracle.Problem(model, data, masks=masks), spectrum, pupil)
+    got = restated_gd(model, data, 3, 4, masks=masks, canonicalize=gauge, **kw)
+    _compare(want, got, 3)
+    if variant == "pupil_recovery":
+        assert np.abs(got["pupil"] - want["pupil"]).max() <= 1e-9 * np.abs(want["pupil"]).max()
+        assert not np.allclose(got["pupil"], model["pupil"])
+    else:
+        assert got["rejected"] > 0
