@@ -114,10 +114,13 @@ def _initial_spectrum(model, data, gains, weights, masks, background):
 
 def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", weights=None, masks=None,
                  gains=None, background=None, recover_gains=False, recover_background=False, order=None,
-                 initial_spectrum=None, progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001):
-    """AP / FPIE / mPIE / EPRY with a fixed pupil, with the reference defaults,
-    sequential schedule, batch 1; EPRY optionally recovers frame gains and
-    backgrounds (update_gain / update_background, common.rs:389-489)."""
+                 initial_spectrum=None, progress_threshold=0.01, reduction_factor=0.5, minimum_object_step=0.001,
+                 recover_pupil=False, pupil_step=0.1, canonicalize=None):
+    """AP / adaptive AP / FPIE / mPIE / EPRY with the reference defaults,
+    batch 1; EPRY optionally recovers frame gains and backgrounds
+    (update_gain / update_background, common.rs:389-489) and the pupil
+    (common.rs:272-302), the runner then canonicalising object and pupil after
+    initialisation and after every pass through `canonicalize`."""
     frames = data.shape[0]
     weights = np.ones(frames) if weights is None else np.asarray(weights, np.float64)
     gains = np.ones(frames) if gains is None else np.array(gains, np.float64)
@@ -131,7 +134,10 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
     }[algorithm]
     spectrum = (_initial_spectrum(model, data, gains, weights, masks, bg) if initial_spectrum is None
                 else np.array(initial_spectrum, np.complex128))
-    pupil = np.asarray(model["pupil"], np.complex128)
+    pupil = np.array(model["pupil"], np.complex128)
+    support = np.asarray(model["support"]) != 0
+    if recover_pupil and canonicalize is not None:
+        spectrum, pupil = canonicalize(spectrum, pupil)
     velocity = np.zeros_like(spectrum)
     anchor = spectrum.copy()
     counter = 0
@@ -182,6 +188,10 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
             else:
                 den = (1.0 - alpha) * power + alpha * maximum + EPS
             _insert_adjoint(spectrum, model, f, np.conj(pupil) * delta / den, fw * step)
+            if recover_pupil:
+                object_power = max(float((np.abs(patch) ** 2).max()), EPS)
+                pupil = pupil + fw * pupil_step * (np.conj(patch) * delta / (object_power + EPS))
+                pupil = np.where(support, pupil, 0.0)
             if momentum:
                 counter += 1
                 if counter == 30:
@@ -189,10 +199,12 @@ def restated_run(model, data, algorithm, iterations, *, loss="amplitude_mse", we
                     spectrum = spectrum + 0.9 * velocity
                     anchor = spectrum.copy()
                     counter = 0
+        if recover_pupil and canonicalize is not None:
+            spectrum, pupil = canonicalize(spectrum, pupil)
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
                 object=_fft_inverse(np.fft.ifftshift(spectrum)), frame_gains=gains, background=bg,
-                object_steps=np.array(steps))
+                object_steps=np.array(steps), pupil=pupil)
 
 
 def _descent_factor(predicted, measured, loss):
@@ -676,3 +688,24 @@ def test_gradient_descent_pupil_recovery_and_truncation_agree(oracle_module, nat
         assert not np.allclose(got["pupil"], model["pupil"])
     else:
         assert got["rejected"] > 0
+
+
+def test_epry_pupil_recovery_trajectory_agrees(oracle_module, native_library):
+    """EPRY recovering an aberrated pupil (apodized start) with masked
+    pixels, the gauge step through the oracle's canonicalisation."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    true_pupil = W.zernike_pupil(model["support"], 6)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 12)
+    intensity = oracle.forward_stack(oracle.Problem(dict(model, pupil=true_pupil), None), oracle.object_spectrum(truth))
+    rng = np.random.default_rng(18)
+    data = rng.poisson(intensity * 300.0) / 300.0
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    problem = oracle.Problem(model, data, masks=masks)
+    want = oracle.run(problem, "epry", iterations=3, recover_pupil=True)
+    got = restated_run(model, data, "epry", 3, masks=masks, recover_pupil=True,
+                       canonicalize=lambda s, p: oracle.canonicalize(problem, s, p))
+    _compare(want, got, 3)
+    assert np.abs(got["pupil"] - want["pupil"]).max() <= 1e-9 * np.abs(want["pupil"]).max()
+    assert not np.allclose(got["pupil"], model["pupil"])
