@@ -219,9 +219,38 @@ def _descent_factor(predicted, measured, loss):
     return np.clip(amplitude - np.sqrt(np.maximum(measured, 0.0)), -1.0, 1.0) / (2.0 * amplitude)
 
 
+def _tv_gradient(values, epsilon):
+    """apply_complex_tv_step's gradient (src/algorithms/regularization.rs:5-45):
+    forward differences, each pixel's pair normalised by
+    sqrt(|dx|^2 + |dy|^2 + eps^2), scattered back with opposite signs."""
+    dh = np.zeros_like(values)
+    dv = np.zeros_like(values)
+    dh[:, :-1] = values[:, 1:] - values[:, :-1]
+    dv[:-1, :] = values[1:, :] - values[:-1, :]
+    norm = np.sqrt(np.abs(dh) ** 2 + np.abs(dv) ** 2 + epsilon * epsilon)
+    nh, nv = dh / norm, dv / norm
+    gradient = -nh - nv
+    gradient[:, 1:] += nh[:, :-1]
+    gradient[1:, :] += nv[:-1, :]
+    return gradient
+
+
+def _smoothing_gradient(values):
+    """apply_quadratic_smoothing_step's gradient (regularization.rs:47-76)."""
+    dh = np.zeros_like(values)
+    dv = np.zeros_like(values)
+    dh[:, :-1] = values[:, 1:] - values[:, :-1]
+    dv[:-1, :] = values[1:, :] - values[:-1, :]
+    gradient = -2.0 * dh - 2.0 * dv
+    gradient[:, 1:] += 2.0 * dh[:, :-1]
+    gradient[1:, :] += 2.0 * dv[:-1, :]
+    return gradient
+
+
 def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", weights=None, masks=None,
                 gains=None, background=None, object_step=0.5, order=None, recover_pupil=False, pupil_step=0.05,
-                truncation_threshold=None, canonicalize=None):
+                truncation_threshold=None, canonicalize=None, object_tv=0.0, object_tv_epsilon=1e-6,
+                pupil_smoothing=0.0):
     """GradientDescent::step (gradient_descent.rs:405-671) without truncation,
     pupil or illumination recovery, or regularisers: per batch, the frames'
     Wirtinger gradients accumulate, each frame scaled by its weight times
@@ -298,6 +327,14 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
                 spectrum = spectrum - (object_step / active) * gradient
                 if recover_pupil:
                     pupil = pupil - (pupil_step / active) * pupil_gradient
+            share = len(batch) / frames
+            if object_tv > 0.0:
+                # apply_object_tv (gradient_descent.rs:1125-1165) on the spatial object.
+                field = _fft_inverse(np.fft.ifftshift(spectrum))
+                field = field - share * object_tv * _tv_gradient(field, object_tv_epsilon)
+                spectrum = np.fft.fftshift(_fft_forward(field))
+            if recover_pupil and pupil_smoothing > 0.0:
+                pupil = pupil - share * pupil_smoothing * _smoothing_gradient(pupil)
             if recover_pupil:
                 pupil = np.where(support, pupil, 0.0)
         if recover_pupil and canonicalize is not None:
@@ -709,3 +746,34 @@ def test_epry_pupil_recovery_trajectory_agrees(oracle_module, native_library):
     _compare(want, got, 3)
     assert np.abs(got["pupil"] - want["pupil"]).max() <= 1e-9 * np.abs(want["pupil"]).max()
     assert not np.allclose(got["pupil"], model["pupil"])
+
+
+@pytest.mark.parametrize("variant", ["object_tv", "pupil_smoothing"])
+def test_gradient_descent_regularisers_agree(oracle_module, native_library, variant):
+    """GD with the object TV step, or with pupil recovery and pupil
+    smoothing, in batches of four with masked pixels and a zero-weight frame
+    (whose batch still counts it in the regulariser share)."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 13)
+    true_pupil = W.zernike_pupil(model["support"], 7)
+    intensity = oracle.forward_stack(oracle.Problem(dict(model, pupil=true_pupil), None), oracle.object_spectrum(truth))
+    rng = np.random.default_rng(19)
+    data = rng.poisson(intensity * 300.0) / 300.0
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    weights = np.ones(data.shape[0])
+    weights[6] = 0.0
+    problem = oracle.Problem(model, data, masks=masks, weights=weights)
+    if variant == "object_tv":
+        kw = dict(object_tv=0.05, object_tv_epsilon=1e-3)
+        oracle_kw = dict(object_tv_weight=0.05, object_tv_epsilon=1e-3)
+    else:
+        kw = dict(recover_pupil=True, pupil_step=0.05, pupil_smoothing=0.02)
+        oracle_kw = dict(recover_pupil=True, pupil_step=0.05, pupil_smoothing_weight=0.02)
+    want = oracle.run(problem, "gd", iterations=3, batch_size=4, **oracle_kw)
+    got = restated_gd(model, data, 3, 4, masks=masks, weights=weights,
+                      canonicalize=lambda s, p: oracle.canonicalize(problem, s, p), **kw)
+    _compare(want, got, 3)
+    if variant == "pupil_smoothing":
+        assert np.abs(got["pupil"] - want["pupil"]).max() <= 1e-9 * np.abs(want["pupil"]).max()
