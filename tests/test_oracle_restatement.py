@@ -45,10 +45,11 @@ def _axis(start: int, length: int, offset: float):
     return lower, lower + (1 if fraction > 0.0 else 0), 1.0 - fraction, fraction
 
 
-def _stencil(model, source):
+def _stencil(model, source, offset=None):
     h, w = model["h"], model["w"]
     sr, sc = int(model["start_row"][source]), int(model["start_col"][source])
-    orow, ocol = float(model["off_row"][source]), float(model["off_col"][source])
+    orow, ocol = ((float(model["off_row"][source]), float(model["off_col"][source])) if offset is None
+                  else offset)
     if abs(orow) <= 1e-12 and abs(ocol) <= 1e-12:
         return [(sr, sc, 1.0)], h, w
     lr, ur, lwr, uwr = _axis(sr, h, orow)
@@ -56,16 +57,26 @@ def _stencil(model, source):
     return [(lr, lc, lwr * lwc), (lr, uc, lwr * uwc), (ur, lc, uwr * lwc), (ur, uc, uwr * uwc)], h, w
 
 
-def _extract(spectrum, model, source):
-    taps, h, w = _stencil(model, source)
+def _offset_inside(model, source, offset):
+    """validate_subpixel_inside (crop.rs:104-113, :286-305) on both axes."""
+    for start, length, bound, value in ((int(model["start_row"][source]), model["h"], model["mh"], offset[0]),
+                                        (int(model["start_col"][source]), model["w"], model["mw"], offset[1])):
+        lower, upper, _, fraction = _axis(start, length, value)
+        if lower < 0 or lower + length > bound or (fraction > 0.0 and lower + length >= bound):
+            return False
+    return True
+
+
+def _extract(spectrum, model, source, offset=None):
+    taps, h, w = _stencil(model, source, offset)
     out = np.zeros((h, w), np.complex128)
     for r, c, weight in taps:
         out = out + spectrum[r:r + h, c:c + w] * weight
     return out
 
 
-def _insert_adjoint(spectrum, model, source, update, scale):
-    taps, h, w = _stencil(model, source)
+def _insert_adjoint(spectrum, model, source, update, scale, offset=None):
+    taps, h, w = _stencil(model, source, offset)
     value = scale * update
     for r, c, weight in taps:
         spectrum[r:r + h, c:c + w] += value * weight
@@ -250,7 +261,8 @@ def _smoothing_gradient(values):
 def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", weights=None, masks=None,
                 gains=None, background=None, object_step=0.5, order=None, recover_pupil=False, pupil_step=0.05,
                 truncation_threshold=None, canonicalize=None, object_tv=0.0, object_tv_epsilon=1e-6,
-                pupil_smoothing=0.0):
+                pupil_smoothing=0.0, recover_illumination=False, illumination_step=0.1,
+                illumination_finite_difference=0.05, illumination_bounds=1.0):
     """GradientDescent::step (gradient_descent.rs:405-671) without truncation,
     pupil or illumination recovery, or regularisers: per batch, the frames'
     Wirtinger gradients accumulate, each frame scaled by its weight times
@@ -274,11 +286,20 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
     n = model["h"] * model["w"]
     objectives = []
     rejected = 0
+    corrections = np.zeros((frames, 2))
     if recover_pupil and canonicalize is not None:
         spectrum, pupil = canonicalize(spectrum, pupil)
 
+    def offset_of(f, extra=(0.0, 0.0)):
+        """effective_source_offset (state.rs:245-267): compiled offset plus correction."""
+        return (float(model["off_row"][f]) + corrections[f, 0] + extra[0],
+                float(model["off_col"][f]) + corrections[f, 1] + extra[1])
+
+    def intensity_at(f, offset):
+        return np.abs(_fft_inverse(np.fft.ifftshift(_extract(spectrum, model, f, offset) * pupil))) ** 2
+
     def frame_terms(f):
-        patch = _extract(spectrum, model, f)
+        patch = _extract(spectrum, model, f, offset_of(f))
         field = _fft_inverse(np.fft.ifftshift(patch * pupil))
         valid = np.ones(field.shape, bool) if masks is None else masks[f] != 0
         target = np.maximum((data[f] - bg[f]) / gains[f], 0.0)
@@ -302,6 +323,9 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
             maximum = max(float((np.abs(pupil) ** 2).max()), EPS)
             gradient = np.zeros_like(spectrum)
             pupil_gradient = np.zeros_like(pupil)
+            source_gradient = np.zeros((frames, 2))
+            source_curvature = np.zeros((frames, 2))
+            source_weight = np.zeros(frames)
             active = 0
             for f in batch:
                 fw = weights[f]
@@ -322,7 +346,32 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
                 if recover_pupil:
                     object_power = max(float((np.abs(patch) ** 2).max()), EPS)
                     pupil_gradient += fw * valid_scale * np.conj(patch) * projected / (object_power + EPS)
-                _insert_adjoint(gradient, model, f, np.conj(pupil) * projected / (maximum + EPS), fw * valid_scale)
+                _insert_adjoint(gradient, model, f, np.conj(pupil) * projected / (maximum + EPS), fw * valid_scale,
+                                offset_of(f))
+                if recover_illumination:
+                    # illumination_gradient / illumination_axis_gradient (gradient_descent.rs:1236-1345).
+                    d = illumination_finite_difference
+                    curvature_factor = {
+                        "amplitude_mse": 0.5 / np.maximum(intrinsic, EPS),
+                        "intensity_mse": np.full(intrinsic.shape, 2.0),
+                        "poisson_nll": 1.0 / np.maximum(intrinsic, EPS),
+                        "huber_amplitude": np.where(np.abs(factor * 2.0 * np.sqrt(np.maximum(intrinsic, EPS))) < 1.0,
+                                                    0.25 / np.maximum(intrinsic, EPS), EPS),
+                    }[loss]
+                    for axis, shift in ((0, (d, 0.0)), (1, (0.0, d))):
+                        plus, minus = offset_of(f, shift), offset_of(f, (-shift[0], -shift[1]))
+                        plus_ok, minus_ok = _offset_inside(model, f, plus), _offset_inside(model, f, minus)
+                        if not (plus_ok or minus_ok):
+                            continue
+                        if plus_ok and minus_ok:
+                            derivative = (intensity_at(f, plus) - intensity_at(f, minus)) / (2.0 * d)
+                        elif plus_ok:
+                            derivative = (intensity_at(f, plus) - intrinsic) / d
+                        else:
+                            derivative = (intrinsic - intensity_at(f, minus)) / d
+                        source_gradient[f, axis] += fw * float(np.sum((factor * derivative)[kept])) / int(valid.sum())
+                        source_curvature[f, axis] += fw * float(np.sum((curvature_factor * derivative ** 2)[kept])) / int(valid.sum())
+                    source_weight[f] += fw
             if active > 0:
                 spectrum = spectrum - (object_step / active) * gradient
                 if recover_pupil:
@@ -337,11 +386,22 @@ def restated_gd(model, data, iterations, batch_size, *, loss="amplitude_mse", we
                 pupil = pupil - share * pupil_smoothing * _smoothing_gradient(pupil)
             if recover_pupil:
                 pupil = np.where(support, pupil, 0.0)
+            if recover_illumination:
+                # apply_illumination_update (gradient_descent.rs:1044-1089).
+                for f in range(frames):
+                    if source_weight[f] == 0.0:
+                        continue
+                    candidate = np.clip(corrections[f] - illumination_step * source_gradient[f]
+                                        / (source_curvature[f] + EPS), -illumination_bounds, illumination_bounds)
+                    trial = (float(model["off_row"][f]) + candidate[0], float(model["off_col"][f]) + candidate[1])
+                    if _offset_inside(model, f, trial):
+                        corrections[f] = candidate
         if recover_pupil and canonicalize is not None:
             spectrum, pupil = canonicalize(spectrum, pupil)
         objectives.append(objective_sum / weight_sum)
     return dict(objectives=np.array(objectives), object_spectrum=spectrum,
-                object=_fft_inverse(np.fft.ifftshift(spectrum)), pupil=pupil, rejected=rejected)
+                object=_fft_inverse(np.fft.ifftshift(spectrum)), pupil=pupil, rejected=rejected,
+                illumination_corrections=corrections)
 
 
 def _schedule(name, model, data, weights, masks, background):
@@ -777,3 +837,26 @@ def test_gradient_descent_regularisers_agree(oracle_module, native_library, vari
     _compare(want, got, 3)
     if variant == "pupil_smoothing":
         assert np.abs(got["pupil"] - want["pupil"]).max() <= 1e-9 * np.abs(want["pupil"]).max()
+
+
+@pytest.mark.parametrize("batch_size,loss", [(1, "amplitude_mse"), (4, "intensity_mse"), (1, "huber_amplitude"),
+                                             (4, "poisson_nll")])
+def test_gradient_descent_illumination_recovery_agrees(oracle_module, native_library, batch_size, loss):
+    """GD recovering per-source offsets from data simulated with shifted
+    sources, masked pixels, under four losses."""
+    import fpm_rs as fpm
+
+    _, model = helpers.planar_model(fpm, 5, 32)
+    shifted = dict(model, off_row=model["off_row"] + 0.3 * np.sin(np.arange(25)),
+                   off_col=model["off_col"] - 0.25 * np.cos(np.arange(25)))
+    truth = W.smooth_random_object((model["mh"], model["mw"]), 14)
+    intensity = oracle.forward_stack(oracle.Problem(shifted, None), oracle.object_spectrum(truth))
+    rng = np.random.default_rng(20)
+    data = rng.poisson(intensity * 300.0) / 300.0
+    masks = (rng.random(data.shape) > 0.1).astype(np.uint8)
+    problem = oracle.Problem(model, data, masks=masks)
+    want = oracle.run(problem, "gd", iterations=3, batch_size=batch_size, loss_type=loss, recover_illumination=True)
+    got = restated_gd(model, data, 3, batch_size, loss=loss, masks=masks, recover_illumination=True)
+    _compare(want, got, 3)
+    assert np.allclose(got["illumination_corrections"], want["illumination_corrections"], rtol=1e-9, atol=1e-12)
+    assert np.abs(got["illumination_corrections"]).max() > 1e-3
